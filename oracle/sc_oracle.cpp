@@ -1,0 +1,1009 @@
+// sc_oracle.cpp -- CPU oracle (TEST INFRASTRUCTURE ONLY; see sc_oracle.h).
+//
+// A plain restatement of the reference's arithmetic in the reference's own
+// operation order, so that verdicts come out bit-identical when compiled
+// without FMA contraction (-ffp-contract=off).  Every function names the
+// reference code it follows (paths relative to the robertvacha/SC tree).
+
+#include "sc_oracle.h"
+
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+namespace {
+
+const double kPI = 3.141592653589793238462643383279;   // scOOP/structures/macros.h:63
+const double kPIH = 1.57079632679489661923132169163975;
+enum { SCN = 10, SCA = 11, PSC = 12, CPSC = 13, CHPSC = 14, CHCPSC = 15, TPSC = 16, TCPSC = 17,
+       TCHPSC = 18, TCHCPSC = 19, SP = 30, SPN = 30, SPA = 31 };
+
+inline or_vec V(double x, double y, double z) { or_vec v; v.x = x; v.y = y; v.z = z; return v; }
+inline double dot(const or_vec& a, const or_vec& b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline or_vec scale(double s, const or_vec& v) { return V(v.x * s, v.y * s, v.z * s); }
+inline or_vec neg(const or_vec& v) { return V(-1.0 * v.x, -1.0 * v.y, -1.0 * v.z); }
+// Vector::size() (scOOP/structures/Vector.h:49-51); gcc folds pow(x,2) into x*x.
+inline double vsize(const or_vec& v) { return sqrt(v.x * v.x + v.y * v.y + v.z * v.z); }
+// vecCrossProduct (scOOP/mc/math_calc.h:40-42)
+inline or_vec cross(const or_vec& A, const or_vec& B) {
+    return V(A.y * B.z - A.z * B.y, -A.x * B.z + A.z * B.x, A.x * B.y - A.y * B.x);
+}
+// Vector::perpProject (Vector.h:266-277)
+inline or_vec perp(const or_vec& a, const or_vec& B) {
+    double dp = dot(a, B);
+    return V(a.x - B.x * dp, a.y - B.y * dp, a.z - B.z * dp);
+}
+// Vector::normalise (Vector.h:57-65)
+inline void normalise(or_vec& v) {
+    double tot = vsize(v);
+    if (tot != 0.0) { tot = 1.0 / tot; v.x *= tot; v.y *= tot; v.z *= tot; }
+}
+// Vector::ortogonalise (Vector.h:128-130)
+inline void ortho(or_vec& a, const or_vec& B) {
+    double dp = dot(a, B);
+    a.x -= dp * B.x; a.y -= dp * B.y; a.z -= dp * B.z;
+}
+// Vector::rotate(axis, cos, sin) (Vector.h:133-157)
+inline void rotate(or_vec& v, const or_vec& axis, double c, double s) {
+    double qw = c, qx = axis.x * s, qy = axis.y * s, qz = axis.z * s;
+    double t2 = qw * qx, t3 = qw * qy, t4 = qw * qz, t5 = -qx * qx, t6 = qx * qy, t7 = qx * qz, t8 = -qy * qy,
+           t9 = qy * qz, t10 = -qz * qz;
+    double nx = 2.0 * ((t8 + t10) * v.x + (t6 - t4) * v.y + (t3 + t7) * v.z) + v.x;
+    double ny = 2.0 * ((t4 + t6) * v.x + (t5 + t10) * v.y + (t9 - t2) * v.z) + v.y;
+    double nz = 2.0 * ((t7 - t3) * v.x + (t2 + t9) * v.y + (t5 + t8) * v.z) + v.z;
+    v.x = nx; v.y = ny; v.z = nz;
+}
+
+// Round-half-even of |d| < 2^31, the value Cuboid::image gets from the low word
+// of d + 1.5*2^52 (scOOP/structures/geometry.h:110-128).
+inline double anint(double d) {
+    volatile double t = d + 6755399441055744.0;
+    double tt = t;
+    uint64_t bits;
+    std::memcpy(&bits, &tt, 8);
+    return (double)(int32_t)(uint32_t)(bits & 0xffffffffu);
+}
+inline or_vec image(const or_vec& r1, const or_vec& r2, const double* box) {
+    double dx = r1.x - r2.x, dy = r1.y - r2.y, dz = r1.z - r2.z;
+    return V(box[0] * (dx - anint(dx)), box[1] * (dy - anint(dy)), box[2] * (dz - anint(dz)));
+}
+
+inline bool isPscF(int g) { return g == PSC || g == CHPSC || g == TPSC || g == TCHPSC; }
+inline bool isCpscF(int g) { return g == CPSC || g == CHCPSC || g == TCPSC || g == TCHCPSC; }
+inline bool isTF(int g) { return g == TPSC || g == TCPSC || g == TCHPSC || g == TCHCPSC; }
+inline bool isCHF(int g) { return g == CHPSC || g == CHCPSC || g == TCHPSC || g == TCHCPSC; }
+
+enum Kind { K_NONE = 0, K_SC_PSC_CPSC, K_SC_CPSC, K_SC_PSC, K_SC_SCN, K_SC_SCA,
+            K_SP_WCA, K_SP_SPA, K_MIX_SCA_SPA, K_MIX_PSC_SP, K_MIX_CPSC_SP };
+
+// Functor table of PairE::initIntFCE (scOOP/mc/paire.cpp:6-80); later rules override earlier ones.
+int functorKind(int g, int o) {
+    int k = K_NONE;
+    if ((isCpscF(g) && isPscF(o)) || (isPscF(g) && isCpscF(o))) k = K_SC_PSC_CPSC;
+    if (isCpscF(g) && isCpscF(o)) k = K_SC_CPSC;
+    if (isPscF(g) && isPscF(o)) k = K_SC_PSC;
+    if (g == SCN && o == SCN) k = K_SC_SCN;
+    if (g == SCA && o == SCA) k = K_SC_SCA;
+    if (g == SPN || o == SPN) k = K_SP_WCA;
+    if (g == SPA && o == SPA) k = K_SP_SPA;
+    if ((g == SCA && o == SPA) || (g == SPA && o == SCA)) k = K_MIX_SCA_SPA;
+    if ((isPscF(g) && (o == SPA || o == SPN)) || ((g == SPA || g == SPN) && isPscF(o))) k = K_MIX_PSC_SP;
+    if ((isCpscF(g) && (o == SPA || o == SPN)) || ((g == SPA || g == SPN) && isCpscF(o))) k = K_MIX_CPSC_SP;
+    return k;
+}
+
+// ConList (scOOP/structures/Conf.h:17-33) by particle index; -1 = none.
+struct Con {
+    bool isEmpty = true;
+    double sp = 0.0, mod[2] = {0.0, 0.0}, c[2] = {0.0, 0.0}, eq[2] = {0.0, 0.0};
+    int idx[4] = {-1, -1, -1, -1};
+};
+
+// ParticleVector::getConlist (scOOP/structures/Conf.h:90-147).
+Con getConlist(const or_system* s, int i) {
+    Con con;
+    const or_particle& p = s->p[i];
+    const or_moltype& m = s->mols[p.molType];
+    if (m.size == 1) return con;
+    int pos = (i - m.first) % m.size;
+    if (m.bond1c >= 0.0 || m.bonddc >= 0.0 || m.bondhc >= 0.0) {
+        if (pos > 0) con.idx[0] = i - 1;
+        if (pos + 1 < m.size) con.idx[1] = i + 1;
+        if (m.bond1c >= 0.0) { con.eq[0] = m.bond1eq; con.c[0] = m.bond1c; con.mod[0] = 0.0; con.mod[1] = 0.0; con.sp = 0.0; }
+        if (m.bonddc >= 0.0) { con.eq[0] = 0.0; con.c[0] = m.bonddc; con.mod[0] = m.bonddeq; con.mod[1] = 0.0; con.sp = 0.0; }
+        if (m.bondhc >= 0.0) { con.eq[0] = 0.0; con.c[0] = m.bondhc; con.mod[0] = m.bondheq; con.mod[1] = m.bondheq; con.sp = m.bondheq; }
+        con.isEmpty = false;
+    }
+    if (m.bond2c >= 0.0) {
+        if (pos > 1) con.idx[2] = i - 2;
+        if (pos + 2 < m.size) con.idx[3] = i + 2;
+        con.eq[1] = m.bond2eq; con.c[1] = m.bond2c;
+        con.isEmpty = false;
+    }
+    return con;
+}
+
+// EBond::harmonicPotential (scOOP/mc/paire.h:202-204)
+inline double harmonic(double a, double eq, double k) { return k * (a - eq) * (a - eq) * 0.5; }
+
+// fanglScale (scOOP/mc/paire.h:12-17)
+inline double fangl(double a, double pcangl, double pcanglsw) {
+    if (a <= pcanglsw) return 0.0;
+    return (a >= pcangl) ? 1.0 : (0.5 - ((pcanglsw + pcangl) * 0.5 - a) / (pcangl - pcanglsw));
+}
+
+// EPatch::minDistSegments (scOOP/mc/paire.cpp:85-241)
+or_vec minDistSegments(const or_vec& segA, const or_vec& segB, double halfl1, double halfl2, const or_vec& r_cm) {
+    or_vec u = scale(2.0 * halfl1, segA), v = scale(2.0 * halfl2, segB), w, vec;
+    double a, b, c, d, e, D, sc, sN, sD, tc, tN, tD;
+    bool par = false;
+    w.x = segB.x * halfl2 - segA.x * halfl1 - r_cm.x;
+    w.y = segB.y * halfl2 - segA.y * halfl1 - r_cm.y;
+    w.z = segB.z * halfl2 - segA.z * halfl1 - r_cm.z;
+    a = dot(u, u); b = dot(u, v); c = dot(v, v); d = dot(u, w); e = dot(v, w);
+    D = a * c - b * b;
+    sc = sN = sD = D; tc = tN = tD = D;
+    if (D < 0.00000001) {
+        par = true; sN = 0.0; sD = 1.0; tN = e; tD = c;
+    } else {
+        sN = (b * e - c * d); tN = (a * e - b * d);
+        if (sN < 0.0) { sN = 0.0; tN = e; tD = c; }
+        else if (sN > sD) { sN = sD; tN = e + b; tD = c; }
+    }
+    if (tN < 0.0) {
+        tN = 0.0;
+        if (-d < 0.0) sN = 0.0;
+        else if (-d > a) sN = sD;
+        else { sN = -d; sD = a; }
+    } else if (tN > tD) {
+        tN = tD;
+        if ((-d + b) < 0.0) sN = 0;
+        else if ((-d + b) > a) sN = sD;
+        else { sN = (-d + b); sD = a; }
+    }
+    sc = (fabs(sN) < 0.00000001) ? 0.0 : sN / sD;
+    tc = (fabs(tN) < 0.00000001) ? 0.0 : tN / tD;
+    vec.x = u.x * sc + w.x - v.x * tc;
+    vec.y = u.y * sc + w.y - v.y * tc;
+    vec.z = u.z * sc + w.z - v.z * tc;
+    if (par) {
+        or_vec vec2;
+        w.x = segA.x * halfl1 - segB.x * halfl2 + r_cm.x;
+        w.y = segA.y * halfl1 - segB.y * halfl2 + r_cm.y;
+        w.z = segA.z * halfl1 - segB.z * halfl2 + r_cm.z;
+        d = dot(v, w); e = dot(u, w);
+        D = a * c - b * b;
+        sc = sN = sD = D; tc = tN = tD = D;
+        if (D < 0.00000001) { sN = 0.0; sD = 1.0; tN = e; tD = a; }
+        if (tN < 0.0) {
+            tN = 0.0;
+            if (-d < 0.0) sN = 0.0;
+            else if (-d > c) sN = sD;
+            else { sN = -d; sD = c; }
+        } else if (tN > tD) {
+            tN = tD;
+            if ((-d + b) < 0.0) sN = 0;
+            else if ((-d + b) > c) sN = sD;
+            else { sN = (-d + b); sD = c; }
+        }
+        sc = (fabs(sN) < 0.00000001) ? 0.0 : sN / sD;
+        tc = (fabs(tN) < 0.00000001) ? 0.0 : tN / tD;
+        vec2.x = v.x * sc + w.x - u.x * tc;
+        vec2.y = v.y * sc + w.y - u.y * tc;
+        vec2.z = v.z * sc + w.z - u.z * tc;
+        if (dot(vec2, vec2) < dot(vec, vec)) return vec2;
+    }
+    return vec;
+}
+
+struct PatchV { or_vec dir, s0, s1; };
+
+// EPatch::testIntrPatch (scOOP/mc/paire.h:86-101)
+inline void testIntrPatch(const or_vec& dir, const or_vec& patchdir, or_vec vec, double cospatch, double ti, double* in) {
+    vec = perp(vec, dir);
+    if (dot(patchdir, vec) >= cospatch * vsize(vec)) {
+        if (in[0] == 0) { in[0] = ti; return; }
+        if (in[1] == 0 && in[0] != ti) { in[1] = ti; return; }
+    }
+}
+
+// EPatch::scToInfiIntr (paire.h:103-119)
+inline void scToInfiIntr(const or_vec& d1, const or_vec& d2, const PatchV& P, const or_vec& r_cm, double pcanglsw,
+                         double halfl1, double halfl2, double* in, double x1) {
+    if ((x1 >= halfl2) || (x1 <= -halfl2)) return;
+    or_vec v1 = V(d2.x * x1 - r_cm.x, d2.y * x1 - r_cm.y, d2.z * x1 - r_cm.z);
+    double e = dot(d1, v1);
+    if ((e >= halfl1) || (e <= -halfl1)) return;
+    testIntrPatch(d1, P.dir, v1, pcanglsw, x1, in);
+}
+
+// EPatch::testIntrAtC (paire.h:121-148)
+void testIntrAtC(const or_vec& d1, const or_vec& d2, const PatchV& P, const or_vec& r_cm, double pcanglsw, double rcutSq,
+                 double halfl1, double halfl2, double* in) {
+    or_vec v1 = cross(neg(r_cm), d1), v2 = cross(d2, d1);
+    double a = dot(v2, v2), b = 2 * dot(v1, v2), c = -rcutSq + dot(v1, v1), d = b * b - 4 * a * c;
+    if (d >= 0) {
+        d = sqrt(d);
+        a = 0.5 / a;
+        double x1 = (-b + d) * a;
+        scToInfiIntr(d1, d2, P, r_cm, pcanglsw, halfl1, halfl2, in, x1);
+        if (d > 0) {
+            x1 = (-b - d) * a;
+            scToInfiIntr(d1, d2, P, r_cm, pcanglsw, halfl1, halfl2, in, x1);
+        }
+    }
+}
+
+// EPatch::findIntersectPlaneUni (paire.h:150-181)
+bool findIntersectPlaneUni(const or_vec& dirA, const or_vec& dirB, double halfl, const or_vec& r_cm, const or_vec& w_vec,
+                           double cospatch, double& ti, double& c, double& d) {
+    or_vec nplane = cross(dirA, w_vec);
+    double a = dot(nplane, dirB);
+    c = 1.0; d = 1.0;
+    if (a == 0.0) return false;
+    ti = dot(nplane, r_cm) / a;
+    if ((ti > halfl) || (ti < -halfl)) return false;
+    or_vec dv = V(ti * dirB.x - r_cm.x, ti * dirB.y - r_cm.y, ti * dirB.z - r_cm.z);
+    c = dot(dv, w_vec);
+    if (c * cospatch < 0) return false;
+    d = fabs(dot(dv, dirA)) - halfl;
+    return true;
+}
+
+// Psc::scToEndSpIntr / calcIntersections / testIntrA (paire.h:588-652)
+inline void scToEndSpIntr(const or_vec& d1, const or_vec& d2, const PatchV& P, const or_vec& r_cm, double pcanglsw,
+                          double halfl1, double halfl2, double* in, double x1) {
+    if ((x1 >= halfl2) || (x1 <= -halfl2)) return;
+    or_vec v1 = V(d2.x * x1 - r_cm.x, d2.y * x1 - r_cm.y, d2.z * x1 - r_cm.z);
+    double e = dot(d1, v1);
+    if ((e >= halfl1) || (e <= -halfl1)) testIntrPatch(d1, P.dir, v1, pcanglsw, x1, in);
+}
+inline void calcIntersections(const or_vec& d1, const or_vec& d2, const PatchV& P, const or_vec& r_cm, double* in,
+                              double pcanglsw, double halfl1, double halfl2, double b, double c) {
+    double d = b * b - 4 * c;
+    if (d >= 0) {
+        d = sqrt(d);
+        c = (-b + d) * 0.5;
+        scToEndSpIntr(d1, d2, P, r_cm, pcanglsw, halfl1, halfl2, in, c);
+        if (d > 0) {
+            c = (-b - d) * 0.5;
+            scToEndSpIntr(d1, d2, P, r_cm, pcanglsw, halfl1, halfl2, in, c);
+        }
+    }
+}
+inline void testIntrA(const or_vec& d1, const or_vec& d2, const PatchV& P, const or_vec& r_cm, double pcanglsw,
+                      double rcutSq, double halfl1, double halfl2, double* in) {
+    or_vec v1 = V(d2.x * halfl2 - r_cm.x, d2.y * halfl2 - r_cm.y, d2.z * halfl2 - r_cm.z);
+    double a = dot(v1, d1);
+    or_vec v2 = V(v1.x - d1.x * a, v1.y - d1.y * a, v1.z - d1.z * a);
+    double b = dot(v2, v2), d = fabs(a) - halfl1, c;
+    if (d <= 0) c = b; else c = d * d + b;
+    if (c < rcutSq) testIntrPatch(d1, P.dir, v1, pcanglsw, halfl2, in);
+}
+
+// Psc::pscIntersect (paire.h:499-583)
+int pscIntersect(const or_vec& d1, const or_vec& d2, const PatchV& P, const or_vec& r_cm, double& in1, double& in2,
+                 double pcanglsw, double rcutSq, double halfl1, double halfl2) {
+    double c, d, ti, disti;
+    double in[2] = {0, 0};
+    if (findIntersectPlaneUni(d1, d2, halfl2, r_cm, P.s0, pcanglsw, ti, c, d)) {
+        disti = (d <= 0) ? c * c : d * d + c * c;
+        if (disti <= rcutSq) in[0] = ti;
+    }
+    if (findIntersectPlaneUni(d1, d2, halfl2, r_cm, P.s1, pcanglsw, ti, c, d)) {
+        disti = (d <= 0) ? c * c : d * d + c * c;
+        if (disti <= rcutSq) {
+            if (in[0] == 0.0) in[0] = ti;
+            else if (ti != in[0]) in[1] = ti;
+        }
+    }
+    if (in[1] != 0.0) { in1 = in[0]; in2 = in[1]; return 2; }
+    testIntrAtC(d1, d2, P, r_cm, pcanglsw, rcutSq, halfl1, halfl2, in);
+    if (in[1] == 0.0) {
+        or_vec v1 = V(d1.x * halfl1 - r_cm.x, d1.y * halfl1 - r_cm.y, d1.z * halfl1 - r_cm.z);
+        or_vec v2 = V(-d1.x * halfl1 - r_cm.x, -d1.y * halfl1 - r_cm.y, -d1.z * halfl1 - r_cm.z);
+        calcIntersections(d1, d2, P, r_cm, in, pcanglsw, halfl1, halfl2, 2.0 * dot(v1, d2), dot(v1, v1) - rcutSq);
+        calcIntersections(d1, d2, P, r_cm, in, pcanglsw, halfl1, halfl2, 2.0 * dot(v2, d2), dot(v2, v2) - rcutSq);
+    } else {
+        in1 = in[0]; in2 = in[1]; return 2;
+    }
+    if (in[1] == 0.0) {
+        testIntrA(d1, d2, P, r_cm, pcanglsw, rcutSq, halfl1, halfl2, in);
+        if (in[1] == 0.0) testIntrA(d1, d2, P, r_cm, pcanglsw, rcutSq, halfl1, -halfl2, in);
+    }
+    in1 = in[0]; in2 = in[1];
+    return (in[1] == 0.0) ? 0 : 2;
+}
+
+// CPsc::cpscIntersect (paire.h:687-826)
+int cpscIntersect(const or_vec& d1, const or_vec& d2, const PatchV& P, const or_vec& r_cm, double& in1, double& in2,
+                  double pcanglsw, double rcutSq, double halfl1, double halfl2) {
+    double a, b, c, d, x1, x2, disti, ti;
+    double in[2] = {0, 0};
+    or_vec v1, v2;
+    if (findIntersectPlaneUni(d1, d2, halfl2, r_cm, P.s0, pcanglsw, ti, c, d)) {
+        if (d <= 0) { disti = c * c; if (disti <= rcutSq) in[0] = ti; }
+    }
+    if (findIntersectPlaneUni(d1, d2, halfl2, r_cm, P.s1, pcanglsw, ti, c, d)) {
+        if (d <= 0) {
+            disti = c * c;
+            if (disti <= rcutSq) {
+                if (in[0] == 0.0) in[0] = ti;
+                else if (ti != in[0]) in[1] = ti;
+            }
+        }
+    }
+    if (in[1] != 0.0) { in1 = in[0]; in2 = in[1]; return 2; }
+    testIntrAtC(d1, d2, P, r_cm, pcanglsw, rcutSq, halfl1, halfl2, in);
+    if (in[1] == 0.0) {
+        a = dot(d1, d2);
+        if (a != 0.0) {
+            v1 = V(r_cm.x + halfl1 * d1.x, r_cm.y + halfl1 * d1.y, r_cm.z + halfl1 * d1.z);
+            x1 = dot(d1, v1) / a;
+            if (!((x1 > halfl2) || (x1 < -halfl2))) {
+                v2 = V(x1 * d2.x - v1.x, x1 * d2.y - v1.y, x1 * d2.z - v1.z);
+                b = dot(v2, v2);
+                if (!(b > rcutSq)) testIntrPatch(d1, P.dir, v2, pcanglsw, x1, in);
+            }
+            v1 = V(r_cm.x - halfl1 * d1.x, r_cm.y - halfl1 * d1.y, r_cm.z - halfl1 * d1.z);
+            x2 = dot(d1, v1) / a;
+            if (!((x2 > halfl2) || (x2 < -halfl2))) {
+                v2 = V(x2 * d2.x - v1.x, x2 * d2.y - v1.y, x2 * d2.z - v1.z);
+                b = dot(v2, v2);
+                if (!(b > rcutSq)) testIntrPatch(d1, P.dir, v2, pcanglsw, x2, in);
+            }
+        }
+    } else {
+        in1 = in[0]; in2 = in[1]; return 2;
+    }
+    if (in[1] == 0.0) {
+        v1 = V(d2.x * halfl2 - r_cm.x, d2.y * halfl2 - r_cm.y, d2.z * halfl2 - r_cm.z);
+        a = dot(v1, d1);
+        v2 = V(v1.x - d1.x * a, v1.y - d1.y * a, v1.z - d1.z * a);
+        b = dot(v2, v2);
+        d = fabs(a) - halfl1;
+        if (d <= 0) { if (b < rcutSq) testIntrPatch(d1, P.dir, v1, pcanglsw, halfl2, in); }
+        if (in[1] == 0.0) {
+            v1 = V(-d2.x * halfl2 - r_cm.x, -d2.y * halfl2 - r_cm.y, -d2.z * halfl2 - r_cm.z);
+            a = dot(v1, d1);
+            v2 = V(v1.x - d1.x * a, v1.y - d1.y * a, v1.z - d1.z * a);
+            b = dot(v2, v2);
+            d = fabs(a) - halfl1;
+            if (d <= 0) { if (b < rcutSq) testIntrPatch(d1, P.dir, v1, pcanglsw, -1.0 * halfl2, in); }
+        }
+    }
+    in1 = in[0]; in2 = in[1];
+    return (in[1] == 0.0) ? 0 : 2;
+}
+
+// EPatch::atrE (scOOP/mc/paire.cpp:243-301)
+double atrE(const or_param& ia, const or_vec& d1, const or_vec& d2, const PatchV& P1, const PatchV& P2, const or_vec& r_cm,
+            int pn1, int pn2, double S1, double S2, double T1, double T2) {
+    double v1 = fabs(S1 - S2), v2 = fabs(T1 - T2), f0 = 0.5 * (v1 + v2);
+    or_vec a1 = scale((S1 + S2) * 0.5, d1), a2 = scale((T1 + T2) * 0.5, d2);
+    or_vec vi = V(a2.x - a1.x - r_cm.x, a2.y - a1.y - r_cm.y, a2.z - a1.z - r_cm.z);
+    or_vec md = minDistSegments(d1, d2, v1, v2, vi);
+    double ndist = sqrt(dot(md, md)), atr;
+    if (ndist < ia.pdis) atr = -ia.epsilon;
+    else { atr = cos(kPIH * (ndist - ia.pdis) / ia.pswitch); atr *= -atr * ia.epsilon; }
+    or_vec w = perp(vi, d1);
+    double a = dot(w, P1.dir) / vsize(w);
+    double f1 = fangl(a, ia.pcangl[0 + 2 * pn1], ia.pcanglsw[0 + 2 * pn1]);
+    w = perp(neg(vi), d2);
+    a = dot(w, P2.dir) / vsize(w);
+    double f2 = fangl(a, ia.pcangl[1 + 2 * pn2], ia.pcanglsw[1 + 2 * pn2]);
+    double paral = 1.0;
+    if (ia.parallel != 0.0) {    // EPatch::scparallel (paire.h:77-84)
+        double cosa = dot(d1, d2);
+        if ((ia.parallel > 0 && cosa > 0) || (ia.parallel < 0 && cosa < 0)) paral = 1.0 + ia.parallel * cosa;
+    }
+    atr *= f0 * f1 * f2 * paral;
+    return atr;
+}
+
+inline const or_param& P(const or_system* s, int a, int b) { return s->params[a * OR_MAXT + b]; }
+
+// HarmonicSc (scOOP/mc/paire.h:239-280)
+double harmonicSc(const or_system* s, double dist, int i1, int i2, const Con& con) {
+    const or_particle& p1 = s->p[i1];
+    const or_particle& p2 = s->p[i2];
+    const or_param& ia = P(s, p1.type, p2.type);
+    if (i2 == con.idx[1] || i2 == con.idx[0]) {
+        bool tail = (i2 == con.idx[0]);
+        double h1 = (ia.geotype[0] < SP) ? (ia.half_len[0] + con.mod[tail ? 0 : 1]) * (tail ? 1.0 : -1.0) : con.sp;
+        double h2 = (ia.geotype[1] < SP) ? (ia.half_len[1] + con.mod[tail ? 1 : 0]) * (tail ? -1.0 : 1.0) : con.sp;
+        or_vec v1 = V(p1.pos.x + (p1.dir.x * h1 / s->box[0]), p1.pos.y + (p1.dir.y * h1 / s->box[1]), p1.pos.z + (p1.dir.z * h1 / s->box[2]));
+        or_vec v2 = V(p2.pos.x + (p2.dir.x * h2 / s->box[0]), p2.pos.y + (p2.dir.y * h2 / s->box[1]), p2.pos.z + (p2.dir.z * h2 / s->box[2]));
+        v1 = image(v1, v2, s->box);
+        return harmonic(sqrt(dot(v1, v1)), con.eq[0], con.c[0]);
+    }
+    if (i2 == con.idx[2] || i2 == con.idx[3]) return harmonic(dist, con.eq[1], con.c[1]);
+    return 0.0;
+}
+
+// HarmonicSp (paire.h:221-236)
+double harmonicSp(double dist, int i2, const Con& con) {
+    if (i2 == con.idx[1] || i2 == con.idx[0]) return harmonic(dist, con.eq[0], con.c[0]);
+    if (i2 == con.idx[2] || i2 == con.idx[3]) return harmonic(dist, con.eq[1], con.c[1]);
+    return 0.0;
+}
+
+// AngleSc::angleEnergyAngle2 (paire.h:340-352)
+double angle2of(const or_particle& a, const or_particle& b) {
+    or_vec ax = cross(a.dir, b.dir);
+    or_vec x1 = cross(a.dir, ax), x2 = cross(b.dir, ax);
+    double v1x = dot(x1, a.pd[0]), v1y = dot(ax, a.pd[0]), v2x = dot(x2, b.pd[0]), v2y = dot(ax, b.pd[0]);
+    return acos((v1x * v2x + v1y * v2y) / (sqrt((v1x * v1x + v1y * v1y) * (v2x * v2x + v2y * v2y))));
+}
+
+// AngleSc (paire.h:283-337)
+double angleSc(const or_system* s, int i1, int i2, const Con& con) {
+    const or_particle& p1 = s->p[i1];
+    const or_particle& p2 = s->p[i2];
+    const or_param& ia = P(s, p1.type, p2.type);
+    const or_moltype& m = s->mols[p1.molType];
+    double e = 0.0;
+    bool partner = (i2 == con.idx[0] || i2 == con.idx[1]);
+    bool tail = (i2 == con.idx[0]);
+    if (m.angle1c >= 0 && partner) {
+        or_vec v1, v2;
+        if (ia.geotype[0] < SP) v1 = p1.dir;
+        else {
+            double h = ia.half_len[1] * (tail ? -1.0 : 1.0);
+            v1 = V(p2.pos.x + p2.dir.x * h / s->box[0], p2.pos.y + p2.dir.y * h / s->box[1], p2.pos.z + p2.dir.z * h / s->box[2]);
+            v1 = image(v1, p1.pos, s->box);
+            normalise(v1);
+        }
+        if (ia.geotype[1] < SP) v2 = p2.dir;
+        else {
+            double h = ia.half_len[0] * (tail ? 1.0 : -1.0);
+            v2 = V(p1.pos.x + p1.dir.x * h / s->box[0], p1.pos.y + p1.dir.y * h / s->box[1], p1.pos.z + p1.dir.z * h / s->box[2]);
+            v2 = image(v2, p2.pos, s->box);
+            normalise(v2);
+        }
+        e += harmonic(acos(dot(v1, v2)), m.angle1eq, m.angle1c);
+    }
+    if (m.angle2c >= 0 && partner) {
+        if ((ia.geotype[0] < SP) && (ia.geotype[1] < SP)) {
+            double ang = tail ? angle2of(p2, p1) : angle2of(p1, p2);
+            e += harmonic(ang, m.angle2eq, m.angle2c);
+        }
+    }
+    return e;
+}
+
+// WcaTruncSq (paire.h:385-393)
+inline double wcaTruncSq(double distSq, const or_param& ia) {
+    if (distSq > ia.rcutwcaSq) return 0.0;
+    return ia.epsilon + ia.A * pow(distSq, -6) - ia.B * pow(distSq, -3);
+}
+
+// PscSpa / CPscSpa / ScaSpa (paire.h:911-1010): attraction of one patch to a sphere.
+double patchToSphere(int kind, double dist, double contt, const or_vec& distvec, const or_param& ia, const or_vec& d1,
+                     const PatchV& P1) {
+    double atr;
+    if (dist < ia.pdis) atr = -ia.epsilon;
+    else { atr = cos(kPIH * (dist - ia.pdis) / ia.pswitch); atr *= -atr * ia.epsilon; }
+    double a = 0.0;
+    if (kind != K_MIX_SCA_SPA) {
+        or_vec w = perp(distvec, d1);
+        a = dot(w, P1.dir) / vsize(w);
+    }
+    double halfl = ia.half_len[0];
+    double b = sqrt(ia.rcutSq - dist * dist), f0;
+    if (contt + b > halfl) f0 = halfl; else f0 = contt + b;
+    if (contt - b < -halfl) f0 -= -halfl; else f0 -= contt - b;
+    if (kind == K_MIX_SCA_SPA) atr *= f0;
+    else atr *= fangl(a, ia.pcangl[0], ia.pcanglsw[0]) * (f0);
+    return atr;
+}
+
+// MixSpSc::closestDist (paire.h:1077-1093)
+inline double mixClosest(const or_vec& rc, const or_vec& d1, double halfl, double& contt, or_vec& dv) {
+    contt = dot(d1, rc);
+    double d = -halfl;
+    if (contt >= halfl) d = halfl;
+    else if (contt > -halfl) d = contt;
+    dv = V(-rc.x + d1.x * d, -rc.y + d1.y * d, -rc.z + d1.z * d);
+    return dot(dv, dv);
+}
+
+}  // namespace
+
+extern "C" {
+
+// PairE::operator() (scOOP/mc/paire.h:1209-1220) with the functor bodies of
+// SpheroCylinder (1114-1197), MixSpSc (1014-1094) and Sphere (1099-1109).
+double or_pair_energy(const or_system* s, int i, int j, unsigned* bitsOut, double* distSqOut) {
+    unsigned bits = 0;
+    double dsqOut = -1.0;
+    Con con = getConlist(s, i);
+    const or_particle& p1 = s->p[i];
+    const or_particle& p2 = s->p[j];
+    or_vec r_cm = image(p1.pos, p2.pos, s->box);
+    double dotrcm = dot(r_cm, r_cm);
+    double energy = 0.0;
+    if (dotrcm > s->sqmaxcut && con.isEmpty) goto done;
+    {
+        bits |= OR_V_EVAL;
+        double dist = sqrt(dotrcm);
+        const or_param& ia = P(s, p1.type, p2.type);
+        int kind = functorKind(ia.geotype[0], ia.geotype[1]);
+        if (kind == K_SC_PSC || kind == K_SC_CPSC || kind == K_SC_PSC_CPSC || kind == K_SC_SCN || kind == K_SC_SCA) {
+            double abE = 0.0;
+            abE = harmonicSc(s, dist, i, j, con);
+            abE += angleSc(s, i, j, con);
+            or_vec md = minDistSegments(p1.dir, p2.dir, ia.half_len[0], ia.half_len[1], r_cm);
+            double distSq = dot(md, md);
+            dsqOut = distSq;
+            double rep = wcaTruncSq(distSq, ia);
+            if (!(distSq > ia.rcutwcaSq)) bits |= OR_V_WCA;
+            double atr = 0.0;
+            if (!((distSq > ia.rcutSq) || (ia.epsilon == 0.0) || ia.exclude)) {
+                bits |= OR_V_ATR;
+                int g0 = ia.geotype[0], g1 = ia.geotype[1];
+                bool fCH = false, sCH = false, fT = false, sT = false;
+                if (kind == K_SC_PSC) {
+                    fCH = (g0 == CHPSC || g0 == TCHPSC); sCH = (g1 == CHPSC || g1 == TCHPSC);
+                    fT = (g0 == TPSC || g0 == TCHPSC); sT = (g1 == TPSC || g1 == TCHPSC);
+                } else if (kind == K_SC_CPSC) {
+                    fCH = (g0 == CHCPSC || g0 == TCHCPSC); sCH = (g1 == CHCPSC || g1 == TCHCPSC);
+                    fT = (g0 == TCPSC || g0 == TCHCPSC); sT = (g1 == TCPSC || g1 == TCHCPSC);
+                } else if (kind == K_SC_PSC_CPSC) {
+                    fCH = isCHF(g0); sCH = isCHF(g1); fT = isTF(g0); sT = isTF(g1);
+                }
+                for (int c = 0; c < 4; ++c) {
+                    int pn1 = c & 1, pn2 = c >> 1;
+                    if ((pn1 && !fT) || (pn2 && !sT)) continue;
+                    if (kind == K_SC_SCN) continue;  // EPatch::operator() returns 0 (paire.h:58-61)
+                    const or_vec& d1 = fCH ? p1.ch[pn1] : p1.dir;
+                    const or_vec& d2 = sCH ? p2.ch[pn2] : p2.dir;
+                    if (kind == K_SC_SCA) {      // Sca::operator() (paire.h:845-852)
+                        or_vec m2 = minDistSegments(d1, d2, ia.half_len[0], ia.half_len[1], r_cm);
+                        double dd = sqrt(dot(m2, m2));
+                        if (!(dd > ia.rcutwca)) atr += ia.A * pow(dd, -12) - ia.B * pow(dd, -6) + ia.epsilon;
+                        continue;
+                    }
+                    PatchV P1{p1.pd[pn1], p1.ps[2 * pn1], p1.ps[2 * pn1 + 1]};
+                    PatchV P2{p2.pd[pn2], p2.ps[2 * pn2], p2.ps[2 * pn2 + 1]};
+                    bool firstPsc = (kind == K_SC_PSC) || (kind == K_SC_PSC_CPSC && isPscF(g0));
+                    bool secondPsc = (kind == K_SC_PSC) || (kind == K_SC_PSC_CPSC && !isPscF(g0));
+                    double T1 = 0, T2 = 0, S1 = 0, S2 = 0;
+                    int na = firstPsc ? pscIntersect(d1, d2, P1, r_cm, T1, T2, ia.pcanglsw[2 * pn1], ia.rcutSq, ia.half_len[0], ia.half_len[1])
+                                      : cpscIntersect(d1, d2, P1, r_cm, T1, T2, ia.pcanglsw[2 * pn1], ia.rcutSq, ia.half_len[0], ia.half_len[1]);
+                    if (na < 2) continue;
+                    bits |= 1u << (8 + 2 * c);
+                    or_vec mr = neg(r_cm);
+                    int nb = secondPsc ? pscIntersect(d2, d1, P2, mr, S1, S2, ia.pcanglsw[2 * pn2 + 1], ia.rcutSq, ia.half_len[1], ia.half_len[0])
+                                       : cpscIntersect(d2, d1, P2, mr, S1, S2, ia.pcanglsw[2 * pn2 + 1], ia.rcutSq, ia.half_len[1], ia.half_len[0]);
+                    if (nb < 2) continue;
+                    bits |= 1u << (9 + 2 * c);
+                    atr += atrE(ia, d1, d2, P1, P2, r_cm, pn1, pn2, S1, S2, T1, T2);
+                }
+            }
+            energy = abE + rep + atr;
+        } else if (kind == K_MIX_SCA_SPA || kind == K_MIX_PSC_SP || kind == K_MIX_CPSC_SP) {
+            bool isp1Spc = (ia.geotype[0] < SP);
+            const or_particle& spc = isp1Spc ? p1 : p2;
+            const or_param& iap = isp1Spc ? P(s, p1.type, p2.type) : P(s, p2.type, p1.type);
+            or_vec rc = isp1Spc ? r_cm : neg(r_cm);
+            double contt = 0.0, abE = 0.0, rep = 0.0, atr = 0.0;
+            or_vec dv;
+            double distSq = mixClosest(rc, spc.dir, iap.half_len[0], contt, dv);
+            dsqOut = distSq;
+            abE = harmonicSc(s, dist, i, j, con);
+            abE += angleSc(s, i, j, con);
+            if (distSq < iap.rcutwcaSq) { rep = wcaTruncSq(distSq, ia); bits |= OR_V_WCA; }
+            bool isFar = (kind == K_MIX_CPSC_SP) && ((contt > iap.half_len[0]) || (contt < -iap.half_len[0]));
+            if (isFar) bits |= OR_V_FAR;
+            if (!((distSq > iap.rcutSq) || (iap.epsilon == 0.0) || iap.exclude || isFar)) {
+                bits |= OR_V_ATR;
+                int g0 = iap.geotype[0];
+                bool chiral = false, sec = false;
+                if (kind == K_MIX_PSC_SP) { chiral = (g0 == CHPSC || g0 == TCHPSC); sec = (g0 == TPSC || g0 == TCHPSC); }
+                if (kind == K_MIX_CPSC_SP) { chiral = (g0 == CHCPSC || g0 == TCHCPSC); sec = (g0 == TCPSC || g0 == TCHCPSC); }
+                if (chiral) distSq = mixClosest(rc, spc.ch[0], iap.half_len[0], contt, dv);
+                double dd = sqrt(distSq);
+                if (dd < iap.rcut) {
+                    bits |= 1u << 8;
+                    PatchV P1{spc.pd[0], spc.ps[0], spc.ps[1]};
+                    atr = patchToSphere(kind, dd, contt, dv, iap, chiral ? spc.ch[0] : spc.dir, P1);
+                }
+                if (sec) {
+                    distSq = mixClosest(rc, chiral ? spc.ch[1] : spc.dir, iap.half_len[0], contt, dv);
+                    dd = sqrt(distSq);
+                    if (dd < iap.rcut) {
+                        bits |= 1u << 9;
+                        PatchV P2{spc.pd[1], spc.ps[2], spc.ps[3]};
+                        atr += patchToSphere(kind, dd, contt, dv, iap, chiral ? spc.ch[1] : spc.dir, P2);
+                    }
+                }
+            }
+            energy = abE + rep + atr;
+        } else if (kind == K_SP_WCA || kind == K_SP_SPA) {
+            dsqOut = dotrcm;
+            double bond = harmonicSp(dist, j, con);
+            double pot = 0.0;
+            if (kind == K_SP_WCA) {      // WcaTrunc (paire.h:376-383)
+                if (!(dist > ia.rcutwca)) { pot = ia.A * pow(dist, -12) - ia.B * pow(dist, -6) + ia.epsilon; bits |= OR_V_WCA; }
+            } else {                      // WcaCos2Taylor (paire.h:416-439)
+                if (!(dist > ia.rcut || ia.epsilon == 0.0 || ia.exclude)) {
+                    bits |= OR_V_ATR;
+                    double e;
+                    if (dist > ia.pdis) {
+                        e = kPIH * (dist - ia.pdis) * ia.pswitchINV;
+                        e *= e;
+                        e = (1 - e + e * e * (1.0 / 3.0) - e * e * e * (2.0 / 45.0) + e * e * e * e * (1.0 / 315.0) -
+                             e * e * e * e * e * (2.0 / 14175.0) + e * e * e * e * e * e * (2.0 / 467775.0) -
+                             e * e * e * e * e * e * e * (4.0 / 42567525) + e * e * e * e * e * e * e * e * (1.0 / 638512875)) *
+                            -ia.epsilon;
+                    } else {
+                        e = -ia.epsilon;
+                    }
+                    if (dist > ia.rcutwca) pot = e;
+                    else { pot = ia.A * pow(dist, -12) - ia.B * pow(dist, -6); bits |= OR_V_WCA; }
+                }
+            }
+            energy = bond + pot;
+        }
+        // K_NONE: EBasic returns 0 (paire.h:207-213)
+    }
+done:
+    if (bitsOut) *bitsOut = bits;
+    if (distSqOut) *distSqOut = dsqOut;
+    return energy;
+}
+
+// TotalEMatrix::oneToAllTrial without pair list (totalenergycalculator.h:383-415): index order.
+double or_one_to_all(const or_system* s, int target) {
+    double e = 0.0;
+    for (int i = 0; i < target; ++i) e += or_pair_energy(s, target, i, nullptr, nullptr);
+    for (int i = target + 1; i < s->n; ++i) e += or_pair_energy(s, target, i, nullptr, nullptr);
+    return e;
+}
+
+// TotalEMatrix::allToAll(EnergyMatrix*) (totalenergycalculator.h:502-521): part1 = i > j.
+double or_all_to_all(const or_system* s) {
+    double e = 0.0;
+    for (int i = 1; i < s->n; ++i)
+        for (int j = 0; j < i; ++j) e += or_pair_energy(s, i, j, nullptr, nullptr);
+    return e;
+}
+
+// TotalEMatrix::mol2othersTrial (totalenergycalculator.h:453-499): empty conlist.
+double or_mol2others(const or_system* s, int first, int size) {
+    // An empty conlist is what a moleculeless system would give: evaluate with a
+    // copy whose molecule table says "single particles".
+    double e = 0.0;
+    or_moltype single{};
+    single.size = 1;
+    std::vector<or_moltype> mols(s->nmol > 0 ? s->nmol : 1, single);
+    or_system t = *s;
+    t.mols = mols.data();
+    for (int j = first; j < first + size; ++j) {
+        for (int i = 0; i < first; ++i) e += or_pair_energy(&t, j, i, nullptr, nullptr);
+        for (int i = first + size; i < s->n; ++i) e += or_pair_energy(&t, j, i, nullptr, nullptr);
+    }
+    return e;
+}
+
+// Inicializer::fillTypes (scOOP/mc/inicializer.cpp:660-852), Topo::genParamPairs and
+// Topo::genTopoParams (scOOP/structures/topo.cpp:5-153).
+int or_derive_params(const or_type_in* types, int ntypes, const unsigned char* excl, or_param* ia, double* sqmaxcutOut,
+                     double* maxcutOut) {
+    std::memset(ia, 0, sizeof(or_param) * OR_MAXT * OR_MAXT);
+    double sqmaxcut = 0.0;
+    for (int k = 0; k < ntypes; ++k) {
+        const or_type_in& t = types[k];
+        if (t.type < 0 || t.type >= OR_MAXT) return -1;
+        or_param& p = ia[t.type * OR_MAXT + t.type];
+        const double* q = t.param;
+        int f = t.nfields, g = t.geotype;
+        p.geotype[0] = p.geotype[1] = g;
+        p.epsilon = q[0];
+        p.sigma = q[1];
+        p.A = 4 * p.epsilon * pow(p.sigma, 12);
+        p.B = 4 * p.epsilon * pow(p.sigma, 6);
+        p.rcutwca = (p.sigma) * pow(2.0, 1.0 / 6.0);
+        p.rcutwcaSq = p.rcutwca * p.rcutwca;
+        if (f > 0 && f != 1 && f != 3) {
+            p.pdis = q[2];
+            p.pswitch = q[3];
+            p.pswitchINV = 1.0 / q[3];
+            p.rcut = (g != SPN) ? p.pswitch + p.pdis : 0.0;
+            p.rcutSq = p.rcut * p.rcut;
+        }
+        if (f == 1) for (int i = 0; i < 2; ++i) { p.len[i] = q[2]; p.half_len[i] = q[2] / 2; }
+        if (f == 3) for (int i = 0; i < 2; ++i) { p.len[i] = q[4]; p.half_len[i] = q[4] / 2; }
+        if (f > 2 && f != 3) {
+            for (int i = 0; i < 2; ++i) {
+                p.len[i] = q[6]; p.half_len[i] = q[6] / 2;
+                p.pcangl[i] = cos(q[4] / 2.0 / 180 * kPI);
+                p.pcanglsw[i] = cos((q[4] / 2.0 + q[5]) / 180 * kPI);
+                p.pcoshalfi[i] = cos((q[4] / 2.0 + q[5]) / 2.0 / 180 * kPI);
+                p.psinhalfi[i] = sqrt(1.0 - p.pcoshalfi[i] * p.pcoshalfi[i]);
+                p.parallel = q[7];
+            }
+        }
+        if (f == 7) for (int i = 0; i < 2; ++i) {
+            p.chiral_cos[i] = cos(q[8] / 360 * kPI);
+            p.chiral_sin[i] = sqrt(1 - p.chiral_cos[i] * p.chiral_cos[i]);
+        }
+        if (f == 9 || f == 10) for (int i = 0; i < 2; ++i) {
+            p.csecpatchrot[i] = cos(q[8] / 360 * kPI);
+            p.ssecpatchrot[i] = sqrt(1 - p.csecpatchrot[i] * p.csecpatchrot[i]);
+            p.pcangl[i + 2] = cos(q[9] / 2.0 / 180 * kPI);
+            p.pcanglsw[i + 2] = cos((q[9] / 2.0 + q[10]) / 180 * kPI);
+            p.pcoshalfi[i + 2] = cos((q[9] / 2.0 + q[10]) / 2.0 / 180 * kPI);
+            p.psinhalfi[i + 2] = sqrt(1.0 - p.pcoshalfi[i + 2] * p.pcoshalfi[i + 2]);
+        }
+        if (f == 10) for (int i = 0; i < 2; ++i) {
+            p.chiral_cos[i] = cos(q[11] / 360 * kPI);
+            p.chiral_sin[i] = sqrt(1 - p.chiral_cos[i] * p.chiral_cos[i]);
+        }
+        if (g < SP)
+            p.volume = 4.0 / 3.0 * kPI * pow((p.sigma) / 2.0, 3.0) + kPI / 2.0 * p.len[0] * pow((p.sigma) / 2.0, 2.0);
+        else
+            p.volume = 4.0 / 3.0 * kPI * pow((p.sigma) / 2.0, 3.0);
+        if (p.rcutwca > sqmaxcut) sqmaxcut = p.rcutwca;
+        if (p.rcut > sqmaxcut) sqmaxcut = p.rcut;
+    }
+    // raw patch angles, needed by the mixed pairs below
+    double pangl[OR_MAXT][4] = {}, panglsw[OR_MAXT][4] = {};
+    for (int k = 0; k < ntypes; ++k) {
+        const or_type_in& t = types[k];
+        if (t.nfields > 2 && t.nfields != 3) { pangl[t.type][0] = t.param[4]; panglsw[t.type][0] = t.param[5]; }
+        if (t.nfields == 9 || t.nfields == 10) { pangl[t.type][2] = t.param[9]; panglsw[t.type][2] = t.param[10]; }
+    }
+    double length = 0;
+    for (int i = 0; i < OR_MAXT; ++i) {
+        for (int j = 0; j < OR_MAXT; ++j) {
+            if (i == j) continue;
+            const or_param& di = ia[i * OR_MAXT + i];
+            const or_param& dj = ia[j * OR_MAXT + j];
+            if (dj.geotype[0] == 0 || di.geotype[0] == 0) continue;
+            or_param& p = ia[i * OR_MAXT + j];
+            int a[2] = {i, j};
+            for (int k = 0; k < 2; ++k) {
+                const or_param& dk = ia[a[k] * OR_MAXT + a[k]];
+                p.geotype[k] = dk.geotype[0];
+                p.len[k] = dk.len[0];
+                if (dk.len[0] > 0) {
+                    if (length == 0) length = dk.len[0];
+                    else if (length > 0 && length != dk.len[0]) return -2;   // topo.cpp:25-32
+                }
+                p.half_len[k] = dk.half_len[0];
+                if (p.geotype[k] >= PSC && p.geotype[k] < SP) {
+                    double pa = pangl[a[k]][0], ps = panglsw[a[k]][0];
+                    p.pcangl[k] = cos(pa / 2.0 / 180 * kPI);
+                    p.pcanglsw[k] = cos((pa / 2.0 + ps) / 180 * kPI);
+                    p.pcoshalfi[k] = cos((pa / 2.0 + ps) / 2.0 / 180 * kPI);
+                    p.psinhalfi[k] = sqrt(1.0 - p.pcoshalfi[k] * p.pcoshalfi[k]);
+                }
+                if (isCHF(p.geotype[k])) { p.chiral_cos[k] = dk.chiral_cos[0]; p.chiral_sin[k] = dk.chiral_sin[0]; }
+                if (isTF(p.geotype[k])) {
+                    p.csecpatchrot[k] = dk.csecpatchrot[0];
+                    p.ssecpatchrot[k] = dk.ssecpatchrot[0];
+                    double pa = pangl[a[k]][2], ps = panglsw[a[k]][2];
+                    p.pcangl[k + 2] = cos(pa / 2.0 / 180 * kPI);
+                    p.pcanglsw[k + 2] = cos((pa / 2.0 + ps) / 180 * kPI);
+                    p.pcoshalfi[k + 2] = cos((pa / 2.0 + ps) / 2.0 / 180 * kPI);
+                    p.psinhalfi[k + 2] = sqrt(1.0 - p.pcoshalfi[k + 2] * p.pcoshalfi[k + 2]);
+                }
+            }
+            p.sigma = ((di.sigma + dj.sigma) * 0.5);
+            p.epsilon = sqrt(di.epsilon * dj.epsilon);
+            p.A = 4 * p.epsilon * pow(p.sigma, 12);
+            p.B = 4 * p.epsilon * pow(p.sigma, 6);
+            p.pswitch = ((di.pswitch + dj.pswitch) * 0.5);
+            p.pswitchINV = 1.0 / p.pswitch;
+            p.rcutwca = (p.sigma) * pow(2.0, 1.0 / 6.0);
+            p.rcutwcaSq = p.rcutwca * p.rcutwca;
+            if ((di.parallel > 0) && (dj.parallel > 0)) p.parallel = sqrt(di.parallel * dj.parallel);
+            if ((di.parallel < 0) && (dj.parallel < 0)) p.parallel = -sqrt(di.parallel * dj.parallel);
+            p.pdis = (((di.pdis - di.rcutwca) + (dj.pdis - dj.rcutwca)) * 0.5) + p.rcutwca;
+            p.rcut = (p.geotype[0] == SPN || p.geotype[1] == SPN) ? 0.0 : p.pswitch + p.pdis;
+            p.rcutSq = p.rcut * p.rcut;
+            if (p.rcutwca > sqmaxcut) sqmaxcut = p.rcutwca;
+            if (p.rcut > sqmaxcut) sqmaxcut = p.rcut;
+        }
+    }
+    for (int i = 0; i < OR_MAXT; ++i)
+        for (int j = 0; j < OR_MAXT; ++j) ia[i * OR_MAXT + j].exclude = excl ? excl[i * OR_MAXT + j] : 0;
+    double maxlength = 0;
+    for (int i = 0; i < OR_MAXT; ++i) if (maxlength < ia[i * OR_MAXT + i].len[0]) maxlength = ia[i * OR_MAXT + i].len[0];
+    sqmaxcut += maxlength;
+    sqmaxcut *= 1.1;
+    *maxcutOut = sqmaxcut;
+    *sqmaxcutOut = sqmaxcut * sqmaxcut;
+    return 0;
+}
+
+// Particle::init (scOOP/structures/particle.cpp:3-79)
+void or_particle_init(or_particle* p, const or_param* d) {
+    int g = d->geotype[0];
+    if (g == SCA || g == SCN) return;
+    normalise(p->dir);
+    ortho(p->pd[0], p->dir);
+    normalise(p->pd[0]);
+    if (g == PSC || g == CPSC || g == TPSC || g == TCPSC) {
+        p->ps[0] = p->pd[0]; rotate(p->ps[0], p->dir, d->pcoshalfi[0], d->psinhalfi[0]);
+        p->ps[1] = p->pd[0]; rotate(p->ps[1], p->dir, d->pcoshalfi[0], -1.0 * d->psinhalfi[0]);
+    }
+    if (isTF(g)) {
+        p->pd[1] = p->pd[0];
+        rotate(p->pd[1], p->dir, d->csecpatchrot[0], d->ssecpatchrot[0]);
+        ortho(p->pd[1], p->dir);
+        normalise(p->pd[1]);
+    }
+    if (g == TPSC || g == TCPSC) {
+        p->ps[2] = p->pd[1]; rotate(p->ps[2], p->dir, d->pcoshalfi[2], d->psinhalfi[2]);
+        p->ps[3] = p->pd[1]; rotate(p->ps[3], p->dir, d->pcoshalfi[2], -1.0 * d->psinhalfi[2]);
+    }
+    if (isCHF(g)) {
+        p->ch[0] = p->dir; rotate(p->ch[0], p->pd[0], d->chiral_cos[0], d->chiral_sin[0]);
+        p->ps[0] = p->pd[0]; rotate(p->ps[0], p->ch[0], d->pcoshalfi[0], d->psinhalfi[0]);
+        p->ps[1] = p->pd[0]; rotate(p->ps[1], p->ch[0], d->pcoshalfi[0], -1.0 * d->psinhalfi[0]);
+    }
+    if (g == TCHPSC || g == TCHCPSC) {
+        p->ch[1] = p->dir; rotate(p->ch[1], p->pd[1], d->chiral_cos[0], d->chiral_sin[0]);
+        p->ps[2] = p->pd[1]; rotate(p->ps[2], p->ch[1], d->pcoshalfi[2], d->psinhalfi[2]);
+        p->ps[3] = p->pd[1]; rotate(p->ps[3], p->ch[1], d->pcoshalfi[2], -1.0 * d->psinhalfi[2]);
+    }
+}
+
+// Particle::pscRotate (scOOP/structures/particle.h:182-272); positive selects +sin.
+void or_psc_rotate(or_particle* p, int g, double angle, or_vec ax, int positive) {
+    double vc = cos(angle);
+    double vs = positive ? sqrt(1.0 - vc * vc) : -sqrt(1.0 - vc * vc);
+    double qw = vc, qx = ax.x * vs, qy = ax.y * vs, qz = ax.z * vs;
+    double t2 = qw * qx, t3 = qw * qy, t4 = qw * qz, t5 = -qx * qx, t6 = qx * qy, t7 = qx * qz, t8 = -qy * qy,
+           t9 = qy * qz, t10 = -qz * qz;
+    double d1 = t8 + t10, d2 = t6 - t4, d3 = t3 + t7, d4 = t4 + t6, d5 = t5 + t10, d6 = t9 - t2, d7 = t7 - t3,
+           d8 = t2 + t9, d9 = t5 + t8;
+    auto rot = [&](or_vec& v) {
+        double nx = 2.0 * (d1 * v.x + d2 * v.y + d3 * v.z) + v.x;
+        double ny = 2.0 * (d4 * v.x + d5 * v.y + d6 * v.z) + v.y;
+        double nz = 2.0 * (d7 * v.x + d8 * v.y + d9 * v.z) + v.z;
+        v.x = nx; v.y = ny; v.z = nz;
+    };
+    rot(p->dir);
+    if (g != SCN && g != SCA) {
+        int m = isTF(g) ? 2 : 1;
+        for (int k = 0; k < m; ++k) { rot(p->pd[k]); rot(p->ps[2 * k]); rot(p->ps[2 * k + 1]); }
+    }
+    if (isCHF(g)) {
+        int m = (g == TCHPSC || g == TCHCPSC) ? 2 : 1;
+        for (int k = 0; k < m; ++k) rot(p->ch[k]);
+    }
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// Sequential Metropolis loop: the reference's Updater::simulate step loop
+// (scOOP/mc/updater.cpp:206-230) with particleMove / partDisplace / partRotate
+// (movecreator.cpp:11-33, 947-1028), the ptype-1 volume move (390-421) and the
+// Verlet pair list of genSimplePairList (updater.cpp:484-552, cutoff main.cpp:117-126).
+// Used only as the timed CPU baseline; it draws from a splitmix64 stream
+// instead of dSFMT, which changes the trajectory but not the algorithm.
+namespace {
+
+struct Rng {
+    uint64_t s;
+    double operator()() {
+        uint64_t z = (s += 0x9e3779b97f4a7c15ull);
+        z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+        z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+        z ^= z >> 31;
+        return (z >> 11) * (1.0 / 9007199254740992.0);
+    }
+};
+
+or_vec randomUnitSphere(Rng& r) {     // Vector::randomUnitSphere (Vector.h:190-205)
+    double a, xi1, xi2;
+    do { xi1 = 1.0 - 2.0 * r(); xi2 = 1.0 - 2.0 * r(); a = xi1 * xi1 + xi2 * xi2; } while (a > 1.0);
+    double b = 2.0 * sqrt(1.0 - a);
+    return V(xi1 * b, xi2 * b, 1.0 - 2.0 * a);
+}
+
+struct PairList {
+    std::vector<std::vector<int>> nb;
+    void build(const or_system* s, double cut2) {
+        nb.assign(s->n, {});
+        for (int i = 0; i < s->n; ++i) {
+            Con con = getConlist(s, i);
+            for (int j = 0; j < s->n; ++j) {
+                if (i == j) continue;
+                or_vec r = image(s->p[i].pos, s->p[j].pos, s->box);
+                bool bonded = (j == con.idx[0] || j == con.idx[1] || j == con.idx[2] || j == con.idx[3]);
+                if (dot(r, r) < cut2 || bonded) nb[i].push_back(j);
+            }
+        }
+    }
+};
+
+double oneToAllList(const or_system* s, int t, const PairList* pl) {
+    if (!pl) return or_one_to_all(s, t);
+    double e = 0.0;
+    for (int j : pl->nb[t]) e += or_pair_energy(s, t, j, nullptr, nullptr);
+    return e;
+}
+
+}  // namespace
+
+extern "C" int or_mc_run(or_system* s, const or_mc_opts* o, or_mc_stats* st) {
+    std::memset(st, 0, sizeof(*st));
+    Rng rng{(uint64_t)o->seed * 0x2545F4914F6CDD1Dull + 1};
+    const int N = s->n;
+    if (N <= 0) return -1;
+    double shprob = o->shave / (double)N;
+    PairList plist;
+    PairList* pl = nullptr;
+    double cut2 = 0.0;
+    if (o->pairlist_update > 0) {
+        double c = o->transmx;    // AVER of equal step sizes
+        c *= (1 + o->pairlist_update) * 2;
+        c += sqrt(s->sqmaxcut);
+        cut2 = c * c;
+        pl = &plist;
+    }
+    auto t0 = std::chrono::steady_clock::now();
+    double energy = or_all_to_all(s);
+    st->energy_start = energy;
+    long moves = 0;
+    for (long sweep = 1; sweep <= o->nsweeps; ++sweep) {
+        if (pl && (sweep == 1 || sweep % o->pairlist_update == 0)) pl->build(s, cut2);
+        for (int step = 1; step <= N; ++step) {
+            if (o->max_moves > 0 && moves >= o->max_moves) goto finish;
+            ++moves;
+            double u = rng();
+            if (u < shprob && o->ptype == 1) {
+                double psch = o->edge_mx * (rng() - 0.5);
+                double pvol = s->box[0] * s->box[1] * s->box[2];
+                double b0[3] = {s->box[0], s->box[1], s->box[2]};
+                s->box[0] += psch; s->box[1] += psch; s->box[2] += psch;
+                double pvoln = s->box[0] * s->box[1] * s->box[2];
+                double enermove = o->press * (pvoln - pvol) - (double)N * o->temper * log(pvoln / pvol);
+                double enew = or_all_to_all(s);
+                enermove += enew;
+                bool rej = !(enermove <= energy) && !(exp(-1.0 * (enermove - energy) / o->temper) > rng());
+                if (rej) { s->box[0] = b0[0]; s->box[1] = b0[1]; s->box[2] = b0[2]; ++st->rej_vol; }
+                else { ++st->acc_vol; energy = enew; }
+                continue;
+            }
+            int target = (int)(rng() * N);
+            or_particle orig = s->p[target];
+            const or_param& d = P(s, orig.type, orig.type);
+            double eold = oneToAllList(s, target, pl);
+            bool displace = (rng() < 0.5) || d.geotype[0] >= SP;
+            if (displace) {
+                or_vec dr = randomUnitSphere(rng);
+                s->p[target].pos.x += dr.x * o->transmx / s->box[0];
+                s->p[target].pos.y += dr.y * o->transmx / s->box[1];
+                s->p[target].pos.z += dr.z * o->transmx / s->box[2];
+            } else {
+                double ang = o->rot_angle * rng();
+                or_vec ax = randomUnitSphere(rng);
+                or_psc_rotate(&s->p[target], d.geotype[0], ang, ax, rng() < 0.5);
+                ortho(s->p[target].pd[0], s->p[target].dir);
+            }
+            double enew = oneToAllList(s, target, pl);
+            bool rej = !(enew <= eold) && !(exp(-1.0 * (enew - eold) / o->temper) > rng());
+            if (rej) {
+                s->p[target] = orig;
+                if (displace) ++st->rej_trans; else ++st->rej_rot;
+            } else {
+                energy += enew - eold;
+                if (displace) ++st->acc_trans; else ++st->acc_rot;
+            }
+        }
+    }
+finish:
+    st->moves = moves;
+    st->energy = energy;
+    st->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return 0;
+}

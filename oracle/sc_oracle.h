@@ -1,0 +1,113 @@
+/* sc_oracle.h -- CPU oracle for the SC Metropolis hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain C++ restatement of the reference's
+ * pair energy, one-particle / total energy and single-particle move loop
+ * (robertvacha/SC, scOOP/mc/paire.h, paire.cpp, totalenergycalculator.h,
+ * movecreator.cpp, updater.cpp, structures/topo.cpp, particle.*), used by the
+ * tests as the checker and by bench.py as the timed CPU baseline.  The product
+ * (sc_gb300/) never includes, links or loads it.
+ *
+ * Parity is pinned: tests/test_oracle_golden.py compares every function below
+ * with golden vectors produced by the reference itself (oracle/ref_dump.cpp,
+ * built from the reference's own sources by oracle/Makefile).
+ */
+#ifndef SC_ORACLE_H
+#define SC_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OR_MAXT 40
+
+typedef struct { double x, y, z; } or_vec;
+
+/* One entry of the reference's Ia_param table (scOOP/structures/structures.h:187-254). */
+typedef struct {
+    int geotype[2];
+    int exclude;
+    int pad_;
+    double sigma, epsilon, A, B, pdis, pswitch, pswitchINV;
+    double pcangl[4], pcanglsw[4];
+    double rcut, rcutSq, rcutwca, rcutwcaSq;
+    double pcoshalfi[4], psinhalfi[4];
+    double csecpatchrot[2], ssecpatchrot[2];
+    double volume;
+    double len[2], half_len[2];
+    double chiral_cos[2], chiral_sin[2];
+    double parallel;
+} or_param;
+
+/* Raw per-type line of the [Types] section of top.init (scOOP/mc/inicializer.cpp:660-852). */
+typedef struct {
+    int type;          /* type number 0..39 */
+    int geotype;       /* SC codes: SCN=10 .. TCHCPSC=19, SPN=30, SPA=31 */
+    int nfields;       /* numeric fields after EPSILON SIGMA (inicializer.cpp:688) */
+    int pad_;
+    double param[12];  /* eps, sigma, pdis, pswitch, pangl, panglsw, len, parallel, secrot|chiral, pangl2, panglsw2, chiral */
+} or_type_in;
+
+/* Particle (scOOP/structures/particle.h:24-37), positions in box fractions. */
+typedef struct {
+    or_vec pos, dir, pd[2], ps[4], ch[2];
+    int type, molType;
+} or_particle;
+
+/* Molecule type (scOOP/structures/moleculeparams.h:10-79) with its place in the particle vector. */
+typedef struct {
+    int size, first, count, pad_;
+    double bond1c, bond1eq, bond2c, bond2eq, bonddc, bonddeq, bondhc, bondheq;
+    double angle1c, angle1eq, angle2c, angle2eq;
+} or_moltype;
+
+typedef struct {
+    int n;
+    int nmol;
+    or_particle* p;
+    const or_moltype* mols;
+    const or_param* params;   /* OR_MAXT*OR_MAXT, row-major [t1][t2] */
+    double box[3];
+    double sqmaxcut;
+} or_system;
+
+/* Verdict bits, shared with the CUDA kernels' layout. */
+enum {
+    OR_V_EVAL = 1u << 0, OR_V_WCA = 1u << 1, OR_V_ATR = 1u << 2, OR_V_FAR = 1u << 3
+};
+
+double or_pair_energy(const or_system* s, int i, int j, unsigned* bits, double* distSq);
+double or_one_to_all(const or_system* s, int target);
+double or_all_to_all(const or_system* s);
+double or_mol2others(const or_system* s, int first, int size);
+
+int or_derive_params(const or_type_in* types, int ntypes, const unsigned char* exclusions /* 40x40 or NULL */,
+                     or_param* out /* 40x40 */, double* sqmaxcut, double* maxcut);
+void or_particle_init(or_particle* p, const or_param* diag);
+void or_psc_rotate(or_particle* p, int geotype, double angle, or_vec axis, int positive);
+
+typedef struct {
+    long nsweeps;
+    long seed;
+    double temper, press, shave, chainprob;
+    double transmx;      /* full displacement length, already doubled as sim.h:365 does */
+    double rot_angle;    /* half-angle bound, rotmx/180*PI/4 as sim.h:359 */
+    double edge_mx;      /* full edge change range, already doubled */
+    double chainmmx, chainr_angle;
+    int ptype;
+    int pairlist_update; /* 0: brute force; k: Verlet list rebuilt every k sweeps */
+    long max_moves;      /* stop after this many attempted moves (0: no bound) */
+} or_mc_opts;
+
+typedef struct {
+    long moves, acc_trans, rej_trans, acc_rot, rej_rot, acc_vol, rej_vol, acc_chain, rej_chain;
+    double energy;       /* running total energy */
+    double energy_start;
+    double seconds;
+} or_mc_stats;
+
+int or_mc_run(or_system* s, const or_mc_opts* o, or_mc_stats* st);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
