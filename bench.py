@@ -1,0 +1,353 @@
+#!/usr/bin/env python3
+"""Benchmark: attempted Metropolis moves per second on one GB300.
+
+Workload (default): the NPT binary mixture -- 4000 particles, 2000 CPSC (length 3,
+cylindrical patch 120 deg) + 2000 attractive spheres SPA (sigma 1, eps 0.5 kT, range
+1.5), P* = 0.5, T = 1, one isotropic volume move per sweep -- as a seeded synthetic
+start (sc_gb300/workloads.py).  A step is one sweep: N attempted single-particle
+moves on the checkerboard plus the volume move, all through the C ABI.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  `value` is device-timed moves/s (CUDA events on the library's
+stream, L2 flushed between steps); `e2e` is the same metric through the public API
+with host buffers (state uploaded before and downloaded after every step).
+`--impl reference` times the CPU restatement of the reference's own loop (oracle/,
+sequential Metropolis with the reference's Verlet list and O(N^2) volume move) on
+all host cores, independent seeds per core.
+"""
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+METRIC = "MC moves/s on 1 GB300: plain FP64 kernel vs surrogate delayed-acceptance"
+UNIT = "moves/s"
+WORKLOAD = "npt_cpsc_spa_4000"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default=WORKLOAD)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def open_workload(name, seed):
+    from sc_gb300 import System, workloads
+
+    opts, top, cfg = workloads.WORKLOADS[name](seed)
+    return System.from_text(opts, top, cfg), (opts, top, cfg)
+
+
+def oracle_system(texts, seed):
+    """The oracle's view of the same start: parameters derived by the oracle itself."""
+    import numpy as np
+
+    import oracle_ffi as O
+    from sc_gb300 import System
+
+    opts, top, cfg = texts
+    s = System.from_text(opts, top, cfg)
+    parts = s.particles()
+    box = list(s.box)
+    p = s.default_run()
+    s.close()
+    types, excl = O.parse_types(top)
+    arr = (O.TypeIn * len(types))(*types)
+    table = (O.Param * (O.MAXT * O.MAXT))()
+    sq, mc = C.c_double(), C.c_double()
+    assert O.lib().or_derive_params(arr, len(types), excl.ctypes.data, table, C.byref(sq), C.byref(mc)) == 0
+    op = (O.Particle * len(parts))()
+    for k, q in enumerate(parts):
+        op[k].pos, op[k].dir = O.vec(q.pos), O.vec(q.dir)
+        for m in range(2):
+            op[k].pd[m], op[k].ch[m] = O.vec(q.patchdir[m]), O.vec(q.chdir[m])
+        for m in range(4):
+            op[k].ps[m] = O.vec(q.patchsides[m])
+        op[k].type, op[k].molType = q.type, q.molType
+    nmol = max(q.molType for q in parts) + 1
+    mols = (O.MolType * nmol)()
+    for m in range(nmol):
+        mols[m].size = 1
+        for key in ("bond1", "bond2", "bondd", "bondh", "angle1", "angle2"):
+            setattr(mols[m], key + "c", -1.0)
+    sysm = O.System()
+    sysm.n, sysm.nmol = len(parts), nmol
+    sysm.p = C.cast(op, C.POINTER(O.Particle))
+    sysm.mols = C.cast(mols, C.POINTER(O.MolType))
+    sysm.params = C.cast(table, C.POINTER(O.Param))
+    for k in range(3):
+        sysm.box[k] = box[k]
+    sysm.sqmaxcut = sq.value
+    o = O.McOpts()
+    o.seed = seed
+    o.temper, o.press, o.shave = p.temper, p.press, 1.0 if p.volume_every else 0.0
+    o.transmx, o.rot_angle, o.edge_mx = p.transmx, p.rot_angle, p.edge_mx
+    o.ptype = p.ptype
+    o.pairlist_update = 10
+    keep = (op, mols, table, arr)
+    return sysm, o, len(parts), keep
+
+
+def cpu_run(texts, seed, nsweeps, max_moves):
+    import oracle_ffi as O
+
+    sysm, o, n, keep = oracle_system(texts, seed)
+    o.nsweeps = nsweeps
+    o.max_moves = max_moves
+    st = O.McStats()
+    O.lib().or_mc_run(C.byref(sysm), C.byref(o), C.byref(st))
+    return st.moves, st.seconds
+
+
+def _worker(args):
+    texts, seed, nsweeps, max_moves = args
+    return cpu_run(texts, seed, nsweeps, max_moves)
+
+
+def run_reference(a, rank, world):
+    """CPU arm: the oracle's restatement of the reference loop on all host cores."""
+    if rank != 0:
+        return
+    import multiprocessing as mp
+
+    from sc_gb300 import workloads
+
+    texts = workloads.WORKLOADS[a.workload](a.seed)
+    n = texts[2].count("\n") - 1
+    cores = os.cpu_count() or 1
+    # size one step so that warm-up + steps stay within a few minutes
+    probe_moves, probe_s = cpu_run(texts, a.seed, 1, n)
+    per_move = probe_s / max(1, probe_moves)
+    budget = 150.0 / max(1, a.steps + a.warmup)
+    step_moves = int(max(100, min(n, budget / per_move)))
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        pool.map(_worker, [(texts, a.seed + 100 + k, 1, step_moves * a.warmup) for k in range(cores)])
+        t0 = time.perf_counter()
+        res = pool.map(_worker, [(texts, a.seed + 1000 + k, 1, step_moves * a.steps) for k in range(cores)])
+        wall = time.perf_counter() - t0
+    moves = sum(m for m, _ in res)
+    value = moves / wall
+    sample = (f"{cores} independent seeds x {step_moves * a.steps} moves of {a.workload} (sequential Metropolis, "
+              f"reference Verlet list every 10 sweeps, O(N^2) volume move with probability 1/N per move)")
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * wall / a.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": a.workload, "n_particles": n, "seed": a.seed, "cores": cores},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    a = parse()
+    rank, world, local = dist_info()
+    if a.impl == "reference":
+        run_reference(a, rank, world)
+        return
+    import numpy as np
+    import torch
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    from sc_gb300 import System  # noqa: F401
+
+    s, texts = open_workload(a.workload, a.seed)
+    from sc_gb300 import _lib as L
+
+    L.check(s._lib.sc_set_device(s._h, local))
+    n = s.n
+    p = s.default_run()
+    p.seed = a.seed + 7919 * rank
+    p.check_every = 0
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
+
+    def l2_flush():
+        flush.zero_()
+        torch.cuda.synchronize()
+
+    # warm-up
+    s.simulate(p, nsweeps=max(3, a.warmup))
+    # kernel-level timing of the move kernels and pair counters (separate short run)
+    prof = s.simulate(p, nsweeps=5, time_phases=1)
+    p.time_phases = 0
+    clocks = Clocks(local)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    dev_s = 0.0
+    moves = 0
+    launches = 0
+    tested = evaluated = 0
+    acc = 0
+    for k in range(a.steps):
+        l2_flush()
+        st = s.simulate(p, nsweeps=1)
+        dev_s += st.seconds
+        moves += st.moves
+        launches += st.launches
+        tested += st.pairs_tested
+        evaluated += st.pairs_evaluated
+        acc += st.acc_trans + st.acc_rot
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    t_max = dev_s
+    if dist:
+        t = torch.tensor([dev_s], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    value = moves * world / t_max
+
+    # end to end through the public API with host buffers
+    state = s.particles()
+    bytes_per_particle = C.sizeof(L.Particle)
+    e2e_moves = 0
+    t0 = time.perf_counter()
+    for k in range(a.steps):
+        s.set_particles(0, state)                 # host -> device (uploaded by the next call)
+        st = s.simulate(p, nsweeps=1)
+        state = s.particles()                     # device -> host
+        e2e_moves += st.moves
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": e2e_moves * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": n * bytes_per_particle,
+           "d2h_bytes_per_step": 2 * n * bytes_per_particle + 64,
+           "note": "state uploaded from pageable host memory before and downloaded after every sweep"}
+
+    peaks, peak_kind = measured_peaks()
+    # algorithmic bytes of the move kernel: 28 B (position + type) per candidate pair tested
+    # (old and new configuration), 24 B axis + 96 B patch vectors per pair evaluated
+    bytes_per_launch = (prof.pairs_tested * 28 + prof.pairs_evaluated * 120) / max(1, prof.phase_launches)
+    t_launch = prof.phase_seconds / max(1, prof.phase_launches)
+    achieved = bytes_per_launch / t_launch / 1e9 if t_launch > 0 else None
+    roof = {"bound": "hbm", "kernel": "kColour", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "frac": (achieved / peaks["hbm_gbs"]) if achieved else None, "traffic": None,
+            "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+            "avg_launch_us": t_launch * 1e6, "algorithmic_bytes_per_launch": bytes_per_launch,
+            "note": "the move kernel is FP64-latency bound; see fp64 for its arithmetic rate"}
+    flops_per_launch = (prof.pairs_tested * 17 + prof.pairs_evaluated * 600) / max(1, prof.phase_launches)
+    fp64 = {"achieved_tflops": flops_per_launch / t_launch / 1e12 if t_launch > 0 else None,
+            "peak_tflops_nominal": 1.25,
+            "note": "17 FP64 ops per candidate pair (image + r^2), ~600 per evaluated pair (estimate from the kernel "
+                    "source); nominal GB300 FP64 peak, not measured"}
+
+    # CPU baseline: the oracle restatement of the reference loop, one core, bounded sample
+    cpu = None
+    if rank == 0:
+        try:
+            probe_moves, probe_s = cpu_run(texts, a.seed, 1, 400)
+            per_move = probe_s / max(1, probe_moves)
+            target = int(max(1000, min(50 * n, a.cpu_seconds / per_move)))
+            m, sec = cpu_run(texts, a.seed, 100, target)
+            cpu = {"value": m / sec, "unit": UNIT, "cores": 1, "kind": "port",
+                   "sample": f"{m} moves of {a.workload} from the same start (oracle/sc_oracle.cpp or_mc_run: "
+                             f"sequential Metropolis, Verlet list every 10 sweeps, O(N^2) volume move)"}
+        except Exception as ex:  # the baseline is reported, not required
+            cpu = {"value": None, "unit": UNIT, "cores": 1, "kind": "port", "sample": f"failed: {ex}"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+                "warmup": a.warmup, "ms_per_step": 1e3 * t_max / a.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": a.workload, "n_particles": n, "step": "one sweep (N moves) + volume move",
+                           "parallelism": "replicas" if world > 1 else "single", "l2": "flushed between steps",
+                           "seed": a.seed, "plain_fp64": True},
+                "clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roof, "fp64": fp64,
+                "cpu_baseline": cpu,
+                "detail": {"acceptance": acc / max(1, moves), "pairs_tested_per_move": tested / max(1, moves),
+                           "pairs_evaluated_per_move": evaluated / max(1, moves)}}
+        print(json.dumps(line), flush=True)
+    s.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

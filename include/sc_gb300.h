@@ -1,0 +1,160 @@
+/* sc_gb300.h -- C ABI of the GB300 Metropolis hot path for patchy spherocylinders.
+ *
+ * Drop-in boundary for the energy / move path of SC (robertvacha/SC, "scOOP").
+ * The reference binds this path at compile time, not through an FFI:
+ *     typedef TotalEMatrix<PairE> TotalEnergyCalculator;   scOOP/mc/totalenergycalculator.h:1227
+ * consumed by Updater (scOOP/mc/updater.h:33) and MoveCreator (scOOP/mc/movecreator.h:15,36)
+ * through the TotalE virtual interface (totalenergycalculator.h:136-297).  Each
+ * entry point below names the reference call it replaces.
+ *
+ * Conventions
+ *   - Every call returns SC_OK (0) or a negative SC_ERR_* code; sc_last_error()
+ *     returns a message for the calling thread.  Nothing here exits the process.
+ *   - Plain pointers and sizes only; host buffers belong to the caller.
+ *   - One context = one system on one CUDA device and one stream.  A context is
+ *     not shared between threads.
+ *   - Positions are box fractions (the reference's internal coordinates),
+ *     energies in the reference's units (kT/epsilon scale of top.init).
+ */
+#ifndef SC_GB300_H
+#define SC_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SC_OK 0
+#define SC_ERR_ARG (-1)        /* bad argument (null pointer, index out of range) */
+#define SC_ERR_IO (-2)         /* a file could not be read or written */
+#define SC_ERR_PARSE (-3)      /* options / top.init / config.init rejected */
+#define SC_ERR_CUDA (-4)       /* a CUDA call failed (no device, launch error) */
+#define SC_ERR_RANGE (-5)      /* a size beyond a documented maximum */
+#define SC_ERR_STATE (-6)      /* call not valid in the current state */
+#define SC_ERR_UNSUPPORTED (-7) /* input outside the GPU path (see sc_last_error) */
+#define SC_ERR_DEVICE (-8)     /* a kernel reported an error status (e.g. cell overflow) */
+
+typedef struct sc_context sc_context;
+
+/* Derived interaction parameters of one type pair: the fields of the reference's
+ * Ia_param (scOOP/structures/structures.h:187-254) that the energy uses. */
+typedef struct {
+    int geotype[2];
+    int exclude;
+    int kind;            /* pair functor chosen as in PairE::initIntFCE (scOOP/mc/paire.cpp:6-80) */
+    double sigma, epsilon, A, B, pdis, pswitch, pswitchINV;
+    double pcangl[4], pcanglsw[4];
+    double rcut, rcutSq, rcutwca, rcutwcaSq;
+    double pcoshalfi[4], psinhalfi[4];
+    double csecpatchrot[2], ssecpatchrot[2];
+    double volume;
+    double len[2], half_len[2];
+    double chiral_cos[2], chiral_sin[2];
+    double parallel;
+} sc_pair_param;
+
+/* State of one particle, as Particle (scOOP/structures/particle.h:24-37). */
+typedef struct {
+    double pos[3];        /* box fractions */
+    double dir[3];
+    double patchdir[2][3];
+    double patchsides[4][3];
+    double chdir[2][3];
+    int type;
+    int molType;
+} sc_particle;
+
+/* Move-loop parameters: the options-file values of Sim (scOOP/structures/sim.h:15-70) the
+ * loop uses, after the unit conversions of sim.h:359-381.  sc_default_run() fills them
+ * from the options file of the context. */
+typedef struct {
+    long nsweeps;
+    unsigned long long seed;
+    double temper;
+    double press;
+    int ptype;              /* 0: NVT, 1: isotropic volume moves (movecreator.cpp:390-421) */
+    int volume_every;       /* sweeps between volume moves (options shave=1 -> every sweep); 0: none */
+    double transmx;         /* displacement length (already doubled, sim.h:365) */
+    double rot_angle;       /* half-angle bound of pscRotate (rotmx/180*PIH*0.5, sim.h:359) */
+    double edge_mx;         /* full edge-change range (already doubled, sim.h:363) */
+    double chainprob;       /* chain moves per particle move (0: none) */
+    double chainmmx;        /* chain displacement length (already doubled) */
+    double chain_angle;     /* chain rotation angle bound, radians */
+    int check_every;        /* sweeps between exact total-energy checks (0: none) */
+    int time_phases;        /* 1: time the move kernels with CUDA events (adds events to the stream) */
+} sc_run_params;
+
+typedef struct {
+    long sweeps;
+    long moves;              /* attempted single-particle moves */
+    long acc_trans, rej_trans, acc_rot, rej_rot;
+    long acc_vol, rej_vol, vol_constrained;   /* vol_constrained: proposals outside the cell-grid range */
+    long acc_chain, rej_chain;
+    long pairs_tested;       /* candidate pairs scanned (old + new configuration) */
+    long pairs_evaluated;    /* pairs that passed the cutoff prefilter */
+    double energy;           /* running total energy */
+    double energy_check;     /* last exact total energy (check_every) */
+    double max_drift;        /* max |running - exact| seen */
+    double seconds;          /* device time of the loop (CUDA events on the context's stream) */
+    double phase_seconds;    /* device time inside the move kernels (time_phases = 1) */
+    long phase_launches;     /* move-kernel launches */
+    long launches;           /* all kernels this call launched */
+} sc_run_stats;
+
+const char* sc_last_error(void);
+const char* sc_version(void);
+
+/* --- set-up: the reference's inputs --------------------------------------------------- */
+/* Reads options / top.init / config.init (Sim::readOptions sim.h:123-406,
+ * Inicializer::initTop inicializer.cpp:16-58, Inicializer::initConfig :89-298) and
+ * derives the interaction table (Topo::genParamPairs topo.cpp:5-153) and the patch
+ * vectors (Conf::partVecInit Conf.cpp:97-102).  No device memory is touched until the
+ * first energy or move call. */
+int sc_open(const char* options_path, const char* top_path, const char* config_path, sc_context** out);
+int sc_open_text(const char* options, const char* top, const char* config, sc_context** out);
+int sc_close(sc_context* ctx);
+int sc_set_device(sc_context* ctx, int device);
+
+/* --- state ------------------------------------------------------------------------------ */
+int sc_num_particles(const sc_context* ctx, int* n);
+int sc_get_box(sc_context* ctx, double box[3]);
+int sc_set_box(sc_context* ctx, const double box[3]);
+int sc_cutoff(const sc_context* ctx, double* sqmaxcut, double* maxcut);
+int sc_get_pair_param(const sc_context* ctx, int type1, int type2, sc_pair_param* out);
+int sc_get_particles(sc_context* ctx, int first, int count, sc_particle* out);
+int sc_set_particles(sc_context* ctx, int first, int count, const sc_particle* in);
+/* Conf::draw (scOOP/structures/Conf.h:388-425): the config.last text format. */
+int sc_write_config(sc_context* ctx, const char* path);
+
+/* --- energies: the TotalE interface ------------------------------------------------------ */
+/* TotalE::p2p (totalenergycalculator.h:200-203): PairE(i, j, conlist(i)). */
+int sc_pair_energy(sc_context* ctx, int i, int j, double* e);
+/* Batched PairE with branch verdicts (bit 0 evaluated, 1 repulsive, 2 attractive branch,
+ * 3 far, 8+ intersections) and the closest segment distance^2 (-1 if not evaluated). */
+int sc_pair_energies(sc_context* ctx, int npairs, const int* i, const int* j, double* e, unsigned* verdict,
+                     double* dist_sq);
+/* TotalEMatrix::oneToAll / oneToAllTrial (totalenergycalculator.h:355-415): energy of
+ * each target with every other particle. */
+int sc_one_to_all(sc_context* ctx, int ntargets, const int* targets, double* e);
+/* TotalEMatrix::allToAll (totalenergycalculator.h:334-353, 502-521). */
+int sc_all_to_all(sc_context* ctx, double* e);
+/* TotalEMatrix::mol2othersTrial (totalenergycalculator.h:453-499). */
+int sc_mol_to_others(sc_context* ctx, int first, int size, double* e);
+/* The energy half of MoveCreator::partDisplace / partRotate (movecreator.cpp:947-1028):
+ * old energy of the target, and its energy after displacing it by dr (box fractions) or
+ * after Particle::pscRotate(angle, axis, sign) (particle.h:182-272) followed by the
+ * re-orthogonalisation of patchdir[0].  The state is unchanged until sc_accept_trial(). */
+int sc_trial_displace(sc_context* ctx, int target, const double dr[3], double* e_old, double* e_new);
+int sc_trial_rotate(sc_context* ctx, int target, double angle, const double axis[3], int positive, double* e_old,
+                    double* e_new, sc_particle* trial_state);
+int sc_accept_trial(sc_context* ctx);
+/* Isotropic volume trial (movecreator.cpp:390-421): allToAllTrial with every box edge + psch. */
+int sc_trial_volume(sc_context* ctx, double psch, double* e_new);
+
+/* --- the move loop: Updater::simulate (scOOP/mc/updater.cpp:45-389) --------------------- */
+int sc_default_run(const sc_context* ctx, sc_run_params* p);
+int sc_simulate(sc_context* ctx, const sc_run_params* p, sc_run_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SC_GB300_H */

@@ -1,0 +1,110 @@
+"""ctypes binding of the C ABI declared in include/sc_gb300.h (libscgpu.so).
+
+There is no fallback: if the CUDA library is missing or fails to load, every
+call raises.  Build it with ``python -c "import __graft_entry__ as g; g.build()"``
+or ``python sc_gb300/build.py``.
+"""
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libscgpu.so")
+
+SC_OK = 0
+ERRORS = {-1: "SC_ERR_ARG", -2: "SC_ERR_IO", -3: "SC_ERR_PARSE", -4: "SC_ERR_CUDA", -5: "SC_ERR_RANGE",
+          -6: "SC_ERR_STATE", -7: "SC_ERR_UNSUPPORTED", -8: "SC_ERR_DEVICE"}
+
+
+class ScError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class PairParam(C.Structure):
+    _fields_ = [("geotype", C.c_int * 2), ("exclude", C.c_int), ("kind", C.c_int),
+                ("sigma", C.c_double), ("epsilon", C.c_double), ("A", C.c_double), ("B", C.c_double),
+                ("pdis", C.c_double), ("pswitch", C.c_double), ("pswitchINV", C.c_double),
+                ("pcangl", C.c_double * 4), ("pcanglsw", C.c_double * 4),
+                ("rcut", C.c_double), ("rcutSq", C.c_double), ("rcutwca", C.c_double), ("rcutwcaSq", C.c_double),
+                ("pcoshalfi", C.c_double * 4), ("psinhalfi", C.c_double * 4),
+                ("csecpatchrot", C.c_double * 2), ("ssecpatchrot", C.c_double * 2), ("volume", C.c_double),
+                ("len", C.c_double * 2), ("half_len", C.c_double * 2), ("chiral_cos", C.c_double * 2),
+                ("chiral_sin", C.c_double * 2), ("parallel", C.c_double)]
+
+
+class Particle(C.Structure):
+    _fields_ = [("pos", C.c_double * 3), ("dir", C.c_double * 3), ("patchdir", (C.c_double * 3) * 2),
+                ("patchsides", (C.c_double * 3) * 4), ("chdir", (C.c_double * 3) * 2), ("type", C.c_int),
+                ("molType", C.c_int)]
+
+
+class RunParams(C.Structure):
+    _fields_ = [("nsweeps", C.c_long), ("seed", C.c_ulonglong), ("temper", C.c_double), ("press", C.c_double),
+                ("ptype", C.c_int), ("volume_every", C.c_int), ("transmx", C.c_double), ("rot_angle", C.c_double),
+                ("edge_mx", C.c_double), ("chainprob", C.c_double), ("chainmmx", C.c_double),
+                ("chain_angle", C.c_double), ("check_every", C.c_int), ("time_phases", C.c_int)]
+
+
+class RunStats(C.Structure):
+    _fields_ = [(k, C.c_long) for k in ("sweeps", "moves", "acc_trans", "rej_trans", "acc_rot", "rej_rot",
+                                        "acc_vol", "rej_vol", "vol_constrained", "acc_chain", "rej_chain",
+                                        "pairs_tested", "pairs_evaluated")] + [
+        (k, C.c_double) for k in ("energy", "energy_check", "max_drift", "seconds", "phase_seconds")] + [
+        ("phase_launches", C.c_long), ("launches", C.c_long)]
+
+
+# (name, restype, argtypes) for every entry point of include/sc_gb300.h
+_P = C.c_void_p
+_D = C.POINTER(C.c_double)
+_I = C.POINTER(C.c_int)
+SIGNATURES = [
+    ("sc_last_error", C.c_char_p, []),
+    ("sc_version", C.c_char_p, []),
+    ("sc_open", C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, C.POINTER(_P)]),
+    ("sc_open_text", C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, C.POINTER(_P)]),
+    ("sc_close", C.c_int, [_P]),
+    ("sc_set_device", C.c_int, [_P, C.c_int]),
+    ("sc_num_particles", C.c_int, [_P, _I]),
+    ("sc_get_box", C.c_int, [_P, _D]),
+    ("sc_set_box", C.c_int, [_P, _D]),
+    ("sc_cutoff", C.c_int, [_P, _D, _D]),
+    ("sc_get_pair_param", C.c_int, [_P, C.c_int, C.c_int, C.POINTER(PairParam)]),
+    ("sc_get_particles", C.c_int, [_P, C.c_int, C.c_int, C.POINTER(Particle)]),
+    ("sc_set_particles", C.c_int, [_P, C.c_int, C.c_int, C.POINTER(Particle)]),
+    ("sc_write_config", C.c_int, [_P, C.c_char_p]),
+    ("sc_pair_energy", C.c_int, [_P, C.c_int, C.c_int, _D]),
+    ("sc_pair_energies", C.c_int, [_P, C.c_int, _I, _I, _D, C.POINTER(C.c_uint), _D]),
+    ("sc_one_to_all", C.c_int, [_P, C.c_int, _I, _D]),
+    ("sc_all_to_all", C.c_int, [_P, _D]),
+    ("sc_mol_to_others", C.c_int, [_P, C.c_int, C.c_int, _D]),
+    ("sc_trial_displace", C.c_int, [_P, C.c_int, _D, _D, _D]),
+    ("sc_trial_rotate", C.c_int, [_P, C.c_int, C.c_double, _D, C.c_int, _D, _D, C.POINTER(Particle)]),
+    ("sc_accept_trial", C.c_int, [_P]),
+    ("sc_trial_volume", C.c_int, [_P, C.c_double, _D]),
+    ("sc_default_run", C.c_int, [_P, C.POINTER(RunParams)]),
+    ("sc_simulate", C.c_int, [_P, C.POINTER(RunParams), C.POINTER(RunStats)]),
+]
+
+_lib = None
+
+
+def load():
+    """Loads libscgpu.so; raises if it is not built (there is no CPU fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build the CUDA library first (python sc_gb300/build.py)")
+        lib = C.CDLL(LIB_PATH)
+        for name, res, args in SIGNATURES:
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def check(rc):
+    if rc != SC_OK:
+        raise ScError(rc, load().sc_last_error().decode(errors="replace"))
+    return rc

@@ -1,0 +1,614 @@
+// sc_context.cu -- the C ABI (include/sc_gb300.h): context set-up, host<->device state
+// and the energy entry points.  The move loop lives in sweep.cu.
+
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/sc_gb300.h"
+#include "kernels.h"
+#include "sc_context.h"
+
+namespace scg {
+
+thread_local std::string g_lastError;
+
+int fail(int code, const std::string& msg) {
+    g_lastError = msg;
+    return code;
+}
+
+int cudaFail(cudaError_t e, const char* where) {
+    return fail(SC_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+Context::~Context() { freeDevice(); }
+
+void Context::freeDevice() {
+    destroyEngine(this);
+    if (!devReady) return;
+    cudaSetDevice(device);
+    for (void* p : allocations) cudaFree(p);
+    allocations.clear();
+    if (stream) cudaStreamDestroy(stream);
+    stream = nullptr;
+    devReady = false;
+}
+
+int Context::allocDev(void** p, size_t bytes) {
+    cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
+    if (e != cudaSuccess) return cudaFail(e, "cudaMalloc");
+    allocations.push_back(*p);
+    return SC_OK;
+}
+
+PairParam Context::devParam(int t1, int t2) const {
+    const IaParam& s = topo.ia[t1][t2];
+    PairParam p;
+    std::memset(&p, 0, sizeof p);
+    int g0 = s.geotype[0], g1 = s.geotype[1];
+    p.geotype[0] = g0;
+    p.geotype[1] = g1;
+    p.kind = functorKind(g0, g1);
+    p.exclude = s.exclude ? 1 : 0;
+    // getGeoTypes of the selected functor (paire.h:486-497, 674-685, 891-906)
+    if (p.kind == K_SC_PSC) {
+        p.fCH = (g0 == CHPSC || g0 == TCHPSC); p.sCH = (g1 == CHPSC || g1 == TCHPSC);
+        p.fT = (g0 == TPSC || g0 == TCHPSC); p.sT = (g1 == TPSC || g1 == TCHPSC);
+        p.firstPsc = p.secondPsc = 1;
+    } else if (p.kind == K_SC_CPSC) {
+        p.fCH = (g0 == CHCPSC || g0 == TCHCPSC); p.sCH = (g1 == CHCPSC || g1 == TCHCPSC);
+        p.fT = (g0 == TCPSC || g0 == TCHCPSC); p.sT = (g1 == TCPSC || g1 == TCHCPSC);
+    } else if (p.kind == K_SC_PSC_CPSC) {
+        p.fCH = isChiral(g0); p.sCH = isChiral(g1); p.fT = isTwoPatch(g0); p.sT = isTwoPatch(g1);
+        p.firstPsc = isPscFamily(g0);
+        p.secondPsc = !p.firstPsc;
+    }
+    // PscSpa / CPscSpa::getGeoTypes (paire.h:981-1005), read from the entry with the SC first
+    if (g0 < SP && p.kind == K_MIX_PSC_SP) { p.mixChiral = (g0 == CHPSC || g0 == TCHPSC); p.mixSec = (g0 == TPSC || g0 == TCHPSC); }
+    if (g0 < SP && p.kind == K_MIX_CPSC_SP) { p.mixChiral = (g0 == CHCPSC || g0 == TCHCPSC); p.mixSec = (g0 == TCPSC || g0 == TCHCPSC); }
+    p.sigma = s.sigma; p.epsilon = s.epsilon; p.A = s.A; p.B = s.B; p.pdis = s.pdis; p.pswitch = s.pswitch;
+    p.pswitchINV = s.pswitchINV;
+    for (int k = 0; k < 4; ++k) { p.pcangl[k] = s.pcangl[k]; p.pcanglsw[k] = s.pcanglsw[k]; }
+    p.rcut = s.rcut; p.rcutSq = s.rcutSq; p.rcutwca = s.rcutwca; p.rcutwcaSq = s.rcutwcaSq;
+    p.half_len[0] = s.half_len[0]; p.half_len[1] = s.half_len[1];
+    p.parallel = s.parallel;
+    return p;
+}
+
+int Context::setup(std::string& err) {
+    // compact type indices for the device table
+    std::memset(compactOf, -1, sizeof compactOf);
+    usedTypes.clear();
+    for (int t = 0; t < MAXT; ++t)
+        if (topo.ia[t][t].geotype[0] != 0) {
+            compactOf[t] = (int)usedTypes.size();
+            usedTypes.push_back(t);
+        }
+    if ((int)usedTypes.size() > MAX_DEV_TYPES) { err = "more particle types than the device table holds (16)"; return SC_ERR_RANGE; }
+    // molecule records
+    mols.clear();
+    for (auto& m : topo.mols) {
+        MolParam mp;
+        std::memset(&mp, 0, sizeof mp);
+        mp.size = (int)m.types.size();
+        // ParticleVector::getConlist (Conf.h:97-146): the last defined bond kind wins
+        if (m.bond1c >= 0.0 || m.bonddc >= 0.0 || m.bondhc >= 0.0) {
+            mp.bonded = 1;
+            if (m.bond1c >= 0.0) { mp.eq0 = m.bond1eq; mp.c0 = m.bond1c; mp.mod0 = 0; mp.mod1 = 0; mp.sp = 0; }
+            if (m.bonddc >= 0.0) { mp.eq0 = 0.0; mp.c0 = m.bonddc; mp.mod0 = m.bonddeq; mp.mod1 = 0; mp.sp = 0; }
+            if (m.bondhc >= 0.0) { mp.eq0 = 0.0; mp.c0 = m.bondhc; mp.mod0 = m.bondheq; mp.mod1 = m.bondheq; mp.sp = m.bondheq; }
+        }
+        if (m.bond2c >= 0.0) { mp.bonded2 = 1; mp.eq1 = m.bond2eq; mp.c1 = m.bond2c; }
+        mp.angle1c = m.angle1c; mp.angle1eq = m.angle1eq; mp.angle2c = m.angle2c; mp.angle2eq = m.angle2eq;
+        mols.push_back(mp);
+    }
+    if (mols.empty()) { MolParam z; std::memset(&z, 0, sizeof z); z.size = 1; mols.push_back(z); }
+    molInfo.resize(conf.p.size());
+    for (size_t i = 0; i < conf.p.size(); ++i) {
+        int m = conf.p[i].molType;
+        int size = (int)topo.mols[m].types.size();
+        int pos = ((int)i - conf.first[m]) % size;
+        molInfo[i] = make_int4(m, pos, size, (int)i - pos);
+    }
+    return SC_OK;
+}
+
+int Context::ensureDevice() {
+    if (!devReady) {
+        cudaError_t e = cudaSetDevice(device);
+        if (e != cudaSuccess) return cudaFail(e, "cudaSetDevice");
+        e = cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) return cudaFail(e, "cudaStreamCreate");
+        int n = (int)conf.p.size();
+        int T = (int)usedTypes.size();
+        int rc;
+        if ((rc = allocDev((void**)&d.pos, sizeof(double4_32a) * n))) return rc;
+        if ((rc = allocDev((void**)&d.dir, sizeof(double4_32a) * n))) return rc;
+        if ((rc = allocDev((void**)&d.patch, sizeof(PatchSet) * n))) return rc;
+        if ((rc = allocDev((void**)&d.mol, sizeof(int4) * n))) return rc;
+        if ((rc = allocDev((void**)&d.box, sizeof(double) * 4))) return rc;
+        if ((rc = allocDev((void**)&dParams, sizeof(PairParam) * T * T))) return rc;
+        if ((rc = allocDev((void**)&dMols, sizeof(MolParam) * mols.size()))) return rc;
+        if ((rc = allocDev((void**)&dTrial, sizeof(TrialSlot)))) return rc;
+        if ((rc = allocDev((void**)&dScalars, sizeof(double) * 64))) return rc;
+        nPartial = allToAllBlocks(n) + 1;
+        if ((rc = allocDev((void**)&dPartial, sizeof(double) * nPartial))) return rc;
+        d.n = n;
+        std::vector<PairParam> hp(T * T);
+        for (int a = 0; a < T; ++a)
+            for (int b = 0; b < T; ++b) hp[a * T + b] = devParam(usedTypes[a], usedTypes[b]);
+        e = cudaMemcpy(dParams, hp.data(), sizeof(PairParam) * T * T, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cudaFail(e, "upload params");
+        e = cudaMemcpy(dMols, mols.data(), sizeof(MolParam) * mols.size(), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cudaFail(e, "upload molecules");
+        e = cudaMemcpy(d.mol, molInfo.data(), sizeof(int4) * n, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cudaFail(e, "upload molecule records");
+        tables.params = dParams;
+        tables.mols = dMols;
+        tables.ntypes = T;
+        tables.sqmaxcut = topo.sqmaxcut;
+        devReady = true;
+        hostNewer = true;
+    }
+    if (hostNewer) {
+        int rc = uploadState();
+        if (rc) return rc;
+    }
+    return SC_OK;
+}
+
+int Context::uploadState() {
+    int n = (int)conf.p.size();
+    std::vector<double4_32a> hp(n), hd(n);
+    std::vector<PatchSet> hs(n);
+    for (int i = 0; i < n; ++i) {
+        const Particle& p = conf.p[i];
+        hp[i] = make_double4_32a(p.pos.x, p.pos.y, p.pos.z, (double)compactOf[p.type]);
+        hd[i] = make_double4_32a(p.dir.x, p.dir.y, p.dir.z, 0.0);
+        PatchSet& s = hs[i];
+        for (int k = 0; k < 2; ++k) { s.pd[k][0] = p.pd[k].x; s.pd[k][1] = p.pd[k].y; s.pd[k][2] = p.pd[k].z; }
+        for (int k = 0; k < 4; ++k) { s.ps[k][0] = p.ps[k].x; s.ps[k][1] = p.ps[k].y; s.ps[k][2] = p.ps[k].z; }
+        for (int k = 0; k < 2; ++k) { s.ch[k][0] = p.ch[k].x; s.ch[k][1] = p.ch[k].y; s.ch[k][2] = p.ch[k].z; }
+    }
+    double box[4] = {conf.box.x, conf.box.y, conf.box.z, 0.0};
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(d.pos, hp.data(), sizeof(double4_32a) * n, cudaMemcpyHostToDevice, stream)) != cudaSuccess) return cudaFail(e, "upload pos");
+    if ((e = cudaMemcpyAsync(d.dir, hd.data(), sizeof(double4_32a) * n, cudaMemcpyHostToDevice, stream)) != cudaSuccess) return cudaFail(e, "upload dir");
+    if ((e = cudaMemcpyAsync(d.patch, hs.data(), sizeof(PatchSet) * n, cudaMemcpyHostToDevice, stream)) != cudaSuccess) return cudaFail(e, "upload patch");
+    if ((e = cudaMemcpyAsync(d.box, box, sizeof(box), cudaMemcpyHostToDevice, stream)) != cudaSuccess) return cudaFail(e, "upload box");
+    if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return cudaFail(e, "upload sync");
+    hostNewer = false;
+    return SC_OK;
+}
+
+int Context::downloadState() {
+    if (!devReady || !devNewer) return SC_OK;
+    int n = (int)conf.p.size();
+    std::vector<double4_32a> hp(n), hd(n);
+    std::vector<PatchSet> hs(n);
+    double box[4];
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(hp.data(), d.pos, sizeof(double4_32a) * n, cudaMemcpyDeviceToHost, stream)) != cudaSuccess) return cudaFail(e, "download pos");
+    if ((e = cudaMemcpyAsync(hd.data(), d.dir, sizeof(double4_32a) * n, cudaMemcpyDeviceToHost, stream)) != cudaSuccess) return cudaFail(e, "download dir");
+    if ((e = cudaMemcpyAsync(hs.data(), d.patch, sizeof(PatchSet) * n, cudaMemcpyDeviceToHost, stream)) != cudaSuccess) return cudaFail(e, "download patch");
+    if ((e = cudaMemcpyAsync(box, d.box, sizeof(box), cudaMemcpyDeviceToHost, stream)) != cudaSuccess) return cudaFail(e, "download box");
+    if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return cudaFail(e, "download sync");
+    for (int i = 0; i < n; ++i) {
+        Particle& p = conf.p[i];
+        p.pos = {hp[i].x, hp[i].y, hp[i].z};
+        p.dir = {hd[i].x, hd[i].y, hd[i].z};
+        const PatchSet& s = hs[i];
+        for (int k = 0; k < 2; ++k) p.pd[k] = {s.pd[k][0], s.pd[k][1], s.pd[k][2]};
+        for (int k = 0; k < 4; ++k) p.ps[k] = {s.ps[k][0], s.ps[k][1], s.ps[k][2]};
+        for (int k = 0; k < 2; ++k) p.ch[k] = {s.ch[k][0], s.ch[k][1], s.ch[k][2]};
+    }
+    conf.box = {box[0], box[1], box[2]};
+    devNewer = false;
+    return SC_OK;
+}
+
+int Context::scratch(size_t bytes) {
+    if (bytes <= scratchBytes) return SC_OK;
+    if (dScratch) {
+        cudaFree(dScratch);
+        for (auto it = allocations.begin(); it != allocations.end(); ++it)
+            if (*it == dScratch) { allocations.erase(it); break; }
+        dScratch = nullptr;
+    }
+    int rc = allocDev(&dScratch, bytes);
+    if (rc) return rc;
+    scratchBytes = bytes;
+    return SC_OK;
+}
+
+// Reads the three inputs into a freshly constructed context.
+int initContext(Context* c, const std::string& opt, const std::string& top, const std::string& cfg) {
+    std::string err;
+    int rc;
+    if (readOptionsText(opt, c->opts, err)) return fail(SC_ERR_PARSE, err);
+    if (readTopologyText(top, c->topo, err)) return fail(err.find("outside") != std::string::npos ? SC_ERR_UNSUPPORTED : SC_ERR_PARSE, err);
+    if (buildParticles(c->topo, c->conf, err)) return fail(SC_ERR_PARSE, err);
+    if (readConfigText(cfg, c->topo, c->conf, err)) return fail(err.find("outside") != std::string::npos ? SC_ERR_UNSUPPORTED : SC_ERR_PARSE, err);
+    partVecInit(c->topo, c->conf);
+    if ((rc = c->setup(err))) return fail(rc, err);
+    return SC_OK;
+}
+
+bool readFile(const char* path, std::string& out) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f) return false;
+    std::ostringstream ss;
+    ss << f.rdbuf();
+    out = ss.str();
+    return true;
+}
+
+}  // namespace scg
+
+using namespace scg;
+
+struct sc_context : public Context {};
+
+static Context* C(sc_context* c) { return static_cast<Context*>(c); }
+static const Context* C(const sc_context* c) { return static_cast<const Context*>(c); }
+
+extern "C" {
+
+const char* sc_last_error(void) { return g_lastError.c_str(); }
+const char* sc_version(void) { return "sc_gb300 0.1 (sm_103a)"; }
+
+int sc_open_text(const char* options, const char* top, const char* config, sc_context** out) {
+    if (!options || !top || !config || !out) return fail(SC_ERR_ARG, "null argument");
+    sc_context* h = new sc_context();
+    int rc = initContext(h, options, top, config);
+    if (rc) { delete h; return rc; }
+    *out = h;
+    return SC_OK;
+}
+
+int sc_open(const char* options_path, const char* top_path, const char* config_path, sc_context** out) {
+    if (!options_path || !top_path || !config_path || !out) return fail(SC_ERR_ARG, "null argument");
+    std::string o, t, c;
+    if (!readFile(options_path, o)) return fail(SC_ERR_IO, std::string("cannot read ") + options_path);
+    if (!readFile(top_path, t)) return fail(SC_ERR_IO, std::string("cannot read ") + top_path);
+    if (!readFile(config_path, c)) return fail(SC_ERR_IO, std::string("cannot read ") + config_path);
+    return sc_open_text(o.c_str(), t.c_str(), c.c_str(), out);
+}
+
+int sc_close(sc_context* ctx) {
+    if (!ctx) return fail(SC_ERR_ARG, "null context");
+    delete ctx;
+    return SC_OK;
+}
+
+int sc_set_device(sc_context* ctx, int device) {
+    if (!ctx) return fail(SC_ERR_ARG, "null context");
+    if (C(ctx)->devReady) return fail(SC_ERR_STATE, "device already in use by this context");
+    C(ctx)->device = device;
+    return SC_OK;
+}
+
+int sc_num_particles(const sc_context* ctx, int* n) {
+    if (!ctx || !n) return fail(SC_ERR_ARG, "null argument");
+    *n = (int)C(ctx)->conf.p.size();
+    return SC_OK;
+}
+
+int sc_get_box(sc_context* ctx, double box[3]) {
+    if (!ctx || !box) return fail(SC_ERR_ARG, "null argument");
+    int rc = C(ctx)->downloadState();
+    if (rc) return rc;
+    box[0] = C(ctx)->conf.box.x; box[1] = C(ctx)->conf.box.y; box[2] = C(ctx)->conf.box.z;
+    return SC_OK;
+}
+
+int sc_set_box(sc_context* ctx, const double box[3]) {
+    if (!ctx || !box) return fail(SC_ERR_ARG, "null argument");
+    if (!(box[0] > 0 && box[1] > 0 && box[2] > 0)) return fail(SC_ERR_ARG, "box edges must be positive");
+    int rc = C(ctx)->downloadState();
+    if (rc) return rc;
+    C(ctx)->conf.box = {box[0], box[1], box[2]};
+    C(ctx)->hostNewer = true;
+    return SC_OK;
+}
+
+int sc_cutoff(const sc_context* ctx, double* sqmaxcut, double* maxcut) {
+    if (!ctx) return fail(SC_ERR_ARG, "null context");
+    if (sqmaxcut) *sqmaxcut = C(ctx)->topo.sqmaxcut;
+    if (maxcut) *maxcut = C(ctx)->topo.maxcut;
+    return SC_OK;
+}
+
+int sc_get_pair_param(const sc_context* ctx, int t1, int t2, sc_pair_param* out) {
+    if (!ctx || !out) return fail(SC_ERR_ARG, "null argument");
+    if (t1 < 0 || t2 < 0 || t1 >= MAXT || t2 >= MAXT) return fail(SC_ERR_ARG, "type out of range");
+    const IaParam& s = C(ctx)->topo.ia[t1][t2];
+    std::memset(out, 0, sizeof *out);
+    out->geotype[0] = s.geotype[0]; out->geotype[1] = s.geotype[1];
+    out->exclude = s.exclude; out->kind = functorKind(s.geotype[0], s.geotype[1]);
+    out->sigma = s.sigma; out->epsilon = s.epsilon; out->A = s.A; out->B = s.B; out->pdis = s.pdis;
+    out->pswitch = s.pswitch; out->pswitchINV = s.pswitchINV;
+    for (int k = 0; k < 4; ++k) {
+        out->pcangl[k] = s.pcangl[k]; out->pcanglsw[k] = s.pcanglsw[k];
+        out->pcoshalfi[k] = s.pcoshalfi[k]; out->psinhalfi[k] = s.psinhalfi[k];
+    }
+    out->rcut = s.rcut; out->rcutSq = s.rcutSq; out->rcutwca = s.rcutwca; out->rcutwcaSq = s.rcutwcaSq;
+    for (int k = 0; k < 2; ++k) {
+        out->csecpatchrot[k] = s.csecpatchrot[k]; out->ssecpatchrot[k] = s.ssecpatchrot[k];
+        out->len[k] = s.len[k]; out->half_len[k] = s.half_len[k];
+        out->chiral_cos[k] = s.chiral_cos[k]; out->chiral_sin[k] = s.chiral_sin[k];
+    }
+    out->volume = s.volume;
+    out->parallel = s.parallel;
+    return SC_OK;
+}
+
+static void toParticle(const Particle& p, sc_particle* o) {
+    o->pos[0] = p.pos.x; o->pos[1] = p.pos.y; o->pos[2] = p.pos.z;
+    o->dir[0] = p.dir.x; o->dir[1] = p.dir.y; o->dir[2] = p.dir.z;
+    for (int k = 0; k < 2; ++k) { o->patchdir[k][0] = p.pd[k].x; o->patchdir[k][1] = p.pd[k].y; o->patchdir[k][2] = p.pd[k].z; }
+    for (int k = 0; k < 4; ++k) { o->patchsides[k][0] = p.ps[k].x; o->patchsides[k][1] = p.ps[k].y; o->patchsides[k][2] = p.ps[k].z; }
+    for (int k = 0; k < 2; ++k) { o->chdir[k][0] = p.ch[k].x; o->chdir[k][1] = p.ch[k].y; o->chdir[k][2] = p.ch[k].z; }
+    o->type = p.type;
+    o->molType = p.molType;
+}
+
+int sc_get_particles(sc_context* ctx, int first, int count, sc_particle* out) {
+    if (!ctx || (!out && count > 0)) return fail(SC_ERR_ARG, "null argument");
+    Context* c = C(ctx);
+    if (first < 0 || count < 0 || first + count > (int)c->conf.p.size()) return fail(SC_ERR_ARG, "particle range out of bounds");
+    int rc = c->downloadState();
+    if (rc) return rc;
+    for (int k = 0; k < count; ++k) toParticle(c->conf.p[first + k], &out[k]);
+    return SC_OK;
+}
+
+int sc_set_particles(sc_context* ctx, int first, int count, const sc_particle* in) {
+    if (!ctx || (!in && count > 0)) return fail(SC_ERR_ARG, "null argument");
+    Context* c = C(ctx);
+    if (first < 0 || count < 0 || first + count > (int)c->conf.p.size()) return fail(SC_ERR_ARG, "particle range out of bounds");
+    int rc = c->downloadState();
+    if (rc) return rc;
+    for (int k = 0; k < count; ++k) {
+        Particle& p = c->conf.p[first + k];
+        const sc_particle& s = in[k];
+        if (s.type != p.type) return fail(SC_ERR_ARG, "sc_set_particles cannot change a particle's type");
+        p.pos = {s.pos[0], s.pos[1], s.pos[2]};
+        p.dir = {s.dir[0], s.dir[1], s.dir[2]};
+        for (int q = 0; q < 2; ++q) p.pd[q] = {s.patchdir[q][0], s.patchdir[q][1], s.patchdir[q][2]};
+        for (int q = 0; q < 4; ++q) p.ps[q] = {s.patchsides[q][0], s.patchsides[q][1], s.patchsides[q][2]};
+        for (int q = 0; q < 2; ++q) p.ch[q] = {s.chdir[q][0], s.chdir[q][1], s.chdir[q][2]};
+    }
+    c->hostNewer = true;
+    return SC_OK;
+}
+
+int sc_write_config(sc_context* ctx, const char* path) {
+    if (!ctx || !path) return fail(SC_ERR_ARG, "null argument");
+    int rc = C(ctx)->downloadState();
+    if (rc) return rc;
+    std::string txt = drawConfig(C(ctx)->conf);
+    FILE* f = std::fopen(path, "w");
+    if (!f) return fail(SC_ERR_IO, std::string("cannot write ") + path);
+    std::fwrite(txt.data(), 1, txt.size(), f);
+    std::fclose(f);
+    return SC_OK;
+}
+
+int sc_pair_energies(sc_context* ctx, int npairs, const int* I, const int* J, double* E, unsigned* V, double* D) {
+    if (!ctx || npairs < 0 || (npairs > 0 && (!I || !J || !E))) return fail(SC_ERR_ARG, "null argument");
+    Context* c = C(ctx);
+    int n = (int)c->conf.p.size();
+    for (int k = 0; k < npairs; ++k)
+        if (I[k] < 0 || J[k] < 0 || I[k] >= n || J[k] >= n) return fail(SC_ERR_ARG, "pair index out of range");
+    if (npairs == 0) return SC_OK;
+    int rc = c->ensureDevice();
+    if (rc) return rc;
+    size_t bytes = (size_t)npairs * (2 * sizeof(int) + 2 * sizeof(double) + sizeof(unsigned)) + 256;
+    if ((rc = c->scratch(bytes))) return rc;
+    char* base = (char*)c->dScratch;
+    int* dI = (int*)base;
+    int* dJ = dI + npairs;
+    double* dE = (double*)(((uintptr_t)(dJ + npairs) + 15) & ~(uintptr_t)15);
+    double* dD = dE + npairs;
+    unsigned* dV = (unsigned*)(dD + npairs);
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(dI, I, sizeof(int) * npairs, cudaMemcpyHostToDevice, c->stream)) != cudaSuccess) return cudaFail(e, "copy pairs");
+    if ((e = cudaMemcpyAsync(dJ, J, sizeof(int) * npairs, cudaMemcpyHostToDevice, c->stream)) != cudaSuccess) return cudaFail(e, "copy pairs");
+    if ((e = launchPairBatch(c->d, c->tables, npairs, dI, dJ, dE, dV, dD, c->stream)) != cudaSuccess) return cudaFail(e, "pair kernel");
+    if ((e = cudaMemcpyAsync(E, dE, sizeof(double) * npairs, cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess) return cudaFail(e, "copy energies");
+    if (V && (e = cudaMemcpyAsync(V, dV, sizeof(unsigned) * npairs, cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess) return cudaFail(e, "copy verdicts");
+    if (D && (e = cudaMemcpyAsync(D, dD, sizeof(double) * npairs, cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess) return cudaFail(e, "copy distances");
+    if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess) return cudaFail(e, "pair energies");
+    return SC_OK;
+}
+
+int sc_pair_energy(sc_context* ctx, int i, int j, double* e) {
+    if (!e) return fail(SC_ERR_ARG, "null argument");
+    return sc_pair_energies(ctx, 1, &i, &j, e, nullptr, nullptr);
+}
+
+static int oneToAllImpl(Context* c, int ntargets, const int* targets, const TrialSlot* trialDev, double* out) {
+    int rc;
+    if ((rc = c->scratch((size_t)ntargets * (sizeof(int) + sizeof(double)) + 64))) return rc;
+    int* dT = (int*)c->dScratch;
+    double* dO = (double*)(((uintptr_t)(dT + ntargets) + 15) & ~(uintptr_t)15);
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(dT, targets, sizeof(int) * ntargets, cudaMemcpyHostToDevice, c->stream)) != cudaSuccess) return cudaFail(e, "copy targets");
+    if ((e = launchOneToAll(c->d, c->tables, ntargets, dT, trialDev, dO, c->stream)) != cudaSuccess) return cudaFail(e, "one-to-all kernel");
+    if ((e = cudaMemcpyAsync(out, dO, sizeof(double) * ntargets, cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess) return cudaFail(e, "copy energies");
+    if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess) return cudaFail(e, "one-to-all");
+    return SC_OK;
+}
+
+int sc_one_to_all(sc_context* ctx, int ntargets, const int* targets, double* out) {
+    if (!ctx || ntargets < 0 || (ntargets > 0 && (!targets || !out))) return fail(SC_ERR_ARG, "null argument");
+    Context* c = C(ctx);
+    int n = (int)c->conf.p.size();
+    for (int k = 0; k < ntargets; ++k) if (targets[k] < 0 || targets[k] >= n) return fail(SC_ERR_ARG, "target out of range");
+    if (ntargets == 0) return SC_OK;
+    int rc = c->ensureDevice();
+    if (rc) return rc;
+    return oneToAllImpl(c, ntargets, targets, nullptr, out);
+}
+
+int sc_all_to_all(sc_context* ctx, double* out) {
+    if (!ctx || !out) return fail(SC_ERR_ARG, "null argument");
+    Context* c = C(ctx);
+    int rc = c->ensureDevice();
+    if (rc) return rc;
+    cudaError_t e;
+    if ((e = launchAllToAll(c->d, c->tables, nullptr, c->dPartial, c->nPartial, c->dScalars, c->stream)) != cudaSuccess) return cudaFail(e, "all-to-all kernel");
+    if ((e = cudaMemcpyAsync(out, c->dScalars, sizeof(double), cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess) return cudaFail(e, "copy energy");
+    if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess) return cudaFail(e, "all-to-all");
+    return SC_OK;
+}
+
+int sc_mol_to_others(sc_context* ctx, int first, int size, double* out) {
+    if (!ctx || !out) return fail(SC_ERR_ARG, "null argument");
+    Context* c = C(ctx);
+    if (first < 0 || size <= 0 || first + size > (int)c->conf.p.size()) return fail(SC_ERR_ARG, "molecule range out of bounds");
+    int rc = c->ensureDevice();
+    if (rc) return rc;
+    cudaError_t e;
+    if ((e = launchMolToOthers(c->d, c->tables, first, size, c->dScalars, c->stream)) != cudaSuccess) return cudaFail(e, "mol2others kernel");
+    if ((e = cudaMemcpyAsync(out, c->dScalars, sizeof(double), cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess) return cudaFail(e, "copy energy");
+    if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess) return cudaFail(e, "mol2others");
+    return SC_OK;
+}
+
+static void rotateParticle(Particle& p, int g, double angle, const double* ax, int positive) {
+    // Particle::pscRotate (scOOP/structures/particle.h:182-272) with the sign given
+    double vc = cos(angle);
+    double vs = positive ? sqrt(1.0 - vc * vc) : -sqrt(1.0 - vc * vc);
+    double qw = vc, qx = ax[0] * vs, qy = ax[1] * vs, qz = ax[2] * vs;
+    double t2 = qw * qx, t3 = qw * qy, t4 = qw * qz, t5 = -qx * qx, t6 = qx * qy, t7 = qx * qz, t8 = -qy * qy,
+           t9 = qy * qz, t10 = -qz * qz;
+    double d1 = t8 + t10, d2 = t6 - t4, d3 = t3 + t7, d4 = t4 + t6, d5 = t5 + t10, d6 = t9 - t2, d7 = t7 - t3,
+           d8 = t2 + t9, d9 = t5 + t8;
+    auto rot = [&](Vec3& v) {
+        double nx = 2.0 * (d1 * v.x + d2 * v.y + d3 * v.z) + v.x;
+        double ny = 2.0 * (d4 * v.x + d5 * v.y + d6 * v.z) + v.y;
+        double nz = 2.0 * (d7 * v.x + d8 * v.y + d9 * v.z) + v.z;
+        v = {nx, ny, nz};
+    };
+    rot(p.dir);
+    if (g != SCN && g != SCA) {
+        int m = isTwoPatch(g) ? 2 : 1;
+        for (int k = 0; k < m; ++k) { rot(p.pd[k]); rot(p.ps[2 * k]); rot(p.ps[2 * k + 1]); }
+    }
+    if (isChiral(g)) {
+        int m = (g == TCHPSC || g == TCHCPSC) ? 2 : 1;
+        for (int k = 0; k < m; ++k) rot(p.ch[k]);
+    }
+    // partRotate: patchdir[0].ortogonalise(dir) (movecreator.cpp:1007)
+    double dp = p.pd[0].x * p.dir.x + p.pd[0].y * p.dir.y + p.pd[0].z * p.dir.z;
+    p.pd[0].x -= dp * p.dir.x; p.pd[0].y -= dp * p.dir.y; p.pd[0].z -= dp * p.dir.z;
+}
+
+static int trialImpl(Context* c, int target, const Particle& trial, double* eOld, double* eNew) {
+    TrialSlot ts;
+    ts.pos = make_double4_32a(trial.pos.x, trial.pos.y, trial.pos.z, (double)c->compactOf[trial.type]);
+    ts.dir = make_double4_32a(trial.dir.x, trial.dir.y, trial.dir.z, 0.0);
+    for (int k = 0; k < 2; ++k) { ts.patch.pd[k][0] = trial.pd[k].x; ts.patch.pd[k][1] = trial.pd[k].y; ts.patch.pd[k][2] = trial.pd[k].z; }
+    for (int k = 0; k < 4; ++k) { ts.patch.ps[k][0] = trial.ps[k].x; ts.patch.ps[k][1] = trial.ps[k].y; ts.patch.ps[k][2] = trial.ps[k].z; }
+    for (int k = 0; k < 2; ++k) { ts.patch.ch[k][0] = trial.ch[k].x; ts.patch.ch[k][1] = trial.ch[k].y; ts.patch.ch[k][2] = trial.ch[k].z; }
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(c->dTrial, &ts, sizeof ts, cudaMemcpyHostToDevice, c->stream)) != cudaSuccess) return cudaFail(e, "copy trial");
+    int rc;
+    double v;
+    if ((rc = oneToAllImpl(c, 1, &target, nullptr, &v))) return rc;
+    *eOld = v;
+    if ((rc = oneToAllImpl(c, 1, &target, c->dTrial, &v))) return rc;
+    *eNew = v;
+    c->trialTarget = target;
+    c->trialState = trial;
+    return SC_OK;
+}
+
+int sc_trial_displace(sc_context* ctx, int target, const double dr[3], double* eOld, double* eNew) {
+    if (!ctx || !dr || !eOld || !eNew) return fail(SC_ERR_ARG, "null argument");
+    Context* c = C(ctx);
+    if (target < 0 || target >= (int)c->conf.p.size()) return fail(SC_ERR_ARG, "target out of range");
+    int rc = c->downloadState();
+    if (rc) return rc;
+    if ((rc = c->ensureDevice())) return rc;
+    Particle t = c->conf.p[target];
+    t.pos.x += dr[0]; t.pos.y += dr[1]; t.pos.z += dr[2];
+    return trialImpl(c, target, t, eOld, eNew);
+}
+
+int sc_trial_rotate(sc_context* ctx, int target, double angle, const double axis[3], int positive, double* eOld,
+                    double* eNew, sc_particle* state) {
+    if (!ctx || !axis || !eOld || !eNew) return fail(SC_ERR_ARG, "null argument");
+    Context* c = C(ctx);
+    if (target < 0 || target >= (int)c->conf.p.size()) return fail(SC_ERR_ARG, "target out of range");
+    int rc = c->downloadState();
+    if (rc) return rc;
+    if ((rc = c->ensureDevice())) return rc;
+    Particle t = c->conf.p[target];
+    rotateParticle(t, c->topo.ia[t.type][t.type].geotype[0], angle, axis, positive);
+    if (state) toParticle(t, state);
+    return trialImpl(c, target, t, eOld, eNew);
+}
+
+int sc_accept_trial(sc_context* ctx) {
+    if (!ctx) return fail(SC_ERR_ARG, "null context");
+    Context* c = C(ctx);
+    if (c->trialTarget < 0) return fail(SC_ERR_STATE, "no trial move pending");
+    int rc = c->downloadState();
+    if (rc) return rc;
+    c->conf.p[c->trialTarget] = c->trialState;
+    c->trialTarget = -1;
+    c->hostNewer = true;
+    return SC_OK;
+}
+
+int sc_trial_volume(sc_context* ctx, double psch, double* eNew) {
+    if (!ctx || !eNew) return fail(SC_ERR_ARG, "null argument");
+    Context* c = C(ctx);
+    int rc = c->ensureDevice();
+    if (rc) return rc;
+    if ((rc = c->downloadState())) return rc;
+    double box[3] = {c->conf.box.x + psch, c->conf.box.y + psch, c->conf.box.z + psch};
+    if (!(box[0] > 0 && box[1] > 0 && box[2] > 0)) return fail(SC_ERR_ARG, "box edge would not be positive");
+    cudaError_t e;
+    double* dBox = c->dScalars + 8;
+    if ((e = cudaMemcpyAsync(dBox, box, sizeof box, cudaMemcpyHostToDevice, c->stream)) != cudaSuccess) return cudaFail(e, "copy box");
+    if ((e = launchAllToAll(c->d, c->tables, dBox, c->dPartial, c->nPartial, c->dScalars, c->stream)) != cudaSuccess) return cudaFail(e, "all-to-all kernel");
+    if ((e = cudaMemcpyAsync(eNew, c->dScalars, sizeof(double), cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess) return cudaFail(e, "copy energy");
+    if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess) return cudaFail(e, "volume trial");
+    return SC_OK;
+}
+
+int sc_default_run(const sc_context* ctx, sc_run_params* p) {
+    if (!ctx || !p) return fail(SC_ERR_ARG, "null argument");
+    const Options& o = C(ctx)->opts;
+    std::memset(p, 0, sizeof *p);
+    p->nsweeps = o.nsweeps;
+    p->seed = (unsigned long long)o.seed;
+    p->temper = o.temper;
+    p->press = o.press;
+    p->ptype = o.ptype;
+    p->volume_every = (o.shave > 0 && o.ptype == 1) ? (int)(1.0 / o.shave + 0.5) : 0;
+    if (p->volume_every < 1 && o.shave > 0 && o.ptype == 1) p->volume_every = 1;
+    p->transmx = o.transmx;
+    p->rot_angle = o.rot_angle;
+    p->edge_mx = o.edge_mx;
+    p->chainprob = o.chainprob;
+    p->chainmmx = o.chainmmx;
+    p->chain_angle = o.chain_angle;
+    p->check_every = 100;
+    return SC_OK;
+}
+
+int sc_simulate(sc_context* ctx, const sc_run_params* p, sc_run_stats* stats) {
+    if (!ctx || !p || !stats) return fail(SC_ERR_ARG, "null argument");
+    return runSweeps(C(ctx), *p, *stats);
+}
+
+}  // extern "C"

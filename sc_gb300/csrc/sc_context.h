@@ -1,0 +1,70 @@
+// sc_context.h -- host-side state behind one sc_context handle.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/sc_gb300.h"
+#include "kernels.h"
+#include "sc_input.h"
+
+namespace scg {
+
+struct SweepEngine;   // sweep.cu
+
+struct Context {
+    Options opts;
+    Topology topo;
+    Config conf;
+    std::vector<MolParam> mols;
+    std::vector<int4> molInfo;
+    std::vector<int> usedTypes;
+    int compactOf[MAXT];
+
+    int device = 0;
+    bool devReady = false;
+    bool hostNewer = true;    // host copy changed since the last upload
+    bool devNewer = false;    // device copy changed (moves) since the last download
+    cudaStream_t stream = nullptr;
+    std::vector<void*> allocations;
+
+    DevState d{};
+    DevTables tables{};
+    PairParam* dParams = nullptr;
+    MolParam* dMols = nullptr;
+    TrialSlot* dTrial = nullptr;
+    double* dScalars = nullptr;
+    double* dPartial = nullptr;
+    int nPartial = 0;
+    void* dScratch = nullptr;
+    size_t scratchBytes = 0;
+
+    int trialTarget = -1;
+    Particle trialState;
+
+    SweepEngine* engine = nullptr;
+    long lastLaunches = 0;     // kernels launched by the last move loop
+
+    Context() = default;
+    Context(const Context&) = delete;
+    Context& operator=(const Context&) = delete;
+    ~Context();
+
+    int setup(std::string& err);
+    int ensureDevice();
+    int uploadState();
+    int downloadState();
+    int allocDev(void** p, size_t bytes);
+    int scratch(size_t bytes);
+    void freeDevice();
+    PairParam devParam(int t1, int t2) const;
+};
+
+int fail(int code, const std::string& msg);
+int cudaFail(cudaError_t e, const char* where);
+int runSweeps(Context* c, const sc_run_params& p, sc_run_stats& st);
+void destroyEngine(Context* c);
+
+}  // namespace scg

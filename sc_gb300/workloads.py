@@ -1,0 +1,142 @@
+"""Seeded synthetic systems in the reference's input format (options, top.init, config.init).
+
+The benchmark systems are described by their physics only (no dataset is
+involved); these generators build them deterministically from a seed:
+random, non-overlapping centres (closest segment distance >= sigma) and uniform
+random orientations, patch vectors perpendicular to the axis.
+
+  npt_cpsc_spa_4000   2000 CPSC (L=3, patch 120 deg) + 2000 SPA (sigma 1, eps 0.5, range 1.5),
+                      P*=0.5, T=1, isotropic volume move every sweep
+  nvt_psc_1000        1000 PSC (L=3, patch 90 deg, switch 10 deg, eps 1, range 1.12 + 0.2),
+                      packing fraction 0.1, T=1
+  psc_cpsc_65536      65,536 PSC/CPSC 50/50 at packing fraction 0.2, T=1
+"""
+import math
+
+import numpy as np
+
+OPTION_DEFAULTS = dict(
+    ptype=1, press=0.0, paralpress=0.0, shave=0, nequil=0, adjust=0, nsweeps=100, paramfrq=0, report=0,
+    nrepchange=0, nGrandCanon=0, nClustMove=0, movie=0, chainprob=0.0, transmx=0.3, rotmx=20.0,
+    edge_mx=0.0, chainmmx=0.0, chainrmx=0.0, temper=1.0, paraltemper=1.0, wlm=0, wlmtype=0,
+    switchprob=0.0, pairlist_update=10, seed=1, write_cluster=0)
+
+
+def options_text(**kw):
+    d = dict(OPTION_DEFAULTS)
+    d.update(kw)
+    d["paraltemper"] = d["temper"]
+    return "".join(f"{k} = {v}\n" for k, v in d.items())
+
+
+def _unit(rng, n):
+    v = rng.normal(size=(n, 3))
+    return v / np.linalg.norm(v, axis=1, keepdims=True)
+
+
+def _perp(rng, d):
+    v = _unit(rng, len(d))
+    v -= (v * d).sum(1, keepdims=True) * d
+    return v / np.linalg.norm(v, axis=1, keepdims=True)
+
+
+def _segdist(p1, d1, h1, P2, D2, H2):
+    """Closest distance between segment (p1, d1, half-length h1) and segments (P2, D2, H2), vectorised."""
+    r = p1[None, :] - P2
+    a = np.full(len(P2), 1.0)
+    b = (D2 @ d1)
+    c = np.full(len(P2), 1.0)
+    dd = r @ d1
+    e = (r * D2).sum(1)
+    den = a * c - b * b
+    with np.errstate(divide="ignore", invalid="ignore"):
+        s = np.where(den > 1e-12, (b * e - c * dd) / den, 0.0)
+    s = np.clip(s, -h1, h1)
+    t = np.clip(b * s + e, -H2, H2)
+    s = np.clip(b * t - dd, -h1, h1)
+    t = np.clip(b * s + e, -H2, H2)
+    diff = r + s[:, None] * d1[None, :] - t[:, None] * D2
+    return np.sqrt((diff * diff).sum(1))
+
+
+def place(rng, halfl, box, dmin=1.0, max_tries=200000):
+    """Random sequential placement; halfl[k] is the half-length of particle k (0 for spheres)."""
+    n = len(halfl)
+    pos = np.zeros((n, 3))
+    dirs = _unit(rng, n)
+    cell = max(2.0 * max(halfl) + dmin, dmin) + 1e-9
+    nc = np.maximum((box // cell).astype(int), 1)
+    grid = {}
+    placed = 0
+    tries = 0
+    while placed < n:
+        tries += 1
+        if tries > max_tries:
+            raise RuntimeError("placement failed: density too high")
+        p = rng.uniform(0, 1, 3) * box
+        key = tuple((p / box * nc).astype(int) % nc)
+        near = []
+        for dx in (-1, 0, 1):
+            for dy in (-1, 0, 1):
+                for dz in (-1, 0, 1):
+                    near += grid.get(((key[0] + dx) % nc[0], (key[1] + dy) % nc[1], (key[2] + dz) % nc[2]), [])
+        if near:
+            idx = np.array(sorted(set(near)))
+            r = pos[idx] - p
+            r -= box * np.round(r / box)
+            q = p + r
+            dist = _segdist(p, dirs[placed], halfl[placed], q, dirs[idx], np.asarray(halfl)[idx])
+            if np.any(dist < dmin):
+                dirs[placed] = _unit(rng, 1)[0]
+                continue
+        pos[placed] = p
+        grid.setdefault(key, []).append(placed)
+        placed += 1
+    return pos, dirs, _perp(rng, dirs)
+
+
+def config_text(box, pos, dirs, pds):
+    lines = ["%.17g %.17g %.17g" % tuple(box)]
+    for p, d, q in zip(pos, dirs, pds):
+        lines.append("%.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g 0" % (*p, *d, *q))
+    return "\n".join(lines) + "\n"
+
+
+def _vol_sc(L, sigma=1.0):
+    return math.pi / 6 * sigma ** 3 + math.pi / 4 * sigma ** 2 * L
+
+
+def npt_cpsc_spa(n=4000, phi=0.1, seed=1, press=0.5, temper=1.0):
+    L = 3.0
+    nc = n // 2
+    ns = n - nc
+    vol = nc * _vol_sc(L) + ns * math.pi / 6
+    box = np.full(3, (vol / phi) ** (1 / 3))
+    rng = np.random.default_rng(seed)
+    halfl = [L / 2] * nc + [0.0] * ns
+    pos, dirs, pds = place(rng, halfl, box)
+    top = ("[Types]\n"
+           "C 1 CPSC 1.0 1.0 1.12 0.2 120.0 10.0 3.0 0.0\n"
+           "A 2 SPA 0.5 1.0 1.1225 0.3775\n"
+           "[Molecules]\nC: {\nparticles: 1\n}\nA: {\nparticles: 2\n}\n"
+           f"[System]\nC {nc}\nA {ns}\n")
+    opts = options_text(ptype=1, press=press, shave=1, edge_mx=0.4, transmx=0.4, rotmx=30.0, temper=temper,
+                        seed=seed)
+    return opts, top, config_text(box, pos, dirs, pds)
+
+
+def nvt_psc(n=1000, phi=0.1, seed=1, temper=1.0):
+    L = 3.0
+    box = np.full(3, (n * _vol_sc(L) / phi) ** (1 / 3))
+    rng = np.random.default_rng(seed)
+    pos, dirs, pds = place(rng, [L / 2] * n, box)
+    top = ("[Types]\nP 1 PSC 1.0 1.0 1.12 0.2 90.0 10.0 3.0 0.0\n"
+           f"[Molecules]\nP: {{\nparticles: 1\n}}\n[System]\nP {n}\n")
+    opts = options_text(ptype=0, transmx=0.4, rotmx=30.0, temper=temper, seed=seed)
+    return opts, top, config_text(box, pos, dirs, pds)
+
+
+WORKLOADS = {
+    "npt_cpsc_spa_4000": lambda seed=1: npt_cpsc_spa(4000, seed=seed),
+    "nvt_psc_1000": lambda seed=1: nvt_psc(1000, seed=seed),
+}

@@ -1,0 +1,149 @@
+#!/usr/bin/env python3
+"""Ensemble goldens: averages sampled by the reference's own Metropolis loop.
+
+Runs the reference binary built from its own sources (oracle/_ref/sc_ref, see
+oracle/Makefile) on seeded synthetic systems, several independent seeds each, and
+stores the time series it writes (energy.dat: total energy and alignmentOrder;
+stat.dat: volume) as tests/golden/ens_<name>.json together with the inputs.  The
+GPU sampler must reproduce the averages within 2 standard errors.
+
+Run here (needs the reference tree): python tests/golden/make_ensemble.py
+"""
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, HERE)
+from make_golden import OPTION_KEYS, config_text, rand_perp, rand_unit, top_text  # noqa: E402
+
+SC_REF = os.path.join(REPO, "oracle", "_ref", "sc_ref")
+
+
+def seg_dist(p1, d1, p2, d2, L):
+    """Closest distance of two segments of length L (numpy, for initial placement only)."""
+    best = 1e9
+    for s in np.linspace(-L / 2, L / 2, 9):
+        a = p1 + s * d1
+        t = np.clip(np.dot(a - p2, d2), -L / 2, L / 2)
+        best = min(best, np.linalg.norm(a - (p2 + t * d2)))
+    return best
+
+
+def place(rng, n, box, L, dmin=1.05, types=None):
+    pos, dirs = [], []
+    tries = 0
+    while len(pos) < n:
+        tries += 1
+        p = rng.uniform(0, 1, 3) * box
+        d = rand_unit(rng, 1)[0]
+        ok = True
+        for q, e in zip(pos, dirs):
+            r = p - q
+            r -= box * np.round(r / box)
+            if np.linalg.norm(r) > L + dmin:
+                continue
+            if seg_dist(q + r, d, q, e, L) < dmin:
+                ok = False
+                break
+        if ok:
+            pos.append(p)
+            dirs.append(d)
+    pos, dirs = np.array(pos), np.array(dirs)
+    return pos, dirs, rand_perp(rng, dirs)
+
+
+def cases():
+    rng = np.random.default_rng(31337)
+    out = {}
+    # PSC, the benchmark model, NVT
+    n = 250
+    phi = 0.2
+    L = 3.0
+    box = np.full(3, (n * (math.pi / 6 + math.pi / 4 * L) / phi) ** (1 / 3))
+    pos, dirs, pds = place(rng, n, box, L)
+    out["psc_nvt"] = dict(
+        top=top_text([("P", 1, "PSC", [1.0, 1.0, 1.12, 0.2, 90.0, 10.0, L, 0.0])], [("P", [1], [])], [("P", n)]),
+        config=config_text(box, pos, dirs, pds),
+        opts=dict(temper=0.6, transmx=0.35, rotmx=30.0, pairlist_update=10),
+        nsweeps=24000, report=20, seeds=6, burn=4000)
+    # CPSC + SPA mixture, NPT
+    n = 200
+    box = np.full(3, 14.5)
+    pos, dirs, pds = place(rng, n, box, L)
+    out["cpsc_spa_npt"] = dict(
+        top=top_text([("C", 1, "CPSC", [1.0, 1.0, 1.12, 0.2, 120.0, 10.0, L, 0.0]),
+                      ("A", 2, "SPA", [0.5, 1.0, 1.1225, 0.3775])],
+                     [("C", [1], []), ("A", [2], [])], [("C", 100), ("A", 100)]),
+        config=config_text(box, pos, dirs, pds),
+        opts=dict(temper=1.0, press=0.5, ptype=1, shave=1, edge_mx=0.25, transmx=0.35, rotmx=30.0,
+                  pairlist_update=0),
+        nsweeps=16000, report=20, seeds=6, burn=4000)
+    return out
+
+
+def run_one(c, seed):
+    with tempfile.TemporaryDirectory() as tmp:
+        opts = dict(OPTION_KEYS)
+        opts.update(c["opts"])
+        opts.update(nsweeps=c["nsweeps"], report=c["report"], seed=seed, paraltemper=opts["temper"])
+        with open(os.path.join(tmp, "options"), "w") as f:
+            f.write("".join(f"{k} = {v}\n" for k, v in opts.items()))
+        with open(os.path.join(tmp, "top.init"), "w") as f:
+            f.write(c["top"])
+        with open(os.path.join(tmp, "config.init"), "w") as f:
+            f.write(c["config"])
+        subprocess.run([SC_REF], cwd=tmp, check=True, capture_output=True)
+        e, al, vol = [], [], []
+        for line in open(os.path.join(tmp, "energy.dat")):
+            if line.startswith("#"):
+                continue
+            sw, rest = line.split(";")
+            a, b = rest.split()
+            e.append((int(sw), float(a), float(b)))
+        for line in open(os.path.join(tmp, "stat.dat")):
+            if line.startswith("#"):
+                continue
+            sw, v = line.split(";")
+            vol.append((int(sw), float(v)))
+        return dict(seed=seed, energy=e, volume=vol)
+
+
+def block_stats(series_per_seed, burn):
+    """Mean and standard error from per-seed means after the burn-in (seeds independent)."""
+    means = [np.mean([v for s, v in ser if s > burn]) for ser in series_per_seed]
+    m = float(np.mean(means))
+    se = float(np.std(means, ddof=1) / math.sqrt(len(means)))
+    return m, se
+
+
+def main():
+    subprocess.run(["make", "-C", os.path.join(REPO, "oracle"), "ref", "-j8"], check=True, capture_output=True)
+    for name, c in cases().items():
+        with ThreadPoolExecutor(max_workers=min(8, c["seeds"])) as ex:
+            runs = list(ex.map(lambda s: run_one(c, s), [1000 + k for k in range(c["seeds"])]))
+        n = sum(cnt for _, cnt in [tuple(l.split()) for l in c["top"].split("[System]\n")[1].splitlines() if l.strip()]
+                for cnt in [int(cnt)])
+        e_ser = [[(s, en / n) for s, en, _ in r["energy"]] for r in runs]
+        a_ser = [[(s, al / n) for s, _, al in r["energy"]] for r in runs]
+        v_ser = [[(s, v / n) for s, v in r["volume"]] for r in runs]
+        stats = {k: block_stats(ser, c["burn"]) for k, ser in (("energy_per_particle", e_ser),
+                                                              ("alignment_per_particle", a_ser),
+                                                              ("volume_per_particle", v_ser))}
+        out = dict(name=name, n=n, inputs={"top.init": c["top"], "config.init": c["config"]}, options=c["opts"],
+                   nsweeps=c["nsweeps"], report=c["report"], burn=c["burn"], seeds=c["seeds"],
+                   stats={k: {"mean": m, "se": s} for k, (m, s) in stats.items()})
+        with open(os.path.join(HERE, f"ens_{name}.json"), "w") as f:
+            json.dump(out, f, indent=1)
+        print(name, json.dumps(out["stats"]))
+
+
+if __name__ == "__main__":
+    main()

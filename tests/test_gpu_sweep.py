@@ -1,0 +1,153 @@
+"""GPU move loop: bookkeeping, reproducibility and ensemble parity with the reference.
+
+The checkerboard sampler visits configurations in another order than the
+reference's sequential loop, so trajectories differ; what must agree is the
+stationary distribution.  tests/golden/ens_*.json hold averages the reference's
+own loop sampled (several seeds, tests/golden/make_ensemble.py); the GPU run from
+the same start must match them within 2 standard errors.
+"""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+import goldens
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def opts_text(extra):
+    from golden.make_golden import OPTION_KEYS
+
+    d = dict(OPTION_KEYS)
+    d.update(extra)
+    d["paraltemper"] = d["temper"]
+    return "".join(f"{k} = {v}\n" for k, v in d.items())
+
+
+def ens(name):
+    with open(os.path.join(GOLDEN, f"ens_{name}.json")) as f:
+        return json.load(f)
+
+
+def open_ens(name):
+    from sc_gb300 import System
+
+    e = ens(name)
+    s = System.from_text(opts_text(e["options"]), e["inputs"]["top.init"], e["inputs"]["config.init"])
+    return e, s
+
+
+def exact_energy(s):
+    return s.all_to_all()
+
+
+def test_running_energy_matches_exact_total():
+    e, s = open_ens("psc_nvt")
+    e0 = exact_energy(s)
+    st = s.simulate(nsweeps=200, seed=11, check_every=50)
+    assert st.moves == 200 * s.n
+    assert st.acc_trans + st.rej_trans + st.acc_rot + st.rej_rot == st.moves
+    assert 0.05 < (st.acc_trans + st.acc_rot) / st.moves < 0.95
+    e1 = exact_energy(s)
+    assert e1 != e0
+    assert abs(st.energy - e1) <= 1e-9 * max(1.0, abs(e1))
+    assert st.max_drift <= 1e-9 * max(1.0, abs(e1))
+    # the cell-list total energy of the last check equals the brute-force one
+    st2 = s.simulate(nsweeps=50, seed=11, check_every=50)
+    assert abs(st2.energy_check - exact_energy(s)) <= 1e-11 * max(1.0, abs(st2.energy_check))
+    s.close()
+
+
+def test_same_seed_same_trajectory():
+    _, s1 = open_ens("psc_nvt")
+    _, s2 = open_ens("psc_nvt")
+    a = s1.simulate(nsweeps=60, seed=5, check_every=0)
+    b = s2.simulate(nsweeps=60, seed=5, check_every=0)
+    assert a.energy == b.energy and a.acc_trans == b.acc_trans and a.acc_rot == b.acc_rot
+    pa, pb = s1.particles(), s2.particles()
+    assert all(list(x.pos) == list(y.pos) and list(x.dir) == list(y.dir) for x, y in zip(pa, pb))
+    c = s2.simulate(nsweeps=1, seed=6, check_every=0)
+    assert c.moves == s2.n
+    s1.close()
+    s2.close()
+
+
+def test_rotations_keep_unit_vectors_and_patch_frame():
+    _, s = open_ens("psc_nvt")
+    s.simulate(nsweeps=100, seed=3, check_every=0)
+    for p in s.particles():
+        d = np.array(p.dir)
+        pd = np.array(p.patchdir[0])
+        assert abs(np.linalg.norm(d) - 1.0) < 1e-9
+        assert abs(np.dot(d, pd)) < 1e-9
+    s.close()
+
+
+def test_volume_moves_change_box_and_keep_energy_exact():
+    e, s = open_ens("cpsc_spa_npt")
+    b0 = s.box.copy()
+    p = s.default_run()
+    st = s.simulate(p, nsweeps=300, seed=21, check_every=100)
+    assert st.acc_vol + st.rej_vol == 300
+    assert st.acc_vol > 0 and st.vol_constrained == 0
+    assert not np.allclose(s.box, b0)
+    e1 = exact_energy(s)
+    assert abs(st.energy - e1) <= 1e-9 * max(1.0, abs(e1))
+    s.close()
+
+
+def alignment_order(s):
+    """Updater::alignmentOrder (scOOP/mc/updater.cpp:466-481)."""
+    parts = s.particles()
+    box = s.box
+    pos = np.array([p.pos for p in parts])
+    d = np.array([p.dir for p in parts])
+    r = pos[:, None, :] - pos[None, :, :]
+    r = (r - np.round(r)) * box
+    close = (r * r).sum(-1) < 1.5 * 1.5
+    iu = np.triu_indices(len(parts), 1)
+    return float((d @ d.T)[iu][close[iu]].sum())
+
+
+def sample(s, golden, nsweeps, seed):
+    p = s.default_run()
+    p.seed = seed
+    p.check_every = 0
+    rep = golden["report"]
+    E, A, V = [], [], []
+    done = 0
+    while done < nsweeps:
+        st = s.simulate(p, nsweeps=rep)
+        done += rep
+        if done > golden["burn"]:
+            E.append(st.energy / s.n)
+            A.append(alignment_order(s) / s.n)
+            V.append(float(np.prod(s.box)) / s.n)
+    return np.array(E), np.array(A), np.array(V)
+
+
+def mean_se(x, nblocks=10):
+    b = np.array_split(x, nblocks)
+    m = np.array([v.mean() for v in b])
+    return float(x.mean()), float(m.std(ddof=1) / math.sqrt(nblocks))
+
+
+@pytest.mark.parametrize("name", ["psc_nvt", "cpsc_spa_npt"])
+def test_ensemble_matches_reference(name):
+    g, s = open_ens(name)
+    E, A, V = sample(s, g, g["nsweeps"], seed=4242)
+    checks = [("energy_per_particle", E), ("alignment_per_particle", A)]
+    if g["options"].get("ptype") == 1:
+        checks.append(("volume_per_particle", V))
+    report = {}
+    for key, x in checks:
+        m, se = mean_se(x)
+        ref = g["stats"][key]
+        sigma = math.sqrt(se ** 2 + ref["se"] ** 2)
+        report[key] = (m, se, ref["mean"], ref["se"])
+        assert abs(m - ref["mean"]) <= 2.0 * sigma, report
+    s.close()
