@@ -672,6 +672,9 @@ struct SweepEngine {
     int nTotBlocks = 0;
     std::vector<void*> allocs;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evP0 = nullptr, evP1 = nullptr;
+    cudaGraphExec_t graphExec = nullptr;
+    SweepArgs graphArgs{};
+    long graphBlock = 0, graphLaunches = 0, graphPhaseLaunches = 0;
     bool energyKnown = false;
     uint64_t seed = 0;
     long launches = 0;
@@ -709,6 +712,7 @@ void destroyEngine(Context* c) {
     for (void* p : e->allocs) cudaFree(p);
     for (cudaEvent_t ev : {e->ev0, e->ev1, e->evP0, e->evP1})
         if (ev) cudaEventDestroy(ev);
+    if (e->graphExec) cudaGraphExecDestroy(e->graphExec);
     delete e;
     c->engine = nullptr;
 }
@@ -830,16 +834,17 @@ int runSweeps(Context* c, const sc_run_params& p, sc_run_stats& st) {
         e->energyKnown = true;
     }
     cudaEventRecord(e->ev0, s);
-    const long chunk = 50;
+    const long chunk = 48;
     double phaseMs = 0.0;
     long phaseLaunches = 0;
-    for (long sw = 0; sw < p.nsweeps; ++sw) {
-        bool volDue = npt && ((sw + 1) % p.volume_every == 0);
+    // one sweep: control block, cell list, the colour phases, energy bookkeeping, volume move
+    auto launchOne = [&](bool volDue, bool timing) -> cudaError_t {
         kBeginSweep<<<1, 32, 0, s>>>(a, volDue ? 1 : 0);
-        if ((r = launchCells(a, s, launches)) != cudaSuccess) return cudaFail(r, "cell list");
-        if (p.time_phases) cudaEventRecord(e->evP0, s);
+        cudaError_t r2 = launchCells(a, s, launches);
+        if (r2 != cudaSuccess) return r2;
+        if (timing) cudaEventRecord(e->evP0, s);
         for (int ph = 0; ph < a.g.ncolours; ++ph) kColour<<<a.g.nactive, kMoveThreads, 0, s>>>(a, ph);
-        if (p.time_phases) {
+        if (timing) {
             cudaEventRecord(e->evP1, s);
             cudaEventSynchronize(e->evP1);
             float pms = 0;
@@ -854,20 +859,58 @@ int runSweeps(Context* c, const sc_run_params& p, sc_run_stats& st) {
             kVolumeAccept<<<1, 32, 0, s>>>(a, e->nTotBlocks);
             launches += 2;
         }
-        if (p.check_every > 0 && (sw + 1) % p.check_every == 0) {
-            if (volDue) {
-                // positions unchanged since the cell list was built; only the box may have
-                kBeginSweep<<<1, 32, 0, s>>>(a, 0);
-                if ((r = launchCells(a, s, launches)) != cudaSuccess) return cudaFail(r, "cell list");
-                launches += 1;
+        return cudaGetLastError();
+    };
+    // Blocks of G sweeps are captured once into a CUDA graph and replayed: the kernels
+    // read everything that changes from sweep to sweep (sweep index, grid offset, colour
+    // order, box, energy) from the device control block.
+    const int ve = npt ? p.volume_every : 1;
+    const long G = (long)ve * std::max(1, (8 + ve - 1) / ve);
+    const bool useGraph = !p.time_phases;
+    long nextCheck = p.check_every > 0 ? p.check_every : -1;
+    long nextRegrid = npt ? chunk : -1;
+    long sw = 0;
+    while (sw < p.nsweeps) {
+        long left = p.nsweeps - sw;
+        if (useGraph && left >= G && sw % G == 0) {
+            if (!e->graphExec || std::memcmp(&e->graphArgs, &a, sizeof a) != 0 || e->graphBlock != G) {
+                if (e->graphExec) { cudaGraphExecDestroy(e->graphExec); e->graphExec = nullptr; }
+                cudaGraph_t graph;
+                long before = launches, beforeP = phaseLaunches;
+                if ((r = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return cudaFail(r, "graph capture");
+                for (long k = 0; k < G; ++k) {
+                    cudaError_t r2 = launchOne(npt && ((k + 1) % ve == 0), false);
+                    if (r2 != cudaSuccess) { cudaStreamEndCapture(s, &graph); return cudaFail(r2, "graph capture launch"); }
+                }
+                if ((r = cudaStreamEndCapture(s, &graph)) != cudaSuccess) return cudaFail(r, "graph capture end");
+                r = cudaGraphInstantiate(&e->graphExec, graph, 0);
+                cudaGraphDestroy(graph);
+                if (r != cudaSuccess) return cudaFail(r, "graph instantiate");
+                e->graphLaunches = launches - before;
+                e->graphPhaseLaunches = phaseLaunches - beforeP;
+                launches = before;
+                phaseLaunches = beforeP;
+                e->graphArgs = a;
+                e->graphBlock = G;
             }
+            if ((r = cudaGraphLaunch(e->graphExec, s)) != cudaSuccess) return cudaFail(r, "graph launch");
+            launches += e->graphLaunches;
+            phaseLaunches += e->graphPhaseLaunches;
+            sw += G;
+        } else {
+            if ((r = launchOne(npt && ((sw + 1) % ve == 0), p.time_phases != 0)) != cudaSuccess) return cudaFail(r, "sweep launch");
+            sw += 1;
+        }
+        if (nextCheck > 0 && sw >= nextCheck) {
+            // the cell list (box fractions) stays valid after an accepted volume move
             kTotalEnergy<<<e->nTotBlocks, kTotThreads, 0, s>>>(a, 0);
             kCheckEnergy<<<1, 32, 0, s>>>(a, e->nTotBlocks);
             launches += 2;
+            while (nextCheck <= sw) nextCheck += p.check_every;
         }
-        if ((r = cudaGetLastError()) != cudaSuccess) return cudaFail(r, "sweep launch");
-        if (npt && (sw + 1) % chunk == 0 && sw + 1 < p.nsweeps) {
+        if (nextRegrid > 0 && sw >= nextRegrid && sw < p.nsweeps) {
             // the box changed on the device: re-derive the cell grid when needed
+            while (nextRegrid <= sw) nextRegrid += chunk;
             cudaMemcpyAsync(box, c->d.box, sizeof box, cudaMemcpyDeviceToHost, s);
             if ((r = cudaStreamSynchronize(s)) != cudaSuccess) return cudaFail(r, "sweep");
             Grid ng = makeGrid(box, c->topo.maxcut, margin);
@@ -876,6 +919,7 @@ int runSweeps(Context* c, const sc_run_params& p, sc_run_stats& st) {
                 a = makeArgs(c, e, p);
             }
         }
+        if ((r = cudaGetLastError()) != cudaSuccess) return cudaFail(r, "sweep launch");
     }
     cudaEventRecord(e->ev1, s);
     if ((r = cudaStreamSynchronize(s)) != cudaSuccess) return cudaFail(r, "sweep");
