@@ -135,6 +135,23 @@ int sc_pair_energies(sc_context* ctx, int npairs, const int* i, const int* j, do
 /* TotalEMatrix::oneToAll / oneToAllTrial (totalenergycalculator.h:355-415): energy of
  * each target with every other particle. */
 int sc_one_to_all(sc_context* ctx, int ntargets, const int* targets, double* e);
+/* No counterpart in the reference.  The same energies as sc_one_to_all, for callers
+ * that must not allocate device memory: code running while another allocator (for
+ * instance a framework's caching allocator) holds all free device memory, so that a
+ * cudaMalloc would fail, and latency-critical loops in which a cudaMalloc / cudaFree
+ * would synchronise the device.  Targets and results are staged in a fixed array
+ * inside the library (SC_NOALLOC_MAX_TARGETS entries, 192 KiB on every GPU that
+ * loads the library, held until the process exits); this call allocates nothing.
+ *   - At most SC_NOALLOC_MAX_TARGETS targets per call (else SC_ERR_RANGE).
+ *   - The context's particle state must already be on the device: make one
+ *     allocating call (e.g. sc_one_to_all) after opening or changing it, else
+ *     SC_ERR_STATE.
+ *   - The first call on a device looks up the array's device address; make that
+ *     first call before any stream capture.
+ *   - All calls share the array: calls that overlap on the GPU (other host threads,
+ *     other contexts' streams) race; serialise them. */
+#define SC_NOALLOC_MAX_TARGETS 16384
+int sc_one_to_all_noalloc(sc_context* ctx, int ntargets, const int* targets, double* e);
 /* TotalEMatrix::allToAll (totalenergycalculator.h:334-353, 502-521). */
 int sc_all_to_all(sc_context* ctx, double* e);
 /* TotalEMatrix::mol2othersTrial (totalenergycalculator.h:453-499). */

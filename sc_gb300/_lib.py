@@ -76,6 +76,7 @@ SIGNATURES = [
     ("sc_pair_energy", C.c_int, [_P, C.c_int, C.c_int, _D]),
     ("sc_pair_energies", C.c_int, [_P, C.c_int, _I, _I, _D, C.POINTER(C.c_uint), _D]),
     ("sc_one_to_all", C.c_int, [_P, C.c_int, _I, _D]),
+    ("sc_one_to_all_noalloc", C.c_int, [_P, C.c_int, _I, _D]),
     ("sc_all_to_all", C.c_int, [_P, _D]),
     ("sc_mol_to_others", C.c_int, [_P, C.c_int, C.c_int, _D]),
     ("sc_trial_displace", C.c_int, [_P, C.c_int, _D, _D, _D]),
