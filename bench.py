@@ -45,6 +45,8 @@ def parse():
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     return ap.parse_args()
 
 
@@ -291,13 +293,13 @@ def main():
     bytes_per_particle = C.sizeof(L.Particle)
     e2e_moves = 0
     t0 = time.perf_counter()
-    for k in range(a.steps):
+    for k in range(0 if a.no_e2e else a.steps):
         s.set_particles(0, state)                 # host -> device (uploaded by the next call)
         st = s.simulate(p, nsweeps=1)
         state = s.particles()                     # device -> host
         e2e_moves += st.moves
-    e2e_s = time.perf_counter() - t0
-    e2e = {"value": e2e_moves * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": n * bytes_per_particle,
+    e2e_s = max(time.perf_counter() - t0, 1e-12)
+    e2e = {"value": e2e_moves * world / e2e_s if e2e_moves else None, "unit": UNIT, "h2d_bytes_per_step": n * bytes_per_particle,
            "d2h_bytes_per_step": 2 * n * bytes_per_particle + 64,
            "note": "state uploaded from pageable host memory before and downloaded after every sweep"}
 
@@ -320,7 +322,7 @@ def main():
 
     # CPU baseline: the oracle restatement of the reference loop, one core, bounded sample
     cpu = None
-    if rank == 0:
+    if rank == 0 and not a.no_cpu:
         try:
             probe_moves, probe_s = cpu_run(texts, a.seed, 1, 400)
             per_move = probe_s / max(1, probe_moves)
