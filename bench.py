@@ -222,6 +222,48 @@ def run_reference(a, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def bench_replicas(steps, seed=1):
+    """64 parallel-tempering replicas of the PSC model (8 systems of uneven N and density,
+    each over a geometric 0.8-1.6 ladder), moved together, exchanges every 100 sweeps;
+    against the same 64 replicas run one after another by the single-system loop."""
+    from sc_gb300 import ReplicaSet, System, workloads
+
+    systems, temps = workloads.pt_ladders(seed=seed)
+    ctxs, T, lad = [], [], []
+    for g, texts in enumerate(systems):
+        for t in temps:
+            ctxs.append(System.from_text(*texts))
+            T.append(t)
+            lad.append(g)
+    R = ReplicaSet(ctxs, T, ladder=lad)
+    # the tuner: cell reach (tile size) that moves the batch fastest
+    best = None
+    for s in (1, 2):
+        st, *_ = R.run(4, exchange_every=100, seed=seed, stencil=s, check_every=0)
+        rate = st.moves / st.seconds
+        if best is None or rate > best[1]:
+            best = (s, rate)
+    st, Tout, E, tried, acc = R.run(steps, exchange_every=100, seed=seed + 1, stencil=best[0], check_every=0)
+    batched = st.moves / st.seconds
+    # plain: every replica alone through the single-system loop (same tuned stencil)
+    moves = secs = 0.0
+    for g, texts in enumerate(systems):
+        s1 = System.from_text(*texts)
+        s1.simulate(nsweeps=2, seed=seed, stencil=best[0], check_every=0)
+        one = s1.simulate(nsweeps=3, seed=seed + 2, stencil=best[0], check_every=0)
+        moves += one.moves * len(temps)
+        secs += one.seconds * len(temps)
+        s1.close()
+    plain = moves / secs
+    R.close()
+    particles = sum(c.n for c in ctxs)
+    for c in ctxs:
+        c.close()
+    return {"workload": "pt64_psc_uneven", "replicas": len(ctxs), "particles": particles, "stencil": best[0],
+            "batched_moves_per_s": batched, "plain_moves_per_s": plain, "speedup": batched / plain,
+            "exchange_acceptance": float(acc.sum() / max(1, tried.sum())), "sweeps": steps}
+
+
 def main():
     a = parse()
     rank, world, local = dist_info()
@@ -334,6 +376,12 @@ def main():
         except Exception as ex:  # the baseline is reported, not required
             cpu = {"value": None, "unit": UNIT, "cores": 1, "kind": "port", "sample": f"failed: {ex}"}
 
+    replicas = None
+    if rank == 0 and not a.no_e2e:
+        try:
+            replicas = bench_replicas(max(10, a.steps), seed=a.seed)
+        except Exception as ex:
+            replicas = {"error": str(ex)}
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
                 "warmup": a.warmup, "ms_per_step": 1e3 * t_max / a.steps, "higher_is_better": True,
@@ -342,7 +390,7 @@ def main():
                            "parallelism": "replicas" if world > 1 else "single", "l2": "flushed between steps",
                            "seed": a.seed, "plain_fp64": True},
                 "clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roof, "fp64": fp64,
-                "cpu_baseline": cpu,
+                "cpu_baseline": cpu, "replicas": replicas,
                 "detail": {"acceptance": acc / max(1, moves), "pairs_tested_per_move": tested / max(1, moves),
                            "pairs_evaluated_per_move": evaluated / max(1, moves)}}
         print(json.dumps(line), flush=True)

@@ -81,6 +81,8 @@ typedef struct {
     double chain_angle;     /* chain rotation angle bound, radians */
     int check_every;        /* sweeps between exact total-energy checks (0: none) */
     int time_phases;        /* 1: time the move kernels with CUDA events (adds events to the stream) */
+    int stencil;            /* cell-list reach s: cells >= maxcut/s wide, (s+1)^3 colours; 0: chosen by the tuner */
+    int pad_;
 } sc_run_params;
 
 typedef struct {
@@ -170,6 +172,26 @@ int sc_trial_volume(sc_context* ctx, double psch, double* e_new);
 /* --- the move loop: Updater::simulate (scOOP/mc/updater.cpp:45-389) --------------------- */
 int sc_default_run(const sc_context* ctx, sc_run_params* p);
 int sc_simulate(sc_context* ctx, const sc_run_params* p, sc_run_stats* stats);
+
+/* --- parallel tempering: replicas moved together ------------------------------------------
+ * The reference runs one replica per MPI rank and exchanges temperatures in
+ * MoveCreator::replicaExchangeMove (scOOP/mc/movecreator.cpp:552-795).  Here all replicas
+ * (contexts on one GPU, any N) are moved by the same kernels in one launch sequence
+ * (captured as a CUDA graph), and the exchange is a device step over the replicas'
+ * running energies.  ladder[k] groups replicas into independent temperature ladders
+ * (NULL: one ladder); members of a ladder must hold the same system (N, types).  The
+ * contexts stay owned by the caller and must outlive the replica set. */
+typedef struct sc_replicas sc_replicas;
+int sc_replicas_create(sc_context* const* systems, int nrep, const double* temperatures, const int* ladder,
+                       sc_replicas** out);
+/* Runs p->nsweeps sweeps of every replica (p's temper is ignored: each replica keeps its
+ * ladder temperature; step sizes come from each replica's options unless p sets them),
+ * with an exchange attempt every exchange_every sweeps (0: none).  Outputs per replica
+ * (each may be NULL): its current temperature, running energy, and the exchange attempts
+ * / acceptances of ladder slot k with slot k+1. */
+int sc_replicas_run(sc_replicas* r, const sc_run_params* p, int exchange_every, sc_run_stats* stats,
+                    double* temperatures, double* energies, long* exchanges_tried, long* exchanges_accepted);
+int sc_replicas_destroy(sc_replicas* r);
 
 #ifdef __cplusplus
 }

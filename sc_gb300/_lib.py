@@ -43,7 +43,8 @@ class RunParams(C.Structure):
     _fields_ = [("nsweeps", C.c_long), ("seed", C.c_ulonglong), ("temper", C.c_double), ("press", C.c_double),
                 ("ptype", C.c_int), ("volume_every", C.c_int), ("transmx", C.c_double), ("rot_angle", C.c_double),
                 ("edge_mx", C.c_double), ("chainprob", C.c_double), ("chainmmx", C.c_double),
-                ("chain_angle", C.c_double), ("check_every", C.c_int), ("time_phases", C.c_int)]
+                ("chain_angle", C.c_double), ("check_every", C.c_int), ("time_phases", C.c_int),
+                ("stencil", C.c_int), ("pad_", C.c_int)]
 
 
 class RunStats(C.Structure):
@@ -85,6 +86,10 @@ SIGNATURES = [
     ("sc_trial_volume", C.c_int, [_P, C.c_double, _D]),
     ("sc_default_run", C.c_int, [_P, C.POINTER(RunParams)]),
     ("sc_simulate", C.c_int, [_P, C.POINTER(RunParams), C.POINTER(RunStats)]),
+    ("sc_replicas_create", C.c_int, [C.POINTER(_P), C.c_int, _D, _I, C.POINTER(_P)]),
+    ("sc_replicas_run", C.c_int, [_P, C.POINTER(RunParams), C.c_int, C.POINTER(RunStats), _D, _D,
+                                  C.POINTER(C.c_long), C.POINTER(C.c_long)]),
+    ("sc_replicas_destroy", C.c_int, [_P]),
 ]
 
 _lib = None

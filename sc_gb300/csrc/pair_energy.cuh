@@ -329,9 +329,26 @@ static __device__ __noinline__ double patchAttraction(const PairParam& ia, doubl
     return atr;
 }
 
+// x^-3 and x^-6 from one reciprocal: a few ulp from pow(x, -3) / pow(x, -6), with a
+// dependent FP64 chain a third as long (FP64 latency dominates the move kernel).
+__device__ __forceinline__ void invPow36(double x, double& i3, double& i6) {
+    double r = 1.0 / x;
+    i3 = r * r * r;
+    i6 = i3 * i3;
+}
+
+// A r^-12 - B r^-6 from r (the Lennard-Jones part of WcaTrunc / Sca / WcaCos2Taylor).
+__device__ __forceinline__ double lj12_6(double r, double A, double B) {
+    double i6, i12;
+    invPow36(r * r, i6, i12);
+    return A * i12 - B * i6;
+}
+
 __device__ __forceinline__ double wcaTruncSq(double distSq, const PairParam& ia) {   // paire.h:385-393
     if (distSq > ia.rcutwcaSq) return 0.0;
-    return ia.epsilon + ia.A * pow(distSq, -6.0) - ia.B * pow(distSq, -3.0);
+    double i3, i6;
+    invPow36(distSq, i3, i6);
+    return ia.epsilon + ia.A * i6 - ia.B * i3;
 }
 
 // HarmonicSc (paire.h:239-280) between particle a and its bonded partner b.
@@ -424,7 +441,7 @@ static __device__ __noinline__ double scScEnergy(const PairParam& ia, const PVie
                 if (ia.kind == K_SC_SCA) {      // Sca::operator() (paire.h:845-852)
                     double3 m2 = minDistSegments(d1, d2, ia.half_len[0], ia.half_len[1], r_cm);
                     double dd = sqrt(dot3(m2, m2));
-                    if (!(dd > ia.rcutwca)) atr += ia.A * pow(dd, -12.0) - ia.B * pow(dd, -6.0) + ia.epsilon;
+                    if (!(dd > ia.rcutwca)) atr += lj12_6(dd, ia.A, ia.B) + ia.epsilon;
                     continue;
                 }
                 PatchV P1{ld3(a.patch->pd[pn1]), ld3(a.patch->ps[2 * pn1]), ld3(a.patch->ps[2 * pn1 + 1])};
@@ -527,7 +544,7 @@ static __device__ __noinline__ double sphereEnergy(const PairParam& ia, const PV
     }
     double pot = 0.0;
     if (ia.kind == K_SP_WCA) {
-        if (!(dist > ia.rcutwca)) { pot = ia.A * pow(dist, -12.0) - ia.B * pow(dist, -6.0) + ia.epsilon; *bits |= V_WCA; }
+        if (!(dist > ia.rcutwca)) { pot = lj12_6(dist, ia.A, ia.B) + ia.epsilon; *bits |= V_WCA; }
     } else if (!(dist > ia.rcut || ia.epsilon == 0.0 || ia.exclude)) {
         *bits |= V_ATR;
         double e;
@@ -543,7 +560,7 @@ static __device__ __noinline__ double sphereEnergy(const PairParam& ia, const PV
             e = -ia.epsilon;
         }
         if (dist > ia.rcutwca) pot = e;
-        else { pot = ia.A * pow(dist, -12.0) - ia.B * pow(dist, -6.0); *bits |= V_WCA; }
+        else { pot = lj12_6(dist, ia.A, ia.B); *bits |= V_WCA; }
     }
     return bond + pot;
 }

@@ -67,6 +67,13 @@ struct PairParam {
     double rcut, rcutSq, rcutwca, rcutwcaSq;
     double half_len[2];
     double parallel;
+    // Exact-zero screen used by the move kernels: the pair energy is exactly 0 when the
+    // closest segment (SC-SC) or point-segment (SC-sphere) distance^2 exceeds screenSq
+    // and the pair is not bonded (the repulsive and attractive branches are both off).
+    int screen;        // 0: none (spheres), 1: segment-segment, 2: point-segment, 3: always zero
+    int scFirst;       // SC-sphere: 1 if the first particle is the spherocylinder
+    double screenSq;
+    double scHalf;     // SC-sphere: half length of the spherocylinder
 };
 
 // Bond / angle constants of a molecule type (scOOP/structures/moleculeparams.h:10-79),

@@ -1,6 +1,7 @@
 // sc_context.cu -- the C ABI (include/sc_gb300.h): context set-up, host<->device state
 // and the energy entry points.  The move loop lives in sweep.cu.
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -76,6 +77,20 @@ PairParam Context::devParam(int t1, int t2) const {
     p.rcut = s.rcut; p.rcutSq = s.rcutSq; p.rcutwca = s.rcutwca; p.rcutwcaSq = s.rcutwcaSq;
     p.half_len[0] = s.half_len[0]; p.half_len[1] = s.half_len[1];
     p.parallel = s.parallel;
+    // beyond these distances the repulsive and attractive branches are both off
+    // (SpheroCylinder::operator() paire.h:1130-1137, MixSpSc::operator() paire.h:1036-1041)
+    if (p.kind >= K_SC_PSC_CPSC && p.kind <= K_SC_SCA) {
+        p.screen = 1;
+        p.screenSq = (s.epsilon == 0.0 || s.exclude) ? s.rcutwcaSq : std::max(s.rcutSq, s.rcutwcaSq);
+    } else if (p.kind >= K_MIX_SCA_SPA) {
+        const IaParam& q = (g0 < SP) ? s : topo.ia[t2][t1];
+        p.screen = 2;
+        p.scFirst = g0 < SP;
+        p.scHalf = q.half_len[0];
+        p.screenSq = (q.epsilon == 0.0 || q.exclude) ? q.rcutwcaSq : std::max(q.rcutSq, q.rcutwcaSq);
+    } else if (p.kind == K_NONE) {
+        p.screen = 3;
+    }
     return p;
 }
 
@@ -609,6 +624,39 @@ int sc_default_run(const sc_context* ctx, sc_run_params* p) {
 int sc_simulate(sc_context* ctx, const sc_run_params* p, sc_run_stats* stats) {
     if (!ctx || !p || !stats) return fail(SC_ERR_ARG, "null argument");
     return runSweeps(C(ctx), *p, *stats);
+}
+
+struct sc_replicas {
+    void* impl;
+};
+
+int sc_replicas_create(sc_context* const* systems, int nrep, const double* temperatures, const int* ladder,
+                       sc_replicas** out) {
+    if (!systems || !temperatures || !out || nrep < 1) return fail(SC_ERR_ARG, "null argument");
+    std::vector<Context*> sys(nrep);
+    for (int k = 0; k < nrep; ++k) sys[k] = systems[k];
+    if (ladder)
+        for (int k = 0; k < nrep; ++k)
+            if (ladder[k] < 0 || ladder[k] >= nrep) return fail(SC_ERR_ARG, "ladder id out of range");
+    void* impl = nullptr;
+    int rc = createReplicas(sys.data(), nrep, temperatures, ladder, &impl);
+    if (rc) return rc;
+    *out = new sc_replicas{impl};
+    return SC_OK;
+}
+
+int sc_replicas_run(sc_replicas* r, const sc_run_params* p, int exchange_every, sc_run_stats* stats,
+                    double* temperatures, double* energies, long* tried, long* accepted) {
+    if (!r || !p || !stats) return fail(SC_ERR_ARG, "null argument");
+    if (exchange_every < 0) return fail(SC_ERR_ARG, "exchange_every must be >= 0");
+    return runReplicas(r->impl, *p, exchange_every, *stats, temperatures, energies, tried, accepted);
+}
+
+int sc_replicas_destroy(sc_replicas* r) {
+    if (!r) return fail(SC_ERR_ARG, "null argument");
+    destroyReplicas(r->impl);
+    delete r;
+    return SC_OK;
 }
 
 }  // extern "C"

@@ -12,7 +12,8 @@
 
 namespace scg {
 
-struct SweepEngine;   // sweep.cu
+struct SweepEngine;   // sweep.cu: device state of the move loop
+struct Batch;         // sweep.cu: systems moved together
 
 struct Context {
     Options opts;
@@ -45,6 +46,7 @@ struct Context {
     Particle trialState;
 
     SweepEngine* engine = nullptr;
+    Batch* batch = nullptr;
     long lastLaunches = 0;     // kernels launched by the last move loop
 
     Context() = default;
@@ -66,5 +68,9 @@ int fail(int code, const std::string& msg);
 int cudaFail(cudaError_t e, const char* where);
 int runSweeps(Context* c, const sc_run_params& p, sc_run_stats& st);
 void destroyEngine(Context* c);
+int createReplicas(Context* const* sys, int nrep, const double* temps, const int* group, void** out);
+void destroyReplicas(void* h);
+int runReplicas(void* h, const sc_run_params& p, int exchangeEvery, sc_run_stats& st, double* tempsOut,
+                double* energiesOut, long* exTried, long* exAcc);
 
 }  // namespace scg

@@ -3,12 +3,12 @@
 // One sweep = N attempted single-particle moves, run as a checkerboard over a cell
 // list so that moves in different cells proceed concurrently without changing the
 // stationary distribution:
-//   * cells are at least maxcut (= sqrt(sqmaxcut), the PairE prefilter range) wide,
-//     so every particle that can interact with a particle of a cell lies in that cell
-//     or one of its 26 neighbours;
-//   * each sweep shifts the cell grid by a random offset, rebuilds the cell list
-//     (counting sort), and visits the 2x2x2 colour classes in random order; cells of
-//     one colour are never neighbours, so their moves are independent;
+//   * cells are at least maxcut/s wide (maxcut = sqrt(sqmaxcut), the PairE prefilter
+//     range; s = stencil reach), so every particle that can interact with a particle of
+//     a cell lies within s cells of it;
+//   * each sweep shifts the grid by a random offset, rebuilds the cell list (counting
+//     sort), and visits the (s+1)^3 colour classes in random order; two cells of one
+//     colour are s+1 cells apart, so their moves are independent;
 //   * a cell performs as many moves as it holds particles, each on a randomly chosen
 //     particle of the cell; a displacement that would leave the cell is rejected
 //     (this keeps the cells independent and the move set symmetric);
@@ -23,14 +23,21 @@
 // All random numbers are Philox draws keyed by (seed, sweep, cell, move), so a run is
 // reproducible and independent of scheduling.
 //
-// One CTA owns one active cell.  For every move its threads scan the candidate list
-// (the cell and its neighbours, staged in shared memory), apply the cutoff prefilter in
-// FP64, compact the surviving (particle, old/new) pairs into a shared queue with a
-// deterministic block scan, evaluate the queue one pair per thread and reduce the old
-// and new energies in a fixed order.
+// One CTA owns one active cell.  The candidate partners (the cell and its stencil) are
+// staged in shared memory once per launch, positions as FP32 box fractions.  For each
+// move, warp 0 builds the proposal (one lane per rotated vector), then three stages
+// narrow the work that needs FP64:
+//   A  FP32 minimum-image distance of every candidate against the old / new position,
+//      with a margin that covers FP32 rounding: a candidate that fails is beyond the
+//      FP64 prefilter for certain;
+//   B  the FP64 prefilter of PairE (bit-exact) and an FP32 closest segment /
+//      point-segment distance: beyond the repulsive and attractive cutoffs (plus a
+//      margin) the reference's pair energy is exactly 0, so the pair is dropped;
+//   C  the full FP64 PairE of the survivors, one pair per thread.
+// Survivors are compacted with deterministic block scans, and the old and new energies
+// are summed in a fixed order, so runs are bit-reproducible.
 
 #include <algorithm>
-#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -44,31 +51,36 @@ namespace scg {
 namespace {
 
 constexpr int kMoveThreads = 128;
+constexpr int kWarps = kMoveThreads / 32;
 constexpr int kCellCap = 256;        // particles per cell
-constexpr int kCandCap = 1536;       // candidates staged in shared memory
-constexpr int kQueueCap = 1024;      // pair queue entries
-constexpr int kTotThreads = 128;
+constexpr int kNbCap = 343;          // stencil cells, (2*3+1)^3
+constexpr int kCandCap = 4096;       // candidates staged in shared memory
+constexpr int kQueueCap = 1536;      // pair queue entries
+constexpr int kChunk = 512;          // candidates per stage-A round
+constexpr int kMaxColours = 64;
+constexpr size_t kDynSmem = (size_t)kCandCap * (sizeof(float4) + sizeof(int));
 
 enum Ctr { C_ACC_T, C_REJ_T, C_ACC_R, C_REJ_R, C_ACC_V, C_REJ_V, C_VOL_CONSTR, C_TESTED, C_EVAL, C_CELL_REJ, C_MOVES,
-           C_COUNT };
-enum ErrBit { E_CELL_OVERFLOW = 1, E_PARTNER_FAR = 2, E_GRID = 4 };
+           C_SCREENED, C_COUNT };
+enum ErrBit { E_CELL_OVERFLOW = 1, E_PARTNER_FAR = 2, E_CAND_OVERFLOW = 4 };
 
 struct Grid {
     int nc[3];
-    int p[3];         // colours per dimension (1 or 2)
+    int p[3];         // colours per dimension (period of the colouring)
+    int s[3];         // stencil reach per dimension
     int ncells;
     int nactive;      // cells per colour
     int ncolours;
     double maxcut;
 };
 
-// Per-sweep control block, device resident (so that a sweep can be replayed as a graph).
+// Per-sweep control block, device resident (so that blocks of sweeps replay as a graph).
 struct Control {
     unsigned long long sweep;
     double shift[3];      // grid offset, box fractions
-    int perm[8];          // colour order
+    int perm[kMaxColours];
     double psch;          // volume move: edge change
-    int volValid;         // trial box keeps cells >= maxcut
+    int volValid;         // trial box keeps cells >= maxcut/s
     int pad_;
     double trialBox[3];
     double energy;        // running total energy
@@ -85,9 +97,10 @@ struct SweepArgs {
     int* cellCount;
     int* cellCursor;
     int* cellIdx;
+    float4* cellPosF;     // wrapped box fractions of cellIdx, FP32
     int* cellOf;
     double* cellDE;
-    double* partial;      // total-energy block sums
+    double* partial;      // per-cell energy sums
     unsigned long long* counters;
     int* err;
     uint64_t seed;
@@ -106,15 +119,24 @@ __device__ __forceinline__ int wrapCell(double x, double shift, int nc) {
     return c >= nc ? nc - 1 : (c < 0 ? 0 : c);
 }
 
-// Offsets of the neighbour cells along one dimension: each distinct cell once.
-__device__ __forceinline__ int neighbourOffsets(int nc, int* off) {
-    if (nc == 1) { off[0] = 0; return 1; }
-    if (nc == 2) { off[0] = 0; off[1] = 1; return 2; }
-    off[0] = -1; off[1] = 0; off[2] = 1;
-    return 3;
+__device__ __forceinline__ float frac32(double x) {
+    double f = x - floor(x);
+    float v = (float)f;
+    return v >= 1.0f ? 0.0f : v;
 }
 
-__global__ void kBeginSweep(SweepArgs a, int volumeDue) {
+// Distinct cells of the stencil along one dimension: -s..s, or every cell when the grid
+// is narrower than the stencil.
+__device__ __forceinline__ int axisCount(int nc, int s) { return nc <= 2 * s ? nc : 2 * s + 1; }
+__device__ __forceinline__ int axisCell(int c, int q, int nc, int s) {
+    return nc <= 2 * s ? q : (c + q - s + nc) % nc;
+}
+
+// Every kernel below serves a batch of independent systems: blockIdx.y selects the
+// system, whose arguments live in device memory (so that replica exchange can change a
+// system's temperature between launches of a captured graph).
+__global__ void kBeginSweep(const SweepArgs* __restrict__ A, int volumeDue) {
+    const SweepArgs& a = A[blockIdx.y];
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     Control& c = *a.ctl;
     Stream r(a.seed, 0xFFFFFFF0u, (uint32_t)c.sweep, (uint32_t)(c.sweep >> 32));
@@ -132,13 +154,20 @@ __global__ void kBeginSweep(SweepArgs a, int volumeDue) {
         bool ok = true;
         for (int d = 0; d < 3; ++d) {
             c.trialBox[d] = a.s.box[d] + c.psch;
-            if (!(c.trialBox[d] > 0.0) || c.trialBox[d] / a.g.nc[d] < a.g.maxcut) ok = false;
+            if (!(c.trialBox[d] > 0.0) || c.trialBox[d] / a.g.nc[d] * a.g.s[d] < a.g.maxcut) ok = false;
         }
         c.volValid = ok ? 1 : 0;
     }
 }
 
-__global__ void kAssign(SweepArgs a) {
+__global__ void kZeroCounts(const SweepArgs* __restrict__ A) {
+    const SweepArgs& a = A[blockIdx.y];
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < a.g.ncells) a.cellCount[c] = 0;
+}
+
+__global__ void kAssign(const SweepArgs* __restrict__ A) {
+    const SweepArgs& a = A[blockIdx.y];
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.s.n) return;
     const Control& c = *a.ctl;
@@ -151,7 +180,8 @@ __global__ void kAssign(SweepArgs a) {
     atomicAdd(&a.cellCount[cell], 1);
 }
 
-__global__ void kScan(SweepArgs a) {
+__global__ void kScan(const SweepArgs* __restrict__ A) {
+    const SweepArgs& a = A[blockIdx.y];
     // single block: exclusive scan of the cell counts
     __shared__ int warpTot[32];
     __shared__ int carry;
@@ -182,7 +212,8 @@ __global__ void kScan(SweepArgs a) {
     }
 }
 
-__global__ void kScatter(SweepArgs a) {
+__global__ void kScatter(const SweepArgs* __restrict__ A) {
+    const SweepArgs& a = A[blockIdx.y];
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.s.n) return;
     int cell = a.cellOf[i];
@@ -190,8 +221,10 @@ __global__ void kScatter(SweepArgs a) {
     a.cellIdx[slot] = i;
 }
 
-// Orders each cell's particles by index (deterministic lists whatever the atomics did).
-__global__ void kSortCells(SweepArgs a) {
+// Orders each cell's particles by index (deterministic lists whatever the atomics did)
+// and writes their FP32 wrapped positions in that order.
+__global__ void kSortCells(const SweepArgs* __restrict__ A) {
+    const SweepArgs& a = A[blockIdx.y];
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= a.g.ncells) return;
     int s = a.cellStart[c], n = a.cellCount[c];
@@ -201,14 +234,19 @@ __global__ void kSortCells(SweepArgs a) {
         while (j >= 0 && v[j] > x) { v[j + 1] = v[j]; --j; }
         v[j + 1] = x;
     }
+    for (int k = 0; k < n; ++k) {
+        double4_32a p = a.s.pos[v[k]];
+        a.cellPosF[s + k] = make_float4(frac32(p.x), frac32(p.y), frac32(p.z), 0.0f);
+    }
 }
 
-struct BlockScan {
-    int warpTot[kMoveThreads / 32];
+struct Scan {
+    int warpTot[kWarps];
+    int nbTot[kWarps];
 };
 
-// Exclusive scan of v over the block; returns the offset, writes the total.
-__device__ __forceinline__ int blockExclusiveScan(int v, int& total, BlockScan& sh) {
+// Exclusive scan of v over the block; returns the offset and the total.
+__device__ __forceinline__ int blockExclusiveScan(int v, int& total, Scan& sh) {
     int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     int incl = v;
 #pragma unroll
@@ -221,7 +259,7 @@ __device__ __forceinline__ int blockExclusiveScan(int v, int& total, BlockScan& 
     int woff = 0;
     total = 0;
 #pragma unroll
-    for (int q = 0; q < kMoveThreads / 32; ++q) {
+    for (int q = 0; q < kWarps; ++q) {
         int t = sh.warpTot[q];
         if (q < w) woff += t;
         total += t;
@@ -242,66 +280,119 @@ __device__ __forceinline__ void blockSum2(double& x, double& y, double (*sh)[2])
     __syncthreads();
     if (threadIdx.x == 0) {
         x = 0.0; y = 0.0;
-        for (int q = 0; q < kMoveThreads / 32; ++q) { x += sh[q][0]; y += sh[q][1]; }
+        for (int q = 0; q < kWarps; ++q) { x += sh[q][0]; y += sh[q][1]; }
     }
     __syncthreads();
 }
 
-struct MoveShared {
-    int list[kCellCap];
-    int cand[kCandCap];
-    int queue[kQueueCap];
-    int nbCell[27];
+// Stencil of a cell and the flattened candidate list, shared by the move and energy kernels.
+struct Stencil {
+    int nbCell[kNbCap];
+    int nbOff[kNbCap + 1];
     int nNb;
     int nCand;
-    // current proposal
-    int target, displace, skip, partners[4], nPartners;
-    double umet;
-    double npos[3], ndir[3];
-    PatchSet npatch;
-    BlockScan scan;
-    double red[kMoveThreads / 32][2];
+    int ownOff;         // offset of the cell's own particles in the candidate list
+    int overflow;
 };
 
-__device__ __forceinline__ void randomUnitSphere(Stream& r, double& x, double& y, double& z) {
-    // Vector::randomUnitSphere (scOOP/structures/Vector.h:190-205)
-    double a, xi1, xi2;
-    do {
-        xi1 = 1.0 - 2.0 * r.next();
-        xi2 = 1.0 - 2.0 * r.next();
-        a = xi1 * xi1 + xi2 * xi2;
-    } while (a > 1.0);
-    double b = 2.0 * sqrt(1.0 - a);
-    x = xi1 * b; y = xi2 * b; z = 1.0 - 2.0 * a;
+__device__ void stageCandidates(const SweepArgs& a, int cx, int cy, int cz, Stencil& st, Scan& sc, int* candIdx,
+                                float4* candPos) {
+    const Grid& g = a.g;
+    const int nx = axisCount(g.nc[0], g.s[0]), ny = axisCount(g.nc[1], g.s[1]), nz = axisCount(g.nc[2], g.s[2]);
+    const int nn = nx * ny * nz;
+    const int own = g.nc[0] <= 2 * g.s[0] ? cx : g.s[0];
+    const int ownY = g.nc[1] <= 2 * g.s[1] ? cy : g.s[1];
+    const int ownZ = g.nc[2] <= 2 * g.s[2] ? cz : g.s[2];
+    const int ownQ = (ownZ * ny + ownY) * nx + own;
+    int carry = 0;
+    for (int base = 0; base < nn; base += kMoveThreads) {
+        int q = base + threadIdx.x;
+        int cnt = 0, cell = 0;
+        if (q < nn) {
+            int qx = q % nx, qy = (q / nx) % ny, qz = q / (nx * ny);
+            int x = axisCell(cx, qx, g.nc[0], g.s[0]);
+            int y = axisCell(cy, qy, g.nc[1], g.s[1]);
+            int z = axisCell(cz, qz, g.nc[2], g.s[2]);
+            cell = (z * g.nc[1] + y) * g.nc[0] + x;
+            cnt = a.cellCount[cell];
+        }
+        int total;
+        int off = blockExclusiveScan(cnt, total, sc);
+        if (q < nn) {
+            st.nbCell[q] = cell;
+            st.nbOff[q] = carry + off;
+        }
+        carry += total;
+    }
+    if (threadIdx.x == 0) {
+        st.nNb = nn;
+        st.nbOff[nn] = carry;
+        st.nCand = carry;
+        st.overflow = carry > kCandCap;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) st.ownOff = st.nbOff[ownQ];
+    if (st.overflow) {
+        if (threadIdx.x == 0) atomicOr(a.err, E_CAND_OVERFLOW);
+        __syncthreads();
+        return;
+    }
+    for (int k = threadIdx.x; k < carry; k += kMoveThreads) {
+        int lo = 0, hi = nn - 1;      // last q with nbOff[q] <= k
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (st.nbOff[mid] <= k) lo = mid; else hi = mid - 1;
+        }
+        int slot = a.cellStart[st.nbCell[lo]] + (k - st.nbOff[lo]);
+        candIdx[k] = a.cellIdx[slot];
+        candPos[k] = a.cellPosF[slot];
+    }
+    __syncthreads();
 }
 
-// Particle::pscRotate (scOOP/structures/particle.h:182-272) followed by the
-// re-orthogonalisation of patchdir[0] in partRotate (movecreator.cpp:1007).
-__device__ void pscRotate(double* dir, PatchSet& ps, int g, double angle, double ax, double ay, double az, bool positive) {
-    double vc = cos(angle);
-    double vs = positive ? sqrt(1.0 - vc * vc) : -sqrt(1.0 - vc * vc);
-    double qw = vc, qx = ax * vs, qy = ay * vs, qz = az * vs;
-    double t2 = qw * qx, t3 = qw * qy, t4 = qw * qz, t5 = -qx * qx, t6 = qx * qy, t7 = qx * qz, t8 = -qy * qy,
-           t9 = qy * qz, t10 = -qz * qz;
-    double d1 = t8 + t10, d2 = t6 - t4, d3 = t3 + t7, d4 = t4 + t6, d5 = t5 + t10, d6 = t9 - t2, d7 = t7 - t3,
-           d8 = t2 + t9, d9 = t5 + t8;
-    auto rot = [&](double* v) {
-        double nx = 2.0 * (d1 * v[0] + d2 * v[1] + d3 * v[2]) + v[0];
-        double ny = 2.0 * (d4 * v[0] + d5 * v[1] + d6 * v[2]) + v[1];
-        double nz = 2.0 * (d7 * v[0] + d8 * v[1] + d9 * v[2]) + v[2];
-        v[0] = nx; v[1] = ny; v[2] = nz;
-    };
-    rot(dir);
-    if (g != SCN && g != SCA) {
-        int m = isTwoPatch(g) ? 2 : 1;
-        for (int k = 0; k < m; ++k) { rot(ps.pd[k]); rot(ps.ps[2 * k]); rot(ps.ps[2 * k + 1]); }
+// FP32 closest distance^2 of two segments (centres r apart, r = c1 - c2, unit axes u, v,
+// half lengths h1, h2): line solution clamped, then alternating clamped minimisation.
+// Any feasible (s, t) bounds the true minimum from above and the error of this
+// sequence is far below the screening margin.
+__device__ __forceinline__ float segDist2f(float3 r, float3 u, float3 v, float h1, float h2) {
+    float b = u.x * v.x + u.y * v.y + u.z * v.z;
+    float d = u.x * r.x + u.y * r.y + u.z * r.z;
+    float e = v.x * r.x + v.y * r.y + v.z * r.z;
+    float den = 1.0f - b * b;
+    float s = den > 1e-6f ? (b * e - d) / den : 0.0f;
+    s = fminf(fmaxf(s, -h1), h1);
+    float t = fminf(fmaxf(b * s + e, -h2), h2);
+    s = fminf(fmaxf(b * t - d, -h1), h1);
+    t = fminf(fmaxf(b * s + e, -h2), h2);
+    float x = r.x + s * u.x - t * v.x, y = r.y + s * u.y - t * v.y, z = r.z + s * u.z - t * v.z;
+    return x * x + y * y + z * z;
+}
+
+__device__ __forceinline__ float pointSegDist2f(float3 rc, float3 u, float h) {
+    float c = u.x * rc.x + u.y * rc.y + u.z * rc.z;
+    c = fminf(fmaxf(c, -h), h);
+    float x = -rc.x + u.x * c, y = -rc.y + u.y * c, z = -rc.z + u.z * c;
+    return x * x + y * y + z * z;
+}
+
+// True when the pair energy is exactly zero by the screen of PairParam (and the pair is
+// not bonded, which the callers exclude).
+__device__ __forceinline__ bool screenedOut(const PairParam& pp, const double3& r_cm, const double3& d1,
+                                           const double3& d2) {
+    if (pp.screen == 3) return true;
+    if (pp.screen == 0) return false;
+    float3 r = make_float3((float)r_cm.x, (float)r_cm.y, (float)r_cm.z);
+    float3 u = make_float3((float)d1.x, (float)d1.y, (float)d1.z);
+    float3 v = make_float3((float)d2.x, (float)d2.y, (float)d2.z);
+    float dd;
+    if (pp.screen == 1) {
+        dd = segDist2f(r, u, v, (float)pp.half_len[0], (float)pp.half_len[1]);
+    } else if (pp.scFirst) {
+        dd = pointSegDist2f(r, u, (float)pp.scHalf);
+    } else {
+        dd = pointSegDist2f(make_float3(-r.x, -r.y, -r.z), v, (float)pp.scHalf);
     }
-    if (isChiral(g)) {
-        int m = (g == TCHPSC || g == TCHCPSC) ? 2 : 1;
-        for (int k = 0; k < m; ++k) rot(ps.ch[k]);
-    }
-    double dp = ps.pd[0][0] * dir[0] + ps.pd[0][1] * dir[1] + ps.pd[0][2] * dir[2];
-    ps.pd[0][0] -= dp * dir[0]; ps.pd[0][1] -= dp * dir[1]; ps.pd[0][2] -= dp * dir[2];
+    return dd > (float)pp.screenSq * 1.001f + 1e-3f;
 }
 
 __device__ __forceinline__ PView viewAt(const DevState& s, int j) {
@@ -317,120 +408,202 @@ __device__ __forceinline__ PView viewAt(const DevState& s, int j) {
     return v;
 }
 
-__global__ void __launch_bounds__(kMoveThreads) kColour(SweepArgs a, int phase) {
-    __shared__ MoveShared sh;
+// FP32 candidate threshold: (maxcut + margin)^2, the margin covering the FP32 rounding
+// of wrapped box fractions times the box.
+__device__ __forceinline__ float candThreshold(double sqmaxcut, const double3& box) {
+    double bmax = fmax(box.x, fmax(box.y, box.z));
+    double r = sqrt(sqmaxcut) + 1e-6 * bmax + 1e-5;
+    return (float)(r * r) * 1.0001f;
+}
+
+__device__ __forceinline__ float dist2f(float4 a, float3 b, const double3& box) {
+    float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+    dx -= rintf(dx); dy -= rintf(dy); dz -= rintf(dz);
+    dx *= (float)box.x; dy *= (float)box.y; dz *= (float)box.z;
+    return dx * dx + dy * dy + dz * dz;
+}
+
+constexpr int kClassCap = 768;       // stage-C queue entries per pair class
+
+// Pair class of the stage-C queue: SC-SC, SC-sphere, everything else.  Entries of one
+// class are evaluated by consecutive threads, so a warp follows one functor's branches.
+__device__ __forceinline__ int pairClass(int kind) {
+    return (kind >= K_SC_PSC_CPSC && kind <= K_SC_SCA) ? 0 : (kind >= K_MIX_SCA_SPA ? 1 : 2);
+}
+
+struct MoveShared {
+    int list[kCellCap];
+    int queueA[kQueueCap];
+    int queueB[3][kClassCap];
+    Stencil st;
+    Scan scan;
+    double red[kWarps][2];
+    // current proposal
+    int target, slotR, displace, skip, partners[4], nPartners;
+    double umet;
+    double npos[3], ndir[3];
+    float3 oldF, newF;
+    PatchSet npatch;
+};
+
+__device__ __forceinline__ void randomUnitSphere(Stream& r, double& x, double& y, double& z) {
+    // Vector::randomUnitSphere (scOOP/structures/Vector.h:190-205)
+    double a, xi1, xi2;
+    do {
+        xi1 = 1.0 - 2.0 * r.next();
+        xi2 = 1.0 - 2.0 * r.next();
+        a = xi1 * xi1 + xi2 * xi2;
+    } while (a > 1.0);
+    double b = 2.0 * sqrt(1.0 - a);
+    x = xi1 * b; y = xi2 * b; z = 1.0 - 2.0 * a;
+}
+
+// Warp 0 builds the proposal of move m.  Particle::pscRotate (particle.h:182-272): every
+// lane forms the rotation matrix, lane k rotates vector k (axis, patch directions, patch
+// sides, chiral axes), then patchdir[0] is re-orthogonalised against the new axis as
+// partRotate does (movecreator.cpp:1007).
+__device__ void buildProposal(const SweepArgs& a, MoveShared& sh, int cell, int cnt, int m, int cx, int cy, int cz,
+                              const double3& box) {
     const Control& ctl = *a.ctl;
-    const Grid& g = a.g;
-    int colour = ctl.perm[phase];
+    const int lane = threadIdx.x & 31;
+    Stream r(a.seed, (uint32_t)cell, (uint32_t)m, (uint32_t)ctl.sweep ^ ((uint32_t)(ctl.sweep >> 32) << 20));
+    int slotR = min((int)(r.next() * cnt), cnt - 1);
+    int t = sh.list[slotR];
+    double4_32a p = a.s.pos[t];
+    double4_32a d = a.s.dir[t];
+    int type = (int)p.w;
+    int geo = a.geo[type];
+    bool displace = (r.next() < 0.5) || geo >= SP;
+    int skip = 0;
+    double npx = p.x, npy = p.y, npz = p.z;
+    if (displace) {
+        double x, y, z;
+        randomUnitSphere(r, x, y, z);
+        double mx = a.trans[type];
+        x *= mx / box.x; y *= mx / box.y; z *= mx / box.z;
+        npx = p.x + x; npy = p.y + y; npz = p.z + z;
+        int nx = wrapCell(npx, ctl.shift[0], a.g.nc[0]);
+        int ny = wrapCell(npy, ctl.shift[1], a.g.nc[1]);
+        int nz = wrapCell(npz, ctl.shift[2], a.g.nc[2]);
+        if (nx != cx || ny != cy || nz != cz) skip = 1;     // would leave the cell
+        if (lane == 0) { sh.ndir[0] = d.x; sh.ndir[1] = d.y; sh.ndir[2] = d.z; }
+    } else {
+        double angle = a.rotAngle * r.next();
+        double ax, ay, az;
+        randomUnitSphere(r, ax, ay, az);
+        bool positive = r.next() < 0.5;
+        double vc = cos(angle);
+        double vs = positive ? sqrt(1.0 - vc * vc) : -sqrt(1.0 - vc * vc);
+        double qw = vc, qx = ax * vs, qy = ay * vs, qz = az * vs;
+        double t2 = qw * qx, t3 = qw * qy, t4 = qw * qz, t5 = -qx * qx, t6 = qx * qy, t7 = qx * qz, t8 = -qy * qy,
+               t9 = qy * qz, t10 = -qz * qz;
+        double d1 = t8 + t10, d2 = t6 - t4, d3 = t3 + t7, d4 = t4 + t6, d5 = t5 + t10, d6 = t9 - t2, d7 = t7 - t3,
+               d8 = t2 + t9, d9 = t5 + t8;
+        // lane k: 0 axis, 1-2 patchdir, 3-6 patchsides, 7-8 chdir
+        const PatchSet& ps = a.s.patch[t];
+        double v[3];
+        bool rotate;
+        int twoP = isTwoPatch(geo) ? 2 : 1;
+        int twoC = (geo == TCHPSC || geo == TCHCPSC) ? 2 : 1;
+        if (lane == 0) { v[0] = d.x; v[1] = d.y; v[2] = d.z; rotate = true; }
+        else if (lane <= 2) { for (int q = 0; q < 3; ++q) v[q] = ps.pd[lane - 1][q]; rotate = geo != SCN && geo != SCA && (lane - 1) < twoP; }
+        else if (lane <= 6) { for (int q = 0; q < 3; ++q) v[q] = ps.ps[lane - 3][q]; rotate = geo != SCN && geo != SCA && ((lane - 3) >> 1) < twoP; }
+        else if (lane <= 8) { for (int q = 0; q < 3; ++q) v[q] = ps.ch[lane - 7][q]; rotate = isChiral(geo) && (lane - 7) < twoC; }
+        else { v[0] = v[1] = v[2] = 0.0; rotate = false; }
+        if (rotate) {
+            double nx = 2.0 * (d1 * v[0] + d2 * v[1] + d3 * v[2]) + v[0];
+            double ny = 2.0 * (d4 * v[0] + d5 * v[1] + d6 * v[2]) + v[1];
+            double nz = 2.0 * (d7 * v[0] + d8 * v[1] + d9 * v[2]) + v[2];
+            v[0] = nx; v[1] = ny; v[2] = nz;
+        }
+        double dx = __shfl_sync(0xffffffffu, v[0], 0), dy = __shfl_sync(0xffffffffu, v[1], 0),
+               dz = __shfl_sync(0xffffffffu, v[2], 0);
+        if (lane == 1) {
+            double dp = v[0] * dx + v[1] * dy + v[2] * dz;
+            v[0] -= dp * dx; v[1] -= dp * dy; v[2] -= dp * dz;
+        }
+        if (lane == 0) { sh.ndir[0] = v[0]; sh.ndir[1] = v[1]; sh.ndir[2] = v[2]; }
+        else if (lane <= 2) { for (int q = 0; q < 3; ++q) sh.npatch.pd[lane - 1][q] = v[q]; }
+        else if (lane <= 6) { for (int q = 0; q < 3; ++q) sh.npatch.ps[lane - 3][q] = v[q]; }
+        else if (lane <= 8) { for (int q = 0; q < 3; ++q) sh.npatch.ch[lane - 7][q] = v[q]; }
+    }
+    double umet = r.next();
+    if (lane == 0) {
+        sh.target = t;
+        sh.slotR = slotR;
+        sh.displace = displace;
+        sh.umet = umet;
+        sh.npos[0] = npx; sh.npos[1] = npy; sh.npos[2] = npz;
+        sh.oldF = make_float3(frac32(p.x), frac32(p.y), frac32(p.z));
+        sh.newF = make_float3(frac32(npx), frac32(npy), frac32(npz));
+        // bonded partners are evaluated explicitly; they must sit inside the stencil
+        DevCtx c;
+        c.mols = a.t.mols;
+        Con con = makeCon(c, t, a.s.mol[t]);
+        int np = 0;
+        for (int q = 0; q < 4; ++q) {
+            int j = con.idx[q];
+            if (j < 0) continue;
+            int cj = a.cellOf[j];
+            bool near = false;
+            for (int w = 0; w < sh.st.nNb; ++w) near |= (sh.st.nbCell[w] == cj);
+            if (!near) { atomicOr(a.err, E_PARTNER_FAR); skip = 1; }
+            sh.partners[np++] = j;
+        }
+        sh.nPartners = np;
+        sh.skip = skip;
+    }
+}
+
+__device__ __forceinline__ void decodeActive(const Grid& g, int colour, int block, int& cx, int& cy, int& cz) {
     int ox = colour % g.p[0], oy = (colour / g.p[0]) % g.p[1], oz = colour / (g.p[0] * g.p[1]);
     int ax = g.nc[0] / g.p[0], ay = g.nc[1] / g.p[1];
-    int bx = blockIdx.x % ax, by = (blockIdx.x / ax) % ay, bz = blockIdx.x / (ax * ay);
-    int cx = ox + g.p[0] * bx, cy = oy + g.p[1] * by, cz = oz + g.p[2] * bz;
+    int bx = block % ax, by = (block / ax) % ay, bz = block / (ax * ay);
+    cx = ox + g.p[0] * bx; cy = oy + g.p[1] * by; cz = oz + g.p[2] * bz;
+}
+
+__global__ void __launch_bounds__(kMoveThreads) kColour(const SweepArgs* __restrict__ A, int phase) {
+    extern __shared__ float4 dynSmem[];
+    float4* candPos = dynSmem;
+    int* candIdx = reinterpret_cast<int*>(candPos + kCandCap);
+    __shared__ MoveShared sh;
+    const SweepArgs& a = A[blockIdx.y];
+    const Control& ctl = *a.ctl;
+    const Grid& g = a.g;
+    if ((int)blockIdx.x >= g.nactive || phase >= g.ncolours) return;
+    int cx, cy, cz;
+    decodeActive(g, ctl.perm[phase], blockIdx.x, cx, cy, cz);
     int cell = (cz * g.nc[1] + cy) * g.nc[0] + cx;
     int cnt = a.cellCount[cell];
     if (cnt == 0 || cnt > kCellCap) return;
-    const int tid = threadIdx.x;
-    const int* idx = a.cellIdx;
-    for (int k = tid; k < cnt; k += kMoveThreads) sh.list[k] = idx[a.cellStart[cell] + k];
-    if (tid == 0) {
-        int offx[3], offy[3], offz[3];
-        int nx = neighbourOffsets(g.nc[0], offx), ny = neighbourOffsets(g.nc[1], offy), nz = neighbourOffsets(g.nc[2], offz);
-        int nn = 0;
-        for (int qz = 0; qz < nz; ++qz)
-            for (int qy = 0; qy < ny; ++qy)
-                for (int qx = 0; qx < nx; ++qx) {
-                    int x = (cx + offx[qx] + g.nc[0]) % g.nc[0];
-                    int y = (cy + offy[qy] + g.nc[1]) % g.nc[1];
-                    int z = (cz + offz[qz] + g.nc[2]) % g.nc[2];
-                    sh.nbCell[nn++] = (z * g.nc[1] + y) * g.nc[0] + x;
-                }
-        sh.nNb = nn;
-        int m = 0;
-        for (int q = 0; q < nn; ++q) m += a.cellCount[sh.nbCell[q]];
-        sh.nCand = m;
-    }
-    __syncthreads();
-    const int nCand = sh.nCand;
-    const bool staged = nCand <= kCandCap;
-    if (staged) {
-        // flatten the candidate list (cells in order, particles by index)
-        int base = 0;
-        for (int q = 0; q < sh.nNb; ++q) {
-            int c2 = sh.nbCell[q], n2 = a.cellCount[c2], s2 = a.cellStart[c2];
-            for (int k = tid; k < n2; k += kMoveThreads) sh.cand[base + k] = idx[s2 + k];
-            base += n2;
-        }
-    }
-    __syncthreads();
+    const int tid = threadIdx.x, warp = tid >> 5;
+    for (int k = tid; k < cnt; k += kMoveThreads) sh.list[k] = a.cellIdx[a.cellStart[cell] + k];
+    stageCandidates(a, cx, cy, cz, sh.st, sh.scan, candIdx, candPos);
+    if (sh.st.overflow) return;
+    const int nCand = sh.st.nCand;
 
     DevCtx c;
     c.params = a.t.params; c.mols = a.t.mols; c.ntypes = a.t.ntypes; c.n = a.s.n; c.sqmaxcut = a.t.sqmaxcut;
     const double3 box = mk(a.s.box[0], a.s.box[1], a.s.box[2]);
+    const float thr32 = candThreshold(c.sqmaxcut, box);
     double dECell = 0.0;
-    unsigned long long nAccT = 0, nRejT = 0, nAccR = 0, nRejR = 0, nTested = 0, nEval = 0, nCellRej = 0;
+    unsigned long long nAccT = 0, nRejT = 0, nAccR = 0, nRejR = 0, nTested = 0, nEval = 0, nCellRej = 0, nScr = 0;
 
     for (int m = 0; m < cnt; ++m) {
-        if (tid == 0) {
-            Stream r(a.seed, (uint32_t)cell, (uint32_t)m, (uint32_t)ctl.sweep ^ ((uint32_t)(ctl.sweep >> 32) << 20));
-            int t = sh.list[min((int)(r.next() * cnt), cnt - 1)];
-            double4_32a p = a.s.pos[t];
-            double4_32a d = a.s.dir[t];
-            int type = (int)p.w;
-            int geo = a.geo[type];
-            bool displace = (r.next() < 0.5) || geo >= SP;
-            sh.target = t;
-            sh.displace = displace;
-            sh.skip = 0;
-            if (displace) {
-                double x, y, z;
-                randomUnitSphere(r, x, y, z);
-                double mx = a.trans[type];
-                x *= mx / box.x; y *= mx / box.y; z *= mx / box.z;
-                sh.npos[0] = p.x + x; sh.npos[1] = p.y + y; sh.npos[2] = p.z + z;
-                sh.ndir[0] = d.x; sh.ndir[1] = d.y; sh.ndir[2] = d.z;
-                int nx = wrapCell(sh.npos[0], ctl.shift[0], g.nc[0]);
-                int ny = wrapCell(sh.npos[1], ctl.shift[1], g.nc[1]);
-                int nz = wrapCell(sh.npos[2], ctl.shift[2], g.nc[2]);
-                if (nx != cx || ny != cy || nz != cz) sh.skip = 1;     // would leave the cell
-            } else {
-                double angle = a.rotAngle * r.next();
-                double x, y, z;
-                randomUnitSphere(r, x, y, z);
-                bool positive = r.next() < 0.5;
-                sh.npos[0] = p.x; sh.npos[1] = p.y; sh.npos[2] = p.z;
-                sh.ndir[0] = d.x; sh.ndir[1] = d.y; sh.ndir[2] = d.z;
-                sh.npatch = a.s.patch[t];
-                pscRotate(sh.ndir, sh.npatch, geo, angle, x, y, z, positive);
-            }
-            sh.umet = r.next();
-            // bonded partners are evaluated explicitly; they must sit in this or a neighbour cell
-            int4 mi = a.s.mol[t];
-            Con con = makeCon(c, t, mi);
-            int np = 0;
-            for (int q = 0; q < 4; ++q) {
-                int j = con.idx[q];
-                if (j < 0) continue;
-                bool near = false;
-                int cj = a.cellOf[j];
-                for (int w = 0; w < sh.nNb; ++w) near |= (sh.nbCell[w] == cj);
-                if (!near) { atomicOr(a.err, E_PARTNER_FAR); sh.skip = 1; }
-                sh.partners[np++] = j;
-            }
-            sh.nPartners = np;
-        }
+        if (warp == 0) buildProposal(a, sh, cell, cnt, m, cx, cy, cz, box);
         __syncthreads();
         const int t = sh.target;
+        const bool displace = sh.displace;
         if (sh.skip) {
-            if (tid == 0) { if (sh.displace) { ++nRejT; ++nCellRej; } else ++nRejR; }
+            if (tid == 0) { if (displace) { ++nRejT; ++nCellRej; } else ++nRejR; }
             __syncthreads();
             continue;
         }
-        const bool displace = sh.displace;
         const int np = sh.nPartners;
         int partners[4] = {-1, -1, -1, -1};
         for (int q = 0; q < np; ++q) partners[q] = sh.partners[q];
-        double4_32a op4 = a.s.pos[t];
-        double4_32a od4 = a.s.dir[t];
+        const double4_32a op4 = a.s.pos[t];
+        const double4_32a od4 = a.s.dir[t];
         PView oldV;
         oldV.pos = mk(op4.x, op4.y, op4.z);
         oldV.dir = mk(od4.x, od4.y, od4.z);
@@ -442,69 +615,89 @@ __global__ void __launch_bounds__(kMoveThreads) kColour(SweepArgs a, int phase) 
         newV.pos = mk(sh.npos[0], sh.npos[1], sh.npos[2]);
         newV.dir = mk(sh.ndir[0], sh.ndir[1], sh.ndir[2]);
         if (!displace) newV.patch = &sh.npatch;
-        Con con = makeCon(c, t, a.s.mol[t]);
+        const Con con = makeCon(c, t, a.s.mol[t]);
+        const float3 oldF = sh.oldF, newF = sh.newF;
 
         double eOld = 0.0, eNew = 0.0;
-        int qn = 0;
-        // bonded partners: both configurations, whatever the distance
-        if (tid < np) {
+        if (tid < np) {     // bonded partners: both configurations, whatever the distance
             PView b = viewAt(a.s, partners[tid]);
             unsigned bb; double dd;
             eOld += pairEnergy(c, oldV, b, con, box, &bb, &dd);
             eNew += pairEnergy(c, newV, b, con, box, &bb, &dd);
         }
-        auto flush = [&](int count) {
+        int qb0 = 0, qb1 = 0, qb2 = 0;
+        auto flushC = [&]() {              // stage C: full FP64 pair energies, class by class
+            __syncthreads();               // queue entries of every thread are visible
+            const int count = qb0 + qb1 + qb2;
             for (int e = tid; e < count; e += kMoveThreads) {
-                int q = sh.queue[e];
-                int j = q >> 1;
-                PView b = viewAt(a.s, j);
+                int q = e < qb0 ? sh.queueB[0][e] : (e < qb0 + qb1 ? sh.queueB[1][e - qb0] : sh.queueB[2][e - qb0 - qb1]);
+                PView b = viewAt(a.s, candIdx[q >> 1]);
                 unsigned bb; double dd;
                 if (q & 1) eNew += pairEnergy(c, newV, b, con, box, &bb, &dd);
                 else eOld += pairEnergy(c, oldV, b, con, box, &bb, &dd);
             }
             __syncthreads();
         };
-        for (int base = 0; base < nCand; base += kMoveThreads) {
-            int k = base + tid;
-            int flags = 0, j = -1;
-            if (k < nCand) {
-                if (staged) j = sh.cand[k];
-                else {
-                    int rem = k;
-                    for (int q = 0; q < sh.nNb; ++q) {
-                        int n2 = a.cellCount[sh.nbCell[q]];
-                        if (rem < n2) { j = idx[a.cellStart[sh.nbCell[q]] + rem]; break; }
-                        rem -= n2;
+        for (int base = 0; base < nCand; base += kChunk) {
+            // stage A: FP32 minimum image against the old and the new position
+            int qa = 0;
+            for (int r0 = base; r0 < min(base + kChunk, nCand); r0 += kMoveThreads) {
+                int k = r0 + tid;
+                int flags = 0;
+                if (k < min(base + kChunk, nCand)) {
+                    int j = candIdx[k];
+                    bool partner = (j == partners[0] || j == partners[1] || j == partners[2] || j == partners[3]);
+                    if (j != t && !partner) {
+                        float4 cp = candPos[k];
+                        bool p0 = dist2f(cp, oldF, box) <= thr32;
+                        bool p1 = displace ? dist2f(cp, newF, box) <= thr32 : p0;
+                        flags = (p0 ? 1 : 0) | (p1 ? 2 : 0);
                     }
                 }
-                bool partner = (j == partners[0] || j == partners[1] || j == partners[2] || j == partners[3]);
-                if (j != t && !partner) {
-                    double4_32a pj = a.s.pos[j];
-                    double3 pp = mk(pj.x, pj.y, pj.z);
-                    double3 r0 = imageVec(oldV.pos, pp, box);
-                    bool pass0 = !(dot3(r0, r0) > c.sqmaxcut);
-                    bool pass1 = pass0;
-                    if (displace) {
-                        double3 r1 = imageVec(newV.pos, pp, box);
-                        pass1 = !(dot3(r1, r1) > c.sqmaxcut);
-                    }
-                    flags = (pass0 ? 1 : 0) | (pass1 ? 2 : 0);
-                }
+                int total;
+                int off = blockExclusiveScan(__popc(flags), total, sh.scan);
+                if (flags & 1) sh.queueA[qa + off++] = k << 1;
+                if (flags & 2) sh.queueA[qa + off] = (k << 1) | 1;
+                qa += total;
             }
-            int total;
-            int off = blockExclusiveScan(__popc(flags), total, sh.scan);
-            if (flags & 1) sh.queue[qn + off++] = j << 1;
-            if (flags & 2) sh.queue[qn + off] = (j << 1) | 1;
-            qn += total;
             __syncthreads();
-            if (qn > kQueueCap - 2 * kMoveThreads) {
-                flush(qn);
-                nEval += qn;
-                qn = 0;
+            // stage B: FP64 prefilter (bit-exact) and the exact-zero screen
+            for (int e0 = 0; e0 < qa; e0 += kMoveThreads) {
+                int e = e0 + tid;
+                int keep = 0, q = 0, cls = 0;
+                if (e < qa) {
+                    q = sh.queueA[e];
+                    int j = candIdx[q >> 1];
+                    const PView& self = (q & 1) ? newV : oldV;
+                    double4_32a pj = a.s.pos[j];
+                    double3 r = imageVec(self.pos, mk(pj.x, pj.y, pj.z), box);
+                    if (!(dot3(r, r) > c.sqmaxcut)) {
+                        double4_32a dj = a.s.dir[j];
+                        const PairParam& pp = c.params[self.type * c.ntypes + (int)pj.w];
+                        keep = screenedOut(pp, r, self.dir, mk(dj.x, dj.y, dj.z)) ? 0 : 1;
+                        cls = pairClass(pp.kind);
+                        if (!keep) ++nScr;
+                    }
+                }
+                // one scan, three 10-bit counters: per-class offsets and totals
+                int total;
+                int off = blockExclusiveScan(keep ? (1 << (10 * cls)) : 0, total, sh.scan);
+                if (keep) {
+                    int base0 = cls == 0 ? qb0 : (cls == 1 ? qb1 : qb2);
+                    sh.queueB[cls][base0 + ((off >> (10 * cls)) & 1023)] = q;
+                }
+                qb0 += total & 1023;
+                qb1 += (total >> 10) & 1023;
+                qb2 += (total >> 20) & 1023;
+                if (qb0 > kClassCap - kMoveThreads || qb1 > kClassCap - kMoveThreads || qb2 > kClassCap - kMoveThreads) {
+                    flushC();
+                    nEval += qb0 + qb1 + qb2;
+                    qb0 = qb1 = qb2 = 0;
+                }
             }
         }
-        flush(qn);
-        nEval += qn + 2 * np;
+        flushC();
+        nEval += qb0 + qb1 + qb2 + 2 * np;
         nTested += (unsigned long long)nCand * (displace ? 2 : 1);
         blockSum2(eOld, eNew, sh.red);
         if (tid == 0) {
@@ -515,6 +708,10 @@ __global__ void __launch_bounds__(kMoveThreads) kColour(SweepArgs a, int phase) 
                 if (!displace) {
                     a.s.dir[t] = make_double4_32a(sh.ndir[0], sh.ndir[1], sh.ndir[2], od4.w);
                     a.s.patch[t] = sh.npatch;
+                } else {
+                    float4 nf = make_float4(newF.x, newF.y, newF.z, 0.0f);
+                    candPos[sh.st.ownOff + sh.slotR] = nf;
+                    a.cellPosF[a.cellStart[cell] + sh.slotR] = nf;
                 }
                 dECell += eNew - eOld;
                 if (displace) ++nAccT; else ++nAccR;
@@ -532,20 +729,22 @@ __global__ void __launch_bounds__(kMoveThreads) kColour(SweepArgs a, int phase) 
         atomicAdd(&a.counters[C_REJ_R], nRejR);
         atomicAdd(&a.counters[C_CELL_REJ], nCellRej);
         atomicAdd(&a.counters[C_MOVES], (unsigned long long)cnt);
+        atomicAdd(&a.counters[C_TESTED], nTested);
+        atomicAdd(&a.counters[C_EVAL], nEval);
     }
-    // per-thread pair counters
-    unsigned long long tested = tid == 0 ? nTested : 0ull, ev = tid == 0 ? nEval : 0ull;
-    if (tid == 0) {
-        atomicAdd(&a.counters[C_TESTED], tested);
-        atomicAdd(&a.counters[C_EVAL], ev);
-    }
+    if (nScr) atomicAdd(&a.counters[C_SCREENED], nScr);
 }
 
-// Adds the cells' energy changes of this sweep, in a fixed order.
-__global__ void kEndSweep(SweepArgs a) {
+// Adds the cells' energy changes of this sweep, in a fixed order, and clears them (a cell
+// without particles writes nothing during the sweep).
+__global__ void kEndSweep(const SweepArgs* __restrict__ A) {
+    const SweepArgs& a = A[blockIdx.y];
     __shared__ double ws[32];
     double v = 0.0;
-    for (int k = threadIdx.x; k < a.g.ncells; k += blockDim.x) v += a.cellDE[k];
+    for (int k = threadIdx.x; k < a.g.ncells; k += blockDim.x) {
+        v += a.cellDE[k];
+        a.cellDE[k] = 0.0;
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
@@ -558,58 +757,127 @@ __global__ void kEndSweep(SweepArgs a) {
     }
 }
 
-// Total energy over the cell list: thread i adds PairE(i, j, conlist(i)) for j < i
-// (allToAll's pair orientation, totalenergycalculator.h:502-521).
-__global__ void __launch_bounds__(kTotThreads) kTotalEnergy(SweepArgs a, int useTrialBox) {
-    __shared__ double ws[kTotThreads / 32];
+struct CellShared {
+    int list[kCellCap];
+    int queueA[kQueueCap];
+    int queueB[kQueueCap];
+    Stencil st;
+    Scan scan;
+    double red[kWarps][2];
+};
+
+// Total energy over the cell list, one CTA per cell: PairE(i, j, conlist(i)) for every
+// particle i of the cell and j < i (allToAll's pair orientation,
+// totalenergycalculator.h:502-521), with the same A/B/C stages as the move kernel.
+__global__ void __launch_bounds__(kMoveThreads) kCellEnergy(const SweepArgs* __restrict__ A, int useTrialBox) {
+    extern __shared__ float4 dynSmem[];
+    float4* candPos = dynSmem;
+    int* candIdx = reinterpret_cast<int*>(candPos + kCandCap);
+    __shared__ CellShared sh;
+    const SweepArgs& a = A[blockIdx.y];
     const Control& ctl = *a.ctl;
-    int i = blockIdx.x * kTotThreads + threadIdx.x;
-    double sum = 0.0;
-    bool run = i < a.s.n && (!useTrialBox || ctl.volValid);
-    if (run) {
-        DevCtx c;
-        c.params = a.t.params; c.mols = a.t.mols; c.ntypes = a.t.ntypes; c.n = a.s.n; c.sqmaxcut = a.t.sqmaxcut;
-        const double* bx = useTrialBox ? ctl.trialBox : a.s.box;
-        double3 box = mk(bx[0], bx[1], bx[2]);
-        const Grid& g = a.g;
-        PView v = viewAt(a.s, i);
+    const Grid& g = a.g;
+    const int cell = blockIdx.x;
+    const int tid = threadIdx.x;
+    if (cell >= g.ncells) return;
+    if (useTrialBox && !ctl.volValid) {
+        if (tid == 0) a.partial[cell] = 0.0;
+        return;
+    }
+    int cnt = a.cellCount[cell];
+    if (cnt == 0 || cnt > kCellCap) {
+        if (tid == 0) a.partial[cell] = 0.0;
+        return;
+    }
+    int cx = cell % g.nc[0], cy = (cell / g.nc[0]) % g.nc[1], cz = cell / (g.nc[0] * g.nc[1]);
+    for (int k = tid; k < cnt; k += kMoveThreads) sh.list[k] = a.cellIdx[a.cellStart[cell] + k];
+    stageCandidates(a, cx, cy, cz, sh.st, sh.scan, candIdx, candPos);
+    if (sh.st.overflow) {
+        if (tid == 0) a.partial[cell] = 0.0;
+        return;
+    }
+    const int nCand = sh.st.nCand, ownOff = sh.st.ownOff;
+    DevCtx c;
+    c.params = a.t.params; c.mols = a.t.mols; c.ntypes = a.t.ntypes; c.n = a.s.n; c.sqmaxcut = a.t.sqmaxcut;
+    const double* bx = useTrialBox ? ctl.trialBox : a.s.box;
+    const double3 box = mk(bx[0], bx[1], bx[2]);
+    const float thr32 = candThreshold(c.sqmaxcut, box);
+    double sum = 0.0, unused = 0.0;
+    // bonded partners j < i, whatever the distance
+    for (int k = tid; k < cnt; k += kMoveThreads) {
+        int i = sh.list[k];
         Con con = makeCon(c, i, a.s.mol[i]);
+        PView vi = viewAt(a.s, i);
         for (int q = 0; q < 4; ++q) {
             int j = con.idx[q];
             if (j >= 0 && j < i) {
                 unsigned bb; double dd;
-                sum += pairEnergy(c, v, viewAt(a.s, j), con, box, &bb, &dd);
+                sum += pairEnergy(c, vi, viewAt(a.s, j), con, box, &bb, &dd);
             }
         }
-        int cell = a.cellOf[i];
-        int cx = cell % g.nc[0], cy = (cell / g.nc[0]) % g.nc[1], cz = cell / (g.nc[0] * g.nc[1]);
-        int offx[3], offy[3], offz[3];
-        int nx = neighbourOffsets(g.nc[0], offx), ny = neighbourOffsets(g.nc[1], offy), nz = neighbourOffsets(g.nc[2], offz);
-        for (int qz = 0; qz < nz; ++qz)
-            for (int qy = 0; qy < ny; ++qy)
-                for (int qx = 0; qx < nx; ++qx) {
-                    int x = (cx + offx[qx] + g.nc[0]) % g.nc[0];
-                    int y = (cy + offy[qy] + g.nc[1]) % g.nc[1];
-                    int z = (cz + offz[qz] + g.nc[2]) % g.nc[2];
-                    int c2 = (z * g.nc[1] + y) * g.nc[0] + x;
-                    int s2 = a.cellStart[c2], n2 = a.cellCount[c2];
-                    for (int k = 0; k < n2; ++k) {
-                        int j = a.cellIdx[s2 + k];
-                        if (j >= i || j == con.idx[0] || j == con.idx[1] || j == con.idx[2] || j == con.idx[3]) continue;
-                        unsigned bb; double dd;
-                        sum += pairEnergy(c, v, viewAt(a.s, j), con, box, &bb, &dd);
+    }
+    const long total = (long)cnt * nCand;
+    int qb = 0;
+    auto flushC = [&](int count) {
+        __syncthreads();                   // queue entries of every thread are visible
+        for (int e = tid; e < count; e += kMoveThreads) {
+            int q = sh.queueB[e];
+            int i = sh.list[q / nCand], j = candIdx[q % nCand];
+            Con con = makeCon(c, i, a.s.mol[i]);
+            unsigned bb; double dd;
+            sum += pairEnergy(c, viewAt(a.s, i), viewAt(a.s, j), con, box, &bb, &dd);
+        }
+        __syncthreads();
+    };
+    for (long base = 0; base < total; base += kChunk) {
+        int qa = 0;
+        long end = min(base + (long)kChunk, total);
+        for (long r0 = base; r0 < end; r0 += kMoveThreads) {
+            long q = r0 + tid;
+            int keep = 0;
+            if (q < end) {
+                int li = (int)(q / nCand), k = (int)(q % nCand);
+                int i = sh.list[li], j = candIdx[k];
+                if (j < i) {
+                    float4 pi = candPos[ownOff + li];
+                    keep = dist2f(candPos[k], make_float3(pi.x, pi.y, pi.z), box) <= thr32;
+                }
+            }
+            int tot;
+            int off = blockExclusiveScan(keep, tot, sh.scan);
+            if (keep) sh.queueA[qa + off] = (int)q;
+            qa += tot;
+        }
+        __syncthreads();
+        for (int e0 = 0; e0 < qa; e0 += kMoveThreads) {
+            int e = e0 + tid;
+            int keep = 0, q = 0;
+            if (e < qa) {
+                q = sh.queueA[e];
+                int i = sh.list[q / nCand], j = candIdx[q % nCand];
+                int4 mi = a.s.mol[i];
+                Con con = makeCon(c, i, mi);
+                bool partner = (j == con.idx[0] || j == con.idx[1] || j == con.idx[2] || j == con.idx[3]);
+                if (!partner) {
+                    double4_32a pi = a.s.pos[i], pj = a.s.pos[j];
+                    double3 r = imageVec(mk(pi.x, pi.y, pi.z), mk(pj.x, pj.y, pj.z), box);
+                    if (!(dot3(r, r) > c.sqmaxcut)) {
+                        double4_32a di = a.s.dir[i], dj = a.s.dir[j];
+                        const PairParam& pp = c.params[(int)pi.w * c.ntypes + (int)pj.w];
+                        keep = screenedOut(pp, r, mk(di.x, di.y, di.z), mk(dj.x, dj.y, dj.z)) ? 0 : 1;
                     }
                 }
+            }
+            int tot;
+            int off = blockExclusiveScan(keep, tot, sh.scan);
+            if (keep) sh.queueB[qb + off] = q;
+            qb += tot;
+            if (qb > kQueueCap - kMoveThreads) { flushC(qb); qb = 0; }
+        }
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
-    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = sum;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double s = 0.0;
-        for (int q = 0; q < kTotThreads / 32; ++q) s += ws[q];
-        a.partial[blockIdx.x] = s;
-    }
+    flushC(qb);
+    blockSum2(sum, unused, sh.red);
+    if (tid == 0) a.partial[cell] = sum;
 }
 
 __device__ double sumPartials(const double* p, int n) {
@@ -619,7 +887,8 @@ __device__ double sumPartials(const double* p, int n) {
 }
 
 // MoveCreator::pressureMove, ptype 1 (movecreator.cpp:390-421), decided on the device.
-__global__ void kVolumeAccept(SweepArgs a, int nblocks) {
+__global__ void kVolumeAccept(const SweepArgs* __restrict__ A) {
+    const SweepArgs& a = A[blockIdx.y];
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     Control& c = *a.ctl;
     if (!c.volValid) {
@@ -627,7 +896,7 @@ __global__ void kVolumeAccept(SweepArgs a, int nblocks) {
         atomicAdd(&a.counters[C_REJ_V], 1ull);
         return;
     }
-    double eNew = sumPartials(a.partial, nblocks);
+    double eNew = sumPartials(a.partial, a.g.ncells);
     double pvol = a.s.box[0] * a.s.box[1] * a.s.box[2];
     double pvoln = c.trialBox[0] * c.trialBox[1] * c.trialBox[2];
     double enermove = a.press * (pvoln - pvol) - (double)a.s.n * a.temper * log(pvoln / pvol);
@@ -645,39 +914,113 @@ __global__ void kVolumeAccept(SweepArgs a, int nblocks) {
     }
 }
 
-__global__ void kSetEnergy(SweepArgs a, int nblocks) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) a.ctl->energy = sumPartials(a.partial, nblocks);
+__global__ void kSetEnergy(const SweepArgs* __restrict__ A) {
+    const SweepArgs& a = A[blockIdx.y];
+    if (threadIdx.x == 0 && blockIdx.x == 0) a.ctl->energy = sumPartials(a.partial, a.g.ncells);
 }
 
-__global__ void kCheckEnergy(SweepArgs a, int nblocks) {
+__global__ void kCheckEnergy(const SweepArgs* __restrict__ A) {
+    const SweepArgs& a = A[blockIdx.y];
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    double e = sumPartials(a.partial, nblocks);
+    double e = sumPartials(a.partial, a.g.ncells);
     Control& c = *a.ctl;
     c.energyCheck = e;
     double d = fabs(c.energy - e);
     if (d > c.maxDrift) c.maxDrift = d;
 }
 
+
+// Replica exchange (MoveCreator::replicaExchangeMove, scOOP/mc/movecreator.cpp:552-795,
+// there over MPI): within each ladder the even and the odd neighbour pairs of the
+// temperature ladder are tried alternately; a swap of temperatures between the replica
+// at rank k (colder) and the one at rank k+1 is accepted with
+// min(1, exp((1/T_k - 1/T_k+1)(E_k - E_k+1) + (P_k/T_k - P_k+1/T_k+1)(V_k - V_k+1))),
+// the canonical plus isobaric rule of the reference (the pressure term vanishes in NVT).
+__global__ void kExchange(SweepArgs* A, int* ladder, const int* ladderStart, int nLadders, uint64_t seed,
+                          unsigned long long* ctr) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    unsigned long long ev = ctr[0]++;
+    int parity = (int)(ev & 1ull);
+    Stream r(seed, 0xFFFFFFE0u, (uint32_t)ev, (uint32_t)(ev >> 32));
+    for (int g = 0; g < nLadders; ++g) {
+        int s0 = ladderStart[g], s1 = ladderStart[g + 1];
+        for (int k = s0 + parity; k + 1 < s1; k += 2) {
+            int ri = ladder[k], rj = ladder[k + 1];
+            double Ti = A[ri].temper, Tj = A[rj].temper;
+            double Ei = A[ri].ctl->energy, Ej = A[rj].ctl->energy;
+            const double* bi = A[ri].s.box;
+            const double* bj = A[rj].s.box;
+            double Vi = bi[0] * bi[1] * bi[2], Vj = bj[0] * bj[1] * bj[2];
+            // canonical and isobaric terms of movecreator.cpp:721-727
+            double delta = (1.0 / Ti - 1.0 / Tj) * (Ei - Ej);
+            delta += (A[ri].press / Ti - A[rj].press / Tj) * (Vi - Vj);
+            double u = r.next();
+            ctr[1 + 2 * k] += 1ull;
+            if (delta >= 0.0 || exp(delta) > u) {
+                A[ri].temper = Tj;
+                A[rj].temper = Ti;
+                ladder[k] = rj;
+                ladder[k + 1] = ri;
+                ctr[2 + 2 * k] += 1ull;
+            }
+        }
+    }
+}
+
 }  // namespace
 
+// Device state of the move loop of one system.
 struct SweepEngine {
     Grid g{};
     Control* ctl = nullptr;
     int *cellStart = nullptr, *cellCount = nullptr, *cellCursor = nullptr, *cellIdx = nullptr, *cellOf = nullptr;
+    float4* cellPosF = nullptr;
     double* cellDE = nullptr;
     double* partial = nullptr;
     unsigned long long* counters = nullptr;
     int* err = nullptr;
     int ncellsAlloc = 0;
-    int nTotBlocks = 0;
     std::vector<void*> allocs;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr, evP0 = nullptr, evP1 = nullptr;
-    cudaGraphExec_t graphExec = nullptr;
-    SweepArgs graphArgs{};
-    long graphBlock = 0, graphLaunches = 0, graphPhaseLaunches = 0;
     bool energyKnown = false;
-    uint64_t seed = 0;
-    long launches = 0;
+    uint64_t seed = ~0ull;
+    int stencil = 0;
+    double margin = 0.0;
+    SweepArgs args{};
+};
+
+// A set of systems moved together: one launch sequence per sweep, blockIdx.y = system.
+struct Batch {
+    std::vector<Context*> sys;
+    std::vector<SweepArgs> hArgs;
+    SweepArgs* dArgs = nullptr;
+    int nArgsAlloc = 0;
+    int maxN = 0, maxCells = 0, maxActive = 0, maxColours = 0;
+    cudaStream_t stream = nullptr;
+    int device = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, evP0 = nullptr, evP1 = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    int graphDims[6] = {0, 0, 0, 0, 0, 0};
+    long graphLaunches = 0, graphPhaseLaunches = 0;
+    // parallel tempering
+    int* dLadder = nullptr;
+    int* dLadderStart = nullptr;
+    int nLadders = 0;
+    unsigned long long* dExCtr = nullptr;
+    std::vector<void*> allocs;
+
+    ~Batch() {
+        cudaSetDevice(device);
+        for (void* p : allocs) cudaFree(p);
+        for (cudaEvent_t e : {ev0, ev1, evP0, evP1})
+            if (e) cudaEventDestroy(e);
+        if (graph) cudaGraphExecDestroy(graph);
+    }
+    int alloc(void** p, size_t bytes) {
+        cudaError_t r = cudaMalloc(p, bytes ? bytes : 16);
+        if (r != cudaSuccess) return cudaFail(r, "cudaMalloc (batch)");
+        allocs.push_back(*p);
+        return SC_OK;
+    }
 };
 
 static int engineAlloc(SweepEngine* e, void** p, size_t bytes) {
@@ -687,17 +1030,29 @@ static int engineAlloc(SweepEngine* e, void** p, size_t bytes) {
     return SC_OK;
 }
 
-// Cell grid for a box: cells at least maxcut*(1+margin) wide, an even count per dimension
-// (or 1 / 2), so that the 2x2x2 colouring keeps same-colour cells apart.
-static Grid makeGrid(const double* box, double maxcut, double margin) {
+// Cell grid for a box.  With reach s the cells are >= maxcut*(1+margin)/s wide and the
+// count per dimension is a multiple of the colour period s+1 (and > 2s, so that the
+// stencil cells are distinct); dimensions too small for that fall back to reach 1 with
+// an even count (or 1 / 2 cells).
+static Grid makeGrid(const double* box, double maxcut, double margin, int sReq) {
     Grid g{};
     g.maxcut = maxcut;
     for (int d = 0; d < 3; ++d) {
-        int nc = (int)std::floor(box[d] / (maxcut * (1.0 + margin)));
-        if (nc < 1) nc = 1;
-        if (nc >= 3 && (nc & 1)) nc -= 1;
-        g.nc[d] = nc;
-        g.p[d] = nc >= 2 ? 2 : 1;
+        bool ok = false;
+        if (sReq >= 2) {
+            int p = sReq + 1;
+            int nc = (int)std::floor(box[d] / (maxcut * (1.0 + margin) / sReq));
+            nc -= nc % p;
+            if (nc > 2 * sReq) { g.nc[d] = nc; g.p[d] = p; g.s[d] = sReq; ok = true; }
+        }
+        if (!ok) {
+            int nc = (int)std::floor(box[d] / (maxcut * (1.0 + margin)));
+            if (nc < 1) nc = 1;
+            if (nc >= 3 && (nc & 1)) nc -= 1;
+            g.nc[d] = nc;
+            g.p[d] = nc >= 2 ? 2 : 1;
+            g.s[d] = 1;
+        }
     }
     g.ncells = g.nc[0] * g.nc[1] * g.nc[2];
     g.nactive = (g.nc[0] / g.p[0]) * (g.nc[1] / g.p[1]) * (g.nc[2] / g.p[2]);
@@ -705,22 +1060,33 @@ static Grid makeGrid(const double* box, double maxcut, double margin) {
     return g;
 }
 
+// Stencil reach: 2 (cells of maxcut/2, 27 colours) when the box holds at least 6 such
+// cells per dimension, else 1.
+static int chooseStencil(const double* box, double maxcut, int requested) {
+    if (requested >= 1 && requested <= 3) return requested;
+    double lim = std::min(box[0], std::min(box[1], box[2]));
+    return lim / (maxcut / 2.0) >= 6.0 ? 2 : 1;
+}
+
 void destroyEngine(Context* c) {
+    if (c->batch) {
+        delete c->batch;
+        c->batch = nullptr;
+    }
     SweepEngine* e = c->engine;
     if (!e) return;
     cudaSetDevice(c->device);
     for (void* p : e->allocs) cudaFree(p);
-    for (cudaEvent_t ev : {e->ev0, e->ev1, e->evP0, e->evP1})
-        if (ev) cudaEventDestroy(ev);
-    if (e->graphExec) cudaGraphExecDestroy(e->graphExec);
     delete e;
     c->engine = nullptr;
 }
 
-static int ensureGrid(Context* c, SweepEngine* e, const double* box, double margin) {
-    Grid g = makeGrid(box, c->topo.maxcut, margin);
+static int ensureGrid(Context* c, SweepEngine* e, const double* box) {
+    Grid g = makeGrid(box, c->topo.maxcut, e->margin, e->stencil);
+    if (g.ncolours > kMaxColours) return fail(SC_ERR_RANGE, "too many colour classes");
     if (g.ncells > e->ncellsAlloc) {
-        for (void** p : {(void**)&e->cellStart, (void**)&e->cellCount, (void**)&e->cellCursor, (void**)&e->cellDE}) {
+        for (void** p : {(void**)&e->cellStart, (void**)&e->cellCount, (void**)&e->cellCursor, (void**)&e->cellDE,
+                         (void**)&e->partial}) {
             if (*p) {
                 cudaFree(*p);
                 e->allocs.erase(std::find(e->allocs.begin(), e->allocs.end(), *p));
@@ -733,21 +1099,24 @@ static int ensureGrid(Context* c, SweepEngine* e, const double* box, double marg
         if ((rc = engineAlloc(e, (void**)&e->cellCount, sizeof(int) * n))) return rc;
         if ((rc = engineAlloc(e, (void**)&e->cellCursor, sizeof(int) * n))) return rc;
         if ((rc = engineAlloc(e, (void**)&e->cellDE, sizeof(double) * n))) return rc;
+        if ((rc = engineAlloc(e, (void**)&e->partial, sizeof(double) * n))) return rc;
+        cudaMemset(e->cellDE, 0, sizeof(double) * n);
         e->ncellsAlloc = n;
     }
     e->g = g;
     return SC_OK;
 }
 
-static SweepArgs makeArgs(Context* c, SweepEngine* e, const sc_run_params& p) {
-    SweepArgs a;
+static void fillArgs(Context* c, SweepEngine* e, const sc_run_params& p) {
+    SweepArgs& a = e->args;
     std::memset(&a, 0, sizeof a);
     a.s = c->d;
     a.t = c->tables;
     a.g = e->g;
     a.ctl = e->ctl;
     a.cellStart = e->cellStart; a.cellCount = e->cellCount; a.cellCursor = e->cellCursor;
-    a.cellIdx = e->cellIdx; a.cellOf = e->cellOf; a.cellDE = e->cellDE; a.partial = e->partial;
+    a.cellIdx = e->cellIdx; a.cellPosF = e->cellPosF; a.cellOf = e->cellOf; a.cellDE = e->cellDE;
+    a.partial = e->partial;
     a.counters = e->counters; a.err = e->err;
     a.seed = p.seed;
     a.temper = p.temper;
@@ -762,46 +1131,25 @@ static SweepArgs makeArgs(Context* c, SweepEngine* e, const sc_run_params& p) {
         a.trans[k] = (base > 0 && perType != base) ? perType * (p.transmx / base) : p.transmx;
         a.geo[k] = c->topo.ia[t][t].geotype[0];
     }
-    return a;
 }
 
-// Cell list for the current positions and control block.
-static cudaError_t launchCells(const SweepArgs& a, cudaStream_t st, long& launches) {
-    int n = a.s.n;
-    cudaError_t r = cudaMemsetAsync(a.cellCount, 0, sizeof(int) * a.g.ncells, st);
-    if (r != cudaSuccess) return r;
-    kAssign<<<(n + 255) / 256, 256, 0, st>>>(a);
-    kScan<<<1, 1024, 0, st>>>(a);
-    kScatter<<<(n + 255) / 256, 256, 0, st>>>(a);
-    kSortCells<<<(a.g.ncells + 127) / 128, 128, 0, st>>>(a);
-    launches += 4;
-    return cudaGetLastError();
-}
-
-int runSweeps(Context* c, const sc_run_params& p, sc_run_stats& st) {
-    std::memset(&st, 0, sizeof st);
-    if (p.nsweeps < 0) return fail(SC_ERR_ARG, "nsweeps must be >= 0");
-    if (!(p.temper > 0)) return fail(SC_ERR_ARG, "temper must be positive");
-    if (p.ptype != 0 && p.ptype != 1) return fail(SC_ERR_UNSUPPORTED, "only ptype 1 (isotropic) volume moves run on the GPU");
+// Device state, grid and arguments of one system for a run with parameters p.
+static int prepareSystem(Context* c, const sc_run_params& p, bool npt) {
+    const bool hostChanged = c->hostNewer;    // the running energy must be recomputed
     int rc = c->ensureDevice();
     if (rc) return rc;
-    if (c->d.n == 0) return SC_OK;
+    if (hostChanged && c->engine) c->engine->energyKnown = false;
     int n = c->d.n;
     SweepEngine* e = c->engine;
     if (!e) {
         e = new SweepEngine();
         c->engine = e;
         if ((rc = engineAlloc(e, (void**)&e->ctl, sizeof(Control)))) return rc;
-        if ((rc = engineAlloc(e, (void**)&e->cellIdx, sizeof(int) * n))) return rc;
-        if ((rc = engineAlloc(e, (void**)&e->cellOf, sizeof(int) * n))) return rc;
-        e->nTotBlocks = (n + kTotThreads - 1) / kTotThreads;
-        if ((rc = engineAlloc(e, (void**)&e->partial, sizeof(double) * e->nTotBlocks))) return rc;
+        if ((rc = engineAlloc(e, (void**)&e->cellIdx, sizeof(int) * std::max(n, 1)))) return rc;
+        if ((rc = engineAlloc(e, (void**)&e->cellPosF, sizeof(float4) * std::max(n, 1)))) return rc;
+        if ((rc = engineAlloc(e, (void**)&e->cellOf, sizeof(int) * std::max(n, 1)))) return rc;
         if ((rc = engineAlloc(e, (void**)&e->counters, sizeof(unsigned long long) * C_COUNT))) return rc;
         if ((rc = engineAlloc(e, (void**)&e->err, sizeof(int)))) return rc;
-        cudaEventCreate(&e->ev0);
-        cudaEventCreate(&e->ev1);
-        cudaEventCreate(&e->evP0);
-        cudaEventCreate(&e->evP1);
         Control z;
         std::memset(&z, 0, sizeof z);
         cudaMemcpy(e->ctl, &z, sizeof z, cudaMemcpyHostToDevice);
@@ -812,127 +1160,46 @@ int runSweeps(Context* c, const sc_run_params& p, sc_run_stats& st) {
         cudaMemcpy(&e->ctl->sweep, &zero, sizeof zero, cudaMemcpyHostToDevice);
         e->seed = p.seed;
     }
-    cudaStream_t s = c->stream;
-    cudaMemsetAsync(e->counters, 0, sizeof(unsigned long long) * C_COUNT, s);
-    cudaMemsetAsync(e->err, 0, sizeof(int), s);
-    cudaMemsetAsync(&e->ctl->maxDrift, 0, sizeof(double), s);
     double box[3];
-    cudaMemcpyAsync(box, c->d.box, sizeof box, cudaMemcpyDeviceToHost, s);
-    cudaStreamSynchronize(s);
-    const bool npt = p.ptype == 1 && p.volume_every > 0;
-    const double margin = npt ? 0.03 : 1e-9;
-    if ((rc = ensureGrid(c, e, box, margin))) return rc;
-    SweepArgs a = makeArgs(c, e, p);
-    long launches = 0;
-    cudaError_t r;
-    // exact starting energy (Updater::simulate calls initEM + allToAll, updater.cpp:128-131)
-    if (!e->energyKnown || c->hostNewer) {
-        kBeginSweep<<<1, 32, 0, s>>>(a, 0);
-        if ((r = launchCells(a, s, launches)) != cudaSuccess) return cudaFail(r, "cell list");
-        kTotalEnergy<<<e->nTotBlocks, kTotThreads, 0, s>>>(a, 0);
-        kSetEnergy<<<1, 32, 0, s>>>(a, e->nTotBlocks);
-        e->energyKnown = true;
+    cudaMemcpy(box, c->d.box, sizeof box, cudaMemcpyDeviceToHost);
+    e->margin = npt ? 0.03 : 1e-9;
+    e->stencil = chooseStencil(box, c->topo.maxcut, p.stencil);
+    if ((rc = ensureGrid(c, e, box))) return rc;
+    fillArgs(c, e, p);
+    cudaMemset(e->counters, 0, sizeof(unsigned long long) * C_COUNT);
+    cudaMemset(e->err, 0, sizeof(int));
+    cudaMemset(&e->ctl->maxDrift, 0, sizeof(double));
+    return SC_OK;
+}
+
+static int uploadArgs(Batch& b) {
+    int ns = (int)b.sys.size();
+    if (ns > b.nArgsAlloc) {
+        int rc = b.alloc((void**)&b.dArgs, sizeof(SweepArgs) * ns);
+        if (rc) return rc;
+        b.nArgsAlloc = ns;
     }
-    cudaEventRecord(e->ev0, s);
-    const long chunk = 48;
-    double phaseMs = 0.0;
-    long phaseLaunches = 0;
-    // one sweep: control block, cell list, the colour phases, energy bookkeeping, volume move
-    auto launchOne = [&](bool volDue, bool timing) -> cudaError_t {
-        kBeginSweep<<<1, 32, 0, s>>>(a, volDue ? 1 : 0);
-        cudaError_t r2 = launchCells(a, s, launches);
-        if (r2 != cudaSuccess) return r2;
-        if (timing) cudaEventRecord(e->evP0, s);
-        for (int ph = 0; ph < a.g.ncolours; ++ph) kColour<<<a.g.nactive, kMoveThreads, 0, s>>>(a, ph);
-        if (timing) {
-            cudaEventRecord(e->evP1, s);
-            cudaEventSynchronize(e->evP1);
-            float pms = 0;
-            cudaEventElapsedTime(&pms, e->evP0, e->evP1);
-            phaseMs += pms;
-        }
-        phaseLaunches += a.g.ncolours;
-        kEndSweep<<<1, 256, 0, s>>>(a);
-        launches += 2 + a.g.ncolours;
-        if (volDue) {
-            kTotalEnergy<<<e->nTotBlocks, kTotThreads, 0, s>>>(a, 1);
-            kVolumeAccept<<<1, 32, 0, s>>>(a, e->nTotBlocks);
-            launches += 2;
-        }
-        return cudaGetLastError();
-    };
-    // Blocks of G sweeps are captured once into a CUDA graph and replayed: the kernels
-    // read everything that changes from sweep to sweep (sweep index, grid offset, colour
-    // order, box, energy) from the device control block.
-    const int ve = npt ? p.volume_every : 1;
-    const long G = (long)ve * std::max(1, (8 + ve - 1) / ve);
-    const bool useGraph = !p.time_phases;
-    long nextCheck = p.check_every > 0 ? p.check_every : -1;
-    long nextRegrid = npt ? chunk : -1;
-    long sw = 0;
-    while (sw < p.nsweeps) {
-        long left = p.nsweeps - sw;
-        if (useGraph && left >= G && sw % G == 0) {
-            if (!e->graphExec || std::memcmp(&e->graphArgs, &a, sizeof a) != 0 || e->graphBlock != G) {
-                if (e->graphExec) { cudaGraphExecDestroy(e->graphExec); e->graphExec = nullptr; }
-                cudaGraph_t graph;
-                long before = launches, beforeP = phaseLaunches;
-                if ((r = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return cudaFail(r, "graph capture");
-                for (long k = 0; k < G; ++k) {
-                    cudaError_t r2 = launchOne(npt && ((k + 1) % ve == 0), false);
-                    if (r2 != cudaSuccess) { cudaStreamEndCapture(s, &graph); return cudaFail(r2, "graph capture launch"); }
-                }
-                if ((r = cudaStreamEndCapture(s, &graph)) != cudaSuccess) return cudaFail(r, "graph capture end");
-                r = cudaGraphInstantiate(&e->graphExec, graph, 0);
-                cudaGraphDestroy(graph);
-                if (r != cudaSuccess) return cudaFail(r, "graph instantiate");
-                e->graphLaunches = launches - before;
-                e->graphPhaseLaunches = phaseLaunches - beforeP;
-                launches = before;
-                phaseLaunches = beforeP;
-                e->graphArgs = a;
-                e->graphBlock = G;
-            }
-            if ((r = cudaGraphLaunch(e->graphExec, s)) != cudaSuccess) return cudaFail(r, "graph launch");
-            launches += e->graphLaunches;
-            phaseLaunches += e->graphPhaseLaunches;
-            sw += G;
-        } else {
-            if ((r = launchOne(npt && ((sw + 1) % ve == 0), p.time_phases != 0)) != cudaSuccess) return cudaFail(r, "sweep launch");
-            sw += 1;
-        }
-        if (nextCheck > 0 && sw >= nextCheck) {
-            // the cell list (box fractions) stays valid after an accepted volume move
-            kTotalEnergy<<<e->nTotBlocks, kTotThreads, 0, s>>>(a, 0);
-            kCheckEnergy<<<1, 32, 0, s>>>(a, e->nTotBlocks);
-            launches += 2;
-            while (nextCheck <= sw) nextCheck += p.check_every;
-        }
-        if (nextRegrid > 0 && sw >= nextRegrid && sw < p.nsweeps) {
-            // the box changed on the device: re-derive the cell grid when needed
-            while (nextRegrid <= sw) nextRegrid += chunk;
-            cudaMemcpyAsync(box, c->d.box, sizeof box, cudaMemcpyDeviceToHost, s);
-            if ((r = cudaStreamSynchronize(s)) != cudaSuccess) return cudaFail(r, "sweep");
-            Grid ng = makeGrid(box, c->topo.maxcut, margin);
-            if (ng.nc[0] != a.g.nc[0] || ng.nc[1] != a.g.nc[1] || ng.nc[2] != a.g.nc[2]) {
-                if ((rc = ensureGrid(c, e, box, margin))) return rc;
-                a = makeArgs(c, e, p);
-            }
-        }
-        if ((r = cudaGetLastError()) != cudaSuccess) return cudaFail(r, "sweep launch");
+    b.hArgs.resize(ns);
+    b.maxN = b.maxCells = b.maxActive = b.maxColours = 0;
+    for (int k = 0; k < ns; ++k) {
+        b.hArgs[k] = b.sys[k]->engine->args;
+        b.maxN = std::max(b.maxN, b.hArgs[k].s.n);
+        b.maxCells = std::max(b.maxCells, b.hArgs[k].g.ncells);
+        b.maxActive = std::max(b.maxActive, b.hArgs[k].g.nactive);
+        b.maxColours = std::max(b.maxColours, b.hArgs[k].g.ncolours);
     }
-    cudaEventRecord(e->ev1, s);
-    if ((r = cudaStreamSynchronize(s)) != cudaSuccess) return cudaFail(r, "sweep");
-    float ms = 0;
-    cudaEventElapsedTime(&ms, e->ev0, e->ev1);
+    cudaError_t r = cudaMemcpy(b.dArgs, b.hArgs.data(), sizeof(SweepArgs) * ns, cudaMemcpyHostToDevice);
+    if (r != cudaSuccess) return cudaFail(r, "upload sweep arguments");
+    return SC_OK;
+}
+
+// Counters / statistics of one system after a run.
+static void collectStats(Context* c, sc_run_stats& st) {
+    SweepEngine* e = c->engine;
     unsigned long long ctr[C_COUNT];
     Control hc;
-    int err = 0;
     cudaMemcpy(ctr, e->counters, sizeof ctr, cudaMemcpyDeviceToHost);
     cudaMemcpy(&hc, e->ctl, sizeof hc, cudaMemcpyDeviceToHost);
-    cudaMemcpy(&err, e->err, sizeof err, cudaMemcpyDeviceToHost);
-    c->devNewer = true;
-    st.sweeps = p.nsweeps;
     st.moves = (long)ctr[C_MOVES];
     st.acc_trans = (long)ctr[C_ACC_T]; st.rej_trans = (long)ctr[C_REJ_T];
     st.acc_rot = (long)ctr[C_ACC_R]; st.rej_rot = (long)ctr[C_REJ_R];
@@ -942,13 +1209,343 @@ int runSweeps(Context* c, const sc_run_params& p, sc_run_stats& st) {
     st.energy = hc.energy;
     st.energy_check = hc.energyCheck;
     st.max_drift = hc.maxDrift;
-    st.seconds = ms * 1e-3;
-    st.phase_seconds = phaseMs * 1e-3;
-    st.phase_launches = phaseLaunches;
-    st.launches = launches;
-    c->lastLaunches = launches;
+}
+
+static int systemErrors(Context* c) {
+    int err = 0;
+    cudaMemcpy(&err, c->engine->err, sizeof err, cudaMemcpyDeviceToHost);
     if (err & E_CELL_OVERFLOW) return fail(SC_ERR_DEVICE, "a cell holds more than 256 particles (density too high for the cell list)");
-    if (err & E_PARTNER_FAR) return fail(SC_ERR_DEVICE, "a bonded partner lies beyond the neighbouring cells (bond longer than maxcut)");
+    if (err & E_CAND_OVERFLOW) return fail(SC_ERR_DEVICE, "a cell stencil holds more than 4096 particles (use a smaller stencil)");
+    if (err & E_PARTNER_FAR) return fail(SC_ERR_DEVICE, "a bonded partner lies beyond the cell stencil (bond longer than maxcut)");
+    return SC_OK;
+}
+
+struct RunOut {
+    double seconds = 0, phaseSeconds = 0;
+    long launches = 0, phaseLaunches = 0;
+};
+
+// Runs nsweeps sweeps of every system of the batch; with exchangeEvery > 0 a replica
+// exchange follows every exchangeEvery sweeps.
+static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchangeEvery, uint64_t exSeed, RunOut& out) {
+    const int ns = (int)b.sys.size();
+    const bool npt = p.ptype == 1 && p.volume_every > 0;
+    cudaStream_t s = b.stream;
+    cudaError_t r;
+    int rc;
+    long launches = 0;
+    double phaseMs = 0;
+    long phaseLaunches = 0;
+    if (!b.ev0) {
+        cudaEventCreate(&b.ev0); cudaEventCreate(&b.ev1); cudaEventCreate(&b.evP0); cudaEventCreate(&b.evP1);
+    }
+    static bool attrSet = false;
+    if (!attrSet) {
+        if ((r = cudaFuncSetAttribute(kColour, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDynSmem)) != cudaSuccess)
+            return cudaFail(r, "shared memory attribute");
+        if ((r = cudaFuncSetAttribute(kCellEnergy, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDynSmem)) != cudaSuccess)
+            return cudaFail(r, "shared memory attribute");
+        attrSet = true;
+    }
+    auto dims = [&](int x) { return dim3((unsigned)std::max(1, x), (unsigned)ns); };
+    auto launchCells = [&]() -> cudaError_t {
+        kZeroCounts<<<dims((b.maxCells + 255) / 256), 256, 0, s>>>(b.dArgs);
+        kAssign<<<dims((b.maxN + 255) / 256), 256, 0, s>>>(b.dArgs);
+        kScan<<<dims(1), 1024, 0, s>>>(b.dArgs);
+        kScatter<<<dims((b.maxN + 255) / 256), 256, 0, s>>>(b.dArgs);
+        kSortCells<<<dims((b.maxCells + 127) / 128), 128, 0, s>>>(b.dArgs);
+        launches += 5;
+        return cudaGetLastError();
+    };
+    auto exactEnergy = [&](bool check) -> cudaError_t {
+        kCellEnergy<<<dims(b.maxCells), kMoveThreads, kDynSmem, s>>>(b.dArgs, 0);
+        if (check) kCheckEnergy<<<dims(1), 32, 0, s>>>(b.dArgs);
+        else kSetEnergy<<<dims(1), 32, 0, s>>>(b.dArgs);
+        launches += 2;
+        return cudaGetLastError();
+    };
+    // exact starting energy (Updater::simulate calls initEM + allToAll, updater.cpp:128-131)
+    bool need = false;
+    for (Context* c : b.sys) need |= (!c->engine->energyKnown || c->hostNewer);
+    if (need) {
+        kBeginSweep<<<dims(1), 32, 0, s>>>(b.dArgs, 0);
+        if ((r = launchCells()) != cudaSuccess) return cudaFail(r, "cell list");
+        if ((r = exactEnergy(false)) != cudaSuccess) return cudaFail(r, "energy");
+        launches += 1;
+        for (Context* c : b.sys) c->engine->energyKnown = true;
+    }
+    auto launchOne = [&](bool volDue, bool timing) -> cudaError_t {
+        kBeginSweep<<<dims(1), 32, 0, s>>>(b.dArgs, volDue ? 1 : 0);
+        cudaError_t r2 = launchCells();
+        if (r2 != cudaSuccess) return r2;
+        if (timing) cudaEventRecord(b.evP0, s);
+        for (int ph = 0; ph < b.maxColours; ++ph) kColour<<<dims(b.maxActive), kMoveThreads, kDynSmem, s>>>(b.dArgs, ph);
+        if (timing) {
+            cudaEventRecord(b.evP1, s);
+            cudaEventSynchronize(b.evP1);
+            float pms = 0;
+            cudaEventElapsedTime(&pms, b.evP0, b.evP1);
+            phaseMs += pms;
+        }
+        phaseLaunches += b.maxColours;
+        kEndSweep<<<dims(1), 256, 0, s>>>(b.dArgs);
+        launches += 2 + b.maxColours;
+        if (volDue) {
+            kCellEnergy<<<dims(b.maxCells), kMoveThreads, kDynSmem, s>>>(b.dArgs, 1);
+            kVolumeAccept<<<dims(1), 32, 0, s>>>(b.dArgs);
+            launches += 2;
+        }
+        return cudaGetLastError();
+    };
+    cudaEventRecord(b.ev0, s);
+    // Blocks of G sweeps are captured once into a CUDA graph and replayed: the kernels
+    // read what changes between sweeps (sweep index, grid offset, colour order, box,
+    // energy, temperature) from device memory.
+    const int ve = npt ? p.volume_every : 1;
+    long G = (long)ve * std::max(1, (8 + ve - 1) / ve);
+    if (exchangeEvery > 0) G = std::max(1L, std::min(G, (long)exchangeEvery));
+    const bool useGraph = !p.time_phases;
+    const long chunk = 48;
+    long nextCheck = p.check_every > 0 ? p.check_every : -1;
+    long nextRegrid = npt ? chunk : -1;
+    long nextExchange = exchangeEvery > 0 ? exchangeEvery : -1;
+    long sw = 0;
+    while (sw < nsweeps) {
+        long left = nsweeps - sw;
+        bool aligned = (sw % G == 0) && (nextExchange < 0 || nextExchange - sw >= G);
+        if (useGraph && left >= G && aligned) {
+            int key[6] = {ns, b.maxN, b.maxCells, b.maxActive, b.maxColours, (int)G};
+            if (!b.graph || std::memcmp(key, b.graphDims, sizeof key) != 0) {
+                if (b.graph) { cudaGraphExecDestroy(b.graph); b.graph = nullptr; }
+                cudaGraph_t graph;
+                long before = launches, beforeP = phaseLaunches;
+                if ((r = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return cudaFail(r, "graph capture");
+                for (long k = 0; k < G; ++k) {
+                    cudaError_t r2 = launchOne(npt && ((k + 1) % ve == 0), false);
+                    if (r2 != cudaSuccess) { cudaStreamEndCapture(s, &graph); return cudaFail(r2, "graph capture launch"); }
+                }
+                if ((r = cudaStreamEndCapture(s, &graph)) != cudaSuccess) return cudaFail(r, "graph capture end");
+                r = cudaGraphInstantiate(&b.graph, graph, 0);
+                cudaGraphDestroy(graph);
+                if (r != cudaSuccess) return cudaFail(r, "graph instantiate");
+                b.graphLaunches = launches - before;
+                b.graphPhaseLaunches = phaseLaunches - beforeP;
+                launches = before;
+                phaseLaunches = beforeP;
+                std::memcpy(b.graphDims, key, sizeof key);
+            }
+            if ((r = cudaGraphLaunch(b.graph, s)) != cudaSuccess) return cudaFail(r, "graph launch");
+            launches += b.graphLaunches;
+            phaseLaunches += b.graphPhaseLaunches;
+            sw += G;
+        } else {
+            if ((r = launchOne(npt && ((sw + 1) % ve == 0), p.time_phases != 0)) != cudaSuccess) return cudaFail(r, "sweep launch");
+            sw += 1;
+        }
+        if (nextExchange > 0 && sw >= nextExchange) {
+            kExchange<<<1, 32, 0, s>>>(b.dArgs, b.dLadder, b.dLadderStart, b.nLadders, exSeed, b.dExCtr);
+            launches += 1;
+            while (nextExchange <= sw) nextExchange += exchangeEvery;
+        }
+        if (nextCheck > 0 && sw >= nextCheck) {
+            // the cell list (box fractions) stays valid after an accepted volume move
+            if ((r = exactEnergy(true)) != cudaSuccess) return cudaFail(r, "energy check");
+            while (nextCheck <= sw) nextCheck += p.check_every;
+        }
+        if (nextRegrid > 0 && sw >= nextRegrid && sw < nsweeps) {
+            // the box changed on the device: re-derive the cell grids when needed
+            while (nextRegrid <= sw) nextRegrid += chunk;
+            if ((r = cudaStreamSynchronize(s)) != cudaSuccess) return cudaFail(r, "sweep");
+            bool changed = false;
+            for (int k = 0; k < ns; ++k) {
+                Context* c = b.sys[k];
+                SweepEngine* e = c->engine;
+                double box[3];
+                cudaMemcpy(box, c->d.box, sizeof box, cudaMemcpyDeviceToHost);
+                Grid ng = makeGrid(box, c->topo.maxcut, e->margin, e->stencil);
+                if (ng.nc[0] != e->g.nc[0] || ng.nc[1] != e->g.nc[1] || ng.nc[2] != e->g.nc[2]) {
+                    if ((rc = ensureGrid(c, e, box))) return rc;
+                    // keep the device-side temperature (replica exchange may have changed it)
+                    SweepArgs cur;
+                    cudaMemcpy(&cur, b.dArgs + k, sizeof cur, cudaMemcpyDeviceToHost);
+                    double T = cur.temper;
+                    sc_run_params q = p;
+                    q.seed = e->args.seed;
+                    fillArgs(c, e, q);
+                    e->args.temper = T;
+                    changed = true;
+                }
+            }
+            if (changed && (rc = uploadArgs(b))) return rc;
+        }
+        if ((r = cudaGetLastError()) != cudaSuccess) return cudaFail(r, "sweep launch");
+    }
+    cudaEventRecord(b.ev1, s);
+    if ((r = cudaStreamSynchronize(s)) != cudaSuccess) return cudaFail(r, "sweep");
+    float ms = 0;
+    cudaEventElapsedTime(&ms, b.ev0, b.ev1);
+    out.seconds = ms * 1e-3;
+    out.phaseSeconds = phaseMs * 1e-3;
+    out.launches = launches;
+    out.phaseLaunches = phaseLaunches;
+    for (Context* c : b.sys) c->devNewer = true;
+    return SC_OK;
+}
+
+static int checkParams(const sc_run_params& p) {
+    if (p.nsweeps < 0) return fail(SC_ERR_ARG, "nsweeps must be >= 0");
+    if (!(p.temper > 0)) return fail(SC_ERR_ARG, "temper must be positive");
+    if (p.ptype != 0 && p.ptype != 1) return fail(SC_ERR_UNSUPPORTED, "only ptype 1 (isotropic) volume moves run on the GPU");
+    if (p.stencil < 0 || p.stencil > 3) return fail(SC_ERR_ARG, "stencil must be 0 (auto), 1, 2 or 3");
+    return SC_OK;
+}
+
+int runSweeps(Context* c, const sc_run_params& p, sc_run_stats& st) {
+    std::memset(&st, 0, sizeof st);
+    int rc = checkParams(p);
+    if (rc) return rc;
+    if (c->conf.p.empty()) return SC_OK;
+    const bool npt = p.ptype == 1 && p.volume_every > 0;
+    if ((rc = prepareSystem(c, p, npt))) return rc;
+    if (!c->batch) {
+        c->batch = new Batch();
+        c->batch->sys = {c};
+        c->batch->stream = c->stream;
+        c->batch->device = c->device;
+    }
+    Batch& b = *c->batch;
+    if ((rc = uploadArgs(b))) return rc;
+    RunOut out;
+    if ((rc = runBatch(b, p, p.nsweeps, 0, 0, out))) return rc;
+    collectStats(c, st);
+    st.sweeps = p.nsweeps;
+    st.seconds = out.seconds;
+    st.phase_seconds = out.phaseSeconds;
+    st.phase_launches = out.phaseLaunches;
+    st.launches = out.launches;
+    c->lastLaunches = out.launches;
+    return systemErrors(c);
+}
+
+// --- parallel-tempering replicas -----------------------------------------------------
+
+struct ReplicaSet {
+    Batch b;
+    std::vector<double> temps;      // temperature of each replica at creation
+    std::vector<int> group;         // ladder of each replica
+    std::vector<int> ladderHost;    // replica at each ladder slot (creation order)
+    std::vector<int> ladderStartHost;
+};
+
+int createReplicas(Context* const* sys, int nrep, const double* temps, const int* group, void** out) {
+    if (nrep < 1) return fail(SC_ERR_ARG, "need at least one replica");
+    ReplicaSet* R = new ReplicaSet();
+    int device = sys[0]->device;
+    for (int k = 0; k < nrep; ++k) {
+        if (!sys[k] || !(temps[k] > 0)) { delete R; return fail(SC_ERR_ARG, "null replica or non-positive temperature"); }
+        if (sys[k]->device != device) { delete R; return fail(SC_ERR_ARG, "all replicas must use the same device"); }
+        for (int q = 0; q < k; ++q)
+            if (sys[q] == sys[k]) { delete R; return fail(SC_ERR_ARG, "a context appears twice in the replica set"); }
+        R->b.sys.push_back(sys[k]);
+        R->temps.push_back(temps[k]);
+        R->group.push_back(group ? group[k] : 0);
+    }
+    // ladders: replicas of one group, ordered by temperature; members must hold the same system
+    int ng = 0;
+    for (int g : R->group) ng = std::max(ng, g + 1);
+    R->ladderStartHost.push_back(0);
+    for (int g = 0; g < ng; ++g) {
+        std::vector<int> mem;
+        for (int k = 0; k < nrep; ++k) if (R->group[k] == g) mem.push_back(k);
+        std::sort(mem.begin(), mem.end(), [&](int x, int y) { return R->temps[x] < R->temps[y]; });
+        for (size_t q = 1; q < mem.size(); ++q) {
+            Context* a = sys[mem[0]];
+            Context* c2 = sys[mem[q]];
+            if (a->conf.p.size() != c2->conf.p.size() || a->usedTypes != c2->usedTypes) {
+                delete R;
+                return fail(SC_ERR_ARG, "replicas of one ladder must hold the same system (N and types)");
+            }
+        }
+        for (int k : mem) R->ladderHost.push_back(k);
+        R->ladderStartHost.push_back((int)R->ladderHost.size());
+    }
+    if ((int)R->ladderHost.size() != nrep) { delete R; return fail(SC_ERR_ARG, "ladder ids must be 0..n-1"); }
+    *out = R;
+    return SC_OK;
+}
+
+void destroyReplicas(void* h) { delete static_cast<ReplicaSet*>(h); }
+
+int runReplicas(void* h, const sc_run_params& p, int exchangeEvery, sc_run_stats& st, double* tempsOut,
+                double* energiesOut, long* exTried, long* exAcc) {
+    ReplicaSet* R = static_cast<ReplicaSet*>(h);
+    std::memset(&st, 0, sizeof st);
+    int rc = checkParams(p);
+    if (rc) return rc;
+    Batch& b = R->b;
+    const int nrep = (int)b.sys.size();
+    const bool npt = p.ptype == 1 && p.volume_every > 0;
+    for (int k = 0; k < nrep; ++k) {
+        Context* c = b.sys[k];
+        if (c->conf.p.empty()) return fail(SC_ERR_ARG, "a replica holds no particles");
+        sc_run_params q = p;
+        sc_default_run(reinterpret_cast<const sc_context*>(c), &q);   // per-replica step sizes
+        q.nsweeps = p.nsweeps; q.seed = p.seed + 0x9E3779B97F4A7C15ull * (unsigned long long)(k + 1);
+        q.temper = R->temps[k]; q.ptype = p.ptype; q.volume_every = p.volume_every; q.check_every = p.check_every;
+        q.stencil = p.stencil; q.time_phases = p.time_phases; q.press = p.press;
+        if (p.transmx > 0) q.transmx = p.transmx;
+        if (p.rot_angle > 0) q.rot_angle = p.rot_angle;
+        if ((rc = prepareSystem(c, q, npt))) return rc;
+    }
+    b.stream = b.sys[0]->stream;
+    b.device = b.sys[0]->device;
+    if (!b.dLadder) {
+        if ((rc = b.alloc((void**)&b.dLadder, sizeof(int) * nrep))) return rc;
+        if ((rc = b.alloc((void**)&b.dLadderStart, sizeof(int) * R->ladderStartHost.size()))) return rc;
+        if ((rc = b.alloc((void**)&b.dExCtr, sizeof(unsigned long long) * (1 + 2 * nrep)))) return rc;
+        cudaMemcpy(b.dLadder, R->ladderHost.data(), sizeof(int) * nrep, cudaMemcpyHostToDevice);
+        cudaMemcpy(b.dLadderStart, R->ladderStartHost.data(), sizeof(int) * R->ladderStartHost.size(), cudaMemcpyHostToDevice);
+        cudaMemset(b.dExCtr, 0, sizeof(unsigned long long) * (1 + 2 * nrep));
+        b.nLadders = (int)R->ladderStartHost.size() - 1;
+    } else {
+        // keep the temperatures the exchanges produced
+        std::vector<SweepArgs> cur(nrep);
+        cudaMemcpy(cur.data(), b.dArgs, sizeof(SweepArgs) * nrep, cudaMemcpyDeviceToHost);
+        for (int k = 0; k < nrep; ++k) b.sys[k]->engine->args.temper = cur[k].temper;
+    }
+    if ((rc = uploadArgs(b))) return rc;
+    RunOut out;
+    if ((rc = runBatch(b, p, p.nsweeps, exchangeEvery, p.seed ^ 0xA5A5A5A5ull, out))) return rc;
+    std::vector<SweepArgs> cur(nrep);
+    cudaMemcpy(cur.data(), b.dArgs, sizeof(SweepArgs) * nrep, cudaMemcpyDeviceToHost);
+    for (int k = 0; k < nrep; ++k) {
+        sc_run_stats s1;
+        std::memset(&s1, 0, sizeof s1);
+        collectStats(b.sys[k], s1);
+        st.moves += s1.moves;
+        st.acc_trans += s1.acc_trans; st.rej_trans += s1.rej_trans;
+        st.acc_rot += s1.acc_rot; st.rej_rot += s1.rej_rot;
+        st.acc_vol += s1.acc_vol; st.rej_vol += s1.rej_vol; st.vol_constrained += s1.vol_constrained;
+        st.pairs_tested += s1.pairs_tested; st.pairs_evaluated += s1.pairs_evaluated;
+        st.energy += s1.energy;
+        st.max_drift = std::max(st.max_drift, s1.max_drift);
+        if (tempsOut) tempsOut[k] = cur[k].temper;
+        if (energiesOut) energiesOut[k] = s1.energy;
+        if ((rc = systemErrors(b.sys[k]))) return rc;
+    }
+    if (exTried || exAcc) {
+        std::vector<unsigned long long> ctr(1 + 2 * nrep);
+        cudaMemcpy(ctr.data(), b.dExCtr, sizeof(unsigned long long) * ctr.size(), cudaMemcpyDeviceToHost);
+        for (int k = 0; k < nrep; ++k) {
+            if (exTried) exTried[k] = (long)ctr[1 + 2 * k];
+            if (exAcc) exAcc[k] = (long)ctr[2 + 2 * k];
+        }
+    }
+    st.sweeps = p.nsweeps;
+    st.seconds = out.seconds;
+    st.phase_seconds = out.phaseSeconds;
+    st.phase_launches = out.phaseLaunches;
+    st.launches = out.launches;
     return SC_OK;
 }
 

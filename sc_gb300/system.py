@@ -169,3 +169,50 @@ class System:
         st = L.RunStats()
         L.check(self._lib.sc_simulate(self._h, C.byref(p), C.byref(st)))
         return st
+
+
+class ReplicaSet:
+    """Replicas moved together on one GPU, with parallel-tempering exchanges.
+
+    The reference runs one replica per MPI rank (MoveCreator::replicaExchangeMove,
+    scOOP/mc/movecreator.cpp:552-795); here every replica's moves run in the same
+    kernels.  `ladder[k]` groups replicas into independent temperature ladders.
+    """
+
+    def __init__(self, systems, temperatures, ladder=None):
+        self._lib = L.load()
+        self.systems = list(systems)
+        n = len(self.systems)
+        hs = (C.c_void_p * n)(*[s._h for s in self.systems])
+        T = np.ascontiguousarray(temperatures, dtype=np.float64)
+        lad = None if ladder is None else np.ascontiguousarray(ladder, dtype=np.int32)
+        h = C.c_void_p()
+        L.check(self._lib.sc_replicas_create(hs, n, _dptr(T), None if lad is None else _iptr(lad), C.byref(h)))
+        self._h = h
+
+    def run(self, nsweeps, exchange_every=0, seed=1, params=None, **overrides):
+        p = params if params is not None else self.systems[0].default_run()
+        p.nsweeps = nsweeps
+        p.seed = seed
+        for k, v in overrides.items():
+            setattr(p, k, v)
+        n = len(self.systems)
+        st = L.RunStats()
+        T = np.zeros(n)
+        E = np.zeros(n)
+        tried = (C.c_long * n)()
+        acc = (C.c_long * n)()
+        L.check(self._lib.sc_replicas_run(self._h, C.byref(p), int(exchange_every), C.byref(st), _dptr(T), _dptr(E),
+                                          tried, acc))
+        return st, T, E, np.array(tried[:]), np.array(acc[:])
+
+    def close(self):
+        if self._h:
+            self._lib.sc_replicas_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -136,6 +136,43 @@ def nvt_psc(n=1000, phi=0.1, seed=1, temper=1.0):
     return opts, top, config_text(box, pos, dirs, pds)
 
 
+def lattice_psc(n, phi=0.2, seed=1, temper=1.0):
+    """PSC start on a lattice (axes within 0.1 rad of z, random patch directions): the
+    dense starts random sequential placement cannot reach."""
+    L = 3.0
+    rng = np.random.default_rng(seed)
+    edge = (n * _vol_sc(L) / phi) ** (1 / 3)
+    nz = max(1, int(edge // (L + 1.05)))
+    nxy = int(math.ceil(math.sqrt(n / nz)))
+    if edge / nxy < 1.05 + 0.35:
+        raise RuntimeError("lattice start: density too high")
+    box = np.full(3, edge)
+    sites = np.array([(i, j, k) for k in range(nz) for j in range(nxy) for i in range(nxy)], float)
+    sites = sites[rng.permutation(len(sites))[:n]]
+    pos = (sites + 0.5) * np.array([edge / nxy, edge / nxy, edge / nz])
+    tilt = rng.uniform(0, 0.1, n)
+    az = rng.uniform(0, 2 * math.pi, n)
+    dirs = np.stack([np.sin(tilt) * np.cos(az), np.sin(tilt) * np.sin(az), np.cos(tilt)], 1)
+    top = ("[Types]\nP 1 PSC 1.0 1.0 1.12 0.2 90.0 10.0 3.0 0.0\n"
+           f"[Molecules]\nP: {{\nparticles: 1\n}}\n[System]\nP {n}\n")
+    opts = options_text(ptype=0, transmx=0.4, rotmx=30.0, temper=temper, seed=seed)
+    return opts, top, config_text(box, pos, dirs, _perp(rng, dirs))
+
+
+def pt_ladders(n_ladders=8, per_ladder=8, seed=1, n_range=(500, 4000), phi_range=(0.10, 0.25), t_range=(0.8, 1.6)):
+    """Parallel-tempering replicas of the PSC model with uneven sizes: n_ladders systems
+    (N and packing fraction drawn uniformly), each replicated over a geometric
+    temperature ladder.  Returns (texts per ladder, temperatures per ladder slot)."""
+    rng = np.random.default_rng(seed)
+    systems = []
+    for g in range(n_ladders):
+        n = int(rng.integers(n_range[0], n_range[1] + 1))
+        phi = float(rng.uniform(*phi_range))
+        systems.append(lattice_psc(n, phi=phi, seed=seed * 1000 + g))
+    temps = list(np.geomspace(t_range[0], t_range[1], per_ladder))
+    return systems, temps
+
+
 WORKLOADS = {
     "npt_cpsc_spa_4000": lambda seed=1: npt_cpsc_spa(4000, seed=seed),
     "nvt_psc_1000": lambda seed=1: nvt_psc(1000, seed=seed),

@@ -1,0 +1,67 @@
+"""Replicas moved together: batching must not change any trajectory, and the
+parallel-tempering exchange keeps every ladder a permutation of its temperatures."""
+import numpy as np
+import pytest
+
+from test_gpu_sweep import ens, opts_text
+
+pytestmark = pytest.mark.gpu
+GOLDEN = 0x9E3779B97F4A7C15
+
+
+def open_systems(name, k):
+    from sc_gb300 import System
+
+    e = ens(name)
+    return [System.from_text(opts_text(e["options"]), e["inputs"]["top.init"], e["inputs"]["config.init"])
+            for _ in range(k)]
+
+
+def test_batched_replicas_reproduce_single_runs():
+    from sc_gb300 import ReplicaSet
+
+    sysA = open_systems("psc_nvt", 3)
+    sysB = open_systems("psc_nvt", 3)
+    temps = [0.6, 0.8, 1.1]
+    R = ReplicaSet(sysA, temps, ladder=[0, 1, 2])
+    st, T, E, _, _ = R.run(40, exchange_every=0, seed=77, stencil=2)
+    assert list(T) == temps
+    for k, s in enumerate(sysB):
+        single = s.simulate(nsweeps=40, seed=(77 + GOLDEN * (k + 1)) % (1 << 64), temper=temps[k], stencil=2,
+                            check_every=0)
+        assert single.energy == E[k]
+        pa, pb = sysA[k].particles(), s.particles()
+        assert all(list(x.pos) == list(y.pos) and list(x.dir) == list(y.dir) for x, y in zip(pa, pb))
+    assert st.moves == 3 * 40 * sysA[0].n
+    R.close()
+
+
+def test_exchanges_keep_ladders_and_energies():
+    from sc_gb300 import ReplicaSet
+
+    sys8 = open_systems("psc_nvt", 8)
+    # neighbouring temperatures close enough that swaps of 250-particle replicas get accepted
+    temps = list(np.geomspace(0.9, 1.0, 4)) * 2
+    ladder = [0] * 4 + [1] * 4
+    R = ReplicaSet(sys8, temps, ladder=ladder)
+    st, T, E, tried, acc = R.run(400, exchange_every=20, seed=5)
+    for g in (0, 1):
+        assert sorted(T[4 * g: 4 * g + 4]) == pytest.approx(sorted(temps[4 * g: 4 * g + 4]))
+    assert tried.sum() > 0 and acc.sum() > 0
+    for k, s in enumerate(sys8):
+        exact = s.all_to_all()
+        assert abs(E[k] - exact) <= 1e-9 * max(1.0, abs(exact))
+    R.close()
+
+
+def test_uneven_sizes_in_one_batch():
+    from sc_gb300 import ReplicaSet, System, workloads
+
+    systems = [System.from_text(*workloads.nvt_psc(n, phi=0.15, seed=3 + n)) for n in (120, 400, 260)]
+    R = ReplicaSet(systems, [1.0, 1.0, 1.0], ladder=[0, 1, 2])
+    st, T, E, _, _ = R.run(30, exchange_every=0, seed=9)
+    assert st.moves == 30 * sum(s.n for s in systems)
+    for k, s in enumerate(systems):
+        exact = s.all_to_all()
+        assert abs(E[k] - exact) <= 1e-9 * max(1.0, abs(exact))
+    R.close()

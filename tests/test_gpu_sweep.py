@@ -45,10 +45,11 @@ def exact_energy(s):
     return s.all_to_all()
 
 
-def test_running_energy_matches_exact_total():
+@pytest.mark.parametrize("stencil", [1, 2])
+def test_running_energy_matches_exact_total(stencil):
     e, s = open_ens("psc_nvt")
     e0 = exact_energy(s)
-    st = s.simulate(nsweeps=200, seed=11, check_every=50)
+    st = s.simulate(nsweeps=200, seed=11, check_every=50, stencil=stencil)
     assert st.moves == 200 * s.n
     assert st.acc_trans + st.rej_trans + st.acc_rot + st.rej_rot == st.moves
     assert 0.05 < (st.acc_trans + st.acc_rot) / st.moves < 0.95
@@ -57,7 +58,7 @@ def test_running_energy_matches_exact_total():
     assert abs(st.energy - e1) <= 1e-9 * max(1.0, abs(e1))
     assert st.max_drift <= 1e-9 * max(1.0, abs(e1))
     # the cell-list total energy of the last check equals the brute-force one
-    st2 = s.simulate(nsweeps=50, seed=11, check_every=50)
+    st2 = s.simulate(nsweeps=50, seed=11, check_every=50, stencil=stencil)
     assert abs(st2.energy_check - exact_energy(s)) <= 1e-11 * max(1.0, abs(st2.energy_check))
     s.close()
 
@@ -113,33 +114,46 @@ def alignment_order(s):
     return float((d @ d.T)[iu][close[iu]].sum())
 
 
-def sample(s, golden, nsweeps, seed):
-    p = s.default_run()
-    p.seed = seed
+def sample(systems, golden, nsweeps, seed):
+    """Independent trajectories (one per system, same start, own Philox stream) moved
+    together as a replica batch without exchanges; returns per-trajectory series."""
+    from sc_gb300 import ReplicaSet
+
+    T = golden["options"]["temper"]
+    R = ReplicaSet(systems, [T] * len(systems), ladder=list(range(len(systems))))
+    p = systems[0].default_run()
     p.check_every = 0
     rep = golden["report"]
-    E, A, V = [], [], []
+    E = [[] for _ in systems]
+    A = [[] for _ in systems]
+    V = [[] for _ in systems]
     done = 0
     while done < nsweeps:
-        st = s.simulate(p, nsweeps=rep)
+        st, _, en, _, _ = R.run(rep, exchange_every=0, seed=seed, params=p)
         done += rep
         if done > golden["burn"]:
-            E.append(st.energy / s.n)
-            A.append(alignment_order(s) / s.n)
-            V.append(float(np.prod(s.box)) / s.n)
-    return np.array(E), np.array(A), np.array(V)
+            for k, s in enumerate(systems):
+                E[k].append(en[k] / s.n)
+                A[k].append(alignment_order(s) / s.n)
+                V[k].append(float(np.prod(s.box)) / s.n)
+    R.close()
+    return [np.array(x) for x in E], [np.array(x) for x in A], [np.array(x) for x in V]
 
 
-def mean_se(x, nblocks=10):
-    b = np.array_split(x, nblocks)
-    m = np.array([v.mean() for v in b])
-    return float(x.mean()), float(m.std(ddof=1) / math.sqrt(nblocks))
+def mean_se(series):
+    """Mean and standard error from the means of independent trajectories."""
+    m = np.array([x.mean() for x in series])
+    return float(m.mean()), float(m.std(ddof=1) / math.sqrt(len(m)))
 
 
 @pytest.mark.parametrize("name", ["psc_nvt", "cpsc_spa_npt"])
 def test_ensemble_matches_reference(name):
-    g, s = open_ens(name)
-    E, A, V = sample(s, g, g["nsweeps"], seed=4242)
+    from sc_gb300 import System
+
+    g = ens(name)
+    systems = [System.from_text(opts_text(g["options"]), g["inputs"]["top.init"], g["inputs"]["config.init"])
+               for _ in range(6)]
+    E, A, V = sample(systems, g, g["nsweeps"], seed=4242)
     checks = [("energy_per_particle", E), ("alignment_per_particle", A)]
     if g["options"].get("ptype") == 1:
         checks.append(("volume_per_particle", V))
@@ -150,4 +164,5 @@ def test_ensemble_matches_reference(name):
         sigma = math.sqrt(se ** 2 + ref["se"] ** 2)
         report[key] = (m, se, ref["mean"], ref["se"])
         assert abs(m - ref["mean"]) <= 2.0 * sigma, report
-    s.close()
+    for s in systems:
+        s.close()
