@@ -261,7 +261,8 @@ def bench_replicas(steps, seed=1):
         c.close()
     return {"workload": "pt64_psc_uneven", "replicas": len(ctxs), "particles": particles, "stencil": best[0],
             "batched_moves_per_s": batched, "plain_moves_per_s": plain, "speedup": batched / plain,
-            "exchange_acceptance": float(acc.sum() / max(1, tried.sum())), "sweeps": steps}
+            "exchanges_tried": int(tried.sum()), "exchange_acceptance": float(acc.sum() / max(1, tried.sum())),
+            "sweeps": steps}
 
 
 def main():
@@ -379,7 +380,7 @@ def main():
     replicas = None
     if rank == 0 and not a.no_e2e:
         try:
-            replicas = bench_replicas(max(10, a.steps), seed=a.seed)
+            replicas = bench_replicas(200, seed=a.seed)
         except Exception as ex:
             replicas = {"error": str(ex)}
     if rank == 0:

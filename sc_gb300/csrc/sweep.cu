@@ -54,7 +54,7 @@ constexpr int kMoveThreads = 128;
 constexpr int kWarps = kMoveThreads / 32;
 constexpr int kCellCap = 256;        // particles per cell
 constexpr int kNbCap = 343;          // stencil cells, (2*3+1)^3
-constexpr int kCandCap = 4096;       // candidates staged in shared memory
+constexpr int kCandCap = 1024;       // candidates staged in shared memory at a time
 constexpr int kQueueCap = 1536;      // pair queue entries
 constexpr int kChunk = 512;          // candidates per stage-A round
 constexpr int kMaxColours = 64;
@@ -62,7 +62,7 @@ constexpr size_t kDynSmem = (size_t)kCandCap * (sizeof(float4) + sizeof(int));
 
 enum Ctr { C_ACC_T, C_REJ_T, C_ACC_R, C_REJ_R, C_ACC_V, C_REJ_V, C_VOL_CONSTR, C_TESTED, C_EVAL, C_CELL_REJ, C_MOVES,
            C_SCREENED, C_COUNT };
-enum ErrBit { E_CELL_OVERFLOW = 1, E_PARTNER_FAR = 2, E_CAND_OVERFLOW = 4 };
+enum ErrBit { E_CELL_OVERFLOW = 1, E_PARTNER_FAR = 2 };
 
 struct Grid {
     int nc[3];
@@ -292,11 +292,11 @@ struct Stencil {
     int nNb;
     int nCand;
     int ownOff;         // offset of the cell's own particles in the candidate list
-    int overflow;
 };
 
-__device__ void stageCandidates(const SweepArgs& a, int cx, int cy, int cz, Stencil& st, Scan& sc, int* candIdx,
-                                float4* candPos) {
+// The stencil of cell (cx, cy, cz): its cells and their offsets in the concatenated
+// candidate list (cells in stencil order, particles in cell-list order).
+__device__ void stageStencil(const SweepArgs& a, int cx, int cy, int cz, Stencil& st, Scan& sc) {
     const Grid& g = a.g;
     const int nx = axisCount(g.nc[0], g.s[0]), ny = axisCount(g.nc[1], g.s[1]), nz = axisCount(g.nc[2], g.s[2]);
     const int nn = nx * ny * nz;
@@ -328,24 +328,27 @@ __device__ void stageCandidates(const SweepArgs& a, int cx, int cy, int cz, Sten
         st.nNb = nn;
         st.nbOff[nn] = carry;
         st.nCand = carry;
-        st.overflow = carry > kCandCap;
     }
     __syncthreads();
     if (threadIdx.x == 0) st.ownOff = st.nbOff[ownQ];
-    if (st.overflow) {
-        if (threadIdx.x == 0) atomicOr(a.err, E_CAND_OVERFLOW);
-        __syncthreads();
-        return;
-    }
-    for (int k = threadIdx.x; k < carry; k += kMoveThreads) {
+    __syncthreads();
+}
+
+// Loads candidates [first, first + count) of the stencil into shared memory (count <=
+// kCandCap).  A stencil larger than the buffer is processed in windows of kCandCap.
+__device__ void loadCandidates(const SweepArgs& a, const Stencil& st, int first, int count, int* candIdx,
+                               float4* candPos) {
+    const int nn = st.nNb;
+    for (int kk = threadIdx.x; kk < count; kk += kMoveThreads) {
+        int k = first + kk;
         int lo = 0, hi = nn - 1;      // last q with nbOff[q] <= k
         while (lo < hi) {
             int mid = (lo + hi + 1) >> 1;
             if (st.nbOff[mid] <= k) lo = mid; else hi = mid - 1;
         }
         int slot = a.cellStart[st.nbCell[lo]] + (k - st.nbOff[lo]);
-        candIdx[k] = a.cellIdx[slot];
-        candPos[k] = a.cellPosF[slot];
+        candIdx[kk] = a.cellIdx[slot];
+        candPos[kk] = a.cellPosF[slot];
     }
     __syncthreads();
 }
@@ -578,9 +581,10 @@ __global__ void __launch_bounds__(kMoveThreads) kColour(const SweepArgs* __restr
     if (cnt == 0 || cnt > kCellCap) return;
     const int tid = threadIdx.x, warp = tid >> 5;
     for (int k = tid; k < cnt; k += kMoveThreads) sh.list[k] = a.cellIdx[a.cellStart[cell] + k];
-    stageCandidates(a, cx, cy, cz, sh.st, sh.scan, candIdx, candPos);
-    if (sh.st.overflow) return;
+    stageStencil(a, cx, cy, cz, sh.st, sh.scan);
     const int nCand = sh.st.nCand;
+    const bool resident = nCand <= kCandCap;
+    if (resident) loadCandidates(a, sh.st, 0, nCand, candIdx, candPos);
 
     DevCtx c;
     c.params = a.t.params; c.mols = a.t.mols; c.ntypes = a.t.ntypes; c.n = a.s.n; c.sqmaxcut = a.t.sqmaxcut;
@@ -638,13 +642,18 @@ __global__ void __launch_bounds__(kMoveThreads) kColour(const SweepArgs* __restr
             }
             __syncthreads();
         };
-        for (int base = 0; base < nCand; base += kChunk) {
+        for (int wbase = 0; wbase < nCand; wbase += kCandCap) {
+          // candidates in shared memory: all of them, or the window [wbase, wend)
+          const int wend = min(wbase + kCandCap, nCand);
+          if (!resident) loadCandidates(a, sh.st, wbase, wend - wbase, candIdx, candPos);
+          for (int base = wbase; base < wend; base += kChunk) {
             // stage A: FP32 minimum image against the old and the new position
             int qa = 0;
-            for (int r0 = base; r0 < min(base + kChunk, nCand); r0 += kMoveThreads) {
-                int k = r0 + tid;
+            const int cend = min(base + kChunk, wend);
+            for (int r0 = base; r0 < cend; r0 += kMoveThreads) {
+                int k = r0 + tid - wbase;   // index in the shared-memory window
                 int flags = 0;
-                if (k < min(base + kChunk, nCand)) {
+                if (r0 + tid < cend) {
                     int j = candIdx[k];
                     bool partner = (j == partners[0] || j == partners[1] || j == partners[2] || j == partners[3]);
                     if (j != t && !partner) {
@@ -695,6 +704,12 @@ __global__ void __launch_bounds__(kMoveThreads) kColour(const SweepArgs* __restr
                     qb0 = qb1 = qb2 = 0;
                 }
             }
+          }
+          if (!resident) {      // queue entries index the window: evaluate them before it changes
+              flushC();
+              nEval += qb0 + qb1 + qb2;
+              qb0 = qb1 = qb2 = 0;
+          }
         }
         flushC();
         nEval += qb0 + qb1 + qb2 + 2 * np;
@@ -710,7 +725,7 @@ __global__ void __launch_bounds__(kMoveThreads) kColour(const SweepArgs* __restr
                     a.s.patch[t] = sh.npatch;
                 } else {
                     float4 nf = make_float4(newF.x, newF.y, newF.z, 0.0f);
-                    candPos[sh.st.ownOff + sh.slotR] = nf;
+                    if (resident) candPos[sh.st.ownOff + sh.slotR] = nf;
                     a.cellPosF[a.cellStart[cell] + sh.slotR] = nf;
                 }
                 dECell += eNew - eOld;
@@ -790,13 +805,10 @@ __global__ void __launch_bounds__(kMoveThreads) kCellEnergy(const SweepArgs* __r
         return;
     }
     int cx = cell % g.nc[0], cy = (cell / g.nc[0]) % g.nc[1], cz = cell / (g.nc[0] * g.nc[1]);
-    for (int k = tid; k < cnt; k += kMoveThreads) sh.list[k] = a.cellIdx[a.cellStart[cell] + k];
-    stageCandidates(a, cx, cy, cz, sh.st, sh.scan, candIdx, candPos);
-    if (sh.st.overflow) {
-        if (tid == 0) a.partial[cell] = 0.0;
-        return;
-    }
-    const int nCand = sh.st.nCand, ownOff = sh.st.ownOff;
+    const int own0 = a.cellStart[cell];
+    for (int k = tid; k < cnt; k += kMoveThreads) sh.list[k] = a.cellIdx[own0 + k];
+    stageStencil(a, cx, cy, cz, sh.st, sh.scan);
+    const int nCand = sh.st.nCand;
     DevCtx c;
     c.params = a.t.params; c.mols = a.t.mols; c.ntypes = a.t.ntypes; c.n = a.s.n; c.sqmaxcut = a.t.sqmaxcut;
     const double* bx = useTrialBox ? ctl.trialBox : a.s.box;
@@ -816,36 +828,40 @@ __global__ void __launch_bounds__(kMoveThreads) kCellEnergy(const SweepArgs* __r
             }
         }
     }
-    const long total = (long)cnt * nCand;
-    int qb = 0;
+    int qb = 0, wlen = 0;
     auto flushC = [&](int count) {
         __syncthreads();                   // queue entries of every thread are visible
         for (int e = tid; e < count; e += kMoveThreads) {
             int q = sh.queueB[e];
-            int i = sh.list[q / nCand], j = candIdx[q % nCand];
+            int i = sh.list[q / wlen], j = candIdx[q % wlen];
             Con con = makeCon(c, i, a.s.mol[i]);
             unsigned bb; double dd;
             sum += pairEnergy(c, viewAt(a.s, i), viewAt(a.s, j), con, box, &bb, &dd);
         }
         __syncthreads();
     };
-    for (long base = 0; base < total; base += kChunk) {
+    for (int wbase = 0; wbase < nCand; wbase += kCandCap) {
+      // the candidates in windows of kCandCap; pair q = (own particle li, window slot k)
+      wlen = min(kCandCap, nCand - wbase);
+      loadCandidates(a, sh.st, wbase, wlen, candIdx, candPos);
+      const int total = cnt * wlen;
+      for (int base = 0; base < total; base += kChunk) {
         int qa = 0;
-        long end = min(base + (long)kChunk, total);
-        for (long r0 = base; r0 < end; r0 += kMoveThreads) {
-            long q = r0 + tid;
+        int end = min(base + kChunk, total);
+        for (int r0 = base; r0 < end; r0 += kMoveThreads) {
+            int q = r0 + tid;
             int keep = 0;
             if (q < end) {
-                int li = (int)(q / nCand), k = (int)(q % nCand);
+                int li = q / wlen, k = q % wlen;
                 int i = sh.list[li], j = candIdx[k];
                 if (j < i) {
-                    float4 pi = candPos[ownOff + li];
+                    float4 pi = a.cellPosF[own0 + li];
                     keep = dist2f(candPos[k], make_float3(pi.x, pi.y, pi.z), box) <= thr32;
                 }
             }
             int tot;
             int off = blockExclusiveScan(keep, tot, sh.scan);
-            if (keep) sh.queueA[qa + off] = (int)q;
+            if (keep) sh.queueA[qa + off] = q;
             qa += tot;
         }
         __syncthreads();
@@ -854,7 +870,7 @@ __global__ void __launch_bounds__(kMoveThreads) kCellEnergy(const SweepArgs* __r
             int keep = 0, q = 0;
             if (e < qa) {
                 q = sh.queueA[e];
-                int i = sh.list[q / nCand], j = candIdx[q % nCand];
+                int i = sh.list[q / wlen], j = candIdx[q % wlen];
                 int4 mi = a.s.mol[i];
                 Con con = makeCon(c, i, mi);
                 bool partner = (j == con.idx[0] || j == con.idx[1] || j == con.idx[2] || j == con.idx[3]);
@@ -874,8 +890,10 @@ __global__ void __launch_bounds__(kMoveThreads) kCellEnergy(const SweepArgs* __r
             qb += tot;
             if (qb > kQueueCap - kMoveThreads) { flushC(qb); qb = 0; }
         }
+      }
+      flushC(qb);           // queue entries index the window
+      qb = 0;
     }
-    flushC(qb);
     blockSum2(sum, unused, sh.red);
     if (tid == 0) a.partial[cell] = sum;
 }
@@ -1215,7 +1233,6 @@ static int systemErrors(Context* c) {
     int err = 0;
     cudaMemcpy(&err, c->engine->err, sizeof err, cudaMemcpyDeviceToHost);
     if (err & E_CELL_OVERFLOW) return fail(SC_ERR_DEVICE, "a cell holds more than 256 particles (density too high for the cell list)");
-    if (err & E_CAND_OVERFLOW) return fail(SC_ERR_DEVICE, "a cell stencil holds more than 4096 particles (use a smaller stencil)");
     if (err & E_PARTNER_FAR) return fail(SC_ERR_DEVICE, "a bonded partner lies beyond the cell stencil (bond longer than maxcut)");
     return SC_OK;
 }

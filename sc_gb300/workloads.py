@@ -136,11 +136,9 @@ def nvt_psc(n=1000, phi=0.1, seed=1, temper=1.0):
     return opts, top, config_text(box, pos, dirs, pds)
 
 
-def lattice_psc(n, phi=0.2, seed=1, temper=1.0):
-    """PSC start on a lattice (axes within 0.1 rad of z, random patch directions): the
-    dense starts random sequential placement cannot reach."""
-    L = 3.0
-    rng = np.random.default_rng(seed)
+def _lattice(rng, n, phi, L=3.0):
+    """Aligned start: axes within 0.1 rad of z on a lattice of layers (random patch
+    directions); reaches the densities random sequential placement cannot."""
     edge = (n * _vol_sc(L) / phi) ** (1 / 3)
     nz = max(1, int(edge // (L + 1.05)))
     nxy = int(math.ceil(math.sqrt(n / nz)))
@@ -153,10 +151,53 @@ def lattice_psc(n, phi=0.2, seed=1, temper=1.0):
     tilt = rng.uniform(0, 0.1, n)
     az = rng.uniform(0, 2 * math.pi, n)
     dirs = np.stack([np.sin(tilt) * np.cos(az), np.sin(tilt) * np.sin(az), np.cos(tilt)], 1)
+    return box, pos, dirs, _perp(rng, dirs)
+
+
+def lattice_psc(n, phi=0.2, seed=1, temper=1.0):
+    """PSC (the nvt_psc model) from an aligned lattice start."""
+    rng = np.random.default_rng(seed)
+    box, pos, dirs, pds = _lattice(rng, n, phi)
     top = ("[Types]\nP 1 PSC 1.0 1.0 1.12 0.2 90.0 10.0 3.0 0.0\n"
            f"[Molecules]\nP: {{\nparticles: 1\n}}\n[System]\nP {n}\n")
     opts = options_text(ptype=0, transmx=0.4, rotmx=30.0, temper=temper, seed=seed)
-    return opts, top, config_text(box, pos, dirs, _perp(rng, dirs))
+    return opts, top, config_text(box, pos, dirs, pds)
+
+
+PSC_CPSC_TYPES = ("P 1 PSC 1.0 1.0 1.12 0.2 90.0 10.0 3.0 0.0\n"
+                  "C 2 CPSC 1.0 1.0 1.12 0.2 120.0 10.0 3.0 0.0\n")
+
+
+def psc_cpsc(n=65536, phi=0.2, seed=1, temper=1.0):
+    """PSC (patch 90 deg) and CPSC (cylindrical patch 120 deg) 50/50, L=3, eps=1,
+    pdis 1.12, pswitch 0.2, from an aligned lattice start (the bench melts it first).
+    Particles of one type are listed together, as the [System] section requires."""
+    rng = np.random.default_rng(seed)
+    box, pos, dirs, pds = _lattice(rng, n, phi)
+    n1 = n // 2
+    top = ("[Types]\n" + PSC_CPSC_TYPES +
+           "[Molecules]\nP: {\nparticles: 1\n}\nC: {\nparticles: 2\n}\n"
+           f"[System]\nP {n1}\nC {n - n1}\n")
+    opts = options_text(ptype=0, transmx=0.4, rotmx=30.0, temper=temper, seed=seed)
+    return opts, top, config_text(box, pos, dirs, pds)
+
+
+def rods_in_spheres(n_spheres=3000, n_rods=2, L=6.0, phi=0.2, seed=1, temper=1.0):
+    """A few long PSC rods among many attractive spheres: the long cut-off makes cell
+    stencils of several thousand particles (the move kernel then stages its candidates
+    in windows)."""
+    rng = np.random.default_rng(seed)
+    vol = n_spheres * math.pi / 6 + n_rods * _vol_sc(L)
+    box = np.full(3, (vol / phi) ** (1 / 3))
+    halfl = [L / 2] * n_rods + [0.0] * n_spheres
+    pos, dirs, pds = place(rng, halfl, box)
+    top = ("[Types]\n"
+           f"P 1 PSC 1.0 1.0 1.12 0.2 90.0 10.0 {L} 0.0\n"
+           "A 2 SPA 0.5 1.0 1.1225 0.3775\n"
+           "[Molecules]\nP: {\nparticles: 1\n}\nA: {\nparticles: 2\n}\n"
+           f"[System]\nP {n_rods}\nA {n_spheres}\n")
+    opts = options_text(ptype=0, transmx=0.3, rotmx=20.0, temper=temper, seed=seed)
+    return opts, top, config_text(box, pos, dirs, pds)
 
 
 def pt_ladders(n_ladders=8, per_ladder=8, seed=1, n_range=(500, 4000), phi_range=(0.10, 0.25), t_range=(0.8, 1.6)):
@@ -176,4 +217,5 @@ def pt_ladders(n_ladders=8, per_ladder=8, seed=1, n_range=(500, 4000), phi_range
 WORKLOADS = {
     "npt_cpsc_spa_4000": lambda seed=1: npt_cpsc_spa(4000, seed=seed),
     "nvt_psc_1000": lambda seed=1: nvt_psc(1000, seed=seed),
+    "psc_cpsc_65536": lambda seed=1: psc_cpsc(65536, seed=seed),
 }

@@ -63,6 +63,22 @@ def test_running_energy_matches_exact_total(stencil):
     s.close()
 
 
+def test_stencil_larger_than_shared_memory_window():
+    """Cells of a long rod's cut-off holding thousands of spheres: candidates are staged
+    in windows, the running energy must stay exact."""
+    from sc_gb300 import System, workloads
+
+    s = System.from_text(*workloads.rods_in_spheres(3000, seed=4))
+    e0 = exact_energy(s)
+    st = s.simulate(nsweeps=8, seed=2, check_every=4, stencil=1)
+    assert st.moves == 8 * s.n and st.pairs_tested > 8 * s.n * 1100
+    e1 = exact_energy(s)
+    assert e1 != e0
+    assert abs(st.energy - e1) <= 1e-9 * max(1.0, abs(e1))
+    assert abs(st.energy_check - e1) <= 1e-9 * max(1.0, abs(e1))
+    s.close()
+
+
 def test_same_seed_same_trajectory():
     _, s1 = open_ens("psc_nvt")
     _, s2 = open_ens("psc_nvt")
