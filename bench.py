@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    ap.add_argument("--only", default="all", choices=["all", "main", "replicas", "surrogate"],
+                    help="run one section alone (prints that section's JSON)")
     return ap.parse_args()
 
 
@@ -265,11 +267,80 @@ def bench_replicas(steps, seed=1):
             "sweeps": steps}
 
 
+def bench_surrogate(steps, seed=1, melt=300, snapshots=30, gap=10, epochs=8):
+    """Surrogate delayed acceptance on 65,536 PSC/CPSC (50/50, packing fraction 0.2, T=1):
+    the aligned start is melted, the exact kernel's pairs of `snapshots` configurations
+    train the network (on the GPU), then plain and delayed-acceptance sweeps are timed
+    alike (CUDA events, L2 flushed between one-sweep steps)."""
+    import torch
+
+    from sc_gb300 import Surrogate, System, workloads
+
+    s = System.from_text(*workloads.psc_cpsc(65536, phi=0.2, seed=seed))
+    t0 = time.perf_counter()
+    s.simulate(nsweeps=melt, seed=seed, check_every=0)
+    melt_s = time.perf_counter() - t0
+    sur = Surrogate(s, seed=seed, capacity=12_000_000)
+    t0 = time.perf_counter()
+    for k in range(snapshots):
+        s.simulate(nsweeps=gap, seed=seed + 1 + k, check_every=0)
+        sur.collect(s)
+    collect_s = time.perf_counter() - t0
+    tr, losses = sur.train(epochs=epochs, batch=8192, lr=2e-3, warmup_steps=200, seed=seed)
+    s.simulate(nsweeps=gap, seed=seed + 999, check_every=0)
+    ev = sur.evaluate(s)                 # a configuration the network was not trained on
+    s.set_surrogate(sur)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    run_seed = seed + 4242
+
+    def timed(delayed):
+        s.simulate(nsweeps=3, seed=run_seed, check_every=0, delayed=delayed)
+        dev = 0.0
+        tot = dict(moves=0, acc=0, s1=0, s2=0, s2rej=0, err2=0.0, launches=0)
+        for _ in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            st = s.simulate(nsweeps=1, seed=run_seed, check_every=0, delayed=delayed)
+            dev += st.seconds
+            tot["moves"] += st.moves
+            tot["acc"] += st.acc_trans + st.acc_rot
+            tot["s1"] += st.da_stage1_rejected
+            tot["s2"] += st.da_stage2_tried
+            tot["s2rej"] += st.da_stage2_rejected
+            tot["err2"] += st.da_err_rms ** 2 * st.da_stage2_tried
+            tot["launches"] += st.launches
+        tot["rate"] = tot["moves"] / dev
+        return tot
+
+    plain = timed(0)
+    da = timed(1)
+    s.set_surrogate(None)
+    sur.close()
+    s.close()
+    return {"workload": "psc_cpsc_65536", "particles": 65536, "sweeps_timed": steps,
+            "plain_moves_per_s": plain["rate"], "delayed_moves_per_s": da["rate"],
+            "speedup": da["rate"] / plain["rate"],
+            "acceptance_plain": plain["acc"] / plain["moves"], "acceptance_delayed": da["acc"] / da["moves"],
+            "stage1_decided": da["s1"] / da["moves"],
+            "stage2_acceptance": 1.0 - da["s2rej"] / max(1, da["s2"]),
+            "move_dE_error_rms": math.sqrt(da["err2"] / max(1, da["s2"])),
+            "pair_error_vs_fp64": {"rmse": ev["rmse"], "mae": ev["mae"], "max_abs": ev["max_abs"],
+                                   "pairs": ev["pairs"]},
+            "training": {"samples": tr.samples, "epochs": epochs, "steps": tr.steps, "seconds": tr.seconds,
+                         "mse_first_batch": tr.loss_first, "mse_last_batch": tr.loss_last,
+                         "collect_seconds": collect_s, "melt_seconds": melt_s, "melt_sweeps": melt}}
+
+
 def main():
     a = parse()
     rank, world, local = dist_info()
     if a.impl == "reference":
         run_reference(a, rank, world)
+        return
+    if a.only in ("replicas", "surrogate"):
+        if rank == 0:
+            fn = bench_replicas if a.only == "replicas" else bench_surrogate
+            print(json.dumps({a.only: fn(200 if a.only == "replicas" else a.steps, seed=a.seed)}), flush=True)
         return
     import numpy as np
     import torch
@@ -377,12 +448,16 @@ def main():
         except Exception as ex:  # the baseline is reported, not required
             cpu = {"value": None, "unit": UNIT, "cores": 1, "kind": "port", "sample": f"failed: {ex}"}
 
-    replicas = None
-    if rank == 0 and not a.no_e2e:
+    replicas = surrogate = None
+    if rank == 0 and a.only == "all" and not a.no_e2e:
         try:
             replicas = bench_replicas(200, seed=a.seed)
         except Exception as ex:
             replicas = {"error": str(ex)}
+        try:
+            surrogate = bench_surrogate(max(5, a.steps // 2), seed=a.seed)
+        except Exception as ex:
+            surrogate = {"error": str(ex)}
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
                 "warmup": a.warmup, "ms_per_step": 1e3 * t_max / a.steps, "higher_is_better": True,
@@ -391,7 +466,7 @@ def main():
                            "parallelism": "replicas" if world > 1 else "single", "l2": "flushed between steps",
                            "seed": a.seed, "plain_fp64": True},
                 "clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roof, "fp64": fp64,
-                "cpu_baseline": cpu, "replicas": replicas,
+                "cpu_baseline": cpu, "replicas": replicas, "surrogate": surrogate,
                 "detail": {"acceptance": acc / max(1, moves), "pairs_tested_per_move": tested / max(1, moves),
                            "pairs_evaluated_per_move": evaluated / max(1, moves)}}
         print(json.dumps(line), flush=True)

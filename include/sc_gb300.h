@@ -82,7 +82,7 @@ typedef struct {
     int check_every;        /* sweeps between exact total-energy checks (0: none) */
     int time_phases;        /* 1: time the move kernels with CUDA events (adds events to the stream) */
     int stencil;            /* cell-list reach s: cells >= maxcut/s wide, (s+1)^3 colours; 0: chosen by the tuner */
-    int pad_;
+    int delayed;            /* 1: two-stage moves with the context's surrogate (sc_set_surrogate) as first stage */
 } sc_run_params;
 
 typedef struct {
@@ -100,6 +100,12 @@ typedef struct {
     double phase_seconds;    /* device time inside the move kernels (time_phases = 1) */
     long phase_launches;     /* move-kernel launches */
     long launches;           /* all kernels this call launched */
+    /* delayed acceptance (delayed = 1) */
+    long da_stage1_rejected; /* moves rejected by the surrogate stage (no exact energy evaluated) */
+    long da_stage2_tried;    /* moves that reached the exact stage */
+    long da_stage2_rejected;
+    double da_err_rms;       /* rms of dE - dEs over the moves that reached the exact stage */
+    double da_err_mean;      /* mean of dE - dEs over the same moves */
 } sc_run_stats;
 
 const char* sc_last_error(void);
@@ -192,6 +198,62 @@ int sc_replicas_create(sc_context* const* systems, int nrep, const double* tempe
 int sc_replicas_run(sc_replicas* r, const sc_run_params* p, int exchange_every, sc_run_stats* stats,
                     double* temperatures, double* energies, long* exchanges_tried, long* exchanges_accepted);
 int sc_replicas_destroy(sc_replicas* r);
+
+/* --- learned pair-energy surrogate and delayed acceptance ------------------------------------
+ * No counterpart in the reference.  A small network (16 -> 64 -> 64 -> 64 -> 1, SiLU, BF16
+ * weights, FP32 accumulation on the tensor cores) learns, per ordered SC-SC pair closer
+ * than the largest patch cut-off, the exact pair energy minus the FP32 WCA of the segment
+ * distance.  With delayed = 1 a move is first tested with the surrogate's energy change
+ * dEs and only then with the exact FP64 change dE against exp(-(dE - dEs)/T): the chain
+ * samples the exact Boltzmann distribution, and moves the first stage rejects never
+ * evaluate an exact pair energy.  A surrogate belongs to the types of the context it was
+ * created from and lives on that context's device. */
+typedef struct sc_surrogate sc_surrogate;
+typedef struct {
+    int epochs;
+    int batch;              /* rows per step, a multiple of 64 */
+    double lr;              /* peak Adam learning rate */
+    double lr_final;        /* end of the cosine decay (0: lr / 50) */
+    int warmup_steps;       /* linear warm-up */
+    int pad_;
+    unsigned long long seed;
+} sc_train_params;
+typedef struct {
+    long steps;
+    long samples;
+    double loss_first;      /* mean squared error of the first step's batch */
+    double loss_last;       /* and of the last step's batch */
+    double seconds;         /* host wall time of the training call */
+} sc_train_stats;
+/* capacity: training samples the surrogate can hold (68 bytes each on the device) */
+int sc_surrogate_create(sc_context* ctx, unsigned long long seed, long capacity, sc_surrogate** out);
+int sc_surrogate_destroy(sc_surrogate* s);
+/* Appends the samples of ctx's current configuration (every ordered SC-SC pair within
+ * range: features and exact FP64 pair energy - WCA32); *total = samples held. */
+int sc_surrogate_collect(sc_surrogate* s, sc_context* ctx, long* total);
+int sc_surrogate_num_samples(const sc_surrogate* s, long* n);
+/* Mini-batch Adam on the collected samples; loss_per_epoch (may be NULL) gets the last
+ * batch's mean squared error of each epoch. */
+int sc_surrogate_train(sc_surrogate* s, const sc_train_params* p, double* loss_per_epoch, sc_train_stats* stats);
+/* Network error against the exact energies of ctx's current configuration. */
+int sc_surrogate_evaluate(sc_surrogate* s, sc_context* ctx, double* rmse, double* mae, double* max_abs, long* npairs);
+/* FP32 master weights, 9409 floats: W1[16][64] (row 12 = first-layer bias, rows 13-15
+ * unused), W2[64][64], b2[64], W3[64][64], b3[64], W4[64], b4. */
+int sc_surrogate_get_weights(sc_surrogate* s, float* theta);
+int sc_surrogate_set_weights(sc_surrogate* s, const float* theta);
+/* One forward/backward on the tensor cores over n given rows (16 inputs each): gradient of
+ * the mean squared error with respect to the 9409 masters, and that error. */
+int sc_surrogate_gradient(sc_surrogate* s, int n, const float* inputs, const float* targets, float* grad,
+                          double* loss);
+/* Network outputs of n given rows (the move kernel's forward). */
+int sc_surrogate_predict(sc_surrogate* s, int n, const float* inputs, float* out);
+/* The 16 inputs, WCA32 and eligibility (1: SC-SC, not bonded, within range) of ordered pairs
+ * (i[k] moved, j[k] neighbour), as the move kernel computes them. */
+int sc_pair_features(sc_context* ctx, int npairs, const int* i, const int* j, float* inputs, float* wca,
+                     int* eligible);
+/* Attaches s (NULL detaches) as the first stage of ctx's delayed-acceptance moves; s must
+ * outlive the attachment. */
+int sc_set_surrogate(sc_context* ctx, sc_surrogate* s);
 
 #ifdef __cplusplus
 }

@@ -4,4 +4,4 @@ The energy and move path of SC (robertvacha/SC) behind a C ABI (include/sc_gb300
 implemented as hand-written CUDA kernels; this package is the Python host mirror.
 """
 from ._lib import ScError, load  # noqa: F401
-from .system import ReplicaSet, System  # noqa: F401
+from .system import ReplicaSet, Surrogate, System  # noqa: F401

@@ -44,7 +44,7 @@ class RunParams(C.Structure):
                 ("ptype", C.c_int), ("volume_every", C.c_int), ("transmx", C.c_double), ("rot_angle", C.c_double),
                 ("edge_mx", C.c_double), ("chainprob", C.c_double), ("chainmmx", C.c_double),
                 ("chain_angle", C.c_double), ("check_every", C.c_int), ("time_phases", C.c_int),
-                ("stencil", C.c_int), ("pad_", C.c_int)]
+                ("stencil", C.c_int), ("delayed", C.c_int)]
 
 
 class RunStats(C.Structure):
@@ -52,13 +52,26 @@ class RunStats(C.Structure):
                                         "acc_vol", "rej_vol", "vol_constrained", "acc_chain", "rej_chain",
                                         "pairs_tested", "pairs_evaluated")] + [
         (k, C.c_double) for k in ("energy", "energy_check", "max_drift", "seconds", "phase_seconds")] + [
-        ("phase_launches", C.c_long), ("launches", C.c_long)]
+        ("phase_launches", C.c_long), ("launches", C.c_long),
+        ("da_stage1_rejected", C.c_long), ("da_stage2_tried", C.c_long), ("da_stage2_rejected", C.c_long),
+        ("da_err_rms", C.c_double), ("da_err_mean", C.c_double)]
+
+
+class TrainParams(C.Structure):
+    _fields_ = [("epochs", C.c_int), ("batch", C.c_int), ("lr", C.c_double), ("lr_final", C.c_double),
+                ("warmup_steps", C.c_int), ("pad_", C.c_int), ("seed", C.c_ulonglong)]
+
+
+class TrainStats(C.Structure):
+    _fields_ = [("steps", C.c_long), ("samples", C.c_long), ("loss_first", C.c_double), ("loss_last", C.c_double),
+                ("seconds", C.c_double)]
 
 
 # (name, restype, argtypes) for every entry point of include/sc_gb300.h
 _P = C.c_void_p
 _D = C.POINTER(C.c_double)
 _I = C.POINTER(C.c_int)
+_F = C.POINTER(C.c_float)
 SIGNATURES = [
     ("sc_last_error", C.c_char_p, []),
     ("sc_version", C.c_char_p, []),
@@ -90,6 +103,18 @@ SIGNATURES = [
     ("sc_replicas_run", C.c_int, [_P, C.POINTER(RunParams), C.c_int, C.POINTER(RunStats), _D, _D,
                                   C.POINTER(C.c_long), C.POINTER(C.c_long)]),
     ("sc_replicas_destroy", C.c_int, [_P]),
+    ("sc_surrogate_create", C.c_int, [_P, C.c_ulonglong, C.c_long, C.POINTER(_P)]),
+    ("sc_surrogate_destroy", C.c_int, [_P]),
+    ("sc_surrogate_collect", C.c_int, [_P, _P, C.POINTER(C.c_long)]),
+    ("sc_surrogate_num_samples", C.c_int, [_P, C.POINTER(C.c_long)]),
+    ("sc_surrogate_train", C.c_int, [_P, C.POINTER(TrainParams), _D, C.POINTER(TrainStats)]),
+    ("sc_surrogate_evaluate", C.c_int, [_P, _P, _D, _D, _D, C.POINTER(C.c_long)]),
+    ("sc_surrogate_get_weights", C.c_int, [_P, _F]),
+    ("sc_surrogate_set_weights", C.c_int, [_P, _F]),
+    ("sc_surrogate_gradient", C.c_int, [_P, C.c_int, _F, _F, _F, _D]),
+    ("sc_surrogate_predict", C.c_int, [_P, C.c_int, _F, _F]),
+    ("sc_pair_features", C.c_int, [_P, C.c_int, _I, _I, _F, _F, _I]),
+    ("sc_set_surrogate", C.c_int, [_P, _P]),
 ]
 
 _lib = None

@@ -14,6 +14,8 @@ namespace scg {
 
 struct SweepEngine;   // sweep.cu: device state of the move loop
 struct Batch;         // sweep.cu: systems moved together
+struct Surrogate;     // surrogate.cu: learned pair-energy surrogate
+struct MlpPacked;     // surrogate.cuh: its BF16 weights in mma fragment order
 
 struct Context {
     Options opts;
@@ -45,6 +47,7 @@ struct Context {
     int trialTarget = -1;
     Particle trialState;
 
+    Surrogate* surrogate = nullptr;   // first stage of delayed-acceptance moves (not owned)
     SweepEngine* engine = nullptr;
     Batch* batch = nullptr;
     long lastLaunches = 0;     // kernels launched by the last move loop
@@ -65,6 +68,9 @@ struct Context {
 };
 
 int fail(int code, const std::string& msg);
+const MlpPacked* surrogatePacked(const Surrogate* s);
+float surrogateCutoff(const Surrogate* s);
+float surrogateRange(Context* c);
 int cudaFail(cudaError_t e, const char* where);
 int runSweeps(Context* c, const sc_run_params& p, sc_run_stats& st);
 void destroyEngine(Context* c);

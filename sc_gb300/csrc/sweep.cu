@@ -45,6 +45,7 @@
 #include "pair_energy.cuh"
 #include "philox.cuh"
 #include "sc_context.h"
+#include "surrogate.cuh"
 
 namespace scg {
 
@@ -61,7 +62,7 @@ constexpr int kMaxColours = 64;
 constexpr size_t kDynSmem = (size_t)kCandCap * (sizeof(float4) + sizeof(int));
 
 enum Ctr { C_ACC_T, C_REJ_T, C_ACC_R, C_REJ_R, C_ACC_V, C_REJ_V, C_VOL_CONSTR, C_TESTED, C_EVAL, C_CELL_REJ, C_MOVES,
-           C_SCREENED, C_COUNT };
+           C_SCREENED, C_S1_REJ, C_S2_TRIED, C_S2_REJ, C_COUNT };
 enum ErrBit { E_CELL_OVERFLOW = 1, E_PARTNER_FAR = 2 };
 
 struct Grid {
@@ -86,6 +87,7 @@ struct Control {
     double energy;        // running total energy
     double energyCheck;   // last exact total energy
     double maxDrift;
+    double daErr2, daErrSum;   // sums of (dE - dEs)^2 and dE - dEs over moves reaching the exact stage
 };
 
 struct SweepArgs {
@@ -109,6 +111,8 @@ struct SweepArgs {
     double edgeMx;
     double trans[MAX_DEV_TYPES];
     int geo[MAX_DEV_TYPES];
+    const MlpPacked* mlp;   // delayed acceptance: the surrogate's weights (nullptr: plain moves)
+    float rcutS;            // its range (FP32 segment distance)
 };
 
 __device__ __forceinline__ int wrapCell(double x, double shift, int nc) {
@@ -119,11 +123,6 @@ __device__ __forceinline__ int wrapCell(double x, double shift, int nc) {
     return c >= nc ? nc - 1 : (c < 0 ? 0 : c);
 }
 
-__device__ __forceinline__ float frac32(double x) {
-    double f = x - floor(x);
-    float v = (float)f;
-    return v >= 1.0f ? 0.0f : v;
-}
 
 // Distinct cells of the stencil along one dimension: -s..s, or every cell when the grid
 // is narrower than the stencil.
@@ -236,7 +235,7 @@ __global__ void kSortCells(const SweepArgs* __restrict__ A) {
     }
     for (int k = 0; k < n; ++k) {
         double4_32a p = a.s.pos[v[k]];
-        a.cellPosF[s + k] = make_float4(frac32(p.x), frac32(p.y), frac32(p.z), 0.0f);
+        a.cellPosF[s + k] = make_float4(frac32(p.x), frac32(p.y), frac32(p.z), (float)p.w);
     }
 }
 
@@ -441,9 +440,14 @@ struct MoveShared {
     Stencil st;
     Scan scan;
     double red[kWarps][2];
+    // surrogate stage: per-warp input rows, WCA32 and sign (+1 new, -1 old) of each row
+    float sx[kWarps][16][kFeat];
+    float swca[kWarps][16];
+    float ssign[kWarps][16];
+    float sred[kWarps];
     // current proposal
     int target, slotR, displace, skip, partners[4], nPartners;
-    double umet;
+    double umet, ustage1;
     double npos[3], ndir[3];
     float3 oldF, newF;
     PatchSet npatch;
@@ -531,11 +535,13 @@ __device__ void buildProposal(const SweepArgs& a, MoveShared& sh, int cell, int 
         else if (lane <= 8) { for (int q = 0; q < 3; ++q) sh.npatch.ch[lane - 7][q] = v[q]; }
     }
     double umet = r.next();
+    double ustage1 = r.next();      // delayed acceptance: uniform of the surrogate stage
     if (lane == 0) {
         sh.target = t;
         sh.slotR = slotR;
         sh.displace = displace;
         sh.umet = umet;
+        sh.ustage1 = ustage1;
         sh.npos[0] = npx; sh.npos[1] = npy; sh.npos[2] = npz;
         sh.oldF = make_float3(frac32(p.x), frac32(p.y), frac32(p.z));
         sh.newF = make_float3(frac32(npx), frac32(npy), frac32(npz));
@@ -556,6 +562,114 @@ __device__ void buildProposal(const SweepArgs& a, MoveShared& sh, int cell, int 
         sh.nPartners = np;
         sh.skip = skip;
     }
+}
+
+__device__ __forceinline__ float3 f3(double x, double y, double z) { return make_float3((float)x, (float)y, (float)z); }
+
+// Surrogate energy change of the proposal (new minus old, summed over the moved
+// particle's SC-SC pairs within rcutS; see surrogate.cuh).  Candidates are screened in
+// FP32 like stage A, the rows of pairs in range go through the tensor-core MLP 16 at a
+// time (warp w takes tiles w, w + 4, ...), and the sum is formed in a fixed order, so
+// the same configuration and proposal always give the same value.
+__device__ __noinline__ float surrogateDelta(const SweepArgs& a, MoveShared& sh, int* candIdx, float4* candPos, bool resident,
+                                int nCand, int t, bool displace, const int (&partners)[4], float3 oldF, float3 newF) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const float bx = (float)a.s.box[0], by = (float)a.s.box[1], bz = (float)a.s.box[2];
+    const float rc2 = a.rcutS * a.rcutS;
+    const double4_32a op = a.s.pos[t];
+    const double4_32a od = a.s.dir[t];
+    const PatchSet& ops = a.s.patch[t];
+    const float3 aOld = f3(od.x, od.y, od.z), pOld = f3(ops.pd[0][0], ops.pd[0][1], ops.pd[0][2]);
+    const float3 aNew = displace ? aOld : f3(sh.ndir[0], sh.ndir[1], sh.ndir[2]);
+    const float3 pNew = displace ? pOld : f3(sh.npatch.pd[0][0], sh.npatch.pd[0][1], sh.npatch.pd[0][2]);
+    const int ti = (int)op.w, nt = a.t.ntypes;
+    const float tci = typeCode(ti, nt);
+    float warpSum = 0.0f;
+    for (int wbase = 0; wbase < nCand; wbase += kCandCap) {
+        const int wend = min(wbase + kCandCap, nCand);
+        if (!resident) loadCandidates(a, sh.st, wbase, wend - wbase, candIdx, candPos);
+        for (int base = wbase; base < wend; base += kChunk) {
+            int qa = 0;
+            const int cend = min(base + kChunk, wend);
+            for (int r0 = base; r0 < cend; r0 += kMoveThreads) {
+                int k = r0 + tid - wbase;
+                int flags = 0;
+                if (r0 + tid < cend) {
+                    int j = candIdx[k];
+                    bool partner = (j == partners[0] || j == partners[1] || j == partners[2] || j == partners[3]);
+                    if (j != t && !partner) {
+                        float4 cp = candPos[k];
+                        const PairParam& pp = a.t.params[ti * nt + (int)cp.w];
+                        if (pp.screen == 1) {
+                            float h1 = (float)pp.half_len[0], h2 = (float)pp.half_len[1];
+                            float reach = a.rcutS + h1 + h2;
+                            float3 ro = pairVecF(oldF, cp, bx, by, bz);
+                            float3 rn = displace ? pairVecF(newF, cp, bx, by, bz) : ro;
+                            bool no = dotf(ro, ro) <= reach * reach, nn = dotf(rn, rn) <= reach * reach;
+                            if (no || nn) {
+                                double4_32a dj = a.s.dir[j];
+                                float3 aj = f3(dj.x, dj.y, dj.z);
+                                float s_, t_;
+                                float3 w_;
+                                if (no && segClosestF(ro, aOld, aj, h1, h2, s_, t_, w_) < rc2) flags |= 1;
+                                if (nn && segClosestF(rn, aNew, aj, h1, h2, s_, t_, w_) < rc2) flags |= 2;
+                            }
+                        }
+                    }
+                }
+                int total;
+                int off = blockExclusiveScan(__popc(flags), total, sh.scan);
+                if (flags & 1) sh.queueA[qa + off++] = k << 1;
+                if (flags & 2) sh.queueA[qa + off] = (k << 1) | 1;
+                qa += total;
+            }
+            __syncthreads();
+            for (int tile = warp; tile * 16 < qa; tile += kWarps) {
+                if (lane < 16) {
+                    int e = tile * 16 + lane;
+                    float* f = sh.sx[warp][lane];
+                    float wv = 0.0f, sign = 0.0f;
+                    if (e < qa) {
+                        int q = sh.queueA[e];
+                        int k = q >> 1;
+                        bool isNew = q & 1;
+                        int j = candIdx[k];
+                        float4 cp = candPos[k];
+                        int tj = (int)cp.w;
+                        const PairParam& pp = a.t.params[ti * nt + tj];
+                        float3 r = pairVecF(isNew ? newF : oldF, cp, bx, by, bz);
+                        double4_32a dj = a.s.dir[j];
+                        const PatchSet& pj = a.s.patch[j];
+                        float d2 = pairFeatures(r, isNew ? aNew : aOld, isNew ? pNew : pOld, (float)pp.half_len[0], tci,
+                                                f3(dj.x, dj.y, dj.z), f3(pj.pd[0][0], pj.pd[0][1], pj.pd[0][2]),
+                                                (float)pp.half_len[1], typeCode(tj, nt), f);
+                        wv = wca32(d2, (float)pp.sigma, (float)pp.epsilon, (float)pp.rcutwcaSq);
+                        sign = isNew ? 1.0f : -1.0f;
+                    } else {
+                        for (int c = 0; c < kFeat; ++c) f[c] = 0.0f;
+                    }
+                    sh.swca[warp][lane] = wv;
+                    sh.ssign[warp][lane] = sign;
+                }
+                __syncwarp();
+                float y0, y1;
+                mlpForward16(a.mlp, sh.sx[warp], y0, y1);
+                float v = 0.0f;
+                if ((lane & 3) == 0) {
+                    int g = lane >> 2;
+                    v = sh.ssign[warp][g] * (y0 + sh.swca[warp][g]) + sh.ssign[warp][g + 8] * (y1 + sh.swca[warp][g + 8]);
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                warpSum += v;
+                __syncwarp();
+            }
+            __syncthreads();            // queueA and the window are reused
+        }
+    }
+    if (lane == 0) sh.sred[warp] = warpSum;
+    __syncthreads();
+    return ((sh.sred[0] + sh.sred[1]) + sh.sred[2]) + sh.sred[3];
 }
 
 __device__ __forceinline__ void decodeActive(const Grid& g, int colour, int block, int& cx, int& cy, int& cz) {
@@ -592,6 +706,8 @@ __global__ void __launch_bounds__(kMoveThreads) kColour(const SweepArgs* __restr
     const float thr32 = candThreshold(c.sqmaxcut, box);
     double dECell = 0.0;
     unsigned long long nAccT = 0, nRejT = 0, nAccR = 0, nRejR = 0, nTested = 0, nEval = 0, nCellRej = 0, nScr = 0;
+    unsigned long long nS1Rej = 0, nS2Tried = 0, nS2Rej = 0;
+    double daErr2 = 0.0, daErrSum = 0.0;
 
     for (int m = 0; m < cnt; ++m) {
         if (warp == 0) buildProposal(a, sh, cell, cnt, m, cx, cy, cz, box);
@@ -621,6 +737,18 @@ __global__ void __launch_bounds__(kMoveThreads) kColour(const SweepArgs* __restr
         if (!displace) newV.patch = &sh.npatch;
         const Con con = makeCon(c, t, a.s.mol[t]);
         const float3 oldF = sh.oldF, newF = sh.newF;
+
+        // delayed acceptance, stage 1: the surrogate's energy change decides first
+        float dEs = 0.0f;
+        if (a.mlp) {
+            dEs = surrogateDelta(a, sh, candIdx, candPos, resident, nCand, t, displace, partners, oldF, newF);
+            bool pass = (dEs <= 0.0f) || (exp(-1.0 * (double)dEs / a.temper) > sh.ustage1);
+            if (!pass) {
+                if (tid == 0) { ++nS1Rej; if (displace) ++nRejT; else ++nRejR; }
+                __syncthreads();
+                continue;
+            }
+        }
 
         double eOld = 0.0, eNew = 0.0;
         if (tid < np) {     // bonded partners: both configurations, whatever the distance
@@ -716,15 +844,26 @@ __global__ void __launch_bounds__(kMoveThreads) kColour(const SweepArgs* __restr
         nTested += (unsigned long long)nCand * (displace ? 2 : 1);
         blockSum2(eOld, eNew, sh.red);
         if (tid == 0) {
-            // MoveCreator::moveTry (movecreator.h:175-187)
-            bool accept = (eNew <= eOld) || (exp(-1.0 * (eNew - eOld) / a.temper) > sh.umet);
+            // MoveCreator::moveTry (movecreator.h:175-187); with a surrogate stage the exact
+            // test is on dE - dEs
+            bool accept;
+            if (a.mlp) {
+                double x = (eNew - eOld) - (double)dEs;
+                accept = (x <= 0.0) || (exp(-1.0 * x / a.temper) > sh.umet);
+                ++nS2Tried;
+                if (!accept) ++nS2Rej;
+                daErr2 += x * x;
+                daErrSum += x;
+            } else {
+                accept = (eNew <= eOld) || (exp(-1.0 * (eNew - eOld) / a.temper) > sh.umet);
+            }
             if (accept) {
                 a.s.pos[t] = make_double4_32a(sh.npos[0], sh.npos[1], sh.npos[2], op4.w);
                 if (!displace) {
                     a.s.dir[t] = make_double4_32a(sh.ndir[0], sh.ndir[1], sh.ndir[2], od4.w);
                     a.s.patch[t] = sh.npatch;
                 } else {
-                    float4 nf = make_float4(newF.x, newF.y, newF.z, 0.0f);
+                    float4 nf = make_float4(newF.x, newF.y, newF.z, (float)op4.w);
                     if (resident) candPos[sh.st.ownOff + sh.slotR] = nf;
                     a.cellPosF[a.cellStart[cell] + sh.slotR] = nf;
                 }
@@ -746,6 +885,13 @@ __global__ void __launch_bounds__(kMoveThreads) kColour(const SweepArgs* __restr
         atomicAdd(&a.counters[C_MOVES], (unsigned long long)cnt);
         atomicAdd(&a.counters[C_TESTED], nTested);
         atomicAdd(&a.counters[C_EVAL], nEval);
+        if (a.mlp) {
+            atomicAdd(&a.counters[C_S1_REJ], nS1Rej);
+            atomicAdd(&a.counters[C_S2_TRIED], nS2Tried);
+            atomicAdd(&a.counters[C_S2_REJ], nS2Rej);
+            atomicAdd(&a.ctl->daErr2, daErr2);
+            atomicAdd(&a.ctl->daErrSum, daErrSum);
+        }
     }
     if (nScr) atomicAdd(&a.counters[C_SCREENED], nScr);
 }
@@ -1149,6 +1295,10 @@ static void fillArgs(Context* c, SweepEngine* e, const sc_run_params& p) {
         a.trans[k] = (base > 0 && perType != base) ? perType * (p.transmx / base) : p.transmx;
         a.geo[k] = c->topo.ia[t][t].geotype[0];
     }
+    if (p.delayed && c->surrogate) {
+        a.mlp = surrogatePacked(c->surrogate);
+        a.rcutS = surrogateCutoff(c->surrogate);
+    }
 }
 
 // Device state, grid and arguments of one system for a run with parameters p.
@@ -1187,6 +1337,7 @@ static int prepareSystem(Context* c, const sc_run_params& p, bool npt) {
     cudaMemset(e->counters, 0, sizeof(unsigned long long) * C_COUNT);
     cudaMemset(e->err, 0, sizeof(int));
     cudaMemset(&e->ctl->maxDrift, 0, sizeof(double));
+    cudaMemset(&e->ctl->daErr2, 0, 2 * sizeof(double));
     return SC_OK;
 }
 
@@ -1224,6 +1375,11 @@ static void collectStats(Context* c, sc_run_stats& st) {
     st.acc_vol = (long)ctr[C_ACC_V]; st.rej_vol = (long)ctr[C_REJ_V]; st.vol_constrained = (long)ctr[C_VOL_CONSTR];
     st.pairs_tested = (long)ctr[C_TESTED];
     st.pairs_evaluated = (long)ctr[C_EVAL];
+    st.da_stage1_rejected = (long)ctr[C_S1_REJ];
+    st.da_stage2_tried = (long)ctr[C_S2_TRIED];
+    st.da_stage2_rejected = (long)ctr[C_S2_REJ];
+    st.da_err_rms = ctr[C_S2_TRIED] ? std::sqrt(hc.daErr2 / (double)ctr[C_S2_TRIED]) : 0.0;
+    st.da_err_mean = ctr[C_S2_TRIED] ? hc.daErrSum / (double)ctr[C_S2_TRIED] : 0.0;
     st.energy = hc.energy;
     st.energy_check = hc.energyCheck;
     st.max_drift = hc.maxDrift;
@@ -1422,6 +1578,7 @@ int runSweeps(Context* c, const sc_run_params& p, sc_run_stats& st) {
     int rc = checkParams(p);
     if (rc) return rc;
     if (c->conf.p.empty()) return SC_OK;
+    if (p.delayed && !c->surrogate) return fail(SC_ERR_STATE, "delayed = 1 needs a surrogate (sc_set_surrogate)");
     const bool npt = p.ptype == 1 && p.volume_every > 0;
     if ((rc = prepareSystem(c, p, npt))) return rc;
     if (!c->batch) {
@@ -1509,7 +1666,8 @@ int runReplicas(void* h, const sc_run_params& p, int exchangeEvery, sc_run_stats
         sc_default_run(reinterpret_cast<const sc_context*>(c), &q);   // per-replica step sizes
         q.nsweeps = p.nsweeps; q.seed = p.seed + 0x9E3779B97F4A7C15ull * (unsigned long long)(k + 1);
         q.temper = R->temps[k]; q.ptype = p.ptype; q.volume_every = p.volume_every; q.check_every = p.check_every;
-        q.stencil = p.stencil; q.time_phases = p.time_phases; q.press = p.press;
+        q.stencil = p.stencil; q.time_phases = p.time_phases; q.press = p.press; q.delayed = p.delayed;
+        if (p.delayed && !c->surrogate) return fail(SC_ERR_STATE, "delayed = 1 needs a surrogate on every replica");
         if (p.transmx > 0) q.transmx = p.transmx;
         if (p.rot_angle > 0) q.rot_angle = p.rot_angle;
         if ((rc = prepareSystem(c, q, npt))) return rc;
@@ -1544,6 +1702,11 @@ int runReplicas(void* h, const sc_run_params& p, int exchangeEvery, sc_run_stats
         st.acc_rot += s1.acc_rot; st.rej_rot += s1.rej_rot;
         st.acc_vol += s1.acc_vol; st.rej_vol += s1.rej_vol; st.vol_constrained += s1.vol_constrained;
         st.pairs_tested += s1.pairs_tested; st.pairs_evaluated += s1.pairs_evaluated;
+        st.da_stage1_rejected += s1.da_stage1_rejected;
+        st.da_stage2_tried += s1.da_stage2_tried;
+        st.da_stage2_rejected += s1.da_stage2_rejected;
+        st.da_err_rms += s1.da_err_rms * s1.da_err_rms * (double)s1.da_stage2_tried;    // sum of squares for now
+        st.da_err_mean += s1.da_err_mean * (double)s1.da_stage2_tried;
         st.energy += s1.energy;
         st.max_drift = std::max(st.max_drift, s1.max_drift);
         if (tempsOut) tempsOut[k] = cur[k].temper;
@@ -1557,6 +1720,10 @@ int runReplicas(void* h, const sc_run_params& p, int exchangeEvery, sc_run_stats
             if (exTried) exTried[k] = (long)ctr[1 + 2 * k];
             if (exAcc) exAcc[k] = (long)ctr[2 + 2 * k];
         }
+    }
+    if (st.da_stage2_tried > 0) {
+        st.da_err_rms = std::sqrt(st.da_err_rms / (double)st.da_stage2_tried);
+        st.da_err_mean /= (double)st.da_stage2_tried;
     }
     st.sweeps = p.nsweeps;
     st.seconds = out.seconds;

@@ -23,6 +23,10 @@ def _iptr(a):
     return a.ctypes.data_as(C.POINTER(C.c_int))
 
 
+def _fptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
 class System:
     def __init__(self, handle):
         self._h = handle
@@ -148,6 +152,20 @@ class System:
                                           C.byref(b), C.byref(st)))
         return a.value, b.value, st
 
+    def pair_features(self, I, J):
+        """Surrogate inputs (n x 16), WCA32 and eligibility of ordered pairs (I moved, J)."""
+        I = np.ascontiguousarray(I, dtype=np.int32)
+        J = np.ascontiguousarray(J, dtype=np.int32)
+        n = len(I)
+        X = np.zeros((n, 16), dtype=np.float32)
+        W = np.zeros(n, dtype=np.float32)
+        E = np.zeros(n, dtype=np.int32)
+        L.check(self._lib.sc_pair_features(self._h, n, _iptr(I), _iptr(J), _fptr(X), _fptr(W), _iptr(E)))
+        return X, W, E.astype(bool)
+
+    def set_surrogate(self, sur):
+        L.check(self._lib.sc_set_surrogate(self._h, sur._h if sur is not None else None))
+
     def accept_trial(self):
         L.check(self._lib.sc_accept_trial(self._h))
 
@@ -209,6 +227,80 @@ class ReplicaSet:
     def close(self):
         if self._h:
             self._lib.sc_replicas_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Surrogate:
+    """Learned pair-energy surrogate (no counterpart in the reference): the first stage of
+    delayed-acceptance moves (``simulate(delayed=1)`` after ``system.set_surrogate``)."""
+
+    N_PARAMS = 9409
+
+    def __init__(self, system, seed=1, capacity=0):
+        self._lib = L.load()
+        h = C.c_void_p()
+        L.check(self._lib.sc_surrogate_create(system._h, int(seed), int(capacity), C.byref(h)))
+        self._h = h
+
+    def collect(self, system):
+        total = C.c_long()
+        L.check(self._lib.sc_surrogate_collect(self._h, system._h, C.byref(total)))
+        return total.value
+
+    @property
+    def num_samples(self):
+        v = C.c_long()
+        L.check(self._lib.sc_surrogate_num_samples(self._h, C.byref(v)))
+        return v.value
+
+    def train(self, epochs, batch=8192, lr=2e-3, lr_final=0.0, warmup_steps=100, seed=1):
+        p = L.TrainParams(epochs=epochs, batch=batch, lr=lr, lr_final=lr_final, warmup_steps=warmup_steps, seed=seed)
+        st = L.TrainStats()
+        losses = np.zeros(max(epochs, 1))
+        L.check(self._lib.sc_surrogate_train(self._h, C.byref(p), _dptr(losses), C.byref(st)))
+        return st, losses[:epochs]
+
+    def evaluate(self, system):
+        a, b, c = C.c_double(), C.c_double(), C.c_double()
+        n = C.c_long()
+        L.check(self._lib.sc_surrogate_evaluate(self._h, system._h, C.byref(a), C.byref(b), C.byref(c), C.byref(n)))
+        return {"rmse": a.value, "mae": b.value, "max_abs": c.value, "pairs": n.value}
+
+    @property
+    def weights(self):
+        w = np.zeros(self.N_PARAMS, dtype=np.float32)
+        L.check(self._lib.sc_surrogate_get_weights(self._h, _fptr(w)))
+        return w
+
+    @weights.setter
+    def weights(self, w):
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        assert w.shape == (self.N_PARAMS,)
+        L.check(self._lib.sc_surrogate_set_weights(self._h, _fptr(w)))
+
+    def gradient(self, X, y):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        g = np.zeros(self.N_PARAMS, dtype=np.float32)
+        loss = C.c_double()
+        L.check(self._lib.sc_surrogate_gradient(self._h, len(y), _fptr(X), _fptr(y), _fptr(g), C.byref(loss)))
+        return g, loss.value
+
+    def predict(self, X):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        out = np.zeros(len(X), dtype=np.float32)
+        L.check(self._lib.sc_surrogate_predict(self._h, len(X), _fptr(X), _fptr(out)))
+        return out
+
+    def close(self):
+        if self._h:
+            self._lib.sc_surrogate_destroy(self._h)
             self._h = None
 
     def __del__(self):

@@ -182,22 +182,35 @@ def psc_cpsc(n=65536, phi=0.2, seed=1, temper=1.0):
     return opts, top, config_text(box, pos, dirs, pds)
 
 
-def rods_in_spheres(n_spheres=3000, n_rods=2, L=6.0, phi=0.2, seed=1, temper=1.0):
-    """A few long PSC rods among many attractive spheres: the long cut-off makes cell
-    stencils of several thousand particles (the move kernel then stages its candidates
-    in windows)."""
+def rods_in_spheres(n_side=21, n_rods=2, L=6.0, edge=34.0, seed=1, temper=1.0):
+    """A few long PSC rods among many attractive spheres (SPA on a cubic lattice of
+    n_side^3 sites, minus the sites the rods overlap): the long cut-off gives 4 cells per
+    edge and cell stencils of several thousand particles, so the move kernel stages its
+    candidates in windows."""
     rng = np.random.default_rng(seed)
-    vol = n_spheres * math.pi / 6 + n_rods * _vol_sc(L)
-    box = np.full(3, (vol / phi) ** (1 / 3))
-    halfl = [L / 2] * n_rods + [0.0] * n_spheres
-    pos, dirs, pds = place(rng, halfl, box)
+    box = np.full(3, edge)
+    a = edge / n_side
+    g = (np.arange(n_side) + 0.5) * a
+    sites = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+    rpos = rng.uniform(0, edge, size=(n_rods, 3))
+    rdir = _unit(rng, n_rods)
+    keep = np.ones(len(sites), bool)
+    for c, d in zip(rpos, rdir):
+        r = sites - c
+        r -= box * np.round(r / box)
+        t = np.clip(r @ d, -L / 2, L / 2)
+        dist = np.linalg.norm(r - t[:, None] * d[None, :], axis=1)
+        keep &= dist > 1.05
+    sph = sites[keep]
+    pos = np.concatenate([rpos, sph])
+    dirs = np.concatenate([rdir, _unit(rng, len(sph))])
     top = ("[Types]\n"
            f"P 1 PSC 1.0 1.0 1.12 0.2 90.0 10.0 {L} 0.0\n"
            "A 2 SPA 0.5 1.0 1.1225 0.3775\n"
            "[Molecules]\nP: {\nparticles: 1\n}\nA: {\nparticles: 2\n}\n"
-           f"[System]\nP {n_rods}\nA {n_spheres}\n")
+           f"[System]\nP {n_rods}\nA {len(sph)}\n")
     opts = options_text(ptype=0, transmx=0.3, rotmx=20.0, temper=temper, seed=seed)
-    return opts, top, config_text(box, pos, dirs, pds)
+    return opts, top, config_text(box, pos, dirs, _perp(rng, dirs))
 
 
 def pt_ladders(n_ladders=8, per_ladder=8, seed=1, n_range=(500, 4000), phi_range=(0.10, 0.25), t_range=(0.8, 1.6)):

@@ -68,7 +68,7 @@ def test_stencil_larger_than_shared_memory_window():
     in windows, the running energy must stay exact."""
     from sc_gb300 import System, workloads
 
-    s = System.from_text(*workloads.rods_in_spheres(3000, seed=4))
+    s = System.from_text(*workloads.rods_in_spheres(seed=4))
     e0 = exact_energy(s)
     st = s.simulate(nsweeps=8, seed=2, check_every=4, stencil=1)
     assert st.moves == 8 * s.n and st.pairs_tested > 8 * s.n * 1100
