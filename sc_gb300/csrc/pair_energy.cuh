@@ -418,6 +418,45 @@ __device__ __forceinline__ double bondedTerms(const PairParam& ia, const PView& 
     return e;
 }
 
+// The three independent FP64 chains of a single-patch PSC/CPSC pair (scScEnergy below
+// with one patch combination), for evaluation by three threads side by side:
+//   role 0: closest segment distance and the WCA term, returns 0.0 + rep (no bond terms:
+//           callers pass non-bonded pairs only), *ok = the attractive branch is on;
+//   role 1: intersections of particle 2's axis with particle 1's patch (T, return na);
+//   role 2: intersections of particle 1's axis with particle 2's patch (S, return nb).
+// The pair energy is then  e0 + patchAttraction(...)  when ok && na >= 2 && nb >= 2, else
+// e0 + 0.0: bit-identical to scScEnergy, which evaluates the same chains in sequence.
+__device__ __forceinline__ double simpleScRole0(const PairParam& ia, const PView& a, const PView& b, const double3& r_cm,
+                                                int* ok) {
+    double3 md = minDistSegments(a.dir, b.dir, ia.half_len[0], ia.half_len[1], r_cm);
+    double distSq = dot3(md, md);
+    double rep = wcaTruncSq(distSq, ia);
+    *ok = !((distSq > ia.rcutSq) || (ia.epsilon == 0.0) || ia.exclude);
+    return 0.0 + rep;
+}
+__device__ __forceinline__ int simpleScRole1(const PairParam& ia, const PView& a, const PView& b, const double3& r_cm,
+                                             double* T) {
+    PatchV P1{ld3(a.patch->pd[0]), ld3(a.patch->ps[0]), ld3(a.patch->ps[1])};
+    return ia.firstPsc ? pscIntersect(a.dir, b.dir, P1, r_cm, T, ia.pcanglsw[0], ia.rcutSq, ia.half_len[0], ia.half_len[1])
+                       : cpscIntersect(a.dir, b.dir, P1, r_cm, T, ia.pcanglsw[0], ia.rcutSq, ia.half_len[0], ia.half_len[1]);
+}
+__device__ __forceinline__ int simpleScRole2(const PairParam& ia, const PView& a, const PView& b, const double3& r_cm,
+                                             double* S) {
+    PatchV P2{ld3(b.patch->pd[0]), ld3(b.patch->ps[0]), ld3(b.patch->ps[1])};
+    double3 mr = neg3(r_cm);
+    return ia.secondPsc ? pscIntersect(b.dir, a.dir, P2, mr, S, ia.pcanglsw[1], ia.rcutSq, ia.half_len[1], ia.half_len[0])
+                        : cpscIntersect(b.dir, a.dir, P2, mr, S, ia.pcanglsw[1], ia.rcutSq, ia.half_len[1], ia.half_len[0]);
+}
+__device__ __forceinline__ double simpleScCombine(const PairParam& ia, const PView& a, const PView& b,
+                                                  const double3& r_cm, double e0, int ok, int na, int nb, const double* T,
+                                                  const double* S) {
+    double atr = 0.0;
+    if (ok && na >= 2 && nb >= 2)
+        atr += patchAttraction(ia, a.dir, b.dir, ld3(a.patch->pd[0]), ld3(b.patch->pd[0]), r_cm, 0, 0, S[0], S[1], T[0],
+                               T[1]);
+    return e0 + atr;
+}
+
 // SC-SC pair (SpheroCylinder::operator(), paire.h:1122-1196).
 static __device__ __noinline__ double scScEnergy(const PairParam& ia, const PView& a, const PView& b, const double3& r_cm,
                                           double dist, const Con& con, const double3& box, unsigned* bits,

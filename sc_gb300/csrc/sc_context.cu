@@ -91,6 +91,8 @@ PairParam Context::devParam(int t1, int t2) const {
     } else if (p.kind == K_NONE) {
         p.screen = 3;
     }
+    p.simple = (p.kind == K_SC_PSC_CPSC || p.kind == K_SC_CPSC || p.kind == K_SC_PSC) && !p.fT && !p.sT && !p.fCH &&
+               !p.sCH;
     return p;
 }
 

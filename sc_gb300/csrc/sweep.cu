@@ -427,11 +427,22 @@ __device__ __forceinline__ float dist2f(float4 a, float3 b, const double3& box) 
 
 constexpr int kClassCap = 768;       // stage-C queue entries per pair class
 
-// Pair class of the stage-C queue: SC-SC, SC-sphere, everything else.  Entries of one
-// class are evaluated by consecutive threads, so a warp follows one functor's branches.
-__device__ __forceinline__ int pairClass(int kind) {
-    return (kind >= K_SC_PSC_CPSC && kind <= K_SC_SCA) ? 0 : (kind >= K_MIX_SCA_SPA ? 1 : 2);
+// Pair class of the stage-C queue: 0 single-patch PSC/CPSC pairs (evaluated as three
+// parallel chains), 1 SC-sphere, 2 everything else.  Each class is evaluated by its own
+// warps, so a warp follows one functor's branches.
+__device__ __forceinline__ int pairClass(const PairParam& pp) {
+    return pp.simple ? 0 : (pp.kind >= K_MIX_SCA_SPA ? 1 : 2);
 }
+
+// Barrier of warps 0-2 only (warp 3 keeps evaluating other pairs meanwhile).
+__device__ __forceinline__ void barWarps012() { asm volatile("bar.sync 1, 96;" ::: "memory"); }
+
+// Stage-C scratch of the three-chain evaluation of class-0 pairs, 32 pairs per round.
+struct SplitShared {
+    double T[32][2], S[32][2];
+    double e0[32];
+    int na[32], nb[32], ok[32];
+};
 
 struct MoveShared {
     int list[kCellCap];
@@ -440,6 +451,7 @@ struct MoveShared {
     Stencil st;
     Scan scan;
     double red[kWarps][2];
+    SplitShared split;
     // surrogate stage: per-warp input rows, WCA32 and sign (+1 new, -1 old) of each row
     float sx[kWarps][16][kFeat];
     float swca[kWarps][16];
@@ -758,15 +770,60 @@ __global__ void __launch_bounds__(kMoveThreads) kColour(const SweepArgs* __restr
             eNew += pairEnergy(c, newV, b, con, box, &bb, &dd);
         }
         int qb0 = 0, qb1 = 0, qb2 = 0;
-        auto flushC = [&]() {              // stage C: full FP64 pair energies, class by class
+        // one queue entry through the full pair energy
+        auto evalEntry = [&](int q) {
+            PView b = viewAt(a.s, candIdx[q >> 1]);
+            unsigned bb; double dd;
+            if (q & 1) eNew += pairEnergy(c, newV, b, con, box, &bb, &dd);
+            else eOld += pairEnergy(c, oldV, b, con, box, &bb, &dd);
+        };
+        // classes 1 and 2 over nw warps starting at warp w0; class 2 starts on a warp boundary
+        auto evalGeneric = [&](int w0, int nw) {
+            const int pad1 = (qb1 + 31) & ~31;
+            for (int g = (warp - w0) * 32 + (tid & 31); g < pad1 + qb2; g += nw * 32) {
+                if (g < pad1) { if (g < qb1) evalEntry(sh.queueB[1][g]); }
+                else evalEntry(sh.queueB[2][g - pad1]);
+            }
+        };
+        auto flushC = [&]() {              // stage C: exact FP64 pair energies
             __syncthreads();               // queue entries of every thread are visible
-            const int count = qb0 + qb1 + qb2;
-            for (int e = tid; e < count; e += kMoveThreads) {
-                int q = e < qb0 ? sh.queueB[0][e] : (e < qb0 + qb1 ? sh.queueB[1][e - qb0] : sh.queueB[2][e - qb0 - qb1]);
-                PView b = viewAt(a.s, candIdx[q >> 1]);
-                unsigned bb; double dd;
-                if (q & 1) eNew += pairEnergy(c, newV, b, con, box, &bb, &dd);
-                else eOld += pairEnergy(c, oldV, b, con, box, &bb, &dd);
+            const int lane = tid & 31;
+            if (qb0 > 0) {
+                if (warp < 3) {
+                    // class 0: warps 0, 1, 2 run the WCA chain and the two intersection
+                    // chains of 32 pairs side by side; warp 0 then adds the attraction
+                    for (int r0 = 0; r0 < qb0; r0 += 32) {
+                        const int k = r0 + lane;
+                        int q = 0, j = 0;
+                        if (k < qb0) {
+                            q = sh.queueB[0][k];
+                            j = candIdx[q >> 1];
+                            const PView& self = (q & 1) ? newV : oldV;
+                            PView b = viewAt(a.s, j);
+                            const PairParam& ia = c.params[self.type * c.ntypes + b.type];
+                            double3 r_cm = imageVec(self.pos, b.pos, box);
+                            if (warp == 0) sh.split.e0[lane] = simpleScRole0(ia, self, b, r_cm, &sh.split.ok[lane]);
+                            else if (warp == 1) sh.split.na[lane] = simpleScRole1(ia, self, b, r_cm, sh.split.T[lane]);
+                            else sh.split.nb[lane] = simpleScRole2(ia, self, b, r_cm, sh.split.S[lane]);
+                        }
+                        barWarps012();
+                        if (warp == 0 && k < qb0) {
+                            const PView& self = (q & 1) ? newV : oldV;
+                            PView b = viewAt(a.s, j);
+                            const PairParam& ia = c.params[self.type * c.ntypes + b.type];
+                            double3 r_cm = imageVec(self.pos, b.pos, box);
+                            double e = simpleScCombine(ia, self, b, r_cm, sh.split.e0[lane], sh.split.ok[lane],
+                                                       sh.split.na[lane], sh.split.nb[lane], sh.split.T[lane],
+                                                       sh.split.S[lane]);
+                            if (q & 1) eNew += e; else eOld += e;
+                        }
+                        barWarps012();
+                    }
+                } else {
+                    evalGeneric(3, 1);
+                }
+            } else {
+                evalGeneric(0, kWarps);
             }
             __syncthreads();
         };
@@ -812,7 +869,7 @@ __global__ void __launch_bounds__(kMoveThreads) kColour(const SweepArgs* __restr
                         double4_32a dj = a.s.dir[j];
                         const PairParam& pp = c.params[self.type * c.ntypes + (int)pj.w];
                         keep = screenedOut(pp, r, self.dir, mk(dj.x, dj.y, dj.z)) ? 0 : 1;
-                        cls = pairClass(pp.kind);
+                        cls = pairClass(pp);
                         if (!keep) ++nScr;
                     }
                 }
