@@ -444,6 +444,17 @@ struct SplitShared {
     int na[32], nb[32], ok[32];
 };
 
+// One move's proposal.  thrMet / thrStage1: the move is accepted when dE <= 0 or
+// dE < thr, thr = -T ln(u) -- the reference's exp(-dE/T) > u (movecreator.h:175-187)
+// with the logarithm taken while the proposal is built, off the critical path.
+struct Proposal {
+    int target, slotR, displace, skip, partners[4], nPartners;
+    double thrMet, thrStage1;
+    double npos[3], ndir[3];
+    float3 oldF, newF;
+    PatchSet npatch;
+};
+
 struct MoveShared {
     int list[kCellCap];
     int queueA[kQueueCap];
@@ -457,12 +468,9 @@ struct MoveShared {
     float swca[kWarps][16];
     float ssign[kWarps][16];
     float sred[kWarps];
-    // current proposal
-    int target, slotR, displace, skip, partners[4], nPartners;
-    double umet, ustage1;
-    double npos[3], ndir[3];
-    float3 oldF, newF;
-    PatchSet npatch;
+    // proposals of the current and (speculatively) the next move
+    Proposal prop[2];
+    int specMove;       // move whose proposal prop[specMove & 1] already holds (-1: none)
 };
 
 __device__ __forceinline__ void randomUnitSphere(Stream& r, double& x, double& y, double& z) {
@@ -481,8 +489,8 @@ __device__ __forceinline__ void randomUnitSphere(Stream& r, double& x, double& y
 // lane forms the rotation matrix, lane k rotates vector k (axis, patch directions, patch
 // sides, chiral axes), then patchdir[0] is re-orthogonalised against the new axis as
 // partRotate does (movecreator.cpp:1007).
-__device__ void buildProposal(const SweepArgs& a, MoveShared& sh, int cell, int cnt, int m, int cx, int cy, int cz,
-                              const double3& box) {
+__device__ void buildProposal(const SweepArgs& a, const MoveShared& sh, Proposal& P, int cell, int cnt, int m, int cx,
+                              int cy, int cz, const double3& box) {
     const Control& ctl = *a.ctl;
     const int lane = threadIdx.x & 31;
     Stream r(a.seed, (uint32_t)cell, (uint32_t)m, (uint32_t)ctl.sweep ^ ((uint32_t)(ctl.sweep >> 32) << 20));
@@ -505,7 +513,7 @@ __device__ void buildProposal(const SweepArgs& a, MoveShared& sh, int cell, int 
         int ny = wrapCell(npy, ctl.shift[1], a.g.nc[1]);
         int nz = wrapCell(npz, ctl.shift[2], a.g.nc[2]);
         if (nx != cx || ny != cy || nz != cz) skip = 1;     // would leave the cell
-        if (lane == 0) { sh.ndir[0] = d.x; sh.ndir[1] = d.y; sh.ndir[2] = d.z; }
+        if (lane == 0) { P.ndir[0] = d.x; P.ndir[1] = d.y; P.ndir[2] = d.z; }
     } else {
         double angle = a.rotAngle * r.next();
         double ax, ay, az;
@@ -541,22 +549,18 @@ __device__ void buildProposal(const SweepArgs& a, MoveShared& sh, int cell, int 
             double dp = v[0] * dx + v[1] * dy + v[2] * dz;
             v[0] -= dp * dx; v[1] -= dp * dy; v[2] -= dp * dz;
         }
-        if (lane == 0) { sh.ndir[0] = v[0]; sh.ndir[1] = v[1]; sh.ndir[2] = v[2]; }
-        else if (lane <= 2) { for (int q = 0; q < 3; ++q) sh.npatch.pd[lane - 1][q] = v[q]; }
-        else if (lane <= 6) { for (int q = 0; q < 3; ++q) sh.npatch.ps[lane - 3][q] = v[q]; }
-        else if (lane <= 8) { for (int q = 0; q < 3; ++q) sh.npatch.ch[lane - 7][q] = v[q]; }
+        if (lane == 0) { P.ndir[0] = v[0]; P.ndir[1] = v[1]; P.ndir[2] = v[2]; }
+        else if (lane <= 2) { for (int q = 0; q < 3; ++q) P.npatch.pd[lane - 1][q] = v[q]; }
+        else if (lane <= 6) { for (int q = 0; q < 3; ++q) P.npatch.ps[lane - 3][q] = v[q]; }
+        else if (lane <= 8) { for (int q = 0; q < 3; ++q) P.npatch.ch[lane - 7][q] = v[q]; }
     }
-    double umet = r.next();
-    double ustage1 = r.next();      // delayed acceptance: uniform of the surrogate stage
     if (lane == 0) {
-        sh.target = t;
-        sh.slotR = slotR;
-        sh.displace = displace;
-        sh.umet = umet;
-        sh.ustage1 = ustage1;
-        sh.npos[0] = npx; sh.npos[1] = npy; sh.npos[2] = npz;
-        sh.oldF = make_float3(frac32(p.x), frac32(p.y), frac32(p.z));
-        sh.newF = make_float3(frac32(npx), frac32(npy), frac32(npz));
+        P.target = t;
+        P.slotR = slotR;
+        P.displace = displace;
+        P.npos[0] = npx; P.npos[1] = npy; P.npos[2] = npz;
+        P.oldF = make_float3(frac32(p.x), frac32(p.y), frac32(p.z));
+        P.newF = make_float3(frac32(npx), frac32(npy), frac32(npz));
         // bonded partners are evaluated explicitly; they must sit inside the stencil
         DevCtx c;
         c.mols = a.t.mols;
@@ -569,12 +573,25 @@ __device__ void buildProposal(const SweepArgs& a, MoveShared& sh, int cell, int 
             bool near = false;
             for (int w = 0; w < sh.st.nNb; ++w) near |= (sh.st.nbCell[w] == cj);
             if (!near) { atomicOr(a.err, E_PARTNER_FAR); skip = 1; }
-            sh.partners[np++] = j;
+            P.partners[np++] = j;
         }
-        sh.nPartners = np;
-        sh.skip = skip;
+        P.nPartners = np;
+        P.skip = skip;
     }
 }
+
+// The uniforms of the acceptance tests come from their own Philox stream, so that one
+// lane can turn them into thresholds while another warp builds the proposal.
+__device__ void acceptThresholds(const SweepArgs& a, Proposal& P, int cell, int m) {
+    const Control& ctl = *a.ctl;
+    Stream r(a.seed ^ 0xD1B54A32D192ED03ull, (uint32_t)cell, (uint32_t)m,
+             (uint32_t)ctl.sweep ^ ((uint32_t)(ctl.sweep >> 32) << 20));
+    double u = r.next(), u1 = r.next();
+    P.thrMet = -a.temper * log(u);        // +inf for u = 0: always accepted, as exp(.) > 0
+    P.thrStage1 = -a.temper * log(u1);
+}
+
+
 
 __device__ __forceinline__ float3 f3(double x, double y, double z) { return make_float3((float)x, (float)y, (float)z); }
 
@@ -583,8 +600,9 @@ __device__ __forceinline__ float3 f3(double x, double y, double z) { return make
 // FP32 like stage A, the rows of pairs in range go through the tensor-core MLP 16 at a
 // time (warp w takes tiles w, w + 4, ...), and the sum is formed in a fixed order, so
 // the same configuration and proposal always give the same value.
-__device__ __noinline__ float surrogateDelta(const SweepArgs& a, MoveShared& sh, int* candIdx, float4* candPos, bool resident,
-                                int nCand, int t, bool displace, const int (&partners)[4], float3 oldF, float3 newF) {
+__device__ __noinline__ float surrogateDelta(const SweepArgs& a, MoveShared& sh, const Proposal& P, int* candIdx,
+                                             float4* candPos, bool resident, int nCand, int t, bool displace,
+                                             const int (&partners)[4], float3 oldF, float3 newF) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const float bx = (float)a.s.box[0], by = (float)a.s.box[1], bz = (float)a.s.box[2];
     const float rc2 = a.rcutS * a.rcutS;
@@ -592,8 +610,8 @@ __device__ __noinline__ float surrogateDelta(const SweepArgs& a, MoveShared& sh,
     const double4_32a od = a.s.dir[t];
     const PatchSet& ops = a.s.patch[t];
     const float3 aOld = f3(od.x, od.y, od.z), pOld = f3(ops.pd[0][0], ops.pd[0][1], ops.pd[0][2]);
-    const float3 aNew = displace ? aOld : f3(sh.ndir[0], sh.ndir[1], sh.ndir[2]);
-    const float3 pNew = displace ? pOld : f3(sh.npatch.pd[0][0], sh.npatch.pd[0][1], sh.npatch.pd[0][2]);
+    const float3 aNew = displace ? aOld : f3(P.ndir[0], P.ndir[1], P.ndir[2]);
+    const float3 pNew = displace ? pOld : f3(P.npatch.pd[0][0], P.npatch.pd[0][1], P.npatch.pd[0][2]);
     const int ti = (int)op.w, nt = a.t.ntypes;
     const float tci = typeCode(ti, nt);
     float warpSum = 0.0f;
@@ -721,19 +739,24 @@ __global__ void __launch_bounds__(kMoveThreads) kColour(const SweepArgs* __restr
     unsigned long long nS1Rej = 0, nS2Tried = 0, nS2Rej = 0;
     double daErr2 = 0.0, daErrSum = 0.0;
 
+    if (tid == 0) sh.specMove = -1;
     for (int m = 0; m < cnt; ++m) {
-        if (warp == 0) buildProposal(a, sh, cell, cnt, m, cx, cy, cz, box);
+        Proposal& P = sh.prop[m & 1];
+        if (sh.specMove != m) {         // no speculative proposal for this move
+            if (warp == 0) buildProposal(a, sh, P, cell, cnt, m, cx, cy, cz, box);
+            else if (tid == 32) acceptThresholds(a, P, cell, m);
+        }
         __syncthreads();
-        const int t = sh.target;
-        const bool displace = sh.displace;
-        if (sh.skip) {
+        const int t = P.target;
+        const bool displace = P.displace;
+        if (P.skip) {
             if (tid == 0) { if (displace) { ++nRejT; ++nCellRej; } else ++nRejR; }
             __syncthreads();
             continue;
         }
-        const int np = sh.nPartners;
+        const int np = P.nPartners;
         int partners[4] = {-1, -1, -1, -1};
-        for (int q = 0; q < np; ++q) partners[q] = sh.partners[q];
+        for (int q = 0; q < np; ++q) partners[q] = P.partners[q];
         const double4_32a op4 = a.s.pos[t];
         const double4_32a od4 = a.s.dir[t];
         PView oldV;
@@ -744,17 +767,17 @@ __global__ void __launch_bounds__(kMoveThreads) kColour(const SweepArgs* __restr
         oldV.index = t;
         oldV.molType = 0;
         PView newV = oldV;
-        newV.pos = mk(sh.npos[0], sh.npos[1], sh.npos[2]);
-        newV.dir = mk(sh.ndir[0], sh.ndir[1], sh.ndir[2]);
-        if (!displace) newV.patch = &sh.npatch;
+        newV.pos = mk(P.npos[0], P.npos[1], P.npos[2]);
+        newV.dir = mk(P.ndir[0], P.ndir[1], P.ndir[2]);
+        if (!displace) newV.patch = &P.npatch;
         const Con con = makeCon(c, t, a.s.mol[t]);
-        const float3 oldF = sh.oldF, newF = sh.newF;
+        const float3 oldF = P.oldF, newF = P.newF;
 
         // delayed acceptance, stage 1: the surrogate's energy change decides first
         float dEs = 0.0f;
         if (a.mlp) {
-            dEs = surrogateDelta(a, sh, candIdx, candPos, resident, nCand, t, displace, partners, oldF, newF);
-            bool pass = (dEs <= 0.0f) || (exp(-1.0 * (double)dEs / a.temper) > sh.ustage1);
+            dEs = surrogateDelta(a, sh, P, candIdx, candPos, resident, nCand, t, displace, partners, oldF, newF);
+            bool pass = (dEs <= 0.0f) || ((double)dEs < P.thrStage1);
             if (!pass) {
                 if (tid == 0) { ++nS1Rej; if (displace) ++nRejT; else ++nRejR; }
                 __syncthreads();
@@ -779,15 +802,27 @@ __global__ void __launch_bounds__(kMoveThreads) kColour(const SweepArgs* __restr
         };
         // classes 1 and 2 over nw warps starting at warp w0; class 2 starts on a warp boundary
         auto evalGeneric = [&](int w0, int nw) {
+            if (warp < w0 || warp >= w0 + nw) return;
             const int pad1 = (qb1 + 31) & ~31;
             for (int g = (warp - w0) * 32 + (tid & 31); g < pad1 + qb2; g += nw * 32) {
                 if (g < pad1) { if (g < qb1) evalEntry(sh.queueB[1][g]); }
                 else evalEntry(sh.queueB[2][g - pad1]);
             }
         };
-        auto flushC = [&]() {              // stage C: exact FP64 pair energies
+        // warp 3 builds the next move's proposal while stage C runs (it stays valid unless
+        // this move is accepted and the next one picks the same particle)
+        auto speculate = [&]() {
+            Proposal& N = sh.prop[(m + 1) & 1];
+            buildProposal(a, sh, N, cell, cnt, m + 1, cx, cy, cz, box);
+            if ((tid & 31) == 0) {
+                acceptThresholds(a, N, cell, m + 1);
+                sh.specMove = m + 1;
+            }
+        };
+        auto flushC = [&](bool last) {     // stage C: exact FP64 pair energies
             __syncthreads();               // queue entries of every thread are visible
             const int lane = tid & 31;
+            const bool spec = last && m + 1 < cnt;
             if (qb0 > 0) {
                 if (warp < 3) {
                     // class 0: warps 0, 1, 2 run the WCA chain and the two intersection
@@ -820,8 +855,12 @@ __global__ void __launch_bounds__(kMoveThreads) kColour(const SweepArgs* __restr
                         barWarps012();
                     }
                 } else {
+                    if (spec) speculate();
                     evalGeneric(3, 1);
                 }
+            } else if (spec) {
+                if (warp == 3) speculate();
+                else evalGeneric(0, 3);
             } else {
                 evalGeneric(0, kWarps);
             }
@@ -884,19 +923,19 @@ __global__ void __launch_bounds__(kMoveThreads) kColour(const SweepArgs* __restr
                 qb1 += (total >> 10) & 1023;
                 qb2 += (total >> 20) & 1023;
                 if (qb0 > kClassCap - kMoveThreads || qb1 > kClassCap - kMoveThreads || qb2 > kClassCap - kMoveThreads) {
-                    flushC();
+                    flushC(false);
                     nEval += qb0 + qb1 + qb2;
                     qb0 = qb1 = qb2 = 0;
                 }
             }
           }
           if (!resident) {      // queue entries index the window: evaluate them before it changes
-              flushC();
+              flushC(false);
               nEval += qb0 + qb1 + qb2;
               qb0 = qb1 = qb2 = 0;
           }
         }
-        flushC();
+        flushC(true);
         nEval += qb0 + qb1 + qb2 + 2 * np;
         nTested += (unsigned long long)nCand * (displace ? 2 : 1);
         blockSum2(eOld, eNew, sh.red);
@@ -906,26 +945,28 @@ __global__ void __launch_bounds__(kMoveThreads) kColour(const SweepArgs* __restr
             bool accept;
             if (a.mlp) {
                 double x = (eNew - eOld) - (double)dEs;
-                accept = (x <= 0.0) || (exp(-1.0 * x / a.temper) > sh.umet);
+                accept = (x <= 0.0) || (x < P.thrMet);
                 ++nS2Tried;
                 if (!accept) ++nS2Rej;
                 daErr2 += x * x;
                 daErrSum += x;
             } else {
-                accept = (eNew <= eOld) || (exp(-1.0 * (eNew - eOld) / a.temper) > sh.umet);
+                accept = (eNew <= eOld) || ((eNew - eOld) < P.thrMet);
             }
             if (accept) {
-                a.s.pos[t] = make_double4_32a(sh.npos[0], sh.npos[1], sh.npos[2], op4.w);
+                a.s.pos[t] = make_double4_32a(P.npos[0], P.npos[1], P.npos[2], op4.w);
                 if (!displace) {
-                    a.s.dir[t] = make_double4_32a(sh.ndir[0], sh.ndir[1], sh.ndir[2], od4.w);
-                    a.s.patch[t] = sh.npatch;
+                    a.s.dir[t] = make_double4_32a(P.ndir[0], P.ndir[1], P.ndir[2], od4.w);
+                    a.s.patch[t] = P.npatch;
                 } else {
                     float4 nf = make_float4(newF.x, newF.y, newF.z, (float)op4.w);
-                    if (resident) candPos[sh.st.ownOff + sh.slotR] = nf;
-                    a.cellPosF[a.cellStart[cell] + sh.slotR] = nf;
+                    if (resident) candPos[sh.st.ownOff + P.slotR] = nf;
+                    a.cellPosF[a.cellStart[cell] + P.slotR] = nf;
                 }
                 dECell += eNew - eOld;
                 if (displace) ++nAccT; else ++nAccR;
+                // the next move's speculative proposal read this particle's old state
+                if (sh.specMove == m + 1 && sh.prop[(m + 1) & 1].target == t) sh.specMove = -1;
             } else {
                 if (displace) ++nRejT; else ++nRejR;
             }
