@@ -56,13 +56,14 @@ constexpr int kWarps = kMoveThreads / 32;
 constexpr int kCellCap = 256;        // particles per cell
 constexpr int kNbCap = 343;          // stencil cells, (2*3+1)^3
 constexpr int kCandCap = 1024;       // candidates staged in shared memory at a time
-constexpr int kQueueCap = 1536;      // pair queue entries
+constexpr int kQueueCap = 2048;      // pair queue entries (old + new of a full window)
 constexpr int kChunk = 512;          // candidates per stage-A round
 constexpr int kMaxColours = 64;
 constexpr size_t kDynSmem = (size_t)kCandCap * (sizeof(float4) + sizeof(int));
+constexpr size_t kDynSmemSurrogate = kDynSmem + (size_t)kCandCap * 2 * sizeof(float4);   // + FP32 axes, patches
 
 enum Ctr { C_ACC_T, C_REJ_T, C_ACC_R, C_REJ_R, C_ACC_V, C_REJ_V, C_VOL_CONSTR, C_TESTED, C_EVAL, C_CELL_REJ, C_MOVES,
-           C_SCREENED, C_S1_REJ, C_S2_TRIED, C_S2_REJ, C_COUNT };
+           C_SCREENED, C_S1_REJ, C_S2_TRIED, C_S2_REJ, C_ACC_CH, C_REJ_CH, C_CH_CONSTR, C_COUNT };
 enum ErrBit { E_CELL_OVERFLOW = 1, E_PARTNER_FAR = 2 };
 
 struct Grid {
@@ -100,6 +101,8 @@ struct SweepArgs {
     int* cellCursor;
     int* cellIdx;
     float4* cellPosF;     // wrapped box fractions of cellIdx, FP32
+    float4* cellDirF;     // FP32 axis and first patch direction of cellIdx (surrogate inputs;
+    float4* cellPatF;     // written only when a surrogate is attached)
     int* cellOf;
     double* cellDE;
     double* partial;      // per-cell energy sums
@@ -113,6 +116,18 @@ struct SweepArgs {
     int geo[MAX_DEV_TYPES];
     const MlpPacked* mlp;   // delayed acceptance: the surrogate's weights (nullptr: plain moves)
     float rcutS;            // its range (FP32 segment distance)
+    // chain moves (records of the chain grid; see kChainColour)
+    double* energyAcc;      // where kEndSweep adds the sweep's energy change (nullptr: ctl->energy)
+    const int2* chains;     // first particle, size of each chain
+    int nChains;
+    int* chainCellStart;
+    int* chainCellCount;
+    int* chainCellIdx;
+    double chainMx;         // chain displacement length
+    double chainAngle;      // chain rotation angle bound
+    double chainFrac;       // chain move attempts per chain per sweep
+    double chainR;          // bound on |particle - chain centre| (real space) the grid was sized for
+    double volW[MAX_DEV_TYPES];   // Ia_param volume of each type (clusterCM weights)
 };
 
 __device__ __forceinline__ int wrapCell(double x, double shift, int nc) {
@@ -236,6 +251,12 @@ __global__ void kSortCells(const SweepArgs* __restrict__ A) {
     for (int k = 0; k < n; ++k) {
         double4_32a p = a.s.pos[v[k]];
         a.cellPosF[s + k] = make_float4(frac32(p.x), frac32(p.y), frac32(p.z), (float)p.w);
+        if (a.mlp) {
+            double4_32a d = a.s.dir[v[k]];
+            const PatchSet& ps = a.s.patch[v[k]];
+            a.cellDirF[s + k] = make_float4((float)d.x, (float)d.y, (float)d.z, 0.0f);
+            a.cellPatF[s + k] = make_float4((float)ps.pd[0][0], (float)ps.pd[0][1], (float)ps.pd[0][2], 0.0f);
+        }
     }
 }
 
@@ -336,7 +357,7 @@ __device__ void stageStencil(const SweepArgs& a, int cx, int cy, int cz, Stencil
 // Loads candidates [first, first + count) of the stencil into shared memory (count <=
 // kCandCap).  A stencil larger than the buffer is processed in windows of kCandCap.
 __device__ void loadCandidates(const SweepArgs& a, const Stencil& st, int first, int count, int* candIdx,
-                               float4* candPos) {
+                               float4* candPos, float4* candDir = nullptr, float4* candPat = nullptr) {
     const int nn = st.nNb;
     for (int kk = threadIdx.x; kk < count; kk += kMoveThreads) {
         int k = first + kk;
@@ -348,6 +369,10 @@ __device__ void loadCandidates(const SweepArgs& a, const Stencil& st, int first,
         int slot = a.cellStart[st.nbCell[lo]] + (k - st.nbOff[lo]);
         candIdx[kk] = a.cellIdx[slot];
         candPos[kk] = a.cellPosF[slot];
+        if (candDir) {
+            candDir[kk] = a.cellDirF[slot];
+            candPat[kk] = a.cellPatF[slot];
+        }
     }
     __syncthreads();
 }
@@ -595,111 +620,124 @@ __device__ void acceptThresholds(const SweepArgs& a, Proposal& P, int cell, int 
 
 __device__ __forceinline__ float3 f3(double x, double y, double z) { return make_float3((float)x, (float)y, (float)z); }
 
-// Surrogate energy change of the proposal (new minus old, summed over the moved
-// particle's SC-SC pairs within rcutS; see surrogate.cuh).  Candidates are screened in
-// FP32 like stage A, the rows of pairs in range go through the tensor-core MLP 16 at a
-// time (warp w takes tiles w, w + 4, ...), and the sum is formed in a fixed order, so
-// the same configuration and proposal always give the same value.
-__device__ __noinline__ float surrogateDelta(const SweepArgs& a, MoveShared& sh, const Proposal& P, int* candIdx,
-                                             float4* candPos, bool resident, int nCand, int t, bool displace,
-                                             const int (&partners)[4], float3 oldF, float3 newF) {
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+// The moved particle as the surrogate sees it (FP32, old and new orientation).
+struct MovedF {
+    float3 aOld, pOld, aNew, pNew;
+    int type;
+    float tc;
+};
+
+// Surrogate screen of candidate k (shared-memory slot): bit 0 the old, bit 1 the new
+// configuration of the moved particle lies within rcutS of it (FP32 segment distance).
+__device__ __forceinline__ int surrogateScreen(const SweepArgs& a, const MovedF& mv, float4 cp, float4 cd,
+                                               bool displace, float3 oldF, float3 newF, float bx, float by, float bz) {
+    const PairParam& pp = a.t.params[mv.type * a.t.ntypes + (int)cp.w];
+    if (pp.screen != 1) return 0;
+    float h1 = (float)pp.half_len[0], h2 = (float)pp.half_len[1];
+    float reach = a.rcutS + h1 + h2;
+    float3 ro = pairVecF(oldF, cp, bx, by, bz);
+    float3 rn = displace ? pairVecF(newF, cp, bx, by, bz) : ro;
+    bool no = dotf(ro, ro) <= reach * reach, nn = dotf(rn, rn) <= reach * reach;
+    int flags = 0;
+    if (no || nn) {
+        float3 aj = make_float3(cd.x, cd.y, cd.z);
+        const float rc2 = a.rcutS * a.rcutS;
+        float s_, t_;
+        float3 w_;
+        if (no && segClosestF(ro, mv.aOld, aj, h1, h2, s_, t_, w_) < rc2) flags |= 1;
+        if (nn && segClosestF(rn, mv.aNew, aj, h1, h2, s_, t_, w_) < rc2) flags |= 2;
+    }
+    return flags;
+}
+
+// Network rows of queue entries queue[0..n) (slot << 1 | new): warp w takes tiles w, w + 4,
+// ...; returns this warp's share of sum(sign * (WCA32 + MLP)), summed in a fixed order.
+__device__ __noinline__ float surrogateTiles(const SweepArgs& a, MoveShared& sh, const MovedF& mv, const int* queue, int n,
+                                const float4* candPos, const float4* candDir, const float4* candPat, float3 oldF,
+                                float3 newF) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const float bx = (float)a.s.box[0], by = (float)a.s.box[1], bz = (float)a.s.box[2];
-    const float rc2 = a.rcutS * a.rcutS;
-    const double4_32a op = a.s.pos[t];
-    const double4_32a od = a.s.dir[t];
-    const PatchSet& ops = a.s.patch[t];
-    const float3 aOld = f3(od.x, od.y, od.z), pOld = f3(ops.pd[0][0], ops.pd[0][1], ops.pd[0][2]);
-    const float3 aNew = displace ? aOld : f3(P.ndir[0], P.ndir[1], P.ndir[2]);
-    const float3 pNew = displace ? pOld : f3(P.npatch.pd[0][0], P.npatch.pd[0][1], P.npatch.pd[0][2]);
-    const int ti = (int)op.w, nt = a.t.ntypes;
-    const float tci = typeCode(ti, nt);
+    const int nt = a.t.ntypes;
+    float warpSum = 0.0f;
+    for (int tile = warp; tile * 16 < n; tile += kWarps) {
+        if (lane < 16) {
+            int e = tile * 16 + lane;
+            float* f = sh.sx[warp][lane];
+            float wv = 0.0f, sign = 0.0f;
+            if (e < n) {
+                int q = queue[e];
+                int k = q >> 1;
+                bool isNew = q & 1;
+                float4 cp = candPos[k], cd = candDir[k], cq = candPat[k];
+                int tj = (int)cp.w;
+                const PairParam& pp = a.t.params[mv.type * nt + tj];
+                float3 r = pairVecF(isNew ? newF : oldF, cp, bx, by, bz);
+                float d2 = pairFeatures(r, isNew ? mv.aNew : mv.aOld, isNew ? mv.pNew : mv.pOld, (float)pp.half_len[0],
+                                        mv.tc, make_float3(cd.x, cd.y, cd.z), make_float3(cq.x, cq.y, cq.z),
+                                        (float)pp.half_len[1], typeCode(tj, nt), f);
+                wv = wca32(d2, (float)pp.sigma, (float)pp.epsilon, (float)pp.rcutwcaSq);
+                sign = isNew ? 1.0f : -1.0f;
+            } else {
+                for (int c = 0; c < kFeat; ++c) f[c] = 0.0f;
+            }
+            sh.swca[warp][lane] = wv;
+            sh.ssign[warp][lane] = sign;
+        }
+        __syncwarp();
+        float y0, y1;
+        mlpForward16(a.mlp, sh.sx[warp], y0, y1);
+        float v = 0.0f;
+        if ((lane & 3) == 0) {
+            int g = lane >> 2;
+            v = sh.ssign[warp][g] * (y0 + sh.swca[warp][g]) + sh.ssign[warp][g + 8] * (y1 + sh.swca[warp][g + 8]);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        warpSum += v;
+        __syncwarp();
+    }
+    return warpSum;
+}
+
+// The per-warp sums of the surrogate stage, added in a fixed order.
+__device__ __forceinline__ float surrogateTotal(MoveShared& sh, float warpSum) {
+    if ((threadIdx.x & 31) == 0) sh.sred[threadIdx.x >> 5] = warpSum;
+    __syncthreads();
+    return ((sh.sred[0] + sh.sred[1]) + sh.sred[2]) + sh.sred[3];
+}
+
+// Surrogate energy change of the proposal when the stencil does not fit in shared memory:
+// the candidates window by window (the resident case fuses this screen into stage A).
+__device__ __noinline__ float surrogateDeltaWindows(const SweepArgs& a, MoveShared& sh, const MovedF& mv,
+                                                    int* candIdx, float4* candPos, float4* candDir, float4* candPat,
+                                                    int nCand, int t, bool displace, const int (&partners)[4],
+                                                    float3 oldF, float3 newF) {
+    const int tid = threadIdx.x;
+    const float bx = (float)a.s.box[0], by = (float)a.s.box[1], bz = (float)a.s.box[2];
     float warpSum = 0.0f;
     for (int wbase = 0; wbase < nCand; wbase += kCandCap) {
         const int wend = min(wbase + kCandCap, nCand);
-        if (!resident) loadCandidates(a, sh.st, wbase, wend - wbase, candIdx, candPos);
-        for (int base = wbase; base < wend; base += kChunk) {
-            int qa = 0;
-            const int cend = min(base + kChunk, wend);
-            for (int r0 = base; r0 < cend; r0 += kMoveThreads) {
-                int k = r0 + tid - wbase;
-                int flags = 0;
-                if (r0 + tid < cend) {
-                    int j = candIdx[k];
-                    bool partner = (j == partners[0] || j == partners[1] || j == partners[2] || j == partners[3]);
-                    if (j != t && !partner) {
-                        float4 cp = candPos[k];
-                        const PairParam& pp = a.t.params[ti * nt + (int)cp.w];
-                        if (pp.screen == 1) {
-                            float h1 = (float)pp.half_len[0], h2 = (float)pp.half_len[1];
-                            float reach = a.rcutS + h1 + h2;
-                            float3 ro = pairVecF(oldF, cp, bx, by, bz);
-                            float3 rn = displace ? pairVecF(newF, cp, bx, by, bz) : ro;
-                            bool no = dotf(ro, ro) <= reach * reach, nn = dotf(rn, rn) <= reach * reach;
-                            if (no || nn) {
-                                double4_32a dj = a.s.dir[j];
-                                float3 aj = f3(dj.x, dj.y, dj.z);
-                                float s_, t_;
-                                float3 w_;
-                                if (no && segClosestF(ro, aOld, aj, h1, h2, s_, t_, w_) < rc2) flags |= 1;
-                                if (nn && segClosestF(rn, aNew, aj, h1, h2, s_, t_, w_) < rc2) flags |= 2;
-                            }
-                        }
-                    }
-                }
-                int total;
-                int off = blockExclusiveScan(__popc(flags), total, sh.scan);
-                if (flags & 1) sh.queueA[qa + off++] = k << 1;
-                if (flags & 2) sh.queueA[qa + off] = (k << 1) | 1;
-                qa += total;
+        loadCandidates(a, sh.st, wbase, wend - wbase, candIdx, candPos, candDir, candPat);
+        int qs = 0;
+        for (int r0 = wbase; r0 < wend; r0 += kMoveThreads) {
+            int k = r0 + tid - wbase;
+            int flags = 0;
+            if (r0 + tid < wend) {
+                int j = candIdx[k];
+                bool partner = (j == partners[0] || j == partners[1] || j == partners[2] || j == partners[3]);
+                if (j != t && !partner) flags = surrogateScreen(a, mv, candPos[k], candDir[k], displace, oldF, newF, bx, by, bz);
             }
-            __syncthreads();
-            for (int tile = warp; tile * 16 < qa; tile += kWarps) {
-                if (lane < 16) {
-                    int e = tile * 16 + lane;
-                    float* f = sh.sx[warp][lane];
-                    float wv = 0.0f, sign = 0.0f;
-                    if (e < qa) {
-                        int q = sh.queueA[e];
-                        int k = q >> 1;
-                        bool isNew = q & 1;
-                        int j = candIdx[k];
-                        float4 cp = candPos[k];
-                        int tj = (int)cp.w;
-                        const PairParam& pp = a.t.params[ti * nt + tj];
-                        float3 r = pairVecF(isNew ? newF : oldF, cp, bx, by, bz);
-                        double4_32a dj = a.s.dir[j];
-                        const PatchSet& pj = a.s.patch[j];
-                        float d2 = pairFeatures(r, isNew ? aNew : aOld, isNew ? pNew : pOld, (float)pp.half_len[0], tci,
-                                                f3(dj.x, dj.y, dj.z), f3(pj.pd[0][0], pj.pd[0][1], pj.pd[0][2]),
-                                                (float)pp.half_len[1], typeCode(tj, nt), f);
-                        wv = wca32(d2, (float)pp.sigma, (float)pp.epsilon, (float)pp.rcutwcaSq);
-                        sign = isNew ? 1.0f : -1.0f;
-                    } else {
-                        for (int c = 0; c < kFeat; ++c) f[c] = 0.0f;
-                    }
-                    sh.swca[warp][lane] = wv;
-                    sh.ssign[warp][lane] = sign;
-                }
-                __syncwarp();
-                float y0, y1;
-                mlpForward16(a.mlp, sh.sx[warp], y0, y1);
-                float v = 0.0f;
-                if ((lane & 3) == 0) {
-                    int g = lane >> 2;
-                    v = sh.ssign[warp][g] * (y0 + sh.swca[warp][g]) + sh.ssign[warp][g + 8] * (y1 + sh.swca[warp][g + 8]);
-                }
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-                warpSum += v;
-                __syncwarp();
-            }
-            __syncthreads();            // queueA and the window are reused
+            int total;
+            int off = blockExclusiveScan(__popc(flags), total, sh.scan);
+            if (flags & 1) sh.queueA[qs + off++] = k << 1;
+            if (flags & 2) sh.queueA[qs + off] = (k << 1) | 1;
+            qs += total;
         }
+        __syncthreads();
+        warpSum += surrogateTiles(a, sh, mv, sh.queueA, qs, candPos, candDir, candPat, oldF, newF);
+        __syncthreads();            // queueA and the window are reused
     }
-    if (lane == 0) sh.sred[warp] = warpSum;
-    __syncthreads();
-    return ((sh.sred[0] + sh.sred[1]) + sh.sred[2]) + sh.sred[3];
+    return surrogateTotal(sh, warpSum);
 }
 
 __device__ __forceinline__ void decodeActive(const Grid& g, int colour, int block, int& cx, int& cy, int& cz) {
@@ -711,10 +749,13 @@ __device__ __forceinline__ void decodeActive(const Grid& g, int colour, int bloc
 
 __global__ void __launch_bounds__(kMoveThreads) kColour(const SweepArgs* __restrict__ A, int phase) {
     extern __shared__ float4 dynSmem[];
-    float4* candPos = dynSmem;
-    int* candIdx = reinterpret_cast<int*>(candPos + kCandCap);
     __shared__ MoveShared sh;
     const SweepArgs& a = A[blockIdx.y];
+    float4* candPos = dynSmem;
+    int* candIdx = reinterpret_cast<int*>(candPos + kCandCap);
+    // with a surrogate: FP32 axes and patch directions of the candidates as well
+    float4* candDir = a.mlp ? reinterpret_cast<float4*>(candIdx + kCandCap) : nullptr;
+    float4* candPat = a.mlp ? candDir + kCandCap : nullptr;
     const Control& ctl = *a.ctl;
     const Grid& g = a.g;
     if ((int)blockIdx.x >= g.nactive || phase >= g.ncolours) return;
@@ -728,7 +769,7 @@ __global__ void __launch_bounds__(kMoveThreads) kColour(const SweepArgs* __restr
     stageStencil(a, cx, cy, cz, sh.st, sh.scan);
     const int nCand = sh.st.nCand;
     const bool resident = nCand <= kCandCap;
-    if (resident) loadCandidates(a, sh.st, 0, nCand, candIdx, candPos);
+    if (resident) loadCandidates(a, sh.st, 0, nCand, candIdx, candPos, candDir, candPat);
 
     DevCtx c;
     c.params = a.t.params; c.mols = a.t.mols; c.ntypes = a.t.ntypes; c.n = a.s.n; c.sqmaxcut = a.t.sqmaxcut;
@@ -775,8 +816,52 @@ __global__ void __launch_bounds__(kMoveThreads) kColour(const SweepArgs* __restr
 
         // delayed acceptance, stage 1: the surrogate's energy change decides first
         float dEs = 0.0f;
+        int qaFused = -1;               // >= 0: stage A was fused into the surrogate screen
         if (a.mlp) {
-            dEs = surrogateDelta(a, sh, P, candIdx, candPos, resident, nCand, t, displace, partners, oldF, newF);
+            MovedF mv;
+            const PatchSet& ops = a.s.patch[t];
+            mv.aOld = f3(od4.x, od4.y, od4.z);
+            mv.pOld = f3(ops.pd[0][0], ops.pd[0][1], ops.pd[0][2]);
+            mv.aNew = displace ? mv.aOld : f3(P.ndir[0], P.ndir[1], P.ndir[2]);
+            mv.pNew = displace ? mv.pOld : f3(P.npatch.pd[0][0], P.npatch.pd[0][1], P.npatch.pd[0][2]);
+            mv.type = (int)op4.w;
+            mv.tc = typeCode(mv.type, c.ntypes);
+            if (resident) {
+                // one pass over the candidates: stage A's screen and the surrogate's
+                const float bx = (float)box.x, by = (float)box.y, bz = (float)box.z;
+                int* queueS = &sh.queueB[0][0];
+                int qa = 0, qs = 0;
+                for (int r0 = 0; r0 < nCand; r0 += kMoveThreads) {
+                    const int k = r0 + tid;
+                    int flags = 0, sflags = 0;
+                    if (k < nCand) {
+                        int j = candIdx[k];
+                        bool partner = (j == partners[0] || j == partners[1] || j == partners[2] || j == partners[3]);
+                        if (j != t && !partner) {
+                            float4 cp = candPos[k];
+                            bool p0 = dist2f(cp, oldF, box) <= thr32;
+                            bool p1 = displace ? dist2f(cp, newF, box) <= thr32 : p0;
+                            flags = (p0 ? 1 : 0) | (p1 ? 2 : 0);
+                            sflags = surrogateScreen(a, mv, cp, candDir[k], displace, oldF, newF, bx, by, bz);
+                        }
+                    }
+                    int total;
+                    int off = blockExclusiveScan(__popc(flags) | (__popc(sflags) << 16), total, sh.scan);
+                    int oa = off & 0xFFFF, os = off >> 16;
+                    if (flags & 1) sh.queueA[qa + oa++] = k << 1;
+                    if (flags & 2) sh.queueA[qa + oa] = (k << 1) | 1;
+                    if (sflags & 1) queueS[qs + os++] = k << 1;
+                    if (sflags & 2) queueS[qs + os] = (k << 1) | 1;
+                    qa += total & 0xFFFF;
+                    qs += total >> 16;
+                }
+                __syncthreads();
+                dEs = surrogateTotal(sh, surrogateTiles(a, sh, mv, queueS, qs, candPos, candDir, candPat, oldF, newF));
+                qaFused = qa;
+            } else {
+                dEs = surrogateDeltaWindows(a, sh, mv, candIdx, candPos, candDir, candPat, nCand, t, displace, partners,
+                                            oldF, newF);
+            }
             bool pass = (dEs <= 0.0f) || ((double)dEs < P.thrStage1);
             if (!pass) {
                 if (tid == 0) { ++nS1Rej; if (displace) ++nRejT; else ++nRejR; }
@@ -866,35 +951,8 @@ __global__ void __launch_bounds__(kMoveThreads) kColour(const SweepArgs* __restr
             }
             __syncthreads();
         };
-        for (int wbase = 0; wbase < nCand; wbase += kCandCap) {
-          // candidates in shared memory: all of them, or the window [wbase, wend)
-          const int wend = min(wbase + kCandCap, nCand);
-          if (!resident) loadCandidates(a, sh.st, wbase, wend - wbase, candIdx, candPos);
-          for (int base = wbase; base < wend; base += kChunk) {
-            // stage A: FP32 minimum image against the old and the new position
-            int qa = 0;
-            const int cend = min(base + kChunk, wend);
-            for (int r0 = base; r0 < cend; r0 += kMoveThreads) {
-                int k = r0 + tid - wbase;   // index in the shared-memory window
-                int flags = 0;
-                if (r0 + tid < cend) {
-                    int j = candIdx[k];
-                    bool partner = (j == partners[0] || j == partners[1] || j == partners[2] || j == partners[3]);
-                    if (j != t && !partner) {
-                        float4 cp = candPos[k];
-                        bool p0 = dist2f(cp, oldF, box) <= thr32;
-                        bool p1 = displace ? dist2f(cp, newF, box) <= thr32 : p0;
-                        flags = (p0 ? 1 : 0) | (p1 ? 2 : 0);
-                    }
-                }
-                int total;
-                int off = blockExclusiveScan(__popc(flags), total, sh.scan);
-                if (flags & 1) sh.queueA[qa + off++] = k << 1;
-                if (flags & 2) sh.queueA[qa + off] = (k << 1) | 1;
-                qa += total;
-            }
-            __syncthreads();
-            // stage B: FP64 prefilter (bit-exact) and the exact-zero screen
+        // stage B over queueA[0, qa): FP64 prefilter (bit-exact) and the exact-zero screen
+        auto stageB = [&](int qa) {
             for (int e0 = 0; e0 < qa; e0 += kMoveThreads) {
                 int e = e0 + tid;
                 int keep = 0, q = 0, cls = 0;
@@ -928,12 +986,46 @@ __global__ void __launch_bounds__(kMoveThreads) kColour(const SweepArgs* __restr
                     qb0 = qb1 = qb2 = 0;
                 }
             }
-          }
-          if (!resident) {      // queue entries index the window: evaluate them before it changes
-              flushC(false);
-              nEval += qb0 + qb1 + qb2;
-              qb0 = qb1 = qb2 = 0;
-          }
+        };
+        if (qaFused >= 0) {
+            stageB(qaFused);
+        } else {
+            for (int wbase = 0; wbase < nCand; wbase += kCandCap) {
+              // candidates in shared memory: all of them, or the window [wbase, wend)
+              const int wend = min(wbase + kCandCap, nCand);
+              if (!resident) loadCandidates(a, sh.st, wbase, wend - wbase, candIdx, candPos);
+              for (int base = wbase; base < wend; base += kChunk) {
+                // stage A: FP32 minimum image against the old and the new position
+                int qa = 0;
+                const int cend = min(base + kChunk, wend);
+                for (int r0 = base; r0 < cend; r0 += kMoveThreads) {
+                    int k = r0 + tid - wbase;   // index in the shared-memory window
+                    int flags = 0;
+                    if (r0 + tid < cend) {
+                        int j = candIdx[k];
+                        bool partner = (j == partners[0] || j == partners[1] || j == partners[2] || j == partners[3]);
+                        if (j != t && !partner) {
+                            float4 cp = candPos[k];
+                            bool p0 = dist2f(cp, oldF, box) <= thr32;
+                            bool p1 = displace ? dist2f(cp, newF, box) <= thr32 : p0;
+                            flags = (p0 ? 1 : 0) | (p1 ? 2 : 0);
+                        }
+                    }
+                    int total;
+                    int off = blockExclusiveScan(__popc(flags), total, sh.scan);
+                    if (flags & 1) sh.queueA[qa + off++] = k << 1;
+                    if (flags & 2) sh.queueA[qa + off] = (k << 1) | 1;
+                    qa += total;
+                }
+                __syncthreads();
+                stageB(qa);
+              }
+              if (!resident) {      // queue entries index the window: evaluate them before it changes
+                  flushC(false);
+                  nEval += qb0 + qb1 + qb2;
+                  qb0 = qb1 = qb2 = 0;
+              }
+            }
         }
         flushC(true);
         nEval += qb0 + qb1 + qb2 + 2 * np;
@@ -958,6 +1050,17 @@ __global__ void __launch_bounds__(kMoveThreads) kColour(const SweepArgs* __restr
                 if (!displace) {
                     a.s.dir[t] = make_double4_32a(P.ndir[0], P.ndir[1], P.ndir[2], od4.w);
                     a.s.patch[t] = P.npatch;
+                    if (a.mlp) {
+                        float4 nd = make_float4((float)P.ndir[0], (float)P.ndir[1], (float)P.ndir[2], 0.0f);
+                        float4 npd = make_float4((float)P.npatch.pd[0][0], (float)P.npatch.pd[0][1],
+                                                 (float)P.npatch.pd[0][2], 0.0f);
+                        a.cellDirF[a.cellStart[cell] + P.slotR] = nd;
+                        a.cellPatF[a.cellStart[cell] + P.slotR] = npd;
+                        if (resident) {
+                            candDir[sh.st.ownOff + P.slotR] = nd;
+                            candPat[sh.st.ownOff + P.slotR] = npd;
+                        }
+                    }
                 } else {
                     float4 nf = make_float4(newF.x, newF.y, newF.z, (float)op4.w);
                     if (resident) candPos[sh.st.ownOff + P.slotR] = nf;
@@ -1011,9 +1114,385 @@ __global__ void kEndSweep(const SweepArgs* __restrict__ A) {
     if (threadIdx.x == 0) {
         double s = 0.0;
         for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += ws[q];
-        a.ctl->energy += s;
+        *(a.energyAcc ? a.energyAcc : &a.ctl->energy) += s;
         a.ctl->sweep += 1;
     }
+}
+
+// ---- chain moves ---------------------------------------------------------------------------
+// MoveCreator::chainMove / chainDisplace / chainRotate / clusterRotate
+// (scOOP/mc/movecreator.cpp:305-328, 1075-1256, 1326-1392): a chain (molecule of more than one
+// particle) is displaced rigidly by a fixed-length random vector, or rotated about its
+// volume-weighted centre by a random quaternion; accepted on mol2others (the chain against
+// every particle outside it, empty conlist, totalenergycalculator.h:417-499).
+//
+// On the GPU the chain moves run in their own checkerboard phase on a coarser grid: a chain
+// belongs to the cell holding its centre, cells are at least (maxcut + 2 R)/s wide (R bounds
+// |particle - centre| plus the displacement), so chains moved by different cells of one
+// colour never come within maxcut of each other; a move whose new centre leaves the cell,
+// or whose chain is wider than R, is rejected (both are symmetric in the move).
+
+constexpr int kMaxChain = 20;       // MAXCHL of the reference
+
+__device__ __forceinline__ double3 chainCentre(const SweepArgs& a, int first, int size) {
+    double x = 0.0, y = 0.0, z = 0.0, v = 0.0;
+    for (int k = 0; k < size; ++k) {      // MoveCreator::clusterCM (movecreator.cpp:1326-1343)
+        double4_32a p = a.s.pos[first + k];
+        double w = a.volW[(int)p.w];
+        x += p.x * w; y += p.y * w; z += p.z * w;
+        v += w;
+    }
+    return mk(x / v, y / v, z / v);
+}
+
+// Chains binned by centre into the chain grid (one CTA per system, fixed order in a cell).
+__global__ void __launch_bounds__(1024) kChainBin(const SweepArgs* __restrict__ A) {
+    const SweepArgs& a = A[blockIdx.y];
+    const Grid& g = a.g;
+    const Control& ctl = *a.ctl;
+    __shared__ int carryS;
+    __shared__ int warpS[32];
+    for (int c = threadIdx.x; c < g.ncells; c += blockDim.x) { a.chainCellCount[c] = 0; a.cellCursor[c] = 0; }
+    __syncthreads();
+    for (int ch = threadIdx.x; ch < a.nChains; ch += blockDim.x) {
+        int2 fs = a.chains[ch];
+        double3 cm = chainCentre(a, fs.x, fs.y);
+        int cx = wrapCell(cm.x, ctl.shift[0], g.nc[0]), cy = wrapCell(cm.y, ctl.shift[1], g.nc[1]),
+            cz = wrapCell(cm.z, ctl.shift[2], g.nc[2]);
+        atomicAdd(&a.chainCellCount[(cz * g.nc[1] + cy) * g.nc[0] + cx], 1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) carryS = 0;
+    __syncthreads();
+    for (int base = 0; base < g.ncells; base += blockDim.x) {      // exclusive scan
+        int c = base + threadIdx.x;
+        int v = c < g.ncells ? a.chainCellCount[c] : 0;
+        int x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, x, o);
+            if ((threadIdx.x & 31) >= o) x += y;
+        }
+        if ((threadIdx.x & 31) == 31) warpS[threadIdx.x >> 5] = x;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            int w = warpS[threadIdx.x];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int y = __shfl_up_sync(0xffffffffu, w, o);
+                if (threadIdx.x >= o) w += y;
+            }
+            warpS[threadIdx.x] = w;
+        }
+        __syncthreads();
+        int before = (threadIdx.x >> 5) ? warpS[(threadIdx.x >> 5) - 1] : 0;
+        if (c < g.ncells) a.chainCellStart[c] = carryS + before + x - v;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carryS += before + x;
+        __syncthreads();
+    }
+    for (int ch = threadIdx.x; ch < a.nChains; ch += blockDim.x) {
+        int2 fs = a.chains[ch];
+        double3 cm = chainCentre(a, fs.x, fs.y);
+        int cx = wrapCell(cm.x, ctl.shift[0], g.nc[0]), cy = wrapCell(cm.y, ctl.shift[1], g.nc[1]),
+            cz = wrapCell(cm.z, ctl.shift[2], g.nc[2]);
+        int cell = (cz * g.nc[1] + cy) * g.nc[0] + cx;
+        a.chainCellIdx[a.chainCellStart[cell] + atomicAdd(&a.cellCursor[cell], 1)] = ch;
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < g.ncells; c += blockDim.x) {     // ascending chain index
+        int* v = a.chainCellIdx + a.chainCellStart[c];
+        int n = a.chainCellCount[c];
+        for (int i = 1; i < n; ++i) {
+            int x = v[i], j = i - 1;
+            while (j >= 0 && v[j] > x) { v[j + 1] = v[j]; --j; }
+            v[j + 1] = x;
+        }
+    }
+}
+
+struct ChainShared {
+    int list[kCellCap];
+    int queueA[kQueueCap];
+    int queueB[kQueueCap];
+    Stencil st;
+    Scan scan;
+    double red[kWarps][2];
+    int first, size, displace, skip, constrained;
+    double thr;
+    double cm[3];
+    double npos[kMaxChain][3], ndir[kMaxChain][3];
+    PatchSet npatch[kMaxChain];
+    float3 oldF[kMaxChain], newF[kMaxChain];
+};
+
+// Quaternion rotation of a vector (Vector::rotate(Quat), scOOP/structures/Vector.h:162-183).
+__device__ __forceinline__ void quatRotate(const double (&q)[4], double* v) {
+    double t2 = q[0] * q[1], t3 = q[0] * q[2], t4 = q[0] * q[3], t5 = -q[1] * q[1], t6 = q[1] * q[2],
+           t7 = q[1] * q[3], t8 = -q[2] * q[2], t9 = q[2] * q[3], t10 = -q[3] * q[3];
+    double x = v[0], y = v[1], z = v[2];
+    v[0] = 2.0 * ((t8 + t10) * x + (t6 - t4) * y + (t3 + t7) * z) + x;
+    v[1] = 2.0 * ((t4 + t6) * x + (t5 + t10) * y + (t9 - t2) * z) + y;
+    v[2] = 2.0 * ((t7 - t3) * x + (t2 + t9) * y + (t5 + t8) * z) + z;
+}
+
+// Warp 0: the chain move proposal of move m of this cell.
+__device__ void buildChainProposal(const SweepArgs& a, ChainShared& sh, int cell, int cnt, int m, int cx, int cy,
+                                   int cz, const double3& box) {
+    const Control& ctl = *a.ctl;
+    const int lane = threadIdx.x & 31;
+    const uint32_t sk = (uint32_t)ctl.sweep ^ ((uint32_t)(ctl.sweep >> 32) << 20);
+    Stream r(a.seed, (uint32_t)cell, (uint32_t)m, sk);
+    int slot = min((int)(r.next() * cnt), cnt - 1);
+    int2 fs = a.chains[sh.list[slot]];
+    const int first = fs.x, size = min(fs.y, kMaxChain);
+    bool displace = r.next() < 0.5;          // chainMove: ran2() < 0.5 displaces
+    double3 cm = chainCentre(a, first, size);
+    double q[4] = {1.0, 0.0, 0.0, 0.0};
+    double dr[3] = {0.0, 0.0, 0.0};
+    if (displace) {
+        double x, y, z;
+        randomUnitSphere(r, x, y, z);
+        dr[0] = x * a.chainMx / box.x; dr[1] = y * a.chainMx / box.y; dr[2] = z * a.chainMx / box.z;
+    } else {
+        double x, y, z;
+        randomUnitSphere(r, x, y, z);
+        double vc = cos(a.chainAngle * r.next());
+        double vs = (r.next() < 0.5) ? sqrt(1.0 - vc * vc) : -sqrt(1.0 - vc * vc);
+        q[0] = vc; q[1] = x * vs; q[2] = y * vs; q[3] = z * vs;
+    }
+    int wide = 0;
+    if (lane < size) {
+        const int i = first + lane;
+        double4_32a p = a.s.pos[i], d = a.s.dir[i];
+        double v[3] = {p.x, p.y, p.z};
+        double rx = (p.x - cm.x) * box.x, ry = (p.y - cm.y) * box.y, rz = (p.z - cm.z) * box.z;
+        wide = (rx * rx + ry * ry + rz * rz > a.chainR * a.chainR);
+        double dd[3] = {d.x, d.y, d.z};
+        if (displace) {
+            for (int k = 0; k < 3; ++k) v[k] += dr[k];
+        } else {
+            // clusterRotate: shift to the centre, scale by the box, rotate, scale back, shift back
+            for (int k = 0; k < 3; ++k) v[k] -= (&cm.x)[k];
+            v[0] *= box.x; v[1] *= box.y; v[2] *= box.z;
+            quatRotate(q, v);
+            v[0] /= box.x; v[1] /= box.y; v[2] /= box.z;
+            for (int k = 0; k < 3; ++k) v[k] += (&cm.x)[k];
+            quatRotate(q, dd);
+            const PatchSet& ps = a.s.patch[i];
+            PatchSet& np = sh.npatch[lane];
+            for (int u = 0; u < 2; ++u) { double w[3] = {ps.pd[u][0], ps.pd[u][1], ps.pd[u][2]}; quatRotate(q, w); for (int k = 0; k < 3; ++k) np.pd[u][k] = w[k]; }
+            for (int u = 0; u < 2; ++u) { double w[3] = {ps.ch[u][0], ps.ch[u][1], ps.ch[u][2]}; quatRotate(q, w); for (int k = 0; k < 3; ++k) np.ch[u][k] = w[k]; }
+            for (int u = 0; u < 4; ++u) { double w[3] = {ps.ps[u][0], ps.ps[u][1], ps.ps[u][2]}; quatRotate(q, w); for (int k = 0; k < 3; ++k) np.ps[u][k] = w[k]; }
+        }
+        for (int k = 0; k < 3; ++k) { sh.npos[lane][k] = v[k]; sh.ndir[lane][k] = dd[k]; }
+        sh.oldF[lane] = make_float3(frac32(p.x), frac32(p.y), frac32(p.z));
+        sh.newF[lane] = make_float3(frac32(v[0]), frac32(v[1]), frac32(v[2]));
+    }
+    wide = __any_sync(0xffffffffu, wide);
+    __syncwarp();
+    if (lane == 0) {
+        // the new centre (from the new positions, as for the reverse move) must stay in the cell
+        double x = 0.0, y = 0.0, z = 0.0, vv = 0.0;
+        for (int k = 0; k < size; ++k) {
+            double w = a.volW[(int)a.s.pos[first + k].w];
+            x += sh.npos[k][0] * w; y += sh.npos[k][1] * w; z += sh.npos[k][2] * w;
+            vv += w;
+        }
+        x /= vv; y /= vv; z /= vv;
+        bool inside = wrapCell(x, ctl.shift[0], a.g.nc[0]) == cx && wrapCell(y, ctl.shift[1], a.g.nc[1]) == cy &&
+                      wrapCell(z, ctl.shift[2], a.g.nc[2]) == cz;
+        sh.first = first;
+        sh.size = size;
+        sh.displace = displace;
+        sh.skip = (!inside || wide) ? 1 : 0;
+        sh.constrained = wide ? 1 : 0;
+        Stream ru(a.seed ^ 0xD1B54A32D192ED03ull, (uint32_t)cell, (uint32_t)m, sk);
+        sh.thr = -a.temper * log(ru.next());
+    }
+}
+
+// One CTA per active cell of the chain grid: that cell's chain moves in sequence (stages
+// A, B, C as in kColour over (chain particle, candidate) pairs, old and new configuration).
+__global__ void __launch_bounds__(kMoveThreads) kChainColour(const SweepArgs* __restrict__ A, int phase) {
+    extern __shared__ float4 dynSmem[];
+    __shared__ ChainShared sh;
+    const SweepArgs& a = A[blockIdx.y];
+    float4* candPos = dynSmem;
+    int* candIdx = reinterpret_cast<int*>(candPos + kCandCap);
+    const Control& ctl = *a.ctl;
+    const Grid& g = a.g;
+    if (a.nChains == 0 || (int)blockIdx.x >= g.nactive || phase >= g.ncolours) return;
+    int cx, cy, cz;
+    decodeActive(g, ctl.perm[phase], blockIdx.x, cx, cy, cz);
+    const int cell = (cz * g.nc[1] + cy) * g.nc[0] + cx;
+    const int cnt = a.chainCellCount[cell];
+    if (cnt > kCellCap && threadIdx.x == 0) atomicOr(a.err, E_CELL_OVERFLOW);
+    if (cnt == 0 || cnt > kCellCap) return;
+    const int tid = threadIdx.x;
+    // attempts of this cell this sweep: cnt * chainFrac, the fraction rounded at random
+    Stream rm(a.seed ^ 0x9E3779B97F4A7C15ull, (uint32_t)cell, 0xC4A1u,
+              (uint32_t)ctl.sweep ^ ((uint32_t)(ctl.sweep >> 32) << 20));
+    const double want = cnt * a.chainFrac;
+    const int moves = (int)want + ((rm.next() < want - floor(want)) ? 1 : 0);
+    if (moves == 0) return;
+    for (int k = tid; k < cnt; k += kMoveThreads) sh.list[k] = a.chainCellIdx[a.chainCellStart[cell] + k];
+    stageStencil(a, cx, cy, cz, sh.st, sh.scan);
+    const int nCand = sh.st.nCand;
+    const bool resident = nCand <= kCandCap;
+    if (resident) loadCandidates(a, sh.st, 0, nCand, candIdx, candPos);
+    DevCtx c;
+    c.params = a.t.params; c.mols = a.t.mols; c.ntypes = a.t.ntypes; c.n = a.s.n; c.sqmaxcut = a.t.sqmaxcut;
+    const Con con = emptyCon(c);
+    const double3 box = mk(a.s.box[0], a.s.box[1], a.s.box[2]);
+    const float thr32 = candThreshold(c.sqmaxcut, box);
+    double dECell = 0.0;
+    unsigned long long nAcc = 0, nRej = 0, nConstr = 0, nTested = 0, nEval = 0;
+
+    for (int m = 0; m < moves; ++m) {
+        if (tid < 32) buildChainProposal(a, sh, cell, cnt, m, cx, cy, cz, box);
+        __syncthreads();
+        if (sh.skip) {
+            if (tid == 0) { ++nRej; nConstr += sh.constrained; }
+            __syncthreads();
+            continue;
+        }
+        const int first = sh.first, size = sh.size;
+        const bool displace = sh.displace;
+        auto view = [&](int i, bool isNew) {
+            PView v = viewAt(a.s, first + i);
+            if (isNew) {
+                v.pos = mk(sh.npos[i][0], sh.npos[i][1], sh.npos[i][2]);
+                v.dir = mk(sh.ndir[i][0], sh.ndir[i][1], sh.ndir[i][2]);
+                if (!displace) v.patch = &sh.npatch[i];
+            }
+            return v;
+        };
+        double eOld = 0.0, eNew = 0.0;
+        int qb = 0;
+        auto flushC = [&]() {
+            __syncthreads();
+            for (int e = tid; e < qb; e += kMoveThreads) {
+                int q = sh.queueB[e];
+                int isNew = q & 1, pi = (q >> 1) % kMaxChain, k = (q >> 1) / kMaxChain;
+                PView self = view(pi, isNew);
+                unsigned bb; double dd;
+                double en = pairEnergy(c, self, viewAt(a.s, candIdx[k]), con, box, &bb, &dd);
+                if (isNew) eNew += en; else eOld += en;
+            }
+            __syncthreads();
+            nEval += qb;
+            qb = 0;
+        };
+        for (int wbase = 0; wbase < nCand; wbase += kCandCap) {
+            const int wlen = min(kCandCap, nCand - wbase);
+            if (!resident) loadCandidates(a, sh.st, wbase, wlen, candIdx, candPos);
+            const int total = wlen * size;
+            for (int base = 0; base < total; base += kChunk) {
+                const int end = min(base + kChunk, total);
+                int qa = 0;
+                for (int r0 = base; r0 < end; r0 += kMoveThreads) {     // stage A
+                    int idx = r0 + tid, flags = 0, k = 0, pi = 0;
+                    if (idx < end) {
+                        k = idx / size;
+                        pi = idx - k * size;
+                        int j = candIdx[k];
+                        if (j < first || j >= first + size) {
+                            float4 cp = candPos[k];
+                            bool p0 = dist2f(cp, sh.oldF[pi], box) <= thr32;
+                            bool p1 = dist2f(cp, sh.newF[pi], box) <= thr32;
+                            flags = (p0 ? 1 : 0) | (p1 ? 2 : 0);
+                        }
+                    }
+                    int tot;
+                    int off = blockExclusiveScan(__popc(flags), tot, sh.scan);
+                    int key = (k * kMaxChain + pi) << 1;
+                    if (flags & 1) sh.queueA[qa + off++] = key;
+                    if (flags & 2) sh.queueA[qa + off] = key | 1;
+                    qa += tot;
+                }
+                __syncthreads();
+                for (int e0 = 0; e0 < qa; e0 += kMoveThreads) {             // stage B
+                    int e = e0 + tid, keep = 0, q = 0;
+                    if (e < qa) {
+                        q = sh.queueA[e];
+                        int isNew = q & 1, pi = (q >> 1) % kMaxChain, k = (q >> 1) / kMaxChain;
+                        PView self = view(pi, isNew);
+                        int j = candIdx[k];
+                        double4_32a pj = a.s.pos[j];
+                        double3 r = imageVec(self.pos, mk(pj.x, pj.y, pj.z), box);
+                        if (!(dot3(r, r) > c.sqmaxcut)) {
+                            double4_32a dj = a.s.dir[j];
+                            const PairParam& pp = c.params[self.type * c.ntypes + (int)pj.w];
+                            keep = screenedOut(pp, r, self.dir, mk(dj.x, dj.y, dj.z)) ? 0 : 1;
+                        }
+                    }
+                    int tot;
+                    int off = blockExclusiveScan(keep, tot, sh.scan);
+                    if (keep) sh.queueB[qb + off] = q;
+                    qb += tot;
+                    if (qb > kQueueCap - kMoveThreads) flushC();
+                }
+            }
+            flushC();          // queue entries index the window
+        }
+        nTested += (unsigned long long)nCand * size * 2;
+        blockSum2(eOld, eNew, sh.red);
+        __shared__ int acceptS;
+        if (tid == 0) {
+            double dE = eNew - eOld;
+            bool accept = (dE <= 0.0) || (dE < sh.thr);
+            acceptS = accept;
+            if (accept) { dECell += dE; ++nAcc; } else ++nRej;
+        }
+        __syncthreads();
+        if (acceptS && tid < size) {
+            const int i = first + tid;
+            double4_32a p = a.s.pos[i];
+            a.s.pos[i] = make_double4_32a(sh.npos[tid][0], sh.npos[tid][1], sh.npos[tid][2], p.w);
+            if (!displace) {
+                double4_32a d = a.s.dir[i];
+                a.s.dir[i] = make_double4_32a(sh.ndir[tid][0], sh.ndir[tid][1], sh.ndir[tid][2], d.w);
+                a.s.patch[i] = sh.npatch[tid];
+            }
+            // the particle's entry in this grid's cell list (and in shared memory)
+            int pc = a.cellOf[i];
+            int s0 = a.cellStart[pc], n0 = a.cellCount[pc];
+            float4 nf = make_float4(sh.newF[tid].x, sh.newF[tid].y, sh.newF[tid].z, (float)p.w);
+            for (int k = 0; k < n0; ++k)
+                if (a.cellIdx[s0 + k] == i) {
+                    a.cellPosF[s0 + k] = nf;
+                    if (resident)
+                        for (int q = 0; q < sh.st.nNb; ++q)
+                            if (sh.st.nbCell[q] == pc) candPos[sh.st.nbOff[q] + k] = nf;
+                    break;
+                }
+        }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        a.cellDE[cell] = dECell;
+        atomicAdd(&a.counters[C_ACC_CH], nAcc);
+        atomicAdd(&a.counters[C_REJ_CH], nRej);
+        if (nConstr) atomicAdd(&a.counters[C_CH_CONSTR], nConstr);
+        atomicAdd(&a.counters[C_TESTED], nTested);
+        atomicAdd(&a.counters[C_EVAL], nEval);
+    }
+}
+
+// Largest |particle - chain centre| (real space) over all chains, as float bits (>= 0).
+__global__ void kChainExtent(SweepArgs a, const int2* chains, int nChains, unsigned* out) {
+    int ch = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ch >= nChains) return;
+    int2 fs = chains[ch];
+    double3 cm = chainCentre(a, fs.x, fs.y);
+    double m = 0.0;
+    for (int k = 0; k < fs.y; ++k) {
+        double4_32a p = a.s.pos[fs.x + k];
+        double x = (p.x - cm.x) * a.s.box[0], y = (p.y - cm.y) * a.s.box[1], z = (p.z - cm.z) * a.s.box[2];
+        m = fmax(m, sqrt(x * x + y * y + z * z));
+    }
+    atomicMax(out, __float_as_uint((float)m));
 }
 
 struct CellShared {
@@ -1198,8 +1677,8 @@ __global__ void kCheckEnergy(const SweepArgs* __restrict__ A) {
 // at rank k (colder) and the one at rank k+1 is accepted with
 // min(1, exp((1/T_k - 1/T_k+1)(E_k - E_k+1) + (P_k/T_k - P_k+1/T_k+1)(V_k - V_k+1))),
 // the canonical plus isobaric rule of the reference (the pressure term vanishes in NVT).
-__global__ void kExchange(SweepArgs* A, int* ladder, const int* ladderStart, int nLadders, uint64_t seed,
-                          unsigned long long* ctr) {
+__global__ void kExchange(SweepArgs* A, SweepArgs* AC, int* ladder, const int* ladderStart, int nLadders,
+                          uint64_t seed, unsigned long long* ctr) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     unsigned long long ev = ctr[0]++;
     int parity = (int)(ev & 1ull);
@@ -1221,6 +1700,7 @@ __global__ void kExchange(SweepArgs* A, int* ladder, const int* ladderStart, int
             if (delta >= 0.0 || exp(delta) > u) {
                 A[ri].temper = Tj;
                 A[rj].temper = Ti;
+                if (AC) { AC[ri].temper = Tj; AC[rj].temper = Ti; }   // the chain phase's records
                 ladder[k] = rj;
                 ladder[k + 1] = ri;
                 ctr[2 + 2 * k] += 1ull;
@@ -1237,6 +1717,8 @@ struct SweepEngine {
     Control* ctl = nullptr;
     int *cellStart = nullptr, *cellCount = nullptr, *cellCursor = nullptr, *cellIdx = nullptr, *cellOf = nullptr;
     float4* cellPosF = nullptr;
+    float4* cellDirF = nullptr;
+    float4* cellPatF = nullptr;
     double* cellDE = nullptr;
     double* partial = nullptr;
     unsigned long long* counters = nullptr;
@@ -1248,6 +1730,21 @@ struct SweepEngine {
     int stencil = 0;
     double margin = 0.0;
     SweepArgs args{};
+    // chain moves: the chain grid's particle cell list, the chains binned by centre
+    struct Chains {
+        bool on = false;
+        Grid g{};
+        Control* ctl = nullptr;
+        int *cellStart = nullptr, *cellCount = nullptr, *cellCursor = nullptr, *cellIdx = nullptr, *cellOf = nullptr;
+        float4* cellPosF = nullptr;
+        double* cellDE = nullptr;
+        int2* chains = nullptr;
+        int nChains = 0;
+        int *chStart = nullptr, *chCount = nullptr, *chIdx = nullptr;
+        int ncellsAlloc = 0;
+        double R = 0.0;
+        SweepArgs args{};
+    } ch;
 };
 
 // A set of systems moved together: one launch sequence per sweep, blockIdx.y = system.
@@ -1257,11 +1754,17 @@ struct Batch {
     SweepArgs* dArgs = nullptr;
     int nArgsAlloc = 0;
     int maxN = 0, maxCells = 0, maxActive = 0, maxColours = 0;
+    // chain phase (every system of the batch holds chains, or none does)
+    bool chains = false;
+    std::vector<SweepArgs> hArgsC;
+    SweepArgs* dArgsC = nullptr;
+    int nArgsCAlloc = 0;
+    int maxCellsC = 0, maxActiveC = 0, maxColoursC = 0;
     cudaStream_t stream = nullptr;
     int device = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evP0 = nullptr, evP1 = nullptr;
     cudaGraphExec_t graph = nullptr;
-    int graphDims[6] = {0, 0, 0, 0, 0, 0};
+    int graphDims[11] = {0};   // launch shape the graph was captured with
     long graphLaunches = 0, graphPhaseLaunches = 0;
     // parallel tempering
     int* dLadder = nullptr;
@@ -1378,6 +1881,7 @@ static void fillArgs(Context* c, SweepEngine* e, const sc_run_params& p) {
     a.ctl = e->ctl;
     a.cellStart = e->cellStart; a.cellCount = e->cellCount; a.cellCursor = e->cellCursor;
     a.cellIdx = e->cellIdx; a.cellPosF = e->cellPosF; a.cellOf = e->cellOf; a.cellDE = e->cellDE;
+    a.cellDirF = e->cellDirF; a.cellPatF = e->cellPatF;
     a.partial = e->partial;
     a.counters = e->counters; a.err = e->err;
     a.seed = p.seed;
@@ -1392,11 +1896,99 @@ static void fillArgs(Context* c, SweepEngine* e, const sc_run_params& p) {
         double perType = c->opts.trans_type[t];
         a.trans[k] = (base > 0 && perType != base) ? perType * (p.transmx / base) : p.transmx;
         a.geo[k] = c->topo.ia[t][t].geotype[0];
+        a.volW[k] = c->topo.ia[t][t].volume;
     }
     if (p.delayed && c->surrogate) {
         a.mlp = surrogatePacked(c->surrogate);
         a.rcutS = surrogateCutoff(c->surrogate);
     }
+}
+
+// Chain phase of one system: chains (molecules of more than one particle), the bound R of
+// their half-extent, the chain grid (cells >= (maxcut + 2 (R + displacement)) / 2) and its
+// arguments.  Off when chainprob is 0 or the system holds no chains.
+static int prepareChains(Context* c, SweepEngine* e, const sc_run_params& p, const double* box) {
+    SweepEngine::Chains& C = e->ch;
+    C.on = false;
+    std::vector<int2> chains;
+    for (size_t i = 0; i < c->molInfo.size(); ++i)
+        if (c->molInfo[i].y == 0 && c->molInfo[i].z > 1) chains.push_back(make_int2((int)i, c->molInfo[i].z));
+    if (!(p.chainprob > 0) || chains.empty()) return SC_OK;
+    for (const int2& ch : chains)
+        if (ch.y > kMaxChain) return fail(SC_ERR_RANGE, "a chain holds more than 20 particles (MAXCHL)");
+    int rc;
+    const int n = c->d.n;
+    if (!C.ctl) {
+        if ((rc = engineAlloc(e, (void**)&C.ctl, sizeof(Control)))) return rc;
+        cudaMemset(C.ctl, 0, sizeof(Control));
+        if ((rc = engineAlloc(e, (void**)&C.cellIdx, sizeof(int) * n))) return rc;
+        if ((rc = engineAlloc(e, (void**)&C.cellOf, sizeof(int) * n))) return rc;
+        if ((rc = engineAlloc(e, (void**)&C.cellPosF, sizeof(float4) * n))) return rc;
+        if ((rc = engineAlloc(e, (void**)&C.chains, sizeof(int2) * chains.size()))) return rc;
+        if ((rc = engineAlloc(e, (void**)&C.chIdx, sizeof(int) * chains.size()))) return rc;
+        cudaMemcpy(C.chains, chains.data(), sizeof(int2) * chains.size(), cudaMemcpyHostToDevice);
+        C.nChains = (int)chains.size();
+    }
+    if (e->seed != p.seed) {
+        unsigned long long zero = 0;
+        cudaMemcpy(&C.ctl->sweep, &zero, sizeof zero, cudaMemcpyHostToDevice);
+    }
+    // half-extent bound from the current configuration, with room to stretch
+    unsigned* dMax = nullptr;
+    if ((rc = engineAlloc(e, (void**)&dMax, sizeof(unsigned)))) return rc;
+    cudaMemset(dMax, 0, sizeof(unsigned));
+    kChainExtent<<<(C.nChains + 127) / 128, 128, 0, c->stream>>>(e->args, C.chains, C.nChains, dMax);
+    unsigned bits = 0;
+    cudaError_t r = cudaMemcpyAsync(&bits, dMax, sizeof bits, cudaMemcpyDeviceToHost, c->stream);
+    if (r == cudaSuccess) r = cudaStreamSynchronize(c->stream);
+    cudaFree(dMax);
+    e->allocs.erase(std::find(e->allocs.begin(), e->allocs.end(), (void*)dMax));
+    if (r != cudaSuccess) return cudaFail(r, "chain extent");
+    float ext;
+    std::memcpy(&ext, &bits, sizeof ext);
+    C.R = std::max(1.2 * ext, ext + 0.5);
+    Grid g = makeGrid(box, c->topo.maxcut + 2.0 * (C.R + p.chainmmx), e->margin, 2);
+    if (g.ncolours > kMaxColours) return fail(SC_ERR_RANGE, "too many colour classes (chain grid)");
+    g.maxcut = c->topo.maxcut + 2.0 * (C.R + p.chainmmx);
+    if (g.ncells > C.ncellsAlloc) {
+        for (void** q : {(void**)&C.cellStart, (void**)&C.cellCount, (void**)&C.cellCursor, (void**)&C.cellDE,
+                         (void**)&C.chStart, (void**)&C.chCount}) {
+            if (*q) {
+                cudaFree(*q);
+                e->allocs.erase(std::find(e->allocs.begin(), e->allocs.end(), *q));
+                *q = nullptr;
+            }
+        }
+        int m = g.ncells;
+        if ((rc = engineAlloc(e, (void**)&C.cellStart, sizeof(int) * m))) return rc;
+        if ((rc = engineAlloc(e, (void**)&C.cellCount, sizeof(int) * m))) return rc;
+        if ((rc = engineAlloc(e, (void**)&C.cellCursor, sizeof(int) * m))) return rc;
+        if ((rc = engineAlloc(e, (void**)&C.cellDE, sizeof(double) * m))) return rc;
+        if ((rc = engineAlloc(e, (void**)&C.chStart, sizeof(int) * m))) return rc;
+        if ((rc = engineAlloc(e, (void**)&C.chCount, sizeof(int) * m))) return rc;
+        cudaMemset(C.cellDE, 0, sizeof(double) * m);
+        C.ncellsAlloc = m;
+    }
+    C.g = g;
+    SweepArgs& a = C.args;
+    a = e->args;
+    a.g = g;
+    a.ctl = C.ctl;
+    a.cellStart = C.cellStart; a.cellCount = C.cellCount; a.cellCursor = C.cellCursor; a.cellIdx = C.cellIdx;
+    a.cellOf = C.cellOf; a.cellPosF = C.cellPosF; a.cellDE = C.cellDE;
+    a.cellDirF = a.cellPatF = nullptr;
+    a.mlp = nullptr;
+    a.seed = p.seed ^ 0x6A09E667F3BCC909ull;
+    a.energyAcc = &e->ctl->energy;
+    a.chains = C.chains;
+    a.nChains = C.nChains;
+    a.chainCellStart = C.chStart; a.chainCellCount = C.chCount; a.chainCellIdx = C.chIdx;
+    a.chainMx = p.chainmmx;
+    a.chainAngle = p.chain_angle;
+    a.chainFrac = p.chainprob * (double)n / (double)C.nChains;   // N * chainprob chain moves per sweep
+    a.chainR = C.R;
+    C.on = true;
+    return SC_OK;
 }
 
 // Device state, grid and arguments of one system for a run with parameters p.
@@ -1413,6 +2005,8 @@ static int prepareSystem(Context* c, const sc_run_params& p, bool npt) {
         if ((rc = engineAlloc(e, (void**)&e->ctl, sizeof(Control)))) return rc;
         if ((rc = engineAlloc(e, (void**)&e->cellIdx, sizeof(int) * std::max(n, 1)))) return rc;
         if ((rc = engineAlloc(e, (void**)&e->cellPosF, sizeof(float4) * std::max(n, 1)))) return rc;
+        if ((rc = engineAlloc(e, (void**)&e->cellDirF, sizeof(float4) * std::max(n, 1)))) return rc;
+        if ((rc = engineAlloc(e, (void**)&e->cellPatF, sizeof(float4) * std::max(n, 1)))) return rc;
         if ((rc = engineAlloc(e, (void**)&e->cellOf, sizeof(int) * std::max(n, 1)))) return rc;
         if ((rc = engineAlloc(e, (void**)&e->counters, sizeof(unsigned long long) * C_COUNT))) return rc;
         if ((rc = engineAlloc(e, (void**)&e->err, sizeof(int)))) return rc;
@@ -1432,6 +2026,7 @@ static int prepareSystem(Context* c, const sc_run_params& p, bool npt) {
     e->stencil = chooseStencil(box, c->topo.maxcut, p.stencil);
     if ((rc = ensureGrid(c, e, box))) return rc;
     fillArgs(c, e, p);
+    if ((rc = prepareChains(c, e, p, box))) return rc;
     cudaMemset(e->counters, 0, sizeof(unsigned long long) * C_COUNT);
     cudaMemset(e->err, 0, sizeof(int));
     cudaMemset(&e->ctl->maxDrift, 0, sizeof(double));
@@ -1457,6 +2052,29 @@ static int uploadArgs(Batch& b) {
     }
     cudaError_t r = cudaMemcpy(b.dArgs, b.hArgs.data(), sizeof(SweepArgs) * ns, cudaMemcpyHostToDevice);
     if (r != cudaSuccess) return cudaFail(r, "upload sweep arguments");
+    int on = 0;
+    for (Context* c : b.sys) on += c->engine->ch.on ? 1 : 0;
+    if (on != 0 && on != ns) return fail(SC_ERR_UNSUPPORTED, "chain moves need every system of a batch to hold chains");
+    b.chains = on > 0;
+    if (b.chains) {
+        if (ns > b.nArgsCAlloc) {
+            int rc = b.alloc((void**)&b.dArgsC, sizeof(SweepArgs) * ns);
+            if (rc) return rc;
+            b.nArgsCAlloc = ns;
+        }
+        b.hArgsC.resize(ns);
+        b.maxCellsC = b.maxActiveC = b.maxColoursC = 0;
+        for (int k = 0; k < ns; ++k) {
+            SweepEngine* e = b.sys[k]->engine;
+            e->ch.args.temper = b.hArgs[k].temper;      // the replica's current temperature
+            b.hArgsC[k] = e->ch.args;
+            b.maxCellsC = std::max(b.maxCellsC, e->ch.g.ncells);
+            b.maxActiveC = std::max(b.maxActiveC, e->ch.g.nactive);
+            b.maxColoursC = std::max(b.maxColoursC, e->ch.g.ncolours);
+        }
+        r = cudaMemcpy(b.dArgsC, b.hArgsC.data(), sizeof(SweepArgs) * ns, cudaMemcpyHostToDevice);
+        if (r != cudaSuccess) return cudaFail(r, "upload chain arguments");
+    }
     return SC_OK;
 }
 
@@ -1473,6 +2091,8 @@ static void collectStats(Context* c, sc_run_stats& st) {
     st.acc_vol = (long)ctr[C_ACC_V]; st.rej_vol = (long)ctr[C_REJ_V]; st.vol_constrained = (long)ctr[C_VOL_CONSTR];
     st.pairs_tested = (long)ctr[C_TESTED];
     st.pairs_evaluated = (long)ctr[C_EVAL];
+    st.acc_chain = (long)ctr[C_ACC_CH];
+    st.rej_chain = (long)ctr[C_REJ_CH];
     st.da_stage1_rejected = (long)ctr[C_S1_REJ];
     st.da_stage2_tried = (long)ctr[C_S2_TRIED];
     st.da_stage2_rejected = (long)ctr[C_S2_REJ];
@@ -1512,22 +2132,28 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
     }
     static bool attrSet = false;
     if (!attrSet) {
-        if ((r = cudaFuncSetAttribute(kColour, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDynSmem)) != cudaSuccess)
+        if ((r = cudaFuncSetAttribute(kColour, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDynSmemSurrogate)) !=
+            cudaSuccess)
             return cudaFail(r, "shared memory attribute");
         if ((r = cudaFuncSetAttribute(kCellEnergy, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDynSmem)) != cudaSuccess)
             return cudaFail(r, "shared memory attribute");
         attrSet = true;
     }
     auto dims = [&](int x) { return dim3((unsigned)std::max(1, x), (unsigned)ns); };
-    auto launchCells = [&]() -> cudaError_t {
-        kZeroCounts<<<dims((b.maxCells + 255) / 256), 256, 0, s>>>(b.dArgs);
-        kAssign<<<dims((b.maxN + 255) / 256), 256, 0, s>>>(b.dArgs);
-        kScan<<<dims(1), 1024, 0, s>>>(b.dArgs);
-        kScatter<<<dims((b.maxN + 255) / 256), 256, 0, s>>>(b.dArgs);
-        kSortCells<<<dims((b.maxCells + 127) / 128), 128, 0, s>>>(b.dArgs);
+    // systems with a surrogate stage their candidates' FP32 axes and patches as well
+    bool anySurrogate = false;
+    for (const SweepArgs& h : b.hArgs) anySurrogate |= (h.mlp != nullptr);
+    const size_t colourSmem = anySurrogate ? kDynSmemSurrogate : kDynSmem;
+    auto launchCellsOf = [&](const SweepArgs* args, int maxCells) -> cudaError_t {
+        kZeroCounts<<<dims((maxCells + 255) / 256), 256, 0, s>>>(args);
+        kAssign<<<dims((b.maxN + 255) / 256), 256, 0, s>>>(args);
+        kScan<<<dims(1), 1024, 0, s>>>(args);
+        kScatter<<<dims((b.maxN + 255) / 256), 256, 0, s>>>(args);
+        kSortCells<<<dims((maxCells + 127) / 128), 128, 0, s>>>(args);
         launches += 5;
         return cudaGetLastError();
     };
+    auto launchCells = [&]() -> cudaError_t { return launchCellsOf(b.dArgs, b.maxCells); };
     auto exactEnergy = [&](bool check) -> cudaError_t {
         kCellEnergy<<<dims(b.maxCells), kMoveThreads, kDynSmem, s>>>(b.dArgs, 0);
         if (check) kCheckEnergy<<<dims(1), 32, 0, s>>>(b.dArgs);
@@ -1550,7 +2176,7 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
         cudaError_t r2 = launchCells();
         if (r2 != cudaSuccess) return r2;
         if (timing) cudaEventRecord(b.evP0, s);
-        for (int ph = 0; ph < b.maxColours; ++ph) kColour<<<dims(b.maxActive), kMoveThreads, kDynSmem, s>>>(b.dArgs, ph);
+        for (int ph = 0; ph < b.maxColours; ++ph) kColour<<<dims(b.maxActive), kMoveThreads, colourSmem, s>>>(b.dArgs, ph);
         if (timing) {
             cudaEventRecord(b.evP1, s);
             cudaEventSynchronize(b.evP1);
@@ -1561,6 +2187,15 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
         phaseLaunches += b.maxColours;
         kEndSweep<<<dims(1), 256, 0, s>>>(b.dArgs);
         launches += 2 + b.maxColours;
+        if (b.chains) {       // chain moves: their own grid, colours and cell list
+            kBeginSweep<<<dims(1), 32, 0, s>>>(b.dArgsC, 0);
+            if ((r2 = launchCellsOf(b.dArgsC, b.maxCellsC)) != cudaSuccess) return r2;
+            kChainBin<<<dims(1), 1024, 0, s>>>(b.dArgsC);
+            for (int ph = 0; ph < b.maxColoursC; ++ph)
+                kChainColour<<<dims(b.maxActiveC), kMoveThreads, kDynSmem, s>>>(b.dArgsC, ph);
+            kEndSweep<<<dims(1), 256, 0, s>>>(b.dArgsC);
+            launches += 3 + b.maxColoursC;
+        }
         if (volDue) {
             kCellEnergy<<<dims(b.maxCells), kMoveThreads, kDynSmem, s>>>(b.dArgs, 1);
             kVolumeAccept<<<dims(1), 32, 0, s>>>(b.dArgs);
@@ -1585,7 +2220,8 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
         long left = nsweeps - sw;
         bool aligned = (sw % G == 0) && (nextExchange < 0 || nextExchange - sw >= G);
         if (useGraph && left >= G && aligned) {
-            int key[6] = {ns, b.maxN, b.maxCells, b.maxActive, b.maxColours, (int)G};
+            int key[11] = {ns, b.maxN, b.maxCells, b.maxActive, b.maxColours, (int)G, anySurrogate ? 1 : 0,
+                           b.chains ? 1 : 0, b.maxCellsC, b.maxActiveC, b.maxColoursC};
             if (!b.graph || std::memcmp(key, b.graphDims, sizeof key) != 0) {
                 if (b.graph) { cudaGraphExecDestroy(b.graph); b.graph = nullptr; }
                 cudaGraph_t graph;
@@ -1614,7 +2250,8 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
             sw += 1;
         }
         if (nextExchange > 0 && sw >= nextExchange) {
-            kExchange<<<1, 32, 0, s>>>(b.dArgs, b.dLadder, b.dLadderStart, b.nLadders, exSeed, b.dExCtr);
+            kExchange<<<1, 32, 0, s>>>(b.dArgs, b.chains ? b.dArgsC : nullptr, b.dLadder, b.dLadderStart, b.nLadders,
+                                       exSeed, b.dExCtr);
             launches += 1;
             while (nextExchange <= sw) nextExchange += exchangeEvery;
         }
@@ -1634,17 +2271,25 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
                 double box[3];
                 cudaMemcpy(box, c->d.box, sizeof box, cudaMemcpyDeviceToHost);
                 Grid ng = makeGrid(box, c->topo.maxcut, e->margin, e->stencil);
-                if (ng.nc[0] != e->g.nc[0] || ng.nc[1] != e->g.nc[1] || ng.nc[2] != e->g.nc[2]) {
-                    if ((rc = ensureGrid(c, e, box))) return rc;
+                const bool mainChanged = ng.nc[0] != e->g.nc[0] || ng.nc[1] != e->g.nc[1] || ng.nc[2] != e->g.nc[2];
+                if (mainChanged || e->ch.on) {
+                    if (mainChanged && (rc = ensureGrid(c, e, box))) return rc;
                     // keep the device-side temperature (replica exchange may have changed it)
                     SweepArgs cur;
                     cudaMemcpy(&cur, b.dArgs + k, sizeof cur, cudaMemcpyDeviceToHost);
                     double T = cur.temper;
                     sc_run_params q = p;
                     q.seed = e->args.seed;
+                    q.temper = T;
+                    Grid oldC = e->ch.g;
                     fillArgs(c, e, q);
                     e->args.temper = T;
-                    changed = true;
+                    if (e->ch.on) {
+                        if ((rc = prepareChains(c, e, q, box))) return rc;
+                        changed |= e->ch.g.nc[0] != oldC.nc[0] || e->ch.g.nc[1] != oldC.nc[1] ||
+                                   e->ch.g.nc[2] != oldC.nc[2];
+                    }
+                    changed |= mainChanged;
                 }
             }
             if (changed && (rc = uploadArgs(b))) return rc;
@@ -1768,6 +2413,9 @@ int runReplicas(void* h, const sc_run_params& p, int exchangeEvery, sc_run_stats
         if (p.delayed && !c->surrogate) return fail(SC_ERR_STATE, "delayed = 1 needs a surrogate on every replica");
         if (p.transmx > 0) q.transmx = p.transmx;
         if (p.rot_angle > 0) q.rot_angle = p.rot_angle;
+        q.chainprob = p.chainprob;
+        if (p.chainmmx > 0) q.chainmmx = p.chainmmx;
+        if (p.chain_angle > 0) q.chain_angle = p.chain_angle;
         if ((rc = prepareSystem(c, q, npt))) return rc;
     }
     b.stream = b.sys[0]->stream;
@@ -1799,6 +2447,7 @@ int runReplicas(void* h, const sc_run_params& p, int exchangeEvery, sc_run_stats
         st.acc_trans += s1.acc_trans; st.rej_trans += s1.rej_trans;
         st.acc_rot += s1.acc_rot; st.rej_rot += s1.rej_rot;
         st.acc_vol += s1.acc_vol; st.rej_vol += s1.rej_vol; st.vol_constrained += s1.vol_constrained;
+        st.acc_chain += s1.acc_chain; st.rej_chain += s1.rej_chain;
         st.pairs_tested += s1.pairs_tested; st.pairs_evaluated += s1.pairs_evaluated;
         st.da_stage1_rejected += s1.da_stage1_rejected;
         st.da_stage2_tried += s1.da_stage2_tried;
