@@ -71,8 +71,10 @@ typedef struct {
     unsigned long long seed;
     double temper;
     double press;
-    int ptype;              /* 0: NVT, 1: isotropic volume moves (movecreator.cpp:390-421) */
-    int volume_every;       /* sweeps between volume moves (options shave=1 -> every sweep); 0: none */
+    int ptype;              /* pressure coupling of volume moves (movecreator.cpp:330-546): 0 one random
+                               edge, 1 isotropic, 2 xy with z fixed, 3 xy at fixed volume, 4 x (the
+                               reference's xy branch), 5 y only */
+    int volume_every;       /* sweeps between volume moves (options shave=1 -> every sweep); 0: none (NVT) */
     double transmx;         /* displacement length (already doubled, sim.h:365) */
     double rot_angle;       /* half-angle bound of pscRotate (rotmx/180*PIH*0.5, sim.h:359) */
     double edge_mx;         /* full edge-change range (already doubled, sim.h:363) */

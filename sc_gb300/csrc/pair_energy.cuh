@@ -304,29 +304,54 @@ static __device__ __noinline__ int cpscIntersect(double3 d1, double3 d2, PatchV 
     return (in[1] == 0.0) ? 0 : 2;
 }
 
-// EPatch::atrE (scOOP/mc/paire.cpp:243-301): attraction of two intersecting patches.
-static __device__ __noinline__ double patchAttraction(const PairParam& ia, double3 d1, double3 d2, double3 p1dir, double3 p2dir,
-                                               double3 r_cm, int pn1, int pn2, double S1, double S2, double T1, double T2) {
-    double v1 = fabs(S1 - S2), v2 = fabs(T1 - T2), f0 = 0.5 * (v1 + v2);
+// EPatch::atrE (scOOP/mc/paire.cpp:243-301): attraction of two intersecting patches, in two
+// independent halves: the distance term of the intersection pieces (A: returns the
+// cos^2 / plateau value, *f0 the length factor) and the angular switches and the parallel
+// factor (B).  atrE = A * (((f0 * f1) * f2) * paral).
+__device__ __forceinline__ double3 patchPieceVec(double3 d1, double3 d2, double3 r_cm, double S1, double S2, double T1,
+                                                 double T2) {
     double3 a1 = scl((S1 + S2) * 0.5, d1), a2 = scl((T1 + T2) * 0.5, d2);
-    double3 vi = mk(a2.x - a1.x - r_cm.x, a2.y - a1.y - r_cm.y, a2.z - a1.z - r_cm.z);
+    return mk(a2.x - a1.x - r_cm.x, a2.y - a1.y - r_cm.y, a2.z - a1.z - r_cm.z);
+}
+static __device__ __noinline__ double patchAttractionA(const PairParam& ia, double3 d1, double3 d2, double3 r_cm,
+                                                       double S1, double S2, double T1, double T2, double* f0out) {
+    double v1 = fabs(S1 - S2), v2 = fabs(T1 - T2), f0 = 0.5 * (v1 + v2);
+    double3 vi = patchPieceVec(d1, d2, r_cm, S1, S2, T1, T2);
     double3 md = minDistSegments(d1, d2, v1, v2, vi);
     double ndist = sqrt(dot3(md, md)), atr;
     if (ndist < ia.pdis) atr = -ia.epsilon;
     else { atr = cos(1.57079632679489661923132169163975 * (ndist - ia.pdis) / ia.pswitch); atr *= -atr * ia.epsilon; }
+    *f0out = f0;
+    return atr;
+}
+static __device__ __noinline__ void patchAttractionB(const PairParam& ia, double3 d1, double3 d2, double3 p1dir,
+                                                     double3 p2dir, double3 r_cm, int pn1, int pn2, double S1,
+                                                     double S2, double T1, double T2, double* f1out, double* f2out,
+                                                     double* paralOut) {
+    double3 vi = patchPieceVec(d1, d2, r_cm, S1, S2, T1, T2);
     double3 w = perpProj(vi, d1);
     double a = dot3(w, p1dir) / vlen(w);
-    double f1 = fanglScale(a, ia.pcangl[0 + 2 * pn1], ia.pcanglsw[0 + 2 * pn1]);
+    *f1out = fanglScale(a, ia.pcangl[0 + 2 * pn1], ia.pcanglsw[0 + 2 * pn1]);
     w = perpProj(neg3(vi), d2);
     a = dot3(w, p2dir) / vlen(w);
-    double f2 = fanglScale(a, ia.pcangl[1 + 2 * pn2], ia.pcanglsw[1 + 2 * pn2]);
+    *f2out = fanglScale(a, ia.pcangl[1 + 2 * pn2], ia.pcanglsw[1 + 2 * pn2]);
     double paral = 1.0;
     if (ia.parallel != 0.0) {   // EPatch::scparallel (paire.h:77-84)
         double cosa = dot3(d1, d2);
         if ((ia.parallel > 0 && cosa > 0) || (ia.parallel < 0 && cosa < 0)) paral = 1.0 + ia.parallel * cosa;
     }
+    *paralOut = paral;
+}
+__device__ __forceinline__ double patchAttractionCombine(double atr, double f0, double f1, double f2, double paral) {
     atr *= f0 * f1 * f2 * paral;
     return atr;
+}
+static __device__ double patchAttraction(const PairParam& ia, double3 d1, double3 d2, double3 p1dir, double3 p2dir,
+                                         double3 r_cm, int pn1, int pn2, double S1, double S2, double T1, double T2) {
+    double f0, f1, f2, paral;
+    double atr = patchAttractionA(ia, d1, d2, r_cm, S1, S2, T1, T2, &f0);
+    patchAttractionB(ia, d1, d2, p1dir, p2dir, r_cm, pn1, pn2, S1, S2, T1, T2, &f1, &f2, &paral);
+    return patchAttractionCombine(atr, f0, f1, f2, paral);
 }
 
 // x^-3 and x^-6 from one reciprocal: a few ulp from pow(x, -3) / pow(x, -6), with a
@@ -455,6 +480,80 @@ __device__ __forceinline__ double simpleScCombine(const PairParam& ia, const PVi
         atr += patchAttraction(ia, a.dir, b.dir, ld3(a.patch->pd[0]), ld3(b.patch->pd[0]), r_cm, 0, 0, S[0], S[1], T[0],
                                T[1]);
     return e0 + atr;
+}
+// The attraction's two halves of a single-patch pair (for two threads), and the sum.
+__device__ __forceinline__ double simpleScAttrA(const PairParam& ia, const PView& a, const PView& b,
+                                                const double3& r_cm, const double* T, const double* S, double* f0) {
+    return patchAttractionA(ia, a.dir, b.dir, r_cm, S[0], S[1], T[0], T[1], f0);
+}
+__device__ __forceinline__ void simpleScAttrB(const PairParam& ia, const PView& a, const PView& b, const double3& r_cm,
+                                              const double* T, const double* S, double* f1, double* f2,
+                                              double* paral) {
+    patchAttractionB(ia, a.dir, b.dir, ld3(a.patch->pd[0]), ld3(b.patch->pd[0]), r_cm, 0, 0, S[0], S[1], T[0], T[1],
+                     f1, f2, paral);
+}
+__device__ __forceinline__ double simpleScSum(double e0, bool attractive, double atrA, double f0, double f1, double f2,
+                                              double paral) {
+    double atr = 0.0;
+    if (attractive) atr += patchAttractionCombine(atrA, f0, f1, f2, paral);
+    return e0 + atr;
+}
+
+// Patch combination c (pn1 = c & 1, pn2 = c >> 1) of an SC-SC pair of patchy types: its two
+// intersection chains and the halves of its attraction, for evaluation by separate threads
+// (the scScEnergy loop below evaluates the same chains in sequence; a combination counts
+// when the attractive branch is on and both intersections give 2 points).
+__device__ __forceinline__ bool comboValid(const PairParam& ia, int c) {
+    int pn1 = c & 1, pn2 = c >> 1;
+    return !((pn1 && !ia.fT) || (pn2 && !ia.sT));
+}
+__device__ __forceinline__ void comboAxes(const PairParam& ia, const PView& a, const PView& b, int c, double3& d1,
+                                          double3& d2) {
+    int pn1 = c & 1, pn2 = c >> 1;
+    d1 = ia.fCH ? ld3(a.patch->ch[pn1]) : a.dir;
+    d2 = ia.sCH ? ld3(b.patch->ch[pn2]) : b.dir;
+}
+__device__ __forceinline__ int comboIntersect1(const PairParam& ia, const PView& a, const PView& b, const double3& r_cm,
+                                               int c, double* T) {
+    int pn1 = c & 1;
+    double3 d1, d2;
+    comboAxes(ia, a, b, c, d1, d2);
+    PatchV P1{ld3(a.patch->pd[pn1]), ld3(a.patch->ps[2 * pn1]), ld3(a.patch->ps[2 * pn1 + 1])};
+    return ia.firstPsc
+        ? pscIntersect(d1, d2, P1, r_cm, T, ia.pcanglsw[2 * pn1], ia.rcutSq, ia.half_len[0], ia.half_len[1])
+        : cpscIntersect(d1, d2, P1, r_cm, T, ia.pcanglsw[2 * pn1], ia.rcutSq, ia.half_len[0], ia.half_len[1]);
+}
+__device__ __forceinline__ int comboIntersect2(const PairParam& ia, const PView& a, const PView& b, const double3& r_cm,
+                                               int c, double* S) {
+    int pn2 = c >> 1;
+    double3 d1, d2;
+    comboAxes(ia, a, b, c, d1, d2);
+    PatchV P2{ld3(b.patch->pd[pn2]), ld3(b.patch->ps[2 * pn2]), ld3(b.patch->ps[2 * pn2 + 1])};
+    double3 mr = neg3(r_cm);
+    return ia.secondPsc
+        ? pscIntersect(d2, d1, P2, mr, S, ia.pcanglsw[2 * pn2 + 1], ia.rcutSq, ia.half_len[1], ia.half_len[0])
+        : cpscIntersect(d2, d1, P2, mr, S, ia.pcanglsw[2 * pn2 + 1], ia.rcutSq, ia.half_len[1], ia.half_len[0]);
+}
+__device__ __forceinline__ double comboAttrA(const PairParam& ia, const PView& a, const PView& b, const double3& r_cm,
+                                             int c, const double* T, const double* S, double* f0) {
+    double3 d1, d2;
+    comboAxes(ia, a, b, c, d1, d2);
+    return patchAttractionA(ia, d1, d2, r_cm, S[0], S[1], T[0], T[1], f0);
+}
+__device__ __forceinline__ void comboAttrB(const PairParam& ia, const PView& a, const PView& b, const double3& r_cm,
+                                           int c, const double* T, const double* S, double* f1, double* f2,
+                                           double* paral) {
+    int pn1 = c & 1, pn2 = c >> 1;
+    double3 d1, d2;
+    comboAxes(ia, a, b, c, d1, d2);
+    patchAttractionB(ia, d1, d2, ld3(a.patch->pd[pn1]), ld3(b.patch->pd[pn2]), r_cm, pn1, pn2, S[0], S[1], T[0], T[1],
+                     f1, f2, paral);
+}
+// The WCA chain of a patchy SC-SC pair: returns 0.0 + rep (callers pass non-bonded pairs),
+// *ok = the attractive branch is on.
+__device__ __forceinline__ double patchyWca(const PairParam& ia, const PView& a, const PView& b, const double3& r_cm,
+                                            int* ok) {
+    return simpleScRole0(ia, a, b, r_cm, ok);
 }
 
 // SC-SC pair (SpheroCylinder::operator(), paire.h:1122-1196).

@@ -72,7 +72,7 @@ struct PairParam {
     // and the pair is not bonded (the repulsive and attractive branches are both off).
     int screen;        // 0: none (spheres), 1: segment-segment, 2: point-segment, 3: always zero
     int scFirst;       // SC-sphere: 1 if the first particle is the spherocylinder
-    int simple;        // SC-SC pair of single-patch, non-chiral PSC/CPSC types (one patch combination)
+    int simple;        // SC-SC pair of patchy types (PSC / CPSC families): evaluated as parallel chains
     int pad2_;
     double screenSq;
     double scHalf;     // SC-sphere: half length of the spherocylinder

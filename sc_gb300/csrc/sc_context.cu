@@ -91,8 +91,7 @@ PairParam Context::devParam(int t1, int t2) const {
     } else if (p.kind == K_NONE) {
         p.screen = 3;
     }
-    p.simple = (p.kind == K_SC_PSC_CPSC || p.kind == K_SC_CPSC || p.kind == K_SC_PSC) && !p.fT && !p.sT && !p.fCH &&
-               !p.sCH;
+    p.simple = (p.kind == K_SC_PSC_CPSC || p.kind == K_SC_CPSC || p.kind == K_SC_PSC);   // patchy SC-SC
     return p;
 }
 
@@ -611,8 +610,9 @@ int sc_default_run(const sc_context* ctx, sc_run_params* p) {
     p->temper = o.temper;
     p->press = o.press;
     p->ptype = o.ptype;
-    p->volume_every = (o.shave > 0 && o.ptype == 1) ? (int)(1.0 / o.shave + 0.5) : 0;
-    if (p->volume_every < 1 && o.shave > 0 && o.ptype == 1) p->volume_every = 1;
+    // shave volume moves per sweep on average (updater.cpp:90), whatever the coupling type
+    p->volume_every = (o.shave > 0) ? (int)(1.0 / o.shave + 0.5) : 0;
+    if (p->volume_every < 1 && o.shave > 0) p->volume_every = 1;
     p->transmx = o.transmx;
     p->rot_angle = o.rot_angle;
     p->edge_mx = o.edge_mx;

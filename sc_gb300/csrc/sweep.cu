@@ -85,6 +85,7 @@ struct Control {
     int volValid;         // trial box keeps cells >= maxcut/s
     int pad_;
     double trialBox[3];
+    double pvTerm;        // volume move: P dV - N T ln(V'/V) of the proposal (per ptype)
     double energy;        // running total energy
     double energyCheck;   // last exact total energy
     double maxDrift;
@@ -128,6 +129,8 @@ struct SweepArgs {
     double chainFrac;       // chain move attempts per chain per sweep
     double chainR;          // bound on |particle - chain centre| (real space) the grid was sized for
     double volW[MAX_DEV_TYPES];   // Ia_param volume of each type (clusterCM weights)
+    int ptype;              // pressure coupling of volume moves (movecreator.cpp:349-546)
+    double boxMinChain[3];  // smallest box edges the chain grid allows (0: no chain phase)
 };
 
 __device__ __forceinline__ int wrapCell(double x, double shift, int nc) {
@@ -164,11 +167,67 @@ __global__ void kBeginSweep(const SweepArgs* __restrict__ A, int volumeDue) {
     }
     c.volValid = 0;
     if (volumeDue) {
-        c.psch = a.edgeMx * (r.next() - 0.5);
+        // MoveCreator::pressureMove (movecreator.cpp:330-546): the box proposal and the
+        // enthalpy term P dV - N T ln(V'/V) of each pressure coupling
+        const double* b = a.s.box;
+        double* tb = c.trialBox;
+        for (int d = 0; d < 3; ++d) tb[d] = b[d];
+        const double NT = (double)a.s.n * a.temper;
+        double pv = 0.0;
+        switch (a.ptype) {
+        case 0: {           // one edge, chosen at random
+            double rs = r.next();
+            int side = rs < 1.0 / 3.0 ? 0 : (rs < 2.0 / 3.0 ? 1 : 2);
+            double area = side == 0 ? b[1] * b[2] : (side == 1 ? b[0] * b[2] : b[0] * b[1]);
+            tb[side] += a.edgeMx * (r.next() - 0.5);
+            pv = a.press * area * (tb[side] - b[side]) - NT * log(tb[side] / b[side]);
+            break;
+        }
+        case 2: {           // x and y together, z constant
+            c.psch = a.edgeMx * (r.next() - 0.5);
+            double pvol = b[0] * b[1];
+            tb[0] += c.psch; tb[1] += c.psch;
+            double pvoln = tb[0] * tb[1];
+            pv = a.press * b[2] * (pvoln - pvol) - NT * log(pvoln / pvol);
+            break;
+        }
+        case 3: {           // x and y together, z keeps the volume
+            c.psch = a.edgeMx * (r.next() - 0.5);
+            double pvol = b[0] * b[1] * b[2];
+            tb[0] += c.psch; tb[1] += c.psch;
+            tb[2] = pvol / tb[0] / tb[1];
+            pv = 0.0;
+            break;
+        }
+        case 4: {           // x or y (the reference's test "if (ran2() - 0.5)" is true unless
+                            // the draw is exactly 0.5, so it changes x; kept as it is)
+            double pvol = b[0] * b[1];
+            if (r.next() - 0.5 != 0.0) tb[0] += a.edgeMx * (r.next() - 0.5);
+            else tb[1] += a.edgeMx * (r.next() - 0.5);
+            double pvoln = tb[0] * tb[1];
+            pv = a.press * b[2] * (pvoln - pvol) - NT * log(pvoln / pvol);
+            break;
+        }
+        case 5: {           // y only
+            double pvol = b[1];
+            tb[1] += a.edgeMx * (r.next() - 0.5);
+            pv = a.press * b[2] * b[0] * (tb[1] - pvol) - NT * log(tb[1] / pvol);
+            break;
+        }
+        default: {          // 1: isotropic
+            c.psch = a.edgeMx * (r.next() - 0.5);
+            double pvol = b[0] * b[1] * b[2];
+            for (int d = 0; d < 3; ++d) tb[d] += c.psch;
+            double pvoln = tb[0] * tb[1] * tb[2];
+            pv = a.press * (pvoln - pvol) - NT * log(pvoln / pvol);
+            break;
+        }
+        }
+        c.pvTerm = pv;
         bool ok = true;
         for (int d = 0; d < 3; ++d) {
-            c.trialBox[d] = a.s.box[d] + c.psch;
-            if (!(c.trialBox[d] > 0.0) || c.trialBox[d] / a.g.nc[d] * a.g.s[d] < a.g.maxcut) ok = false;
+            if (!(tb[d] > 0.0) || tb[d] / a.g.nc[d] * a.g.s[d] < a.g.maxcut) ok = false;
+            if (tb[d] < a.boxMinChain[d]) ok = false;      // the chain grid must stay valid too
         }
         c.volValid = ok ? 1 : 0;
     }
@@ -205,7 +264,7 @@ __global__ void kScan(const SweepArgs* __restrict__ A) {
     for (int base = 0; base < a.g.ncells; base += blockDim.x) {
         int k = base + threadIdx.x;
         int v = k < a.g.ncells ? a.cellCount[k] : 0;
-        if (v > kCellCap) atomicOr(a.err, E_CELL_OVERFLOW);
+        if (v > kCellCap && !a.chains) atomicOr(a.err, E_CELL_OVERFLOW);   // chain grids: any size
         int incl = v;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -452,9 +511,9 @@ __device__ __forceinline__ float dist2f(float4 a, float3 b, const double3& box) 
 
 constexpr int kClassCap = 768;       // stage-C queue entries per pair class
 
-// Pair class of the stage-C queue: 0 single-patch PSC/CPSC pairs (evaluated as three
-// parallel chains), 1 SC-sphere, 2 everything else.  Each class is evaluated by its own
-// warps, so a warp follows one functor's branches.
+// Pair class of the stage-C queue: 0 patchy SC-SC pairs (evaluated as parallel chains),
+// 1 SC-sphere, 2 everything else.  Each class is evaluated by its own warps, so a warp
+// follows one functor's branches.
 __device__ __forceinline__ int pairClass(const PairParam& pp) {
     return pp.simple ? 0 : (pp.kind >= K_MIX_SCA_SPA ? 1 : 2);
 }
@@ -462,12 +521,77 @@ __device__ __forceinline__ int pairClass(const PairParam& pp) {
 // Barrier of warps 0-2 only (warp 3 keeps evaluating other pairs meanwhile).
 __device__ __forceinline__ void barWarps012() { asm volatile("bar.sync 1, 96;" ::: "memory"); }
 
-// Stage-C scratch of the three-chain evaluation of class-0 pairs, 32 pairs per round.
+// Stage-C scratch of the parallel-chain evaluation of class-0 pairs, 32 pairs per round.
 struct SplitShared {
-    double T[32][2], S[32][2];
+    double T[4][32][2], S[4][32][2];     // intersections of each patch combination
     double e0[32];
-    int na[32], nb[32], ok[32];
+    double atrA[4][32], f0[4][32], f1[4][32], f2[4][32], paral[4][32];
+    int na[4][32], nb[4][32], ok[32];
 };
+
+// Up to 32 class-0 pairs (entries queue[r0, r0 + 32), get(entry, self, other) resolves one)
+// on warps 0-2.  The WCA chain and the two intersection chains of every valid patch
+// combination are separate tasks (task t: 0 WCA, 1 + 2c first and 2 + 2c second
+// intersection of combination c; warp w takes t = w, w + 3, w + 6), then the two halves of
+// the attraction of every combination with two intersections on each side (A on warp
+// c mod 3, B on warp c + 1 mod 3), then warp 0 adds them in combination order -- the
+// value of scScEnergy, whose loop runs the same chains one after another.  Returns the
+// pair energy of entry r0 + lane to the lanes of warp 0.
+__device__ __noinline__ void patchyTask(SplitShared& sp, const PairParam& ia, const PView& self, const PView& b,
+                                        const double3& r_cm, int t, int lane) {
+    if (t == 0) { sp.e0[lane] = patchyWca(ia, self, b, r_cm, &sp.ok[lane]); return; }
+    const int cc = (t - 1) >> 1;
+    const bool second = (t - 1) & 1;
+    if (!comboValid(ia, cc)) {
+        if (second) sp.nb[cc][lane] = 0; else sp.na[cc][lane] = 0;
+    } else if (second) {
+        sp.nb[cc][lane] = comboIntersect2(ia, self, b, r_cm, cc, sp.S[cc][lane]);
+    } else {
+        sp.na[cc][lane] = comboIntersect1(ia, self, b, r_cm, cc, sp.T[cc][lane]);
+    }
+}
+__device__ __noinline__ void patchyAttr(SplitShared& sp, const PairParam& ia, const PView& self, const PView& b,
+                                        const double3& r_cm, int warp, int lane) {
+    for (int cc = 0; cc < 4; ++cc) {
+        if (!(sp.na[cc][lane] >= 2 && sp.nb[cc][lane] >= 2)) continue;
+        if (warp == cc % 3)
+            sp.atrA[cc][lane] = comboAttrA(ia, self, b, r_cm, cc, sp.T[cc][lane], sp.S[cc][lane], &sp.f0[cc][lane]);
+        if (warp == (cc + 1) % 3)
+            comboAttrB(ia, self, b, r_cm, cc, sp.T[cc][lane], sp.S[cc][lane], &sp.f1[cc][lane], &sp.f2[cc][lane],
+                       &sp.paral[cc][lane]);
+    }
+}
+
+template <class Get>
+__device__ double patchyRound(SplitShared& sp, const DevCtx& c, const double3& box, const int* queue, int count,
+                              int r0, Get get) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool have = r0 + lane < count;
+    PView self, b;
+    const PairParam* iap = nullptr;
+    double3 r_cm = mk(0.0, 0.0, 0.0);
+    if (have) {
+        get(queue[r0 + lane], self, b);
+        iap = &c.params[self.type * c.ntypes + b.type];
+        r_cm = imageVec(self.pos, b.pos, box);
+        for (int t = warp; t < 9; t += 3) patchyTask(sp, *iap, self, b, r_cm, t, lane);
+    }
+    barWarps012();
+    if (have && sp.ok[lane]) patchyAttr(sp, *iap, self, b, r_cm, warp, lane);
+    barWarps012();
+    double e = 0.0;
+    if (warp == 0 && have) {
+        double atr = 0.0;
+        if (sp.ok[lane])
+            for (int cc = 0; cc < 4; ++cc)
+                if (sp.na[cc][lane] >= 2 && sp.nb[cc][lane] >= 2)
+                    atr += patchAttractionCombine(sp.atrA[cc][lane], sp.f0[cc][lane], sp.f1[cc][lane], sp.f2[cc][lane],
+                                                  sp.paral[cc][lane]);
+        e = sp.e0[lane] + atr;
+    }
+    barWarps012();            // the scratch is reused by the next round
+    return e;
+}
 
 // One move's proposal.  thrMet / thrStage1: the move is accepted when dE <= 0 or
 // dE < thr, thr = -T ln(u) -- the reference's exp(-dE/T) > u (movecreator.h:175-187)
@@ -894,6 +1018,11 @@ __global__ void __launch_bounds__(kMoveThreads) kColour(const SweepArgs* __restr
                 else evalEntry(sh.queueB[2][g - pad1]);
             }
         };
+        auto evalClass = [&](int cls, int w0, int nw) {     // one class over nw warps from w0
+            if (warp < w0 || warp >= w0 + nw) return;
+            const int n = cls == 1 ? qb1 : qb2;
+            for (int g = (warp - w0) * 32 + (tid & 31); g < n; g += nw * 32) evalEntry(sh.queueB[cls][g]);
+        };
         // warp 3 builds the next move's proposal while stage C runs (it stays valid unless
         // this move is accepted and the next one picks the same particle)
         auto speculate = [&]() {
@@ -910,38 +1039,22 @@ __global__ void __launch_bounds__(kMoveThreads) kColour(const SweepArgs* __restr
             const bool spec = last && m + 1 < cnt;
             if (qb0 > 0) {
                 if (warp < 3) {
-                    // class 0: warps 0, 1, 2 run the WCA chain and the two intersection
-                    // chains of 32 pairs side by side; warp 0 then adds the attraction
+                    // class 0: warps 0, 1, 2 run the pairs' independent FP64 chains side by side
+                    auto getPair = [&](int q, PView& self, PView& other) {
+                        self = (q & 1) ? newV : oldV;
+                        other = viewAt(a.s, candIdx[q >> 1]);
+                    };
                     for (int r0 = 0; r0 < qb0; r0 += 32) {
-                        const int k = r0 + lane;
-                        int q = 0, j = 0;
-                        if (k < qb0) {
-                            q = sh.queueB[0][k];
-                            j = candIdx[q >> 1];
-                            const PView& self = (q & 1) ? newV : oldV;
-                            PView b = viewAt(a.s, j);
-                            const PairParam& ia = c.params[self.type * c.ntypes + b.type];
-                            double3 r_cm = imageVec(self.pos, b.pos, box);
-                            if (warp == 0) sh.split.e0[lane] = simpleScRole0(ia, self, b, r_cm, &sh.split.ok[lane]);
-                            else if (warp == 1) sh.split.na[lane] = simpleScRole1(ia, self, b, r_cm, sh.split.T[lane]);
-                            else sh.split.nb[lane] = simpleScRole2(ia, self, b, r_cm, sh.split.S[lane]);
+                        double e = patchyRound(sh.split, c, box, sh.queueB[0], qb0, r0, getPair);
+                        if (warp == 0 && r0 + lane < qb0) {
+                            if (sh.queueB[0][r0 + lane] & 1) eNew += e; else eOld += e;
                         }
-                        barWarps012();
-                        if (warp == 0 && k < qb0) {
-                            const PView& self = (q & 1) ? newV : oldV;
-                            PView b = viewAt(a.s, j);
-                            const PairParam& ia = c.params[self.type * c.ntypes + b.type];
-                            double3 r_cm = imageVec(self.pos, b.pos, box);
-                            double e = simpleScCombine(ia, self, b, r_cm, sh.split.e0[lane], sh.split.ok[lane],
-                                                       sh.split.na[lane], sh.split.nb[lane], sh.split.T[lane],
-                                                       sh.split.S[lane]);
-                            if (q & 1) eNew += e; else eOld += e;
-                        }
-                        barWarps012();
                     }
+                    // the short class-2 pairs (sphere-sphere and others) on warps 1 and 2
+                    evalClass(2, 1, 2);
                 } else {
                     if (spec) speculate();
-                    evalGeneric(3, 1);
+                    evalClass(1, 3, 1);
                 }
             } else if (spec) {
                 if (warp == 3) speculate();
@@ -1214,7 +1327,8 @@ __global__ void __launch_bounds__(1024) kChainBin(const SweepArgs* __restrict__ 
 struct ChainShared {
     int list[kCellCap];
     int queueA[kQueueCap];
-    int queueB[kQueueCap];
+    int queueB[3][kClassCap];
+    SplitShared split;
     Stencil st;
     Scan scan;
     double red[kWarps][2];
@@ -1341,6 +1455,7 @@ __global__ void __launch_bounds__(kMoveThreads) kChainColour(const SweepArgs* __
     const int nCand = sh.st.nCand;
     const bool resident = nCand <= kCandCap;
     if (resident) loadCandidates(a, sh.st, 0, nCand, candIdx, candPos);
+    const int warp = tid >> 5;
     DevCtx c;
     c.params = a.t.params; c.mols = a.t.mols; c.ntypes = a.t.ntypes; c.n = a.s.n; c.sqmaxcut = a.t.sqmaxcut;
     const Con con = emptyCon(c);
@@ -1369,20 +1484,46 @@ __global__ void __launch_bounds__(kMoveThreads) kChainColour(const SweepArgs* __
             return v;
         };
         double eOld = 0.0, eNew = 0.0;
-        int qb = 0;
+        int qb0 = 0, qb1 = 0, qb2 = 0;
+        auto getPair = [&](int q, PView& self, PView& other) {
+            self = view((q >> 1) % kMaxChain, q & 1);
+            other = viewAt(a.s, candIdx[(q >> 1) / kMaxChain]);
+        };
+        auto evalEntry = [&](int q) {
+            PView self, other;
+            getPair(q, self, other);
+            unsigned bb; double dd;
+            double en = pairEnergy(c, self, other, con, box, &bb, &dd);
+            if (q & 1) eNew += en; else eOld += en;
+        };
+        auto evalClass = [&](int cls, int w0, int nw) {     // one class over nw warps from w0
+            if (warp < w0 || warp >= w0 + nw) return;
+            const int n = cls == 1 ? qb1 : qb2;
+            for (int g = (warp - w0) * 32 + (tid & 31); g < n; g += nw * 32) evalEntry(sh.queueB[cls][g]);
+        };
+        // stage C as in kColour: patchy SC-SC pairs as parallel chains on warps 0-2,
+        // SC-sphere pairs on warp 3, the rest on warps 1-2 afterwards
         auto flushC = [&]() {
             __syncthreads();
-            for (int e = tid; e < qb; e += kMoveThreads) {
-                int q = sh.queueB[e];
-                int isNew = q & 1, pi = (q >> 1) % kMaxChain, k = (q >> 1) / kMaxChain;
-                PView self = view(pi, isNew);
-                unsigned bb; double dd;
-                double en = pairEnergy(c, self, viewAt(a.s, candIdx[k]), con, box, &bb, &dd);
-                if (isNew) eNew += en; else eOld += en;
+            if (qb0 > 0) {
+                if (warp < 3) {
+                    for (int r0 = 0; r0 < qb0; r0 += 32) {
+                        double en = patchyRound(sh.split, c, box, sh.queueB[0], qb0, r0, getPair);
+                        if (warp == 0 && r0 + (tid & 31) < qb0) {
+                            if (sh.queueB[0][r0 + (tid & 31)] & 1) eNew += en; else eOld += en;
+                        }
+                    }
+                    evalClass(2, 1, 2);
+                } else {
+                    evalClass(1, 3, 1);
+                }
+            } else {
+                evalClass(1, 0, 2);
+                evalClass(2, 2, 2);
             }
             __syncthreads();
-            nEval += qb;
-            qb = 0;
+            nEval += qb0 + qb1 + qb2;
+            qb0 = qb1 = qb2 = 0;
         };
         for (int wbase = 0; wbase < nCand; wbase += kCandCap) {
             const int wlen = min(kCandCap, nCand - wbase);
@@ -1413,7 +1554,7 @@ __global__ void __launch_bounds__(kMoveThreads) kChainColour(const SweepArgs* __
                 }
                 __syncthreads();
                 for (int e0 = 0; e0 < qa; e0 += kMoveThreads) {             // stage B
-                    int e = e0 + tid, keep = 0, q = 0;
+                    int e = e0 + tid, keep = 0, q = 0, cls = 0;
                     if (e < qa) {
                         q = sh.queueA[e];
                         int isNew = q & 1, pi = (q >> 1) % kMaxChain, k = (q >> 1) / kMaxChain;
@@ -1425,13 +1566,20 @@ __global__ void __launch_bounds__(kMoveThreads) kChainColour(const SweepArgs* __
                             double4_32a dj = a.s.dir[j];
                             const PairParam& pp = c.params[self.type * c.ntypes + (int)pj.w];
                             keep = screenedOut(pp, r, self.dir, mk(dj.x, dj.y, dj.z)) ? 0 : 1;
+                            cls = pairClass(pp);
                         }
                     }
                     int tot;
-                    int off = blockExclusiveScan(keep, tot, sh.scan);
-                    if (keep) sh.queueB[qb + off] = q;
-                    qb += tot;
-                    if (qb > kQueueCap - kMoveThreads) flushC();
+                    int off = blockExclusiveScan(keep ? (1 << (10 * cls)) : 0, tot, sh.scan);
+                    if (keep) {
+                        int base0 = cls == 0 ? qb0 : (cls == 1 ? qb1 : qb2);
+                        sh.queueB[cls][base0 + ((off >> (10 * cls)) & 1023)] = q;
+                    }
+                    qb0 += tot & 1023;
+                    qb1 += (tot >> 10) & 1023;
+                    qb2 += (tot >> 20) & 1023;
+                    if (qb0 > kClassCap - kMoveThreads || qb1 > kClassCap - kMoveThreads || qb2 > kClassCap - kMoveThreads)
+                        flushC();
                 }
             }
             flushC();          // queue entries index the window
@@ -1638,9 +1786,7 @@ __global__ void kVolumeAccept(const SweepArgs* __restrict__ A) {
         return;
     }
     double eNew = sumPartials(a.partial, a.g.ncells);
-    double pvol = a.s.box[0] * a.s.box[1] * a.s.box[2];
-    double pvoln = c.trialBox[0] * c.trialBox[1] * c.trialBox[2];
-    double enermove = a.press * (pvoln - pvol) - (double)a.s.n * a.temper * log(pvoln / pvol);
+    double enermove = c.pvTerm;
     enermove += eNew;
     Stream r(a.seed, 0xFFFFFFF1u, (uint32_t)c.sweep, (uint32_t)(c.sweep >> 32));
     double u = r.next();
@@ -1889,6 +2035,7 @@ static void fillArgs(Context* c, SweepEngine* e, const sc_run_params& p) {
     a.press = p.press;
     a.rotAngle = p.rot_angle;
     a.edgeMx = p.edge_mx;
+    a.ptype = p.ptype;
     for (size_t k = 0; k < c->usedTypes.size() && k < (size_t)MAX_DEV_TYPES; ++k) {
         int t = c->usedTypes[k];
         // per-type displacement (sim.h:368-373); the run's transmx replaces the options value
@@ -1988,6 +2135,9 @@ static int prepareChains(Context* c, SweepEngine* e, const sc_run_params& p, con
     a.chainFrac = p.chainprob * (double)n / (double)C.nChains;   // N * chainprob chain moves per sweep
     a.chainR = C.R;
     C.on = true;
+    // volume moves must leave the chain cells wide enough as well
+    for (int d = 0; d < 3; ++d) e->args.boxMinChain[d] = g.nc[d] * g.maxcut / g.s[d];
+    a.boxMinChain[0] = a.boxMinChain[1] = a.boxMinChain[2] = 0.0;
     return SC_OK;
 }
 
@@ -2120,7 +2270,7 @@ struct RunOut {
 // exchange follows every exchangeEvery sweeps.
 static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchangeEvery, uint64_t exSeed, RunOut& out) {
     const int ns = (int)b.sys.size();
-    const bool npt = p.ptype == 1 && p.volume_every > 0;
+    const bool npt = p.volume_every > 0;
     cudaStream_t s = b.stream;
     cudaError_t r;
     int rc;
@@ -2311,7 +2461,7 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
 static int checkParams(const sc_run_params& p) {
     if (p.nsweeps < 0) return fail(SC_ERR_ARG, "nsweeps must be >= 0");
     if (!(p.temper > 0)) return fail(SC_ERR_ARG, "temper must be positive");
-    if (p.ptype != 0 && p.ptype != 1) return fail(SC_ERR_UNSUPPORTED, "only ptype 1 (isotropic) volume moves run on the GPU");
+    if (p.ptype < 0 || p.ptype > 5) return fail(SC_ERR_ARG, "ptype must be 0..5 (movecreator.cpp:349-546)");
     if (p.stencil < 0 || p.stencil > 3) return fail(SC_ERR_ARG, "stencil must be 0 (auto), 1, 2 or 3");
     return SC_OK;
 }
@@ -2322,7 +2472,7 @@ int runSweeps(Context* c, const sc_run_params& p, sc_run_stats& st) {
     if (rc) return rc;
     if (c->conf.p.empty()) return SC_OK;
     if (p.delayed && !c->surrogate) return fail(SC_ERR_STATE, "delayed = 1 needs a surrogate (sc_set_surrogate)");
-    const bool npt = p.ptype == 1 && p.volume_every > 0;
+    const bool npt = p.volume_every > 0;
     if ((rc = prepareSystem(c, p, npt))) return rc;
     if (!c->batch) {
         c->batch = new Batch();
@@ -2401,7 +2551,7 @@ int runReplicas(void* h, const sc_run_params& p, int exchangeEvery, sc_run_stats
     if (rc) return rc;
     Batch& b = R->b;
     const int nrep = (int)b.sys.size();
-    const bool npt = p.ptype == 1 && p.volume_every > 0;
+    const bool npt = p.volume_every > 0;
     for (int k = 0; k < nrep; ++k) {
         Context* c = b.sys[k];
         if (c->conf.p.empty()) return fail(SC_ERR_ARG, "a replica holds no particles");

@@ -213,6 +213,92 @@ def rods_in_spheres(n_side=21, n_rods=2, L=6.0, edge=34.0, seed=1, temper=1.0):
     return opts, top, config_text(box, pos, dirs, _perp(rng, dirs))
 
 
+LIPID_TOP = ("[Types]\n"
+             "H 1 SPN 1.0 1.0\n"
+             "T 2 TPSC 1.0 1.0 1.12 0.2 90.0 10.0 2.0 0.0 180.0 90.0 10.0\n"
+             "[Molecules]\nL: {\nparticles: 1\nparticles: 2\nparticles: 2\nbond1: 50.0 1.0\n}\n")
+
+
+def _lipid(centre_head, u):
+    """Particle centres of a straight lipid whose head sits at centre_head, tails along -u:
+    bonds (50 kT, rest length 1) join the head centre to the first tail's +u end and the
+    tails' facing ends."""
+    return [centre_head, centre_head - 2.0 * u, centre_head - 5.0 * u]
+
+
+def _lipid_texts(box, heads, axes, rng, opts):
+    pos, dirs = [], []
+    for h, u in zip(heads, axes):
+        pos += _lipid(h, u)
+        dirs += [u, u, u]
+    pos, dirs = np.array(pos), np.array(dirs)
+    # each particle's axis tilted by ~0.03 rad on its own: exactly collinear bonded tails sit
+    # on the reference's intersection branch points (its pair energy jumps there, so the
+    # energy of a chain would change under a rigid move by rounding alone)
+    dirs = dirs + 0.03 * rng.normal(size=dirs.shape)
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    top = LIPID_TOP + f"[System]\nL {len(heads)}\n"
+    return opts, top, config_text(box, pos, dirs, _perp(rng, dirs))
+
+
+def lipids_dilute(n=64, edge=14.0, seed=1, temper=1.5, chainprob=0.2):
+    """n three-bead lipids (SPN head, two TPSC tails of length 2, bonds k=50, r0=1) at random,
+    non-overlapping positions and orientations in a cubic box."""
+    rng = np.random.default_rng(seed)
+    box = np.full(3, edge)
+    heads, axes, segs = [], [], []
+    while len(heads) < n:
+        h = rng.uniform(0, edge, 3)
+        u = _unit(rng, 1)[0]
+        mine = [(c, l) for c, l in zip(_lipid(h, u), (0.0, 1.0, 1.0))]
+        ok = True
+        for (c1, l1) in mine:
+            for (c2, d2, l2) in segs:
+                r = c1 - c2
+                r -= box * np.round(r / box)
+                if np.linalg.norm(r) > l1 + l2 + 1.05:
+                    continue
+                if _segdist(c2 + r, u, l1, c2[None, :], d2[None, :], np.array([l2]))[0] < 1.05:
+                    ok = False
+                    break
+            if not ok:
+                break
+        if ok:
+            heads.append(h)
+            axes.append(u)
+            segs += [(c, u, l) for c, l in mine]
+    opts = options_text(ptype=0, transmx=0.3, rotmx=20.0, temper=temper, seed=seed, chainprob=chainprob,
+                        chainmmx=0.3, chainrmx=15.0)
+    return _lipid_texts(box, np.array(heads), np.array(axes), rng, opts)
+
+
+def bilayers(n_side=50, box=(60.0, 60.0, 40.0), seed=1, temper=1.0, chainprob=0.1):
+    """Lipid bilayers: 4 n_side^2 three-bead lipids (10,000 for n_side = 50) in two flat
+    bilayers normal to z (centred at a quarter and three quarters of the box height), heads
+    on a square lattice of spacing box_x / n_side in each leaflet, tails towards the
+    bilayer middle."""
+    rng = np.random.default_rng(seed)
+    box = np.asarray(box, float)
+    a = box[0] / n_side
+    g = (np.arange(n_side) + 0.5) * a
+    xy = np.stack(np.meshgrid(g, g, indexing="ij"), -1).reshape(-1, 2)
+    heads, axes = [], []
+    for zc in (0.25 * box[2], 0.75 * box[2]):
+        for side in (+1.0, -1.0):
+            # the lower leaflet is shifted by half a spacing and every lipid tilted by up to
+            # 0.05 rad: exactly stacked, parallel tails make the reference's patch angle
+            # 0/0 (perpendicular part of a vector along the axis)
+            off = 0.0 if side > 0 else 0.5 * a
+            for x, y in xy:
+                tilt, az = rng.uniform(0.01, 0.05), rng.uniform(0, 2 * math.pi)
+                u = side * np.array([math.sin(tilt) * math.cos(az), math.sin(tilt) * math.sin(az), math.cos(tilt)])
+                heads.append(np.array([x + off, y + off, zc + side * 6.5]))
+                axes.append(u)
+    opts = options_text(ptype=0, transmx=0.3, rotmx=20.0, temper=temper, seed=seed, chainprob=chainprob,
+                        chainmmx=0.3, chainrmx=15.0)
+    return _lipid_texts(box, np.array(heads), np.array(axes), rng, opts)
+
+
 def pt_ladders(n_ladders=8, per_ladder=8, seed=1, n_range=(500, 4000), phi_range=(0.10, 0.25), t_range=(0.8, 1.6)):
     """Parallel-tempering replicas of the PSC model with uneven sizes: n_ladders systems
     (N and packing fraction drawn uniformly), each replicated over a geometric
@@ -231,4 +317,5 @@ WORKLOADS = {
     "npt_cpsc_spa_4000": lambda seed=1: npt_cpsc_spa(4000, seed=seed),
     "nvt_psc_1000": lambda seed=1: nvt_psc(1000, seed=seed),
     "psc_cpsc_65536": lambda seed=1: psc_cpsc(65536, seed=seed),
+    "bilayer_30000": lambda seed=1: bilayers(50, seed=seed),
 }

@@ -86,6 +86,18 @@ def cases():
         opts=dict(temper=1.0, press=0.5, ptype=1, shave=1, edge_mx=0.25, transmx=0.35, rotmx=30.0,
                   pairlist_update=0),
         nsweeps=16000, report=20, seeds=6, burn=4000)
+    # three-bead lipids (SPN head, two TPSC tails, bond1), chain + single-particle moves, NVT
+    sys.path.insert(0, REPO)
+    from sc_gb300 import workloads
+
+    opts_text, top, config = workloads.lipids_dilute(64, seed=3)
+    lip_opts = dict(l.split(" = ") for l in opts_text.strip().splitlines())
+    out["lipids_chain"] = dict(
+        top=top, config=config, n_particles=192,
+        opts=dict(temper=1.5, transmx=0.3, rotmx=20.0, chainprob=0.2, chainmmx=0.3, chainrmx=15.0,
+                  pairlist_update=10),
+        nsweeps=30000, report=20, seeds=6, burn=5000)
+    assert float(lip_opts["chainprob"]) == 0.2
     return out
 
 
@@ -126,11 +138,15 @@ def block_stats(series_per_seed, burn):
 
 def main():
     subprocess.run(["make", "-C", os.path.join(REPO, "oracle"), "ref", "-j8"], check=True, capture_output=True)
+    only = sys.argv[1:]
     for name, c in cases().items():
+        if only and name not in only:
+            continue
         with ThreadPoolExecutor(max_workers=min(8, c["seeds"])) as ex:
             runs = list(ex.map(lambda s: run_one(c, s), [1000 + k for k in range(c["seeds"])]))
-        n = sum(cnt for _, cnt in [tuple(l.split()) for l in c["top"].split("[System]\n")[1].splitlines() if l.strip()]
-                for cnt in [int(cnt)])
+        n = c.get("n_particles") or sum(
+            cnt for _, cnt in [tuple(l.split()) for l in c["top"].split("[System]\n")[1].splitlines() if l.strip()]
+            for cnt in [int(cnt)])
         e_ser = [[(s, en / n) for s, en, _ in r["energy"]] for r in runs]
         a_ser = [[(s, al / n) for s, _, al in r["energy"]] for r in runs]
         v_ser = [[(s, v / n) for s, v in r["volume"]] for r in runs]

@@ -117,6 +117,32 @@ def test_volume_moves_change_box_and_keep_energy_exact():
     s.close()
 
 
+@pytest.mark.parametrize("ptype", [0, 2, 3, 4, 5])
+def test_pressure_couplings_change_the_box_as_the_reference(ptype):
+    """MoveCreator::pressureMove (movecreator.cpp:330-546): which edges a volume move changes,
+    and the running energy stays exact."""
+    e, s = open_ens("cpsc_spa_npt")
+    b0 = s.box.copy()
+    p = s.default_run()
+    st = s.simulate(p, nsweeps=200, seed=31, check_every=100, ptype=ptype)
+    assert st.acc_vol + st.rej_vol == 200 and st.acc_vol > 0
+    b1 = s.box
+    same = np.isclose(b1, b0, rtol=0, atol=0)
+    if ptype == 2:
+        assert same[2] and not same[0] and np.isclose(b1[0], b1[1])
+    elif ptype == 3:
+        assert not same[0] and abs(np.prod(b1) / np.prod(b0) - 1) < 1e-9
+    elif ptype == 4:
+        assert not same[0] and same[1] and same[2]
+    elif ptype == 5:
+        assert same[0] and not same[1] and same[2]
+    else:
+        assert not same.all() and len(set(np.round(b1, 12))) > 1
+    e1 = exact_energy(s)
+    assert abs(st.energy - e1) <= 1e-9 * max(1.0, abs(e1))
+    s.close()
+
+
 def alignment_order(s):
     """Updater::alignmentOrder (scOOP/mc/updater.cpp:466-481)."""
     parts = s.particles()
