@@ -116,6 +116,20 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
+def profiled_traffic(kernel, workload):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary of this workload
+    (profiles/<kernel>_<workload>.md, line 'traffic_bytes_per_launch = N'), else None."""
+    import re
+
+    path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
+    try:
+        with open(path) as f:
+            m = re.search(r"traffic_bytes_per_launch\s*=\s*([0-9.eE+]+)", f.read())
+        return float(m.group(1)) if m else None
+    except OSError:
+        return None
+
+
 def open_workload(name, seed):
     from sc_gb300 import System, workloads
 
@@ -473,7 +487,9 @@ def main():
     t_launch = prof.phase_seconds / max(1, prof.phase_launches)
     achieved = bytes_per_launch / t_launch / 1e9 if t_launch > 0 else None
     roof = {"bound": "hbm", "kernel": "kColour", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-            "frac": (achieved / peaks["hbm_gbs"]) if achieved else None, "traffic": None,
+            "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
+            "traffic": profiled_traffic("kColour", a.workload),
+            "traffic_source": f"profiles/kColour_{a.workload}.md (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
             "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
             "avg_launch_us": t_launch * 1e6, "algorithmic_bytes_per_launch": bytes_per_launch,
             "note": "the move kernel is FP64-latency bound; see fp64 for its arithmetic rate"}

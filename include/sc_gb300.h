@@ -164,6 +164,9 @@ int sc_one_to_all(sc_context* ctx, int ntargets, const int* targets, double* e);
 int sc_one_to_all_noalloc(sc_context* ctx, int ntargets, const int* targets, double* e);
 /* TotalEMatrix::allToAll (totalenergycalculator.h:334-353, 502-521). */
 int sc_all_to_all(sc_context* ctx, double* e);
+/* Updater::alignmentOrder (scOOP/mc/updater.cpp:466-481): sum of axis dot products over pairs
+ * whose centres are closer than 1.5 (the second column of energy.dat). */
+int sc_alignment_order(sc_context* ctx, double* order);
 /* TotalEMatrix::mol2othersTrial (totalenergycalculator.h:453-499). */
 int sc_mol_to_others(sc_context* ctx, int first, int size, double* e);
 /* The energy half of MoveCreator::partDisplace / partRotate (movecreator.cpp:947-1028):

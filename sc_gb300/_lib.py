@@ -92,6 +92,7 @@ SIGNATURES = [
     ("sc_one_to_all", C.c_int, [_P, C.c_int, _I, _D]),
     ("sc_one_to_all_noalloc", C.c_int, [_P, C.c_int, _I, _D]),
     ("sc_all_to_all", C.c_int, [_P, _D]),
+    ("sc_alignment_order", C.c_int, [_P, _D]),
     ("sc_mol_to_others", C.c_int, [_P, C.c_int, C.c_int, _D]),
     ("sc_trial_displace", C.c_int, [_P, C.c_int, _D, _D, _D]),
     ("sc_trial_rotate", C.c_int, [_P, C.c_int, C.c_double, _D, C.c_int, _D, _D, C.POINTER(Particle)]),

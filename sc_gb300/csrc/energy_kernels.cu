@@ -130,6 +130,33 @@ __global__ void __launch_bounds__(kAllBlock) kAllToAll(DevState s, DevTables t, 
     if (threadIdx.x == 0) partial[blockIdx.x] = v;
 }
 
+// Updater::alignmentOrder (scOOP/mc/updater.cpp:466-481): sum of dir_i . dir_j over pairs
+// closer than 1.5 (minimum image, centres); thread per row pair (i, n-1-i), j > i.
+__global__ void __launch_bounds__(kAllBlock) kAlignment(DevState s, double* partial) {
+    double3 box = mk(s.box[0], s.box[1], s.box[2]);
+    double sum = 0.0;
+    int half = (s.n + 1) / 2;
+    int r = blockIdx.x * kAllBlock + threadIdx.x;
+    if (r < half) {
+        int rows[2] = {r, s.n - 1 - r};
+        for (int q = 0; q < 2; ++q) {
+            int i = rows[q];
+            if (q == 1 && i == rows[0]) break;
+            double4_32a pi = s.pos[i], di = s.dir[i];
+            for (int j = i + 1; j < s.n; ++j) {
+                double4_32a pj = s.pos[j];
+                double3 rc = imageVec(mk(pi.x, pi.y, pi.z), mk(pj.x, pj.y, pj.z), box);
+                if (dot3(rc, rc) < 1.5 * 1.5) {
+                    double4_32a dj = s.dir[j];
+                    sum += di.x * dj.x + di.y * dj.y + di.z * dj.z;
+                }
+            }
+        }
+    }
+    double v = blockSum<kAllBlock>(sum);
+    if (threadIdx.x == 0) partial[blockIdx.x] = v;
+}
+
 __global__ void kFinalSum(const double* partial, int n, double* out) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         double r = 0.0;
@@ -175,6 +202,14 @@ cudaError_t launchOneToAll(const DevState& s, const DevTables& t, int ntargets, 
 }
 
 int allToAllBlocks(int n) { return ((n + 1) / 2 + kAllBlock - 1) / kAllBlock; }
+
+cudaError_t launchAlignment(const DevState& s, double* partial, int npartial, double* out, cudaStream_t st) {
+    int nb = allToAllBlocks(s.n);
+    if (nb > npartial) return cudaErrorInvalidValue;
+    if (nb > 0) kAlignment<<<nb, kAllBlock, 0, st>>>(s, partial);
+    kFinalSum<<<1, 32, 0, st>>>(partial, nb, out);
+    return cudaGetLastError();
+}
 
 cudaError_t launchAllToAll(const DevState& s, const DevTables& t, const double* boxOverride, double* partial,
                            int npartial, double* out, cudaStream_t st) {

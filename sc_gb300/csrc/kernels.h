@@ -41,6 +41,8 @@ cudaError_t launchOneToAll(const DevState& s, const DevTables& t, int ntargets, 
 cudaError_t launchAllToAll(const DevState& s, const DevTables& t, const double* boxOverride, double* partial,
                            int npartial, double* out, cudaStream_t st);
 int allToAllBlocks(int n);
+// Updater::alignmentOrder: sum of axis dot products over pairs closer than 1.5.
+cudaError_t launchAlignment(const DevState& s, double* partial, int npartial, double* out, cudaStream_t st);
 // mol2othersTrial: molecule [first, first+size) against the rest with an empty conlist.
 cudaError_t launchMolToOthers(const DevState& s, const DevTables& t, int first, int size, double* out, cudaStream_t st);
 

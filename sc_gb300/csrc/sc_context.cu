@@ -484,6 +484,19 @@ int sc_all_to_all(sc_context* ctx, double* out) {
     return SC_OK;
 }
 
+int sc_alignment_order(sc_context* ctx, double* out) {
+    if (!ctx || !out) return fail(SC_ERR_ARG, "null argument");
+    Context* c = C(ctx);
+    int rc = c->ensureDevice();
+    if (rc) return rc;
+    if (c->hostNewer && (rc = c->uploadState())) return rc;
+    cudaError_t e;
+    if ((e = launchAlignment(c->d, c->dPartial, c->nPartial, c->dScalars, c->stream)) != cudaSuccess) return cudaFail(e, "alignment kernel");
+    if ((e = cudaMemcpyAsync(out, c->dScalars, sizeof(double), cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess) return cudaFail(e, "copy");
+    if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess) return cudaFail(e, "alignment");
+    return SC_OK;
+}
+
 int sc_mol_to_others(sc_context* ctx, int first, int size, double* out) {
     if (!ctx || !out) return fail(SC_ERR_ARG, "null argument");
     Context* c = C(ctx);

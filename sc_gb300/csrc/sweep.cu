@@ -124,6 +124,7 @@ struct SweepArgs {
     int* chainCellStart;
     int* chainCellCount;
     int* chainCellIdx;
+    int* slotOf;            // chain grid: slot of each particle in cellIdx (written by kSortCells)
     double chainMx;         // chain displacement length
     double chainAngle;      // chain rotation angle bound
     double chainFrac;       // chain move attempts per chain per sweep
@@ -310,6 +311,7 @@ __global__ void kSortCells(const SweepArgs* __restrict__ A) {
     for (int k = 0; k < n; ++k) {
         double4_32a p = a.s.pos[v[k]];
         a.cellPosF[s + k] = make_float4(frac32(p.x), frac32(p.y), frac32(p.z), (float)p.w);
+        if (a.slotOf) a.slotOf[v[k]] = s + k;
         if (a.mlp) {
             double4_32a d = a.s.dir[v[k]];
             const PatchSet& ps = a.s.patch[v[k]];
@@ -1332,9 +1334,11 @@ struct ChainShared {
     Stencil st;
     Scan scan;
     double red[kWarps][2];
+    int nearIdx[kCandCap];      // candidates within reach of the chain (old or new centre)
     int first, size, displace, skip, constrained;
     double thr;
     double cm[3];
+    float3 cmOldF, cmNewF;
     double npos[kMaxChain][3], ndir[kMaxChain][3];
     PatchSet npatch[kMaxChain];
     float3 oldF[kMaxChain], newF[kMaxChain];
@@ -1419,6 +1423,8 @@ __device__ void buildChainProposal(const SweepArgs& a, ChainShared& sh, int cell
         sh.first = first;
         sh.size = size;
         sh.displace = displace;
+        sh.cmOldF = make_float3(frac32(cm.x), frac32(cm.y), frac32(cm.z));
+        sh.cmNewF = make_float3(frac32(x), frac32(y), frac32(z));
         sh.skip = (!inside || wide) ? 1 : 0;
         sh.constrained = wide ? 1 : 0;
         Stream ru(a.seed ^ 0xD1B54A32D192ED03ull, (uint32_t)cell, (uint32_t)m, sk);
@@ -1461,6 +1467,8 @@ __global__ void __launch_bounds__(kMoveThreads) kChainColour(const SweepArgs* __
     const Con con = emptyCon(c);
     const double3 box = mk(a.s.box[0], a.s.box[1], a.s.box[2]);
     const float thr32 = candThreshold(c.sqmaxcut, box);
+    const float reachNear = sqrtf(thr32) + (float)a.chainR + 1e-3f;
+    const float thrNear = reachNear * reachNear * 1.0001f;
     double dECell = 0.0;
     unsigned long long nAcc = 0, nRej = 0, nConstr = 0, nTested = 0, nEval = 0;
 
@@ -1528,22 +1536,38 @@ __global__ void __launch_bounds__(kMoveThreads) kChainColour(const SweepArgs* __
         for (int wbase = 0; wbase < nCand; wbase += kCandCap) {
             const int wlen = min(kCandCap, nCand - wbase);
             if (!resident) loadCandidates(a, sh.st, wbase, wlen, candIdx, candPos);
-            const int total = wlen * size;
+            // stage A0: the candidates within chainR + cut-off of the old or the new centre
+            // (every chain particle lies within chainR of its centre), outside the chain
+            int nNear = 0;
+            for (int r0 = 0; r0 < wlen; r0 += kMoveThreads) {
+                int k = r0 + tid, flag = 0;
+                if (k < wlen) {
+                    int j = candIdx[k];
+                    if (j < first || j >= first + size) {
+                        float4 cp = candPos[k];
+                        flag = (dist2f(cp, sh.cmOldF, box) <= thrNear || dist2f(cp, sh.cmNewF, box) <= thrNear) ? 1 : 0;
+                    }
+                }
+                int tot;
+                int off = blockExclusiveScan(flag, tot, sh.scan);
+                if (flag) sh.nearIdx[nNear + off] = k;
+                nNear += tot;
+            }
+            __syncthreads();
+            const int total = nNear * size;
             for (int base = 0; base < total; base += kChunk) {
                 const int end = min(base + kChunk, total);
                 int qa = 0;
                 for (int r0 = base; r0 < end; r0 += kMoveThreads) {     // stage A
                     int idx = r0 + tid, flags = 0, k = 0, pi = 0;
                     if (idx < end) {
-                        k = idx / size;
-                        pi = idx - k * size;
-                        int j = candIdx[k];
-                        if (j < first || j >= first + size) {
-                            float4 cp = candPos[k];
-                            bool p0 = dist2f(cp, sh.oldF[pi], box) <= thr32;
-                            bool p1 = dist2f(cp, sh.newF[pi], box) <= thr32;
-                            flags = (p0 ? 1 : 0) | (p1 ? 2 : 0);
-                        }
+                        int kk = idx / size;
+                        pi = idx - kk * size;
+                        k = sh.nearIdx[kk];
+                        float4 cp = candPos[k];
+                        bool p0 = dist2f(cp, sh.oldF[pi], box) <= thr32;
+                        bool p1 = dist2f(cp, sh.newF[pi], box) <= thr32;
+                        flags = (p0 ? 1 : 0) | (p1 ? 2 : 0);
                     }
                     int tot;
                     int off = blockExclusiveScan(__popc(flags), tot, sh.scan);
@@ -1604,17 +1628,12 @@ __global__ void __launch_bounds__(kMoveThreads) kChainColour(const SweepArgs* __
                 a.s.patch[i] = sh.npatch[tid];
             }
             // the particle's entry in this grid's cell list (and in shared memory)
-            int pc = a.cellOf[i];
-            int s0 = a.cellStart[pc], n0 = a.cellCount[pc];
+            const int pc = a.cellOf[i], slot = a.slotOf[i];
             float4 nf = make_float4(sh.newF[tid].x, sh.newF[tid].y, sh.newF[tid].z, (float)p.w);
-            for (int k = 0; k < n0; ++k)
-                if (a.cellIdx[s0 + k] == i) {
-                    a.cellPosF[s0 + k] = nf;
-                    if (resident)
-                        for (int q = 0; q < sh.st.nNb; ++q)
-                            if (sh.st.nbCell[q] == pc) candPos[sh.st.nbOff[q] + k] = nf;
-                    break;
-                }
+            a.cellPosF[slot] = nf;
+            if (resident)
+                for (int q = 0; q < sh.st.nNb; ++q)
+                    if (sh.st.nbCell[q] == pc) candPos[sh.st.nbOff[q] + (slot - a.cellStart[pc])] = nf;
         }
         __syncthreads();
     }
@@ -1882,6 +1901,7 @@ struct SweepEngine {
         Grid g{};
         Control* ctl = nullptr;
         int *cellStart = nullptr, *cellCount = nullptr, *cellCursor = nullptr, *cellIdx = nullptr, *cellOf = nullptr;
+        int* slotOf = nullptr;
         float4* cellPosF = nullptr;
         double* cellDE = nullptr;
         int2* chains = nullptr;
@@ -2070,6 +2090,7 @@ static int prepareChains(Context* c, SweepEngine* e, const sc_run_params& p, con
         cudaMemset(C.ctl, 0, sizeof(Control));
         if ((rc = engineAlloc(e, (void**)&C.cellIdx, sizeof(int) * n))) return rc;
         if ((rc = engineAlloc(e, (void**)&C.cellOf, sizeof(int) * n))) return rc;
+        if ((rc = engineAlloc(e, (void**)&C.slotOf, sizeof(int) * n))) return rc;
         if ((rc = engineAlloc(e, (void**)&C.cellPosF, sizeof(float4) * n))) return rc;
         if ((rc = engineAlloc(e, (void**)&C.chains, sizeof(int2) * chains.size()))) return rc;
         if ((rc = engineAlloc(e, (void**)&C.chIdx, sizeof(int) * chains.size()))) return rc;
@@ -2123,6 +2144,7 @@ static int prepareChains(Context* c, SweepEngine* e, const sc_run_params& p, con
     a.ctl = C.ctl;
     a.cellStart = C.cellStart; a.cellCount = C.cellCount; a.cellCursor = C.cellCursor; a.cellIdx = C.cellIdx;
     a.cellOf = C.cellOf; a.cellPosF = C.cellPosF; a.cellDE = C.cellDE;
+    a.slotOf = C.slotOf;
     a.cellDirF = a.cellPatF = nullptr;
     a.mlp = nullptr;
     a.seed = p.seed ^ 0x6A09E667F3BCC909ull;
@@ -2286,6 +2308,9 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
             cudaSuccess)
             return cudaFail(r, "shared memory attribute");
         if ((r = cudaFuncSetAttribute(kCellEnergy, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDynSmem)) != cudaSuccess)
+            return cudaFail(r, "shared memory attribute");
+        if ((r = cudaFuncSetAttribute(kChainColour, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDynSmem)) !=
+            cudaSuccess)
             return cudaFail(r, "shared memory attribute");
         attrSet = true;
     }

@@ -133,6 +133,12 @@ class System:
         L.check(self._lib.sc_all_to_all(self._h, C.byref(e)))
         return e.value
 
+    def alignment_order(self):
+        """Updater::alignmentOrder: sum of axis dot products over pairs closer than 1.5."""
+        e = C.c_double()
+        L.check(self._lib.sc_alignment_order(self._h, C.byref(e)))
+        return e.value
+
     def mol2others(self, first, size):
         e = C.c_double()
         L.check(self._lib.sc_mol_to_others(self._h, first, size, C.byref(e)))

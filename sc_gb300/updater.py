@@ -1,0 +1,65 @@
+"""The output side of Updater::simulate (scOOP/mc/updater.cpp:45-389) around the GPU move loop.
+
+The reference appends, every `report` sweeps, the exact total energy and the alignment
+order to energy.dat and the box volume to stat.dat (updater.cpp:313-318), every `movie`
+sweeps a frame to the movie file (Updater::dumpMovie, updater.h:82-93, with Conf::draw,
+Conf.h:388-424), and at the end writes config.last (Conf.h:413-422).  `run` does the same
+around blocks of GPU sweeps, in the reference's formats.
+"""
+import os
+
+
+def _frame(system, sweep):
+    parts = system.particles()
+    box = system.box
+    lines = [f"{len(parts)}", f"sweep {sweep}; box {box[0]:.10f} {box[1]:.10f} {box[2]:.10f}"]
+    for p in parts:
+        # Conf::draw: wrapped real-space position, axis, first patch direction, switched, molType
+        x = [box[k] * (p.pos[k] - round(p.pos[k])) for k in range(3)]
+        v = list(x) + list(p.dir) + list(p.patchdir[0])
+        lines.append("%15.8e %15.8e %15.8e   %15.8e %15.8e %15.8e   %15.8e %15.8e %15.8e %d %d" % (*v, 0, p.molType))
+    return "\n".join(lines) + "\n"
+
+
+def run(system, nsweeps, report=0, movie=0, directory=".", params=None, **overrides):
+    """Runs nsweeps sweeps on the GPU, writing energy.dat / stat.dat every `report` sweeps,
+    movie frames every `movie` sweeps and config.last at the end.  Returns the summed stats
+    counters (moves, acceptances) of the blocks."""
+    p = params if params is not None else system.default_run()
+    for k, v in overrides.items():
+        setattr(p, k, v)
+    ef = os.path.join(directory, "energy.dat")
+    sf = os.path.join(directory, "stat.dat")
+    mf = os.path.join(directory, "movie")
+    # Updater::emptyFiles writes the headers (updater.cpp:77-85)
+    with open(ef, "w") as f:
+        f.write("# sweep    energy\n")
+    with open(sf, "w") as f:
+        f.write("# sweep    volume\n")
+    if movie:
+        open(mf, "w").close()
+    totals = {}
+    sweep = 0
+    next_dump = report if report > 0 else None
+    next_frame = movie if movie > 0 else None
+    while sweep < nsweeps:
+        stops = [nsweeps] + [x for x in (next_dump, next_frame) if x]
+        block = min(stops) - sweep
+        st = system.simulate(p, nsweeps=block)
+        for name, _ in type(st)._fields_:
+            if name.startswith(("acc_", "rej_", "moves", "pairs_")):
+                totals[name] = totals.get(name, 0) + getattr(st, name)
+        sweep += block
+        if next_dump and sweep == next_dump:
+            box = system.box
+            with open(sf, "a") as f:
+                f.write(" %d; %.10f\n" % (sweep, box[0] * box[1] * box[2]))
+            with open(ef, "a") as f:
+                f.write(" %d; %.10f  %f \n" % (sweep, system.all_to_all(), system.alignment_order()))
+            next_dump += report
+        if next_frame and sweep == next_frame:
+            with open(mf, "a") as f:
+                f.write(_frame(system, sweep))
+            next_frame += movie
+    system.write_config(os.path.join(directory, "config.last"))
+    return totals
