@@ -255,12 +255,28 @@ def bench_replicas(steps, seed=1):
     # the tuner: cell reach (tile size) that moves the batch fastest
     best = None
     for s in (1, 2):
-        st, *_ = R.run(4, exchange_every=100, seed=seed, stencil=s, check_every=0)
+        R.run(4, exchange_every=100, seed=seed, stencil=s, check_every=0)          # grid, graph capture
+        st, *_ = R.run(8, exchange_every=100, seed=seed, stencil=s, check_every=0)
         rate = st.moves / st.seconds
         if best is None or rate > best[1]:
             best = (s, rate)
     st, Tout, E, tried, acc = R.run(steps, exchange_every=100, seed=seed + 1, stencil=best[0], check_every=0)
     batched = st.moves / st.seconds
+    # the two forms together: the same batch with a surrogate first stage (trained on the
+    # exact pairs of the ladders' configurations) -- delayed-acceptance sweeps
+    from sc_gb300 import Surrogate
+
+    sur = Surrogate(ctxs[0], seed=seed, capacity=4_000_000)
+    for g in range(len(systems)):
+        sur.collect(ctxs[g * len(temps)])
+    sur.train(epochs=6, batch=8192, lr=2e-3, warmup_steps=100, seed=seed)
+    for c in ctxs:
+        c.set_surrogate(sur)
+    std, *_ = R.run(steps, exchange_every=100, seed=seed + 3, stencil=best[0], check_every=0, delayed=1)
+    batched_da = std.moves / std.seconds
+    for c in ctxs:
+        c.set_surrogate(None)
+    sur.close()
     # plain: every replica alone through the single-system loop (same tuned stencil)
     moves = secs = 0.0
     for g, texts in enumerate(systems):
@@ -277,6 +293,8 @@ def bench_replicas(steps, seed=1):
         c.close()
     return {"workload": "pt64_psc_uneven", "replicas": len(ctxs), "particles": particles, "stencil": best[0],
             "batched_moves_per_s": batched, "plain_moves_per_s": plain, "speedup": batched / plain,
+            "batched_delayed_moves_per_s": batched_da, "speedup_batched_delayed": batched_da / plain,
+            "delayed_stage1_decided": std.da_stage1_rejected / max(1, std.moves),
             "exchanges_tried": int(tried.sum()), "exchange_acceptance": float(acc.sum() / max(1, tried.sum())),
             "sweeps": steps}
 
@@ -423,7 +441,8 @@ def main():
     best = None
     for reach in (1, 2, 3):
         try:
-            st = s.simulate(p, nsweeps=4, stencil=reach)
+            s.simulate(p, nsweeps=4, stencil=reach)            # grid, graph capture
+            st = s.simulate(p, nsweeps=8, stencil=reach)
         except Exception:
             continue
         rate = st.moves / max(st.seconds, 1e-12)
