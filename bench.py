@@ -438,16 +438,20 @@ def main():
 
     # tuner: the cell-list reach (cell size maxcut/s, (s+1)^3 colours) that moves this
     # system fastest, timed on a few sweeps each
+    # (on a copy, so that the measured system starts from the same state as the reference arm)
     best = None
+    tune, _ = open_workload(a.workload, a.seed)
+    L.check(tune._lib.sc_set_device(tune._h, local))
     for reach in (1, 2, 3):
         try:
-            s.simulate(p, nsweeps=4, stencil=reach)            # grid, graph capture
-            st = s.simulate(p, nsweeps=8, stencil=reach)
+            tune.simulate(p, nsweeps=4, stencil=reach)            # grid, graph capture
+            st = tune.simulate(p, nsweeps=10, stencil=reach)
         except Exception:
             continue
         rate = st.moves / max(st.seconds, 1e-12)
         if best is None or rate > best[1]:
             best = (reach, rate)
+    tune.close()
     p.stencil = best[0]
     # warm-up
     s.simulate(p, nsweeps=max(3, a.warmup))

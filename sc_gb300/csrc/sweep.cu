@@ -465,13 +465,9 @@ __device__ __forceinline__ float pointSegDist2f(float3 rc, float3 u, float h) {
 
 // True when the pair energy is exactly zero by the screen of PairParam (and the pair is
 // not bonded, which the callers exclude).
-__device__ __forceinline__ bool screenedOut(const PairParam& pp, const double3& r_cm, const double3& d1,
-                                           const double3& d2) {
+__device__ __forceinline__ bool screenedOutF(const PairParam& pp, float3 r, float3 u, float3 v) {
     if (pp.screen == 3) return true;
     if (pp.screen == 0) return false;
-    float3 r = make_float3((float)r_cm.x, (float)r_cm.y, (float)r_cm.z);
-    float3 u = make_float3((float)d1.x, (float)d1.y, (float)d1.z);
-    float3 v = make_float3((float)d2.x, (float)d2.y, (float)d2.z);
     float dd;
     if (pp.screen == 1) {
         dd = segDist2f(r, u, v, (float)pp.half_len[0], (float)pp.half_len[1]);
@@ -481,6 +477,11 @@ __device__ __forceinline__ bool screenedOut(const PairParam& pp, const double3& 
         dd = pointSegDist2f(make_float3(-r.x, -r.y, -r.z), v, (float)pp.scHalf);
     }
     return dd > (float)pp.screenSq * 1.001f + 1e-3f;
+}
+__device__ __forceinline__ bool screenedOut(const PairParam& pp, const double3& r_cm, const double3& d1,
+                                           const double3& d2) {
+    return screenedOutF(pp, make_float3((float)r_cm.x, (float)r_cm.y, (float)r_cm.z),
+                        make_float3((float)d1.x, (float)d1.y, (float)d1.z), make_float3((float)d2.x, (float)d2.y, (float)d2.z));
 }
 
 __device__ __forceinline__ PView viewAt(const DevState& s, int j) {
@@ -1067,23 +1068,27 @@ __global__ void __launch_bounds__(kMoveThreads) kColour(const SweepArgs* __restr
             __syncthreads();
         };
         // stage B over queueA[0, qa): FP64 prefilter (bit-exact) and the exact-zero screen
+        // stage B over queueA[0, qa): the exact-zero screen in FP32 on the FP32 separation (its
+        // margin covers the rounding of the FP32 box fractions).  Pairs it keeps get the full
+        // FP64 pair energy, whose own prefilter (r^2 > sqmaxcut) is bit-exact; pairs it drops
+        // have energy 0 exactly, so the FP64 prefilter need not run here.
+        const float3 dOldF = f3(oldV.dir.x, oldV.dir.y, oldV.dir.z), dNewF = f3(newV.dir.x, newV.dir.y, newV.dir.z);
+        const float bxF = (float)box.x, byF = (float)box.y, bzF = (float)box.z;
         auto stageB = [&](int qa) {
             for (int e0 = 0; e0 < qa; e0 += kMoveThreads) {
                 int e = e0 + tid;
                 int keep = 0, q = 0, cls = 0;
                 if (e < qa) {
                     q = sh.queueA[e];
-                    int j = candIdx[q >> 1];
-                    const PView& self = (q & 1) ? newV : oldV;
-                    double4_32a pj = a.s.pos[j];
-                    double3 r = imageVec(self.pos, mk(pj.x, pj.y, pj.z), box);
-                    if (!(dot3(r, r) > c.sqmaxcut)) {
-                        double4_32a dj = a.s.dir[j];
-                        const PairParam& pp = c.params[self.type * c.ntypes + (int)pj.w];
-                        keep = screenedOut(pp, r, self.dir, mk(dj.x, dj.y, dj.z)) ? 0 : 1;
-                        cls = pairClass(pp);
-                        if (!keep) ++nScr;
-                    }
+                    const int k = q >> 1;
+                    const bool isNew = q & 1;
+                    float4 cp = candPos[k];
+                    float3 r = pairVecF(isNew ? newF : oldF, cp, bxF, byF, bzF);
+                    double4_32a dj = a.s.dir[candIdx[k]];
+                    const PairParam& pp = c.params[oldV.type * c.ntypes + (int)cp.w];
+                    keep = screenedOutF(pp, r, isNew ? dNewF : dOldF, f3(dj.x, dj.y, dj.z)) ? 0 : 1;
+                    cls = pairClass(pp);
+                    if (!keep) ++nScr;
                 }
                 // one scan, three 10-bit counters: per-class offsets and totals
                 int total;
@@ -1495,7 +1500,7 @@ __global__ void __launch_bounds__(kMoveThreads) kChainColour(const SweepArgs* __
         int qb0 = 0, qb1 = 0, qb2 = 0;
         auto getPair = [&](int q, PView& self, PView& other) {
             self = view((q >> 1) % kMaxChain, q & 1);
-            other = viewAt(a.s, candIdx[(q >> 1) / kMaxChain]);
+            other = viewAt(a.s, (q >> 1) / kMaxChain);
         };
         auto evalEntry = [&](int q) {
             PView self, other;
@@ -1571,7 +1576,9 @@ __global__ void __launch_bounds__(kMoveThreads) kChainColour(const SweepArgs* __
                     }
                     int tot;
                     int off = blockExclusiveScan(__popc(flags), tot, sh.scan);
-                    int key = (k * kMaxChain + pi) << 1;
+                    // entries name the particle, not the window slot: stage C runs once
+                    // over all windows
+                    int key = flags ? ((candIdx[k] * kMaxChain + pi) << 1) : 0;
                     if (flags & 1) sh.queueA[qa + off++] = key;
                     if (flags & 2) sh.queueA[qa + off] = key | 1;
                     qa += tot;
@@ -1581,9 +1588,8 @@ __global__ void __launch_bounds__(kMoveThreads) kChainColour(const SweepArgs* __
                     int e = e0 + tid, keep = 0, q = 0, cls = 0;
                     if (e < qa) {
                         q = sh.queueA[e];
-                        int isNew = q & 1, pi = (q >> 1) % kMaxChain, k = (q >> 1) / kMaxChain;
+                        int isNew = q & 1, pi = (q >> 1) % kMaxChain, j = (q >> 1) / kMaxChain;
                         PView self = view(pi, isNew);
-                        int j = candIdx[k];
                         double4_32a pj = a.s.pos[j];
                         double3 r = imageVec(self.pos, mk(pj.x, pj.y, pj.z), box);
                         if (!(dot3(r, r) > c.sqmaxcut)) {
@@ -1606,8 +1612,8 @@ __global__ void __launch_bounds__(kMoveThreads) kChainColour(const SweepArgs* __
                         flushC();
                 }
             }
-            flushC();          // queue entries index the window
         }
+        flushC();
         nTested += (unsigned long long)nCand * size * 2;
         blockSum2(eOld, eNew, sh.red);
         __shared__ int acceptS;
