@@ -874,7 +874,8 @@ __device__ __forceinline__ void decodeActive(const Grid& g, int colour, int bloc
     cx = ox + g.p[0] * bx; cy = oy + g.p[1] * by; cz = oz + g.p[2] * bz;
 }
 
-__global__ void __launch_bounds__(kMoveThreads) kColour(const SweepArgs* __restrict__ A, int phase) {
+// The move kernel body; instantiated twice (see kColour / kColourDense below).
+__device__ __forceinline__ void colourBody(const SweepArgs* __restrict__ A, int phase) {
     extern __shared__ float4 dynSmem[];
     __shared__ MoveShared sh;
     const SweepArgs& a = A[blockIdx.y];
@@ -1215,6 +1216,17 @@ __global__ void __launch_bounds__(kMoveThreads) kColour(const SweepArgs* __restr
         }
     }
     if (nScr) atomicAdd(&a.counters[C_SCREENED], nScr);
+}
+
+// One CTA per active cell of a colour.  Two register budgets of the same code: kColour
+// (up to 255 registers, two CTAs per SM: the shortest move latency, for systems whose
+// colours hold few cells) and kColourDense (at most 170 registers, three CTAs per SM:
+// more moves in flight per SM, for large systems); the bench's tuner picks one.
+__global__ void __launch_bounds__(kMoveThreads) kColour(const SweepArgs* __restrict__ A, int phase) {
+    colourBody(A, phase);
+}
+__global__ void __launch_bounds__(kMoveThreads, 3) kColourDense(const SweepArgs* __restrict__ A, int phase) {
+    colourBody(A, phase);
 }
 
 // Adds the cells' energy changes of this sweep, in a fixed order, and clears them (a cell
@@ -1936,7 +1948,7 @@ struct Batch {
     int device = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evP0 = nullptr, evP1 = nullptr;
     cudaGraphExec_t graph = nullptr;
-    int graphDims[11] = {0};   // launch shape the graph was captured with
+    int graphDims[12] = {0};   // launch shape the graph was captured with
     long graphLaunches = 0, graphPhaseLaunches = 0;
     // parallel tempering
     int* dLadder = nullptr;
@@ -2313,6 +2325,9 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
         if ((r = cudaFuncSetAttribute(kColour, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDynSmemSurrogate)) !=
             cudaSuccess)
             return cudaFail(r, "shared memory attribute");
+        if ((r = cudaFuncSetAttribute(kColourDense, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)kDynSmemSurrogate)) != cudaSuccess)
+            return cudaFail(r, "shared memory attribute");
         if ((r = cudaFuncSetAttribute(kCellEnergy, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDynSmem)) != cudaSuccess)
             return cudaFail(r, "shared memory attribute");
         if ((r = cudaFuncSetAttribute(kChainColour, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDynSmem)) !=
@@ -2325,6 +2340,7 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
     bool anySurrogate = false;
     for (const SweepArgs& h : b.hArgs) anySurrogate |= (h.mlp != nullptr);
     const size_t colourSmem = anySurrogate ? kDynSmemSurrogate : kDynSmem;
+    const bool dense = p.variant == 1;
     auto launchCellsOf = [&](const SweepArgs* args, int maxCells) -> cudaError_t {
         kZeroCounts<<<dims((maxCells + 255) / 256), 256, 0, s>>>(args);
         kAssign<<<dims((b.maxN + 255) / 256), 256, 0, s>>>(args);
@@ -2357,7 +2373,10 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
         cudaError_t r2 = launchCells();
         if (r2 != cudaSuccess) return r2;
         if (timing) cudaEventRecord(b.evP0, s);
-        for (int ph = 0; ph < b.maxColours; ++ph) kColour<<<dims(b.maxActive), kMoveThreads, colourSmem, s>>>(b.dArgs, ph);
+        for (int ph = 0; ph < b.maxColours; ++ph) {
+            if (dense) kColourDense<<<dims(b.maxActive), kMoveThreads, colourSmem, s>>>(b.dArgs, ph);
+            else kColour<<<dims(b.maxActive), kMoveThreads, colourSmem, s>>>(b.dArgs, ph);
+        }
         if (timing) {
             cudaEventRecord(b.evP1, s);
             cudaEventSynchronize(b.evP1);
@@ -2401,8 +2420,8 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
         long left = nsweeps - sw;
         bool aligned = (sw % G == 0) && (nextExchange < 0 || nextExchange - sw >= G);
         if (useGraph && left >= G && aligned) {
-            int key[11] = {ns, b.maxN, b.maxCells, b.maxActive, b.maxColours, (int)G, anySurrogate ? 1 : 0,
-                           b.chains ? 1 : 0, b.maxCellsC, b.maxActiveC, b.maxColoursC};
+            int key[12] = {ns, b.maxN, b.maxCells, b.maxActive, b.maxColours, (int)G, anySurrogate ? 1 : 0,
+                           b.chains ? 1 : 0, b.maxCellsC, b.maxActiveC, b.maxColoursC, dense ? 1 : 0};
             if (!b.graph || std::memcmp(key, b.graphDims, sizeof key) != 0) {
                 if (b.graph) { cudaGraphExecDestroy(b.graph); b.graph = nullptr; }
                 cudaGraph_t graph;
@@ -2494,6 +2513,7 @@ static int checkParams(const sc_run_params& p) {
     if (!(p.temper > 0)) return fail(SC_ERR_ARG, "temper must be positive");
     if (p.ptype < 0 || p.ptype > 5) return fail(SC_ERR_ARG, "ptype must be 0..5 (movecreator.cpp:349-546)");
     if (p.stencil < 0 || p.stencil > 3) return fail(SC_ERR_ARG, "stencil must be 0 (auto), 1, 2 or 3");
+    if (p.variant < 0 || p.variant > 1) return fail(SC_ERR_ARG, "variant must be 0 or 1");
     return SC_OK;
 }
 
@@ -2591,6 +2611,7 @@ int runReplicas(void* h, const sc_run_params& p, int exchangeEvery, sc_run_stats
         q.nsweeps = p.nsweeps; q.seed = p.seed + 0x9E3779B97F4A7C15ull * (unsigned long long)(k + 1);
         q.temper = R->temps[k]; q.ptype = p.ptype; q.volume_every = p.volume_every; q.check_every = p.check_every;
         q.stencil = p.stencil; q.time_phases = p.time_phases; q.press = p.press; q.delayed = p.delayed;
+        q.variant = p.variant;
         if (p.delayed && !c->surrogate) return fail(SC_ERR_STATE, "delayed = 1 needs a surrogate on every replica");
         if (p.transmx > 0) q.transmx = p.transmx;
         if (p.rot_angle > 0) q.rot_angle = p.rot_angle;

@@ -93,6 +93,18 @@ def test_same_seed_same_trajectory():
     s2.close()
 
 
+def test_kernel_variants_give_the_same_trajectory():
+    """kColour and kColourDense are the same code under two register budgets."""
+    _, s1 = open_ens("psc_nvt")
+    _, s2 = open_ens("psc_nvt")
+    a = s1.simulate(nsweeps=40, seed=8, check_every=0, variant=0)
+    b = s2.simulate(nsweeps=40, seed=8, check_every=0, variant=1)
+    assert a.energy == b.energy and a.acc_trans == b.acc_trans and a.acc_rot == b.acc_rot
+    assert all(list(x.pos) == list(y.pos) for x, y in zip(s1.particles(), s2.particles()))
+    s1.close()
+    s2.close()
+
+
 def test_rotations_keep_unit_vectors_and_patch_frame():
     _, s = open_ens("psc_nvt")
     s.simulate(nsweeps=100, seed=3, check_every=0)
