@@ -521,7 +521,7 @@ def main():
     e2e_s = max(time.perf_counter() - t0, 1e-12)
     e2e = {"value": e2e_moves * world / e2e_s if e2e_moves else None, "unit": UNIT, "h2d_bytes_per_step": n * bytes_per_particle,
            "d2h_bytes_per_step": 2 * n * bytes_per_particle + 64,
-           "note": "state uploaded from pageable host memory before and downloaded after every sweep"}
+           "note": "state passed in and out as host sc_particle arrays around every sweep (staged by the library through pinned host memory)"}
 
     peaks, peak_kind = measured_peaks()
     # algorithmic bytes of the move kernel: 28 B (position + type) per candidate pair tested

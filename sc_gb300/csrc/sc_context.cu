@@ -34,6 +34,8 @@ void Context::freeDevice() {
     cudaSetDevice(device);
     for (void* p : allocations) cudaFree(p);
     allocations.clear();
+    if (hostStage) cudaFreeHost(hostStage);
+    hostStage = nullptr;
     if (stream) cudaStreamDestroy(stream);
     stream = nullptr;
     devReady = false;
@@ -154,6 +156,8 @@ int Context::ensureDevice() {
         nPartial = allToAllBlocks(n) + 1;
         if ((rc = allocDev((void**)&dPartial, sizeof(double) * nPartial))) return rc;
         d.n = n;
+        e = cudaMallocHost(&hostStage, (sizeof(double4_32a) * 2 + sizeof(PatchSet)) * std::max(n, 1) + 64);
+        if (e != cudaSuccess) { hostStage = nullptr; return cudaFail(e, "cudaMallocHost (state staging)"); }
         std::vector<PairParam> hp(T * T);
         for (int a = 0; a < T; ++a)
             for (int b = 0; b < T; ++b) hp[a * T + b] = devParam(usedTypes[a], usedTypes[b]);
@@ -179,8 +183,11 @@ int Context::ensureDevice() {
 
 int Context::uploadState() {
     int n = (int)conf.p.size();
-    std::vector<double4_32a> hp(n), hd(n);
-    std::vector<PatchSet> hs(n);
+    // the state goes through one pinned staging block, so the copies are true DMA
+    double* box = (double*)hostStage;
+    double4_32a* hp = (double4_32a*)((char*)hostStage + 64);
+    double4_32a* hd = hp + n;
+    PatchSet* hs = (PatchSet*)(hd + n);
     for (int i = 0; i < n; ++i) {
         const Particle& p = conf.p[i];
         hp[i] = make_double4_32a(p.pos.x, p.pos.y, p.pos.z, (double)compactOf[p.type]);
@@ -190,12 +197,12 @@ int Context::uploadState() {
         for (int k = 0; k < 4; ++k) { s.ps[k][0] = p.ps[k].x; s.ps[k][1] = p.ps[k].y; s.ps[k][2] = p.ps[k].z; }
         for (int k = 0; k < 2; ++k) { s.ch[k][0] = p.ch[k].x; s.ch[k][1] = p.ch[k].y; s.ch[k][2] = p.ch[k].z; }
     }
-    double box[4] = {conf.box.x, conf.box.y, conf.box.z, 0.0};
+    box[0] = conf.box.x; box[1] = conf.box.y; box[2] = conf.box.z; box[3] = 0.0;
     cudaError_t e;
-    if ((e = cudaMemcpyAsync(d.pos, hp.data(), sizeof(double4_32a) * n, cudaMemcpyHostToDevice, stream)) != cudaSuccess) return cudaFail(e, "upload pos");
-    if ((e = cudaMemcpyAsync(d.dir, hd.data(), sizeof(double4_32a) * n, cudaMemcpyHostToDevice, stream)) != cudaSuccess) return cudaFail(e, "upload dir");
-    if ((e = cudaMemcpyAsync(d.patch, hs.data(), sizeof(PatchSet) * n, cudaMemcpyHostToDevice, stream)) != cudaSuccess) return cudaFail(e, "upload patch");
-    if ((e = cudaMemcpyAsync(d.box, box, sizeof(box), cudaMemcpyHostToDevice, stream)) != cudaSuccess) return cudaFail(e, "upload box");
+    if ((e = cudaMemcpyAsync(d.pos, hp, sizeof(double4_32a) * n, cudaMemcpyHostToDevice, stream)) != cudaSuccess) return cudaFail(e, "upload pos");
+    if ((e = cudaMemcpyAsync(d.dir, hd, sizeof(double4_32a) * n, cudaMemcpyHostToDevice, stream)) != cudaSuccess) return cudaFail(e, "upload dir");
+    if ((e = cudaMemcpyAsync(d.patch, hs, sizeof(PatchSet) * n, cudaMemcpyHostToDevice, stream)) != cudaSuccess) return cudaFail(e, "upload patch");
+    if ((e = cudaMemcpyAsync(d.box, box, sizeof(double) * 4, cudaMemcpyHostToDevice, stream)) != cudaSuccess) return cudaFail(e, "upload box");
     if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return cudaFail(e, "upload sync");
     hostNewer = false;
     return SC_OK;
@@ -204,14 +211,15 @@ int Context::uploadState() {
 int Context::downloadState() {
     if (!devReady || !devNewer) return SC_OK;
     int n = (int)conf.p.size();
-    std::vector<double4_32a> hp(n), hd(n);
-    std::vector<PatchSet> hs(n);
-    double box[4];
+    double* box = (double*)hostStage;
+    double4_32a* hp = (double4_32a*)((char*)hostStage + 64);
+    double4_32a* hd = hp + n;
+    PatchSet* hs = (PatchSet*)(hd + n);
     cudaError_t e;
-    if ((e = cudaMemcpyAsync(hp.data(), d.pos, sizeof(double4_32a) * n, cudaMemcpyDeviceToHost, stream)) != cudaSuccess) return cudaFail(e, "download pos");
-    if ((e = cudaMemcpyAsync(hd.data(), d.dir, sizeof(double4_32a) * n, cudaMemcpyDeviceToHost, stream)) != cudaSuccess) return cudaFail(e, "download dir");
-    if ((e = cudaMemcpyAsync(hs.data(), d.patch, sizeof(PatchSet) * n, cudaMemcpyDeviceToHost, stream)) != cudaSuccess) return cudaFail(e, "download patch");
-    if ((e = cudaMemcpyAsync(box, d.box, sizeof(box), cudaMemcpyDeviceToHost, stream)) != cudaSuccess) return cudaFail(e, "download box");
+    if ((e = cudaMemcpyAsync(hp, d.pos, sizeof(double4_32a) * n, cudaMemcpyDeviceToHost, stream)) != cudaSuccess) return cudaFail(e, "download pos");
+    if ((e = cudaMemcpyAsync(hd, d.dir, sizeof(double4_32a) * n, cudaMemcpyDeviceToHost, stream)) != cudaSuccess) return cudaFail(e, "download dir");
+    if ((e = cudaMemcpyAsync(hs, d.patch, sizeof(PatchSet) * n, cudaMemcpyDeviceToHost, stream)) != cudaSuccess) return cudaFail(e, "download patch");
+    if ((e = cudaMemcpyAsync(box, d.box, sizeof(double) * 4, cudaMemcpyDeviceToHost, stream)) != cudaSuccess) return cudaFail(e, "download box");
     if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return cudaFail(e, "download sync");
     for (int i = 0; i < n; ++i) {
         Particle& p = conf.p[i];

@@ -32,6 +32,7 @@ struct Context {
     bool devNewer = false;    // device copy changed (moves) since the last download
     cudaStream_t stream = nullptr;
     std::vector<void*> allocations;
+    void* hostStage = nullptr;   // pinned staging of the state copies (positions, axes, patches, box)
 
     DevState d{};
     DevTables tables{};

@@ -93,13 +93,18 @@ class System:
         return p
 
     def particles(self, first=0, count=None):
+        """A ctypes array of ``sc_particle`` records (indexable, iterable, and accepted
+        as is by ``set_particles``)."""
         count = self.n - first if count is None else count
-        arr = (L.Particle * max(count, 1))()
+        arr = (L.Particle * count)()
         L.check(self._lib.sc_get_particles(self._h, first, count, arr))
-        return arr[:count]
+        return arr
 
     def set_particles(self, first, parts):
-        arr = (L.Particle * len(parts))(*parts)
+        if isinstance(parts, C.Array) and parts._type_ is L.Particle:
+            arr = parts
+        else:
+            arr = (L.Particle * len(parts))(*parts)
         L.check(self._lib.sc_set_particles(self._h, first, len(parts), arr))
 
     def write_config(self, path):
