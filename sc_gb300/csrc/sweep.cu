@@ -60,6 +60,7 @@ constexpr int kQueueCap = 2048;      // pair queue entries (old + new of a full 
 constexpr int kChunk = 512;          // candidates per stage-A round
 constexpr int kMaxColours = 64;
 constexpr size_t kDynSmem = (size_t)kCandCap * (sizeof(float4) + sizeof(int));
+constexpr size_t kDynSmemColour = kDynSmem + (size_t)kCandCap * sizeof(float4);            // + FP32 axes
 constexpr size_t kDynSmemSurrogate = kDynSmem + (size_t)kCandCap * 2 * sizeof(float4);   // + FP32 axes, patches
 
 enum Ctr { C_ACC_T, C_REJ_T, C_ACC_R, C_REJ_R, C_ACC_V, C_REJ_V, C_VOL_CONSTR, C_TESTED, C_EVAL, C_CELL_REJ, C_MOVES,
@@ -102,8 +103,8 @@ struct SweepArgs {
     int* cellCursor;
     int* cellIdx;
     float4* cellPosF;     // wrapped box fractions of cellIdx, FP32
-    float4* cellDirF;     // FP32 axis and first patch direction of cellIdx (surrogate inputs;
-    float4* cellPatF;     // written only when a surrogate is attached)
+    float4* cellDirF;     // FP32 axis of cellIdx (stage B's screen, the surrogate's inputs)
+    float4* cellPatF;     // FP32 first patch direction (written only when a surrogate is attached)
     int* cellOf;
     double* cellDE;
     double* partial;      // per-cell energy sums
@@ -312,10 +313,12 @@ __global__ void kSortCells(const SweepArgs* __restrict__ A) {
         double4_32a p = a.s.pos[v[k]];
         a.cellPosF[s + k] = make_float4(frac32(p.x), frac32(p.y), frac32(p.z), (float)p.w);
         if (a.slotOf) a.slotOf[v[k]] = s + k;
-        if (a.mlp) {
+        if (a.cellDirF) {
             double4_32a d = a.s.dir[v[k]];
-            const PatchSet& ps = a.s.patch[v[k]];
             a.cellDirF[s + k] = make_float4((float)d.x, (float)d.y, (float)d.z, 0.0f);
+        }
+        if (a.mlp) {
+            const PatchSet& ps = a.s.patch[v[k]];
             a.cellPatF[s + k] = make_float4((float)ps.pd[0][0], (float)ps.pd[0][1], (float)ps.pd[0][2], 0.0f);
         }
     }
@@ -326,8 +329,17 @@ struct Scan {
     int nbTot[kWarps];
 };
 
-// Exclusive scan of v over the block; returns the offset and the total.
-__device__ __forceinline__ int blockExclusiveScan(int v, int& total, Scan& sh) {
+// Barrier of the first NW warps of the block: the whole block, or warps 0..NW-1 on named
+// barrier 2 (while the other warps do something else).
+template <int NW>
+__device__ __forceinline__ void groupBar() {
+    if (NW == kWarps) __syncthreads();
+    else asm volatile("bar.sync 2, %0;" ::"n"(NW * 32) : "memory");
+}
+
+// Exclusive scan of v over the first NW warps; returns the offset and the total.
+template <int NW>
+__device__ __forceinline__ int groupExclusiveScan(int v, int& total, Scan& sh) {
     int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     int incl = v;
 #pragma unroll
@@ -336,17 +348,22 @@ __device__ __forceinline__ int blockExclusiveScan(int v, int& total, Scan& sh) {
         if (lane >= o) incl += t;
     }
     if (lane == 31) sh.warpTot[w] = incl;
-    __syncthreads();
+    groupBar<NW>();
     int woff = 0;
     total = 0;
 #pragma unroll
-    for (int q = 0; q < kWarps; ++q) {
+    for (int q = 0; q < NW; ++q) {
         int t = sh.warpTot[q];
         if (q < w) woff += t;
         total += t;
     }
-    __syncthreads();
+    groupBar<NW>();
     return woff + incl - v;
+}
+
+// Exclusive scan of v over the block; returns the offset and the total.
+__device__ __forceinline__ int blockExclusiveScan(int v, int& total, Scan& sh) {
+    return groupExclusiveScan<kWarps>(v, total, sh);
 }
 
 // Fixed-order block sum of two doubles; result valid in thread 0.
@@ -366,6 +383,25 @@ __device__ __forceinline__ void blockSum2(double& x, double& y, double (*sh)[2])
     __syncthreads();
 }
 
+// Fixed-order block sum of four doubles; results valid in thread 0.
+__device__ __forceinline__ void blockSum4(double& x0, double& x1, double& x2, double& x3, double (*sh)[4]) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        x0 += __shfl_down_sync(0xffffffffu, x0, o);
+        x1 += __shfl_down_sync(0xffffffffu, x1, o);
+        x2 += __shfl_down_sync(0xffffffffu, x2, o);
+        x3 += __shfl_down_sync(0xffffffffu, x3, o);
+    }
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) { sh[w][0] = x0; sh[w][1] = x1; sh[w][2] = x2; sh[w][3] = x3; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        x0 = x1 = x2 = x3 = 0.0;
+        for (int q = 0; q < kWarps; ++q) { x0 += sh[q][0]; x1 += sh[q][1]; x2 += sh[q][2]; x3 += sh[q][3]; }
+    }
+    __syncthreads();
+}
+
 // Stencil of a cell and the flattened candidate list, shared by the move and energy kernels.
 struct Stencil {
     int nbCell[kNbCap];
@@ -376,7 +412,9 @@ struct Stencil {
 };
 
 // The stencil of cell (cx, cy, cz): its cells and their offsets in the concatenated
-// candidate list (cells in stencil order, particles in cell-list order).
+// candidate list (cells in stencil order, particles in cell-list order).  Run by the first
+// NW warps of the block.
+template <int NW = kWarps>
 __device__ void stageStencil(const SweepArgs& a, int cx, int cy, int cz, Stencil& st, Scan& sc) {
     const Grid& g = a.g;
     const int nx = axisCount(g.nc[0], g.s[0]), ny = axisCount(g.nc[1], g.s[1]), nz = axisCount(g.nc[2], g.s[2]);
@@ -386,7 +424,7 @@ __device__ void stageStencil(const SweepArgs& a, int cx, int cy, int cz, Stencil
     const int ownZ = g.nc[2] <= 2 * g.s[2] ? cz : g.s[2];
     const int ownQ = (ownZ * ny + ownY) * nx + own;
     int carry = 0;
-    for (int base = 0; base < nn; base += kMoveThreads) {
+    for (int base = 0; base < nn; base += NW * 32) {
         int q = base + threadIdx.x;
         int cnt = 0, cell = 0;
         if (q < nn) {
@@ -398,7 +436,7 @@ __device__ void stageStencil(const SweepArgs& a, int cx, int cy, int cz, Stencil
             cnt = a.cellCount[cell];
         }
         int total;
-        int off = blockExclusiveScan(cnt, total, sc);
+        int off = groupExclusiveScan<NW>(cnt, total, sc);
         if (q < nn) {
             st.nbCell[q] = cell;
             st.nbOff[q] = carry + off;
@@ -410,17 +448,19 @@ __device__ void stageStencil(const SweepArgs& a, int cx, int cy, int cz, Stencil
         st.nbOff[nn] = carry;
         st.nCand = carry;
     }
-    __syncthreads();
+    groupBar<NW>();
     if (threadIdx.x == 0) st.ownOff = st.nbOff[ownQ];
-    __syncthreads();
+    groupBar<NW>();
 }
 
 // Loads candidates [first, first + count) of the stencil into shared memory (count <=
-// kCandCap).  A stencil larger than the buffer is processed in windows of kCandCap.
+// kCandCap).  A stencil larger than the buffer is processed in windows of kCandCap.  Run by
+// the first NW warps of the block.
+template <int NW = kWarps>
 __device__ void loadCandidates(const SweepArgs& a, const Stencil& st, int first, int count, int* candIdx,
                                float4* candPos, float4* candDir = nullptr, float4* candPat = nullptr) {
     const int nn = st.nNb;
-    for (int kk = threadIdx.x; kk < count; kk += kMoveThreads) {
+    for (int kk = threadIdx.x; kk < count; kk += NW * 32) {
         int k = first + kk;
         int lo = 0, hi = nn - 1;      // last q with nbOff[q] <= k
         while (lo < hi) {
@@ -430,12 +470,10 @@ __device__ void loadCandidates(const SweepArgs& a, const Stencil& st, int first,
         int slot = a.cellStart[st.nbCell[lo]] + (k - st.nbOff[lo]);
         candIdx[kk] = a.cellIdx[slot];
         candPos[kk] = a.cellPosF[slot];
-        if (candDir) {
-            candDir[kk] = a.cellDirF[slot];
-            candPat[kk] = a.cellPatF[slot];
-        }
+        if (candDir) candDir[kk] = a.cellDirF[slot];
+        if (candPat) candPat[kk] = a.cellPatF[slot];
     }
-    __syncthreads();
+    groupBar<NW>();
 }
 
 // FP32 closest distance^2 of two segments (centres r apart, r = c1 - c2, unit axes u, v,
@@ -596,12 +634,20 @@ __device__ double patchyRound(SplitShared& sp, const DevCtx& c, const double3& b
     return e;
 }
 
+__device__ __forceinline__ bool partnerInStencil(const SweepArgs& a, const Stencil& st, int j) {
+    int cj = a.cellOf[j];
+    bool near = false;
+    for (int w = 0; w < st.nNb; ++w) near |= (st.nbCell[w] == cj);
+    return near;
+}
+
 // One move's proposal.  thrMet / thrStage1: the move is accepted when dE <= 0 or
 // dE < thr, thr = -T ln(u) -- the reference's exp(-dE/T) > u (movecreator.h:175-187)
 // with the logarithm taken while the proposal is built, off the critical path.
 struct Proposal {
-    int target, slotR, displace, skip, partners[4], nPartners;
+    int target, slotR, displace, skip, partners[4], nPartners, type;
     double thrMet, thrStage1;
+    double opos[3], odir[3], dirW;      // the target's state the proposal was built from
     double npos[3], ndir[3];
     float3 oldF, newF;
     PatchSet npatch;
@@ -613,16 +659,17 @@ struct MoveShared {
     int queueB[3][kClassCap];
     Stencil st;
     Scan scan;
-    double red[kWarps][2];
+    double red[kWarps][4];
     SplitShared split;
     // surrogate stage: per-warp input rows, WCA32 and sign (+1 new, -1 old) of each row
     float sx[kWarps][16][kFeat];
     float swca[kWarps][16];
     float ssign[kWarps][16];
     float sred[kWarps];
-    // proposals of the current and (speculatively) the next move
-    Proposal prop[2];
-    int specMove;       // move whose proposal prop[specMove & 1] already holds (-1: none)
+    // proposals: move k in slot k & 3; propFor[slot] is the move the slot holds (-1: none)
+    Proposal prop[4];
+    int propFor[4];
+    int passDone;       // moves a pass decided (1 or 2)
 };
 
 __device__ __forceinline__ void randomUnitSphere(Stream& r, double& x, double& y, double& z) {
@@ -642,7 +689,7 @@ __device__ __forceinline__ void randomUnitSphere(Stream& r, double& x, double& y
 // sides, chiral axes), then patchdir[0] is re-orthogonalised against the new axis as
 // partRotate does (movecreator.cpp:1007).
 __device__ void buildProposal(const SweepArgs& a, const MoveShared& sh, Proposal& P, int cell, int cnt, int m, int cx,
-                              int cy, int cz, const double3& box) {
+                              int cy, int cz, const double3& box, bool stencilReady = true) {
     const Control& ctl = *a.ctl;
     const int lane = threadIdx.x & 31;
     Stream r(a.seed, (uint32_t)cell, (uint32_t)m, (uint32_t)ctl.sweep ^ ((uint32_t)(ctl.sweep >> 32) << 20));
@@ -710,10 +757,15 @@ __device__ void buildProposal(const SweepArgs& a, const MoveShared& sh, Proposal
         P.target = t;
         P.slotR = slotR;
         P.displace = displace;
+        P.type = type;
+        P.opos[0] = p.x; P.opos[1] = p.y; P.opos[2] = p.z;
+        P.odir[0] = d.x; P.odir[1] = d.y; P.odir[2] = d.z;
+        P.dirW = d.w;
         P.npos[0] = npx; P.npos[1] = npy; P.npos[2] = npz;
         P.oldF = make_float3(frac32(p.x), frac32(p.y), frac32(p.z));
         P.newF = make_float3(frac32(npx), frac32(npy), frac32(npz));
-        // bonded partners are evaluated explicitly; they must sit inside the stencil
+        // bonded partners are evaluated explicitly; they must sit inside the stencil (checked
+        // here, or by checkPartners once the stencil is staged)
         DevCtx c;
         c.mols = a.t.mols;
         Con con = makeCon(c, t, a.s.mol[t]);
@@ -721,15 +773,42 @@ __device__ void buildProposal(const SweepArgs& a, const MoveShared& sh, Proposal
         for (int q = 0; q < 4; ++q) {
             int j = con.idx[q];
             if (j < 0) continue;
-            int cj = a.cellOf[j];
-            bool near = false;
-            for (int w = 0; w < sh.st.nNb; ++w) near |= (sh.st.nbCell[w] == cj);
-            if (!near) { atomicOr(a.err, E_PARTNER_FAR); skip = 1; }
+            if (stencilReady && !partnerInStencil(a, sh.st, j)) { atomicOr(a.err, E_PARTNER_FAR); skip = 1; }
             P.partners[np++] = j;
         }
         P.nPartners = np;
         P.skip = skip;
     }
+}
+
+// The deferred stencil check of a proposal built before the stencil was staged (one thread).
+__device__ void checkPartners(const SweepArgs& a, const MoveShared& sh, Proposal& P) {
+    for (int q = 0; q < P.nPartners; ++q)
+        if (!partnerInStencil(a, sh.st, P.partners[q])) { atomicOr(a.err, E_PARTNER_FAR); P.skip = 1; }
+}
+
+__device__ __forceinline__ bool isPartner(const Proposal& P, int j) {
+    bool r = false;
+    for (int q = 0; q < P.nPartners; ++q) r |= (P.partners[q] == j);
+    return r;
+}
+
+// The moved particle of proposal P in its old (isNew = false) or new configuration.
+__device__ __forceinline__ PView moveView(const DevState& s, const Proposal& P, bool isNew) {
+    PView v;
+    v.type = P.type;
+    v.index = P.target;
+    v.molType = 0;
+    if (isNew) {
+        v.pos = mk(P.npos[0], P.npos[1], P.npos[2]);
+        v.dir = mk(P.ndir[0], P.ndir[1], P.ndir[2]);
+        v.patch = P.displace ? &s.patch[P.target] : &P.npatch;
+    } else {
+        v.pos = mk(P.opos[0], P.opos[1], P.opos[2]);
+        v.dir = mk(P.odir[0], P.odir[1], P.odir[2]);
+        v.patch = &s.patch[P.target];
+    }
+    return v;
 }
 
 // The uniforms of the acceptance tests come from their own Philox stream, so that one
@@ -881,8 +960,8 @@ __device__ __forceinline__ void colourBody(const SweepArgs* __restrict__ A, int 
     const SweepArgs& a = A[blockIdx.y];
     float4* candPos = dynSmem;
     int* candIdx = reinterpret_cast<int*>(candPos + kCandCap);
-    // with a surrogate: FP32 axes and patch directions of the candidates as well
-    float4* candDir = a.mlp ? reinterpret_cast<float4*>(candIdx + kCandCap) : nullptr;
+    // FP32 axes of the candidates (stage B), with a surrogate their patch directions as well
+    float4* candDir = reinterpret_cast<float4*>(candIdx + kCandCap);
     float4* candPat = a.mlp ? candDir + kCandCap : nullptr;
     const Control& ctl = *a.ctl;
     const Grid& g = a.g;
@@ -893,70 +972,100 @@ __device__ __forceinline__ void colourBody(const SweepArgs* __restrict__ A, int 
     int cnt = a.cellCount[cell];
     if (cnt == 0 || cnt > kCellCap) return;
     const int tid = threadIdx.x, warp = tid >> 5;
+    const double3 box = mk(a.s.box[0], a.s.box[1], a.s.box[2]);
     for (int k = tid; k < cnt; k += kMoveThreads) sh.list[k] = a.cellIdx[a.cellStart[cell] + k];
-    stageStencil(a, cx, cy, cz, sh.st, sh.scan);
+    __syncthreads();
+    // the first pass's proposals (warp 3) while warps 0-2 stage the stencil and its candidates
+    const int first = (!a.mlp && cnt > 1) ? 2 : 1;
+    if (warp == 3) {
+        for (int q = 0; q < first; ++q) {
+            buildProposal(a, sh, sh.prop[q], cell, cnt, q, cx, cy, cz, box, false);
+            if (tid == 96) acceptThresholds(a, sh.prop[q], cell, q);
+        }
+    } else {
+        stageStencil<3>(a, cx, cy, cz, sh.st, sh.scan);
+        if (sh.st.nCand <= kCandCap) loadCandidates<3>(a, sh.st, 0, sh.st.nCand, candIdx, candPos, candDir, candPat);
+    }
+    __syncthreads();
+    if (tid == 96) {
+        for (int q = 0; q < 4; ++q) {
+            if (q < first) checkPartners(a, sh, sh.prop[q]);
+            sh.propFor[q] = q < first ? q : -1;
+        }
+    }
+    __syncthreads();
     const int nCand = sh.st.nCand;
     const bool resident = nCand <= kCandCap;
-    if (resident) loadCandidates(a, sh.st, 0, nCand, candIdx, candPos, candDir, candPat);
 
     DevCtx c;
     c.params = a.t.params; c.mols = a.t.mols; c.ntypes = a.t.ntypes; c.n = a.s.n; c.sqmaxcut = a.t.sqmaxcut;
-    const double3 box = mk(a.s.box[0], a.s.box[1], a.s.box[2]);
     const float thr32 = candThreshold(c.sqmaxcut, box);
     double dECell = 0.0;
-    unsigned long long nAccT = 0, nRejT = 0, nAccR = 0, nRejR = 0, nTested = 0, nEval = 0, nCellRej = 0, nScr = 0;
+    unsigned long long nAccT = 0, nRejT = 0, nAccR = 0, nRejR = 0, nTested = 0, nCellRej = 0, nScr = 0;
     unsigned long long nS1Rej = 0, nS2Tried = 0, nS2Rej = 0;
     double daErr2 = 0.0, daErrSum = 0.0;
 
-    if (tid == 0) sh.specMove = -1;
+    // Moves run in passes.  A pass evaluates move m and -- without a surrogate stage -- move
+    // m + 1 as well, both against the state before move m; queue entries carry the move in
+    // bit 1 and the configuration (0 old, 1 new) in bit 0, so the two moves' pairs share
+    // the lanes of one stage C.  Move m is decided first; move m + 1's energies stand when
+    // move m was rejected or when the two targets are out of each other's range, and its
+    // decision is then the one a pass of its own would take (same proposal, same
+    // thresholds, same pair energies); otherwise the next pass evaluates it again.
+    // Proposals live in a ring of four slots; warps 2 and 3 build the next pass's during
+    // stage C.
+    const float bxF = (float)box.x, byF = (float)box.y, bzF = (float)box.z;
+    unsigned evalMine = 0;          // pairs this thread evaluated for moves that were decided
     for (int m = 0; m < cnt; ++m) {
-        Proposal& P = sh.prop[m & 1];
-        if (sh.specMove != m) {         // no speculative proposal for this move
-            if (warp == 0) buildProposal(a, sh, P, cell, cnt, m, cx, cy, cz, box);
-            else if (tid == 32) acceptThresholds(a, P, cell, m);
-        }
-        __syncthreads();
-        const int t = P.target;
-        const bool displace = P.displace;
-        if (P.skip) {
-            if (tid == 0) { if (displace) { ++nRejT; ++nCellRej; } else ++nRejR; }
+        const bool pair = !a.mlp && m + 1 < cnt;
+        {
+            const bool need0 = sh.propFor[m & 3] != m;
+            const bool need1 = pair && sh.propFor[(m + 1) & 3] != m + 1;
+            if (need0) {
+                if (warp == 0) buildProposal(a, sh, sh.prop[m & 3], cell, cnt, m, cx, cy, cz, box);
+                else if (tid == 64) acceptThresholds(a, sh.prop[m & 3], cell, m);
+            }
+            if (need1) {
+                if (warp == 1) buildProposal(a, sh, sh.prop[(m + 1) & 3], cell, cnt, m + 1, cx, cy, cz, box);
+                else if (tid == 96) acceptThresholds(a, sh.prop[(m + 1) & 3], cell, m + 1);
+            }
             __syncthreads();
+            if (tid == 0) {
+                if (need0) sh.propFor[m & 3] = m;
+                if (need1) sh.propFor[(m + 1) & 3] = m + 1;
+            }
+            __syncthreads();
+        }
+        const Proposal& P0 = sh.prop[m & 3];
+        const Proposal& P1 = sh.prop[(m + 1) & 3];
+        if (P0.skip) {
+            if (tid == 0) { if (P0.displace) { ++nRejT; ++nCellRej; } else ++nRejR; }
             continue;
         }
-        const int np = P.nPartners;
-        int partners[4] = {-1, -1, -1, -1};
-        for (int q = 0; q < np; ++q) partners[q] = P.partners[q];
-        const double4_32a op4 = a.s.pos[t];
-        const double4_32a od4 = a.s.dir[t];
-        PView oldV;
-        oldV.pos = mk(op4.x, op4.y, op4.z);
-        oldV.dir = mk(od4.x, od4.y, od4.z);
-        oldV.patch = &a.s.patch[t];
-        oldV.type = (int)op4.w;
-        oldV.index = t;
-        oldV.molType = 0;
-        PView newV = oldV;
-        newV.pos = mk(P.npos[0], P.npos[1], P.npos[2]);
-        newV.dir = mk(P.ndir[0], P.ndir[1], P.ndir[2]);
-        if (!displace) newV.patch = &P.npatch;
-        const Con con = makeCon(c, t, a.s.mol[t]);
-        const float3 oldF = P.oldF, newF = P.newF;
+        const bool eval1 = pair && !P1.skip;
+        const int t = P0.target;
+        const bool displace = P0.displace;
+        const float3 oldF = P0.oldF, newF = P0.newF;
+        const float3 oldF1 = eval1 ? P1.oldF : oldF, newF1 = eval1 ? P1.newF : newF;
+        const bool displace1 = eval1 && P1.displace;
+        const int t1 = eval1 ? P1.target : -1;
 
         // delayed acceptance, stage 1: the surrogate's energy change decides first
         float dEs = 0.0f;
         int qaFused = -1;               // >= 0: stage A was fused into the surrogate screen
         if (a.mlp) {
+            int partners[4] = {-1, -1, -1, -1};
+            for (int q = 0; q < P0.nPartners; ++q) partners[q] = P0.partners[q];
             MovedF mv;
             const PatchSet& ops = a.s.patch[t];
-            mv.aOld = f3(od4.x, od4.y, od4.z);
+            mv.aOld = f3(P0.odir[0], P0.odir[1], P0.odir[2]);
             mv.pOld = f3(ops.pd[0][0], ops.pd[0][1], ops.pd[0][2]);
-            mv.aNew = displace ? mv.aOld : f3(P.ndir[0], P.ndir[1], P.ndir[2]);
-            mv.pNew = displace ? mv.pOld : f3(P.npatch.pd[0][0], P.npatch.pd[0][1], P.npatch.pd[0][2]);
-            mv.type = (int)op4.w;
+            mv.aNew = displace ? mv.aOld : f3(P0.ndir[0], P0.ndir[1], P0.ndir[2]);
+            mv.pNew = displace ? mv.pOld : f3(P0.npatch.pd[0][0], P0.npatch.pd[0][1], P0.npatch.pd[0][2]);
+            mv.type = P0.type;
             mv.tc = typeCode(mv.type, c.ntypes);
             if (resident) {
                 // one pass over the candidates: stage A's screen and the surrogate's
-                const float bx = (float)box.x, by = (float)box.y, bz = (float)box.z;
                 int* queueS = &sh.queueB[0][0];
                 int qa = 0, qs = 0;
                 for (int r0 = 0; r0 < nCand; r0 += kMoveThreads) {
@@ -970,14 +1079,14 @@ __device__ __forceinline__ void colourBody(const SweepArgs* __restrict__ A, int 
                             bool p0 = dist2f(cp, oldF, box) <= thr32;
                             bool p1 = displace ? dist2f(cp, newF, box) <= thr32 : p0;
                             flags = (p0 ? 1 : 0) | (p1 ? 2 : 0);
-                            sflags = surrogateScreen(a, mv, cp, candDir[k], displace, oldF, newF, bx, by, bz);
+                            sflags = surrogateScreen(a, mv, cp, candDir[k], displace, oldF, newF, bxF, byF, bzF);
                         }
                     }
                     int total;
                     int off = blockExclusiveScan(__popc(flags) | (__popc(sflags) << 16), total, sh.scan);
                     int oa = off & 0xFFFF, os = off >> 16;
-                    if (flags & 1) sh.queueA[qa + oa++] = k << 1;
-                    if (flags & 2) sh.queueA[qa + oa] = (k << 1) | 1;
+                    if (flags & 1) sh.queueA[qa + oa++] = k << 2;
+                    if (flags & 2) sh.queueA[qa + oa] = (k << 2) | 1;
                     if (sflags & 1) queueS[qs + os++] = k << 1;
                     if (sflags & 2) queueS[qs + os] = (k << 1) | 1;
                     qa += total & 0xFFFF;
@@ -990,7 +1099,7 @@ __device__ __forceinline__ void colourBody(const SweepArgs* __restrict__ A, int 
                 dEs = surrogateDeltaWindows(a, sh, mv, candIdx, candPos, candDir, candPat, nCand, t, displace, partners,
                                             oldF, newF);
             }
-            bool pass = (dEs <= 0.0f) || ((double)dEs < P.thrStage1);
+            bool pass = (dEs <= 0.0f) || ((double)dEs < P0.thrStage1);
             if (!pass) {
                 if (tid == 0) { ++nS1Rej; if (displace) ++nRejT; else ++nRejR; }
                 __syncthreads();
@@ -998,20 +1107,32 @@ __device__ __forceinline__ void colourBody(const SweepArgs* __restrict__ A, int 
             }
         }
 
-        double eOld = 0.0, eNew = 0.0;
-        if (tid < np) {     // bonded partners: both configurations, whatever the distance
-            PView b = viewAt(a.s, partners[tid]);
-            unsigned bb; double dd;
-            eOld += pairEnergy(c, oldV, b, con, box, &bb, &dd);
-            eNew += pairEnergy(c, newV, b, con, box, &bb, &dd);
+        // energies of move m (0 old, 1 new) and move m + 1 (2 old, 3 new)
+        double e0 = 0.0, e1 = 0.0, e2 = 0.0, e3 = 0.0;
+        auto addE = [&](int b, double en) {
+            if (b == 0) e0 += en; else if (b == 1) e1 += en; else if (b == 2) e2 += en; else e3 += en;
+        };
+        unsigned kept0 = 0, kept1 = 0;
+        // bonded partners: both configurations, whatever the distance (warp 0: move m, warp 1: m + 1)
+        {
+            const int lane = tid & 31;
+            const Proposal* Pp = warp == 0 ? &P0 : (warp == 1 && eval1 ? &P1 : nullptr);
+            if (Pp && lane < Pp->nPartners) {
+                PView b = viewAt(a.s, Pp->partners[lane]);
+                Con cn = makeCon(c, Pp->target, a.s.mol[Pp->target]);
+                unsigned bb; double dd;
+                addE(warp * 2, pairEnergy(c, moveView(a.s, *Pp, false), b, cn, box, &bb, &dd));
+                addE(warp * 2 + 1, pairEnergy(c, moveView(a.s, *Pp, true), b, cn, box, &bb, &dd));
+            }
         }
         int qb0 = 0, qb1 = 0, qb2 = 0;
         // one queue entry through the full pair energy
         auto evalEntry = [&](int q) {
-            PView b = viewAt(a.s, candIdx[q >> 1]);
+            const Proposal& Pq = (q & 2) ? P1 : P0;
+            PView b = viewAt(a.s, candIdx[q >> 2]);
+            Con cn = makeCon(c, Pq.target, a.s.mol[Pq.target]);
             unsigned bb; double dd;
-            if (q & 1) eNew += pairEnergy(c, newV, b, con, box, &bb, &dd);
-            else eOld += pairEnergy(c, oldV, b, con, box, &bb, &dd);
+            addE(q & 3, pairEnergy(c, moveView(a.s, Pq, q & 1), b, cn, box, &bb, &dd));
         };
         // classes 1 and 2 over nw warps starting at warp w0; class 2 starts on a warp boundary
         auto evalGeneric = [&](int w0, int nw) {
@@ -1027,69 +1148,73 @@ __device__ __forceinline__ void colourBody(const SweepArgs* __restrict__ A, int 
             const int n = cls == 1 ? qb1 : qb2;
             for (int g = (warp - w0) * 32 + (tid & 31); g < n; g += nw * 32) evalEntry(sh.queueB[cls][g]);
         };
-        // warp 3 builds the next move's proposal while stage C runs (it stays valid unless
-        // this move is accepted and the next one picks the same particle)
-        auto speculate = [&]() {
-            Proposal& N = sh.prop[(m + 1) & 1];
-            buildProposal(a, sh, N, cell, cnt, m + 1, cx, cy, cz, box);
+        // the next pass's proposals, built while stage C runs: move m + 2 (and m + 3) after a
+        // pair, m + 1 otherwise.  They stay valid unless a move of this pass is accepted on the
+        // same particle.
+        const int specA = pair ? m + 2 : m + 1, specB = pair ? m + 3 : cnt;
+        auto speculate = [&](int mv) {
+            if (sh.propFor[mv & 3] == mv) return;      // still valid from an earlier pass
+            Proposal& N = sh.prop[mv & 3];
+            buildProposal(a, sh, N, cell, cnt, mv, cx, cy, cz, box);
             if ((tid & 31) == 0) {
-                acceptThresholds(a, N, cell, m + 1);
-                sh.specMove = m + 1;
+                acceptThresholds(a, N, cell, mv);
+                sh.propFor[mv & 3] = mv;
             }
         };
         auto flushC = [&](bool last) {     // stage C: exact FP64 pair energies
             __syncthreads();               // queue entries of every thread are visible
             const int lane = tid & 31;
-            const bool spec = last && m + 1 < cnt;
+            const bool spec = last && specA < cnt, spec2 = last && specB < cnt;
             if (qb0 > 0) {
                 if (warp < 3) {
                     // class 0: warps 0, 1, 2 run the pairs' independent FP64 chains side by side
                     auto getPair = [&](int q, PView& self, PView& other) {
-                        self = (q & 1) ? newV : oldV;
-                        other = viewAt(a.s, candIdx[q >> 1]);
+                        self = moveView(a.s, (q & 2) ? P1 : P0, q & 1);
+                        other = viewAt(a.s, candIdx[q >> 2]);
                     };
                     for (int r0 = 0; r0 < qb0; r0 += 32) {
                         double e = patchyRound(sh.split, c, box, sh.queueB[0], qb0, r0, getPair);
-                        if (warp == 0 && r0 + lane < qb0) {
-                            if (sh.queueB[0][r0 + lane] & 1) eNew += e; else eOld += e;
-                        }
+                        if (warp == 0 && r0 + lane < qb0) addE(sh.queueB[0][r0 + lane] & 3, e);
                     }
                     // the short class-2 pairs (sphere-sphere and others) on warps 1 and 2
                     evalClass(2, 1, 2);
+                    if (warp == 2 && spec2) speculate(specB);
                 } else {
-                    if (spec) speculate();
+                    if (spec) speculate(specA);
                     evalClass(1, 3, 1);
                 }
             } else if (spec) {
-                if (warp == 3) speculate();
+                if (warp == 3) speculate(specA);
                 else evalGeneric(0, 3);
+                if (warp == 2 && spec2) speculate(specB);
             } else {
                 evalGeneric(0, kWarps);
             }
             __syncthreads();
         };
-        // stage B over queueA[0, qa): FP64 prefilter (bit-exact) and the exact-zero screen
         // stage B over queueA[0, qa): the exact-zero screen in FP32 on the FP32 separation (its
         // margin covers the rounding of the FP32 box fractions).  Pairs it keeps get the full
         // FP64 pair energy, whose own prefilter (r^2 > sqmaxcut) is bit-exact; pairs it drops
         // have energy 0 exactly, so the FP64 prefilter need not run here.
-        const float3 dOldF = f3(oldV.dir.x, oldV.dir.y, oldV.dir.z), dNewF = f3(newV.dir.x, newV.dir.y, newV.dir.z);
-        const float bxF = (float)box.x, byF = (float)box.y, bzF = (float)box.z;
+        const float3 dOld0 = f3(P0.odir[0], P0.odir[1], P0.odir[2]), dNew0 = f3(P0.ndir[0], P0.ndir[1], P0.ndir[2]);
+        const float3 dOld1 = f3(P1.odir[0], P1.odir[1], P1.odir[2]), dNew1 = f3(P1.ndir[0], P1.ndir[1], P1.ndir[2]);
         auto stageB = [&](int qa) {
-            for (int e0 = 0; e0 < qa; e0 += kMoveThreads) {
-                int e = e0 + tid;
+            for (int e0_ = 0; e0_ < qa; e0_ += kMoveThreads) {
+                int e = e0_ + tid;
                 int keep = 0, q = 0, cls = 0;
                 if (e < qa) {
                     q = sh.queueA[e];
-                    const int k = q >> 1;
-                    const bool isNew = q & 1;
-                    float4 cp = candPos[k];
-                    float3 r = pairVecF(isNew ? newF : oldF, cp, bxF, byF, bzF);
-                    double4_32a dj = a.s.dir[candIdx[k]];
-                    const PairParam& pp = c.params[oldV.type * c.ntypes + (int)cp.w];
-                    keep = screenedOutF(pp, r, isNew ? dNewF : dOldF, f3(dj.x, dj.y, dj.z)) ? 0 : 1;
+                    const int k = q >> 2, b = q & 3;
+                    float4 cp = candPos[k], cd = candDir[k];
+                    const float3 sp = b == 0 ? oldF : (b == 1 ? newF : (b == 2 ? oldF1 : newF1));
+                    const float3 sd = b == 0 ? dOld0 : (b == 1 ? dNew0 : (b == 2 ? dOld1 : dNew1));
+                    float3 r = pairVecF(sp, cp, bxF, byF, bzF);
+                    const PairParam& pp = c.params[((b & 2) ? P1.type : P0.type) * c.ntypes + (int)cp.w];
+                    keep = screenedOutF(pp, r, sd, make_float3(cd.x, cd.y, cd.z)) ? 0 : 1;
                     cls = pairClass(pp);
                     if (!keep) ++nScr;
+                    else if (b & 2) ++kept1;
+                    else ++kept0;
                 }
                 // one scan, three 10-bit counters: per-class offsets and totals
                 int total;
@@ -1103,7 +1228,6 @@ __device__ __forceinline__ void colourBody(const SweepArgs* __restrict__ A, int 
                 qb2 += (total >> 20) & 1023;
                 if (qb0 > kClassCap - kMoveThreads || qb1 > kClassCap - kMoveThreads || qb2 > kClassCap - kMoveThreads) {
                     flushC(false);
-                    nEval += qb0 + qb1 + qb2;
                     qb0 = qb1 = qb2 = 0;
                 }
             }
@@ -1114,9 +1238,9 @@ __device__ __forceinline__ void colourBody(const SweepArgs* __restrict__ A, int 
             for (int wbase = 0; wbase < nCand; wbase += kCandCap) {
               // candidates in shared memory: all of them, or the window [wbase, wend)
               const int wend = min(wbase + kCandCap, nCand);
-              if (!resident) loadCandidates(a, sh.st, wbase, wend - wbase, candIdx, candPos);
+              if (!resident) loadCandidates(a, sh.st, wbase, wend - wbase, candIdx, candPos, candDir);
               for (int base = wbase; base < wend; base += kChunk) {
-                // stage A: FP32 minimum image against the old and the new position
+                // stage A: FP32 minimum image against the old and the new position of each move
                 int qa = 0;
                 const int cend = min(base + kChunk, wend);
                 for (int r0 = base; r0 < cend; r0 += kMoveThreads) {
@@ -1124,18 +1248,23 @@ __device__ __forceinline__ void colourBody(const SweepArgs* __restrict__ A, int 
                     int flags = 0;
                     if (r0 + tid < cend) {
                         int j = candIdx[k];
-                        bool partner = (j == partners[0] || j == partners[1] || j == partners[2] || j == partners[3]);
-                        if (j != t && !partner) {
-                            float4 cp = candPos[k];
+                        float4 cp = candPos[k];
+                        if (j != t && !isPartner(P0, j)) {
                             bool p0 = dist2f(cp, oldF, box) <= thr32;
                             bool p1 = displace ? dist2f(cp, newF, box) <= thr32 : p0;
                             flags = (p0 ? 1 : 0) | (p1 ? 2 : 0);
                         }
+                        if (eval1 && j != t1 && !isPartner(P1, j)) {
+                            bool p0 = dist2f(cp, oldF1, box) <= thr32;
+                            bool p1 = displace1 ? dist2f(cp, newF1, box) <= thr32 : p0;
+                            flags |= (p0 ? 4 : 0) | (p1 ? 8 : 0);
+                        }
                     }
                     int total;
                     int off = blockExclusiveScan(__popc(flags), total, sh.scan);
-                    if (flags & 1) sh.queueA[qa + off++] = k << 1;
-                    if (flags & 2) sh.queueA[qa + off] = (k << 1) | 1;
+#pragma unroll
+                    for (int b = 0; b < 4; ++b)
+                        if (flags & (1 << b)) sh.queueA[qa + off++] = (k << 2) | b;
                     qa += total;
                 }
                 __syncthreads();
@@ -1143,59 +1272,96 @@ __device__ __forceinline__ void colourBody(const SweepArgs* __restrict__ A, int 
               }
               if (!resident) {      // queue entries index the window: evaluate them before it changes
                   flushC(false);
-                  nEval += qb0 + qb1 + qb2;
                   qb0 = qb1 = qb2 = 0;
               }
             }
         }
         flushC(true);
-        nEval += qb0 + qb1 + qb2 + 2 * np;
-        nTested += (unsigned long long)nCand * (displace ? 2 : 1);
-        blockSum2(eOld, eNew, sh.red);
+        blockSum4(e0, e1, e2, e3, sh.red);
         if (tid == 0) {
             // MoveCreator::moveTry (movecreator.h:175-187); with a surrogate stage the exact
             // test is on dE - dEs
             bool accept;
             if (a.mlp) {
-                double x = (eNew - eOld) - (double)dEs;
-                accept = (x <= 0.0) || (x < P.thrMet);
+                double x = (e1 - e0) - (double)dEs;
+                accept = (x <= 0.0) || (x < P0.thrMet);
                 ++nS2Tried;
                 if (!accept) ++nS2Rej;
                 daErr2 += x * x;
                 daErrSum += x;
             } else {
-                accept = (eNew <= eOld) || ((eNew - eOld) < P.thrMet);
+                accept = (e1 <= e0) || ((e1 - e0) < P0.thrMet);
             }
-            if (accept) {
-                a.s.pos[t] = make_double4_32a(P.npos[0], P.npos[1], P.npos[2], op4.w);
-                if (!displace) {
-                    a.s.dir[t] = make_double4_32a(P.ndir[0], P.ndir[1], P.ndir[2], od4.w);
-                    a.s.patch[t] = P.npatch;
+            nTested += (unsigned long long)nCand * (displace ? 2 : 1);
+            evalMine += 2 * P0.nPartners;
+            // the accepted state, in global memory and in the cell's staged candidates
+            auto commit = [&](const Proposal& P, double dE) {
+                const int tt = P.target;
+                a.s.pos[tt] = make_double4_32a(P.npos[0], P.npos[1], P.npos[2], (double)P.type);
+                if (!P.displace) {
+                    a.s.dir[tt] = make_double4_32a(P.ndir[0], P.ndir[1], P.ndir[2], P.dirW);
+                    a.s.patch[tt] = P.npatch;
+                    float4 nd = make_float4((float)P.ndir[0], (float)P.ndir[1], (float)P.ndir[2], 0.0f);
+                    a.cellDirF[a.cellStart[cell] + P.slotR] = nd;
+                    if (resident) candDir[sh.st.ownOff + P.slotR] = nd;
                     if (a.mlp) {
-                        float4 nd = make_float4((float)P.ndir[0], (float)P.ndir[1], (float)P.ndir[2], 0.0f);
                         float4 npd = make_float4((float)P.npatch.pd[0][0], (float)P.npatch.pd[0][1],
                                                  (float)P.npatch.pd[0][2], 0.0f);
-                        a.cellDirF[a.cellStart[cell] + P.slotR] = nd;
                         a.cellPatF[a.cellStart[cell] + P.slotR] = npd;
-                        if (resident) {
-                            candDir[sh.st.ownOff + P.slotR] = nd;
-                            candPat[sh.st.ownOff + P.slotR] = npd;
-                        }
+                        if (resident) candPat[sh.st.ownOff + P.slotR] = npd;
                     }
+                    ++nAccR;
                 } else {
-                    float4 nf = make_float4(newF.x, newF.y, newF.z, (float)op4.w);
+                    float4 nf = make_float4(P.newF.x, P.newF.y, P.newF.z, (float)P.type);
                     if (resident) candPos[sh.st.ownOff + P.slotR] = nf;
                     a.cellPosF[a.cellStart[cell] + P.slotR] = nf;
+                    ++nAccT;
                 }
-                dECell += eNew - eOld;
-                if (displace) ++nAccT; else ++nAccR;
-                // the next move's speculative proposal read this particle's old state
-                if (sh.specMove == m + 1 && sh.prop[(m + 1) & 1].target == t) sh.specMove = -1;
+                dECell += dE;
+            };
+            // proposals built ahead from a particle this pass moved are stale
+            auto invalidate = [&](int after, int tt) {
+                for (int q = 0; q < 4; ++q)
+                    if (sh.propFor[q] > after && sh.prop[q].target == tt) sh.propFor[q] = -1;
+            };
+            if (accept) {
+                commit(P0, e1 - e0);
+                invalidate(m, t);
             } else {
                 if (displace) ++nRejT; else ++nRejR;
             }
+            int done = 1;
+            if (pair) {
+                // move m + 1 stands if move m changed nothing it saw
+                bool valid = !accept;
+                if (!valid && P1.target != t && !isPartner(P1, t)) {
+                    float4 o = make_float4(P0.oldF.x, P0.oldF.y, P0.oldF.z, 0.0f);
+                    float4 n = make_float4(P0.newF.x, P0.newF.y, P0.newF.z, 0.0f);
+                    valid = dist2f(o, P1.oldF, box) > thr32 && dist2f(o, P1.newF, box) > thr32 &&
+                            dist2f(n, P1.oldF, box) > thr32 && dist2f(n, P1.newF, box) > thr32;
+                }
+                if (valid) {
+                    done = 2;
+                    if (P1.skip) {
+                        if (P1.displace) { ++nRejT; ++nCellRej; } else ++nRejR;
+                    } else {
+                        nTested += (unsigned long long)nCand * (P1.displace ? 2 : 1);
+                        evalMine += 2 * P1.nPartners;
+                        if ((e3 <= e2) || ((e3 - e2) < P1.thrMet)) {
+                            commit(P1, e3 - e2);
+                            invalidate(m + 1, P1.target);
+                        } else {
+                            if (P1.displace) ++nRejT; else ++nRejR;
+                        }
+                    }
+                }
+            }
+            sh.passDone = done;
         }
         __syncthreads();
+        const int done = sh.passDone;
+        evalMine += kept0 + (done == 2 ? kept1 : 0);
+        m += done - 1;
     }
     if (tid == 0) {
         a.cellDE[cell] = dECell;
@@ -1206,7 +1372,6 @@ __device__ __forceinline__ void colourBody(const SweepArgs* __restrict__ A, int 
         atomicAdd(&a.counters[C_CELL_REJ], nCellRej);
         atomicAdd(&a.counters[C_MOVES], (unsigned long long)cnt);
         atomicAdd(&a.counters[C_TESTED], nTested);
-        atomicAdd(&a.counters[C_EVAL], nEval);
         if (a.mlp) {
             atomicAdd(&a.counters[C_S1_REJ], nS1Rej);
             atomicAdd(&a.counters[C_S2_TRIED], nS2Tried);
@@ -1216,6 +1381,8 @@ __device__ __forceinline__ void colourBody(const SweepArgs* __restrict__ A, int 
         }
     }
     if (nScr) atomicAdd(&a.counters[C_SCREENED], nScr);
+    evalMine = __reduce_add_sync(0xffffffffu, evalMine);
+    if ((tid & 31) == 0 && evalMine) atomicAdd(&a.counters[C_EVAL], (unsigned long long)evalMine);
 }
 
 // One CTA per active cell of a colour.  Two register budgets of the same code: kColour
@@ -1806,23 +1973,37 @@ __global__ void __launch_bounds__(kMoveThreads) kCellEnergy(const SweepArgs* __r
     if (tid == 0) a.partial[cell] = sum;
 }
 
+// Sum of the per-cell partials p[0, n) by all threads of one block in a fixed order (strided
+// per-thread sums, a shuffle tree per warp, the warps in order): every thread gets the same
+// value, launch after launch.  A single-thread loop over the 3000+ cells of a small system
+// is a dependent FP64 chain of ~0.1 ms.
 __device__ double sumPartials(const double* p, int n) {
+    __shared__ double ws[32];
+    double v = 0.0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) v += p[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
+    __syncthreads();
     double s = 0.0;
-    for (int k = 0; k < n; ++k) s += p[k];
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += ws[q];
     return s;
 }
 
 // MoveCreator::pressureMove, ptype 1 (movecreator.cpp:390-421), decided on the device.
 __global__ void kVolumeAccept(const SweepArgs* __restrict__ A) {
     const SweepArgs& a = A[blockIdx.y];
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (blockIdx.x != 0) return;
     Control& c = *a.ctl;
     if (!c.volValid) {
-        atomicAdd(&a.counters[C_VOL_CONSTR], 1ull);
-        atomicAdd(&a.counters[C_REJ_V], 1ull);
+        if (threadIdx.x == 0) {
+            atomicAdd(&a.counters[C_VOL_CONSTR], 1ull);
+            atomicAdd(&a.counters[C_REJ_V], 1ull);
+        }
         return;
     }
     double eNew = sumPartials(a.partial, a.g.ncells);
+    if (threadIdx.x != 0) return;
     double enermove = c.pvTerm;
     enermove += eNew;
     Stream r(a.seed, 0xFFFFFFF1u, (uint32_t)c.sweep, (uint32_t)(c.sweep >> 32));
@@ -1840,13 +2021,16 @@ __global__ void kVolumeAccept(const SweepArgs* __restrict__ A) {
 
 __global__ void kSetEnergy(const SweepArgs* __restrict__ A) {
     const SweepArgs& a = A[blockIdx.y];
-    if (threadIdx.x == 0 && blockIdx.x == 0) a.ctl->energy = sumPartials(a.partial, a.g.ncells);
+    if (blockIdx.x != 0) return;
+    double e = sumPartials(a.partial, a.g.ncells);
+    if (threadIdx.x == 0) a.ctl->energy = e;
 }
 
 __global__ void kCheckEnergy(const SweepArgs* __restrict__ A) {
     const SweepArgs& a = A[blockIdx.y];
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (blockIdx.x != 0) return;
     double e = sumPartials(a.partial, a.g.ncells);
+    if (threadIdx.x != 0) return;
     Control& c = *a.ctl;
     c.energyCheck = e;
     double d = fabs(c.energy - e);
@@ -2339,7 +2523,7 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
     // systems with a surrogate stage their candidates' FP32 axes and patches as well
     bool anySurrogate = false;
     for (const SweepArgs& h : b.hArgs) anySurrogate |= (h.mlp != nullptr);
-    const size_t colourSmem = anySurrogate ? kDynSmemSurrogate : kDynSmem;
+    const size_t colourSmem = anySurrogate ? kDynSmemSurrogate : kDynSmemColour;
     const bool dense = p.variant == 1;
     auto launchCellsOf = [&](const SweepArgs* args, int maxCells) -> cudaError_t {
         kZeroCounts<<<dims((maxCells + 255) / 256), 256, 0, s>>>(args);
@@ -2353,8 +2537,8 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
     auto launchCells = [&]() -> cudaError_t { return launchCellsOf(b.dArgs, b.maxCells); };
     auto exactEnergy = [&](bool check) -> cudaError_t {
         kCellEnergy<<<dims(b.maxCells), kMoveThreads, kDynSmem, s>>>(b.dArgs, 0);
-        if (check) kCheckEnergy<<<dims(1), 32, 0, s>>>(b.dArgs);
-        else kSetEnergy<<<dims(1), 32, 0, s>>>(b.dArgs);
+        if (check) kCheckEnergy<<<dims(1), 256, 0, s>>>(b.dArgs);
+        else kSetEnergy<<<dims(1), 256, 0, s>>>(b.dArgs);
         launches += 2;
         return cudaGetLastError();
     };
@@ -2397,8 +2581,10 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
             launches += 3 + b.maxColoursC;
         }
         if (volDue) {
+            // chain moves left particles outside the cells of this sweep's list: list them anew
+            if (b.chains && (r2 = launchCells()) != cudaSuccess) return r2;
             kCellEnergy<<<dims(b.maxCells), kMoveThreads, kDynSmem, s>>>(b.dArgs, 1);
-            kVolumeAccept<<<dims(1), 32, 0, s>>>(b.dArgs);
+            kVolumeAccept<<<dims(1), 256, 0, s>>>(b.dArgs);
             launches += 2;
         }
         return cudaGetLastError();

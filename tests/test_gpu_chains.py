@@ -74,3 +74,19 @@ def test_chain_ensemble_matches_reference():
     assert abs(mean - ref["mean"]) <= 2.0 * sigma, (mean, se, ref)
     for s in systems:
         s.close()
+
+
+def test_chain_moves_with_volume_moves_keep_the_running_energy_exact():
+    """Isotropic volume moves after the chain phase: the trial energy is taken on cell
+    lists built after the chains moved."""
+    from sc_gb300 import System, workloads
+
+    s = System.from_text(*workloads.lipids_dilute(64, seed=4))
+    p = s.default_run()
+    p.ptype, p.volume_every, p.press, p.edge_mx = 1, 1, 0.3, 0.1
+    st = s.simulate(p, nsweeps=80, seed=6, check_every=40)
+    assert st.acc_chain > 0 and st.acc_vol > 0
+    e1 = s.all_to_all()
+    assert abs(st.energy - e1) <= 1e-9 * max(1.0, abs(e1))
+    assert abs(st.energy_check - e1) <= 1e-9 * max(1.0, abs(e1))
+    s.close()
