@@ -85,7 +85,8 @@ typedef struct {
     int time_phases;        /* 1: time the move kernels with CUDA events (adds events to the stream) */
     int stencil;            /* cell-list reach s: cells >= maxcut/s wide, (s+1)^3 colours; 0: chosen by the tuner */
     int delayed;            /* 1: two-stage moves with the context's surrogate (sc_set_surrogate) as first stage */
-    int variant;            /* move kernel: 0 lowest latency per move, 1 more moves in flight per SM (large systems) */
+    int variant;            /* move kernel, bit 0: more moves in flight per SM (large systems), else lowest
+                               latency per move; bit 1: paired passes (two moves per stage C) */
     int pad_;
 } sc_run_params;
 

@@ -117,6 +117,7 @@ struct SweepArgs {
     double trans[MAX_DEV_TYPES];
     int geo[MAX_DEV_TYPES];
     const MlpPacked* mlp;   // delayed acceptance: the surrogate's weights (nullptr: plain moves)
+    int pairMoves;          // paired passes in the move kernel (two moves per stage C)
     float rcutS;            // its range (FP32 segment distance)
     // chain moves (records of the chain grid; see kChainColour)
     double* energyAcc;      // where kEndSweep adds the sweep's energy change (nullptr: ctl->energy)
@@ -329,17 +330,8 @@ struct Scan {
     int nbTot[kWarps];
 };
 
-// Barrier of the first NW warps of the block: the whole block, or warps 0..NW-1 on named
-// barrier 2 (while the other warps do something else).
-template <int NW>
-__device__ __forceinline__ void groupBar() {
-    if (NW == kWarps) __syncthreads();
-    else asm volatile("bar.sync 2, %0;" ::"n"(NW * 32) : "memory");
-}
-
-// Exclusive scan of v over the first NW warps; returns the offset and the total.
-template <int NW>
-__device__ __forceinline__ int groupExclusiveScan(int v, int& total, Scan& sh) {
+// Exclusive scan of v over the block; returns the offset and the total.
+__device__ __forceinline__ int blockExclusiveScan(int v, int& total, Scan& sh) {
     int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     int incl = v;
 #pragma unroll
@@ -348,22 +340,17 @@ __device__ __forceinline__ int groupExclusiveScan(int v, int& total, Scan& sh) {
         if (lane >= o) incl += t;
     }
     if (lane == 31) sh.warpTot[w] = incl;
-    groupBar<NW>();
+    __syncthreads();
     int woff = 0;
     total = 0;
 #pragma unroll
-    for (int q = 0; q < NW; ++q) {
+    for (int q = 0; q < kWarps; ++q) {
         int t = sh.warpTot[q];
         if (q < w) woff += t;
         total += t;
     }
-    groupBar<NW>();
+    __syncthreads();
     return woff + incl - v;
-}
-
-// Exclusive scan of v over the block; returns the offset and the total.
-__device__ __forceinline__ int blockExclusiveScan(int v, int& total, Scan& sh) {
-    return groupExclusiveScan<kWarps>(v, total, sh);
 }
 
 // Fixed-order block sum of two doubles; result valid in thread 0.
@@ -412,9 +399,7 @@ struct Stencil {
 };
 
 // The stencil of cell (cx, cy, cz): its cells and their offsets in the concatenated
-// candidate list (cells in stencil order, particles in cell-list order).  Run by the first
-// NW warps of the block.
-template <int NW = kWarps>
+// candidate list (cells in stencil order, particles in cell-list order).
 __device__ void stageStencil(const SweepArgs& a, int cx, int cy, int cz, Stencil& st, Scan& sc) {
     const Grid& g = a.g;
     const int nx = axisCount(g.nc[0], g.s[0]), ny = axisCount(g.nc[1], g.s[1]), nz = axisCount(g.nc[2], g.s[2]);
@@ -424,7 +409,7 @@ __device__ void stageStencil(const SweepArgs& a, int cx, int cy, int cz, Stencil
     const int ownZ = g.nc[2] <= 2 * g.s[2] ? cz : g.s[2];
     const int ownQ = (ownZ * ny + ownY) * nx + own;
     int carry = 0;
-    for (int base = 0; base < nn; base += NW * 32) {
+    for (int base = 0; base < nn; base += kMoveThreads) {
         int q = base + threadIdx.x;
         int cnt = 0, cell = 0;
         if (q < nn) {
@@ -436,7 +421,7 @@ __device__ void stageStencil(const SweepArgs& a, int cx, int cy, int cz, Stencil
             cnt = a.cellCount[cell];
         }
         int total;
-        int off = groupExclusiveScan<NW>(cnt, total, sc);
+        int off = blockExclusiveScan(cnt, total, sc);
         if (q < nn) {
             st.nbCell[q] = cell;
             st.nbOff[q] = carry + off;
@@ -448,19 +433,17 @@ __device__ void stageStencil(const SweepArgs& a, int cx, int cy, int cz, Stencil
         st.nbOff[nn] = carry;
         st.nCand = carry;
     }
-    groupBar<NW>();
+    __syncthreads();
     if (threadIdx.x == 0) st.ownOff = st.nbOff[ownQ];
-    groupBar<NW>();
+    __syncthreads();
 }
 
 // Loads candidates [first, first + count) of the stencil into shared memory (count <=
-// kCandCap).  A stencil larger than the buffer is processed in windows of kCandCap.  Run by
-// the first NW warps of the block.
-template <int NW = kWarps>
+// kCandCap).  A stencil larger than the buffer is processed in windows of kCandCap.
 __device__ void loadCandidates(const SweepArgs& a, const Stencil& st, int first, int count, int* candIdx,
                                float4* candPos, float4* candDir = nullptr, float4* candPat = nullptr) {
     const int nn = st.nNb;
-    for (int kk = threadIdx.x; kk < count; kk += NW * 32) {
+    for (int kk = threadIdx.x; kk < count; kk += kMoveThreads) {
         int k = first + kk;
         int lo = 0, hi = nn - 1;      // last q with nbOff[q] <= k
         while (lo < hi) {
@@ -473,7 +456,7 @@ __device__ void loadCandidates(const SweepArgs& a, const Stencil& st, int first,
         if (candDir) candDir[kk] = a.cellDirF[slot];
         if (candPat) candPat[kk] = a.cellPatF[slot];
     }
-    groupBar<NW>();
+    __syncthreads();
 }
 
 // FP32 closest distance^2 of two segments (centres r apart, r = c1 - c2, unit axes u, v,
@@ -689,7 +672,7 @@ __device__ __forceinline__ void randomUnitSphere(Stream& r, double& x, double& y
 // sides, chiral axes), then patchdir[0] is re-orthogonalised against the new axis as
 // partRotate does (movecreator.cpp:1007).
 __device__ void buildProposal(const SweepArgs& a, const MoveShared& sh, Proposal& P, int cell, int cnt, int m, int cx,
-                              int cy, int cz, const double3& box, bool stencilReady = true) {
+                              int cy, int cz, const double3& box) {
     const Control& ctl = *a.ctl;
     const int lane = threadIdx.x & 31;
     Stream r(a.seed, (uint32_t)cell, (uint32_t)m, (uint32_t)ctl.sweep ^ ((uint32_t)(ctl.sweep >> 32) << 20));
@@ -764,8 +747,7 @@ __device__ void buildProposal(const SweepArgs& a, const MoveShared& sh, Proposal
         P.npos[0] = npx; P.npos[1] = npy; P.npos[2] = npz;
         P.oldF = make_float3(frac32(p.x), frac32(p.y), frac32(p.z));
         P.newF = make_float3(frac32(npx), frac32(npy), frac32(npz));
-        // bonded partners are evaluated explicitly; they must sit inside the stencil (checked
-        // here, or by checkPartners once the stencil is staged)
+        // bonded partners are evaluated explicitly; they must sit inside the stencil
         DevCtx c;
         c.mols = a.t.mols;
         Con con = makeCon(c, t, a.s.mol[t]);
@@ -773,18 +755,12 @@ __device__ void buildProposal(const SweepArgs& a, const MoveShared& sh, Proposal
         for (int q = 0; q < 4; ++q) {
             int j = con.idx[q];
             if (j < 0) continue;
-            if (stencilReady && !partnerInStencil(a, sh.st, j)) { atomicOr(a.err, E_PARTNER_FAR); skip = 1; }
+            if (!partnerInStencil(a, sh.st, j)) { atomicOr(a.err, E_PARTNER_FAR); skip = 1; }
             P.partners[np++] = j;
         }
         P.nPartners = np;
         P.skip = skip;
     }
-}
-
-// The deferred stencil check of a proposal built before the stencil was staged (one thread).
-__device__ void checkPartners(const SweepArgs& a, const MoveShared& sh, Proposal& P) {
-    for (int q = 0; q < P.nPartners; ++q)
-        if (!partnerInStencil(a, sh.st, P.partners[q])) { atomicOr(a.err, E_PARTNER_FAR); P.skip = 1; }
 }
 
 __device__ __forceinline__ bool isPartner(const Proposal& P, int j) {
@@ -974,26 +950,9 @@ __device__ __forceinline__ void colourBody(const SweepArgs* __restrict__ A, int 
     const int tid = threadIdx.x, warp = tid >> 5;
     const double3 box = mk(a.s.box[0], a.s.box[1], a.s.box[2]);
     for (int k = tid; k < cnt; k += kMoveThreads) sh.list[k] = a.cellIdx[a.cellStart[cell] + k];
-    __syncthreads();
-    // the first pass's proposals (warp 3) while warps 0-2 stage the stencil and its candidates
-    const int first = (!a.mlp && cnt > 1) ? 2 : 1;
-    if (warp == 3) {
-        for (int q = 0; q < first; ++q) {
-            buildProposal(a, sh, sh.prop[q], cell, cnt, q, cx, cy, cz, box, false);
-            if (tid == 96) acceptThresholds(a, sh.prop[q], cell, q);
-        }
-    } else {
-        stageStencil<3>(a, cx, cy, cz, sh.st, sh.scan);
-        if (sh.st.nCand <= kCandCap) loadCandidates<3>(a, sh.st, 0, sh.st.nCand, candIdx, candPos, candDir, candPat);
-    }
-    __syncthreads();
-    if (tid == 96) {
-        for (int q = 0; q < 4; ++q) {
-            if (q < first) checkPartners(a, sh, sh.prop[q]);
-            sh.propFor[q] = q < first ? q : -1;
-        }
-    }
-    __syncthreads();
+    if (tid < 4) sh.propFor[tid] = -1;
+    stageStencil(a, cx, cy, cz, sh.st, sh.scan);
+    if (sh.st.nCand <= kCandCap) loadCandidates(a, sh.st, 0, sh.st.nCand, candIdx, candPos, candDir, candPat);
     const int nCand = sh.st.nCand;
     const bool resident = nCand <= kCandCap;
 
@@ -1005,19 +964,20 @@ __device__ __forceinline__ void colourBody(const SweepArgs* __restrict__ A, int 
     unsigned long long nS1Rej = 0, nS2Tried = 0, nS2Rej = 0;
     double daErr2 = 0.0, daErrSum = 0.0;
 
-    // Moves run in passes.  A pass evaluates move m and -- without a surrogate stage -- move
-    // m + 1 as well, both against the state before move m; queue entries carry the move in
-    // bit 1 and the configuration (0 old, 1 new) in bit 0, so the two moves' pairs share
-    // the lanes of one stage C.  Move m is decided first; move m + 1's energies stand when
-    // move m was rejected or when the two targets are out of each other's range, and its
-    // decision is then the one a pass of its own would take (same proposal, same
-    // thresholds, same pair energies); otherwise the next pass evaluates it again.
-    // Proposals live in a ring of four slots; warps 2 and 3 build the next pass's during
-    // stage C.
+    // Moves run in passes of one move, or -- with paired passes on and no surrogate stage --
+    // of two: move m + 1 is evaluated together with move m, both against the state before
+    // move m; queue entries carry the move in bit 1 and the configuration (0 old, 1 new) in
+    // bit 0, so the two moves' pairs share the lanes of one stage C.  Move m is decided
+    // first; move m + 1's energies stand when move m was rejected or when the two targets
+    // are out of each other's range, and its decision is then the one a pass of its own
+    // would take (same proposal, same thresholds, same pair energies); otherwise the next
+    // pass evaluates it again.  Proposals live in a ring of four slots; warps 2 and 3 build
+    // the next pass's during stage C.
     const float bxF = (float)box.x, byF = (float)box.y, bzF = (float)box.z;
     unsigned evalMine = 0;          // pairs this thread evaluated for moves that were decided
     for (int m = 0; m < cnt; ++m) {
-        const bool pair = !a.mlp && m + 1 < cnt;
+        // paired passes start with the second pass (the first builds their proposals)
+        const bool pair = a.pairMoves && !a.mlp && m > 0 && m + 1 < cnt;
         {
             const bool need0 = sh.propFor[m & 3] != m;
             const bool need1 = pair && sh.propFor[(m + 1) & 3] != m + 1;
@@ -1109,6 +1069,8 @@ __device__ __forceinline__ void colourBody(const SweepArgs* __restrict__ A, int 
 
         // energies of move m (0 old, 1 new) and move m + 1 (2 old, 3 new)
         double e0 = 0.0, e1 = 0.0, e2 = 0.0, e3 = 0.0;
+        const Con con0 = makeCon(c, t, a.s.mol[t]);
+        const Con con1 = eval1 ? makeCon(c, t1, a.s.mol[t1]) : con0;
         auto addE = [&](int b, double en) {
             if (b == 0) e0 += en; else if (b == 1) e1 += en; else if (b == 2) e2 += en; else e3 += en;
         };
@@ -1119,7 +1081,7 @@ __device__ __forceinline__ void colourBody(const SweepArgs* __restrict__ A, int 
             const Proposal* Pp = warp == 0 ? &P0 : (warp == 1 && eval1 ? &P1 : nullptr);
             if (Pp && lane < Pp->nPartners) {
                 PView b = viewAt(a.s, Pp->partners[lane]);
-                Con cn = makeCon(c, Pp->target, a.s.mol[Pp->target]);
+                const Con& cn = warp == 0 ? con0 : con1;
                 unsigned bb; double dd;
                 addE(warp * 2, pairEnergy(c, moveView(a.s, *Pp, false), b, cn, box, &bb, &dd));
                 addE(warp * 2 + 1, pairEnergy(c, moveView(a.s, *Pp, true), b, cn, box, &bb, &dd));
@@ -1130,9 +1092,8 @@ __device__ __forceinline__ void colourBody(const SweepArgs* __restrict__ A, int 
         auto evalEntry = [&](int q) {
             const Proposal& Pq = (q & 2) ? P1 : P0;
             PView b = viewAt(a.s, candIdx[q >> 2]);
-            Con cn = makeCon(c, Pq.target, a.s.mol[Pq.target]);
             unsigned bb; double dd;
-            addE(q & 3, pairEnergy(c, moveView(a.s, Pq, q & 1), b, cn, box, &bb, &dd));
+            addE(q & 3, pairEnergy(c, moveView(a.s, Pq, q & 1), b, (q & 2) ? con1 : con0, box, &bb, &dd));
         };
         // classes 1 and 2 over nw warps starting at warp w0; class 2 starts on a warp boundary
         auto evalGeneric = [&](int w0, int nw) {
@@ -1151,7 +1112,7 @@ __device__ __forceinline__ void colourBody(const SweepArgs* __restrict__ A, int 
         // the next pass's proposals, built while stage C runs: move m + 2 (and m + 3) after a
         // pair, m + 1 otherwise.  They stay valid unless a move of this pass is accepted on the
         // same particle.
-        const int specA = pair ? m + 2 : m + 1, specB = pair ? m + 3 : cnt;
+        const int specA = pair ? m + 2 : m + 1, specB = pair ? m + 3 : (a.pairMoves && !a.mlp && m == 0 ? m + 2 : cnt);
         auto speculate = [&](int mv) {
             if (sh.propFor[mv & 3] == mv) return;      // still valid from an earlier pass
             Proposal& N = sh.prop[mv & 3];
@@ -1389,7 +1350,7 @@ __device__ __forceinline__ void colourBody(const SweepArgs* __restrict__ A, int 
 // (up to 255 registers, two CTAs per SM: the shortest move latency, for systems whose
 // colours hold few cells) and kColourDense (at most 170 registers, three CTAs per SM:
 // more moves in flight per SM, for large systems); the bench's tuner picks one.
-__global__ void __launch_bounds__(kMoveThreads) kColour(const SweepArgs* __restrict__ A, int phase) {
+__global__ void __launch_bounds__(kMoveThreads, 1) kColour(const SweepArgs* __restrict__ A, int phase) {
     colourBody(A, phase);
 }
 __global__ void __launch_bounds__(kMoveThreads, 3) kColourDense(const SweepArgs* __restrict__ A, int phase) {
@@ -2258,6 +2219,7 @@ static void fillArgs(Context* c, SweepEngine* e, const sc_run_params& p) {
     a.rotAngle = p.rot_angle;
     a.edgeMx = p.edge_mx;
     a.ptype = p.ptype;
+    a.pairMoves = (p.variant & 2) ? 1 : 0;
     for (size_t k = 0; k < c->usedTypes.size() && k < (size_t)MAX_DEV_TYPES; ++k) {
         int t = c->usedTypes[k];
         // per-type displacement (sim.h:368-373); the run's transmx replaces the options value
@@ -2524,7 +2486,7 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
     bool anySurrogate = false;
     for (const SweepArgs& h : b.hArgs) anySurrogate |= (h.mlp != nullptr);
     const size_t colourSmem = anySurrogate ? kDynSmemSurrogate : kDynSmemColour;
-    const bool dense = p.variant == 1;
+    const bool dense = (p.variant & 1) != 0;
     auto launchCellsOf = [&](const SweepArgs* args, int maxCells) -> cudaError_t {
         kZeroCounts<<<dims((maxCells + 255) / 256), 256, 0, s>>>(args);
         kAssign<<<dims((b.maxN + 255) / 256), 256, 0, s>>>(args);
@@ -2699,7 +2661,7 @@ static int checkParams(const sc_run_params& p) {
     if (!(p.temper > 0)) return fail(SC_ERR_ARG, "temper must be positive");
     if (p.ptype < 0 || p.ptype > 5) return fail(SC_ERR_ARG, "ptype must be 0..5 (movecreator.cpp:349-546)");
     if (p.stencil < 0 || p.stencil > 3) return fail(SC_ERR_ARG, "stencil must be 0 (auto), 1, 2 or 3");
-    if (p.variant < 0 || p.variant > 1) return fail(SC_ERR_ARG, "variant must be 0 or 1");
+    if (p.variant < 0 || p.variant > 3) return fail(SC_ERR_ARG, "variant must be 0..3");
     return SC_OK;
 }
 

@@ -105,6 +105,25 @@ def test_kernel_variants_give_the_same_trajectory():
     s2.close()
 
 
+@pytest.mark.parametrize("name", ["psc_nvt", "cpsc_spa_npt"])
+def test_paired_passes_keep_the_running_energy_exact(name):
+    """Paired passes (move m + 1 evaluated with move m, kept when move m changed nothing it
+    saw): exact running energy, and both register budgets on the same trajectory."""
+    _, s1 = open_ens(name)
+    _, s2 = open_ens(name)
+    p = s1.default_run()
+    p.stencil = 1                      # larger cells: several moves per cell
+    a = s1.simulate(p, nsweeps=60, seed=12, check_every=30, variant=2)
+    b = s2.simulate(p, nsweeps=60, seed=12, check_every=30, variant=3)
+    assert a.energy == b.energy and a.acc_trans == b.acc_trans and a.acc_rot == b.acc_rot
+    assert a.moves == 60 * s1.n and a.acc_trans + a.acc_rot > 0
+    e1 = s1.all_to_all()
+    assert abs(a.energy - e1) <= 1e-9 * max(1.0, abs(e1))
+    assert abs(a.energy_check - e1) <= 1e-9 * max(1.0, abs(e1))
+    s1.close()
+    s2.close()
+
+
 def test_rotations_keep_unit_vectors_and_patch_frame():
     _, s = open_ens("psc_nvt")
     s.simulate(nsweeps=100, seed=3, check_every=0)
