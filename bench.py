@@ -301,9 +301,10 @@ def bench_replicas(steps, seed=1):
 
 def tune_variant(s, p, delayed=0):
     """The move-kernel variant that runs s fastest (bit 0: more CTAs per SM instead of the
-    lowest latency per move; bit 1: paired passes, plain moves only)."""
+    lowest latency per move; bit 1: paired passes, plain moves only; bit 2: one dataflow
+    launch per sweep instead of one launch per colour)."""
     best = None
-    for v in ((0, 1) if delayed else (0, 1, 2, 3)):
+    for v in ((0, 1, 4, 5) if delayed else (0, 1, 2, 3, 4, 5)):
         s.simulate(p, nsweeps=2, variant=v, delayed=delayed)
         st = s.simulate(p, nsweeps=4, variant=v, delayed=delayed)
         rate = st.moves / max(st.seconds, 1e-12)
@@ -463,7 +464,7 @@ def main():
     best = None
     tune, _ = open_workload(a.workload, a.seed)
     L.check(tune._lib.sc_set_device(tune._h, local))
-    for reach, variant in ((1, 0), (2, 0), (3, 0), (2, 1), (1, 2), (2, 2)):
+    for reach, variant in ((1, 0), (2, 0), (3, 0), (2, 1), (1, 2), (2, 2), (1, 4), (2, 4), (3, 4), (2, 5)):
         try:
             tune.simulate(p, nsweeps=4, stencil=reach, variant=variant)            # grid, graph capture
             st = tune.simulate(p, nsweeps=10, stencil=reach, variant=variant)

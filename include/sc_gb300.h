@@ -86,7 +86,8 @@ typedef struct {
     int stencil;            /* cell-list reach s: cells >= maxcut/s wide, (s+1)^3 colours; 0: chosen by the tuner */
     int delayed;            /* 1: two-stage moves with the context's surrogate (sc_set_surrogate) as first stage */
     int variant;            /* move kernel, bit 0: more moves in flight per SM (large systems), else lowest
-                               latency per move; bit 1: paired passes (two moves per stage C) */
+                               latency per move; bit 1: paired passes (two moves per stage C); bit 2: one
+                               dataflow launch per sweep instead of one launch per colour */
     int pad_;
 } sc_run_params;
 

@@ -65,7 +65,7 @@ constexpr size_t kDynSmemSurrogate = kDynSmem + (size_t)kCandCap * 2 * sizeof(fl
 
 enum Ctr { C_ACC_T, C_REJ_T, C_ACC_R, C_REJ_R, C_ACC_V, C_REJ_V, C_VOL_CONSTR, C_TESTED, C_EVAL, C_CELL_REJ, C_MOVES,
            C_SCREENED, C_S1_REJ, C_S2_TRIED, C_S2_REJ, C_ACC_CH, C_REJ_CH, C_CH_CONSTR, C_COUNT };
-enum ErrBit { E_CELL_OVERFLOW = 1, E_PARTNER_FAR = 2 };
+enum ErrBit { E_CELL_OVERFLOW = 1, E_PARTNER_FAR = 2, E_FLOW_WAIT = 4 };
 
 struct Grid {
     int nc[3];
@@ -91,6 +91,8 @@ struct Control {
     double energyCheck;   // last exact total energy
     double maxDrift;
     double daErr2, daErrSum;   // sums of (dE - dEs)^2 and dE - dEs over moves reaching the exact stage
+    unsigned epoch;       // sweeps begun, never reset (stamps of the dataflow sweep's cells)
+    int ticket;           // next cell of the dataflow sweep
 };
 
 struct SweepArgs {
@@ -107,6 +109,7 @@ struct SweepArgs {
     float4* cellPatF;     // FP32 first patch direction (written only when a surrogate is attached)
     int* cellOf;
     double* cellDE;
+    unsigned* cellDone;   // dataflow sweep: epoch of the sweep in which the cell finished
     double* partial;      // per-cell energy sums
     unsigned long long* counters;
     int* err;
@@ -159,6 +162,8 @@ __global__ void kBeginSweep(const SweepArgs* __restrict__ A, int volumeDue) {
     const SweepArgs& a = A[blockIdx.y];
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     Control& c = *a.ctl;
+    c.epoch += 1;
+    c.ticket = 0;
     Stream r(a.seed, 0xFFFFFFF0u, (uint32_t)c.sweep, (uint32_t)(c.sweep >> 32));
     for (int d = 0; d < 3; ++d) c.shift[d] = r.next() / a.g.nc[d];
     int n = a.g.ncolours;
@@ -929,21 +934,18 @@ __device__ __forceinline__ void decodeActive(const Grid& g, int colour, int bloc
     cx = ox + g.p[0] * bx; cy = oy + g.p[1] * by; cz = oz + g.p[2] * bz;
 }
 
-// The move kernel body; instantiated twice (see kColour / kColourDense below).
-__device__ __forceinline__ void colourBody(const SweepArgs* __restrict__ A, int phase) {
+// The moves of cell (cx, cy, cz), by the whole CTA: the move kernel body, run once per CTA
+// by the colour-phase kernels (kColour / kColourDense) and once per taken cell by the
+// dataflow kernels (kColourFlow / kColourFlowDense).
+__device__ __forceinline__ void moveCell(const SweepArgs& a, int cx, int cy, int cz) {
     extern __shared__ float4 dynSmem[];
     __shared__ MoveShared sh;
-    const SweepArgs& a = A[blockIdx.y];
     float4* candPos = dynSmem;
     int* candIdx = reinterpret_cast<int*>(candPos + kCandCap);
     // FP32 axes of the candidates (stage B), with a surrogate their patch directions as well
     float4* candDir = reinterpret_cast<float4*>(candIdx + kCandCap);
     float4* candPat = a.mlp ? candDir + kCandCap : nullptr;
-    const Control& ctl = *a.ctl;
     const Grid& g = a.g;
-    if ((int)blockIdx.x >= g.nactive || phase >= g.ncolours) return;
-    int cx, cy, cz;
-    decodeActive(g, ctl.perm[phase], blockIdx.x, cx, cy, cz);
     int cell = (cz * g.nc[1] + cy) * g.nc[0] + cx;
     int cnt = a.cellCount[cell];
     if (cnt == 0 || cnt > kCellCap) return;
@@ -1346,6 +1348,16 @@ __device__ __forceinline__ void colourBody(const SweepArgs* __restrict__ A, int 
     if ((tid & 31) == 0 && evalMine) atomicAdd(&a.counters[C_EVAL], (unsigned long long)evalMine);
 }
 
+// One colour phase: CTA blockIdx.x takes active cell blockIdx.x of the phase's colour.
+__device__ __forceinline__ void colourBody(const SweepArgs* __restrict__ A, int phase) {
+    const SweepArgs& a = A[blockIdx.y];
+    const Grid& g = a.g;
+    if ((int)blockIdx.x >= g.nactive || phase >= g.ncolours) return;
+    int cx, cy, cz;
+    decodeActive(g, a.ctl->perm[phase], blockIdx.x, cx, cy, cz);
+    moveCell(a, cx, cy, cz);
+}
+
 // One CTA per active cell of a colour.  Two register budgets of the same code: kColour
 // (up to 255 registers, two CTAs per SM: the shortest move latency, for systems whose
 // colours hold few cells) and kColourDense (at most 170 registers, three CTAs per SM:
@@ -1356,6 +1368,85 @@ __global__ void __launch_bounds__(kMoveThreads, 1) kColour(const SweepArgs* __re
 __global__ void __launch_bounds__(kMoveThreads, 3) kColourDense(const SweepArgs* __restrict__ A, int phase) {
     colourBody(A, phase);
 }
+
+// ---- dataflow sweep ---------------------------------------------------------------------
+// All colour phases of a sweep in one launch.  CTAs take cells in phase order from a ticket
+// counter; a cell first waits until every cell of an earlier phase within its stencil (+-s
+// cells per axis: the cells whose particles its moves read, and whose moves read its
+// particles) has finished, then moves exactly as in its colour phase.  Cells of one phase
+// never touch each other and every pair of cells that does is ordered by phase as the phase
+// kernels order it, so each cell sees the states it sees there: the trajectory is the
+// phase kernels' (same states, same random numbers), without a grid-wide barrier between
+// phases.  Forward progress: a CTA waits only on cells with smaller tickets, taken earlier
+// by CTAs that are running, and the smallest unfinished ticket waits on nothing.  Every
+// wait is bounded: after kFlowSpin polls the CTA sets E_FLOW_WAIT and every CTA returns.
+constexpr int kFlowSpin = 1 << 19;      // polls of one wait (~0.2 s; a legitimate wait is < 20 ms)
+
+__device__ __forceinline__ unsigned loadAcquireGpu(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void storeReleaseGpu(unsigned* p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ void flowBody(const SweepArgs* __restrict__ A) {
+    const SweepArgs& a = A[blockIdx.y];
+    const Grid& g = a.g;
+    __shared__ int sTicket, sFail;
+    __shared__ int posOf[kMaxColours];       // phase of each colour in this sweep
+    const int tid = threadIdx.x;
+    const unsigned stamp = a.ctl->epoch;
+    for (int k = tid; k < g.ncolours; k += kMoveThreads) posOf[a.ctl->perm[k]] = k;
+    const int total = g.ncolours * g.nactive;
+    const int nx = axisCount(g.nc[0], g.s[0]), ny = axisCount(g.nc[1], g.s[1]), nz = axisCount(g.nc[2], g.s[2]);
+    const int nn = nx * ny * nz;
+    for (;;) {
+        __syncthreads();            // the previous cell's shared state is free; posOf is visible
+        if (tid == 0) {
+            sTicket = atomicAdd(&a.ctl->ticket, 1);
+            sFail = 0;
+        }
+        __syncthreads();
+        const int tk = sTicket;
+        if (tk >= total) break;
+        const int phase = tk / g.nactive;
+        int cx, cy, cz;
+        decodeActive(g, a.ctl->perm[phase], tk - phase * g.nactive, cx, cy, cz);
+        for (int q = tid; q < nn && !*(volatile int*)&sFail; q += kMoveThreads) {
+            int qx = q % nx, qy = (q / nx) % ny, qz = q / (nx * ny);
+            int x = axisCell(cx, qx, g.nc[0], g.s[0]);
+            int y = axisCell(cy, qy, g.nc[1], g.s[1]);
+            int z = axisCell(cz, qz, g.nc[2], g.s[2]);
+            int colour = (x % g.p[0]) + g.p[0] * ((y % g.p[1]) + g.p[1] * (z % g.p[2]));
+            if (posOf[colour] >= phase) continue;
+            const unsigned* f = &a.cellDone[(z * g.nc[1] + y) * g.nc[0] + x];
+            for (int spin = 0; loadAcquireGpu(f) != stamp; ++spin) {
+                if (spin >= kFlowSpin || ((spin & 255) == 255 && (*(volatile int*)a.err & E_FLOW_WAIT))) {
+                    sFail = 1;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __syncthreads();
+        if (sFail) {
+            if (tid == 0) atomicOr(a.err, E_FLOW_WAIT);
+            break;
+        }
+        __threadfence();            // every thread reads the neighbours' states after the waits
+        moveCell(a, cx, cy, cz);
+        __syncthreads();            // the cell's state writes (thread 0) are issued
+        if (tid == 0) {
+            __threadfence();
+            storeReleaseGpu(&a.cellDone[(cz * g.nc[1] + cy) * g.nc[0] + cx], stamp);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kMoveThreads, 1) kColourFlow(const SweepArgs* __restrict__ A) { flowBody(A); }
+__global__ void __launch_bounds__(kMoveThreads, 3) kColourFlowDense(const SweepArgs* __restrict__ A) { flowBody(A); }
 
 // Adds the cells' energy changes of this sweep, in a fixed order, and clears them (a cell
 // without particles writes nothing during the sweep).
@@ -2048,6 +2139,7 @@ struct SweepEngine {
     float4* cellDirF = nullptr;
     float4* cellPatF = nullptr;
     double* cellDE = nullptr;
+    unsigned* cellDone = nullptr;
     double* partial = nullptr;
     unsigned long long* counters = nullptr;
     int* err = nullptr;
@@ -2180,7 +2272,7 @@ static int ensureGrid(Context* c, SweepEngine* e, const double* box) {
     if (g.ncolours > kMaxColours) return fail(SC_ERR_RANGE, "too many colour classes");
     if (g.ncells > e->ncellsAlloc) {
         for (void** p : {(void**)&e->cellStart, (void**)&e->cellCount, (void**)&e->cellCursor, (void**)&e->cellDE,
-                         (void**)&e->partial}) {
+                         (void**)&e->partial, (void**)&e->cellDone}) {
             if (*p) {
                 cudaFree(*p);
                 e->allocs.erase(std::find(e->allocs.begin(), e->allocs.end(), *p));
@@ -2194,7 +2286,9 @@ static int ensureGrid(Context* c, SweepEngine* e, const double* box) {
         if ((rc = engineAlloc(e, (void**)&e->cellCursor, sizeof(int) * n))) return rc;
         if ((rc = engineAlloc(e, (void**)&e->cellDE, sizeof(double) * n))) return rc;
         if ((rc = engineAlloc(e, (void**)&e->partial, sizeof(double) * n))) return rc;
+        if ((rc = engineAlloc(e, (void**)&e->cellDone, sizeof(unsigned) * n))) return rc;
         cudaMemset(e->cellDE, 0, sizeof(double) * n);
+        cudaMemset(e->cellDone, 0, sizeof(unsigned) * n);
         e->ncellsAlloc = n;
     }
     e->g = g;
@@ -2211,6 +2305,7 @@ static void fillArgs(Context* c, SweepEngine* e, const sc_run_params& p) {
     a.cellStart = e->cellStart; a.cellCount = e->cellCount; a.cellCursor = e->cellCursor;
     a.cellIdx = e->cellIdx; a.cellPosF = e->cellPosF; a.cellOf = e->cellOf; a.cellDE = e->cellDE;
     a.cellDirF = e->cellDirF; a.cellPatF = e->cellPatF;
+    a.cellDone = e->cellDone;
     a.partial = e->partial;
     a.counters = e->counters; a.err = e->err;
     a.seed = p.seed;
@@ -2444,6 +2539,7 @@ static int systemErrors(Context* c) {
     cudaMemcpy(&err, c->engine->err, sizeof err, cudaMemcpyDeviceToHost);
     if (err & E_CELL_OVERFLOW) return fail(SC_ERR_DEVICE, "a cell holds more than 256 particles (density too high for the cell list)");
     if (err & E_PARTNER_FAR) return fail(SC_ERR_DEVICE, "a bonded partner lies beyond the cell stencil (bond longer than maxcut)");
+    if (err & E_FLOW_WAIT) return fail(SC_ERR_DEVICE, "dataflow sweep: a cell waited too long for its neighbours");
     return SC_OK;
 }
 
@@ -2474,6 +2570,12 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
         if ((r = cudaFuncSetAttribute(kColourDense, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)kDynSmemSurrogate)) != cudaSuccess)
             return cudaFail(r, "shared memory attribute");
+        if ((r = cudaFuncSetAttribute(kColourFlow, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)kDynSmemSurrogate)) != cudaSuccess)
+            return cudaFail(r, "shared memory attribute");
+        if ((r = cudaFuncSetAttribute(kColourFlowDense, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)kDynSmemSurrogate)) != cudaSuccess)
+            return cudaFail(r, "shared memory attribute");
         if ((r = cudaFuncSetAttribute(kCellEnergy, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDynSmem)) != cudaSuccess)
             return cudaFail(r, "shared memory attribute");
         if ((r = cudaFuncSetAttribute(kChainColour, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDynSmem)) !=
@@ -2487,6 +2589,12 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
     for (const SweepArgs& h : b.hArgs) anySurrogate |= (h.mlp != nullptr);
     const size_t colourSmem = anySurrogate ? kDynSmemSurrogate : kDynSmemColour;
     const bool dense = (p.variant & 1) != 0;
+    // dataflow sweep: one launch per sweep, CTAs per system so that the batch fills the SMs
+    // (two CTAs per SM at up to 255 registers, three at 170)
+    const bool flow = (p.variant & 4) != 0;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b.sys[0]->device);
+    const int flowCtas = std::max(1, std::min(b.maxColours * b.maxActive, std::max(1, sms) * (dense ? 3 : 2) / ns));
     auto launchCellsOf = [&](const SweepArgs* args, int maxCells) -> cudaError_t {
         kZeroCounts<<<dims((maxCells + 255) / 256), 256, 0, s>>>(args);
         kAssign<<<dims((b.maxN + 255) / 256), 256, 0, s>>>(args);
@@ -2519,9 +2627,14 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
         cudaError_t r2 = launchCells();
         if (r2 != cudaSuccess) return r2;
         if (timing) cudaEventRecord(b.evP0, s);
-        for (int ph = 0; ph < b.maxColours; ++ph) {
-            if (dense) kColourDense<<<dims(b.maxActive), kMoveThreads, colourSmem, s>>>(b.dArgs, ph);
-            else kColour<<<dims(b.maxActive), kMoveThreads, colourSmem, s>>>(b.dArgs, ph);
+        if (flow) {
+            if (dense) kColourFlowDense<<<dims(flowCtas), kMoveThreads, colourSmem, s>>>(b.dArgs);
+            else kColourFlow<<<dims(flowCtas), kMoveThreads, colourSmem, s>>>(b.dArgs);
+        } else {
+            for (int ph = 0; ph < b.maxColours; ++ph) {
+                if (dense) kColourDense<<<dims(b.maxActive), kMoveThreads, colourSmem, s>>>(b.dArgs, ph);
+                else kColour<<<dims(b.maxActive), kMoveThreads, colourSmem, s>>>(b.dArgs, ph);
+            }
         }
         if (timing) {
             cudaEventRecord(b.evP1, s);
@@ -2530,9 +2643,9 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
             cudaEventElapsedTime(&pms, b.evP0, b.evP1);
             phaseMs += pms;
         }
-        phaseLaunches += b.maxColours;
+        phaseLaunches += flow ? 1 : b.maxColours;
         kEndSweep<<<dims(1), 256, 0, s>>>(b.dArgs);
-        launches += 2 + b.maxColours;
+        launches += 2 + (flow ? 1 : b.maxColours);
         if (b.chains) {       // chain moves: their own grid, colours and cell list
             kBeginSweep<<<dims(1), 32, 0, s>>>(b.dArgsC, 0);
             if ((r2 = launchCellsOf(b.dArgsC, b.maxCellsC)) != cudaSuccess) return r2;
@@ -2661,7 +2774,7 @@ static int checkParams(const sc_run_params& p) {
     if (!(p.temper > 0)) return fail(SC_ERR_ARG, "temper must be positive");
     if (p.ptype < 0 || p.ptype > 5) return fail(SC_ERR_ARG, "ptype must be 0..5 (movecreator.cpp:349-546)");
     if (p.stencil < 0 || p.stencil > 3) return fail(SC_ERR_ARG, "stencil must be 0 (auto), 1, 2 or 3");
-    if (p.variant < 0 || p.variant > 3) return fail(SC_ERR_ARG, "variant must be 0..3");
+    if (p.variant < 0 || p.variant > 7) return fail(SC_ERR_ARG, "variant must be 0..7");
     return SC_OK;
 }
 

@@ -65,3 +65,27 @@ def test_uneven_sizes_in_one_batch():
         exact = s.all_to_all()
         assert abs(E[k] - exact) <= 1e-9 * max(1.0, abs(exact))
     R.close()
+
+
+def test_dataflow_sweep_in_a_batch_of_uneven_systems():
+    """The dataflow launch over a batch: each system takes its cells from its own ticket
+    counter; trajectories equal those of the colour-phase launches."""
+    from sc_gb300 import ReplicaSet, System, workloads
+
+    def batch(variant):
+        systems = [System.from_text(*workloads.nvt_psc(n, phi=0.15, seed=3 + n)) for n in (120, 400, 260)]
+        R = ReplicaSet(systems, [1.0, 0.9, 1.1], ladder=[0, 1, 2])
+        st, T, E, _, _ = R.run(30, exchange_every=10, seed=19, variant=variant)
+        R.close()
+        return systems, st, T, E
+
+    sa, a, Ta, Ea = batch(0)
+    sb, b, Tb, Eb = batch(4)
+    assert list(Ea) == list(Eb) and list(Ta) == list(Tb)
+    assert a.acc_trans == b.acc_trans and a.acc_rot == b.acc_rot
+    for x, y in zip(sa, sb):
+        assert all(list(p.pos) == list(q.pos) for p, q in zip(x.particles(), y.particles()))
+        exact = y.all_to_all()
+        assert abs(Eb[sb.index(y)] - exact) <= 1e-9 * max(1.0, abs(exact))
+    for s in sa + sb:
+        s.close()

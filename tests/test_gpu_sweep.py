@@ -105,6 +105,31 @@ def test_kernel_variants_give_the_same_trajectory():
     s2.close()
 
 
+@pytest.mark.parametrize("name,stencil", [("psc_nvt", 1), ("psc_nvt", 2), ("cpsc_spa_npt", 2)])
+def test_dataflow_sweep_gives_the_colour_phase_trajectory(name, stencil):
+    """One dataflow launch per sweep (cells wait for their earlier-phase neighbours) moves
+    every cell against the states the colour-phase launches show it: same trajectory, bit
+    for bit, under both register budgets."""
+    _, s1 = open_ens(name)
+    _, s2 = open_ens(name)
+    _, s3 = open_ens(name)
+    p = s1.default_run()
+    p.stencil = stencil
+    a = s1.simulate(p, nsweeps=40, seed=21, check_every=20, variant=0)
+    b = s2.simulate(p, nsweeps=40, seed=21, check_every=20, variant=4)
+    c = s3.simulate(p, nsweeps=40, seed=21, check_every=20, variant=5)
+    for x in (b, c):
+        assert x.energy == a.energy and x.acc_trans == a.acc_trans and x.acc_rot == a.acc_rot
+        assert x.acc_vol == a.acc_vol and x.moves == a.moves
+    assert b.launches < a.launches
+    for s in (s2, s3):
+        assert all(list(x.pos) == list(y.pos) and list(x.dir) == list(y.dir)
+                   for x, y in zip(s1.particles(), s.particles()))
+    assert list(s2.box) == list(s1.box)
+    for s in (s1, s2, s3):
+        s.close()
+
+
 @pytest.mark.parametrize("name", ["psc_nvt", "cpsc_spa_npt"])
 def test_paired_passes_keep_the_running_energy_exact(name):
     """Paired passes (move m + 1 evaluated with move m, kept when move m changed nothing it
