@@ -252,15 +252,17 @@ def bench_replicas(steps, seed=1):
             T.append(t)
             lad.append(g)
     R = ReplicaSet(ctxs, T, ladder=lad)
-    # the tuner: cell reach (tile size) that moves the batch fastest
+    # the tuner: cell reach (tile size) and kernel variant (colour-phase launches or one
+    # dataflow launch per sweep) that move the batch fastest
     best = None
-    for s in (1, 2):
-        R.run(4, exchange_every=100, seed=seed, stencil=s, check_every=0)          # grid, graph capture
-        st, *_ = R.run(8, exchange_every=100, seed=seed, stencil=s, check_every=0)
+    for s, v in ((1, 0), (2, 0), (1, 4), (2, 4)):
+        R.run(4, exchange_every=100, seed=seed, stencil=s, variant=v, check_every=0)   # grid, graph capture
+        st, *_ = R.run(8, exchange_every=100, seed=seed, stencil=s, variant=v, check_every=0)
         rate = st.moves / st.seconds
-        if best is None or rate > best[1]:
-            best = (s, rate)
-    st, Tout, E, tried, acc = R.run(steps, exchange_every=100, seed=seed + 1, stencil=best[0], check_every=0)
+        if best is None or rate > best[2]:
+            best = (s, v, rate)
+    st, Tout, E, tried, acc = R.run(steps, exchange_every=100, seed=seed + 1, stencil=best[0], variant=best[1],
+                                    check_every=0)
     batched = st.moves / st.seconds
     # the two forms together: the same batch with a surrogate first stage (trained on the
     # exact pairs of the ladders' configurations) -- delayed-acceptance sweeps
@@ -272,17 +274,22 @@ def bench_replicas(steps, seed=1):
     sur.train(epochs=6, batch=8192, lr=2e-3, warmup_steps=100, seed=seed)
     for c in ctxs:
         c.set_surrogate(sur)
-    std, *_ = R.run(steps, exchange_every=100, seed=seed + 3, stencil=best[0], check_every=0, delayed=1)
+    std, *_ = R.run(steps, exchange_every=100, seed=seed + 3, stencil=best[0], variant=best[1], check_every=0,
+                    delayed=1)
     batched_da = std.moves / std.seconds
     for c in ctxs:
         c.set_surrogate(None)
     sur.close()
-    # plain: every replica alone through the single-system loop (same tuned stencil)
+    # plain: every replica alone through the single-system loop (same tuned stencil, the
+    # kernel variant that runs a single system fastest)
+    s1 = System.from_text(*systems[0])
+    solo = tune_variant(s1, s1.default_run(), 0, stencil=best[0], candidates=(0, 4))
+    s1.close()
     moves = secs = 0.0
     for g, texts in enumerate(systems):
         s1 = System.from_text(*texts)
-        s1.simulate(nsweeps=2, seed=seed, stencil=best[0], check_every=0)
-        one = s1.simulate(nsweeps=3, seed=seed + 2, stencil=best[0], check_every=0)
+        s1.simulate(nsweeps=2, seed=seed, stencil=best[0], variant=solo, check_every=0)
+        one = s1.simulate(nsweeps=3, seed=seed + 2, stencil=best[0], variant=solo, check_every=0)
         moves += one.moves * len(temps)
         secs += one.seconds * len(temps)
         s1.close()
@@ -292,6 +299,7 @@ def bench_replicas(steps, seed=1):
     for c in ctxs:
         c.close()
     return {"workload": "pt64_psc_uneven", "replicas": len(ctxs), "particles": particles, "stencil": best[0],
+            "kernel_variant": {"batched": best[1], "plain": solo},
             "batched_moves_per_s": batched, "plain_moves_per_s": plain, "speedup": batched / plain,
             "batched_delayed_moves_per_s": batched_da, "speedup_batched_delayed": batched_da / plain,
             "delayed_stage1_decided": std.da_stage1_rejected / max(1, std.moves),
@@ -299,14 +307,16 @@ def bench_replicas(steps, seed=1):
             "sweeps": steps}
 
 
-def tune_variant(s, p, delayed=0):
+def tune_variant(s, p, delayed=0, stencil=0, candidates=None):
     """The move-kernel variant that runs s fastest (bit 0: more CTAs per SM instead of the
     lowest latency per move; bit 1: paired passes, plain moves only; bit 2: one dataflow
     launch per sweep instead of one launch per colour)."""
     best = None
-    for v in ((0, 1, 4, 5) if delayed else (0, 1, 2, 3, 4, 5)):
-        s.simulate(p, nsweeps=2, variant=v, delayed=delayed)
-        st = s.simulate(p, nsweeps=4, variant=v, delayed=delayed)
+    if candidates is None:
+        candidates = (0, 1, 4, 5) if delayed else (0, 1, 2, 3, 4, 5)
+    for v in candidates:
+        s.simulate(p, nsweeps=2, variant=v, delayed=delayed, stencil=stencil)
+        st = s.simulate(p, nsweeps=4, variant=v, delayed=delayed, stencil=stencil)
         rate = st.moves / max(st.seconds, 1e-12)
         if best is None or rate > best[1]:
             best = (v, rate)
@@ -461,19 +471,22 @@ def main():
     # tuner: the cell-list reach (cell size maxcut/s, (s+1)^3 colours) that moves this
     # system fastest, timed on a few sweeps each
     # (on a copy, so that the measured system starts from the same state as the reference arm)
+    # each candidate on a fresh copy of the start (an NPT system compresses while it runs,
+    # so one copy moved through all candidates would favour the first ones)
     best = None
-    tune, _ = open_workload(a.workload, a.seed)
-    L.check(tune._lib.sc_set_device(tune._h, local))
     for reach, variant in ((1, 0), (2, 0), (3, 0), (2, 1), (1, 2), (2, 2), (1, 4), (2, 4), (3, 4), (2, 5)):
+        tune, _ = open_workload(a.workload, a.seed)
+        L.check(tune._lib.sc_set_device(tune._h, local))
         try:
             tune.simulate(p, nsweeps=4, stencil=reach, variant=variant)            # grid, graph capture
             st = tune.simulate(p, nsweeps=10, stencil=reach, variant=variant)
         except Exception:
+            tune.close()
             continue
+        tune.close()
         rate = st.moves / max(st.seconds, 1e-12)
         if best is None or rate > best[2]:
             best = (reach, variant, rate)
-    tune.close()
     p.stencil, p.variant = best[0], best[1]
     # warm-up
     s.simulate(p, nsweeps=max(3, a.warmup))
@@ -531,10 +544,11 @@ def main():
     bytes_per_launch = (prof.pairs_tested * 28 + prof.pairs_evaluated * 120) / max(1, prof.phase_launches)
     t_launch = prof.phase_seconds / max(1, prof.phase_launches)
     achieved = bytes_per_launch / t_launch / 1e9 if t_launch > 0 else None
-    roof = {"bound": "hbm", "kernel": "kColour", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+    kernel = ["kColour", "kColourDense", None, None, "kColourFlow", "kColourFlowDense"][int(p.variant) & 5]
+    roof = {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
             "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
-            "traffic": profiled_traffic("kColour", a.workload),
-            "traffic_source": f"profiles/kColour_{a.workload}.md (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
+            "traffic": profiled_traffic(kernel, a.workload),
+            "traffic_source": f"profiles/{kernel}_{a.workload}.md (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
             "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
             "avg_launch_us": t_launch * 1e6, "algorithmic_bytes_per_launch": bytes_per_launch,
             "note": "the move kernel is FP64-latency bound; see fp64 for its arithmetic rate"}
