@@ -1414,6 +1414,11 @@ __device__ __forceinline__ void flowBody(const SweepArgs* __restrict__ A) {
         const int phase = tk / g.nactive;
         int cx, cy, cz;
         decodeActive(g, a.ctl->perm[phase], tk - phase * g.nactive, cx, cy, cz);
+        const int cell = (cz * g.nc[1] + cy) * g.nc[0] + cx;
+        if (a.cellCount[cell] == 0) {           // no moves: nothing to wait for, nothing to publish first
+            if (tid == 0) storeReleaseGpu(&a.cellDone[cell], stamp);
+            continue;
+        }
         for (int q = tid; q < nn && !*(volatile int*)&sFail; q += kMoveThreads) {
             int qx = q % nx, qy = (q / nx) % ny, qz = q / (nx * ny);
             int x = axisCell(cx, qx, g.nc[0], g.s[0]);
@@ -1440,7 +1445,7 @@ __device__ __forceinline__ void flowBody(const SweepArgs* __restrict__ A) {
         __syncthreads();            // the cell's state writes (thread 0) are issued
         if (tid == 0) {
             __threadfence();
-            storeReleaseGpu(&a.cellDone[(cz * g.nc[1] + cy) * g.nc[0] + cx], stamp);
+            storeReleaseGpu(&a.cellDone[cell], stamp);
         }
     }
 }
