@@ -1391,9 +1391,14 @@ __device__ __forceinline__ void storeReleaseGpu(unsigned* p, unsigned v) {
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+__device__ __forceinline__ void chainCell(const SweepArgs& a, int cx, int cy, int cz);
+
+template <bool CHAIN>
 __device__ __forceinline__ void flowBody(const SweepArgs* __restrict__ A) {
     const SweepArgs& a = A[blockIdx.y];
     const Grid& g = a.g;
+    if (CHAIN && a.nChains == 0) return;
+    const int* counts = CHAIN ? a.chainCellCount : a.cellCount;
     __shared__ int sTicket, sFail;
     __shared__ int posOf[kMaxColours];       // phase of each colour in this sweep
     const int tid = threadIdx.x;
@@ -1415,7 +1420,7 @@ __device__ __forceinline__ void flowBody(const SweepArgs* __restrict__ A) {
         int cx, cy, cz;
         decodeActive(g, a.ctl->perm[phase], tk - phase * g.nactive, cx, cy, cz);
         const int cell = (cz * g.nc[1] + cy) * g.nc[0] + cx;
-        if (a.cellCount[cell] == 0) {           // no moves: nothing to wait for, nothing to publish first
+        if (counts[cell] == 0) {                // no moves: nothing to wait for, nothing to publish first
             if (tid == 0) storeReleaseGpu(&a.cellDone[cell], stamp);
             continue;
         }
@@ -1441,7 +1446,8 @@ __device__ __forceinline__ void flowBody(const SweepArgs* __restrict__ A) {
             break;
         }
         __threadfence();            // every thread reads the neighbours' states after the waits
-        moveCell(a, cx, cy, cz);
+        if (CHAIN) chainCell(a, cx, cy, cz);
+        else moveCell(a, cx, cy, cz);
         __syncthreads();            // the cell's state writes (thread 0) are issued
         if (tid == 0) {
             __threadfence();
@@ -1450,8 +1456,10 @@ __device__ __forceinline__ void flowBody(const SweepArgs* __restrict__ A) {
     }
 }
 
-__global__ void __launch_bounds__(kMoveThreads, 1) kColourFlow(const SweepArgs* __restrict__ A) { flowBody(A); }
-__global__ void __launch_bounds__(kMoveThreads, 3) kColourFlowDense(const SweepArgs* __restrict__ A) { flowBody(A); }
+__global__ void __launch_bounds__(kMoveThreads, 1) kColourFlow(const SweepArgs* __restrict__ A) { flowBody<false>(A); }
+__global__ void __launch_bounds__(kMoveThreads, 3) kColourFlowDense(const SweepArgs* __restrict__ A) {
+    flowBody<false>(A);
+}
 
 // Adds the cells' energy changes of this sweep, in a fixed order, and clears them (a cell
 // without particles writes nothing during the sweep).
@@ -1675,17 +1683,15 @@ __device__ void buildChainProposal(const SweepArgs& a, ChainShared& sh, int cell
 
 // One CTA per active cell of the chain grid: that cell's chain moves in sequence (stages
 // A, B, C as in kColour over (chain particle, candidate) pairs, old and new configuration).
-__global__ void __launch_bounds__(kMoveThreads) kChainColour(const SweepArgs* __restrict__ A, int phase) {
+// The chain moves of chain cell (cx, cy, cz), by the whole CTA (kChainColour: one colour
+// phase; kChainFlow: the dataflow sweep of the chain grid).
+__device__ __forceinline__ void chainCell(const SweepArgs& a, int cx, int cy, int cz) {
     extern __shared__ float4 dynSmem[];
     __shared__ ChainShared sh;
-    const SweepArgs& a = A[blockIdx.y];
     float4* candPos = dynSmem;
     int* candIdx = reinterpret_cast<int*>(candPos + kCandCap);
     const Control& ctl = *a.ctl;
     const Grid& g = a.g;
-    if (a.nChains == 0 || (int)blockIdx.x >= g.nactive || phase >= g.ncolours) return;
-    int cx, cy, cz;
-    decodeActive(g, ctl.perm[phase], blockIdx.x, cx, cy, cz);
     const int cell = (cz * g.nc[1] + cy) * g.nc[0] + cx;
     const int cnt = a.chainCellCount[cell];
     if (cnt > kCellCap && threadIdx.x == 0) atomicOr(a.err, E_CELL_OVERFLOW);
@@ -1888,6 +1894,21 @@ __global__ void __launch_bounds__(kMoveThreads) kChainColour(const SweepArgs* __
         atomicAdd(&a.counters[C_EVAL], nEval);
     }
 }
+
+// One colour phase of the chain grid: CTA blockIdx.x takes active chain cell blockIdx.x.
+__global__ void __launch_bounds__(kMoveThreads, 1) kChainColour(const SweepArgs* __restrict__ A, int phase) {
+    const SweepArgs& a = A[blockIdx.y];
+    const Grid& g = a.g;
+    if (a.nChains == 0 || (int)blockIdx.x >= g.nactive || phase >= g.ncolours) return;
+    int cx, cy, cz;
+    decodeActive(g, a.ctl->perm[phase], blockIdx.x, cx, cy, cz);
+    chainCell(a, cx, cy, cz);
+}
+
+// The chain grid's dataflow sweep: chains centred in cells of one colour are more than
+// maxcut apart whatever they do (cells >= (maxcut + 2 (R + displacement)) / 2), and a chain
+// cell can only interact with chain cells within +-2 cells -- the stencil the flow waits on.
+__global__ void __launch_bounds__(kMoveThreads, 1) kChainFlow(const SweepArgs* __restrict__ A) { flowBody<true>(A); }
 
 // Largest |particle - chain centre| (real space) over all chains, as float bits (>= 0).
 __global__ void kChainExtent(SweepArgs a, const int2* chains, int nChains, unsigned* out) {
@@ -2164,6 +2185,7 @@ struct SweepEngine {
         int* slotOf = nullptr;
         float4* cellPosF = nullptr;
         double* cellDE = nullptr;
+        unsigned* cellDone = nullptr;
         int2* chains = nullptr;
         int nChains = 0;
         int *chStart = nullptr, *chCount = nullptr, *chIdx = nullptr;
@@ -2384,7 +2406,7 @@ static int prepareChains(Context* c, SweepEngine* e, const sc_run_params& p, con
     g.maxcut = c->topo.maxcut + 2.0 * (C.R + p.chainmmx);
     if (g.ncells > C.ncellsAlloc) {
         for (void** q : {(void**)&C.cellStart, (void**)&C.cellCount, (void**)&C.cellCursor, (void**)&C.cellDE,
-                         (void**)&C.chStart, (void**)&C.chCount}) {
+                         (void**)&C.chStart, (void**)&C.chCount, (void**)&C.cellDone}) {
             if (*q) {
                 cudaFree(*q);
                 e->allocs.erase(std::find(e->allocs.begin(), e->allocs.end(), *q));
@@ -2398,7 +2420,9 @@ static int prepareChains(Context* c, SweepEngine* e, const sc_run_params& p, con
         if ((rc = engineAlloc(e, (void**)&C.cellDE, sizeof(double) * m))) return rc;
         if ((rc = engineAlloc(e, (void**)&C.chStart, sizeof(int) * m))) return rc;
         if ((rc = engineAlloc(e, (void**)&C.chCount, sizeof(int) * m))) return rc;
+        if ((rc = engineAlloc(e, (void**)&C.cellDone, sizeof(unsigned) * m))) return rc;
         cudaMemset(C.cellDE, 0, sizeof(double) * m);
+        cudaMemset(C.cellDone, 0, sizeof(unsigned) * m);
         C.ncellsAlloc = m;
     }
     C.g = g;
@@ -2408,6 +2432,7 @@ static int prepareChains(Context* c, SweepEngine* e, const sc_run_params& p, con
     a.ctl = C.ctl;
     a.cellStart = C.cellStart; a.cellCount = C.cellCount; a.cellCursor = C.cellCursor; a.cellIdx = C.cellIdx;
     a.cellOf = C.cellOf; a.cellPosF = C.cellPosF; a.cellDE = C.cellDE;
+    a.cellDone = C.cellDone;
     a.slotOf = C.slotOf;
     a.cellDirF = a.cellPatF = nullptr;
     a.mlp = nullptr;
@@ -2586,6 +2611,9 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
         if ((r = cudaFuncSetAttribute(kChainColour, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDynSmem)) !=
             cudaSuccess)
             return cudaFail(r, "shared memory attribute");
+        if ((r = cudaFuncSetAttribute(kChainFlow, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDynSmem)) !=
+            cudaSuccess)
+            return cudaFail(r, "shared memory attribute");
         attrSet = true;
     }
     auto dims = [&](int x) { return dim3((unsigned)std::max(1, x), (unsigned)ns); };
@@ -2655,10 +2683,15 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
             kBeginSweep<<<dims(1), 32, 0, s>>>(b.dArgsC, 0);
             if ((r2 = launchCellsOf(b.dArgsC, b.maxCellsC)) != cudaSuccess) return r2;
             kChainBin<<<dims(1), 1024, 0, s>>>(b.dArgsC);
-            for (int ph = 0; ph < b.maxColoursC; ++ph)
-                kChainColour<<<dims(b.maxActiveC), kMoveThreads, kDynSmem, s>>>(b.dArgsC, ph);
+            if (flow) {
+                const int ctas = std::max(1, std::min(b.maxColoursC * b.maxActiveC, std::max(1, sms) * 2 / ns));
+                kChainFlow<<<dims(ctas), kMoveThreads, kDynSmem, s>>>(b.dArgsC);
+            } else {
+                for (int ph = 0; ph < b.maxColoursC; ++ph)
+                    kChainColour<<<dims(b.maxActiveC), kMoveThreads, kDynSmem, s>>>(b.dArgsC, ph);
+            }
             kEndSweep<<<dims(1), 256, 0, s>>>(b.dArgsC);
-            launches += 3 + b.maxColoursC;
+            launches += 3 + (flow ? 1 : b.maxColoursC);
         }
         if (volDue) {
             // chain moves left particles outside the cells of this sweep's list: list them anew

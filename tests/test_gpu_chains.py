@@ -90,3 +90,23 @@ def test_chain_moves_with_volume_moves_keep_the_running_energy_exact():
     assert abs(st.energy - e1) <= 1e-9 * max(1.0, abs(e1))
     assert abs(st.energy_check - e1) <= 1e-9 * max(1.0, abs(e1))
     s.close()
+
+
+def test_dataflow_sweeps_give_the_colour_phase_trajectory_with_chains():
+    """Single-particle and chain phases both as dataflow launches: the trajectory of the
+    colour-phase launches, bit for bit."""
+    from sc_gb300 import System, workloads
+
+    texts = workloads.bilayers(10, box=(12.0, 12.0, 40.0), seed=5)
+    s1, s2 = System.from_text(*texts), System.from_text(*texts)
+    a = s1.simulate(nsweeps=30, seed=8, check_every=15, chainprob=0.3, variant=0)
+    b = s2.simulate(nsweeps=30, seed=8, check_every=15, chainprob=0.3, variant=4)
+    assert a.acc_chain > 0 and b.launches < a.launches
+    assert (a.energy, a.acc_trans, a.acc_rot, a.acc_chain, a.rej_chain) == \
+           (b.energy, b.acc_trans, b.acc_rot, b.acc_chain, b.rej_chain)
+    assert all(list(x.pos) == list(y.pos) and list(x.dir) == list(y.dir)
+               for x, y in zip(s1.particles(), s2.particles()))
+    e1 = s2.all_to_all()
+    assert abs(b.energy - e1) <= 1e-9 * max(1.0, abs(e1))
+    s1.close()
+    s2.close()
