@@ -934,10 +934,20 @@ __device__ __forceinline__ void decodeActive(const Grid& g, int colour, int bloc
     cx = ox + g.p[0] * bx; cy = oy + g.p[1] * by; cz = oz + g.p[2] * bz;
 }
 
+// No wait: the colour-phase kernels run a cell when its whole phase may run.
+struct NoWait {
+    __device__ bool operator()() const { return true; }
+};
+
 // The moves of cell (cx, cy, cz), by the whole CTA: the move kernel body, run once per CTA
 // by the colour-phase kernels (kColour / kColourDense) and once per taken cell by the
-// dataflow kernels (kColourFlow / kColourFlowDense).
-__device__ __forceinline__ void moveCell(const SweepArgs& a, int cx, int cy, int cz) {
+// dataflow kernels (kColourFlow / kColourFlowDense).  What reads only static data or this
+// cell's own particles (which no other cell moves) comes first: the cell's list, the
+// stencil's layout and the first move's proposal; then `wait()` (the dataflow kernels wait
+// there for the earlier-phase neighbours; false: give up), then everything that reads the
+// neighbours' particles.
+template <class Wait>
+__device__ __forceinline__ void moveCell(const SweepArgs& a, int cx, int cy, int cz, Wait wait) {
     extern __shared__ float4 dynSmem[];
     __shared__ MoveShared sh;
     float4* candPos = dynSmem;
@@ -954,6 +964,11 @@ __device__ __forceinline__ void moveCell(const SweepArgs& a, int cx, int cy, int
     for (int k = tid; k < cnt; k += kMoveThreads) sh.list[k] = a.cellIdx[a.cellStart[cell] + k];
     if (tid < 4) sh.propFor[tid] = -1;
     stageStencil(a, cx, cy, cz, sh.st, sh.scan);
+    if (warp == 0) buildProposal(a, sh, sh.prop[0], cell, cnt, 0, cx, cy, cz, box);
+    else if (tid == 64) acceptThresholds(a, sh.prop[0], cell, 0);
+    __syncthreads();
+    if (tid == 0) sh.propFor[0] = 0;
+    if (!wait()) return;
     if (sh.st.nCand <= kCandCap) loadCandidates(a, sh.st, 0, sh.st.nCand, candIdx, candPos, candDir, candPat);
     const int nCand = sh.st.nCand;
     const bool resident = nCand <= kCandCap;
@@ -1355,7 +1370,7 @@ __device__ __forceinline__ void colourBody(const SweepArgs* __restrict__ A, int 
     if ((int)blockIdx.x >= g.nactive || phase >= g.ncolours) return;
     int cx, cy, cz;
     decodeActive(g, a.ctl->perm[phase], blockIdx.x, cx, cy, cz);
-    moveCell(a, cx, cy, cz);
+    moveCell(a, cx, cy, cz, NoWait());
 }
 
 // One CTA per active cell of a colour.  Two register budgets of the same code: kColour
@@ -1391,7 +1406,8 @@ __device__ __forceinline__ void storeReleaseGpu(unsigned* p, unsigned v) {
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-__device__ __forceinline__ void chainCell(const SweepArgs& a, int cx, int cy, int cz);
+template <class Wait>
+__device__ __forceinline__ void chainCell(const SweepArgs& a, int cx, int cy, int cz, Wait wait);
 
 template <bool CHAIN>
 __device__ __forceinline__ void flowBody(const SweepArgs* __restrict__ A) {
@@ -1424,35 +1440,38 @@ __device__ __forceinline__ void flowBody(const SweepArgs* __restrict__ A) {
             if (tid == 0) storeReleaseGpu(&a.cellDone[cell], stamp);
             continue;
         }
-        for (int q = tid; q < nn && !*(volatile int*)&sFail; q += kMoveThreads) {
-            int qx = q % nx, qy = (q / nx) % ny, qz = q / (nx * ny);
-            int x = axisCell(cx, qx, g.nc[0], g.s[0]);
-            int y = axisCell(cy, qy, g.nc[1], g.s[1]);
-            int z = axisCell(cz, qz, g.nc[2], g.s[2]);
-            int colour = (x % g.p[0]) + g.p[0] * ((y % g.p[1]) + g.p[1] * (z % g.p[2]));
-            if (posOf[colour] >= phase) continue;
-            const unsigned* f = &a.cellDone[(z * g.nc[1] + y) * g.nc[0] + x];
-            for (int spin = 0; loadAcquireGpu(f) != stamp; ++spin) {
-                if (spin >= kFlowSpin || ((spin & 255) == 255 && (*(volatile int*)a.err & E_FLOW_WAIT))) {
-                    sFail = 1;
-                    break;
+        // the earlier-phase cells of the stencil have finished (false: a wait gave up)
+        auto waitNeighbours = [&]() -> bool {
+            for (int q = tid; q < nn && !*(volatile int*)&sFail; q += kMoveThreads) {
+                int qx = q % nx, qy = (q / nx) % ny, qz = q / (nx * ny);
+                int x = axisCell(cx, qx, g.nc[0], g.s[0]);
+                int y = axisCell(cy, qy, g.nc[1], g.s[1]);
+                int z = axisCell(cz, qz, g.nc[2], g.s[2]);
+                int colour = (x % g.p[0]) + g.p[0] * ((y % g.p[1]) + g.p[1] * (z % g.p[2]));
+                if (posOf[colour] >= phase) continue;
+                const unsigned* f = &a.cellDone[(z * g.nc[1] + y) * g.nc[0] + x];
+                for (int spin = 0; loadAcquireGpu(f) != stamp; ++spin) {
+                    if (spin >= kFlowSpin || ((spin & 255) == 255 && (*(volatile int*)a.err & E_FLOW_WAIT))) {
+                        sFail = 1;
+                        break;
+                    }
+                    __nanosleep(64);
                 }
-                __nanosleep(64);
             }
-        }
+            __syncthreads();
+            __threadfence();        // every thread reads the neighbours' states after the waits
+            return !sFail;
+        };
+        if (CHAIN) chainCell(a, cx, cy, cz, waitNeighbours);
+        else moveCell(a, cx, cy, cz, waitNeighbours);
         __syncthreads();
         if (sFail) {
             if (tid == 0) atomicOr(a.err, E_FLOW_WAIT);
             break;
         }
-        __threadfence();            // every thread reads the neighbours' states after the waits
-        if (CHAIN) chainCell(a, cx, cy, cz);
-        else moveCell(a, cx, cy, cz);
-        __syncthreads();            // the cell's state writes (thread 0) are issued
-        if (tid == 0) {
-            __threadfence();
-            storeReleaseGpu(&a.cellDone[cell], stamp);
-        }
+        __threadfence();            // each thread's state writes are visible GPU-wide ...
+        __syncthreads();
+        if (tid == 0) storeReleaseGpu(&a.cellDone[cell], stamp);     // ... before the flag
     }
 }
 
@@ -1684,8 +1703,10 @@ __device__ void buildChainProposal(const SweepArgs& a, ChainShared& sh, int cell
 // One CTA per active cell of the chain grid: that cell's chain moves in sequence (stages
 // A, B, C as in kColour over (chain particle, candidate) pairs, old and new configuration).
 // The chain moves of chain cell (cx, cy, cz), by the whole CTA (kChainColour: one colour
-// phase; kChainFlow: the dataflow sweep of the chain grid).
-__device__ __forceinline__ void chainCell(const SweepArgs& a, int cx, int cy, int cz) {
+// phase; kChainFlow: the dataflow sweep of the chain grid, which waits in `wait()` after the
+// static layout is staged; false: give up).
+template <class Wait>
+__device__ __forceinline__ void chainCell(const SweepArgs& a, int cx, int cy, int cz, Wait wait) {
     extern __shared__ float4 dynSmem[];
     __shared__ ChainShared sh;
     float4* candPos = dynSmem;
@@ -1705,6 +1726,7 @@ __device__ __forceinline__ void chainCell(const SweepArgs& a, int cx, int cy, in
     if (moves == 0) return;
     for (int k = tid; k < cnt; k += kMoveThreads) sh.list[k] = a.chainCellIdx[a.chainCellStart[cell] + k];
     stageStencil(a, cx, cy, cz, sh.st, sh.scan);
+    if (!wait()) return;
     const int nCand = sh.st.nCand;
     const bool resident = nCand <= kCandCap;
     if (resident) loadCandidates(a, sh.st, 0, nCand, candIdx, candPos);
@@ -1902,7 +1924,7 @@ __global__ void __launch_bounds__(kMoveThreads, 1) kChainColour(const SweepArgs*
     if (a.nChains == 0 || (int)blockIdx.x >= g.nactive || phase >= g.ncolours) return;
     int cx, cy, cz;
     decodeActive(g, a.ctl->perm[phase], blockIdx.x, cx, cy, cz);
-    chainCell(a, cx, cy, cz);
+    chainCell(a, cx, cy, cz, NoWait());
 }
 
 // The chain grid's dataflow sweep: chains centred in cells of one colour are more than
