@@ -335,7 +335,8 @@ struct Scan {
     int nbTot[kWarps];
 };
 
-// Exclusive scan of v over the block; returns the offset and the total.
+// Exclusive scan of v over the block of NT threads; returns the offset and the total.
+template <int NT = kMoveThreads>
 __device__ __forceinline__ int blockExclusiveScan(int v, int& total, Scan& sh) {
     int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     int incl = v;
@@ -344,12 +345,16 @@ __device__ __forceinline__ int blockExclusiveScan(int v, int& total, Scan& sh) {
         int t = __shfl_up_sync(0xffffffffu, incl, o);
         if (lane >= o) incl += t;
     }
+    if (NT == 32) {                 // one warp: no shared memory, no barrier
+        total = __shfl_sync(0xffffffffu, incl, 31);
+        return incl - v;
+    }
     if (lane == 31) sh.warpTot[w] = incl;
     __syncthreads();
     int woff = 0;
     total = 0;
 #pragma unroll
-    for (int q = 0; q < kWarps; ++q) {
+    for (int q = 0; q < NT / 32; ++q) {
         int t = sh.warpTot[q];
         if (q < w) woff += t;
         total += t;
@@ -404,7 +409,8 @@ struct Stencil {
 };
 
 // The stencil of cell (cx, cy, cz): its cells and their offsets in the concatenated
-// candidate list (cells in stencil order, particles in cell-list order).
+// candidate list (cells in stencil order, particles in cell-list order); NT threads.
+template <int NT = kMoveThreads>
 __device__ void stageStencil(const SweepArgs& a, int cx, int cy, int cz, Stencil& st, Scan& sc) {
     const Grid& g = a.g;
     const int nx = axisCount(g.nc[0], g.s[0]), ny = axisCount(g.nc[1], g.s[1]), nz = axisCount(g.nc[2], g.s[2]);
@@ -414,7 +420,7 @@ __device__ void stageStencil(const SweepArgs& a, int cx, int cy, int cz, Stencil
     const int ownZ = g.nc[2] <= 2 * g.s[2] ? cz : g.s[2];
     const int ownQ = (ownZ * ny + ownY) * nx + own;
     int carry = 0;
-    for (int base = 0; base < nn; base += kMoveThreads) {
+    for (int base = 0; base < nn; base += NT) {
         int q = base + threadIdx.x;
         int cnt = 0, cell = 0;
         if (q < nn) {
@@ -426,7 +432,7 @@ __device__ void stageStencil(const SweepArgs& a, int cx, int cy, int cz, Stencil
             cnt = a.cellCount[cell];
         }
         int total;
-        int off = blockExclusiveScan(cnt, total, sc);
+        int off = blockExclusiveScan<NT>(cnt, total, sc);
         if (q < nn) {
             st.nbCell[q] = cell;
             st.nbOff[q] = carry + off;
@@ -444,11 +450,12 @@ __device__ void stageStencil(const SweepArgs& a, int cx, int cy, int cz, Stencil
 }
 
 // Loads candidates [first, first + count) of the stencil into shared memory (count <=
-// kCandCap).  A stencil larger than the buffer is processed in windows of kCandCap.
+// kCandCap).  A stencil larger than the buffer is processed in windows of kCandCap.  NT threads.
+template <int NT = kMoveThreads>
 __device__ void loadCandidates(const SweepArgs& a, const Stencil& st, int first, int count, int* candIdx,
                                float4* candPos, float4* candDir = nullptr, float4* candPat = nullptr) {
     const int nn = st.nNb;
-    for (int kk = threadIdx.x; kk < count; kk += kMoveThreads) {
+    for (int kk = threadIdx.x; kk < count; kk += NT) {
         int k = first + kk;
         int lo = 0, hi = nn - 1;      // last q with nbOff[q] <= k
         while (lo < hi) {
@@ -1947,22 +1954,29 @@ __global__ void kChainExtent(SweepArgs a, const int2* chains, int nChains, unsig
     atomicMax(out, __float_as_uint((float)m));
 }
 
+// The cell-energy kernel runs one warp per cell (many cells in flight per SM: a cell holds
+// a few particles and a few pairs in range, so the staging latency, not the arithmetic,
+// sets its time), with candidate windows of kCellCandCap and queues of kCellQueueCap.
+constexpr int kCellThreads = 32;
+constexpr int kCellCandCap = 256;
+constexpr int kCellQueueCap = 512;
+constexpr size_t kDynSmemCell = (size_t)kCellCandCap * (sizeof(float4) + sizeof(int));
+
 struct CellShared {
     int list[kCellCap];
-    int queueA[kQueueCap];
-    int queueB[kQueueCap];
+    int queueA[kCellQueueCap];
+    int queueB[kCellQueueCap];
     Stencil st;
     Scan scan;
-    double red[kWarps][2];
 };
 
 // Total energy over the cell list, one CTA per cell: PairE(i, j, conlist(i)) for every
 // particle i of the cell and j < i (allToAll's pair orientation,
 // totalenergycalculator.h:502-521), with the same A/B/C stages as the move kernel.
-__global__ void __launch_bounds__(kMoveThreads) kCellEnergy(const SweepArgs* __restrict__ A, int useTrialBox) {
+__global__ void __launch_bounds__(kCellThreads) kCellEnergy(const SweepArgs* __restrict__ A, int useTrialBox) {
     extern __shared__ float4 dynSmem[];
     float4* candPos = dynSmem;
-    int* candIdx = reinterpret_cast<int*>(candPos + kCandCap);
+    int* candIdx = reinterpret_cast<int*>(candPos + kCellCandCap);
     __shared__ CellShared sh;
     const SweepArgs& a = A[blockIdx.y];
     const Control& ctl = *a.ctl;
@@ -1981,17 +1995,17 @@ __global__ void __launch_bounds__(kMoveThreads) kCellEnergy(const SweepArgs* __r
     }
     int cx = cell % g.nc[0], cy = (cell / g.nc[0]) % g.nc[1], cz = cell / (g.nc[0] * g.nc[1]);
     const int own0 = a.cellStart[cell];
-    for (int k = tid; k < cnt; k += kMoveThreads) sh.list[k] = a.cellIdx[own0 + k];
-    stageStencil(a, cx, cy, cz, sh.st, sh.scan);
+    for (int k = tid; k < cnt; k += kCellThreads) sh.list[k] = a.cellIdx[own0 + k];
+    stageStencil<kCellThreads>(a, cx, cy, cz, sh.st, sh.scan);
     const int nCand = sh.st.nCand;
     DevCtx c;
     c.params = a.t.params; c.mols = a.t.mols; c.ntypes = a.t.ntypes; c.n = a.s.n; c.sqmaxcut = a.t.sqmaxcut;
     const double* bx = useTrialBox ? ctl.trialBox : a.s.box;
     const double3 box = mk(bx[0], bx[1], bx[2]);
     const float thr32 = candThreshold(c.sqmaxcut, box);
-    double sum = 0.0, unused = 0.0;
+    double sum = 0.0;
     // bonded partners j < i, whatever the distance
-    for (int k = tid; k < cnt; k += kMoveThreads) {
+    for (int k = tid; k < cnt; k += kCellThreads) {
         int i = sh.list[k];
         Con con = makeCon(c, i, a.s.mol[i]);
         PView vi = viewAt(a.s, i);
@@ -2006,7 +2020,7 @@ __global__ void __launch_bounds__(kMoveThreads) kCellEnergy(const SweepArgs* __r
     int qb = 0, wlen = 0;
     auto flushC = [&](int count) {
         __syncthreads();                   // queue entries of every thread are visible
-        for (int e = tid; e < count; e += kMoveThreads) {
+        for (int e = tid; e < count; e += kCellThreads) {
             int q = sh.queueB[e];
             int i = sh.list[q / wlen], j = candIdx[q % wlen];
             Con con = makeCon(c, i, a.s.mol[i]);
@@ -2015,15 +2029,15 @@ __global__ void __launch_bounds__(kMoveThreads) kCellEnergy(const SweepArgs* __r
         }
         __syncthreads();
     };
-    for (int wbase = 0; wbase < nCand; wbase += kCandCap) {
-      // the candidates in windows of kCandCap; pair q = (own particle li, window slot k)
-      wlen = min(kCandCap, nCand - wbase);
-      loadCandidates(a, sh.st, wbase, wlen, candIdx, candPos);
+    for (int wbase = 0; wbase < nCand; wbase += kCellCandCap) {
+      // the candidates in windows of kCellCandCap; pair q = (own particle li, window slot k)
+      wlen = min(kCellCandCap, nCand - wbase);
+      loadCandidates<kCellThreads>(a, sh.st, wbase, wlen, candIdx, candPos);
       const int total = cnt * wlen;
       for (int base = 0; base < total; base += kChunk) {
         int qa = 0;
         int end = min(base + kChunk, total);
-        for (int r0 = base; r0 < end; r0 += kMoveThreads) {
+        for (int r0 = base; r0 < end; r0 += kCellThreads) {
             int q = r0 + tid;
             int keep = 0;
             if (q < end) {
@@ -2035,12 +2049,12 @@ __global__ void __launch_bounds__(kMoveThreads) kCellEnergy(const SweepArgs* __r
                 }
             }
             int tot;
-            int off = blockExclusiveScan(keep, tot, sh.scan);
+            int off = blockExclusiveScan<kCellThreads>(keep, tot, sh.scan);
             if (keep) sh.queueA[qa + off] = q;
             qa += tot;
         }
         __syncthreads();
-        for (int e0 = 0; e0 < qa; e0 += kMoveThreads) {
+        for (int e0 = 0; e0 < qa; e0 += kCellThreads) {
             int e = e0 + tid;
             int keep = 0, q = 0;
             if (e < qa) {
@@ -2060,16 +2074,17 @@ __global__ void __launch_bounds__(kMoveThreads) kCellEnergy(const SweepArgs* __r
                 }
             }
             int tot;
-            int off = blockExclusiveScan(keep, tot, sh.scan);
+            int off = blockExclusiveScan<kCellThreads>(keep, tot, sh.scan);
             if (keep) sh.queueB[qb + off] = q;
             qb += tot;
-            if (qb > kQueueCap - kMoveThreads) { flushC(qb); qb = 0; }
+            if (qb > kCellQueueCap - kCellThreads) { flushC(qb); qb = 0; }
         }
       }
       flushC(qb);           // queue entries index the window
       qb = 0;
     }
-    blockSum2(sum, unused, sh.red);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);     // fixed order
     if (tid == 0) a.partial[cell] = sum;
 }
 
@@ -2628,7 +2643,8 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
         if ((r = cudaFuncSetAttribute(kColourFlowDense, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)kDynSmemSurrogate)) != cudaSuccess)
             return cudaFail(r, "shared memory attribute");
-        if ((r = cudaFuncSetAttribute(kCellEnergy, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDynSmem)) != cudaSuccess)
+        if ((r = cudaFuncSetAttribute(kCellEnergy, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDynSmemCell)) !=
+            cudaSuccess)
             return cudaFail(r, "shared memory attribute");
         if ((r = cudaFuncSetAttribute(kChainColour, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDynSmem)) !=
             cudaSuccess)
@@ -2661,7 +2677,7 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
     };
     auto launchCells = [&]() -> cudaError_t { return launchCellsOf(b.dArgs, b.maxCells); };
     auto exactEnergy = [&](bool check) -> cudaError_t {
-        kCellEnergy<<<dims(b.maxCells), kMoveThreads, kDynSmem, s>>>(b.dArgs, 0);
+        kCellEnergy<<<dims(b.maxCells), kCellThreads, kDynSmemCell, s>>>(b.dArgs, 0);
         if (check) kCheckEnergy<<<dims(1), 256, 0, s>>>(b.dArgs);
         else kSetEnergy<<<dims(1), 256, 0, s>>>(b.dArgs);
         launches += 2;
@@ -2718,7 +2734,7 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
         if (volDue) {
             // chain moves left particles outside the cells of this sweep's list: list them anew
             if (b.chains && (r2 = launchCells()) != cudaSuccess) return r2;
-            kCellEnergy<<<dims(b.maxCells), kMoveThreads, kDynSmem, s>>>(b.dArgs, 1);
+            kCellEnergy<<<dims(b.maxCells), kCellThreads, kDynSmemCell, s>>>(b.dArgs, 1);
             kVolumeAccept<<<dims(1), 256, 0, s>>>(b.dArgs);
             launches += 2;
         }
