@@ -490,9 +490,9 @@ def main():
     p.stencil, p.variant = best[0], best[1]
     # warm-up
     s.simulate(p, nsweeps=max(3, a.warmup))
-    # kernel-level timing of the move kernels and pair counters (separate short run)
-    prof = s.simulate(p, nsweeps=5, time_phases=1)
-    p.time_phases = 0
+    # the timed sweeps also time their move launches with CUDA events on the library's
+    # stream (recorded around the launches, read after each sweep: no synchronisation inside)
+    p.time_phases = 1
     clocks = Clocks(local)
     if dist:
         dist.barrier()
@@ -503,6 +503,7 @@ def main():
     launches = 0
     tested = evaluated = 0
     acc = 0
+    phase_s, phase_n = 0.0, 0
     for k in range(a.steps):
         l2_flush()
         st = s.simulate(p, nsweeps=1)
@@ -512,6 +513,9 @@ def main():
         tested += st.pairs_tested
         evaluated += st.pairs_evaluated
         acc += st.acc_trans + st.acc_rot
+        phase_s += st.phase_seconds
+        phase_n += st.phase_launches
+    p.time_phases = 0
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
@@ -541,8 +545,8 @@ def main():
     peaks, peak_kind = measured_peaks()
     # algorithmic bytes of the move kernel: 28 B (position + type) per candidate pair tested
     # (old and new configuration), 24 B axis + 96 B patch vectors per pair evaluated
-    bytes_per_launch = (prof.pairs_tested * 28 + prof.pairs_evaluated * 120) / max(1, prof.phase_launches)
-    t_launch = prof.phase_seconds / max(1, prof.phase_launches)
+    bytes_per_launch = (tested * 28 + evaluated * 120) / max(1, phase_n)
+    t_launch = phase_s / max(1, phase_n)
     achieved = bytes_per_launch / t_launch / 1e9 if t_launch > 0 else None
     kernel = ["kColour", "kColourDense", None, None, "kColourFlow", "kColourFlowDense"][int(p.variant) & 5]
     roof = {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
@@ -552,7 +556,7 @@ def main():
             "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
             "avg_launch_us": t_launch * 1e6, "algorithmic_bytes_per_launch": bytes_per_launch,
             "note": "the move kernel is FP64-latency bound; see fp64 for its arithmetic rate"}
-    flops_per_launch = (prof.pairs_tested * 17 + prof.pairs_evaluated * 600) / max(1, prof.phase_launches)
+    flops_per_launch = (tested * 17 + evaluated * 600) / max(1, phase_n)
     fp64 = {"achieved_tflops": flops_per_launch / t_launch / 1e12 if t_launch > 0 else None,
             "peak_tflops_nominal": 1.25,
             "note": "17 FP64 ops per candidate pair (image + r^2), ~600 per evaluated pair (estimate from the kernel "

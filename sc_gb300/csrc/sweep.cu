@@ -2247,9 +2247,10 @@ struct Batch {
     int maxCellsC = 0, maxActiveC = 0, maxColoursC = 0;
     cudaStream_t stream = nullptr;
     int device = 0;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr, evP0 = nullptr, evP1 = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<cudaEvent_t> evPhase;     // time_phases: start / end of each sweep's move launches
     cudaGraphExec_t graph = nullptr;
-    int graphDims[12] = {0};   // launch shape the graph was captured with
+    int graphDims[13] = {0};   // launch shape the graph was captured with
     long graphLaunches = 0, graphPhaseLaunches = 0;
     // parallel tempering
     int* dLadder = nullptr;
@@ -2261,8 +2262,9 @@ struct Batch {
     ~Batch() {
         cudaSetDevice(device);
         for (void* p : allocs) cudaFree(p);
-        for (cudaEvent_t e : {ev0, ev1, evP0, evP1})
+        for (cudaEvent_t e : {ev0, ev1})
             if (e) cudaEventDestroy(e);
+        for (cudaEvent_t e : evPhase) cudaEventDestroy(e);
         if (graph) cudaGraphExecDestroy(graph);
     }
     int alloc(void** p, size_t bytes) {
@@ -2627,7 +2629,18 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
     double phaseMs = 0;
     long phaseLaunches = 0;
     if (!b.ev0) {
-        cudaEventCreate(&b.ev0); cudaEventCreate(&b.ev1); cudaEventCreate(&b.evP0); cudaEventCreate(&b.evP1);
+        cudaEventCreate(&b.ev0); cudaEventCreate(&b.ev1);
+    }
+    // time_phases: one pair of events per sweep, read after the run (no synchronisation
+    // inside the sweeps, so the timed launches run as they would untimed)
+    int phaseEvents = 0;
+    if (p.time_phases) {
+        const size_t want = 2 * (size_t)std::min<long>(nsweeps, 4096);
+        while (b.evPhase.size() < want) {
+            cudaEvent_t e;
+            if ((r = cudaEventCreate(&e)) != cudaSuccess) return cudaFail(r, "phase events");
+            b.evPhase.push_back(e);
+        }
     }
     static bool attrSet = false;
     if (!attrSet) {
@@ -2697,7 +2710,8 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
         kBeginSweep<<<dims(1), 32, 0, s>>>(b.dArgs, volDue ? 1 : 0);
         cudaError_t r2 = launchCells();
         if (r2 != cudaSuccess) return r2;
-        if (timing) cudaEventRecord(b.evP0, s);
+        const bool timed = timing && 2 * phaseEvents + 1 < (int)b.evPhase.size();
+        if (timed) cudaEventRecord(b.evPhase[2 * phaseEvents], s);
         if (flow) {
             if (dense) kColourFlowDense<<<dims(flowCtas), kMoveThreads, colourSmem, s>>>(b.dArgs);
             else kColourFlow<<<dims(flowCtas), kMoveThreads, colourSmem, s>>>(b.dArgs);
@@ -2707,14 +2721,11 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
                 else kColour<<<dims(b.maxActive), kMoveThreads, colourSmem, s>>>(b.dArgs, ph);
             }
         }
-        if (timing) {
-            cudaEventRecord(b.evP1, s);
-            cudaEventSynchronize(b.evP1);
-            float pms = 0;
-            cudaEventElapsedTime(&pms, b.evP0, b.evP1);
-            phaseMs += pms;
+        if (timed) {
+            cudaEventRecord(b.evPhase[2 * phaseEvents + 1], s);
+            ++phaseEvents;
         }
-        phaseLaunches += flow ? 1 : b.maxColours;
+        if (timed || !timing) phaseLaunches += flow ? 1 : b.maxColours;
         kEndSweep<<<dims(1), 256, 0, s>>>(b.dArgs);
         launches += 2 + (flow ? 1 : b.maxColours);
         if (b.chains) {       // chain moves: their own grid, colours and cell list
@@ -2757,8 +2768,8 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
         long left = nsweeps - sw;
         bool aligned = (sw % G == 0) && (nextExchange < 0 || nextExchange - sw >= G);
         if (useGraph && left >= G && aligned) {
-            int key[12] = {ns, b.maxN, b.maxCells, b.maxActive, b.maxColours, (int)G, anySurrogate ? 1 : 0,
-                           b.chains ? 1 : 0, b.maxCellsC, b.maxActiveC, b.maxColoursC, dense ? 1 : 0};
+            int key[13] = {ns, b.maxN, b.maxCells, b.maxActive, b.maxColours, (int)G, anySurrogate ? 1 : 0,
+                           b.chains ? 1 : 0, b.maxCellsC, b.maxActiveC, b.maxColoursC, dense ? 1 : 0, flow ? 1 : 0};
             if (!b.graph || std::memcmp(key, b.graphDims, sizeof key) != 0) {
                 if (b.graph) { cudaGraphExecDestroy(b.graph); b.graph = nullptr; }
                 cudaGraph_t graph;
@@ -2838,6 +2849,11 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
     float ms = 0;
     cudaEventElapsedTime(&ms, b.ev0, b.ev1);
     out.seconds = ms * 1e-3;
+    for (int k = 0; k < phaseEvents; ++k) {
+        float pms = 0;
+        cudaEventElapsedTime(&pms, b.evPhase[2 * k], b.evPhase[2 * k + 1]);
+        phaseMs += pms;
+    }
     out.phaseSeconds = phaseMs * 1e-3;
     out.launches = launches;
     out.phaseLaunches = phaseLaunches;
