@@ -47,7 +47,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
-    ap.add_argument("--only", default="all", choices=["all", "main", "replicas", "surrogate", "bilayer"],
+    ap.add_argument("--only", default="all", choices=["all", "main", "replicas", "surrogate", "bilayer", "wl"],
                     help="run one section alone (prints that section's JSON)")
     return ap.parse_args()
 
@@ -432,15 +432,58 @@ def bench_bilayer(steps, seed=1, warm=20):
             "running_energy_error": drift, "launches": launches}
 
 
+def bench_wl(steps, seed=1, warm=20):
+    """Wang-Landau (WangLandau, scOOP/mc/wanglandau.h): a CPSC particle above a bilayer of
+    800 three-bead lipids (2401 particles, chain moves on) with adaptive weights over its
+    height relative to the system centre and its axis z component (options wlm = 1 3, the
+    reference's membrane example), against the same system without the bias; device-timed,
+    L2 flushed between one-sweep steps."""
+    import torch
+
+    from sc_gb300 import System, workloads
+
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    out = {"workload": "protein_bilayer_2401", "particles": 2401, "order_parameters": [1, 3], "sweeps_timed": steps}
+    for key, wlm in (("plain", (0, 0)), ("wang_landau", (1, 3))):
+        opts, top, cfg, wl = workloads.protein_bilayer(seed=seed, wlm=wlm)
+        s = System.from_text(opts, top, cfg)
+        if wlm[0]:
+            s.wl_load(text=wl)
+        p = s.default_run()
+        p.check_every = 0
+        p.seed = seed
+        s.simulate(p, nsweeps=warm)
+        dev = 0.0
+        moves = launches = 0
+        for _ in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            st = s.simulate(p, nsweeps=1)
+            dev += st.seconds
+            moves += st.moves + st.acc_chain + st.rej_chain
+            launches += st.launches
+        out[key + "_moves_per_s"] = moves / dev
+        out[key + "_ms_per_sweep"] = 1e3 * dev / steps
+        if wlm[0]:
+            i = s.wl_info()
+            out["alpha"] = i.alpha
+            out["bins"] = [i.currorder[0], i.currorder[1]]
+            out["launches_per_sweep"] = launches / steps
+        s.close()
+    out["wl_cost"] = out["plain_moves_per_s"] / out["wang_landau_moves_per_s"]
+    return out
+
+
 def main():
     a = parse()
     rank, world, local = dist_info()
     if a.impl == "reference":
         run_reference(a, rank, world)
         return
-    if a.only in ("replicas", "surrogate", "bilayer"):
+    if a.only in ("replicas", "surrogate", "bilayer", "wl"):
         if rank == 0:
-            fn = {"replicas": bench_replicas, "surrogate": bench_surrogate, "bilayer": bench_bilayer}[a.only]
+            fn = {"replicas": bench_replicas, "surrogate": bench_surrogate, "bilayer": bench_bilayer,
+                  "wl": bench_wl}[a.only]
             print(json.dumps({a.only: fn(200 if a.only == "replicas" else a.steps, seed=a.seed)}), flush=True)
         return
     import numpy as np
@@ -576,7 +619,7 @@ def main():
         except Exception as ex:  # the baseline is reported, not required
             cpu = {"value": None, "unit": UNIT, "cores": 1, "kind": "port", "sample": f"failed: {ex}"}
 
-    replicas = surrogate = bilayer = None
+    replicas = surrogate = bilayer = wang_landau = None
     if rank == 0 and a.only == "all" and not a.no_e2e:
         try:
             replicas = bench_replicas(200, seed=a.seed)
@@ -590,6 +633,10 @@ def main():
             bilayer = bench_bilayer(max(5, a.steps // 2), seed=a.seed)
         except Exception as ex:
             bilayer = {"error": str(ex)}
+        try:
+            wang_landau = bench_wl(max(5, a.steps // 2), seed=a.seed)
+        except Exception as ex:
+            wang_landau = {"error": str(ex)}
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
                 "warmup": a.warmup, "ms_per_step": 1e3 * t_max / a.steps, "higher_is_better": True,
@@ -600,6 +647,7 @@ def main():
                            "seed": a.seed, "plain_fp64": True},
                 "clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roof, "fp64": fp64,
                 "cpu_baseline": cpu, "replicas": replicas, "surrogate": surrogate, "bilayer": bilayer,
+                "wang_landau": wang_landau,
                 "detail": {"acceptance": acc / max(1, moves), "pairs_tested_per_move": tested / max(1, moves),
                            "pairs_evaluated_per_move": evaluated / max(1, moves)}}
         print(json.dumps(line), flush=True)

@@ -188,6 +188,41 @@ int sc_trial_volume(sc_context* ctx, double psch, double* e_new);
 int sc_default_run(const sc_context* ctx, sc_run_params* p);
 int sc_simulate(sc_context* ctx, const sc_run_params* p, sc_run_stats* stats);
 
+/* --- Wang-Landau flat-histogram sampling --------------------------------------------------
+ * WangLandau (scOOP/mc/wanglandau.h:16-690, wanglandau.cpp): with options wlm > 0 every move
+ * is biased by the weights of one or two order parameters, the visited bin's weight drops
+ * by alpha after every move, and every 1000 sweeps alpha is halved once the histogram is
+ * flat (the run ends when alpha falls below 1e-8).  Supported order parameters (options wlm):
+ * 1 z of particle 0 relative to the system's volume-weighted centre, 3 z component of
+ * particle 0's axis, 4 xy distance of particles 0 and 1, 8 / 9 box length in x / y.
+ * sc_simulate applies the bias once weights are loaded; with wlm > 0 and none loaded it
+ * returns SC_ERR_STATE (the reference stops without wl.dat).  sc_open loads wl.dat from
+ * the options file's directory when it exists. */
+typedef struct {
+    int dim;                 /* order parameters (1 or 2) */
+    int wlm[2];
+    int length[2];           /* bins; length[1] = 0 for one order parameter, as the reference */
+    int converged;           /* a flatness check found alpha below 1e-8: the run stops there */
+    double minorder[2], dorder[2];
+    double alpha;
+    long currorder[2];       /* current bins */
+    long updates;            /* alpha halvings so far */
+    double syscm[3];         /* system centre (box fractions) the order 1 bin is measured from */
+} sc_wl_info;
+/* WangLandau::initCalc + init (wanglandau.cpp:49-137, 168-299): reads the weights file (alpha,
+ * then "order weight hist" or "order0 order1 weight hist" lines) and computes the starting
+ * bins; a starting bin outside the file's range is SC_ERR_RANGE. */
+int sc_wl_load(sc_context* ctx, const char* path);
+int sc_wl_load_text(sc_context* ctx, const char* text);
+int sc_wl_get_info(sc_context* ctx, sc_wl_info* out);
+/* Current weights and histogram, length[0] * max(1, length[1]) entries each (either may be NULL). */
+int sc_wl_get(sc_context* ctx, double* weights, long* hist);
+/* WangLandau::write (wanglandau.cpp:139-166): the weights file format. */
+int sc_wl_write(sc_context* ctx, const char* path);
+/* WangLandau::endWangLandau (wanglandau.cpp:404-433): shifts 2-D weights by the first bin's
+ * (its loop leaves 1-D weights as they are) and writes the file. */
+int sc_wl_end(sc_context* ctx, const char* path);
+
 /* --- parallel tempering: replicas moved together ------------------------------------------
  * The reference runs one replica per MPI rank and exchanges temperatures in
  * MoveCreator::replicaExchangeMove (scOOP/mc/movecreator.cpp:552-795).  Here all replicas

@@ -30,6 +30,7 @@
 #include <vector>
 
 #include "mc/inicializer.h"
+#include "mc/wanglandau.h"
 #include "mc/paire.h"
 #include "mc/randomGenerator.h"
 
@@ -391,6 +392,32 @@ int main(int argc, char** argv) {
         conf.pvec[target] = orig;
     }
     fprintf(out, "],\n");
+
+    // Wang-Landau: the reference's own WangLandau::init on this configuration (starting
+    // bins, system centre) and WangLandau::write of the weights it read (wanglandau.cpp).
+    if (sim.wlm[0] > 0 && access(files.wlinfile, R_OK) == 0) {
+        fflush(stdout);
+        int keep = dup(1);
+        dup2(2, 1);
+        WangLandau wl(&conf, &sim);
+        wl.init(files.wlinfile);
+        wl.write((char*)"wl-ref-written.dat");
+        fflush(stdout);
+        dup2(keep, 1);
+        fprintf(out, "\"wl\": {\"currorder\": [%ld, %ld], \"length\": [%ld, %ld], \"alpha\": %s, ", wl.currorder[0],
+                wl.currorder[1], wl.length[0], wl.length[1], J(wl.alpha));
+        fprintf(out, "\"minorder\": [%s, %s], \"dorder\": [%s, %s], \"sysvolume\": %s, ", J(wl.minorder[0]),
+                J(wl.minorder[1]), J(wl.dorder[0]), J(wl.dorder[1]), J(conf.sysvolume));
+        pv("syscm", conf.syscm);
+        fprintf(out, "\"written\": \"");
+        FILE* wf = fopen("wl-ref-written.dat", "r");
+        for (int ch; wf && (ch = fgetc(wf)) != EOF;) {
+            if (ch == '\n') fprintf(out, "\\n");
+            else fputc(ch, out);
+        }
+        if (wf) fclose(wf);
+        fprintf(out, "\"},\n");
+    }
 
     // Isotropic volume trials: box edges += psch (movecreator.cpp:390-421).
     fprintf(out, "\"volume_trials\": [");

@@ -1007,3 +1007,43 @@ finish:
     st->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return 0;
 }
+
+// ---- Wang-Landau order parameters --------------------------------------------------------
+// WangLandau::init (scOOP/mc/wanglandau.cpp:49-137): the starting bin of each order
+// parameter.  Order 1: Conf::massCenter (scOOP/structures/Conf.cpp:78-95) over the
+// anInt-wrapped positions weighted by the Ia_param volumes, then zOrder
+// (wanglandau.h:551-554); 3: zOrient (:321-324, floor); 4: twoPartDist (:395-398); 8 / 9:
+// the box lengths (:375-382).  Returns -1 for an order parameter outside {1, 3, 4, 8, 9}.
+extern "C" int or_wl_orders(const or_system* s, const int wlm[2], const double minorder[2], const double dorder[2],
+                            long out[2], double syscm[3], double* sysvolume) {
+    double sv = 0.0;
+    for (int i = 0; i < s->n; ++i) sv += s->params[s->p[i].type * OR_MAXT + s->p[i].type].volume;
+    or_vec cm = V(0, 0, 0);
+    for (int i = 0; i < s->n; ++i) {
+        const double v = s->params[s->p[i].type * OR_MAXT + s->p[i].type].volume;
+        const or_vec& r = s->p[i].pos;
+        cm.x += (r.x - anint(r.x)) * v;
+        cm.y += (r.y - anint(r.y)) * v;
+        cm.z += (r.z - anint(r.z)) * v;
+    }
+    cm.x /= sv; cm.y /= sv; cm.z /= sv;
+    syscm[0] = cm.x; syscm[1] = cm.y; syscm[2] = cm.z;
+    *sysvolume = sv;
+    out[0] = out[1] = 0;
+    for (int k = 0; k < 2; ++k) {
+        if (wlm[k] == 0) continue;
+        switch (wlm[k]) {
+        case 1: out[k] = (long)std::ceil(((s->p[0].pos.z - cm.z) * s->box[2] - minorder[k]) / dorder[k]); break;
+        case 3: out[k] = (long)std::floor((s->p[0].dir.z - minorder[k]) / dorder[k]); break;
+        case 4: {
+            or_vec r = image(s->p[0].pos, s->p[1].pos, s->box);
+            out[k] = (long)std::ceil((std::sqrt(r.x * r.x + r.y * r.y) - minorder[k]) / dorder[k]);
+            break;
+        }
+        case 8: out[k] = (long)std::ceil((s->box[0] - minorder[k]) / dorder[k]); break;
+        case 9: out[k] = (long)std::ceil((s->box[1] - minorder[k]) / dorder[k]); break;
+        default: return -1;
+        }
+    }
+    return 0;
+}

@@ -107,6 +107,11 @@ typedef struct {
 
 int or_mc_run(or_system* s, const or_mc_opts* o, or_mc_stats* st);
 
+/* Wang-Landau starting bins (WangLandau::init, scOOP/mc/wanglandau.cpp:49-137) of order
+ * parameters 1, 3, 4, 8, 9, with the system centre and sysvolume they use. */
+int or_wl_orders(const or_system* s, const int wlm[2], const double minorder[2], const double dorder[2], long out[2],
+                 double syscm[3], double* sysvolume);
+
 #ifdef __cplusplus
 }
 #endif

@@ -67,6 +67,12 @@ class TrainStats(C.Structure):
                 ("seconds", C.c_double)]
 
 
+class WlInfo(C.Structure):
+    _fields_ = [("dim", C.c_int), ("wlm", C.c_int * 2), ("length", C.c_int * 2), ("converged", C.c_int),
+                ("minorder", C.c_double * 2), ("dorder", C.c_double * 2), ("alpha", C.c_double),
+                ("currorder", C.c_long * 2), ("updates", C.c_long), ("syscm", C.c_double * 3)]
+
+
 # (name, restype, argtypes) for every entry point of include/sc_gb300.h
 _P = C.c_void_p
 _D = C.POINTER(C.c_double)
@@ -100,6 +106,12 @@ SIGNATURES = [
     ("sc_trial_volume", C.c_int, [_P, C.c_double, _D]),
     ("sc_default_run", C.c_int, [_P, C.POINTER(RunParams)]),
     ("sc_simulate", C.c_int, [_P, C.POINTER(RunParams), C.POINTER(RunStats)]),
+    ("sc_wl_load", C.c_int, [_P, C.c_char_p]),
+    ("sc_wl_load_text", C.c_int, [_P, C.c_char_p]),
+    ("sc_wl_get_info", C.c_int, [_P, C.POINTER(WlInfo)]),
+    ("sc_wl_get", C.c_int, [_P, _D, C.POINTER(C.c_long)]),
+    ("sc_wl_write", C.c_int, [_P, C.c_char_p]),
+    ("sc_wl_end", C.c_int, [_P, C.c_char_p]),
     ("sc_replicas_create", C.c_int, [C.POINTER(_P), C.c_int, _D, _I, C.POINTER(_P)]),
     ("sc_replicas_run", C.c_int, [_P, C.POINTER(RunParams), C.c_int, C.POINTER(RunStats), _D, _D,
                                   C.POINTER(C.c_long), C.POINTER(C.c_long)]),

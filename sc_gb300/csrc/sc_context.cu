@@ -30,6 +30,7 @@ Context::~Context() { freeDevice(); }
 
 void Context::freeDevice() {
     destroyEngine(this);
+    destroyWl(this);
     if (!devReady) return;
     cudaSetDevice(device);
     for (void* p : allocations) cudaFree(p);
@@ -300,7 +301,19 @@ int sc_open(const char* options_path, const char* top_path, const char* config_p
     if (!readFile(options_path, o)) return fail(SC_ERR_IO, std::string("cannot read ") + options_path);
     if (!readFile(top_path, t)) return fail(SC_ERR_IO, std::string("cannot read ") + top_path);
     if (!readFile(config_path, c)) return fail(SC_ERR_IO, std::string("cannot read ") + config_path);
-    return sc_open_text(o.c_str(), t.c_str(), c.c_str(), out);
+    int rc = sc_open_text(o.c_str(), t.c_str(), c.c_str(), out);
+    if (rc || C(*out)->opts.wlm[0] <= 0) return rc;
+    // the reference reads its Wang-Landau weights from wl.dat (structures.h:93, updater.h:19)
+    std::string dir = options_path;
+    size_t slash = dir.find_last_of('/');
+    std::string wl = (slash == std::string::npos ? std::string() : dir.substr(0, slash + 1)) + "wl.dat";
+    std::string text;
+    if (!readFile(wl.c_str(), text)) return SC_OK;
+    if ((rc = sc_wl_load_text(*out, text.c_str()))) {
+        sc_close(*out);
+        *out = nullptr;
+    }
+    return rc;
 }
 
 int sc_close(sc_context* ctx) {

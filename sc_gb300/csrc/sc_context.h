@@ -16,6 +16,8 @@ struct SweepEngine;   // sweep.cu: device state of the move loop
 struct Batch;         // sweep.cu: systems moved together
 struct Surrogate;     // surrogate.cu: learned pair-energy surrogate
 struct MlpPacked;     // surrogate.cuh: its BF16 weights in mma fragment order
+struct WlHost;        // wanglandau.cu: Wang-Landau weights and histogram
+struct WlDev;         // wanglandau.h: their device record
 
 struct Context {
     Options opts;
@@ -49,6 +51,7 @@ struct Context {
     Particle trialState;
 
     Surrogate* surrogate = nullptr;   // first stage of delayed-acceptance moves (not owned)
+    WlHost* wl = nullptr;             // Wang-Landau bias (sc_wl_load), owned
     SweepEngine* engine = nullptr;
     Batch* batch = nullptr;
     long lastLaunches = 0;     // kernels launched by the last move loop
@@ -79,5 +82,12 @@ int createReplicas(Context* const* sys, int nrep, const double* temps, const int
 void destroyReplicas(void* h);
 int runReplicas(void* h, const sc_run_params& p, int exchangeEvery, sc_run_stats& st, double* tempsOut,
                 double* energiesOut, long* exTried, long* exAcc);
+// Wang-Landau (wanglandau.cu)
+bool wlActive(const Context* c);                      // weights loaded and options wlm > 0
+int wlCheckRun(const Context* c, const sc_run_params& p);
+int wlPrepare(Context* c, bool hostChanged);          // device record current before a run
+WlDev* wlDevice(const Context* c);                    // nullptr when inactive
+bool wlConverged(Context* c);                         // reads the device flag (stream synchronised)
+void destroyWl(Context* c);
 
 }  // namespace scg

@@ -46,6 +46,7 @@
 #include "philox.cuh"
 #include "sc_context.h"
 #include "surrogate.cuh"
+#include "wanglandau.h"
 
 namespace scg {
 
@@ -137,6 +138,7 @@ struct SweepArgs {
     double volW[MAX_DEV_TYPES];   // Ia_param volume of each type (clusterCM weights)
     int ptype;              // pressure coupling of volume moves (movecreator.cpp:349-546)
     double boxMinChain[3];  // smallest box edges the chain grid allows (0: no chain phase)
+    WlDev* wl;              // Wang-Landau bias (nullptr: none; only the particle grid's records)
 };
 
 __device__ __forceinline__ int wrapCell(double x, double shift, int nc) {
@@ -259,6 +261,10 @@ __global__ void kAssign(const SweepArgs* __restrict__ A) {
     int cell = (cz * a.g.nc[1] + cy) * a.g.nc[0] + cx;
     a.cellOf[i] = cell;
     atomicAdd(&a.cellCount[cell], 1);
+    if (a.wl) {             // the cells of the particles that change the order parameters
+        if (i == a.wl->part[0]) a.wl->cell[0] = cell;
+        if (i == a.wl->part[1]) a.wl->cell[1] = cell;
+    }
 }
 
 __global__ void kScan(const SweepArgs* __restrict__ A) {
@@ -812,6 +818,59 @@ __device__ void acceptThresholds(const SweepArgs& a, Proposal& P, int cell, int 
 
 
 
+// ---- Wang-Landau bias (cells holding the order parameters' particles) -------------------
+// The cells that hold particles 0 / 1 (the particles whose moves change the supported order
+// parameters) are not moved in their colour phase: kWlCells moves them, one after the other,
+// after every other cell of the sweep, so that each of their moves sees the current bins and
+// weights, exactly as the reference's sequential loop does for some order of the sweep's moves.
+__device__ __forceinline__ bool isWlCell(const WlDev& w, int cell) { return cell == w.cell[0] || cell == w.cell[1]; }
+
+// One visit of the current bin (WangLandau::accept / reject, wanglandau.h:262-290): the
+// histogram counts it and the weight drops by alpha (implicit in wlWeight).
+__device__ __forceinline__ void wlVisit(WlDev& w) {
+    atomicAdd((unsigned long long*)&w.hist[wlIndex(w, w.cur)], 1ull);
+}
+
+// The bins after proposal P (WangLandau::run for displacements, runRot for rotations,
+// wanglandau.h:124-217) and the system centre after it (zDir, :293-299); false when a bin
+// leaves the histogram (the move is rejected).
+__device__ bool wlProposal(const SweepArgs& a, const WlDev& w, const Proposal& P, const double3& box, long long nw[2],
+                           double cmNew[3]) {
+    const int t = P.target;
+    for (int d = 0; d < 3; ++d) cmNew[d] = w.syscm[d];
+    if (P.displace && w.needCM) {
+        const double vol = a.volW[P.type];
+        for (int d = 0; d < 3; ++d) cmNew[d] += ((P.npos[d] - P.opos[d]) * vol) / w.sysvol;
+    }
+    nw[0] = w.cur[0];
+    nw[1] = w.cur[1];
+    const double bx[3] = {box.x, box.y, box.z};
+    for (int k = 0; k < w.dim; ++k) {
+        switch (w.wlm[k]) {
+        case 1:             // z of particle 0 relative to the centre: every displacement moves the centre
+            if (P.displace) nw[k] = wlZOrder(w, k, t == 0 ? P.npos[2] : a.s.pos[0].z, cmNew[2], box.z);
+            break;
+        case 3:             // z component of particle 0's axis: its rotations
+            if (!P.displace && t == 0) nw[k] = wlOrientOrder(w, k, P.ndir[2]);
+            break;
+        case 4:             // xy distance of particles 0 and 1: their displacements
+            if (P.displace && (t == 0 || t == 1)) {
+                double p0[3], p1[3];
+                const double4_32a q0 = a.s.pos[0], q1 = a.s.pos[1];
+                p0[0] = q0.x; p0[1] = q0.y; p0[2] = q0.z;
+                p1[0] = q1.x; p1[1] = q1.y; p1[2] = q1.z;
+                double* moved = t == 0 ? p0 : p1;
+                for (int d = 0; d < 3; ++d) moved[d] = P.npos[d];
+                nw[k] = wlDistOrder(w, k, p0, p1, bx);
+            }
+            break;
+        default:            // 8, 9: box lengths, changed by volume moves only
+            break;
+        }
+    }
+    return wlInRange(w, nw);
+}
+
 __device__ __forceinline__ float3 f3(double x, double y, double z) { return make_float3((float)x, (float)y, (float)z); }
 
 // The moved particle as the surrogate sees it (FP32, old and new orientation).
@@ -953,7 +1012,7 @@ struct NoWait {
 // stencil's layout and the first move's proposal; then `wait()` (the dataflow kernels wait
 // there for the earlier-phase neighbours; false: give up), then everything that reads the
 // neighbours' particles.
-template <class Wait>
+template <bool WL, class Wait>
 __device__ __forceinline__ void moveCell(const SweepArgs& a, int cx, int cy, int cz, Wait wait) {
     extern __shared__ float4 dynSmem[];
     __shared__ MoveShared sh;
@@ -1001,7 +1060,7 @@ __device__ __forceinline__ void moveCell(const SweepArgs& a, int cx, int cy, int
     unsigned evalMine = 0;          // pairs this thread evaluated for moves that were decided
     for (int m = 0; m < cnt; ++m) {
         // paired passes start with the second pass (the first builds their proposals)
-        const bool pair = a.pairMoves && !a.mlp && m > 0 && m + 1 < cnt;
+        const bool pair = !WL && a.pairMoves && !a.mlp && m > 0 && m + 1 < cnt;
         {
             const bool need0 = sh.propFor[m & 3] != m;
             const bool need1 = pair && sh.propFor[(m + 1) & 3] != m + 1;
@@ -1023,7 +1082,10 @@ __device__ __forceinline__ void moveCell(const SweepArgs& a, int cx, int cy, int
         const Proposal& P0 = sh.prop[m & 3];
         const Proposal& P1 = sh.prop[(m + 1) & 3];
         if (P0.skip) {
-            if (tid == 0) { if (P0.displace) { ++nRejT; ++nCellRej; } else ++nRejR; }
+            if (tid == 0) {
+                if (P0.displace) { ++nRejT; ++nCellRej; } else ++nRejR;
+                if (WL) wlVisit(*a.wl);         // a rejected move visits the current bin
+            }
             continue;
         }
         const bool eval1 = pair && !P1.skip;
@@ -1274,6 +1336,22 @@ __device__ __forceinline__ void moveCell(const SweepArgs& a, int cx, int cy, int
                 if (!accept) ++nS2Rej;
                 daErr2 += x * x;
                 daErrSum += x;
+            } else if (WL) {
+                // WangLandau::run / runRot (wanglandau.h:124-217): the bins after the move; a
+                // bin outside the histogram rejects it, else the weight difference wlener
+                // enters moveTry(energy + wlener, enermove) (movecreator.cpp:966-987, 1009-1023)
+                WlDev& w = *a.wl;
+                long long nw[2];
+                double cmNew[3];
+                const bool inRange = wlProposal(a, w, P0, box, nw, cmNew);
+                double eOld = e0;
+                if (inRange) eOld += wlWeight(w, wlIndex(w, nw)) - wlWeight(w, wlIndex(w, w.cur));
+                accept = inRange && ((e1 <= eOld) || ((e1 - eOld) < P0.thrMet));
+                if (accept) {
+                    w.cur[0] = nw[0]; w.cur[1] = nw[1];
+                    for (int d = 0; d < 3; ++d) w.syscm[d] = cmNew[d];
+                }
+                wlVisit(w);
             } else {
                 accept = (e1 <= e0) || ((e1 - e0) < P0.thrMet);
             }
@@ -1377,7 +1455,8 @@ __device__ __forceinline__ void colourBody(const SweepArgs* __restrict__ A, int 
     if ((int)blockIdx.x >= g.nactive || phase >= g.ncolours) return;
     int cx, cy, cz;
     decodeActive(g, a.ctl->perm[phase], blockIdx.x, cx, cy, cz);
-    moveCell(a, cx, cy, cz, NoWait());
+    if (a.wl && isWlCell(*a.wl, (cz * g.nc[1] + cy) * g.nc[0] + cx)) return;     // moved by kWlCells
+    moveCell<false>(a, cx, cy, cz, NoWait());
 }
 
 // One CTA per active cell of a colour.  Two register budgets of the same code: kColour
@@ -1443,7 +1522,9 @@ __device__ __forceinline__ void flowBody(const SweepArgs* __restrict__ A) {
         int cx, cy, cz;
         decodeActive(g, a.ctl->perm[phase], tk - phase * g.nactive, cx, cy, cz);
         const int cell = (cz * g.nc[1] + cy) * g.nc[0] + cx;
-        if (counts[cell] == 0) {                // no moves: nothing to wait for, nothing to publish first
+        // no moves (or, with a Wang-Landau bias, the cells kWlCells moves after the sweep's
+        // other cells): nothing to wait for, nothing to publish first
+        if (counts[cell] == 0 || (!CHAIN && a.wl && isWlCell(*a.wl, cell))) {
             if (tid == 0) storeReleaseGpu(&a.cellDone[cell], stamp);
             continue;
         }
@@ -1470,7 +1551,7 @@ __device__ __forceinline__ void flowBody(const SweepArgs* __restrict__ A) {
             return !sFail;
         };
         if (CHAIN) chainCell(a, cx, cy, cz, waitNeighbours);
-        else moveCell(a, cx, cy, cz, waitNeighbours);
+        else moveCell<false>(a, cx, cy, cz, waitNeighbours);
         __syncthreads();
         if (sFail) {
             if (tid == 0) atomicOr(a.err, E_FLOW_WAIT);
@@ -1485,6 +1566,130 @@ __device__ __forceinline__ void flowBody(const SweepArgs* __restrict__ A) {
 __global__ void __launch_bounds__(kMoveThreads, 1) kColourFlow(const SweepArgs* __restrict__ A) { flowBody<false>(A); }
 __global__ void __launch_bounds__(kMoveThreads, 3) kColourFlowDense(const SweepArgs* __restrict__ A) {
     flowBody<false>(A);
+}
+
+// ---- Wang-Landau: the order parameters' cells, chain moves, flatness ---------------------
+// Sum over particles of volume * position, in a fixed order (block of kMoveThreads): with
+// cmK it gives the system centre Conf::syscm as the reference accumulates it (massCenter at
+// the start, Conf.cpp:78-95, then + volume * displacement / sysvolume per move).
+__device__ void wlCentre(const SweepArgs& a, WlDev& w) {
+    __shared__ double red[32][3];
+    double s[3] = {0.0, 0.0, 0.0};
+    for (int i = threadIdx.x; i < a.s.n; i += blockDim.x) {
+        const double4_32a p = a.s.pos[i];
+        const double v = a.volW[(int)p.w];
+        s[0] += v * p.x; s[1] += v * p.y; s[2] += v * p.z;
+    }
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s[d] += __shfl_down_sync(0xffffffffu, s[d], o);
+    if ((threadIdx.x & 31) == 0)
+        for (int d = 0; d < 3; ++d) red[threadIdx.x >> 5][d] = s[d];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int d = 0; d < 3; ++d) {
+            double t = 0.0;
+            for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += red[q][d];
+            w.syscm[d] = (t - w.cmK[d]) / w.sysvol;
+        }
+    }
+    __syncthreads();
+}
+
+// After the colour phases: the sweep's other moves each visited the current bin (they do
+// not change the supported order parameters, except order 1 through the system centre,
+// which is re-derived here from the positions); then the cells of particles 0 / 1 make their
+// moves with the bias, one cell after the other.
+__global__ void __launch_bounds__(kMoveThreads, 1) kWlCells(const SweepArgs* __restrict__ A) {
+    const SweepArgs& a = A[blockIdx.y];
+    if (!a.wl) return;
+    WlDev& w = *a.wl;
+    const Grid& g = a.g;
+    if (threadIdx.x == 0) {
+        long long others = a.s.n;
+        for (int q = 0; q < 2; ++q) {
+            const int cell = w.cell[q];
+            if (cell >= 0 && !(q == 1 && cell == w.cell[0])) others -= a.cellCount[cell];
+        }
+        w.hist[wlIndex(w, w.cur)] += others;
+    }
+    if (w.needCM) {
+        wlCentre(a, w);
+        if (threadIdx.x == 0) {
+            long long o[2] = {w.cur[0], w.cur[1]};
+            for (int k = 0; k < w.dim; ++k)
+                if (w.wlm[k] == 1) o[k] = wlZOrder(w, k, a.s.pos[0].z, w.syscm[2], a.s.box[2]);
+            if (wlInRange(w, o)) { w.cur[0] = o[0]; w.cur[1] = o[1]; }
+        }
+    }
+    __syncthreads();
+    for (int q = 0; q < 2; ++q) {
+        const int cell = w.cell[q];
+        const bool run = cell >= 0 && cell < g.ncells && !(q == 1 && cell == w.cell[0]);
+        if (run) {
+            const int cx = cell % g.nc[0], cy = (cell / g.nc[0]) % g.nc[1], cz = cell / (g.nc[0] * g.nc[1]);
+            moveCell<true>(a, cx, cy, cz, NoWait());
+        }
+        __syncthreads();
+    }
+}
+
+// After the chain phase: each chain-move attempt visited the current bin.
+__global__ void kWlAfterChains(const SweepArgs* __restrict__ A) {
+    const SweepArgs& a = A[blockIdx.y];
+    if (!a.wl || threadIdx.x != 0 || blockIdx.x != 0) return;
+    WlDev& w = *a.wl;
+    const unsigned long long seen = a.counters[C_ACC_CH] + a.counters[C_REJ_CH];
+    w.hist[wlIndex(w, w.cur)] += (long long)(seen - w.chainSeen);
+    w.chainSeen = seen;
+}
+
+// End of a sweep: every kWlUpdateEvery sweeps, WangLandau::update (wanglandau.h:66-120): when
+// the smallest bin count exceeds WL_MINHIST and temper * log(max / min) < WL_GERR (max / min
+// an integer quotient, as the reference's longs give), alpha is halved, the histogram
+// cleared and the weights shifted by the first bin's; below WL_ALPHATOL the run is over.
+__global__ void kWlEndSweep(const SweepArgs* __restrict__ A) {
+    const SweepArgs& a = A[blockIdx.y];
+    if (!a.wl || blockIdx.x != 0) return;
+    WlDev& w = *a.wl;
+    if (!(w.alpha > 0.0) || w.converged || a.ctl->sweep % kWlUpdateEvery != 0) return;
+    __shared__ long long smin[32], smax[32];
+    __shared__ int flat;
+    __shared__ double wmin;
+    const long long nb = (long long)w.len[0] * w.len[1];
+    long long mn = w.hist[0], mx = w.hist[0];
+    for (long long i = threadIdx.x; i < nb; i += blockDim.x) {
+        mn = min(mn, w.hist[i]);
+        mx = max(mx, w.hist[i]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mn = min(mn, __shfl_down_sync(0xffffffffu, mn, o));
+        mx = max(mx, __shfl_down_sync(0xffffffffu, mx, o));
+    }
+    if ((threadIdx.x & 31) == 0) { smin[threadIdx.x >> 5] = mn; smax[threadIdx.x >> 5] = mx; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) { mn = min(mn, smin[q]); mx = max(mx, smax[q]); }
+        flat = 0;
+        if (mn > kWlMinHist && a.temper * log((double)(mx / mn)) < kWlGerr) {
+            if (w.alpha < kWlAlphaTol) w.converged = 1;
+            else flat = 1;
+        }
+        wmin = wlWeight(w, 0);
+    }
+    __syncthreads();
+    if (!flat) return;
+    for (long long i = threadIdx.x; i < nb; i += blockDim.x) {
+        w.base[i] = wlWeight(w, i) - wmin;
+        w.hist[i] = 0;
+        w.hist0[i] = 0;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        w.alpha /= 2.0;
+        w.updates += 1;
+    }
 }
 
 // Adds the cells' energy changes of this sweep, in a fixed order, and clears them (a cell
@@ -2114,24 +2319,56 @@ __global__ void kVolumeAccept(const SweepArgs* __restrict__ A) {
         if (threadIdx.x == 0) {
             atomicAdd(&a.counters[C_VOL_CONSTR], 1ull);
             atomicAdd(&a.counters[C_REJ_V], 1ull);
+            if (a.wl) wlVisit(*a.wl);
         }
         return;
     }
     double eNew = sumPartials(a.partial, a.g.ncells);
+    if (a.wl && a.wl->needCM) wlCentre(a, *a.wl);
     if (threadIdx.x != 0) return;
     double enermove = c.pvTerm;
     enermove += eNew;
     Stream r(a.seed, 0xFFFFFFF1u, (uint32_t)c.sweep, (uint32_t)(c.sweep >> 32));
     double u = r.next();
     double energy = c.energy;
-    bool accept = (enermove <= energy) || (exp(-1.0 * (enermove - energy) / a.temper) > u);
+    long long nw[2];
+    bool inRange = true;
+    if (a.wl) {
+        // WangLandau::runPress (wanglandau.h:168-196) with the trial box: order 1 (not for
+        // ptype 2, whose z stays), 4 and the box lengths 8 / 9 change; wlener enters
+        // moveTry(energy + wlener, enermove)
+        WlDev& w = *a.wl;
+        const double* tb = c.trialBox;
+        nw[0] = w.cur[0]; nw[1] = w.cur[1];
+        for (int k = 0; k < w.dim; ++k) {
+            switch (w.wlm[k]) {
+            case 1:
+                if (a.ptype != 2) nw[k] = wlZOrder(w, k, a.s.pos[0].z, w.syscm[2], tb[2]);
+                break;
+            case 4: {
+                const double4_32a q0 = a.s.pos[0], q1 = a.s.pos[1];
+                const double p0[3] = {q0.x, q0.y, q0.z}, p1[3] = {q1.x, q1.y, q1.z};
+                nw[k] = wlDistOrder(w, k, p0, p1, tb);
+                break;
+            }
+            case 8: nw[k] = wlBoxOrder(w, k, tb[0]); break;
+            case 9: nw[k] = wlBoxOrder(w, k, tb[1]); break;
+            default: break;
+            }
+        }
+        inRange = wlInRange(w, nw);
+        if (inRange) energy += wlWeight(w, wlIndex(w, nw)) - wlWeight(w, wlIndex(w, w.cur));
+    }
+    bool accept = inRange && ((enermove <= energy) || (exp(-1.0 * (enermove - energy) / a.temper) > u));
     if (accept) {
         for (int d = 0; d < 3; ++d) a.s.box[d] = c.trialBox[d];
         c.energy = eNew;
         atomicAdd(&a.counters[C_ACC_V], 1ull);
+        if (a.wl) { a.wl->cur[0] = nw[0]; a.wl->cur[1] = nw[1]; }
     } else {
         atomicAdd(&a.counters[C_REJ_V], 1ull);
     }
+    if (a.wl) wlVisit(*a.wl);
 }
 
 __global__ void kSetEnergy(const SweepArgs* __restrict__ A) {
@@ -2241,6 +2478,7 @@ struct Batch {
     int maxN = 0, maxCells = 0, maxActive = 0, maxColours = 0;
     // chain phase (every system of the batch holds chains, or none does)
     bool chains = false;
+    bool wl = false;          // a system carries a Wang-Landau bias
     std::vector<SweepArgs> hArgsC;
     SweepArgs* dArgsC = nullptr;
     int nArgsCAlloc = 0;
@@ -2250,7 +2488,7 @@ struct Batch {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<cudaEvent_t> evPhase;     // time_phases: start / end of each sweep's move launches
     cudaGraphExec_t graph = nullptr;
-    int graphDims[13] = {0};   // launch shape the graph was captured with
+    int graphDims[14] = {0};   // launch shape the graph was captured with
     long graphLaunches = 0, graphPhaseLaunches = 0;
     // parallel tempering
     int* dLadder = nullptr;
@@ -2394,6 +2632,7 @@ static void fillArgs(Context* c, SweepEngine* e, const sc_run_params& p) {
         a.mlp = surrogatePacked(c->surrogate);
         a.rcutS = surrogateCutoff(c->surrogate);
     }
+    a.wl = wlDevice(c);
 }
 
 // Chain phase of one system: chains (molecules of more than one particle), the bound R of
@@ -2476,6 +2715,7 @@ static int prepareChains(Context* c, SweepEngine* e, const sc_run_params& p, con
     a.cellDirF = a.cellPatF = nullptr;
     a.mlp = nullptr;
     a.seed = p.seed ^ 0x6A09E667F3BCC909ull;
+    a.wl = nullptr;
     a.energyAcc = &e->ctl->energy;
     a.chains = C.chains;
     a.nChains = C.nChains;
@@ -2496,6 +2736,7 @@ static int prepareSystem(Context* c, const sc_run_params& p, bool npt) {
     const bool hostChanged = c->hostNewer;    // the running energy must be recomputed
     int rc = c->ensureDevice();
     if (rc) return rc;
+    if ((rc = wlPrepare(c, hostChanged))) return rc;
     if (hostChanged && c->engine) c->engine->energyKnown = false;
     int n = c->d.n;
     SweepEngine* e = c->engine;
@@ -2523,7 +2764,10 @@ static int prepareSystem(Context* c, const sc_run_params& p, bool npt) {
     double box[3];
     cudaMemcpy(box, c->d.box, sizeof box, cudaMemcpyDeviceToHost);
     e->margin = npt ? 0.03 : 1e-9;
-    e->stencil = chooseStencil(box, c->topo.maxcut, p.stencil);
+    // Wang-Landau: the order parameters' particles diffuse as fast as the cells let them
+    // (a displacement that leaves its cell is rejected), so an automatic reach is 1, the
+    // widest cells
+    e->stencil = chooseStencil(box, c->topo.maxcut, p.stencil == 0 && wlActive(c) ? 1 : p.stencil);
     if ((rc = ensureGrid(c, e, box))) return rc;
     fillArgs(c, e, p);
     if ((rc = prepareChains(c, e, p, box))) return rc;
@@ -2552,6 +2796,8 @@ static int uploadArgs(Batch& b) {
     }
     cudaError_t r = cudaMemcpy(b.dArgs, b.hArgs.data(), sizeof(SweepArgs) * ns, cudaMemcpyHostToDevice);
     if (r != cudaSuccess) return cudaFail(r, "upload sweep arguments");
+    b.wl = false;
+    for (const SweepArgs& h : b.hArgs) b.wl |= (h.wl != nullptr);
     int on = 0;
     for (Context* c : b.sys) on += c->engine->ch.on ? 1 : 0;
     if (on != 0 && on != ns) return fail(SC_ERR_UNSUPPORTED, "chain moves need every system of a batch to hold chains");
@@ -2615,6 +2861,7 @@ static int systemErrors(Context* c) {
 struct RunOut {
     double seconds = 0, phaseSeconds = 0;
     long launches = 0, phaseLaunches = 0;
+    long sweeps = 0;        // sweeps run (fewer than asked when Wang-Landau converged)
 };
 
 // Runs nsweeps sweeps of every system of the batch; with exchangeEvery > 0 a replica
@@ -2663,6 +2910,9 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
             cudaSuccess)
             return cudaFail(r, "shared memory attribute");
         if ((r = cudaFuncSetAttribute(kChainFlow, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDynSmem)) !=
+            cudaSuccess)
+            return cudaFail(r, "shared memory attribute");
+        if ((r = cudaFuncSetAttribute(kWlCells, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDynSmemColour)) !=
             cudaSuccess)
             return cudaFail(r, "shared memory attribute");
         attrSet = true;
@@ -2726,6 +2976,10 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
             ++phaseEvents;
         }
         if (timed || !timing) phaseLaunches += flow ? 1 : b.maxColours;
+        if (b.wl) {         // Wang-Landau: the cells of the order parameters' particles, last
+            kWlCells<<<dims(1), kMoveThreads, kDynSmemColour, s>>>(b.dArgs);
+            launches += 1;
+        }
         kEndSweep<<<dims(1), 256, 0, s>>>(b.dArgs);
         launches += 2 + (flow ? 1 : b.maxColours);
         if (b.chains) {       // chain moves: their own grid, colours and cell list
@@ -2741,6 +2995,10 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
             }
             kEndSweep<<<dims(1), 256, 0, s>>>(b.dArgsC);
             launches += 3 + (flow ? 1 : b.maxColoursC);
+            if (b.wl) {
+                kWlAfterChains<<<dims(1), 32, 0, s>>>(b.dArgs);
+                launches += 1;
+            }
         }
         if (volDue) {
             // chain moves left particles outside the cells of this sweep's list: list them anew
@@ -2748,6 +3006,10 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
             kCellEnergy<<<dims(b.maxCells), kCellThreads, kDynSmemCell, s>>>(b.dArgs, 1);
             kVolumeAccept<<<dims(1), 256, 0, s>>>(b.dArgs);
             launches += 2;
+        }
+        if (b.wl) {
+            kWlEndSweep<<<dims(1), 256, 0, s>>>(b.dArgs);
+            launches += 1;
         }
         return cudaGetLastError();
     };
@@ -2763,13 +3025,23 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
     long nextCheck = p.check_every > 0 ? p.check_every : -1;
     long nextRegrid = npt ? chunk : -1;
     long nextExchange = exchangeEvery > 0 ? exchangeEvery : -1;
+    // Wang-Landau: the flatness check runs every kWlUpdateEvery sweeps of the device's count;
+    // the host looks for convergence at those sweeps and stops there, as the reference does
+    long nextWl = -1;
+    if (b.wl) {
+        unsigned long long done = 0;
+        cudaMemcpy(&done, &b.sys[0]->engine->ctl->sweep, sizeof done, cudaMemcpyDeviceToHost);
+        nextWl = (long)(kWlUpdateEvery - (long)(done % kWlUpdateEvery));
+    }
+    out.sweeps = nsweeps;
     long sw = 0;
     while (sw < nsweeps) {
         long left = nsweeps - sw;
-        bool aligned = (sw % G == 0) && (nextExchange < 0 || nextExchange - sw >= G);
+        bool aligned = (sw % G == 0) && (nextExchange < 0 || nextExchange - sw >= G) && (nextWl < 0 || nextWl - sw >= G);
         if (useGraph && left >= G && aligned) {
-            int key[13] = {ns, b.maxN, b.maxCells, b.maxActive, b.maxColours, (int)G, anySurrogate ? 1 : 0,
-                           b.chains ? 1 : 0, b.maxCellsC, b.maxActiveC, b.maxColoursC, dense ? 1 : 0, flow ? 1 : 0};
+            int key[14] = {ns, b.maxN, b.maxCells, b.maxActive, b.maxColours, (int)G, anySurrogate ? 1 : 0,
+                           b.chains ? 1 : 0, b.maxCellsC, b.maxActiveC, b.maxColoursC, dense ? 1 : 0, flow ? 1 : 0,
+                           b.wl ? 1 : 0};
             if (!b.graph || std::memcmp(key, b.graphDims, sizeof key) != 0) {
                 if (b.graph) { cudaGraphExecDestroy(b.graph); b.graph = nullptr; }
                 cudaGraph_t graph;
@@ -2796,6 +3068,13 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
         } else {
             if ((r = launchOne(npt && ((sw + 1) % ve == 0), p.time_phases != 0)) != cudaSuccess) return cudaFail(r, "sweep launch");
             sw += 1;
+        }
+        if (nextWl > 0 && sw >= nextWl) {
+            while (nextWl <= sw) nextWl += kWlUpdateEvery;
+            if ((r = cudaStreamSynchronize(s)) != cudaSuccess) return cudaFail(r, "sweep");
+            bool allDone = true;
+            for (Context* c : b.sys) allDone &= wlConverged(c);
+            if (allDone) { out.sweeps = sw; break; }
         }
         if (nextExchange > 0 && sw >= nextExchange) {
             kExchange<<<1, 32, 0, s>>>(b.dArgs, b.chains ? b.dArgsC : nullptr, b.dLadder, b.dLadderStart, b.nLadders,
@@ -2876,6 +3155,7 @@ int runSweeps(Context* c, const sc_run_params& p, sc_run_stats& st) {
     if (rc) return rc;
     if (c->conf.p.empty()) return SC_OK;
     if (p.delayed && !c->surrogate) return fail(SC_ERR_STATE, "delayed = 1 needs a surrogate (sc_set_surrogate)");
+    if ((rc = wlCheckRun(c, p))) return rc;
     const bool npt = p.volume_every > 0;
     if ((rc = prepareSystem(c, p, npt))) return rc;
     if (!c->batch) {
@@ -2889,7 +3169,7 @@ int runSweeps(Context* c, const sc_run_params& p, sc_run_stats& st) {
     RunOut out;
     if ((rc = runBatch(b, p, p.nsweeps, 0, 0, out))) return rc;
     collectStats(c, st);
-    st.sweeps = p.nsweeps;
+    st.sweeps = out.sweeps;
     st.seconds = out.seconds;
     st.phase_seconds = out.phaseSeconds;
     st.phase_launches = out.phaseLaunches;
@@ -2959,6 +3239,9 @@ int runReplicas(void* h, const sc_run_params& p, int exchangeEvery, sc_run_stats
     for (int k = 0; k < nrep; ++k) {
         Context* c = b.sys[k];
         if (c->conf.p.empty()) return fail(SC_ERR_ARG, "a replica holds no particles");
+        if (wlActive(c))
+            return fail(SC_ERR_UNSUPPORTED, "Wang-Landau weights in a replica batch (the exchange would need their terms, "
+                                            "movecreator.cpp:736-740): run the walker with sc_simulate");
         sc_run_params q = p;
         sc_default_run(reinterpret_cast<const sc_context*>(c), &q);   // per-replica step sizes
         q.nsweeps = p.nsweeps; q.seed = p.seed + 0x9E3779B97F4A7C15ull * (unsigned long long)(k + 1);

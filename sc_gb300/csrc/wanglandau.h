@@ -1,0 +1,82 @@
+// wanglandau.h -- Wang-Landau flat-histogram sampling on the GPU move loop.
+//
+// The reference's WangLandau class (scOOP/mc/wanglandau.h:16-690, wanglandau.cpp) biases
+// every move by weights of one or two order parameters and lowers the weight of the
+// visited bin by alpha after every move (accept / reject, wanglandau.h:262-290); alpha is
+// halved when the histogram is flat (update, :66-120).  This build supports the order
+// parameters whose value only the moves of particles 0 and 1 and the box change:
+//   1  z of particle 0 relative to the system's volume-weighted centre   (zOrder,  :551-554)
+//   3  z component of particle 0's axis                                  (zOrient, :321-324)
+//   4  xy distance of particles 0 and 1                                  (twoPartDist, :395-398)
+//   8  box length in x, 9 box length in y                                (boxSize_x/_y, :376-382)
+//
+// Weights are kept as w[i] = base[i] - alpha * (hist[i] - hist0[i]): base and hist0 are
+// set when alpha changes, hist counts visits as the reference's histogram does, so the
+// weight decrements of all moves are integer counts (exact, independent of the order in
+// which concurrent updates land).
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace scg {
+
+constexpr double kWlGerr = 0.0001;        // WL_GERR     scOOP/structures/macros.h:103
+constexpr double kWlAlphaTol = 1.0e-8;    // WL_ALPHATOL macros.h:104
+constexpr long kWlMinHist = 1000;         // WL_MINHIST  macros.h:105
+constexpr int kWlUpdateEvery = 1000;      // sweeps between flatness checks, updater.cpp:255
+
+struct WlDev {
+    int dim;                 // 1 or 2 order parameters
+    int wlm[2];              // order parameter kinds (0: none)
+    int len[2];              // bins per dimension (len[1] = 1 for one dimension)
+    int part[2];             // particles whose moves change the orders (-1: none)
+    int cell[2];             // their cells in the current sweep (written by kAssign)
+    int needCM;              // order 1 in use: the system centre is tracked
+    int converged;           // update() found a flat histogram with alpha below tolerance
+    int volDone;             // this sweep's volume move counted (kVolumeAccept)
+    double minorder[2], dorder[2];
+    double alpha;
+    double sysvol;           // sum of the particles' Ia_param volumes (Conf::sysvolume)
+    double cmK[3];           // sum of volume * anInt(position) when the orders were set up
+    double syscm[3];         // volume-weighted centre, box fractions (Conf::syscm)
+    long long cur[2];        // current bins
+    long long curBeforeVol;  // bin before this sweep's volume move
+    long long updates;       // alpha halvings so far
+    unsigned long long chainSeen;   // chain-move attempts already counted
+    double* base;            // weights when alpha last changed
+    long long* hist;         // histogram (reset when alpha changes)
+    long long* hist0;        // histogram when alpha last changed
+};
+
+__host__ __device__ inline double wlWeight(const WlDev& w, long long i) {
+    return w.base[i] - w.alpha * (double)(w.hist[i] - w.hist0[i]);
+}
+__host__ __device__ inline long long wlIndex(const WlDev& w, const long long o[2]) {
+    return o[0] + o[1] * (long long)w.len[0];
+}
+__host__ __device__ inline bool wlInRange(const WlDev& w, const long long o[2]) {
+    for (int k = 0; k < w.dim; ++k)
+        if (o[k] < 0 || o[k] >= w.len[k]) return false;
+    return true;
+}
+
+// Order-parameter bins, as the reference computes them (ceil for positions and box
+// lengths, floor for the orientation).
+__host__ __device__ inline long long wlZOrder(const WlDev& w, int k, double z0, double cmz, double boxz) {
+    return (long long)ceil(((z0 - cmz) * boxz - w.minorder[k]) / w.dorder[k]);
+}
+__host__ __device__ inline long long wlOrientOrder(const WlDev& w, int k, double dirz) {
+    return (long long)floor((dirz - w.minorder[k]) / w.dorder[k]);
+}
+__host__ __device__ inline long long wlDistOrder(const WlDev& w, int k, const double* p0, const double* p1,
+                                                 const double* box) {
+    // Cuboid::image (geometry.h:110-128): rint is the reference's round-half-even
+    double dx = p0[0] - p1[0], dy = p0[1] - p1[1];
+    double rx = box[0] * (dx - rint(dx)), ry = box[1] * (dy - rint(dy));
+    return (long long)ceil((sqrt(rx * rx + ry * ry) - w.minorder[k]) / w.dorder[k]);
+}
+__host__ __device__ inline long long wlBoxOrder(const WlDev& w, int k, double edge) {
+    return (long long)ceil((edge - w.minorder[k]) / w.dorder[k]);
+}
+
+}  // namespace scg

@@ -6,6 +6,7 @@ Method names follow the reference (robertvacha/SC, scOOP):
   all_to_all       TotalEMatrix::allToAll         totalenergycalculator.h:334-353
   mol2others       TotalEMatrix::mol2othersTrial  totalenergycalculator.h:453-499
   simulate         Updater::simulate              scOOP/mc/updater.cpp:45-389
+  wl_*             WangLandau init / write / end  scOOP/mc/wanglandau.cpp:49-433
 Every call goes to the CUDA library; a missing library raises.
 """
 import ctypes as C
@@ -36,7 +37,7 @@ class System:
     def open(cls, options_path, top_path, config_path):
         lib = L.load()
         h = C.c_void_p()
-        L.check(lib.sc_open(options_path.encode(), top_path.encode(), config_path.encode(), C.byref(h)))
+        L.check(lib.sc_open(str(options_path).encode(), str(top_path).encode(), str(config_path).encode(), C.byref(h)))
         return cls(h)
 
     @classmethod
@@ -198,6 +199,35 @@ class System:
         st = L.RunStats()
         L.check(self._lib.sc_simulate(self._h, C.byref(p), C.byref(st)))
         return st
+
+    # --- Wang-Landau (WangLandau, scOOP/mc/wanglandau.h, wanglandau.cpp) ----------------
+    def wl_load(self, path=None, text=None):
+        """WangLandau::initCalc + init: weights file by path or as text."""
+        if text is not None:
+            L.check(self._lib.sc_wl_load_text(self._h, text.encode()))
+        else:
+            L.check(self._lib.sc_wl_load(self._h, str(path).encode()))
+
+    def wl_info(self):
+        i = L.WlInfo()
+        L.check(self._lib.sc_wl_get_info(self._h, C.byref(i)))
+        return i
+
+    def wl_weights(self):
+        """(weights, hist) of every bin, order 0 running fastest."""
+        i = self.wl_info()
+        nb = i.length[0] * max(1, i.length[1])
+        w = np.zeros(nb)
+        h = np.zeros(nb, dtype=np.int64)
+        L.check(self._lib.sc_wl_get(self._h, _dptr(w), h.ctypes.data_as(C.POINTER(C.c_long))))
+        return w, h
+
+    def wl_write(self, path):
+        L.check(self._lib.sc_wl_write(self._h, str(path).encode()))
+
+    def wl_end(self, path):
+        """WangLandau::endWangLandau: the final weights file."""
+        L.check(self._lib.sc_wl_end(self._h, str(path).encode()))
 
 
 class ReplicaSet:

@@ -299,6 +299,45 @@ def bilayers(n_side=50, box=(60.0, 60.0, 40.0), seed=1, temper=1.0, chainprob=0.
     return _lipid_texts(box, np.array(heads), np.array(axes), rng, opts)
 
 
+def protein_bilayer(n_side=20, box=(30.0, 30.0, 40.0), seed=1, temper=1.0, chainprob=0.1, wlm=(1, 3)):
+    """A cylindrical-patch particle (CPSC, length 2: the tails' length, one SC length per
+    system) above one lipid bilayer of 2 n_side^2 three-bead lipids, with Wang-Landau weights
+    over its height relative to the system centre (order 1) and its axis z component
+    (order 3) -- the setting of the reference's membrane example (options wlm = 1 3).
+    Returns options, top.init, config.init and the weights file (flat, alpha 0.05)."""
+    rng = np.random.default_rng(seed)
+    box = np.asarray(box, float)
+    a = box[0] / n_side
+    g = (np.arange(n_side) + 0.5) * a
+    xy = np.stack(np.meshgrid(g, g, indexing="ij"), -1).reshape(-1, 2)
+    heads, axes = [], []
+    zc = 0.0                # the bilayer at z = 0, where the wrapped centre of Conf::massCenter sits
+    for side in (+1.0, -1.0):
+        off = 0.0 if side > 0 else 0.5 * a
+        for x, y in xy:
+            tilt, az = rng.uniform(0.01, 0.05), rng.uniform(0, 2 * math.pi)
+            u = side * np.array([math.sin(tilt) * math.cos(az), math.sin(tilt) * math.sin(az), math.cos(tilt)])
+            heads.append(np.array([x + off, y + off, zc + side * 6.5]))
+            axes.append(u)
+    pos, dirs = [np.array([0.5 * box[0], 0.5 * box[1], 0.3 * box[2]])], [_unit(rng, 1)[0]]
+    for h, u in zip(heads, axes):
+        pos += _lipid(h, u)
+        dirs += [u, u, u]
+    pos, dirs = np.array(pos), np.array(dirs)
+    dirs = dirs + 0.03 * rng.normal(size=dirs.shape)
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    top = LIPID_TOP.replace("[Molecules]\n", "P 3 CPSC 1.0 1.0 1.12 0.2 120.0 10.0 2.0 0.0\n[Molecules]\nP: {\nparticles: 3\n}\n")
+    top += f"[System]\nP 1\nL {len(heads)}\n"
+    opts = options_text(ptype=0, transmx=0.3, rotmx=20.0, temper=temper, seed=seed, chainprob=chainprob,
+                        chainmmx=0.3, chainrmx=15.0, wlm=" ".join(str(m) for m in wlm), wlmtype=3)
+    lines = ["0.05"]
+    for j in range(21):
+        for i in range(79):
+            lines.append(f"{-19.5 + 0.5 * i:.6f} {-1.0 + 0.1 * j:.6f} 0.0 0")
+    wl = "\n".join(lines) + "\n"
+    return opts, top, config_text(box, pos, dirs, _perp(rng, dirs)), wl
+
+
 def pt_ladders(n_ladders=8, per_ladder=8, seed=1, n_range=(500, 4000), phi_range=(0.10, 0.25), t_range=(0.8, 1.6)):
     """Parallel-tempering replicas of the PSC model with uneven sizes: n_ladders systems
     (N and packing fraction drawn uniformly), each replicated over a geometric

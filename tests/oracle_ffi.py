@@ -91,6 +91,10 @@ def lib():
         L.or_psc_rotate.argtypes = [C.POINTER(Particle), C.c_int, C.c_double, Vec, C.c_int]
         L.or_mc_run.restype = C.c_int
         L.or_mc_run.argtypes = [C.POINTER(System), C.POINTER(McOpts), C.POINTER(McStats)]
+        L.or_wl_orders.restype = C.c_int
+        L.or_wl_orders.argtypes = [C.POINTER(System), C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                   C.POINTER(C.c_double), C.POINTER(C.c_long), C.POINTER(C.c_double),
+                                   C.POINTER(C.c_double)]
         _lib = L
     return _lib
 
@@ -171,6 +175,17 @@ class OracleSystem:
 
     def mol2others(self, first, size):
         return lib().or_mol2others(C.byref(self.sys), first, size)
+
+    def wl_orders(self, wlm, minorder, dorder):
+        """Starting Wang-Landau bins, system centre and sysvolume (or_wl_orders)."""
+        m = (C.c_int * 2)(*wlm)
+        lo = (C.c_double * 2)(*minorder)
+        d = (C.c_double * 2)(*dorder)
+        out = (C.c_long * 2)()
+        cm = (C.c_double * 3)()
+        sv = C.c_double()
+        rc = lib().or_wl_orders(C.byref(self.sys), m, lo, d, out, cm, C.byref(sv))
+        return rc, [out[0], out[1]], [cm[0], cm[1], cm[2]], sv.value
 
 
 def parse_types(top_text):

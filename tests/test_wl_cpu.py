@@ -1,0 +1,145 @@
+"""Wang-Landau without a GPU: the weights file, the starting bins and the system centre.
+
+The goldens (tests/golden/wl/cases.json.gz, made by tests/golden/make_wl.py) hold what the
+reference itself computes with its WangLandau::init and writes with WangLandau::write
+(scOOP/mc/wanglandau.cpp:49-166) for seeded systems and weights files.  Both the oracle's
+restatement (or_wl_orders) and the library's host code (sc_wl_load / sc_wl_get_info /
+sc_wl_write, which run before any device work) must reproduce them exactly.
+"""
+import gzip
+import json
+import os
+
+import pytest
+
+import oracle_ffi as O
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+WL_GOLDEN = os.path.join(HERE, "golden", "wl", "cases.json.gz")
+ERR_STATE, ERR_UNSUPPORTED, ERR_RANGE, ERR_PARSE = -6, -7, -5, -3
+
+
+def cases():
+    with gzip.open(WL_GOLDEN, "rt") as f:
+        return json.load(f)["cases"]
+
+
+CASES = cases()
+
+
+@pytest.fixture(scope="module")
+def System():
+    from sc_gb300 import System as S
+    from sc_gb300 import build as B
+
+    B.build()
+    return S
+
+
+def wlm_of(c):
+    for line in c["inputs"]["options"].splitlines():
+        k, _, v = line.partition("=")
+        if k.strip() == "wlm":
+            w = [int(x) for x in v.split()]
+            return (w + [0])[:2]
+    raise KeyError("wlm")
+
+
+@pytest.mark.parametrize("c", CASES, ids=[c["name"] for c in CASES])
+def test_oracle_starting_bins_match_reference(c):
+    ref = c["ref"]
+    o = O.OracleSystem(c["system"])
+    rc, bins, cm, sv = o.wl_orders(wlm_of(c), ref["minorder"], ref["dorder"])
+    assert rc == 0
+    dim = 2 if wlm_of(c)[1] else 1
+    assert bins[:dim] == ref["currorder"][:dim]
+    assert sv == ref["sysvolume"]
+    if 1 in wlm_of(c):                      # the reference computes the centre for order 1 only
+        assert cm == ref["syscm"]
+
+
+@pytest.mark.parametrize("c", CASES, ids=[c["name"] for c in CASES])
+def test_library_loads_weights_like_the_reference(System, c, tmp_path):
+    inp = c["inputs"]
+    ref = c["ref"]
+    s = System.from_text(inp["options"], inp["top.init"], inp["config.init"])
+    s.wl_load(text=inp["wl.dat"])
+    i = s.wl_info()
+    dim = 2 if wlm_of(c)[1] else 1
+    assert i.dim == dim
+    assert [i.length[0], i.length[1]] == ref["length"]
+    assert [i.currorder[0], i.currorder[1]][:dim] == ref["currorder"][:dim]
+    assert i.alpha == ref["alpha"]
+    assert [i.minorder[0], i.minorder[1]][:dim] == ref["minorder"][:dim]
+    assert [i.dorder[0], i.dorder[1]][:dim] == ref["dorder"][:dim]
+    if 1 in wlm_of(c):
+        assert [i.syscm[0], i.syscm[1], i.syscm[2]] == ref["syscm"]
+    # WangLandau::write of the weights just read: the same text
+    out = tmp_path / "wl-out.dat"
+    s.wl_write(out)
+    assert out.read_text() == ref["written"]
+    s.close()
+
+
+def test_open_reads_wl_dat_beside_the_options(System, tmp_path):
+    c = CASES[0]
+    for fn in ("options", "top.init", "config.init", "wl.dat"):
+        (tmp_path / fn).write_text(c["inputs"][fn])
+    s = System.open(tmp_path / "options", tmp_path / "top.init", tmp_path / "config.init")
+    assert s.wl_info().currorder[0] == c["ref"]["currorder"][0]
+    s.close()
+
+
+def test_end_shifts_two_dimensional_weights_only(System, tmp_path):
+    for c in CASES:
+        inp = c["inputs"]
+        s = System.from_text(inp["options"], inp["top.init"], inp["config.init"])
+        s.wl_load(text=inp["wl.dat"])
+        w, _ = s.wl_weights()
+        s.wl_end(tmp_path / "end.dat")
+        rows = [l.split() for l in (tmp_path / "end.dat").read_text().splitlines()[1:] if l.strip()]
+        got = [float(r[-2]) for r in rows]
+        want = (w - w[0]) if s.wl_info().dim == 2 else w
+        assert got == pytest.approx(list(want), abs=1e-7, rel=1e-7)
+        s.close()
+
+
+def _sub(text, key, value):
+    out = []
+    for line in text.splitlines():
+        if line.split("=")[0].strip() == key:
+            line = f"{key} = {value}"
+        out.append(line)
+    return "\n".join(out) + "\n"
+
+
+def test_rejections(System):
+    from sc_gb300._lib import ScError
+
+    c = next(c for c in CASES if c["name"] == "o4_pair")
+    inp = c["inputs"]
+    # mesh / pore / contact order parameters are not on the GPU path
+    for m in (2, 5, 6, 7):
+        s = System.from_text(_sub(inp["options"], "wlm", f"{m} 0"), inp["top.init"], inp["config.init"])
+        with pytest.raises(ScError) as e:
+            s.wl_load(text=inp["wl.dat"])
+        assert e.value.code == ERR_UNSUPPORTED
+        s.close()
+    # a starting bin outside the file's range
+    s = System.from_text(inp["options"], inp["top.init"], inp["config.init"])
+    lines = inp["wl.dat"].splitlines()
+    short = "\n".join(lines[:4]) + "\n"           # alpha + three bins below the start
+    with pytest.raises(ScError) as e:
+        s.wl_load(text=short)
+    assert e.value.code == ERR_RANGE
+    # two order parameters in the options, one in the file
+    s2 = System.from_text(_sub(inp["options"], "wlm", "4 8"), inp["top.init"], inp["config.init"])
+    with pytest.raises(ScError) as e:
+        s2.wl_load(text=inp["wl.dat"])
+    assert e.value.code == ERR_PARSE
+    # wlm > 0 and no weights: the move loop refuses before touching the device
+    with pytest.raises(ScError) as e:
+        s.simulate(nsweeps=1)
+    assert e.value.code == ERR_STATE
+    s.close()
+    s2.close()
