@@ -434,10 +434,12 @@ def bench_bilayer(steps, seed=1, warm=20):
 
 def bench_wl(steps, seed=1, warm=20):
     """Wang-Landau (WangLandau, scOOP/mc/wanglandau.h): a CPSC particle above a bilayer of
-    800 three-bead lipids (2401 particles, chain moves on) with adaptive weights over its
-    height relative to the system centre and its axis z component (options wlm = 1 3, the
-    reference's membrane example), against the same system without the bias; device-timed,
-    L2 flushed between one-sweep steps."""
+    800 three-bead lipids (2401 particles) with adaptive weights over its height relative to
+    the system centre and its axis z component (options wlm = 1 3, the reference's membrane
+    example), against the same system without the bias, both with cells of the full cut-off
+    (the reach Wang-Landau runs choose) and the dataflow sweep; single-particle moves only (a
+    chain phase on this small box -- few, crowded chain cells -- would dominate both
+    timings); device-timed, L2 flushed between one-sweep steps."""
     import torch
 
     from sc_gb300 import System, workloads
@@ -445,13 +447,15 @@ def bench_wl(steps, seed=1, warm=20):
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
     out = {"workload": "protein_bilayer_2401", "particles": 2401, "order_parameters": [1, 3], "sweeps_timed": steps}
     for key, wlm in (("plain", (0, 0)), ("wang_landau", (1, 3))):
-        opts, top, cfg, wl = workloads.protein_bilayer(seed=seed, wlm=wlm)
+        opts, top, cfg, wl = workloads.protein_bilayer(seed=seed, wlm=wlm, chainprob=0.0)
         s = System.from_text(opts, top, cfg)
         if wlm[0]:
             s.wl_load(text=wl)
         p = s.default_run()
         p.check_every = 0
         p.seed = seed
+        p.stencil = 1       # the reach Wang-Landau runs choose (widest cells), for both runs
+        p.variant = 4
         s.simulate(p, nsweeps=warm)
         dev = 0.0
         moves = launches = 0

@@ -197,7 +197,8 @@ int sc_simulate(sc_context* ctx, const sc_run_params* p, sc_run_stats* stats);
  * particle 0's axis, 4 xy distance of particles 0 and 1, 8 / 9 box length in x / y.
  * sc_simulate applies the bias once weights are loaded; with wlm > 0 and none loaded it
  * returns SC_ERR_STATE (the reference stops without wl.dat).  sc_open loads wl.dat from
- * the options file's directory when it exists. */
+ * the options file's directory when it exists.  Wang-Landau weights in a replica batch
+ * need exchange_every = 0 (walkers, see sc_wl_share). */
 typedef struct {
     int dim;                 /* order parameters (1 or 2) */
     int wlm[2];
@@ -215,6 +216,12 @@ typedef struct {
 int sc_wl_load(sc_context* ctx, const char* path);
 int sc_wl_load_text(sc_context* ctx, const char* text);
 int sc_wl_get_info(sc_context* ctx, sc_wl_info* out);
+/* Multiple walkers (the reference's MPI walkers sharing weights and histogram through
+ * shared-memory windows, wanglandau.cpp:184-218): walkers[1..n-1] drop their own weights and
+ * update walkers[0]'s, which runs the flatness checks.  All need the same order parameters
+ * and bins and one device; run them together with sc_replicas_run (exchange_every = 0),
+ * where every walker's moves of a sweep update the shared histogram before the check. */
+int sc_wl_share(sc_context* const* walkers, int n);
 /* Current weights and histogram, length[0] * max(1, length[1]) entries each (either may be NULL). */
 int sc_wl_get(sc_context* ctx, double* weights, long* hist);
 /* WangLandau::write (wanglandau.cpp:139-166): the weights file format. */

@@ -109,6 +109,7 @@ SIGNATURES = [
     ("sc_wl_load", C.c_int, [_P, C.c_char_p]),
     ("sc_wl_load_text", C.c_int, [_P, C.c_char_p]),
     ("sc_wl_get_info", C.c_int, [_P, C.POINTER(WlInfo)]),
+    ("sc_wl_share", C.c_int, [C.POINTER(_P), C.c_int]),
     ("sc_wl_get", C.c_int, [_P, _D, C.POINTER(C.c_long)]),
     ("sc_wl_write", C.c_int, [_P, C.c_char_p]),
     ("sc_wl_end", C.c_int, [_P, C.c_char_p]),

@@ -828,7 +828,7 @@ __device__ __forceinline__ bool isWlCell(const WlDev& w, int cell) { return cell
 // One visit of the current bin (WangLandau::accept / reject, wanglandau.h:262-290): the
 // histogram counts it and the weight drops by alpha (implicit in wlWeight).
 __device__ __forceinline__ void wlVisit(WlDev& w) {
-    atomicAdd((unsigned long long*)&w.hist[wlIndex(w, w.cur)], 1ull);
+    atomicAdd((unsigned long long*)&w.tab->hist[wlIndex(w, w.cur)], 1ull);
 }
 
 // The bins after proposal P (WangLandau::run for displacements, runRot for rotations,
@@ -1345,7 +1345,7 @@ __device__ __forceinline__ void moveCell(const SweepArgs& a, int cx, int cy, int
                 double cmNew[3];
                 const bool inRange = wlProposal(a, w, P0, box, nw, cmNew);
                 double eOld = e0;
-                if (inRange) eOld += wlWeight(w, wlIndex(w, nw)) - wlWeight(w, wlIndex(w, w.cur));
+                if (inRange) eOld += wlWeight(*w.tab, wlIndex(w, nw)) - wlWeight(*w.tab, wlIndex(w, w.cur));
                 accept = inRange && ((e1 <= eOld) || ((e1 - eOld) < P0.thrMet));
                 if (accept) {
                     w.cur[0] = nw[0]; w.cur[1] = nw[1];
@@ -1611,7 +1611,7 @@ __global__ void __launch_bounds__(kMoveThreads, 1) kWlCells(const SweepArgs* __r
             const int cell = w.cell[q];
             if (cell >= 0 && !(q == 1 && cell == w.cell[0])) others -= a.cellCount[cell];
         }
-        w.hist[wlIndex(w, w.cur)] += others;
+        atomicAdd((unsigned long long*)&w.tab->hist[wlIndex(w, w.cur)], (unsigned long long)others);
     }
     if (w.needCM) {
         wlCentre(a, w);
@@ -1640,7 +1640,7 @@ __global__ void kWlAfterChains(const SweepArgs* __restrict__ A) {
     if (!a.wl || threadIdx.x != 0 || blockIdx.x != 0) return;
     WlDev& w = *a.wl;
     const unsigned long long seen = a.counters[C_ACC_CH] + a.counters[C_REJ_CH];
-    w.hist[wlIndex(w, w.cur)] += (long long)(seen - w.chainSeen);
+    atomicAdd((unsigned long long*)&w.tab->hist[wlIndex(w, w.cur)], seen - w.chainSeen);
     w.chainSeen = seen;
 }
 
@@ -1648,19 +1648,22 @@ __global__ void kWlAfterChains(const SweepArgs* __restrict__ A) {
 // the smallest bin count exceeds WL_MINHIST and temper * log(max / min) < WL_GERR (max / min
 // an integer quotient, as the reference's longs give), alpha is halved, the histogram
 // cleared and the weights shifted by the first bin's; below WL_ALPHATOL the run is over.
+// A table shared by several walkers is checked by its owner only (the reference's rank 0),
+// after every walker's moves of the sweep.
 __global__ void kWlEndSweep(const SweepArgs* __restrict__ A) {
     const SweepArgs& a = A[blockIdx.y];
-    if (!a.wl || blockIdx.x != 0) return;
-    WlDev& w = *a.wl;
-    if (!(w.alpha > 0.0) || w.converged || a.ctl->sweep % kWlUpdateEvery != 0) return;
+    if (!a.wl || blockIdx.x != 0 || !a.wl->owner) return;
+    const WlDev& w = *a.wl;
+    WlTable& t = *w.tab;
+    if (!(t.alpha > 0.0) || t.converged || a.ctl->sweep % kWlUpdateEvery != 0) return;
     __shared__ long long smin[32], smax[32];
     __shared__ int flat;
     __shared__ double wmin;
     const long long nb = (long long)w.len[0] * w.len[1];
-    long long mn = w.hist[0], mx = w.hist[0];
+    long long mn = t.hist[0], mx = t.hist[0];
     for (long long i = threadIdx.x; i < nb; i += blockDim.x) {
-        mn = min(mn, w.hist[i]);
-        mx = max(mx, w.hist[i]);
+        mn = min(mn, t.hist[i]);
+        mx = max(mx, t.hist[i]);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -1673,22 +1676,22 @@ __global__ void kWlEndSweep(const SweepArgs* __restrict__ A) {
         for (int q = 0; q < (int)(blockDim.x >> 5); ++q) { mn = min(mn, smin[q]); mx = max(mx, smax[q]); }
         flat = 0;
         if (mn > kWlMinHist && a.temper * log((double)(mx / mn)) < kWlGerr) {
-            if (w.alpha < kWlAlphaTol) w.converged = 1;
+            if (t.alpha < kWlAlphaTol) t.converged = 1;
             else flat = 1;
         }
-        wmin = wlWeight(w, 0);
+        wmin = wlWeight(t, 0);
     }
     __syncthreads();
     if (!flat) return;
     for (long long i = threadIdx.x; i < nb; i += blockDim.x) {
-        w.base[i] = wlWeight(w, i) - wmin;
-        w.hist[i] = 0;
-        w.hist0[i] = 0;
+        t.base[i] = wlWeight(t, i) - wmin;
+        t.hist[i] = 0;
+        t.hist0[i] = 0;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        w.alpha /= 2.0;
-        w.updates += 1;
+        t.alpha /= 2.0;
+        t.updates += 1;
     }
 }
 
@@ -2357,7 +2360,7 @@ __global__ void kVolumeAccept(const SweepArgs* __restrict__ A) {
             }
         }
         inRange = wlInRange(w, nw);
-        if (inRange) energy += wlWeight(w, wlIndex(w, nw)) - wlWeight(w, wlIndex(w, w.cur));
+        if (inRange) energy += wlWeight(*w.tab, wlIndex(w, nw)) - wlWeight(*w.tab, wlIndex(w, w.cur));
     }
     bool accept = inRange && ((enermove <= energy) || (exp(-1.0 * (enermove - energy) / a.temper) > u));
     if (accept) {
@@ -3239,9 +3242,9 @@ int runReplicas(void* h, const sc_run_params& p, int exchangeEvery, sc_run_stats
     for (int k = 0; k < nrep; ++k) {
         Context* c = b.sys[k];
         if (c->conf.p.empty()) return fail(SC_ERR_ARG, "a replica holds no particles");
-        if (wlActive(c))
-            return fail(SC_ERR_UNSUPPORTED, "Wang-Landau weights in a replica batch (the exchange would need their terms, "
-                                            "movecreator.cpp:736-740): run the walker with sc_simulate");
+        if (wlActive(c) && exchangeEvery > 0)
+            return fail(SC_ERR_UNSUPPORTED, "Wang-Landau weights with replica exchange (the exchange would need their "
+                                            "terms, movecreator.cpp:736-740); walkers run with exchange_every = 0");
         sc_run_params q = p;
         sc_default_run(reinterpret_cast<const sc_context*>(c), &q);   // per-replica step sizes
         q.nsweeps = p.nsweeps; q.seed = p.seed + 0x9E3779B97F4A7C15ull * (unsigned long long)(k + 1);
@@ -3249,6 +3252,7 @@ int runReplicas(void* h, const sc_run_params& p, int exchangeEvery, sc_run_stats
         q.stencil = p.stencil; q.time_phases = p.time_phases; q.press = p.press; q.delayed = p.delayed;
         q.variant = p.variant;
         if (p.delayed && !c->surrogate) return fail(SC_ERR_STATE, "delayed = 1 needs a surrogate on every replica");
+        if ((rc = wlCheckRun(c, q))) return rc;
         if (p.transmx > 0) q.transmx = p.transmx;
         if (p.rot_angle > 0) q.rot_angle = p.rot_angle;
         q.chainprob = p.chainprob;
@@ -3310,7 +3314,7 @@ int runReplicas(void* h, const sc_run_params& p, int exchangeEvery, sc_run_stats
         st.da_err_rms = std::sqrt(st.da_err_rms / (double)st.da_stage2_tried);
         st.da_err_mean /= (double)st.da_stage2_tried;
     }
-    st.sweeps = p.nsweeps;
+    st.sweeps = out.sweeps;
     st.seconds = out.seconds;
     st.phase_seconds = out.phaseSeconds;
     st.phase_launches = out.phaseLaunches;

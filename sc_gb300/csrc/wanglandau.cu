@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <sstream>
 #include <string>
 #include <vector>
@@ -18,13 +19,30 @@ namespace scg {
 
 bool readFile(const char* path, std::string& out);   // sc_context.cu
 
-struct WlHost {
-    WlDev h{};                       // host values; h.base / h.hist / h.hist0 are device arrays
+// Weights and histogram of one run, shared by its walkers (sc_wl_share).
+struct WlTableHost {
+    WlTable h{};                     // host values; h.base / h.hist / h.hist0 are device arrays
     std::vector<double> base;        // host copies of the arrays
     std::vector<long long> hist, hist0;
-    WlDev* d = nullptr;              // the device record
+    WlTable* d = nullptr;            // the device record
     int device = -1;
     bool onDevice = false;           // the device copy is the current one
+    ~WlTableHost() {
+        if (!d) return;
+        cudaSetDevice(device);
+        cudaFree(d);
+        cudaFree(h.base);
+        cudaFree(h.hist);
+        cudaFree(h.hist0);
+    }
+};
+
+struct WlHost {
+    WlDev h{};                       // host values of the walker record (h.tab: device table)
+    std::shared_ptr<WlTableHost> T;  // its table
+    WlDev* d = nullptr;              // the device record
+    int device = -1;
+    bool onDevice = false;
 };
 
 // Bins of the current configuration (WangLandau::init): order 1 needs the system centre
@@ -85,10 +103,11 @@ static int wlParse(const std::string& text, WlHost& W, std::string& err) {
     int i = 0, fields = 0;
     double f[4] = {0, 0, 0, 0};
     WlDev& w = W.h;
+    WlTableHost& T = *W.T;
     w.len[0] = 0;
     w.len[1] = 0;
-    W.base.clear();
-    W.hist.clear();
+    T.base.clear();
+    T.hist.clear();
     while (std::getline(in, line)) {
         size_t hash = line.find('#');
         if (hash != std::string::npos) line.resize(hash);
@@ -96,28 +115,28 @@ static int wlParse(const std::string& text, WlHost& W, std::string& err) {
         if (a == std::string::npos) continue;
         line = line.substr(a, b - a + 1);
         if (i == 0) {
-            if (sscanf(line.c_str(), "%le", &w.alpha) != 1) { err = "Wang-Landau file: could not read alpha at the beginning"; return SC_ERR_PARSE; }
+            if (sscanf(line.c_str(), "%le", &T.h.alpha) != 1) { err = "Wang-Landau file: could not read alpha at the beginning"; return SC_ERR_PARSE; }
             ++i;
             continue;
         }
         fields = sscanf(line.c_str(), "%le %le %le %le", &f[0], &f[1], &f[2], &f[3]);
         if (fields == 3) {
             if (i == 1) w.minorder[0] = f[0];
-            W.base.push_back(f[1]);
-            W.hist.push_back((long long)f[2]);
+            T.base.push_back(f[1]);
+            T.hist.push_back((long long)f[2]);
             w.len[0]++;
         } else if (fields == 4) {
             if (i == 1) { w.minorder[0] = f[0]; w.minorder[1] = f[1]; }
             if (w.minorder[1] == f[1]) w.len[0]++;
-            W.base.push_back(f[2]);
-            W.hist.push_back((long long)f[3]);
+            T.base.push_back(f[2]);
+            T.hist.push_back((long long)f[3]);
         } else {
             err = "Wang-Landau file: could not read the order parameter at line " + std::to_string(i);
             return SC_ERR_PARSE;
         }
         ++i;
     }
-    const long total = (long)W.base.size();
+    const long total = (long)T.base.size();
     if (total < 2 || w.len[0] < 2) { err = "Wang-Landau file: fewer than two bins"; return SC_ERR_PARSE; }
     if (fields == 4) {
         w.len[1] = (int)(total / w.len[0]);
@@ -136,8 +155,8 @@ static int wlParse(const std::string& text, WlHost& W, std::string& err) {
     }
     w.dorder[0] = (f[0] - w.minorder[0]) / (w.len[0] - 1);
     // WangLandau::init: a negligible alpha samples with fixed weights
-    if (w.alpha < kWlAlphaTol / 100) w.alpha = 0.0;
-    W.hist0 = W.hist;
+    if (T.h.alpha < kWlAlphaTol / 100) T.h.alpha = 0.0;
+    T.hist0 = T.hist;
     return SC_OK;
 }
 
@@ -162,68 +181,90 @@ int wlCheckRun(const Context* c, const sc_run_params& p) {
     return SC_OK;
 }
 
-static int wlUpload(Context* c, bool arrays) {
-    WlHost& W = *c->wl;
-    const size_t nb = W.base.size();
+// The table on the device (allocated on first use; arrays copied when `arrays`).
+static int tableUpload(WlTableHost& T, int device, bool arrays) {
+    const size_t nb = T.base.size();
     cudaError_t r;
-    if (!W.d || W.device != c->device) {
-        if ((r = cudaMalloc((void**)&W.d, sizeof(WlDev))) != cudaSuccess) return cudaFail(r, "cudaMalloc (Wang-Landau)");
-        if ((r = cudaMalloc((void**)&W.h.base, sizeof(double) * nb)) != cudaSuccess) return cudaFail(r, "cudaMalloc (Wang-Landau)");
-        if ((r = cudaMalloc((void**)&W.h.hist, sizeof(long long) * nb)) != cudaSuccess) return cudaFail(r, "cudaMalloc (Wang-Landau)");
-        if ((r = cudaMalloc((void**)&W.h.hist0, sizeof(long long) * nb)) != cudaSuccess) return cudaFail(r, "cudaMalloc (Wang-Landau)");
-        W.device = c->device;
+    cudaSetDevice(device);
+    if (!T.d) {
+        if ((r = cudaMalloc((void**)&T.d, sizeof(WlTable))) != cudaSuccess) return cudaFail(r, "cudaMalloc (Wang-Landau)");
+        if ((r = cudaMalloc((void**)&T.h.base, sizeof(double) * nb)) != cudaSuccess) return cudaFail(r, "cudaMalloc (Wang-Landau)");
+        if ((r = cudaMalloc((void**)&T.h.hist, sizeof(long long) * nb)) != cudaSuccess) return cudaFail(r, "cudaMalloc (Wang-Landau)");
+        if ((r = cudaMalloc((void**)&T.h.hist0, sizeof(long long) * nb)) != cudaSuccess) return cudaFail(r, "cudaMalloc (Wang-Landau)");
+        T.device = device;
         arrays = true;
     }
     if (arrays) {
-        cudaMemcpy(W.h.base, W.base.data(), sizeof(double) * nb, cudaMemcpyHostToDevice);
-        cudaMemcpy(W.h.hist, W.hist.data(), sizeof(long long) * nb, cudaMemcpyHostToDevice);
-        cudaMemcpy(W.h.hist0, W.hist0.data(), sizeof(long long) * nb, cudaMemcpyHostToDevice);
+        cudaMemcpy(T.h.base, T.base.data(), sizeof(double) * nb, cudaMemcpyHostToDevice);
+        cudaMemcpy(T.h.hist, T.hist.data(), sizeof(long long) * nb, cudaMemcpyHostToDevice);
+        cudaMemcpy(T.h.hist0, T.hist0.data(), sizeof(long long) * nb, cudaMemcpyHostToDevice);
     }
-    if ((r = cudaMemcpy(W.d, &W.h, sizeof(WlDev), cudaMemcpyHostToDevice)) != cudaSuccess)
-        return cudaFail(r, "upload Wang-Landau record");
-    W.onDevice = true;
+    if ((r = cudaMemcpy(T.d, &T.h, sizeof(WlTable), cudaMemcpyHostToDevice)) != cudaSuccess)
+        return cudaFail(r, "upload Wang-Landau table");
+    T.onDevice = true;
     return SC_OK;
 }
 
-// The device copy back to the host (arrays and record).
+// The device copies back to the host: the walker's record and its table (every walker of a
+// shared table may have moved: the whole device is synchronised).
 static int wlDownload(Context* c) {
     WlHost& W = *c->wl;
-    if (!W.onDevice) return SC_OK;
-    cudaSetDevice(c->device);
-    if (c->stream) cudaStreamSynchronize(c->stream);
-    WlDev rec;
-    cudaError_t r = cudaMemcpy(&rec, W.d, sizeof rec, cudaMemcpyDeviceToHost);
-    if (r != cudaSuccess) return cudaFail(r, "download Wang-Landau record");
-    const size_t nb = W.base.size();
-    cudaMemcpy(W.base.data(), W.h.base, sizeof(double) * nb, cudaMemcpyDeviceToHost);
-    cudaMemcpy(W.hist.data(), W.h.hist, sizeof(long long) * nb, cudaMemcpyDeviceToHost);
-    cudaMemcpy(W.hist0.data(), W.h.hist0, sizeof(long long) * nb, cudaMemcpyDeviceToHost);
-    W.h = rec;
+    WlTableHost& T = *W.T;
+    cudaError_t r;
+    if (W.onDevice) {
+        cudaSetDevice(W.device);
+        cudaDeviceSynchronize();
+        if ((r = cudaMemcpy(&W.h, W.d, sizeof(WlDev), cudaMemcpyDeviceToHost)) != cudaSuccess)
+            return cudaFail(r, "download Wang-Landau record");
+    }
+    if (T.onDevice) {
+        cudaSetDevice(T.device);
+        cudaDeviceSynchronize();
+        if ((r = cudaMemcpy(&T.h, T.d, sizeof(WlTable), cudaMemcpyDeviceToHost)) != cudaSuccess)
+            return cudaFail(r, "download Wang-Landau table");
+        const size_t nb = T.base.size();
+        cudaMemcpy(T.base.data(), T.h.base, sizeof(double) * nb, cudaMemcpyDeviceToHost);
+        cudaMemcpy(T.hist.data(), T.h.hist, sizeof(long long) * nb, cudaMemcpyDeviceToHost);
+        cudaMemcpy(T.hist0.data(), T.h.hist0, sizeof(long long) * nb, cudaMemcpyDeviceToHost);
+    }
     return SC_OK;
 }
 
 int wlPrepare(Context* c, bool hostChanged) {
     if (!wlActive(c)) return SC_OK;
     WlHost& W = *c->wl;
+    WlTableHost& T = *W.T;
     std::string err;
     int rc;
+    cudaError_t r;
     if (W.onDevice) {
-        // the device record is the current one (bins, centre, alpha, flags)
+        // the device record is the current one (bins, centre)
         if (c->stream) cudaStreamSynchronize(c->stream);
-        cudaError_t r = cudaMemcpy(&W.h, W.d, sizeof(WlDev), cudaMemcpyDeviceToHost);
-        if (r != cudaSuccess) return cudaFail(r, "download Wang-Landau record");
-        // the caller replaced the state: the bins and the centre follow it (the arrays stay)
+        if ((r = cudaMemcpy(&W.h, W.d, sizeof(WlDev), cudaMemcpyDeviceToHost)) != cudaSuccess)
+            return cudaFail(r, "download Wang-Landau record");
+        // the caller replaced the state: the bins and the centre follow it (the table stays)
         if (hostChanged && (rc = wlOrders(c, W.h, err))) return fail(rc, err);
+    }
+    if (T.onDevice && T.device != c->device)
+        return fail(SC_ERR_UNSUPPORTED, "Wang-Landau walkers sharing weights must be on one device");
+    if (!T.onDevice && (rc = tableUpload(T, c->device, true))) return rc;
+    if (!W.d) {
+        if ((r = cudaMalloc((void**)&W.d, sizeof(WlDev))) != cudaSuccess) return cudaFail(r, "cudaMalloc (Wang-Landau)");
+        W.device = c->device;
     }
     W.h.chainSeen = 0;          // the run's counters start from zero
     W.h.cell[0] = W.h.cell[1] = -1;
-    return wlUpload(c, !W.onDevice);
+    W.h.tab = T.d;
+    if ((r = cudaMemcpy(W.d, &W.h, sizeof(WlDev), cudaMemcpyHostToDevice)) != cudaSuccess)
+        return cudaFail(r, "upload Wang-Landau record");
+    W.onDevice = true;
+    return SC_OK;
 }
 
 bool wlConverged(Context* c) {
-    if (!wlActive(c) || !c->wl->onDevice) return false;
+    if (!wlActive(c) || !c->wl->T->onDevice) return false;
     int v = 0;
-    cudaMemcpy(&v, &c->wl->d->converged, sizeof v, cudaMemcpyDeviceToHost);
+    cudaMemcpy(&v, &c->wl->T->d->converged, sizeof v, cudaMemcpyDeviceToHost);
     return v != 0;
 }
 
@@ -233,11 +274,8 @@ void destroyWl(Context* c) {
     if (W.d) {
         cudaSetDevice(W.device);
         cudaFree(W.d);
-        cudaFree(W.h.base);
-        cudaFree(W.h.hist);
-        cudaFree(W.h.hist0);
     }
-    delete c->wl;
+    delete c->wl;       // the table goes with its last walker
     c->wl = nullptr;
 }
 
@@ -257,6 +295,7 @@ static int wlLoad(Context* c, const std::string& text) {
     int rc;
     if (c->devNewer && (rc = c->downloadState())) return rc;
     WlHost* W = new WlHost();
+    W->T = std::make_shared<WlTableHost>();
     std::string err;
     if ((rc = wlParse(text, *W, err))) { delete W; return fail(rc, err); }
     WlDev& w = W->h;
@@ -274,6 +313,7 @@ static int wlLoad(Context* c, const std::string& text) {
     w.part[0] = (uses[1] || uses[3] || uses[4]) ? 0 : -1;
     w.part[1] = uses[4] ? 1 : -1;
     w.cell[0] = w.cell[1] = -1;
+    w.owner = 1;
     if ((rc = wlOrders(c, w, err))) { delete W; return fail(rc, err); }
     destroyWl(c);
     c->wl = W;
@@ -282,13 +322,14 @@ static int wlLoad(Context* c, const std::string& text) {
 
 static std::string wlFormat(const WlHost& W, const std::vector<double>& wt) {
     const WlDev& w = W.h;
+    const WlTableHost& T = *W.T;
     std::string s;
     char b[128];
-    snprintf(b, sizeof b, "%15.8e \n", w.alpha);
+    snprintf(b, sizeof b, "%15.8e \n", T.h.alpha);
     s += b;
     if (w.dim == 1) {
         for (int i = 0; i < w.len[0]; ++i) {
-            snprintf(b, sizeof b, "%15.8e %15.8e %ld \n", w.minorder[0] + i * w.dorder[0], wt[i], (long)W.hist[i]);
+            snprintf(b, sizeof b, "%15.8e %15.8e %ld \n", w.minorder[0] + i * w.dorder[0], wt[i], (long)T.hist[i]);
             s += b;
         }
     } else {
@@ -296,7 +337,7 @@ static std::string wlFormat(const WlHost& W, const std::vector<double>& wt) {
             for (int i = 0; i < w.len[0]; ++i) {
                 const size_t k = (size_t)i + (size_t)w.len[0] * j;
                 snprintf(b, sizeof b, "%15.8e %15.8e %15.8e %ld \n", w.minorder[0] + i * w.dorder[0],
-                         w.minorder[1] + j * w.dorder[1], wt[k], (long)W.hist[k]);
+                         w.minorder[1] + j * w.dorder[1], wt[k], (long)T.hist[k]);
                 s += b;
             }
             s += " \n";
@@ -306,9 +347,35 @@ static std::string wlFormat(const WlHost& W, const std::vector<double>& wt) {
 }
 
 static std::vector<double> wlWeights(const WlHost& W) {
-    std::vector<double> wt(W.base.size());
-    for (size_t i = 0; i < wt.size(); ++i) wt[i] = W.base[i] - W.h.alpha * (double)(W.hist[i] - W.hist0[i]);
+    const WlTableHost& T = *W.T;
+    std::vector<double> wt(T.base.size());
+    for (size_t i = 0; i < wt.size(); ++i) wt[i] = T.base[i] - T.h.alpha * (double)(T.hist[i] - T.hist0[i]);
     return wt;
+}
+
+// Walkers 1..n-1 take walker 0's table: the reference's multiple walkers, which update one
+// set of weights and one histogram (MPI shared windows, wanglandau.cpp:184-218); walker 0
+// runs the flatness checks (update() on rank 0, wanglandau.h:66-120).
+static int wlShare(Context* const* ws, int n) {
+    if (n < 1) return fail(SC_ERR_ARG, "no walkers");
+    for (int k = 0; k < n; ++k)
+        if (!ws[k] || !wlActive(ws[k])) return fail(SC_ERR_STATE, "every walker needs Wang-Landau weights loaded");
+    const WlDev& a = ws[0]->wl->h;
+    for (int k = 1; k < n; ++k) {
+        const WlDev& b = ws[k]->wl->h;
+        bool same = a.dim == b.dim && a.len[0] == b.len[0] && a.len[1] == b.len[1];
+        for (int q = 0; q < 2 && same; ++q)
+            same = a.wlm[q] == b.wlm[q] && a.minorder[q] == b.minorder[q] && a.dorder[q] == b.dorder[q];
+        if (!same) return fail(SC_ERR_ARG, "Wang-Landau walkers sharing weights need the same order parameters and bins");
+        if (ws[k]->device != ws[0]->device) return fail(SC_ERR_ARG, "walkers sharing weights must be on one device");
+    }
+    for (int k = 1; k < n; ++k) {
+        if (ws[k]->wl->T == ws[0]->wl->T) continue;
+        ws[k]->wl->T = ws[0]->wl->T;
+        ws[k]->wl->h.owner = 0;
+    }
+    ws[0]->wl->h.owner = 1;
+    return SC_OK;
 }
 
 }  // namespace scg
@@ -355,11 +422,19 @@ int sc_wl_get_info(sc_context* ctx, sc_wl_info* out) {
     }
     out->length[0] = w.len[0];
     out->length[1] = w.dim == 2 ? w.len[1] : 0;
-    out->alpha = w.alpha;
-    out->updates = (long)w.updates;
-    out->converged = w.converged;
+    const WlTable& t = ctx->wl->T->h;
+    out->alpha = t.alpha;
+    out->updates = (long)t.updates;
+    out->converged = t.converged;
     for (int d = 0; d < 3; ++d) out->syscm[d] = w.syscm[d];
     return SC_OK;
+}
+
+int sc_wl_share(sc_context* const* walkers, int n) {
+    if (!walkers) return fail(SC_ERR_ARG, "null argument");
+    std::vector<Context*> ws(n > 0 ? n : 0);
+    for (int k = 0; k < n; ++k) ws[k] = walkers[k];
+    return wlShare(ws.data(), n);
 }
 
 int sc_wl_get(sc_context* ctx, double* weights, long* hist) {
@@ -371,7 +446,7 @@ int sc_wl_get(sc_context* ctx, double* weights, long* hist) {
     std::vector<double> wt = wlWeights(W);
     for (size_t i = 0; i < wt.size(); ++i) {
         if (weights) weights[i] = wt[i];
-        if (hist) hist[i] = (long)W.hist[i];
+        if (hist) hist[i] = (long)W.T->hist[i];
     }
     return SC_OK;
 }

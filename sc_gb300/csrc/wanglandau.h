@@ -13,7 +13,10 @@
 // Weights are kept as w[i] = base[i] - alpha * (hist[i] - hist0[i]): base and hist0 are
 // set when alpha changes, hist counts visits as the reference's histogram does, so the
 // weight decrements of all moves are integer counts (exact, independent of the order in
-// which concurrent updates land).
+// which concurrent updates land).  The table (alpha, weights, histogram) can be shared by
+// several walkers -- the reference's multiple walkers, which share weights and histogram
+// through MPI shared-memory windows (wanglandau.cpp:184-218) -- while each walker keeps its
+// own bins and system centre.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -25,6 +28,18 @@ constexpr double kWlAlphaTol = 1.0e-8;    // WL_ALPHATOL macros.h:104
 constexpr long kWlMinHist = 1000;         // WL_MINHIST  macros.h:105
 constexpr int kWlUpdateEvery = 1000;      // sweeps between flatness checks, updater.cpp:255
 
+// Weights and histogram, shared by the walkers of one Wang-Landau run.
+struct WlTable {
+    double alpha;
+    long long updates;       // alpha halvings so far
+    int converged;           // update() found a flat histogram with alpha below tolerance
+    int pad_;
+    double* base;            // weights when alpha last changed
+    long long* hist;         // histogram (reset when alpha changes)
+    long long* hist0;        // histogram when alpha last changed
+};
+
+// One walker: its bins, system centre and the table it biases with.
 struct WlDev {
     int dim;                 // 1 or 2 order parameters
     int wlm[2];              // order parameter kinds (0: none)
@@ -32,24 +47,18 @@ struct WlDev {
     int part[2];             // particles whose moves change the orders (-1: none)
     int cell[2];             // their cells in the current sweep (written by kAssign)
     int needCM;              // order 1 in use: the system centre is tracked
-    int converged;           // update() found a flat histogram with alpha below tolerance
-    int volDone;             // this sweep's volume move counted (kVolumeAccept)
+    int owner;               // this walker runs the table's flatness checks
     double minorder[2], dorder[2];
-    double alpha;
     double sysvol;           // sum of the particles' Ia_param volumes (Conf::sysvolume)
     double cmK[3];           // sum of volume * anInt(position) when the orders were set up
     double syscm[3];         // volume-weighted centre, box fractions (Conf::syscm)
     long long cur[2];        // current bins
-    long long curBeforeVol;  // bin before this sweep's volume move
-    long long updates;       // alpha halvings so far
     unsigned long long chainSeen;   // chain-move attempts already counted
-    double* base;            // weights when alpha last changed
-    long long* hist;         // histogram (reset when alpha changes)
-    long long* hist0;        // histogram when alpha last changed
+    WlTable* tab;            // weights and histogram (device)
 };
 
-__host__ __device__ inline double wlWeight(const WlDev& w, long long i) {
-    return w.base[i] - w.alpha * (double)(w.hist[i] - w.hist0[i]);
+__host__ __device__ inline double wlWeight(const WlTable& t, long long i) {
+    return t.base[i] - t.alpha * (double)(t.hist[i] - t.hist0[i]);
 }
 __host__ __device__ inline long long wlIndex(const WlDev& w, const long long o[2]) {
     return o[0] + o[1] * (long long)w.len[0];

@@ -222,6 +222,14 @@ class System:
         L.check(self._lib.sc_wl_get(self._h, _dptr(w), h.ctypes.data_as(C.POINTER(C.c_long))))
         return w, h
 
+    @staticmethod
+    def wl_share(walkers):
+        """Walkers 1.. update walkers[0]'s weights and histogram (the reference's multiple
+        walkers); run them together in a ReplicaSet with exchange_every = 0."""
+        lib = L.load()
+        hs = (C.c_void_p * len(walkers))(*[w._h for w in walkers])
+        L.check(lib.sc_wl_share(hs, len(walkers)))
+
     def wl_write(self, path):
         L.check(self._lib.sc_wl_write(self._h, str(path).encode()))
 

@@ -188,3 +188,47 @@ def test_chain_moves_visit_the_current_bin(variant):
     assert st.max_drift <= 1e-9 * max(1.0, abs(st.energy)), (st.max_drift, st.energy)
     assert i.currorder[1] == math.floor((parts[0].dir[2] - i.minorder[1]) / i.dorder[1])
     assert i.currorder[0] == math.ceil(((parts[0].pos[2] - i.syscm[2]) * box[2] - i.minorder[0]) / i.dorder[0])
+
+
+def test_walkers_share_one_table():
+    # four walkers of the two-particle distance case update one table (the reference's
+    # multiple walkers): every walker's moves count in the shared histogram, the owner's
+    # flatness checks halve the shared alpha, and the weights approach the reference's
+    from sc_gb300 import ReplicaSet, System
+
+    c = CASES["o4_pair"]
+    inp = c["inputs"]
+    ws = []
+    for k in range(4):
+        s = System.from_text(inp["options"], inp["top.init"], inp["config.init"])
+        s.wl_load(text=inp["wl.dat"])
+        ws.append(s)
+    System.wl_share(ws)
+    R = ReplicaSet(ws, temperatures=[1.0] * 4)
+    st, _, _, _, _ = R.run(400, exchange_every=0, seed=4, variant=4)
+    _, h = ws[2].wl_weights()
+    assert int(h.sum()) == st.moves == 4 * 400 * c["n"]
+    for s in ws:
+        i = s.wl_info()
+        parts = s.particles()
+        box = s.box
+        dx, dy = parts[0].pos[0] - parts[1].pos[0], parts[0].pos[1] - parts[1].pos[1]
+        rx, ry = box[0] * (dx - np.rint(dx)), box[1] * (dy - np.rint(dy))
+        assert i.currorder[0] == math.ceil((math.sqrt(rx * rx + ry * ry) - i.minorder[0]) / i.dorder[0])
+    st, _, _, _, _ = R.run(20000, exchange_every=0, seed=5, variant=4)
+    infos = [s.wl_info() for s in ws]
+    assert len({(i.alpha, i.updates) for i in infos}) == 1          # one alpha for all walkers
+    assert infos[0].updates >= 6, infos[0].updates
+    w, _ = ws[0].wl_weights()
+    assert np.array_equal(w, ws[3].wl_weights()[0])
+    lo, hi = 2, 29
+    ref = np.array([r["weights"] for r in c["ref_runs"]])[:, lo:hi]
+    ref = (ref - ref.mean(1, keepdims=True)).mean(0)
+    got = w[lo:hi] - w[lo:hi].mean()
+    rms = float(np.sqrt(((got - ref) ** 2).mean()))
+    assert rms < 0.45, (rms, np.round(got, 2), np.round(ref, 2))
+    with pytest.raises(Exception):
+        R.run(10, exchange_every=5, seed=6)                         # no exchange with weights
+    R.close()
+    for s in ws:
+        s.close()
