@@ -537,6 +537,9 @@ def main():
     p.stencil, p.variant = best[0], best[1]
     # warm-up
     s.simulate(p, nsweeps=max(3, a.warmup))
+    # the state the timed sweeps start from: the end-to-end leg starts from it as well (an
+    # NPT system compresses while it runs, and denser states take longer per sweep)
+    start_state, start_box = s.particles(), s.box
     # the timed sweeps also time their move launches with CUDA events on the library's
     # stream (recorded around the launches, read after each sweep: no synchronisation inside)
     p.time_phases = 1
@@ -574,8 +577,9 @@ def main():
         t_max = float(t.item())
     value = moves * world / t_max
 
-    # end to end through the public API with host buffers
-    state = s.particles()
+    # end to end through the public API with host buffers, from the same start
+    state = start_state
+    s.box = start_box
     bytes_per_particle = C.sizeof(L.Particle)
     e2e_moves = 0
     t0 = time.perf_counter()
