@@ -1047,3 +1047,111 @@ extern "C" int or_wl_orders(const or_system* s, const int wlm[2], const double m
     }
     return 0;
 }
+
+// ---- Wang-Landau move loop ------------------------------------------------------------------
+// The reference's sequential loop with a Wang-Landau bias, single-particle moves only:
+// MoveCreator::partDisplace / partRotate with WangLandau::run / runRot (movecreator.cpp:
+// 947-1028, wanglandau.h:124-217): the bins after the move (order 1: the system centre moves
+// by volume * displacement / sysvolume, zDir :293-299; 3: zOrient of particle 0; 4:
+// twoPartDist), a bin outside the histogram rejects the move, else
+// moveTry(energy + w[new] - w[cur], enermove); then accept / reject (:262-290): the current
+// bin's weight drops by alpha and its count grows by one.  Every 1000 sweeps
+// WangLandau::update (:66-120, integer max / min) halves alpha when the histogram is flat;
+// below WL_ALPHATOL the run stops.
+extern "C" int or_wl_run(or_system* s, const or_mc_opts* o, or_wl* wl, or_mc_stats* st) {
+    std::memset(st, 0, sizeof(*st));
+    Rng rng{(uint64_t)o->seed * 0x2545F4914F6CDD1Dull + 1};
+    const int N = s->n;
+    if (N <= 0) return -1;
+    const int dim = wl->wlm[1] > 0 ? 2 : 1;
+    const long nb = (long)wl->len[0] * wl->len[1];
+    double sv = 0.0;
+    for (int i = 0; i < N; ++i) sv += P(s, s->p[i].type, s->p[i].type).volume;
+    or_vec cm = V(0, 0, 0);
+    for (int i = 0; i < N; ++i) {
+        const double v = P(s, s->p[i].type, s->p[i].type).volume;
+        const or_vec& r = s->p[i].pos;
+        cm.x += (r.x - anint(r.x)) * v; cm.y += (r.y - anint(r.y)) * v; cm.z += (r.z - anint(r.z)) * v;
+    }
+    cm.x /= sv; cm.y /= sv; cm.z /= sv;
+    auto idx = [&](const long* b) { return b[0] + b[1] * (long)wl->len[0]; };
+    auto inRange = [&](const long* b) {
+        for (int k = 0; k < dim; ++k)
+            if (b[k] < 0 || b[k] >= wl->len[k]) return false;
+        return true;
+    };
+    auto visit = [&]() {
+        wl->weights[idx(wl->cur)] -= wl->alpha;
+        wl->hist[idx(wl->cur)] += 1;
+    };
+    auto t0 = std::chrono::steady_clock::now();
+    long moves = 0;
+    for (long sweep = 1; sweep <= o->nsweeps; ++sweep) {
+        for (int step = 1; step <= N; ++step) {
+            if (o->max_moves > 0 && moves >= o->max_moves) goto finish;
+            ++moves;
+            int target = (int)(rng() * N);
+            or_particle orig = s->p[target];
+            const or_param& d = P(s, orig.type, orig.type);
+            const or_vec cmOld = cm;
+            double eold = or_one_to_all(s, target);
+            bool displace = (rng() < 0.5) || d.geotype[0] >= SP;
+            long nw[2] = {wl->cur[0], wl->cur[1]};
+            if (displace) {
+                or_vec dr = randomUnitSphere(rng);
+                dr.x *= o->transmx / s->box[0]; dr.y *= o->transmx / s->box[1]; dr.z *= o->transmx / s->box[2];
+                s->p[target].pos.x += dr.x; s->p[target].pos.y += dr.y; s->p[target].pos.z += dr.z;
+                for (int k = 0; k < dim; ++k) {
+                    if (wl->wlm[k] == 1) {
+                        cm.x += dr.x * d.volume / sv; cm.y += dr.y * d.volume / sv; cm.z += dr.z * d.volume / sv;
+                        nw[k] = (long)std::ceil(((s->p[0].pos.z - cm.z) * s->box[2] - wl->minorder[k]) / wl->dorder[k]);
+                    } else if (wl->wlm[k] == 4) {
+                        or_vec r = image(s->p[0].pos, s->p[1].pos, s->box);
+                        nw[k] = (long)std::ceil((std::sqrt(r.x * r.x + r.y * r.y) - wl->minorder[k]) / wl->dorder[k]);
+                    }
+                }
+            } else {
+                double ang = o->rot_angle * rng();
+                or_vec ax = randomUnitSphere(rng);
+                or_psc_rotate(&s->p[target], d.geotype[0], ang, ax, rng() < 0.5);
+                ortho(s->p[target].pd[0], s->p[target].dir);
+                for (int k = 0; k < dim; ++k)
+                    if (wl->wlm[k] == 3 && target == 0)
+                        nw[k] = (long)std::floor((s->p[0].dir.z - wl->minorder[k]) / wl->dorder[k]);
+            }
+            bool rej = !inRange(nw);
+            double wlener = 0.0, enew = 0.0;
+            if (!rej) {
+                wlener = wl->weights[idx(nw)] - wl->weights[idx(wl->cur)];
+                enew = or_one_to_all(s, target);
+                double eo = eold + wlener;
+                rej = !(enew <= eo) && !(exp(-1.0 * (enew - eo) / o->temper) > rng());
+            }
+            if (rej) {
+                s->p[target] = orig;
+                cm = cmOld;
+                if (displace) ++st->rej_trans; else ++st->rej_rot;
+            } else {
+                wl->cur[0] = nw[0]; wl->cur[1] = nw[1];
+                st->energy += enew - eold;
+                if (displace) ++st->acc_trans; else ++st->acc_rot;
+            }
+            visit();
+        }
+        if (wl->alpha > 0.0 && sweep % 1000 == 0) {
+            long mn = wl->hist[0], mx = wl->hist[0];
+            for (long i = 0; i < nb; ++i) { mn = std::min(mn, wl->hist[i]); mx = std::max(mx, wl->hist[i]); }
+            if (mn > 1000 && o->temper * std::log((double)(mx / mn)) < 0.0001) {
+                if (wl->alpha < 1.0e-8) { wl->converged = 1; break; }
+                wl->alpha /= 2.0;
+                wl->updates += 1;
+                const double wmin = wl->weights[0];
+                for (long i = 0; i < nb; ++i) { wl->hist[i] = 0; wl->weights[i] -= wmin; }
+            }
+        }
+    }
+finish:
+    st->moves = moves;
+    st->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return 0;
+}

@@ -107,6 +107,24 @@ typedef struct {
 
 int or_mc_run(or_system* s, const or_mc_opts* o, or_mc_stats* st);
 
+/* Wang-Landau table and walker state of or_wl_run. */
+typedef struct {
+    int wlm[2];
+    int len[2];            /* bins per order parameter (len[1] = 1 for one) */
+    double minorder[2], dorder[2];
+    double alpha;
+    double* weights;       /* len[0] * len[1], order 0 fastest; updated in place */
+    long* hist;
+    long cur[2];           /* current bins (set by the caller, e.g. from or_wl_orders) */
+    long updates;
+    int converged;
+    int pad_;
+} or_wl;
+
+/* The reference's sequential loop with a Wang-Landau bias (single-particle moves, order
+ * parameters 1, 3, 4), WangLandau::run / runRot / accept / reject / update. */
+int or_wl_run(or_system* s, const or_mc_opts* o, or_wl* wl, or_mc_stats* st);
+
 /* Wang-Landau starting bins (WangLandau::init, scOOP/mc/wanglandau.cpp:49-137) of order
  * parameters 1, 3, 4, 8, 9, with the system centre and sysvolume they use. */
 int or_wl_orders(const or_system* s, const int wlm[2], const double minorder[2], const double dorder[2], long out[2],

@@ -67,6 +67,12 @@ class McStats(C.Structure):
         ("energy", C.c_double), ("energy_start", C.c_double), ("seconds", C.c_double)]
 
 
+class WlState(C.Structure):
+    _fields_ = [("wlm", C.c_int * 2), ("len", C.c_int * 2), ("minorder", C.c_double * 2), ("dorder", C.c_double * 2),
+                ("alpha", C.c_double), ("weights", C.POINTER(C.c_double)), ("hist", C.POINTER(C.c_long)),
+                ("cur", C.c_long * 2), ("updates", C.c_long), ("converged", C.c_int), ("pad_", C.c_int)]
+
+
 _lib = None
 
 
@@ -91,6 +97,8 @@ def lib():
         L.or_psc_rotate.argtypes = [C.POINTER(Particle), C.c_int, C.c_double, Vec, C.c_int]
         L.or_mc_run.restype = C.c_int
         L.or_mc_run.argtypes = [C.POINTER(System), C.POINTER(McOpts), C.POINTER(McStats)]
+        L.or_wl_run.restype = C.c_int
+        L.or_wl_run.argtypes = [C.POINTER(System), C.POINTER(McOpts), C.POINTER(WlState), C.POINTER(McStats)]
         L.or_wl_orders.restype = C.c_int
         L.or_wl_orders.argtypes = [C.POINTER(System), C.POINTER(C.c_int), C.POINTER(C.c_double),
                                    C.POINTER(C.c_double), C.POINTER(C.c_long), C.POINTER(C.c_double),
@@ -175,6 +183,26 @@ class OracleSystem:
 
     def mol2others(self, first, size):
         return lib().or_mol2others(C.byref(self.sys), first, size)
+
+    def wl_run(self, opts, wlm, minorder, dorder, length, alpha, weights, hist):
+        """Sequential Wang-Landau run (or_wl_run); returns (weights, hist, state, stats)."""
+        w = np.ascontiguousarray(weights, dtype=np.float64).copy()
+        h = np.ascontiguousarray(hist, dtype=np.int64).copy()
+        st = WlState()
+        st.wlm[0], st.wlm[1] = wlm
+        st.len[0], st.len[1] = length
+        st.minorder[0], st.minorder[1] = minorder
+        st.dorder[0], st.dorder[1] = dorder
+        st.alpha = alpha
+        st.weights = w.ctypes.data_as(C.POINTER(C.c_double))
+        st.hist = h.ctypes.data_as(C.POINTER(C.c_long))
+        rc, cur, _, _ = self.wl_orders(wlm, minorder, dorder)
+        assert rc == 0
+        st.cur[0], st.cur[1] = cur
+        ms = McStats()
+        rc = lib().or_wl_run(C.byref(self.sys), C.byref(opts), C.byref(st), C.byref(ms))
+        assert rc == 0
+        return w, h, st, ms
 
     def wl_orders(self, wlm, minorder, dorder):
         """Starting Wang-Landau bins, system centre and sysvolume (or_wl_orders)."""

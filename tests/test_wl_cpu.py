@@ -4,7 +4,8 @@ The goldens (tests/golden/wl/cases.json.gz, made by tests/golden/make_wl.py) hol
 reference itself computes with its WangLandau::init and writes with WangLandau::write
 (scOOP/mc/wanglandau.cpp:49-166) for seeded systems and weights files.  Both the oracle's
 restatement (or_wl_orders) and the library's host code (sc_wl_load / sc_wl_get_info /
-sc_wl_write, which run before any device work) must reproduce them exactly.
+sc_wl_write, which run before any device work) must reproduce them exactly.  The oracle's
+sequential Wang-Landau loop (or_wl_run) is checked against the reference's own adaptive runs.
 """
 import gzip
 import json
@@ -143,3 +144,27 @@ def test_rejections(System):
     assert e.value.code == ERR_STATE
     s.close()
     s2.close()
+
+
+def test_oracle_wang_landau_run_matches_the_reference_runs():
+    # or_wl_run (the oracle's sequential loop with the bias) on the two-particle distance
+    # case: its adaptive weights match the reference's own runs of the same system
+    import numpy as np
+
+    c = next(c for c in CASES if c["name"] == "o4_pair")
+    ref = c["ref"]
+    o = O.OracleSystem(c["system"])
+    opts = O.McOpts()
+    opts.nsweeps, opts.seed, opts.temper = 60000, 7, 1.0
+    opts.transmx = 0.6                    # options transmx 0.3, doubled as sim.h:365 does
+    nb = ref["length"][0]
+    w, h, st, ms = o.wl_run(opts, (4, 0), ref["minorder"], ref["dorder"], (nb, 1), ref["alpha"],
+                            np.zeros(nb), np.zeros(nb, dtype=np.int64))
+    assert ms.moves == 60000 * c["n"]
+    assert st.updates >= 8, st.updates
+    lo, hi = 2, 29
+    R = np.array([r["weights"] for r in c["ref_runs"]])[:, lo:hi]
+    R = (R - R.mean(1, keepdims=True)).mean(0)
+    got = w[lo:hi] - w[lo:hi].mean()
+    rms = float(np.sqrt(((got - R) ** 2).mean()))
+    assert rms < 0.25, (rms, np.round(got, 2), np.round(R, 2))
