@@ -523,17 +523,6 @@ __device__ __forceinline__ bool screenedOut(const PairParam& pp, const double3& 
                         make_float3((float)d1.x, (float)d1.y, (float)d1.z), make_float3((float)d2.x, (float)d2.y, (float)d2.z));
 }
 
-// Prefetch of particle j's FP64 position, axis and patch vectors (the lines of its PatchSet)
-// into L1; j indexes the state arrays.
-__device__ __forceinline__ void prefetchParticle(const DevState& s, int j) {
-    const char* pt = reinterpret_cast<const char*>(&s.patch[j]);
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(&s.pos[j]));
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(&s.dir[j]));
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(pt));
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(pt + 128));
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(pt + sizeof(PatchSet) - 1));
-}
-
 __device__ __forceinline__ PView viewAt(const DevState& s, int j) {
     PView v;
     double4_32a p = s.pos[j];
@@ -1273,9 +1262,6 @@ __device__ __forceinline__ void moveCell(const SweepArgs& a, int cx, int cy, int
                     if (!keep) ++nScr;
                     else if (b & 2) ++kept1;
                     else ++kept0;
-                    // stage C reads the survivor's FP64 state and patch vectors: start them
-                    // towards L1 now, off the FP64 chain
-                    if (keep) prefetchParticle(a.s, candIdx[k]);
                 }
                 // one scan, three 10-bit counters: per-class offsets and totals
                 int total;
