@@ -2892,8 +2892,11 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
             b.evPhase.push_back(e);
         }
     }
-    static bool attrSet = false;
-    if (!attrSet) {
+    // the kernels' shared-memory limits are set once per device (an attribute of the
+    // device's context)
+    static unsigned long long attrSet = 0;
+    const unsigned long long devBit = 1ull << (b.device & 63);
+    if (!(attrSet & devBit)) {
         if ((r = cudaFuncSetAttribute(kColour, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDynSmemSurrogate)) !=
             cudaSuccess)
             return cudaFail(r, "shared memory attribute");
@@ -2918,7 +2921,7 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
         if ((r = cudaFuncSetAttribute(kWlCells, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDynSmemColour)) !=
             cudaSuccess)
             return cudaFail(r, "shared memory attribute");
-        attrSet = true;
+        attrSet |= devBit;
     }
     auto dims = [&](int x) { return dim3((unsigned)std::max(1, x), (unsigned)ns); };
     // systems with a surrogate stage their candidates' FP32 axes and patches as well
