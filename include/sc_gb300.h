@@ -186,6 +186,8 @@ int sc_trial_volume(sc_context* ctx, double psch, double* e_new);
 
 /* --- the move loop: Updater::simulate (scOOP/mc/updater.cpp:45-389) --------------------- */
 int sc_default_run(const sc_context* ctx, sc_run_params* p);
+/* Runs p->nsweeps sweeps on the device; stats->sweeps is the number run (fewer when a
+ * Wang-Landau run converged, as the reference's loop stops there, updater.cpp:255-265). */
 int sc_simulate(sc_context* ctx, const sc_run_params* p, sc_run_stats* stats);
 
 /* --- Wang-Landau flat-histogram sampling --------------------------------------------------

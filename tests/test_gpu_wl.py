@@ -232,3 +232,21 @@ def test_walkers_share_one_table():
     R.close()
     for s in ws:
         s.close()
+
+
+def test_run_stops_where_the_reference_stops(tmp_path):
+    # alpha below WL_ALPHATOL and a histogram that is flat at the first check (10^9 visits
+    # per bin): WangLandau::update reports convergence and the loop ends at that sweep
+    s, c = open_case("o4_pair")
+    lines = c["inputs"]["wl.dat"].splitlines()
+    text = "5e-9\n" + "".join(f"{l.split()[0]} 0.0 1000000000\n" for l in lines[1:])
+    s.wl_load(text=text)
+    p = s.default_run()
+    p.variant = 4
+    st = s.simulate(p, nsweeps=5000, seed=33)
+    i = s.wl_info()
+    assert st.sweeps == 1000 and st.moves == 1000 * c["n"]
+    assert i.converged == 1 and i.updates == 0 and i.alpha == 5e-9
+    s.wl_end(tmp_path / "wl-new.dat")
+    assert (tmp_path / "wl-new.dat").read_text().startswith(" 5.00000000e-09")
+    s.close()
