@@ -475,6 +475,34 @@ def bench_wl(steps, seed=1, warm=20):
             out["launches_per_sweep"] = launches / steps
         s.close()
     out["wl_cost"] = out["plain_moves_per_s"] / out["wang_landau_moves_per_s"]
+    # eight walkers updating one table (the reference's multiple walkers over MPI), moved
+    # by the same launches
+    from sc_gb300 import ReplicaSet
+
+    nw = 8
+    opts, top, cfg, wl = workloads.protein_bilayer(seed=seed, wlm=(1, 3), chainprob=0.0)
+    ws = []
+    for k in range(nw):
+        w = System.from_text(opts, top, cfg)
+        w.wl_load(text=wl)
+        ws.append(w)
+    System.wl_share(ws)
+    R = ReplicaSet(ws, temperatures=[1.0] * nw)
+    R.run(warm, exchange_every=0, seed=seed, stencil=1, variant=4)
+    dev = 0.0
+    moves = 0
+    for k in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        st, _, _, _, _ = R.run(1, exchange_every=0, seed=seed, stencil=1, variant=4)
+        dev += st.seconds
+        moves += st.moves
+    out["walkers"] = nw
+    out["walkers_moves_per_s"] = moves / dev
+    out["walkers_gain"] = out["walkers_moves_per_s"] / out["wang_landau_moves_per_s"]
+    R.close()
+    for w in ws:
+        w.close()
     return out
 
 
