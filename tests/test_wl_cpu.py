@@ -168,3 +168,26 @@ def test_oracle_wang_landau_run_matches_the_reference_runs():
     got = w[lo:hi] - w[lo:hi].mean()
     rms = float(np.sqrt(((got - R) ** 2).mean()))
     assert rms < 0.25, (rms, np.round(got, 2), np.round(R, 2))
+
+
+def test_share_checks_its_walkers(System):
+    from sc_gb300._lib import ScError
+
+    a = next(c for c in CASES if c["name"] == "o4_pair")
+    b = next(c for c in CASES if c["name"] == "o1_bath")
+    sa = System.from_text(a["inputs"]["options"], a["inputs"]["top.init"], a["inputs"]["config.init"])
+    sb = System.from_text(b["inputs"]["options"], b["inputs"]["top.init"], b["inputs"]["config.init"])
+    with pytest.raises(ScError) as e:
+        System.wl_share([sa, sb])                  # no weights loaded yet
+    assert e.value.code == ERR_STATE
+    sa.wl_load(text=a["inputs"]["wl.dat"])
+    sb.wl_load(text=b["inputs"]["wl.dat"])
+    with pytest.raises(ScError) as e:
+        System.wl_share([sa, sb])                  # other order parameters and bins
+    assert e.value.code == -1
+    s2 = System.from_text(a["inputs"]["options"], a["inputs"]["top.init"], a["inputs"]["config.init"])
+    s2.wl_load(text=a["inputs"]["wl.dat"])
+    System.wl_share([sa, s2])                      # same bins: one table
+    assert s2.wl_info().currorder[0] == sa.wl_info().currorder[0]
+    for s in (sa, sb, s2):
+        s.close()
