@@ -108,6 +108,18 @@ class Clocks:
                 "samples": len(sm)}
 
 
+def max_over_ranks(seconds, dist=None, device="cpu"):
+    """The slowest rank's time (the whole job's time: ranks run independent replicas, so
+    the job's moves/s is the sum of all ranks' moves over this time)."""
+    if dist is None:
+        return seconds
+    import torch
+
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -598,11 +610,7 @@ def main():
     if dist:
         dist.barrier()
     clk = clocks.stop()
-    t_max = dev_s
-    if dist:
-        t = torch.tensor([dev_s], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
+    t_max = max_over_ranks(dev_s, dist, f"cuda:{local}")
     value = moves * world / t_max
 
     # end to end through the public API with host buffers, from the same start
