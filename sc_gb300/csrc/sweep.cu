@@ -3146,6 +3146,15 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
     return SC_OK;
 }
 
+// Moves of the options that the GPU loop does not make.
+static int checkMoves(const Context* c) {
+    if (c->opts.coneAngle != 0.0)
+        return fail(SC_ERR_UNSUPPORTED, "options coneAngle != 0: rotations about axes in a cone around the particle "
+                                        "axis (MoveCreator::partAxialRotate, movecreator.cpp:1030-1073) are not on "
+                                        "the GPU path");
+    return SC_OK;
+}
+
 static int checkParams(const sc_run_params& p) {
     if (p.nsweeps < 0) return fail(SC_ERR_ARG, "nsweeps must be >= 0");
     if (!(p.temper > 0)) return fail(SC_ERR_ARG, "temper must be positive");
@@ -3161,6 +3170,7 @@ int runSweeps(Context* c, const sc_run_params& p, sc_run_stats& st) {
     if (rc) return rc;
     if (c->conf.p.empty()) return SC_OK;
     if (p.delayed && !c->surrogate) return fail(SC_ERR_STATE, "delayed = 1 needs a surrogate (sc_set_surrogate)");
+    if ((rc = checkMoves(c))) return rc;
     if ((rc = wlCheckRun(c, p))) return rc;
     const bool npt = p.volume_every > 0;
     if ((rc = prepareSystem(c, p, npt))) return rc;
@@ -3245,6 +3255,7 @@ int runReplicas(void* h, const sc_run_params& p, int exchangeEvery, sc_run_stats
     for (int k = 0; k < nrep; ++k) {
         Context* c = b.sys[k];
         if (c->conf.p.empty()) return fail(SC_ERR_ARG, "a replica holds no particles");
+        if ((rc = checkMoves(c))) return rc;
         if (wlActive(c) && exchangeEvery > 0)
             return fail(SC_ERR_UNSUPPORTED, "Wang-Landau weights with replica exchange (the exchange would need their "
                                             "terms, movecreator.cpp:736-740); walkers run with exchange_every = 0");

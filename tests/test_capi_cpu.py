@@ -100,6 +100,20 @@ def test_options_errors_are_reported_not_fatal(lib):
         System.open("/nonexistent/options", "/nonexistent/top", "/nonexistent/config")
 
 
+def test_moves_outside_the_gpu_loop_are_refused(lib):
+    # options coneAngle != 0 asks for MoveCreator::partAxialRotate (movecreator.cpp:1030-1073):
+    # the move loop refuses before touching the device
+    from sc_gb300 import ScError, System
+
+    g = goldens.load(NAMES[0])["inputs"]
+    opts = g["options"] + "coneAngle = 10.0\n"
+    s = System.from_text(opts, g["top.init"], g["config.init"])
+    with pytest.raises(ScError) as ei:
+        s.simulate(nsweeps=1)
+    assert ei.value.code == -7 and "coneAngle" in str(ei.value)
+    s.close()
+
+
 def test_write_config_format(lib, tmp_path):
     from sc_gb300 import System
 
