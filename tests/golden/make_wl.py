@@ -8,9 +8,9 @@ a weights file ``wl.dat``:
 * ``oracle/_ref/ref_dump`` (the reference's ``WangLandau::init`` and ``write``): the
   starting bins, the system centre and sysvolume, and the text the reference writes back
   for the weights it read;
-* ``oracle/_ref/sc_ref`` (the reference's own ``main``) for adaptive runs of the
-  two-particle distance case, several seeds: the weights and histogram it ends with
-  (``wl-new.dat``), for the convergence comparison.
+* ``oracle/_ref/sc_ref`` (the reference's own ``main``), several seeds: adaptive runs of
+  the two-particle distance case and fixed-weight runs of the orientation case, the weights
+  and histogram they end with (``wl-new.dat``), for the comparisons.
 
 Run here (needs the reference tree):  python tests/golden/make_wl.py
 """
@@ -182,11 +182,13 @@ def main():
                                                    "config.init": c["config"], "wl.dat": c["wl"]},
                      "ref": dump["wl"], "n": dump["n"],
                      "system": {k: dump[k] for k in ("box", "sqmaxcut", "ia_params", "particles", "molecules")}}
-            if c["name"] == "o4_pair":
+            if c["name"] in ("o4_pair", "o3_orient"):
                 # the reference's own adaptive runs, three seeds
                 runs = []
                 for seed in (101, 202, 303):
                     opts = dict(c["options"], seed=seed)
+                    if c["name"] == "o3_orient":
+                        opts["nsweeps"] = 20000
                     with open(os.path.join(tmp, "options"), "w") as f:
                         f.write(options_text(**opts))
                     with open(os.path.join(tmp, "wl.dat"), "w") as f:

@@ -191,3 +191,34 @@ def test_share_checks_its_walkers(System):
     assert s2.wl_info().currorder[0] == sa.wl_info().currorder[0]
     for s in (sa, sb, s2):
         s.close()
+
+
+def test_oracle_fixed_weights_bias_like_the_reference():
+    # fixed weights w = 1.5 o of particle 0's axis z component: the oracle's loop and the
+    # reference's own runs both give a histogram ln H = w / T + c (T = 1)
+    import math
+
+    import numpy as np
+
+    c = next(c for c in CASES if c["name"] == "o3_orient")
+    ref = c["ref"]
+    o = O.OracleSystem(c["system"])
+    opts = O.McOpts()
+    opts.nsweeps, opts.seed, opts.temper = 50000, 11, 1.0
+    opts.transmx = 0.4                          # options transmx 0.2, doubled (sim.h:365)
+    opts.rot_angle = 120.0 / 180.0 * math.pi / 2 * 0.5     # rotmx 120 (sim.h:359)
+    nb = ref["length"][0]
+    orders = -1.0 + 0.05 * np.arange(nb)
+    w, h, st, ms = o.wl_run(opts, (3, 0), ref["minorder"], ref["dorder"], (nb, 1), 0.0, 1.5 * orders,
+                            np.zeros(nb, dtype=np.int64))
+    assert st.updates == 0 and np.array_equal(w, 1.5 * orders)
+
+    def slope(hist):
+        hist = np.asarray(hist, float)[:40]
+        sel = hist > 0
+        return np.polyfit(orders[:40][sel], np.log(hist[sel]), 1, w=np.sqrt(hist[sel]))[0]
+
+    mine = slope(h)
+    theirs = [slope(r["hist"]) for r in c["ref_runs"]]
+    assert abs(mine - 1.5) < 0.2, mine
+    assert abs(mine - float(np.mean(theirs))) < 0.35, (mine, theirs)
