@@ -3038,6 +3038,12 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
         unsigned long long done = 0;
         cudaMemcpy(&done, &b.sys[0]->engine->ctl->sweep, sizeof done, cudaMemcpyDeviceToHost);
         nextWl = (long)(kWlUpdateEvery - (long)(done % kWlUpdateEvery));
+        bool allDone = true;
+        for (Context* c : b.sys) allDone &= wlConverged(c);
+        if (allDone) {              // an earlier call's flatness check ended the run
+            out.sweeps = 0;
+            return SC_OK;
+        }
     }
     out.sweeps = nsweeps;
     long sw = 0;

@@ -3,10 +3,23 @@
 The reference appends, every `report` sweeps, the exact total energy and the alignment
 order to energy.dat and the box volume to stat.dat (updater.cpp:313-318), every `movie`
 sweeps a frame to the movie file (Updater::dumpMovie, updater.h:82-93, with Conf::draw,
-Conf.h:388-424), and at the end writes config.last (Conf.h:413-422).  `run` does the same
-around blocks of GPU sweeps, in the reference's formats.
+Conf.h:388-424), and at the end writes config.last (Conf.h:413-422).  With Wang-Landau
+weights it also writes the weights file every `report` sweeps (WangLandau::write,
+updater.cpp:320-322), stops where the flatness schedule ends the run (updater.cpp:255-265)
+and writes the final file (WangLandau::endWangLandau, updater.cpp:388).  `run` does the
+same around blocks of GPU sweeps, in the reference's formats.
 """
 import os
+
+from ._lib import ScError
+
+
+def _has_wl(system):
+    try:
+        system.wl_info()
+        return True
+    except ScError:
+        return False
 
 
 def _frame(system, sweep):
@@ -21,10 +34,11 @@ def _frame(system, sweep):
     return "\n".join(lines) + "\n"
 
 
-def run(system, nsweeps, report=0, movie=0, directory=".", params=None, **overrides):
+def run(system, nsweeps, report=0, movie=0, directory=".", params=None, wl_file="wl-new.dat", **overrides):
     """Runs nsweeps sweeps on the GPU, writing energy.dat / stat.dat every `report` sweeps,
-    movie frames every `movie` sweeps and config.last at the end.  Returns the summed stats
-    counters (moves, acceptances) of the blocks."""
+    movie frames every `movie` sweeps and config.last at the end (and, with Wang-Landau
+    weights, `wl_file`).  Returns the summed stats counters (moves, acceptances) of the
+    blocks and the sweeps run."""
     p = params if params is not None else system.default_run()
     for k, v in overrides.items():
         setattr(p, k, v)
@@ -38,6 +52,8 @@ def run(system, nsweeps, report=0, movie=0, directory=".", params=None, **overri
         f.write("# sweep    volume\n")
     if movie:
         open(mf, "w").close()
+    wl = _has_wl(system)
+    wf = os.path.join(directory, wl_file)
     totals = {}
     sweep = 0
     next_dump = report if report > 0 else None
@@ -49,17 +65,24 @@ def run(system, nsweeps, report=0, movie=0, directory=".", params=None, **overri
         for name, _ in type(st)._fields_:
             if name.startswith(("acc_", "rej_", "moves", "pairs_")):
                 totals[name] = totals.get(name, 0) + getattr(st, name)
-        sweep += block
+        sweep += st.sweeps
+        if st.sweeps < block:           # Wang-Landau converged: the reference stops here
+            break
         if next_dump and sweep == next_dump:
             box = system.box
             with open(sf, "a") as f:
                 f.write(" %d; %.10f\n" % (sweep, box[0] * box[1] * box[2]))
             with open(ef, "a") as f:
                 f.write(" %d; %.10f  %f \n" % (sweep, system.all_to_all(), system.alignment_order()))
+            if wl:
+                system.wl_write(wf)
             next_dump += report
         if next_frame and sweep == next_frame:
             with open(mf, "a") as f:
                 f.write(_frame(system, sweep))
             next_frame += movie
     system.write_config(os.path.join(directory, "config.last"))
+    if wl:
+        system.wl_end(wf)
+    totals["sweeps"] = sweep
     return totals

@@ -35,3 +35,26 @@ def test_run_writes_the_reference_files(tmp_path):
     last = open(tmp_path / "config.last").read().splitlines()
     assert len(last) >= s.n + 1
     s.close()
+
+
+def test_run_writes_the_wang_landau_file_and_stops_where_the_reference_stops(tmp_path):
+    import gzip
+    import json
+
+    from sc_gb300 import System, updater
+
+    here = os.path.dirname(os.path.abspath(__file__))
+    with gzip.open(os.path.join(here, "golden", "wl", "cases.json.gz"), "rt") as f:
+        c = {c["name"]: c for c in json.load(f)["cases"]}["o4_pair"]
+    inp = c["inputs"]
+    s = System.from_text(inp["options"], inp["top.init"], inp["config.init"])
+    lines = inp["wl.dat"].splitlines()
+    # alpha below WL_ALPHATOL, a histogram flat at the first check: the run ends at sweep 1000
+    s.wl_load(text="5e-9\n" + "".join(f"{l.split()[0]} 0.0 1000000000\n" for l in lines[1:]))
+    totals = updater.run(s, 3000, report=500, directory=str(tmp_path), seed=5, variant=4)
+    assert totals["sweeps"] == 1000 and totals["moves"] == 1000 * s.n
+    e = [l for l in open(tmp_path / "energy.dat") if not l.startswith("#")]
+    assert [int(l.split(";")[0]) for l in e] == [500, 1000]
+    wl = open(tmp_path / "wl-new.dat").read().splitlines()
+    assert wl[0].strip() == "5.00000000e-09" and len(wl) == 1 + len(lines) - 1
+    s.close()
