@@ -222,3 +222,32 @@ def test_oracle_fixed_weights_bias_like_the_reference():
     theirs = [slope(r["hist"]) for r in c["ref_runs"]]
     assert abs(mine - 1.5) < 0.2, mine
     assert abs(mine - float(np.mean(theirs))) < 0.35, (mine, theirs)
+
+
+def test_weights_file_reader_follows_init_calc(System):
+    # WangLandau::initCalc: '#' comments and blank lines are skipped, alpha comes first, a
+    # grid of two order parameters needs whole rows; a negligible alpha means fixed weights
+    from sc_gb300._lib import ScError
+
+    c = next(c for c in CASES if c["name"] == "o4_pair")
+    inp = c["inputs"]
+    lines = inp["wl.dat"].splitlines()
+    noisy = "# weights\n\n" + lines[0] + "   # alpha\n" + "\n".join(l + "  # bin" for l in lines[1:]) + "\n\n"
+    s = System.from_text(inp["options"], inp["top.init"], inp["config.init"])
+    s.wl_load(text=noisy)
+    i = s.wl_info()
+    assert i.length[0] == len(lines) - 1 and i.currorder[0] == c["ref"]["currorder"][0]
+    s.wl_load(text="1e-11\n" + "\n".join(lines[1:]) + "\n")
+    assert s.wl_info().alpha == 0.0                     # below WL_ALPHATOL / 100
+    for bad in ("", "x\n0 0 0\n", lines[0] + "\n0.1 0 0\n", lines[0] + "\n0.1 0\n0.2 0\n"):
+        with pytest.raises(ScError) as e:
+            s.wl_load(text=bad)
+        assert e.value.code == ERR_PARSE
+    s.close()
+    d = next(c for c in CASES if c["name"] == "o8_o9")
+    rows = d["inputs"]["wl.dat"].splitlines()
+    s = System.from_text(d["inputs"]["options"], d["inputs"]["top.init"], d["inputs"]["config.init"])
+    with pytest.raises(ScError) as e:
+        s.wl_load(text="\n".join(rows[:-1]) + "\n")     # the last row one bin short
+    assert e.value.code == ERR_PARSE
+    s.close()
