@@ -199,6 +199,93 @@ def oracle_system(texts, seed):
     return sysm, o, len(parts), keep
 
 
+def _oracle_molecules(top, O):
+    """Molecule records of a top.init for the oracle: size, first particle, count and bond
+    constants of each [Molecules] entry in definition order (the molType index), placed in
+    the particle vector in [System] order (Inicializer::setParticlesParamss)."""
+    defs, order, key, cur = [], [], None, None
+    for raw in top.splitlines():
+        line = raw.split("#", 1)[0].strip()
+        if not line:
+            continue
+        if line.startswith("["):
+            key = line[1:].split("]")[0].strip().upper()
+            continue
+        if key == "MOLECULES":
+            if "{" in line:
+                cur = {"name": line.split(":")[0].strip(), "size": 0, "bonds": {}}
+                defs.append(cur)
+            elif line.startswith("}"):
+                cur = None
+            elif cur is not None and ":" in line:
+                k, v = line.split(":", 1)
+                k = k.strip().lower()
+                if k == "particles":
+                    cur["size"] += 1
+                else:
+                    cur["bonds"][k] = [float(x) for x in v.split()[:2]]
+        elif key == "SYSTEM":
+            name, cnt = line.split()[:2]
+            order.append((name, int(cnt)))
+    mols = (O.MolType * max(1, len(defs)))()
+    first = 0
+    starts = {}
+    for name, cnt in order:
+        d = next(d for d in defs if d["name"] == name)
+        starts.setdefault(name, (first, cnt))
+        first += d["size"] * cnt
+    for k, d in enumerate(defs):
+        m = mols[k]
+        m.size = d["size"]
+        m.first, m.count = starts.get(d["name"], (0, 0))
+        for b in ("bond1", "bond2", "bondd", "bondh", "angle1", "angle2"):
+            c, eq = d["bonds"].get(b, [-1.0, -1.0])
+            setattr(m, b + "c", c)
+            setattr(m, b + "eq", eq)
+    return mols, len(defs)
+
+
+def wl_cpu_baseline(texts, wl_text, seed, max_moves=3000):
+    """One core of the oracle's sequential loop with the Wang-Landau bias (or_wl_run, the
+    reference's partDisplace / partRotate with WangLandau::run / runRot) on a bounded
+    sample of the same system and weights: moves/s."""
+    import numpy as np
+
+    import oracle_ffi as O
+
+    opts, top, cfg = texts
+    sysm, o, n, keep = oracle_system(texts, seed)
+    mols, nmol = _oracle_molecules(top, O)
+    sysm.mols, sysm.nmol = C.cast(mols, C.POINTER(O.MolType)), nmol
+    rows = [l.split() for l in wl_text.splitlines() if l.strip()]
+    alpha, rows = float(rows[0][0]), [[float(x) for x in r] for r in rows[1:]]
+    two = len(rows[0]) == 4
+    o0 = sorted({r[0] for r in rows})
+    o1 = sorted({r[1] for r in rows}) if two else [0.0]
+    st = O.WlState()
+    wlm = [int(x) for x in next(l for l in opts.splitlines() if l.split("=")[0].strip() == "wlm").split("=")[1].split()]
+    st.wlm[0], st.wlm[1] = (wlm + [0])[:2]
+    st.len[0], st.len[1] = len(o0), len(o1)
+    st.minorder[0], st.minorder[1] = o0[0], o1[0]
+    st.dorder[0] = (o0[-1] - o0[0]) / (len(o0) - 1)
+    st.dorder[1] = (o1[-1] - o1[0]) / (len(o1) - 1) if two else 0.0
+    st.alpha = alpha
+    w = np.array([r[-2] for r in rows], dtype=np.float64)
+    h = np.array([r[-1] for r in rows], dtype=np.int64)
+    st.weights = w.ctypes.data_as(C.POINTER(C.c_double))
+    st.hist = h.ctypes.data_as(C.POINTER(C.c_long))
+    cur = (C.c_long * 2)()
+    cm = (C.c_double * 3)()
+    sv = C.c_double()
+    if O.lib().or_wl_orders(C.byref(sysm), st.wlm, st.minorder, st.dorder, cur, cm, C.byref(sv)) != 0:
+        raise RuntimeError("oracle: order parameters outside its restatement")
+    st.cur[0], st.cur[1] = cur[0], cur[1]
+    o.nsweeps, o.max_moves = 1 << 30, max_moves
+    ms = O.McStats()
+    O.lib().or_wl_run(C.byref(sysm), C.byref(o), C.byref(st), C.byref(ms))
+    return ms.moves / max(ms.seconds, 1e-12), ms.moves
+
+
 def cpu_run(texts, seed, nsweeps, max_moves):
     import oracle_ffi as O
 
@@ -487,6 +574,14 @@ def bench_wl(steps, seed=1, warm=20):
             out["launches_per_sweep"] = launches / steps
         s.close()
     out["wl_cost"] = out["plain_moves_per_s"] / out["wang_landau_moves_per_s"]
+    try:
+        opts, top, cfg, wl = workloads.protein_bilayer(seed=seed, wlm=(1, 3), chainprob=0.0)
+        rate, m = wl_cpu_baseline((opts, top, cfg), wl, seed)
+        out["cpu_port_moves_per_s"] = rate
+        out["cpu_port_sample"] = f"{m} moves, one core (oracle/sc_oracle.cpp or_wl_run: the reference's loop with the bias)"
+    except Exception as ex:      # the baseline is reported, not required
+        out["cpu_port_moves_per_s"] = None
+        out["cpu_port_sample"] = f"failed: {ex}"
     # eight walkers updating one table (the reference's multiple walkers over MPI), moved
     # by the same launches
     from sc_gb300 import ReplicaSet
