@@ -1049,7 +1049,7 @@ extern "C" int or_wl_orders(const or_system* s, const int wlm[2], const double m
 }
 
 // ---- Wang-Landau move loop ------------------------------------------------------------------
-// The reference's sequential loop with a Wang-Landau bias, single-particle moves only:
+// The reference's sequential loop with a Wang-Landau bias, single-particle and volume moves:
 // MoveCreator::partDisplace / partRotate with WangLandau::run / runRot (movecreator.cpp:
 // 947-1028, wanglandau.h:124-217): the bins after the move (order 1: the system centre moves
 // by volume * displacement / sysvolume, zDir :293-299; 3: zOrient of particle 0; 4:
@@ -1084,12 +1084,88 @@ extern "C" int or_wl_run(or_system* s, const or_mc_opts* o, or_wl* wl, or_mc_sta
         wl->weights[idx(wl->cur)] -= wl->alpha;
         wl->hist[idx(wl->cur)] += 1;
     };
+    const double shprob = o->shave / (double)N;
+    // MoveCreator::pressureMove (movecreator.cpp:330-546) with WangLandau::runPress
+    // (wanglandau.h:168-196): the bins of the trial box (order 1 keeps the centre, and ptype
+    // 2 keeps order 1; 4 the two particles' distance; 8 / 9 the box lengths)
+    auto volumeMove = [&]() {
+        const double energy = or_all_to_all(s);
+        const double b0[3] = {s->box[0], s->box[1], s->box[2]};
+        const double NT = (double)N * o->temper;
+        double enermove = 0.0;
+        switch (o->ptype) {
+        case 0: {
+            double rs = rng();
+            int side = rs < 1.0 / 3.0 ? 0 : (rs < 2.0 / 3.0 ? 1 : 2);
+            double area = side == 0 ? b0[1] * b0[2] : (side == 1 ? b0[0] * b0[2] : b0[0] * b0[1]);
+            s->box[side] += o->edge_mx * (rng() - 0.5);
+            enermove = o->press * area * (s->box[side] - b0[side]) - NT * log(s->box[side] / b0[side]);
+            break;
+        }
+        case 2: {
+            double psch = o->edge_mx * (rng() - 0.5);
+            double pvol = b0[0] * b0[1];
+            s->box[0] += psch; s->box[1] += psch;
+            double pvoln = s->box[0] * s->box[1];
+            enermove = o->press * s->box[2] * (pvoln - pvol) - NT * log(pvoln / pvol);
+            break;
+        }
+        case 5: {
+            s->box[1] += o->edge_mx * (rng() - 0.5);
+            enermove = o->press * s->box[2] * s->box[0] * (s->box[1] - b0[1]) - NT * log(s->box[1] / b0[1]);
+            break;
+        }
+        default: {          // 1: isotropic
+            double psch = o->edge_mx * (rng() - 0.5);
+            double pvol = b0[0] * b0[1] * b0[2];
+            for (int k = 0; k < 3; ++k) s->box[k] += psch;
+            double pvoln = s->box[0] * s->box[1] * s->box[2];
+            enermove = o->press * (pvoln - pvol) - NT * log(pvoln / pvol);
+            break;
+        }
+        }
+        long nw[2] = {wl->cur[0], wl->cur[1]};
+        for (int k = 0; k < dim; ++k) {
+            switch (wl->wlm[k]) {
+            case 1:
+                if (o->ptype != 2)
+                    nw[k] = (long)std::ceil(((s->p[0].pos.z - cm.z) * s->box[2] - wl->minorder[k]) / wl->dorder[k]);
+                break;
+            case 4: {
+                or_vec r = image(s->p[0].pos, s->p[1].pos, s->box);
+                nw[k] = (long)std::ceil((std::sqrt(r.x * r.x + r.y * r.y) - wl->minorder[k]) / wl->dorder[k]);
+                break;
+            }
+            case 8: nw[k] = (long)std::ceil((s->box[0] - wl->minorder[k]) / wl->dorder[k]); break;
+            case 9: nw[k] = (long)std::ceil((s->box[1] - wl->minorder[k]) / wl->dorder[k]); break;
+            default: break;
+            }
+        }
+        bool rej = !inRange(nw) || !(s->box[0] > 0 && s->box[1] > 0 && s->box[2] > 0);
+        if (!rej) {
+            enermove += or_all_to_all(s);
+            const double eo = energy + wl->weights[idx(nw)] - wl->weights[idx(wl->cur)];
+            rej = !(enermove <= eo) && !(exp(-1.0 * (enermove - eo) / o->temper) > rng());
+        }
+        if (rej) {
+            s->box[0] = b0[0]; s->box[1] = b0[1]; s->box[2] = b0[2];
+            ++st->rej_vol;
+        } else {
+            wl->cur[0] = nw[0]; wl->cur[1] = nw[1];
+            ++st->acc_vol;
+        }
+        visit();
+    };
     auto t0 = std::chrono::steady_clock::now();
     long moves = 0;
     for (long sweep = 1; sweep <= o->nsweeps; ++sweep) {
         for (int step = 1; step <= N; ++step) {
             if (o->max_moves > 0 && moves >= o->max_moves) goto finish;
             ++moves;
+            if (shprob > 0.0 && rng() < shprob) {      // Updater::simulate's step choice
+                volumeMove();
+                continue;
+            }
             int target = (int)(rng() * N);
             or_particle orig = s->p[target];
             const or_param& d = P(s, orig.type, orig.type);

@@ -121,8 +121,9 @@ typedef struct {
     int pad_;
 } or_wl;
 
-/* The reference's sequential loop with a Wang-Landau bias (single-particle moves, order
- * parameters 1, 3, 4), WangLandau::run / runRot / accept / reject / update. */
+/* The reference's sequential loop with a Wang-Landau bias (single-particle moves; volume
+ * moves of ptype 0, 1, 2, 5 with probability shave / N per step; order parameters 1, 3, 4,
+ * 8, 9), WangLandau::run / runRot / runPress / accept / reject / update. */
 int or_wl_run(or_system* s, const or_mc_opts* o, or_wl* wl, or_mc_stats* st);
 
 /* Wang-Landau starting bins (WangLandau::init, scOOP/mc/wanglandau.cpp:49-137) of order

@@ -139,6 +139,12 @@ def cases():
     out.append(dict(name="o9_box", wlm=(9, 0), options=dict(wlm="9 0", transmx=0.2, rotmx=0.0, nsweeps=0, seed=16,
                                                               shave=1, ptype=5, edge_mx=0.1),
                     top=top, config=cfg, wl=wl_text(0.0, grid1(6.0, 0.05, 21), [0.2 * k for k in range(21)])))
+    # (6) a weight wall on the box length in y (ptype 5): weights 0 inside bins 5..15, -1e4
+    # outside, fixed (alpha 0)
+    wall = [0.0 if 5 <= k <= 15 else -1e4 for k in range(21)]
+    out.append(dict(name="o9_wall", wlm=(9, 0), options=dict(wlm="9 0", transmx=0.2, rotmx=0.0, nsweeps=3000,
+                                                               seed=17, shave=1, ptype=5, edge_mx=0.1),
+                    top=top, config=cfg, wl=wl_text(0.0, grid1(6.0, 0.05, 21), wall)))
     return out
 
 
@@ -182,10 +188,10 @@ def main():
                                                    "config.init": c["config"], "wl.dat": c["wl"]},
                      "ref": dump["wl"], "n": dump["n"],
                      "system": {k: dump[k] for k in ("box", "sqmaxcut", "ia_params", "particles", "molecules")}}
-            if c["name"] in ("o4_pair", "o3_orient"):
+            if c["name"] in ("o4_pair", "o3_orient", "o9_wall"):
                 # the reference's own adaptive runs, three seeds
                 runs = []
-                for seed in (101, 202, 303):
+                for seed in ((101,) if c["name"] == "o9_wall" else (101, 202, 303)):
                     opts = dict(c["options"], seed=seed)
                     if c["name"] == "o3_orient":
                         opts["nsweeps"] = 20000

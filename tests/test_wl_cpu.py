@@ -251,3 +251,27 @@ def test_weights_file_reader_follows_init_calc(System):
         s.wl_load(text="\n".join(rows[:-1]) + "\n")     # the last row one bin short
     assert e.value.code == ERR_PARSE
     s.close()
+
+
+def test_oracle_volume_moves_respect_a_weight_wall_like_the_reference():
+    # fixed weights 0 inside bins 5..15 of the box length in y and -1e4 outside (ptype 5:
+    # only y changes): neither the reference nor the oracle's loop ever enters the wall,
+    # and both pile up against its upper side (no pressure: the box wants to grow)
+    import numpy as np
+
+    c = next(c for c in CASES if c["name"] == "o9_wall")
+    ref = c["ref"]
+    o = O.OracleSystem(c["system"])
+    opts = O.McOpts()
+    opts.nsweeps, opts.seed, opts.temper, opts.press = 3000, 5, 1.0, 0.0
+    opts.transmx, opts.edge_mx, opts.shave, opts.ptype = 0.4, 0.2, 1.0, 5   # options values doubled (sim.h:363-365)
+    nb = ref["length"][0]
+    w0 = np.array([0.0 if 5 <= k <= 15 else -1e4 for k in range(nb)])
+    w, h, st, ms = o.wl_run(opts, (9, 0), ref["minorder"], ref["dorder"], (nb, 1), 0.0, w0,
+                            np.zeros(nb, dtype=np.int64))
+    theirs = np.array(c["ref_runs"][0]["hist"])
+    for hist in (h, theirs):
+        assert hist[:5].sum() == 0 and hist[16:].sum() == 0
+        assert hist[15] > hist[5]
+    assert int(h.sum()) == ms.moves == 3000 * c["n"]
+    assert ms.acc_vol > 0 and ms.rej_vol > 0
