@@ -15,6 +15,14 @@ with host buffers (state uploaded before and downloaded after every step).
 `--impl reference` times the CPU restatement of the reference's own loop (oracle/,
 sequential Metropolis with the reference's Verlet list and O(N^2) volume move) on
 all host cores, independent seeds per core.
+
+Sections of the same line (rank 0, default run): `replicas` (64 uneven parallel-tempering
+replicas in one batch against the same replicas one after another), `surrogate` (65,536
+PSC/CPSC, plain against delayed acceptance with the network trained in the run),
+`bilayer` (30,000-particle lipid bilayers with chain moves), `wang_landau` (a particle
+above a bilayer with and without Wang-Landau weights, eight walkers sharing one table,
+and the oracle's sequential loop with the bias as the CPU baseline).  `--only <section>`
+runs one of them alone.
 """
 import argparse
 import ctypes as C
