@@ -12,7 +12,8 @@
  *     returns a message for the calling thread.  Nothing here exits the process.
  *   - Plain pointers and sizes only; host buffers belong to the caller.
  *   - One context = one system on one CUDA device and one stream.  A context is
- *     not shared between threads.
+ *     not shared between threads.  Every call makes the context's device current
+ *     while it runs and restores the calling thread's current device on return.
  *   - Positions are box fractions (the reference's internal coordinates),
  *     energies in the reference's units (kT/epsilon scale of top.init).
  */
@@ -88,7 +89,9 @@ typedef struct {
     int variant;            /* move kernel, bit 0: more moves in flight per SM (large systems), else lowest
                                latency per move; bit 1: paired passes (two moves per stage C); bit 2: one
                                dataflow launch per sweep instead of one launch per colour */
-    int pad_;
+    int flow_wait_polls;    /* dataflow sweep: polls of one wait for a neighbouring cell before the
+                               kernel gives up and the call returns SC_ERR_DEVICE (0: 2^19, about
+                               0.2 s; a wait in a sound run lasts well under 20 ms) */
 } sc_run_params;
 
 typedef struct {
@@ -160,8 +163,11 @@ int sc_one_to_all(sc_context* ctx, int ntargets, const int* targets, double* e);
  *   - The context's particle state must already be on the device: make one
  *     allocating call (e.g. sc_one_to_all) after opening or changing it, else
  *     SC_ERR_STATE.
- *   - The first call on a device looks up the array's device address; make that
- *     first call before any stream capture.
+ *   - The array is committed on a device by the first allocating call of any context
+ *     there (the lookup of its device address loads the module that holds it), not by
+ *     this call: even the first no-alloc call on a device allocates nothing.
+ *   - The call runs with the context's device current and gives the caller's current
+ *     device back before it returns.
  *   - All calls share the array: calls that overlap on the GPU (other host threads,
  *     other contexts' streams) race; serialise them. */
 #define SC_NOALLOC_MAX_TARGETS 16384

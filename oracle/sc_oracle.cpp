@@ -1085,6 +1085,8 @@ extern "C" int or_wl_run(or_system* s, const or_mc_opts* o, or_wl* wl, or_mc_sta
         wl->hist[idx(wl->cur)] += 1;
     };
     const double shprob = o->shave / (double)N;
+    // volume moves of ptype 3 and 4 (movecreator.cpp:454-510) are not restated here
+    if (shprob > 0.0 && o->ptype != 0 && o->ptype != 1 && o->ptype != 2 && o->ptype != 5) return -2;
     // MoveCreator::pressureMove (movecreator.cpp:330-546) with WangLandau::runPress
     // (wanglandau.h:168-196): the bins of the trial box (order 1 keeps the centre, and ptype
     // 2 keeps order 1; 4 the two particles' distance; 8 / 9 the box lengths)
@@ -1115,7 +1117,7 @@ extern "C" int or_wl_run(or_system* s, const or_mc_opts* o, or_wl* wl, or_mc_sta
             enermove = o->press * s->box[2] * s->box[0] * (s->box[1] - b0[1]) - NT * log(s->box[1] / b0[1]);
             break;
         }
-        default: {          // 1: isotropic
+        case 1: {           // isotropic
             double psch = o->edge_mx * (rng() - 0.5);
             double pvol = b0[0] * b0[1] * b0[2];
             for (int k = 0; k < 3; ++k) s->box[k] += psch;

@@ -123,7 +123,8 @@ typedef struct {
 
 /* The reference's sequential loop with a Wang-Landau bias (single-particle moves; volume
  * moves of ptype 0, 1, 2, 5 with probability shave / N per step; order parameters 1, 3, 4,
- * 8, 9), WangLandau::run / runRot / runPress / accept / reject / update. */
+ * 8, 9), WangLandau::run / runRot / runPress / accept / reject / update.  Returns -2 for
+ * volume moves of another ptype (3, 4), -1 for an empty system, else 0. */
 int or_wl_run(or_system* s, const or_mc_opts* o, or_wl* wl, or_mc_stats* st);
 
 /* Wang-Landau starting bins (WangLandau::init, scOOP/mc/wanglandau.cpp:49-137) of order

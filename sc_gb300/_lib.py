@@ -44,7 +44,7 @@ class RunParams(C.Structure):
                 ("ptype", C.c_int), ("volume_every", C.c_int), ("transmx", C.c_double), ("rot_angle", C.c_double),
                 ("edge_mx", C.c_double), ("chainprob", C.c_double), ("chainmmx", C.c_double),
                 ("chain_angle", C.c_double), ("check_every", C.c_int), ("time_phases", C.c_int),
-                ("stencil", C.c_int), ("delayed", C.c_int), ("variant", C.c_int), ("pad_", C.c_int)]
+                ("stencil", C.c_int), ("delayed", C.c_int), ("variant", C.c_int), ("flow_wait_polls", C.c_int)]
 
 
 class RunStats(C.Structure):

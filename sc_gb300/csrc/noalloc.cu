@@ -34,28 +34,30 @@ constexpr int kMaxDevices = 64;
 std::mutex g_noallocMutex;
 void* g_noallocAddr[kMaxDevices] = {};
 
-// Device address of the array on `device`.  In host code the name g_noallocScratch
-// only denotes a host-side stand-in, never a device address, so the address is
-// looked up once per device (with that device current) and cached.
-int noallocScratch(int device, void** out) {
+}  // namespace
+
+// Device address of the array on `device`.  In host code the name g_noallocScratch only
+// denotes a host-side stand-in, never a device address, so the address is looked up with
+// that device current and cached.  CUDA loads a module lazily: this lookup is what loads
+// the array's module (and commits its memory) on the device, so it runs inside the first
+// allocating call on the device (Context::ensureDevice), never inside the no-alloc call.
+int noallocLookup(int device) {
     if (device < 0 || device >= kMaxDevices) return fail(SC_ERR_ARG, "device index out of range");
     std::lock_guard<std::mutex> lock(g_noallocMutex);
-    if (!g_noallocAddr[device]) {
-        int current = -1;
-        cudaError_t e = cudaGetDevice(&current);
-        if (e != cudaSuccess) return cudaFail(e, "cudaGetDevice");
-        if (current != device && (e = cudaSetDevice(device)) != cudaSuccess) return cudaFail(e, "cudaSetDevice");
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noallocScratch);
-        if (current != device) cudaSetDevice(current);
-        if (e != cudaSuccess) return cudaFail(e, "cudaGetSymbolAddress(no-alloc scratch)");
-        g_noallocAddr[device] = p;
-    }
-    *out = g_noallocAddr[device];
+    if (g_noallocAddr[device]) return SC_OK;
+    DeviceScope dev(device);
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noallocScratch);
+    if (e != cudaSuccess) return cudaFail(e, "cudaGetSymbolAddress(no-alloc scratch)");
+    g_noallocAddr[device] = p;
     return SC_OK;
 }
 
-}  // namespace
+void* noallocCached(int device) {
+    if (device < 0 || device >= kMaxDevices) return nullptr;
+    std::lock_guard<std::mutex> lock(g_noallocMutex);
+    return g_noallocAddr[device];
+}
 
 }  // namespace scg
 
@@ -64,6 +66,8 @@ using namespace scg;
 extern "C" int sc_one_to_all_noalloc(sc_context* ctx, int ntargets, const int* targets, double* out) {
     if (!ctx || ntargets < 0 || (ntargets > 0 && (!targets || !out))) return fail(SC_ERR_ARG, "null argument");
     Context* c = reinterpret_cast<Context*>(ctx);
+    // the copies and the launch go to c->stream, which belongs to c->device
+    DeviceScope dev(c->device);
     if (ntargets > kNoallocMaxTargets)
         return fail(SC_ERR_RANGE, "sc_one_to_all_noalloc takes at most " + std::to_string(kNoallocMaxTargets) +
                                       " targets per call");
@@ -74,9 +78,10 @@ extern "C" int sc_one_to_all_noalloc(sc_context* ctx, int ntargets, const int* t
         return fail(SC_ERR_STATE, "the particle state is not on the device: make one allocating call "
                                   "(e.g. sc_one_to_all) after changing it, then use the no-alloc variant");
     if (ntargets == 0) return SC_OK;
-    void* base = nullptr;
-    int rc = noallocScratch(c->device, &base);
-    if (rc) return rc;
+    void* base = noallocCached(c->device);
+    if (!base)
+        return fail(SC_ERR_STATE, "the no-alloc array of this device is not set up: make one allocating call "
+                                  "(e.g. sc_one_to_all) on the device first");
     int* dT = (int*)base;
     double* dO = (double*)((unsigned char*)base + kTargetsBytes);
     cudaError_t e;

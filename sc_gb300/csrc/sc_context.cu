@@ -32,7 +32,7 @@ void Context::freeDevice() {
     destroyEngine(this);
     destroyWl(this);
     if (!devReady) return;
-    cudaSetDevice(device);
+    DeviceScope dev(device);
     for (void* p : allocations) cudaFree(p);
     allocations.clear();
     if (hostStage) cudaFreeHost(hostStage);
@@ -137,9 +137,15 @@ int Context::setup(std::string& err) {
 }
 
 int Context::ensureDevice() {
+    // every call: the stream and the buffers below belong to `device` (the entry points
+    // hold a DeviceScope that gives the caller's device back when they return)
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return cudaFail(e, "cudaSetDevice");
     if (!devReady) {
-        cudaError_t e = cudaSetDevice(device);
-        if (e != cudaSuccess) return cudaFail(e, "cudaSetDevice");
+        // the no-allocation entry point's array: its address lookup loads the module that
+        // holds it, which may allocate, so it is done here, in an allocating call
+        int rc0 = noallocLookup(device);
+        if (rc0) return rc0;
         e = cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
         if (e != cudaSuccess) return cudaFail(e, "cudaStreamCreate");
         int n = (int)conf.p.size();
@@ -211,6 +217,7 @@ int Context::uploadState() {
 
 int Context::downloadState() {
     if (!devReady || !devNewer) return SC_OK;
+    DeviceScope dev(device);
     int n = (int)conf.p.size();
     double* box = (double*)hostStage;
     double4_32a* hp = (double4_32a*)((char*)hostStage + 64);
@@ -439,6 +446,7 @@ int sc_write_config(sc_context* ctx, const char* path) {
 int sc_pair_energies(sc_context* ctx, int npairs, const int* I, const int* J, double* E, unsigned* V, double* D) {
     if (!ctx || npairs < 0 || (npairs > 0 && (!I || !J || !E))) return fail(SC_ERR_ARG, "null argument");
     Context* c = C(ctx);
+    DeviceScope dev(c->device);
     int n = (int)c->conf.p.size();
     for (int k = 0; k < npairs; ++k)
         if (I[k] < 0 || J[k] < 0 || I[k] >= n || J[k] >= n) return fail(SC_ERR_ARG, "pair index out of range");
@@ -485,6 +493,7 @@ static int oneToAllImpl(Context* c, int ntargets, const int* targets, const Tria
 int sc_one_to_all(sc_context* ctx, int ntargets, const int* targets, double* out) {
     if (!ctx || ntargets < 0 || (ntargets > 0 && (!targets || !out))) return fail(SC_ERR_ARG, "null argument");
     Context* c = C(ctx);
+    DeviceScope dev(c->device);
     int n = (int)c->conf.p.size();
     for (int k = 0; k < ntargets; ++k) if (targets[k] < 0 || targets[k] >= n) return fail(SC_ERR_ARG, "target out of range");
     if (ntargets == 0) return SC_OK;
@@ -496,6 +505,7 @@ int sc_one_to_all(sc_context* ctx, int ntargets, const int* targets, double* out
 int sc_all_to_all(sc_context* ctx, double* out) {
     if (!ctx || !out) return fail(SC_ERR_ARG, "null argument");
     Context* c = C(ctx);
+    DeviceScope dev(c->device);
     int rc = c->ensureDevice();
     if (rc) return rc;
     cudaError_t e;
@@ -508,6 +518,7 @@ int sc_all_to_all(sc_context* ctx, double* out) {
 int sc_alignment_order(sc_context* ctx, double* out) {
     if (!ctx || !out) return fail(SC_ERR_ARG, "null argument");
     Context* c = C(ctx);
+    DeviceScope dev(c->device);
     int rc = c->ensureDevice();
     if (rc) return rc;
     if (c->hostNewer && (rc = c->uploadState())) return rc;
@@ -521,6 +532,7 @@ int sc_alignment_order(sc_context* ctx, double* out) {
 int sc_mol_to_others(sc_context* ctx, int first, int size, double* out) {
     if (!ctx || !out) return fail(SC_ERR_ARG, "null argument");
     Context* c = C(ctx);
+    DeviceScope dev(c->device);
     if (first < 0 || size <= 0 || first + size > (int)c->conf.p.size()) return fail(SC_ERR_ARG, "molecule range out of bounds");
     int rc = c->ensureDevice();
     if (rc) return rc;
@@ -583,6 +595,7 @@ static int trialImpl(Context* c, int target, const Particle& trial, double* eOld
 int sc_trial_displace(sc_context* ctx, int target, const double dr[3], double* eOld, double* eNew) {
     if (!ctx || !dr || !eOld || !eNew) return fail(SC_ERR_ARG, "null argument");
     Context* c = C(ctx);
+    DeviceScope dev(c->device);
     if (target < 0 || target >= (int)c->conf.p.size()) return fail(SC_ERR_ARG, "target out of range");
     int rc = c->downloadState();
     if (rc) return rc;
@@ -596,6 +609,7 @@ int sc_trial_rotate(sc_context* ctx, int target, double angle, const double axis
                     double* eNew, sc_particle* state) {
     if (!ctx || !axis || !eOld || !eNew) return fail(SC_ERR_ARG, "null argument");
     Context* c = C(ctx);
+    DeviceScope dev(c->device);
     if (target < 0 || target >= (int)c->conf.p.size()) return fail(SC_ERR_ARG, "target out of range");
     int rc = c->downloadState();
     if (rc) return rc;
@@ -621,6 +635,7 @@ int sc_accept_trial(sc_context* ctx) {
 int sc_trial_volume(sc_context* ctx, double psch, double* eNew) {
     if (!ctx || !eNew) return fail(SC_ERR_ARG, "null argument");
     Context* c = C(ctx);
+    DeviceScope dev(c->device);
     int rc = c->ensureDevice();
     if (rc) return rc;
     if ((rc = c->downloadState())) return rc;
@@ -659,6 +674,7 @@ int sc_default_run(const sc_context* ctx, sc_run_params* p) {
 
 int sc_simulate(sc_context* ctx, const sc_run_params* p, sc_run_stats* stats) {
     if (!ctx || !p || !stats) return fail(SC_ERR_ARG, "null argument");
+    DeviceScope dev(C(ctx)->device);
     return runSweeps(C(ctx), *p, *stats);
 }
 

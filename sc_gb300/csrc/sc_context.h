@@ -71,7 +71,31 @@ struct Context {
     PairParam devParam(int t1, int t2) const;
 };
 
+// Makes a context's device the calling thread's current device for the lifetime of the
+// scope and gives the caller's device back afterwards, so that every copy and launch of
+// an entry point goes to the device (and the stream) the context lives on, whatever
+// device the calling thread had selected.  Without a usable CUDA device it does nothing.
+struct DeviceScope {
+    int prev = -1;
+    int want = -1;
+    explicit DeviceScope(int device) {
+        if (cudaGetDevice(&prev) != cudaSuccess) { prev = -1; cudaGetLastError(); return; }
+        want = device;
+        if (prev != device && cudaSetDevice(device) != cudaSuccess) { want = prev; cudaGetLastError(); }
+    }
+    ~DeviceScope() {
+        if (prev >= 0 && want != prev) cudaSetDevice(prev);
+    }
+    DeviceScope(const DeviceScope&) = delete;
+    DeviceScope& operator=(const DeviceScope&) = delete;
+};
+
 int fail(int code, const std::string& msg);
+// Device address of the no-allocation entry point's fixed array on `device` (noalloc.cu).
+// Looked up by the first allocating call on the device (Context::ensureDevice), because
+// the lookup loads the array's module, which may allocate; afterwards it only reads a cache.
+int noallocLookup(int device);
+void* noallocCached(int device);
 const MlpPacked* surrogatePacked(const Surrogate* s);
 float surrogateCutoff(const Surrogate* s);
 float surrogateRange(Context* c);

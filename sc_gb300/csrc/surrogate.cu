@@ -608,6 +608,7 @@ extern "C" {
 int sc_surrogate_create(sc_context* ctx, unsigned long long seed, long capacity, sc_surrogate** out) {
     if (!ctx || !out || capacity < 0) return fail(SC_ERR_ARG, "sc_surrogate_create: bad arguments");
     Context* c = reinterpret_cast<Context*>(ctx);
+    DeviceScope dev(c->device);
     int rc = c->ensureDevice();
     if (rc) return rc;
     sc_surrogate* h = new sc_surrogate();
@@ -646,7 +647,7 @@ int sc_surrogate_create(sc_context* ctx, unsigned long long seed, long capacity,
 int sc_surrogate_destroy(sc_surrogate* h) {
     if (!h) return SC_OK;
     Surrogate& s = h->impl;
-    cudaSetDevice(s.device);
+    DeviceScope dev(s.device);
     if (s.stream) cudaStreamSynchronize(s.stream);
     void* ptrs[] = {s.theta, s.mom, s.vel, s.grad, s.packed, s.part, s.dLoss, s.feats, s.target};
     for (void* p : ptrs)
@@ -659,7 +660,7 @@ int sc_surrogate_destroy(sc_surrogate* h) {
 int sc_surrogate_get_weights(sc_surrogate* h, float* out) {
     if (!h || !out) return fail(SC_ERR_ARG, "sc_surrogate_get_weights: null argument");
     Surrogate& s = h->impl;
-    cudaSetDevice(s.device);
+    DeviceScope dev(s.device);
     cudaError_t r = cudaMemcpyAsync(out, s.theta, kParams * sizeof(float), cudaMemcpyDeviceToHost, s.stream);
     if (r == cudaSuccess) r = cudaStreamSynchronize(s.stream);
     return r == cudaSuccess ? SC_OK : surFail(r, "sc_surrogate_get_weights");
@@ -668,7 +669,7 @@ int sc_surrogate_get_weights(sc_surrogate* h, float* out) {
 int sc_surrogate_set_weights(sc_surrogate* h, const float* in) {
     if (!h || !in) return fail(SC_ERR_ARG, "sc_surrogate_set_weights: null argument");
     Surrogate& s = h->impl;
-    cudaSetDevice(s.device);
+    DeviceScope dev(s.device);
     std::vector<float> th(kParamsPad, 0.0f);
     std::memcpy(th.data(), in, kParams * sizeof(float));
     for (int k = 13 * kHidden; k < kFeat * kHidden; ++k) th[kOffW1 + k] = 0.0f;   // zero inputs 13..15
@@ -744,7 +745,7 @@ int sc_surrogate_collect(sc_surrogate* h, sc_context* ctx, long* total) {
     Surrogate& s = h->impl;
     Context* c = reinterpret_cast<Context*>(ctx);
     if (c->device != s.device) return fail(SC_ERR_ARG, "sc_surrogate_collect: context on another device");
-    cudaSetDevice(s.device);
+    DeviceScope dev(s.device);
     long got = 0;
     long room = s.cap - s.count;
     if (room > 0) {
@@ -762,7 +763,7 @@ int sc_surrogate_train(sc_surrogate* h, const sc_train_params* p, double* loss_p
     if (s.count <= 0) return fail(SC_ERR_STATE, "sc_surrogate_train: no samples collected");
     if (p->epochs < 0 || p->batch < kChunkRows || p->batch % kChunkRows || !(p->lr > 0))
         return fail(SC_ERR_ARG, "sc_surrogate_train: epochs >= 0, batch a multiple of 64, lr > 0");
-    cudaSetDevice(s.device);
+    DeviceScope dev(s.device);
     const int rowsPerCta = p->batch >= 64 * 152 * 2 ? 128 : 64;
     const int nCta = p->batch / rowsPerCta;
     const int chunks = rowsPerCta / kChunkRows;
@@ -813,7 +814,7 @@ int sc_surrogate_gradient(sc_surrogate* h, int n, const float* feats, const floa
                           double* loss) {
     if (!h || n <= 0 || !feats || !targets || !grad_out) return fail(SC_ERR_ARG, "sc_surrogate_gradient: bad arguments");
     Surrogate& s = h->impl;
-    cudaSetDevice(s.device);
+    DeviceScope dev(s.device);
     float *df = nullptr, *dt = nullptr;
     cudaError_t r = cudaMalloc(&df, (size_t)n * kFeat * sizeof(float));
     if (r == cudaSuccess) r = cudaMalloc(&dt, (size_t)n * sizeof(float));
@@ -840,7 +841,7 @@ int sc_surrogate_predict(sc_surrogate* h, int n, const float* feats, float* out)
     if (!h || n < 0 || (n && (!feats || !out))) return fail(SC_ERR_ARG, "sc_surrogate_predict: bad arguments");
     if (n == 0) return SC_OK;
     Surrogate& s = h->impl;
-    cudaSetDevice(s.device);
+    DeviceScope dev(s.device);
     float *df = nullptr, *dy = nullptr;
     cudaError_t r = cudaMalloc(&df, (size_t)n * kFeat * sizeof(float));
     if (r == cudaSuccess) r = cudaMalloc(&dy, (size_t)n * sizeof(float));
@@ -860,7 +861,7 @@ int sc_surrogate_evaluate(sc_surrogate* h, sc_context* ctx, double* rmse, double
     if (!h || !ctx) return fail(SC_ERR_ARG, "sc_surrogate_evaluate: null argument");
     Surrogate& s = h->impl;
     Context* c = reinterpret_cast<Context*>(ctx);
-    cudaSetDevice(s.device);
+    DeviceScope dev(s.device);
     const long cap = (long)c->d.n * 64 + 1024;
     float *df = nullptr, *dt = nullptr, *dy = nullptr;
     cudaError_t r = cudaMalloc(&df, (size_t)cap * kFeat * sizeof(float));
@@ -902,6 +903,7 @@ int sc_pair_features(sc_context* ctx, int npairs, const int* I, const int* J, fl
     if (!ctx || npairs < 0 || (npairs && (!I || !J || !feats || !wca || !eligible)))
         return fail(SC_ERR_ARG, "sc_pair_features: bad arguments");
     Context* c = reinterpret_cast<Context*>(ctx);
+    DeviceScope dev(c->device);
     int rc = c->ensureDevice();
     if (rc) return rc;
     for (int k = 0; k < npairs; ++k)
@@ -935,6 +937,7 @@ int sc_set_surrogate(sc_context* ctx, sc_surrogate* h) {
     if (!ctx) return fail(SC_ERR_ARG, "sc_set_surrogate: null context");
     Context* c = reinterpret_cast<Context*>(ctx);
     if (h) {
+        DeviceScope dev(c->device);
         int rc = c->ensureDevice();
         if (rc) return rc;
         if (h->impl.device != c->device) return fail(SC_ERR_ARG, "sc_set_surrogate: surrogate on another device");

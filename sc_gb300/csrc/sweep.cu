@@ -139,6 +139,7 @@ struct SweepArgs {
     int ptype;              // pressure coupling of volume moves (movecreator.cpp:349-546)
     double boxMinChain[3];  // smallest box edges the chain grid allows (0: no chain phase)
     WlDev* wl;              // Wang-Landau bias (nullptr: none; only the particle grid's records)
+    int flowSpin;           // dataflow sweep: polls of one wait before the CTA gives up
 };
 
 __device__ __forceinline__ int wrapCell(double x, double shift, int nc) {
@@ -1480,7 +1481,9 @@ __global__ void __launch_bounds__(kMoveThreads, 3) kColourDense(const SweepArgs*
 // phase kernels' (same states, same random numbers), without a grid-wide barrier between
 // phases.  Forward progress: a CTA waits only on cells with smaller tickets, taken earlier
 // by CTAs that are running, and the smallest unfinished ticket waits on nothing.  Every
-// wait is bounded: after kFlowSpin polls the CTA sets E_FLOW_WAIT and every CTA returns.
+// wait is bounded: after a.flowSpin polls (default kFlowSpin) the CTA sets E_FLOW_WAIT and
+// every CTA returns; a cell gives up before any of its moves, so every cell of the sweep is
+// either moved completely or not at all.
 constexpr int kFlowSpin = 1 << 19;      // polls of one wait (~0.2 s; a legitimate wait is < 20 ms)
 
 __device__ __forceinline__ unsigned loadAcquireGpu(const unsigned* p) {
@@ -1539,7 +1542,7 @@ __device__ __forceinline__ void flowBody(const SweepArgs* __restrict__ A) {
                 if (posOf[colour] >= phase) continue;
                 const unsigned* f = &a.cellDone[(z * g.nc[1] + y) * g.nc[0] + x];
                 for (int spin = 0; loadAcquireGpu(f) != stamp; ++spin) {
-                    if (spin >= kFlowSpin || ((spin & 255) == 255 && (*(volatile int*)a.err & E_FLOW_WAIT))) {
+                    if (spin >= a.flowSpin || ((spin & 255) == 255 && (*(volatile int*)a.err & E_FLOW_WAIT))) {
                         sFail = 1;
                         break;
                     }
@@ -2501,7 +2504,7 @@ struct Batch {
     std::vector<void*> allocs;
 
     ~Batch() {
-        cudaSetDevice(device);
+        DeviceScope dev(device);
         for (void* p : allocs) cudaFree(p);
         for (cudaEvent_t e : {ev0, ev1})
             if (e) cudaEventDestroy(e);
@@ -2568,7 +2571,7 @@ void destroyEngine(Context* c) {
     }
     SweepEngine* e = c->engine;
     if (!e) return;
-    cudaSetDevice(c->device);
+    DeviceScope dev(c->device);
     for (void* p : e->allocs) cudaFree(p);
     delete e;
     c->engine = nullptr;
@@ -2636,6 +2639,7 @@ static void fillArgs(Context* c, SweepEngine* e, const sc_run_params& p) {
         a.rcutS = surrogateCutoff(c->surrogate);
     }
     a.wl = wlDevice(c);
+    a.flowSpin = p.flow_wait_polls > 0 ? p.flow_wait_polls : kFlowSpin;
 }
 
 // Chain phase of one system: chains (molecules of more than one particle), the bound R of
@@ -3167,6 +3171,7 @@ static int checkParams(const sc_run_params& p) {
     if (p.ptype < 0 || p.ptype > 5) return fail(SC_ERR_ARG, "ptype must be 0..5 (movecreator.cpp:349-546)");
     if (p.stencil < 0 || p.stencil > 3) return fail(SC_ERR_ARG, "stencil must be 0 (auto), 1, 2 or 3");
     if (p.variant < 0 || p.variant > 7) return fail(SC_ERR_ARG, "variant must be 0..7");
+    if (p.flow_wait_polls < 0) return fail(SC_ERR_ARG, "flow_wait_polls must be >= 0");
     return SC_OK;
 }
 
@@ -3197,7 +3202,11 @@ int runSweeps(Context* c, const sc_run_params& p, sc_run_stats& st) {
     st.phase_launches = out.phaseLaunches;
     st.launches = out.launches;
     c->lastLaunches = out.launches;
-    return systemErrors(c);
+    rc = systemErrors(c);
+    // a sweep that stopped early (a dataflow wait gave up, a cell overflowed) leaves cells
+    // unmoved and their energy changes unsummed: the next run recomputes the exact energy
+    if (rc) c->engine->energyKnown = false;
+    return rc;
 }
 
 // --- parallel-tempering replicas -----------------------------------------------------
@@ -3258,6 +3267,7 @@ int runReplicas(void* h, const sc_run_params& p, int exchangeEvery, sc_run_stats
     Batch& b = R->b;
     const int nrep = (int)b.sys.size();
     const bool npt = p.volume_every > 0;
+    DeviceScope dev(b.sys[0]->device);
     for (int k = 0; k < nrep; ++k) {
         Context* c = b.sys[k];
         if (c->conf.p.empty()) return fail(SC_ERR_ARG, "a replica holds no particles");
@@ -3320,7 +3330,10 @@ int runReplicas(void* h, const sc_run_params& p, int exchangeEvery, sc_run_stats
         st.max_drift = std::max(st.max_drift, s1.max_drift);
         if (tempsOut) tempsOut[k] = cur[k].temper;
         if (energiesOut) energiesOut[k] = s1.energy;
-        if ((rc = systemErrors(b.sys[k]))) return rc;
+        if ((rc = systemErrors(b.sys[k]))) {
+            for (Context* c : b.sys) c->engine->energyKnown = false;   // see runSweeps
+            return rc;
+        }
     }
     if (exTried || exAcc) {
         std::vector<unsigned long long> ctr(1 + 2 * nrep);

@@ -29,7 +29,7 @@ struct WlTableHost {
     bool onDevice = false;           // the device copy is the current one
     ~WlTableHost() {
         if (!d) return;
-        cudaSetDevice(device);
+        DeviceScope dev(device);
         cudaFree(d);
         cudaFree(h.base);
         cudaFree(h.hist);
@@ -185,7 +185,7 @@ int wlCheckRun(const Context* c, const sc_run_params& p) {
 static int tableUpload(WlTableHost& T, int device, bool arrays) {
     const size_t nb = T.base.size();
     cudaError_t r;
-    cudaSetDevice(device);
+    DeviceScope dev(device);
     if (!T.d) {
         if ((r = cudaMalloc((void**)&T.d, sizeof(WlTable))) != cudaSuccess) return cudaFail(r, "cudaMalloc (Wang-Landau)");
         if ((r = cudaMalloc((void**)&T.h.base, sizeof(double) * nb)) != cudaSuccess) return cudaFail(r, "cudaMalloc (Wang-Landau)");
@@ -211,6 +211,7 @@ static int wlDownload(Context* c) {
     WlHost& W = *c->wl;
     WlTableHost& T = *W.T;
     cudaError_t r;
+    DeviceScope dev(c->device);
     if (W.onDevice) {
         cudaSetDevice(W.device);
         cudaDeviceSynchronize();
@@ -272,7 +273,7 @@ void destroyWl(Context* c) {
     if (!c->wl) return;
     WlHost& W = *c->wl;
     if (W.d) {
-        cudaSetDevice(W.device);
+        DeviceScope dev(W.device);
         cudaFree(W.d);
     }
     delete c->wl;       // the table goes with its last walker

@@ -34,7 +34,19 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF_ROOT = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+
+
+def _reference_root():
+    """The reference checkout: the first argument, else the one oracle/Makefile resolves
+    (SC_REFERENCE in the environment overrides the recipe's default)."""
+    if len(sys.argv) > 1:
+        return sys.argv[1]
+    r = subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "print-ref"], capture_output=True,
+                       text=True, check=True)
+    return os.path.dirname(r.stdout.strip())
+
+
+REF_ROOT = _reference_root()
 DUMP = os.path.join(REPO, "oracle", "_ref", "ref_dump")
 
 OPTION_KEYS = dict(

@@ -169,6 +169,20 @@ class OracleSystem:
             self.sys.box[k] = float(ref["box"][k])
         self.sys.sqmaxcut = float(ref["sqmaxcut"])
 
+    def set_state(self, parts, box):
+        """Takes a configuration from the GPU path (sc_particle records and box edges), e.g.
+        after device sweeps, so that the oracle evaluates that state."""
+        for k, q in enumerate(parts):
+            o = self.parts[k]
+            o.pos, o.dir = vec(q.pos), vec(q.dir)
+            for m in range(2):
+                o.pd[m], o.ch[m] = vec(q.patchdir[m]), vec(q.chdir[m])
+            for m in range(4):
+                o.ps[m] = vec(q.patchsides[m])
+            assert o.type == q.type
+        for k in range(3):
+            self.sys.box[k] = float(box[k])
+
     def pair(self, i, j):
         bits = C.c_uint(0)
         dsq = C.c_double(0)

@@ -264,3 +264,29 @@ def test_ensemble_matches_reference(name):
         assert abs(m - ref["mean"]) <= 2.0 * sigma, report
     for s in systems:
         s.close()
+
+
+def test_dataflow_wait_limit_reports_and_recovers():
+    """The dataflow sweep's bounded wait: with a limit of one poll, a cell that finds an
+    earlier-phase neighbour unfinished gives up, the kernel returns and the call reports
+    SC_ERR_DEVICE; the context stays usable, and the next run (default limit) recomputes the
+    exact energy and keeps it exact."""
+    from sc_gb300 import ScError, System
+
+    g = goldens.load("syn_cpsc_spa_npt_small")
+    inp = g["inputs"]
+    s = System.from_text(inp["options"], inp["top.init"], inp["config.init"])
+    s.simulate(nsweeps=2, seed=5, variant=4, check_every=0)
+    failed = 0
+    for k in range(5):
+        try:
+            s.simulate(nsweeps=4, seed=6 + k, variant=4, check_every=0, flow_wait_polls=1)
+        except ScError as ex:
+            assert "DEVICE" in str(ex) and "waited too long" in str(ex), str(ex)
+            failed += 1
+    assert failed > 0
+    st = s.simulate(nsweeps=5, seed=20, variant=4, check_every=0)
+    assert st.sweeps == 5
+    exact = s.all_to_all()
+    assert abs(st.energy - exact) <= 1e-9 * max(1.0, abs(exact)), (st.energy, exact)
+    s.close()
