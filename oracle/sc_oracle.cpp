@@ -59,8 +59,7 @@ inline void rotate(or_vec& v, const or_vec& axis, double c, double s) {
 // Round-half-even of |d| < 2^31, the value Cuboid::image gets from the low word
 // of d + 1.5*2^52 (scOOP/structures/geometry.h:110-128).
 inline double anint(double d) {
-    volatile double t = d + 6755399441055744.0;
-    double tt = t;
+    const double tt = d + 6755399441055744.0;
     uint64_t bits;
     std::memcpy(&bits, &tt, 8);
     return (double)(int32_t)(uint32_t)(bits & 0xffffffffu);
@@ -512,14 +511,23 @@ inline double mixClosest(const or_vec& rc, const or_vec& d1, double halfl, doubl
 
 }  // namespace
 
+double pairEnergyCon(const or_system* s, int i, int j, const Con& con, unsigned* bitsOut, double* distSqOut);
+
 extern "C" {
 
 // PairE::operator() (scOOP/mc/paire.h:1209-1220) with the functor bodies of
 // SpheroCylinder (1114-1197), MixSpSc (1014-1094) and Sphere (1099-1109).
 double or_pair_energy(const or_system* s, int i, int j, unsigned* bitsOut, double* distSqOut) {
+    return pairEnergyCon(s, i, j, getConlist(s, i), bitsOut, distSqOut);
+}
+
+}  // extern "C"
+
+// PairE::operator() with the conlist of particle i given (the reference builds it once per
+// oneToAllTrial / allToAll row, totalenergycalculator.h:389, 511).
+double pairEnergyCon(const or_system* s, int i, int j, const Con& con, unsigned* bitsOut, double* distSqOut) {
     unsigned bits = 0;
     double dsqOut = -1.0;
-    Con con = getConlist(s, i);
     const or_particle& p1 = s->p[i];
     const or_particle& p2 = s->p[j];
     or_vec r_cm = image(p1.pos, p2.pos, s->box);
@@ -656,6 +664,8 @@ done:
     return energy;
 }
 
+extern "C" {
+
 // TotalEMatrix::oneToAllTrial without pair list (totalenergycalculator.h:383-415): index order.
 double or_one_to_all(const or_system* s, int target) {
     double e = 0.0;
@@ -667,9 +677,39 @@ double or_one_to_all(const or_system* s, int target) {
 // TotalEMatrix::allToAll(EnergyMatrix*) (totalenergycalculator.h:502-521): part1 = i > j.
 double or_all_to_all(const or_system* s) {
     double e = 0.0;
-    for (int i = 1; i < s->n; ++i)
-        for (int j = 0; j < i; ++j) e += or_pair_energy(s, i, j, nullptr, nullptr);
+    for (int i = 1; i < s->n; ++i) {
+        const Con con = getConlist(s, i);
+        for (int j = 0; j < i; ++j) e += pairEnergyCon(s, i, j, con, nullptr, nullptr);
+    }
     return e;
+}
+
+// PairE over a batch of ordered pairs (i[k] with the conlist of i[k]).
+void or_pair_energies(const or_system* s, long n, const int* I, const int* J, double* E, unsigned* bits,
+                      double* dsq) {
+    for (long k = 0; k < n; ++k)
+        E[k] = pairEnergyCon(s, I[k], J[k], getConlist(s, I[k]), bits ? &bits[k] : nullptr, dsq ? &dsq[k] : nullptr);
+}
+
+// The pairs PairE's prefilter admits (paire.h:1209-1215): ordered (i, j), i a target
+// (targets[0..nt), or every particle when targets is NULL), j != i, with the image
+// distance^2 <= sqmaxcut or j bonded to i (conlist); at most cap written, *count all.
+void or_prefilter_pairs(const or_system* s, int nt, const int* targets, long cap, int* I, int* J, long* count) {
+    long c = 0;
+    const int ntt = targets ? nt : s->n;
+    for (int a = 0; a < ntt; ++a) {
+        const int i = targets ? targets[a] : a;
+        const Con con = getConlist(s, i);
+        for (int j = 0; j < s->n; ++j) {
+            if (j == i) continue;
+            or_vec r = image(s->p[i].pos, s->p[j].pos, s->box);
+            const bool bonded = j == con.idx[0] || j == con.idx[1] || j == con.idx[2] || j == con.idx[3];
+            if (dot(r, r) > s->sqmaxcut && !bonded) continue;
+            if (c < cap) { I[c] = i; J[c] = j; }
+            ++c;
+        }
+    }
+    *count = c;
 }
 
 // TotalEMatrix::mol2othersTrial (totalenergycalculator.h:453-499): empty conlist.
@@ -909,103 +949,265 @@ or_vec randomUnitSphere(Rng& r) {     // Vector::randomUnitSphere (Vector.h:190-
     return V(xi1 * b, xi2 * b, 1.0 - 2.0 * a);
 }
 
+// Verlet list of genSimplePairList (updater.cpp:484-552): every pair (i < j) with
+// |r_cm|^2 <= cut2 or bonded to i+1 (bond1/bondd/bondh) or i+2 (bond2), both directions,
+// neighbours in ascending index order.  Flat storage (start offsets + ids).
 struct PairList {
-    std::vector<std::vector<int>> nb;
+    std::vector<int> start, count, ids;
     void build(const or_system* s, double cut2) {
-        nb.assign(s->n, {});
-        for (int i = 0; i < s->n; ++i) {
-            Con con = getConlist(s, i);
-            for (int j = 0; j < s->n; ++j) {
-                if (i == j) continue;
+        const int n = s->n;
+        count.assign(n, 0);
+        auto bondedPair = [&](int i, int j) {
+            if (j > i + 2) return false;
+            const or_moltype& m = s->mols[s->p[i].molType];
+            int pos = (i - m.first) % m.size;
+            if ((m.bond1c >= 0.0 || m.bonddc >= 0.0 || m.bondhc >= 0.0) && pos + 1 < m.size && i + 1 == j) return true;
+            if (m.bond2c >= 0.0 && pos + 2 < m.size && i + 2 == j) return true;
+            return false;
+        };
+        std::vector<std::pair<int, int>> pairs;
+        pairs.reserve((size_t)n * 64);
+        for (int i = 0; i + 1 < n; ++i)
+            for (int j = i + 1; j < n; ++j) {
                 or_vec r = image(s->p[i].pos, s->p[j].pos, s->box);
-                bool bonded = (j == con.idx[0] || j == con.idx[1] || j == con.idx[2] || j == con.idx[3]);
-                if (dot(r, r) < cut2 || bonded) nb[i].push_back(j);
+                if (dot(r, r) <= cut2 || bondedPair(i, j)) {
+                    pairs.emplace_back(i, j);
+                    ++count[i];
+                    ++count[j];
+                }
             }
+        start.assign(n + 1, 0);
+        for (int i = 0; i < n; ++i) start[i + 1] = start[i] + count[i];
+        ids.resize(start[n]);
+        std::vector<int> fill(start.begin(), start.end() - 1);
+        // pairs are ordered by i then j: particle t receives its j < t neighbours (as the
+        // partner of earlier i) before its j > t ones, each in ascending order
+        for (auto& pr : pairs) {
+            ids[fill[pr.first]++] = pr.second;
+            ids[fill[pr.second]++] = pr.first;
         }
     }
 };
 
-double oneToAllList(const or_system* s, int t, const PairList* pl) {
-    if (!pl) return or_one_to_all(s, t);
+// Lower-triangular energy matrix of EnergyMatrixF (totalenergycalculator.h:16-128),
+// entry (i, j), i > j, at i (i - 1) / 2 + j.
+inline size_t emIdx(int i, int j) { return i > j ? (size_t)i * (i - 1) / 2 + j : (size_t)j * (j - 1) / 2 + i; }
+
+}  // namespace
+
+// The sequential loop as a resumable state: or_mc_open does what precedes the reference's
+// timed loop (the initial energy, TotalEMatrix::initEM, and the first pair list), or_mc_advance
+// runs the next moves of the sweep loop, so that a caller can time the moves alone.
+struct or_mc {
+    or_system* s;
+    or_mc_opts o;
+    Rng rng;
+    int N;
+    double shprob;
+    double cut2 = 0.0;
+    bool list = false;
+    PairList pl;
+    bool matrix = false;             // TotalEMatrix (else TotalEFull)
+    std::vector<double> em, emTrial, changes;
+    double energy = 0.0;
+    long sweep = 1;                  // current sweep (1-based, as updater.cpp)
+    long step = 1;                   // next step of the current sweep (1..N)
+    double setupSeconds = 0.0;
+};
+
+namespace {
+
+// TotalEMatrix::oneToAll / TotalEFull::oneToAll with the pair list (totalenergycalculator.h:
+// 355-381, 561-580): the target's old energy from the matrix, or by pair energies.
+double mcOld(or_mc& m, int t) {
     double e = 0.0;
-    for (int j : pl->nb[t]) e += or_pair_energy(s, t, j, nullptr, nullptr);
+    if (m.list) {
+        const int* id = m.pl.ids.data() + m.pl.start[t];
+        const int cnt = m.pl.count[t];
+        if (m.matrix) {
+            for (int k = 0; k < cnt; ++k) e += m.em[emIdx(t, id[k])];
+        } else {
+            const Con con = getConlist(m.s, t);
+            for (int k = 0; k < cnt; ++k) e += pairEnergyCon(m.s, t, id[k], con, nullptr, nullptr);
+        }
+        return e;
+    }
+    if (m.matrix) {
+        for (int i = 0; i < m.N; ++i) if (i != t) e += m.em[emIdx(t, i)];
+        return e;
+    }
+    return or_one_to_all(m.s, t);
+}
+
+// oneToAllTrial (:383-415): pair energies of the moved target, kept in `changes`.
+double mcTrial(or_mc& m, int t) {
+    double e = 0.0;
+    const Con con = getConlist(m.s, t);
+    if (m.list) {
+        const int* id = m.pl.ids.data() + m.pl.start[t];
+        const int cnt = m.pl.count[t];
+        if (m.matrix) m.changes.resize(cnt);
+        for (int k = 0; k < cnt; ++k) {
+            double v = pairEnergyCon(m.s, t, id[k], con, nullptr, nullptr);
+            if (m.matrix) m.changes[k] = v;
+            e += v;
+        }
+        return e;
+    }
+    if (m.matrix) m.changes.assign(m.N, 0.0);
+    for (int i = 0; i < m.N; ++i) {
+        if (i == t) continue;
+        double v = pairEnergyCon(m.s, t, i, con, nullptr, nullptr);
+        if (m.matrix) m.changes[i] = v;
+        e += v;
+    }
+    return e;
+}
+
+// EnergyMatrixF::fixEMatrixSingle (:61-79)
+void mcCommit(or_mc& m, int t) {
+    if (!m.matrix) return;
+    if (m.list) {
+        const int* id = m.pl.ids.data() + m.pl.start[t];
+        for (int k = 0; k < m.pl.count[t]; ++k) m.em[emIdx(t, id[k])] = m.changes[k];
+    } else {
+        for (int i = 0; i < m.N; ++i) if (i != t) m.em[emIdx(t, i)] = m.changes[i];
+    }
+}
+
+// allToAll(energyMatrix) (:502-521) into `out`, or TotalEFull::allToAll (:540-556).
+double mcAllPairs(or_mc& m, std::vector<double>* out) {
+    if (!out) return or_all_to_all(m.s);
+    double e = 0.0;
+    for (int i = 1; i < m.N; ++i) {
+        const Con con = getConlist(m.s, i);
+        for (int j = 0; j < i; ++j) {
+            double v = pairEnergyCon(m.s, i, j, con, nullptr, nullptr);
+            (*out)[emIdx(i, j)] = v;
+            e += v;
+        }
+    }
     return e;
 }
 
 }  // namespace
 
-extern "C" int or_mc_run(or_system* s, const or_mc_opts* o, or_mc_stats* st) {
-    std::memset(st, 0, sizeof(*st));
-    Rng rng{(uint64_t)o->seed * 0x2545F4914F6CDD1Dull + 1};
-    const int N = s->n;
-    if (N <= 0) return -1;
-    double shprob = o->shave / (double)N;
-    PairList plist;
-    PairList* pl = nullptr;
-    double cut2 = 0.0;
+extern "C" or_mc* or_mc_open(or_system* s, const or_mc_opts* o) {
+    if (!s || !o || s->n <= 0) return nullptr;
+    if (o->shave > 0.0 && o->ptype != 1) return nullptr;     // ptype 1 volume moves only
+    auto t0 = std::chrono::steady_clock::now();
+    or_mc* m = new or_mc();
+    m->s = s;
+    m->o = *o;
+    m->rng = Rng{(uint64_t)o->seed * 0x2545F4914F6CDD1Dull + 1};
+    m->N = s->n;
+    m->shprob = o->shave / (double)s->n;
+    m->matrix = o->energy_matrix != 0;
     if (o->pairlist_update > 0) {
-        double c = o->transmx;    // AVER of equal step sizes
+        // the pair-list cutoff of main.cpp:117-126 (equal step sizes: AVER is the step)
+        double c = o->transmx;
         c *= (1 + o->pairlist_update) * 2;
         c += sqrt(s->sqmaxcut);
-        cut2 = c * c;
-        pl = &plist;
+        m->cut2 = c * c;
+        m->list = true;
     }
+    if (m->matrix) {
+        size_t sz = (size_t)m->N * (m->N - 1) / 2 + 1;
+        m->em.assign(sz, 0.0);
+        m->emTrial.assign(sz, 0.0);
+        m->energy = mcAllPairs(*m, &m->em);      // initEM
+    } else {
+        m->energy = or_all_to_all(s);
+    }
+    if (m->list) m->pl.build(s, m->cut2);          // before the first sweep (updater.cpp:176-190)
+    m->setupSeconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return m;
+}
+
+extern "C" void or_mc_close(or_mc* m) { delete m; }
+
+extern "C" double or_mc_energy(const or_mc* m) { return m ? m->energy : 0.0; }
+
+extern "C" double or_mc_setup_seconds(const or_mc* m) { return m ? m->setupSeconds : 0.0; }
+
+// Runs `moves` more steps of the sweep loop (updater.cpp:192-230); stats accumulate into st
+// (moves, acceptance counts, running energy, seconds spent here).
+extern "C" int or_mc_advance(or_mc* m, long moves, or_mc_stats* st) {
+    if (!m || !st || moves < 0) return -1;
+    or_system* s = m->s;
+    const or_mc_opts* o = &m->o;
+    const int N = m->N;
     auto t0 = std::chrono::steady_clock::now();
-    double energy = or_all_to_all(s);
-    st->energy_start = energy;
-    long moves = 0;
-    for (long sweep = 1; sweep <= o->nsweeps; ++sweep) {
-        if (pl && (sweep == 1 || sweep % o->pairlist_update == 0)) pl->build(s, cut2);
-        for (int step = 1; step <= N; ++step) {
-            if (o->max_moves > 0 && moves >= o->max_moves) goto finish;
-            ++moves;
-            double u = rng();
-            if (u < shprob && o->ptype == 1) {
-                double psch = o->edge_mx * (rng() - 0.5);
-                double pvol = s->box[0] * s->box[1] * s->box[2];
-                double b0[3] = {s->box[0], s->box[1], s->box[2]};
-                s->box[0] += psch; s->box[1] += psch; s->box[2] += psch;
-                double pvoln = s->box[0] * s->box[1] * s->box[2];
-                double enermove = o->press * (pvoln - pvol) - (double)N * o->temper * log(pvoln / pvol);
-                double enew = or_all_to_all(s);
-                enermove += enew;
-                bool rej = !(enermove <= energy) && !(exp(-1.0 * (enermove - energy) / o->temper) > rng());
-                if (rej) { s->box[0] = b0[0]; s->box[1] = b0[1]; s->box[2] = b0[2]; ++st->rej_vol; }
-                else { ++st->acc_vol; energy = enew; }
-                continue;
+    long done = 0;
+    while (done < moves) {
+        if (m->step > N) { m->step = 1; ++m->sweep; }
+        if (m->step == 1 && m->list && m->sweep > 1 && m->sweep % o->pairlist_update == 0) m->pl.build(s, m->cut2);
+        ++m->step;
+        ++done;
+        double u = m->rng();
+        if (u < m->shprob) {
+            // pressureMove, ptype 1 (movecreator.cpp:390-421)
+            double psch = o->edge_mx * (m->rng() - 0.5);
+            double pvol = s->box[0] * s->box[1] * s->box[2];
+            double b0[3] = {s->box[0], s->box[1], s->box[2]};
+            s->box[0] += psch; s->box[1] += psch; s->box[2] += psch;
+            double pvoln = s->box[0] * s->box[1] * s->box[2];
+            double enermove = o->press * (pvoln - pvol) - (double)N * o->temper * log(pvoln / pvol);
+            double enew = mcAllPairs(*m, m->matrix ? &m->emTrial : nullptr);
+            enermove += enew;
+            bool rej = !(enermove <= m->energy) && !(exp(-1.0 * (enermove - m->energy) / o->temper) > m->rng());
+            if (rej) { s->box[0] = b0[0]; s->box[1] = b0[1]; s->box[2] = b0[2]; ++st->rej_vol; }
+            else {
+                ++st->acc_vol;
+                m->energy = enew;
+                if (m->matrix) std::swap(m->em, m->emTrial);   // update(): swapEMatrices
             }
-            int target = (int)(rng() * N);
-            or_particle orig = s->p[target];
-            const or_param& d = P(s, orig.type, orig.type);
-            double eold = oneToAllList(s, target, pl);
-            bool displace = (rng() < 0.5) || d.geotype[0] >= SP;
-            if (displace) {
-                or_vec dr = randomUnitSphere(rng);
-                s->p[target].pos.x += dr.x * o->transmx / s->box[0];
-                s->p[target].pos.y += dr.y * o->transmx / s->box[1];
-                s->p[target].pos.z += dr.z * o->transmx / s->box[2];
-            } else {
-                double ang = o->rot_angle * rng();
-                or_vec ax = randomUnitSphere(rng);
-                or_psc_rotate(&s->p[target], d.geotype[0], ang, ax, rng() < 0.5);
-                ortho(s->p[target].pd[0], s->p[target].dir);
-            }
-            double enew = oneToAllList(s, target, pl);
-            bool rej = !(enew <= eold) && !(exp(-1.0 * (enew - eold) / o->temper) > rng());
-            if (rej) {
-                s->p[target] = orig;
-                if (displace) ++st->rej_trans; else ++st->rej_rot;
-            } else {
-                energy += enew - eold;
-                if (displace) ++st->acc_trans; else ++st->acc_rot;
-            }
+            continue;
+        }
+        int target = (int)(m->rng() * N);
+        or_particle orig = s->p[target];
+        const or_param& d = P(s, orig.type, orig.type);
+        bool displace = (m->rng() < 0.5) || d.geotype[0] >= SP;
+        double eold = mcOld(*m, target);
+        if (displace) {
+            or_vec dr = randomUnitSphere(m->rng);
+            s->p[target].pos.x += dr.x * o->transmx / s->box[0];
+            s->p[target].pos.y += dr.y * o->transmx / s->box[1];
+            s->p[target].pos.z += dr.z * o->transmx / s->box[2];
+        } else {
+            double ang = o->rot_angle * m->rng();
+            or_vec ax = randomUnitSphere(m->rng);
+            or_psc_rotate(&s->p[target], d.geotype[0], ang, ax, m->rng() < 0.5);
+            ortho(s->p[target].pd[0], s->p[target].dir);
+        }
+        double enew = mcTrial(*m, target);
+        bool rej = !(enew <= eold) && !(exp(-1.0 * (enew - eold) / o->temper) > m->rng());
+        if (rej) {
+            s->p[target] = orig;
+            if (displace) ++st->rej_trans; else ++st->rej_rot;
+        } else {
+            m->energy += enew - eold;
+            mcCommit(*m, target);
+            if (displace) ++st->acc_trans; else ++st->acc_rot;
         }
     }
-finish:
-    st->moves = moves;
-    st->energy = energy;
-    st->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    st->moves += done;
+    st->energy = m->energy;
+    st->seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return 0;
+}
+
+extern "C" int or_mc_run(or_system* s, const or_mc_opts* o, or_mc_stats* st) {
+    std::memset(st, 0, sizeof(*st));
+    or_mc* m = or_mc_open(s, o);
+    if (!m) return -1;
+    st->energy_start = m->energy;
+    long total = o->nsweeps * (long)s->n;
+    if (o->max_moves > 0 && o->max_moves < total) total = o->max_moves;
+    int rc = or_mc_advance(m, total, st);
+    st->seconds += m->setupSeconds;
+    or_mc_close(m);
+    return rc;
 }
 
 // ---- Wang-Landau order parameters --------------------------------------------------------

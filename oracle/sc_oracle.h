@@ -79,6 +79,12 @@ double or_pair_energy(const or_system* s, int i, int j, unsigned* bits, double* 
 double or_one_to_all(const or_system* s, int target);
 double or_all_to_all(const or_system* s);
 double or_mol2others(const or_system* s, int first, int size);
+/* PairE over a batch of ordered pairs (bits, dsq may be NULL). */
+void or_pair_energies(const or_system* s, long n, const int* I, const int* J, double* E, unsigned* bits, double* dsq);
+/* The ordered pairs (i a target, or any particle when targets is NULL; j != i) that PairE's
+ * prefilter admits (paire.h:1209-1215): image distance^2 <= sqmaxcut, or j bonded to i.
+ * At most cap written; *count = all of them. */
+void or_prefilter_pairs(const or_system* s, int nt, const int* targets, long cap, int* I, int* J, long* count);
 
 int or_derive_params(const or_type_in* types, int ntypes, const unsigned char* exclusions /* 40x40 or NULL */,
                      or_param* out /* 40x40 */, double* sqmaxcut, double* maxcut);
@@ -96,6 +102,9 @@ typedef struct {
     int ptype;
     int pairlist_update; /* 0: brute force; k: Verlet list rebuilt every k sweeps */
     long max_moves;      /* stop after this many attempted moves (0: no bound) */
+    int energy_matrix;   /* 1: TotalEMatrix (old energies from the stored pair energies, the reference's
+                            default); 0: TotalEFull (old and new energies by pair evaluation) */
+    int pad_;
 } or_mc_opts;
 
 typedef struct {
@@ -106,6 +115,17 @@ typedef struct {
 } or_mc_stats;
 
 int or_mc_run(or_system* s, const or_mc_opts* o, or_mc_stats* st);
+
+/* The same loop as a resumable state, so that the moves can be timed apart from the set-up
+ * the reference does before its timed loop (initial energy / energy matrix, first pair
+ * list).  or_mc_open returns NULL for an empty system or volume moves of a ptype other than
+ * 1; or_mc_advance runs `moves` more steps and adds to *st (moves, acceptances, seconds). */
+typedef struct or_mc or_mc;
+or_mc* or_mc_open(or_system* s, const or_mc_opts* o);
+int or_mc_advance(or_mc* m, long moves, or_mc_stats* st);
+double or_mc_energy(const or_mc* m);
+double or_mc_setup_seconds(const or_mc* m);
+void or_mc_close(or_mc* m);
 
 /* Wang-Landau table and walker state of or_wl_run. */
 typedef struct {

@@ -4,6 +4,7 @@ The oracle is test infrastructure: only tests/, __graft_entry__.smoke() and the
 CPU-baseline leg of bench.py use it, always as the checker.
 """
 import ctypes as C
+import math
 import os
 import subprocess
 
@@ -58,7 +59,7 @@ class McOpts(C.Structure):
                 ("shave", C.c_double), ("chainprob", C.c_double), ("transmx", C.c_double),
                 ("rot_angle", C.c_double), ("edge_mx", C.c_double), ("chainmmx", C.c_double),
                 ("chainr_angle", C.c_double), ("ptype", C.c_int), ("pairlist_update", C.c_int),
-                ("max_moves", C.c_long)]
+                ("max_moves", C.c_long), ("energy_matrix", C.c_int), ("pad_", C.c_int)]
 
 
 class McStats(C.Structure):
@@ -73,15 +74,22 @@ class WlState(C.Structure):
                 ("cur", C.c_long * 2), ("updates", C.c_long), ("converged", C.c_int), ("pad_", C.c_int)]
 
 
-_lib = None
+LIB_FAST = os.path.join(ROOT, "oracle", "_build", "liboracle_fast.so")
+_libs = {}
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        if not os.path.exists(LIB):
+def lib(fast=False):
+    """The oracle library; fast=True: its -Ofast build (CPU timing legs only)."""
+    path = LIB_FAST if fast else LIB
+    if path not in _libs:
+        if not os.path.exists(path):
             subprocess.run(["make", "-C", os.path.join(ROOT, "oracle")], check=True, capture_output=True)
-        L = C.CDLL(LIB)
+        _libs[path] = _bind(C.CDLL(path))
+    return _libs[path]
+
+
+def _bind(L):
+    if True:
         L.or_pair_energy.restype = C.c_double
         L.or_pair_energy.argtypes = [C.POINTER(System), C.c_int, C.c_int, C.POINTER(C.c_uint), C.POINTER(C.c_double)]
         L.or_one_to_all.restype = C.c_double
@@ -103,8 +111,22 @@ def lib():
         L.or_wl_orders.argtypes = [C.POINTER(System), C.POINTER(C.c_int), C.POINTER(C.c_double),
                                    C.POINTER(C.c_double), C.POINTER(C.c_long), C.POINTER(C.c_double),
                                    C.POINTER(C.c_double)]
-        _lib = L
-    return _lib
+        L.or_pair_energies.restype = None
+        L.or_pair_energies.argtypes = [C.POINTER(System), C.c_long, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                       C.POINTER(C.c_double), C.POINTER(C.c_uint), C.POINTER(C.c_double)]
+        L.or_prefilter_pairs.restype = None
+        L.or_prefilter_pairs.argtypes = [C.POINTER(System), C.c_int, C.POINTER(C.c_int), C.c_long,
+                                         C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_long)]
+        L.or_mc_open.restype = C.c_void_p
+        L.or_mc_open.argtypes = [C.POINTER(System), C.POINTER(McOpts)]
+        L.or_mc_advance.restype = C.c_int
+        L.or_mc_advance.argtypes = [C.c_void_p, C.c_long, C.POINTER(McStats)]
+        L.or_mc_energy.restype = C.c_double
+        L.or_mc_energy.argtypes = [C.c_void_p]
+        L.or_mc_setup_seconds.restype = C.c_double
+        L.or_mc_setup_seconds.argtypes = [C.c_void_p]
+        L.or_mc_close.argtypes = [C.c_void_p]
+    return L
 
 
 def vec(a):
@@ -255,3 +277,224 @@ def parse_types(top_text):
             for a, b in zip(nums[::2], nums[1::2]):
                 excl[a, b] = excl[b, a] = 1
     return out, excl
+
+
+# --- the oracle's own set-up from the reference's three inputs ---------------------------------
+# Restates Sim::readOptions (scOOP/structures/sim.h:123-406, unit conversions :359-366),
+# Inicializer::initTop / initConfig (scOOP/mc/inicializer.cpp:16-298: [Types], [Molecules],
+# [System], the box line, per-particle lines, usePBC, makeMoleculeWhole) and partVecInit
+# (scOOP/structures/Conf.cpp:97-102) without the GPU library, so that a CPU baseline sets up
+# its system from the same texts the GPU path reads.
+
+PIH = 1.57079632679489661923132169163975
+
+
+def parse_options(text):
+    d = {}
+    for raw in text.splitlines():
+        line = raw.split("#", 1)[0]
+        if "=" not in line:
+            continue
+        k, v = line.split("=", 1)
+        d[k.strip()] = v.strip()
+    return d
+
+
+def molecules(top):
+    """[Molecules] definitions (name, particle types, bond constants) in definition order (the
+    molType index) and the [System] entries (name, count) in order."""
+    defs, order, key, cur = [], [], None, None
+    for raw in top.splitlines():
+        line = raw.split("#", 1)[0].strip()
+        if not line:
+            continue
+        if line.startswith("["):
+            key = line[1:].split("]")[0].strip().upper()
+            continue
+        if key == "MOLECULES":
+            if "{" in line:
+                cur = {"name": line.split(":")[0].strip(), "types": [], "bonds": {}}
+                defs.append(cur)
+            elif line.startswith("}"):
+                cur = None
+            elif cur is not None and ":" in line:
+                k, v = line.split(":", 1)
+                k = k.strip().lower()
+                if k == "particles":
+                    cur["types"].append(int(v.split()[0]))
+                else:
+                    cur["bonds"][k] = [float(x) for x in v.split()[:2]]
+        elif key == "SYSTEM":
+            name, cnt = line.split()[:2]
+            order.append((name, int(cnt)))
+    return defs, order
+
+
+def _normalise(v):
+    t = math.sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2])
+    if t != 0.0:
+        t = 1.0 / t
+        return [v[0] * t, v[1] * t, v[2] * t]
+    return v
+
+
+class TextSystem:
+    """An or_system (with its ctypes buffers) and McOpts set up from options / top.init /
+    config.init texts by the oracle alone."""
+
+    def __init__(self, options, top, config):
+        opts = parse_options(options)
+        types, excl = parse_types(top)
+        arr = (TypeIn * len(types))(*types)
+        self.params = (Param * (MAXT * MAXT))()
+        sq, mc = C.c_double(), C.c_double()
+        if lib().or_derive_params(arr, len(types), excl.ctypes.data, self.params, C.byref(sq), C.byref(mc)) != 0:
+            raise ValueError("oracle: top.init rejected")
+        defs, order = molecules(top)
+        ptypes, pmol = [], []
+        first = {}
+        for name, cnt in order:
+            m = next(k for k, d in enumerate(defs) if d["name"] == name)
+            first.setdefault(m, (len(ptypes), cnt))
+            for _ in range(cnt):
+                for ty in defs[m]["types"]:
+                    ptypes.append(ty)
+                    pmol.append(m)
+        self.mols = (MolType * max(1, len(defs)))()
+        for k, d in enumerate(defs):
+            ms = self.mols[k]
+            ms.size = len(d["types"])
+            ms.first, ms.count = first.get(k, (0, 0))
+            for b in ("bond1", "bond2", "bondd", "bondh", "angle1", "angle2"):
+                c, eq = d["bonds"].get(b, [-1.0, -1.0])
+                setattr(ms, b + "c", c)
+                setattr(ms, b + "eq", eq)
+        lines = [l.split("#", 1)[0].strip() for l in config.splitlines()]
+        lines = [l for l in lines if l]
+        box = [float(x) for x in lines[0].replace("x", " ").split()[-3:]]
+        n = len(ptypes)
+        if len(lines) - 1 < n:
+            raise ValueError("config.init: fewer particle lines than [System] declares")
+        self.parts = (Particle * n)()
+        for i in range(n):
+            f = [float(x) for x in lines[1 + i].split()[:9]]
+            pos = [f[0] / box[0], f[1] / box[1], f[2] / box[2]]
+            for k in range(3):                      # Cuboid::usePBC
+                while pos[k] < 0.0:
+                    pos[k] += 1.0
+                while pos[k] > 1.0:
+                    pos[k] -= 1.0
+            d = _normalise(f[3:6])
+            pd = f[6:9]
+            dp = pd[0] * d[0] + pd[1] * d[1] + pd[2] * d[2]
+            pd = _normalise([pd[0] - dp * d[0], pd[1] - dp * d[1], pd[2] - dp * d[2]])
+            p = self.parts[i]
+            p.pos, p.dir, p.pd[0] = vec(pos), vec(d), vec(pd)
+            p.type, p.molType = ptypes[i], pmol[i]
+        for k, d in enumerate(defs):                # Conf::makeMoleculeWhole
+            size = len(d["types"])
+            if size <= 1:
+                continue
+            f0, cnt = first.get(k, (0, 0))
+            for s in range(f0, f0 + size * cnt, size):
+                for q in range(s + 1, s + size):
+                    a, b = self.parts[q].pos, self.parts[q - 1].pos
+                    r = [(a.x - b.x), (a.y - b.y), (a.z - b.z)]
+                    r = [(x - round(x)) for x in r]
+                    self.parts[q].pos = Vec(b.x + r[0], b.y + r[1], b.z + r[2])
+        for i in range(n):
+            t = self.parts[i].type
+            lib().or_particle_init(C.byref(self.parts[i]), C.byref(self.params[t * MAXT + t]))
+        self.sys = System()
+        self.sys.n, self.sys.nmol = n, len(defs)
+        self.sys.p = C.cast(self.parts, C.POINTER(Particle))
+        self.sys.mols = C.cast(self.mols, C.POINTER(MolType))
+        self.sys.params = C.cast(self.params, C.POINTER(Param))
+        for k in range(3):
+            self.sys.box[k] = box[k]
+        self.sys.sqmaxcut = sq.value
+        o = McOpts()
+        o.seed = int(opts.get("seed", "1"))
+        o.temper = float(opts.get("temper", "1"))
+        o.press = float(opts.get("press", "0"))
+        o.shave = float(opts.get("shave", "0"))
+        o.transmx = 2.0 * float(opts.get("transmx", "0"))
+        o.rot_angle = float(opts.get("rotmx", "0")) / 180.0 * PIH * 0.5
+        o.edge_mx = 2.0 * float(opts.get("edge_mx", "0"))
+        o.chainprob = float(opts.get("chainprob", "0"))
+        o.chainmmx = 2.0 * float(opts.get("chainmmx", "0"))
+        o.chainr_angle = float(opts.get("chainrmx", "0")) / 180.0 * PIH
+        o.ptype = int(opts.get("ptype", "0").split()[0])
+        o.pairlist_update = int(opts.get("pairlist_update", "0"))
+        o.nsweeps = int(opts.get("nsweeps", "0"))
+        self.opts = o
+
+    def all_to_all(self):
+        return lib().or_all_to_all(C.byref(self.sys))
+
+    def one_to_all(self, t):
+        return lib().or_one_to_all(C.byref(self.sys), int(t))
+
+    def set_state(self, parts, box):
+        """Takes a configuration from the GPU path (sc_particle records and box edges)."""
+        OracleSystem.set_state(self, parts, box)
+
+    def pair_energies(self, I, J):
+        I = np.ascontiguousarray(I, dtype=np.int32)
+        J = np.ascontiguousarray(J, dtype=np.int32)
+        n = len(I)
+        E = np.zeros(n)
+        B = np.zeros(n, np.uint32)
+        D = np.zeros(n)
+        lib().or_pair_energies(C.byref(self.sys), n, I.ctypes.data_as(C.POINTER(C.c_int)),
+                               J.ctypes.data_as(C.POINTER(C.c_int)), E.ctypes.data_as(C.POINTER(C.c_double)),
+                               B.ctypes.data_as(C.POINTER(C.c_uint)), D.ctypes.data_as(C.POINTER(C.c_double)))
+        return E, B, D
+
+    def prefilter_pairs(self, targets=None):
+        """Ordered pairs (i, j) PairE's prefilter admits (distance or bond)."""
+        T = None if targets is None else np.ascontiguousarray(targets, dtype=np.int32)
+        nt = self.sys.n if T is None else len(T)
+        tp = None if T is None else T.ctypes.data_as(C.POINTER(C.c_int))
+        cnt = C.c_long()
+        lib().or_prefilter_pairs(C.byref(self.sys), nt, tp, 0, None, None, C.byref(cnt))
+        I = np.zeros(max(1, cnt.value), np.int32)
+        J = np.zeros(max(1, cnt.value), np.int32)
+        lib().or_prefilter_pairs(C.byref(self.sys), nt, tp, cnt.value, I.ctypes.data_as(C.POINTER(C.c_int)),
+                                 J.ctypes.data_as(C.POINTER(C.c_int)), C.byref(cnt))
+        return I[:cnt.value], J[:cnt.value]
+
+
+class McRun:
+    """The oracle's sequential loop on a TextSystem, opened once (set-up outside any timing)
+    and advanced by `moves` at a time."""
+
+    def __init__(self, ts, seed=None, energy_matrix=True, fast=False):
+        self.ts = ts
+        self.L = lib(fast)
+        o = ts.opts
+        if seed is not None:
+            o.seed = seed
+        o.energy_matrix = 1 if energy_matrix else 0
+        self.h = self.L.or_mc_open(C.byref(ts.sys), C.byref(o))
+        if not self.h:
+            raise ValueError("oracle: loop refused (empty system or volume moves of a ptype other than 1)")
+        self.stats = McStats()
+
+    @property
+    def setup_seconds(self):
+        return self.L.or_mc_setup_seconds(self.h)
+
+    @property
+    def energy(self):
+        return self.L.or_mc_energy(self.h)
+
+    def advance(self, moves):
+        if self.L.or_mc_advance(self.h, int(moves), C.byref(self.stats)) != 0:
+            raise RuntimeError("oracle: or_mc_advance failed")
+        return self.stats
+
+    def close(self):
+        if self.h:
+            self.L.or_mc_close(self.h)
+            self.h = None
