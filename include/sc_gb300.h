@@ -88,7 +88,9 @@ typedef struct {
     int delayed;            /* 1: two-stage moves with the context's surrogate (sc_set_surrogate) as first stage */
     int variant;            /* move kernel, bit 0: more moves in flight per SM (large systems), else lowest
                                latency per move; bit 1: paired passes (two moves per stage C); bit 2: one
-                               dataflow launch per sweep instead of one launch per colour */
+                               dataflow launch per sweep instead of one launch per colour; -1: the reach
+                               and variant sc_tune measured fastest for this context (stencil 0 takes
+                               the tuned reach), else the dataflow sweep */
     int flow_wait_polls;    /* dataflow sweep: polls of one wait for a neighbouring cell before the
                                kernel gives up and the call returns SC_ERR_DEVICE (0: 2^19, about
                                0.2 s; a wait in a sound run lasts well under 20 ms) */
@@ -195,6 +197,40 @@ int sc_default_run(const sc_context* ctx, sc_run_params* p);
 /* Runs p->nsweeps sweeps on the device; stats->sweeps is the number run (fewer when a
  * Wang-Landau run converged, as the reference's loop stops there, updater.cpp:255-265). */
 int sc_simulate(sc_context* ctx, const sc_run_params* p, sc_run_stats* stats);
+
+/* No counterpart in the reference (its loop has no launch shapes to choose).  Times every
+ * candidate launch shape of the move kernel for p's mode (plain or delayed) on the context's
+ * current state, `sweeps` sweeps each after two warm-up sweeps: cell reach 1, 2, 3 (cells
+ * maxcut/reach wide: how many cells move at once and how many neighbours each stages) times
+ * kernel variants {colour-phase launches, dataflow sweep} x {lowest latency per move, more
+ * CTAs per SM}, plus paired passes for plain moves.  The state is restored before every
+ * candidate and at the end (the next run recomputes the exact energy).  *best = *p with the
+ * fastest stencil and variant, which later runs with variant = -1 use.  rates (may be NULL,
+ * room for 18) gets each candidate's moves/s, *ncand (may be NULL) their number.  Not with
+ * Wang-Landau weights (SC_ERR_UNSUPPORTED: the tuning sweeps would change them). */
+int sc_tune(sc_context* ctx, const sc_run_params* p, int sweeps, sc_run_params* best, double* rates, int* ncand);
+
+/* No counterpart in the reference: the move kernels' candidate screens, exposed so that
+ * they can be checked against the reference's prefilter (PairE::operator(), paire.h:1209-1215:
+ * r^2 > sqmaxcut and no bond -> energy 0).  For every target (targets[0..ntargets), or every
+ * particle when targets is NULL) and every other particle j, stage A is the FP32 candidate
+ * screen the kernels stage neighbours with (wrapped FP32 box fractions against (maxcut +
+ * margin)^2) and stage B their FP32 exact-zero screen (segment or point-segment distance
+ * beyond every branch's cut-off).  The pairs that pass stage A go to i[], j[] (in no
+ * particular order) with stage_b[k] = 1 when stage B keeps the pair; *count gets their
+ * number, SC_ERR_RANGE when it exceeds cap (nothing beyond cap is written).  The kernels
+ * evaluate bonded partners whatever these screens say. */
+int sc_screen_survivors(sc_context* ctx, int ntargets, const int* targets, long cap, int* i, int* j,
+                        unsigned char* stage_b, long* count);
+
+/* No counterpart in the reference.  FP64 rates of `device`, measured by the library's own
+ * probe kernels (the denominators of the move kernel's FP64 roofline): separate DMUL + DADD
+ * instructions per second with every SM full of warps; the same with one active lane per
+ * warp (per-lane rate; equal to the full rate / 32 when an FP64 warp instruction costs the
+ * same whatever its active lanes); DFMA FLOP/s (2 per FMA); the dependent latency of one
+ * FP64 operation in cycles.  Any output may be NULL.  Allocates and frees a small buffer. */
+int sc_fp64_rates(int device, double* dmul_dadd_per_s, double* one_lane_per_s, double* fma_flops,
+                  double* latency_cycles);
 
 /* --- Wang-Landau flat-histogram sampling --------------------------------------------------
  * WangLandau (scOOP/mc/wanglandau.h:16-690, wanglandau.cpp): with options wlm > 0 every move

@@ -106,6 +106,12 @@ SIGNATURES = [
     ("sc_trial_volume", C.c_int, [_P, C.c_double, _D]),
     ("sc_default_run", C.c_int, [_P, C.POINTER(RunParams)]),
     ("sc_simulate", C.c_int, [_P, C.POINTER(RunParams), C.POINTER(RunStats)]),
+    ("sc_tune", C.c_int, [_P, C.POINTER(RunParams), C.c_int, C.POINTER(RunParams), C.POINTER(C.c_double),
+                          C.POINTER(C.c_int)]),
+    ("sc_screen_survivors", C.c_int, [_P, C.c_int, C.POINTER(C.c_int), C.c_long, C.POINTER(C.c_int),
+                                      C.POINTER(C.c_int), C.POINTER(C.c_ubyte), C.POINTER(C.c_long)]),
+    ("sc_fp64_rates", C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                C.POINTER(C.c_double)]),
     ("sc_wl_load", C.c_int, [_P, C.c_char_p]),
     ("sc_wl_load_text", C.c_int, [_P, C.c_char_p]),
     ("sc_wl_get_info", C.c_int, [_P, C.POINTER(WlInfo)]),

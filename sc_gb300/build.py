@@ -15,7 +15,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libscgpu.so")
 
-SOURCES = ["sc_input.cpp", "sc_context.cu", "energy_kernels.cu", "sweep.cu", "noalloc.cu", "surrogate.cu", "wanglandau.cu"]
+SOURCES = ["sc_input.cpp", "sc_context.cu", "energy_kernels.cu", "sweep.cu", "noalloc.cu", "surrogate.cu", "wanglandau.cu",
+           "fp64_probe.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
          "--expt-relaxed-constexpr", "-diag-suppress", "1444"]

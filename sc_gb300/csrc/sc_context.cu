@@ -669,6 +669,7 @@ int sc_default_run(const sc_context* ctx, sc_run_params* p) {
     p->chainmmx = o.chainmmx;
     p->chain_angle = o.chain_angle;
     p->check_every = 100;
+    p->variant = -1;       // sc_tune's choice for this context, else the dataflow sweep
     return SC_OK;
 }
 
@@ -676,6 +677,19 @@ int sc_simulate(sc_context* ctx, const sc_run_params* p, sc_run_stats* stats) {
     if (!ctx || !p || !stats) return fail(SC_ERR_ARG, "null argument");
     DeviceScope dev(C(ctx)->device);
     return runSweeps(C(ctx), *p, *stats);
+}
+
+int sc_screen_survivors(sc_context* ctx, int ntargets, const int* targets, long cap, int* i, int* j,
+                        unsigned char* stage_b, long* count) {
+    if (!ctx || !count || cap < 0 || (cap > 0 && (!i || !j || !stage_b))) return fail(SC_ERR_ARG, "null argument");
+    DeviceScope dev(C(ctx)->device);
+    return screenSurvivors(C(ctx), targets ? ntargets : (int)C(ctx)->conf.p.size(), targets, cap, i, j, stage_b, count);
+}
+
+int sc_tune(sc_context* ctx, const sc_run_params* p, int sweeps, sc_run_params* best, double* rates, int* ncand) {
+    if (!ctx || !p || !best) return fail(SC_ERR_ARG, "null argument");
+    DeviceScope dev(C(ctx)->device);
+    return tuneSweeps(C(ctx), *p, sweeps, *best, rates, ncand);
 }
 
 struct sc_replicas {

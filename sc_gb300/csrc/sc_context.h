@@ -55,6 +55,10 @@ struct Context {
     SweepEngine* engine = nullptr;
     Batch* batch = nullptr;
     long lastLaunches = 0;     // kernels launched by the last move loop
+    // sc_tune's choice per mode (index: delayed 0 / 1): stencil reach and kernel variant
+    // used by runs that pass variant = -1 (stencil 0 then takes the tuned reach too)
+    int tunedStencil[2] = {0, 0};
+    int tunedVariant[2] = {-1, -1};
 
     Context() = default;
     Context(const Context&) = delete;
@@ -101,6 +105,9 @@ float surrogateCutoff(const Surrogate* s);
 float surrogateRange(Context* c);
 int cudaFail(cudaError_t e, const char* where);
 int runSweeps(Context* c, const sc_run_params& p, sc_run_stats& st);
+int tuneSweeps(Context* c, const sc_run_params& p, int sweeps, sc_run_params& best, double* rates, int* ncand);
+int screenSurvivors(Context* c, int ntargets, const int* targets, long cap, int* I, int* J, unsigned char* B,
+                    long* count);
 void destroyEngine(Context* c);
 int createReplicas(Context* const* sys, int nrep, const double* temps, const int* group, void** out);
 void destroyReplicas(void* h);

@@ -1471,6 +1471,38 @@ __global__ void __launch_bounds__(kMoveThreads, 3) kColourDense(const SweepArgs*
     colourBody(A, phase);
 }
 
+// ---- verification of the candidate screens ---------------------------------------------
+// For targets i (a list, or every particle) and every other particle j: stage A (the FP32
+// candidate screen: wrapped FP32 box fractions, distance^2 against candThreshold) and stage
+// B (the FP32 exact-zero screen, screenedOutF on the FP32 separation and axes), computed by
+// the same device functions from the same FP32 values as the move kernels (frac32 of the
+// FP64 box fractions, as kSortCells and buildProposal make them; FP32 axes as cellDirF).
+// Pairs that pass stage A are appended (in no particular order) with their stage-B verdict.
+__global__ void kScreenSurvivors(DevState s, DevTables t, const int* targets, int ntargets, long long cap, int* outI,
+                                 int* outJ, unsigned char* outB, unsigned long long* count) {
+    const double3 box = make_double3(s.box[0], s.box[1], s.box[2]);
+    const float thr32 = candThreshold(t.sqmaxcut, box);
+    const float bxF = (float)box.x, byF = (float)box.y, bzF = (float)box.z;
+    const long long total = (long long)ntargets * s.n;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += stride) {
+        const int ti = (int)(e / s.n), j = (int)(e - (long long)ti * s.n);
+        const int i = targets ? targets[ti] : ti;
+        if (i == j) continue;
+        const double4_32a pi = s.pos[i], pj = s.pos[j];
+        const float3 fi = make_float3(frac32(pi.x), frac32(pi.y), frac32(pi.z));
+        const float4 cj = make_float4(frac32(pj.x), frac32(pj.y), frac32(pj.z), (float)pj.w);
+        if (!(dist2f(cj, fi, box) <= thr32)) continue;
+        const double4_32a di = s.dir[i], dj = s.dir[j];
+        const float3 r = pairVecF(fi, cj, bxF, byF, bzF);
+        const PairParam& pp = t.params[(int)pi.w * t.ntypes + (int)pj.w];
+        const bool keep = !screenedOutF(pp, r, make_float3((float)di.x, (float)di.y, (float)di.z),
+                                        make_float3((float)dj.x, (float)dj.y, (float)dj.z));
+        const unsigned long long k = atomicAdd(count, 1ull);
+        if ((long long)k < cap) { outI[k] = i; outJ[k] = j; outB[k] = keep ? 1 : 0; }
+    }
+}
+
 // ---- dataflow sweep ---------------------------------------------------------------------
 // All colour phases of a sweep in one launch.  CTAs take cells in phase order from a ticket
 // counter; a cell first waits until every cell of an earlier phase within its stencil (+-s
@@ -3170,15 +3202,28 @@ static int checkParams(const sc_run_params& p) {
     if (!(p.temper > 0)) return fail(SC_ERR_ARG, "temper must be positive");
     if (p.ptype < 0 || p.ptype > 5) return fail(SC_ERR_ARG, "ptype must be 0..5 (movecreator.cpp:349-546)");
     if (p.stencil < 0 || p.stencil > 3) return fail(SC_ERR_ARG, "stencil must be 0 (auto), 1, 2 or 3");
-    if (p.variant < 0 || p.variant > 7) return fail(SC_ERR_ARG, "variant must be 0..7");
+    if (p.variant < -1 || p.variant > 7) return fail(SC_ERR_ARG, "variant must be -1 (tuned) or 0..7");
     if (p.flow_wait_polls < 0) return fail(SC_ERR_ARG, "flow_wait_polls must be >= 0");
     return SC_OK;
 }
 
-int runSweeps(Context* c, const sc_run_params& p, sc_run_stats& st) {
+// variant = -1: the reach and kernel variant sc_tune measured fastest for this context and
+// mode (stencil 0 takes the tuned reach; an explicit stencil is kept), else the dataflow
+// sweep with the default reach.
+static sc_run_params resolveTuned(const Context* c, const sc_run_params& p) {
+    sc_run_params q = p;
+    if (p.variant != -1) return q;
+    const int m = p.delayed ? 1 : 0;
+    q.variant = c->tunedVariant[m] >= 0 ? c->tunedVariant[m] : 4;
+    if (p.stencil == 0 && c->tunedVariant[m] >= 0) q.stencil = c->tunedStencil[m];
+    return q;
+}
+
+int runSweeps(Context* c, const sc_run_params& p0, sc_run_stats& st) {
     std::memset(&st, 0, sizeof st);
-    int rc = checkParams(p);
+    int rc = checkParams(p0);
     if (rc) return rc;
+    const sc_run_params p = resolveTuned(c, p0);
     if (c->conf.p.empty()) return SC_OK;
     if (p.delayed && !c->surrogate) return fail(SC_ERR_STATE, "delayed = 1 needs a surrogate (sc_set_surrogate)");
     if ((rc = checkMoves(c))) return rc;
@@ -3207,6 +3252,109 @@ int runSweeps(Context* c, const sc_run_params& p, sc_run_stats& st) {
     // unmoved and their energy changes unsummed: the next run recomputes the exact energy
     if (rc) c->engine->energyKnown = false;
     return rc;
+}
+
+// The candidate screens of the move kernels over every (target, particle) pair: the pairs
+// that pass stage A, with stage B's verdict (kScreenSurvivors).
+int screenSurvivors(Context* c, int ntargets, const int* targets, long cap, int* I, int* J, unsigned char* B,
+                    long* count) {
+    int rc = c->ensureDevice();
+    if (rc) return rc;
+    const int n = (int)c->conf.p.size();
+    if (ntargets < 0 || (!targets && ntargets != n)) return fail(SC_ERR_ARG, "sc_screen_survivors: targets");
+    for (int k = 0; targets && k < ntargets; ++k)
+        if (targets[k] < 0 || targets[k] >= n) return fail(SC_ERR_ARG, "sc_screen_survivors: target out of range");
+    int *dT = nullptr, *dI = nullptr, *dJ = nullptr;
+    unsigned char* dB = nullptr;
+    unsigned long long* dN = nullptr;
+    const long capd = std::max(cap, 1L);
+    cudaError_t e = cudaSuccess;
+    auto freeAll = [&]() { cudaFree(dT); cudaFree(dI); cudaFree(dJ); cudaFree(dB); cudaFree(dN); };
+    if (targets) e = cudaMalloc(&dT, sizeof(int) * std::max(ntargets, 1));
+    if (e == cudaSuccess) e = cudaMalloc(&dI, sizeof(int) * capd);
+    if (e == cudaSuccess) e = cudaMalloc(&dJ, sizeof(int) * capd);
+    if (e == cudaSuccess) e = cudaMalloc(&dB, capd);
+    if (e == cudaSuccess) e = cudaMalloc(&dN, sizeof(unsigned long long));
+    if (e == cudaSuccess && targets)
+        e = cudaMemcpyAsync(dT, targets, sizeof(int) * ntargets, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(dN, 0, sizeof(unsigned long long), c->stream);
+    if (e != cudaSuccess) { freeAll(); return cudaFail(e, "sc_screen_survivors: buffers"); }
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    kScreenSurvivors<<<std::max(1, sms) * 8, 256, 0, c->stream>>>(c->d, c->tables, dT, ntargets, cap, dI, dJ, dB, dN);
+    unsigned long long cnt = 0;
+    e = cudaMemcpyAsync(&cnt, dN, sizeof cnt, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    const long got = (long)std::min<unsigned long long>(cnt, (unsigned long long)cap);
+    if (e == cudaSuccess && got > 0) {
+        e = cudaMemcpy(I, dI, sizeof(int) * got, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) e = cudaMemcpy(J, dJ, sizeof(int) * got, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) e = cudaMemcpy(B, dB, got, cudaMemcpyDeviceToHost);
+    }
+    freeAll();
+    if (e != cudaSuccess) return cudaFail(e, "sc_screen_survivors");
+    *count = (long)cnt;
+    if ((long long)cnt > (long long)cap) return fail(SC_ERR_RANGE, "sc_screen_survivors: more survivors than cap");
+    return SC_OK;
+}
+
+// The tuner: times every (reach, kernel variant) candidate for p's mode on the context's
+// current state (restored before every candidate and at the end, so the state the caller
+// sees is unchanged; the running energy is recomputed by the next run), and keeps the
+// fastest for later runs with variant = -1.  Candidates: reach 1, 2, 3 (cells maxcut/s
+// wide: how many cells move at once and how many candidates each stages) times variants
+// {colour-phase launches, dataflow sweep} x {lowest latency, more CTAs per SM}, plus paired
+// passes for plain moves.
+int tuneSweeps(Context* c, const sc_run_params& p, int sweeps, sc_run_params& best, double* rates, int* ncand) {
+    if (sweeps < 1) return fail(SC_ERR_ARG, "sc_tune: sweeps must be >= 1");
+    if (wlActive(c)) return fail(SC_ERR_UNSUPPORTED, "sc_tune with Wang-Landau weights: tuning sweeps would change them");
+    int rc = checkParams(p);
+    if (rc) return rc;
+    if (c->conf.p.empty()) return fail(SC_ERR_STATE, "sc_tune: no particles");
+    if ((rc = c->ensureDevice())) return rc;
+    if ((rc = c->downloadState())) return rc;
+    const std::vector<Particle> snap = c->conf.p;
+    const Vec3 snapBox = c->conf.box;
+    auto restore = [&]() {
+        c->conf.p = snap;
+        c->conf.box = snapBox;
+        c->hostNewer = true;
+        c->devNewer = false;
+    };
+    std::vector<int> variants = p.delayed ? std::vector<int>{0, 1, 4, 5} : std::vector<int>{0, 1, 2, 3, 4, 5};
+    double bestRate = -1.0;
+    int k = 0;
+    best = p;
+    for (int reach = 1; reach <= 3; ++reach)
+        for (int v : variants) {
+            restore();
+            sc_run_params q = p;
+            q.stencil = reach;
+            q.variant = v;
+            q.check_every = 0;
+            q.time_phases = 0;
+            q.nsweeps = 2;                     // grid, graph capture, caches
+            sc_run_stats st;
+            double rate = 0.0;
+            if (runSweeps(c, q, st) == SC_OK) {
+                q.nsweeps = sweeps;
+                if (runSweeps(c, q, st) == SC_OK && st.seconds > 0) rate = (double)st.moves / st.seconds;
+            }
+            if (rates) rates[k] = rate;
+            ++k;
+            if (rate > bestRate) {
+                bestRate = rate;
+                best.stencil = reach;
+                best.variant = v;
+            }
+        }
+    restore();
+    if (ncand) *ncand = k;
+    if (bestRate <= 0.0) return fail(SC_ERR_STATE, "sc_tune: no candidate ran");
+    const int m = p.delayed ? 1 : 0;
+    c->tunedStencil[m] = best.stencil;
+    c->tunedVariant[m] = best.variant;
+    return SC_OK;
 }
 
 // --- parallel-tempering replicas -----------------------------------------------------
@@ -3280,7 +3428,7 @@ int runReplicas(void* h, const sc_run_params& p, int exchangeEvery, sc_run_stats
         q.nsweeps = p.nsweeps; q.seed = p.seed + 0x9E3779B97F4A7C15ull * (unsigned long long)(k + 1);
         q.temper = R->temps[k]; q.ptype = p.ptype; q.volume_every = p.volume_every; q.check_every = p.check_every;
         q.stencil = p.stencil; q.time_phases = p.time_phases; q.press = p.press; q.delayed = p.delayed;
-        q.variant = p.variant;
+        q.variant = p.variant < 0 ? 4 : p.variant;     // a batch has no tuned choice of its own
         if (p.delayed && !c->surrogate) return fail(SC_ERR_STATE, "delayed = 1 needs a surrogate on every replica");
         if ((rc = wlCheckRun(c, q))) return rc;
         if (p.transmx > 0) q.transmx = p.transmx;

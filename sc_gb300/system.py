@@ -192,6 +192,34 @@ class System:
         L.check(self._lib.sc_default_run(self._h, C.byref(p)))
         return p
 
+    def screen_survivors(self, targets=None, cap=None):
+        """The move kernels' candidate screens over every (target, particle) pair: (i, j,
+        stage_b) of the pairs that pass stage A (see sc_screen_survivors)."""
+        T = None if targets is None else np.ascontiguousarray(targets, dtype=np.int32)
+        nt = self.n if T is None else len(T)
+        cap = cap if cap is not None else max(1024, nt * 512)
+        I = np.zeros(cap, np.int32)
+        J = np.zeros(cap, np.int32)
+        B = np.zeros(cap, np.uint8)
+        cnt = C.c_long()
+        L.check(self._lib.sc_screen_survivors(self._h, nt, None if T is None else _iptr(T), cap, _iptr(I), _iptr(J),
+                                              B.ctypes.data_as(C.POINTER(C.c_ubyte)), C.byref(cnt)))
+        k = cnt.value
+        return I[:k], J[:k], B[:k]
+
+    def tune(self, params=None, sweeps=8, **overrides):
+        """sc_tune: the fastest (stencil, variant) for params' mode on the current state (which
+        it leaves unchanged); later runs with variant = -1 use it.  Returns (best params,
+        moves/s of every candidate)."""
+        p = params if params is not None else self.default_run()
+        for k, v in overrides.items():
+            setattr(p, k, v)
+        best = L.RunParams()
+        rates = (C.c_double * 32)()
+        n = C.c_int()
+        L.check(self._lib.sc_tune(self._h, C.byref(p), int(sweeps), C.byref(best), rates, C.byref(n)))
+        return best, [rates[k] for k in range(n.value)]
+
     def simulate(self, params=None, **overrides):
         p = params if params is not None else self.default_run()
         for k, v in overrides.items():

@@ -89,3 +89,72 @@ def test_dataflow_sweep_in_a_batch_of_uneven_systems():
         assert abs(Eb[sb.index(y)] - exact) <= 1e-9 * max(1.0, abs(exact))
     for s in sa + sb:
         s.close()
+
+
+# --- the exchange decision against a restatement of the reference's rule -------------------
+_M = 0xFFFFFFFF
+
+
+def _philox(c, k0, k1):
+    """Philox4x32-10 (Salmon et al., SC'11), as the kernels' counter-based stream uses it."""
+    x, y, z, w = c
+    for _ in range(10):
+        p0, p1 = 0xD2511F53 * x, 0xCD9E8D57 * z
+        x, y, z, w = ((p1 >> 32) ^ y ^ k0) & _M, p1 & _M, ((p0 >> 32) ^ w ^ k1) & _M, p0 & _M
+        k0, k1 = (k0 + 0x9E3779B9) & _M, (k1 + 0xBB67AE85) & _M
+    return x, y, z, w
+
+
+def _uniforms(seed, a, b, c):
+    """The uniforms of one (stream id, event) Philox stream, two per block."""
+    k0, k1 = seed & _M, (seed >> 32) & _M
+    w = 0
+    while True:
+        r = _philox((a, b, c, w), k0, k1)
+        w += 1
+        for hi, lo in ((r[0], r[1]), (r[2], r[3])):
+            yield (((hi << 21) ^ (lo >> 11)) & ((1 << 53) - 1)) / 9007199254740992.0
+
+
+def test_philox_known_answers():
+    """The restatement reproduces Random123's published Philox4x32-10 vectors."""
+    assert _philox((0, 0, 0, 0), 0, 0) == (0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8)
+    assert _philox((_M, _M, _M, _M), _M, _M) == (0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD)
+
+
+def test_exchange_decisions_follow_the_reference_rule():
+    """Every exchange decision of the device step equals the one the reference's rule takes
+    (MoveCreator::replicaExchangeMove, movecreator.cpp:713-745: accept when
+    change = (1/T_i - 1/T_j)(E_i - E_j) + (P_i/T_i - P_j/T_j)(V_i - V_j) > 0 or a uniform is
+    below exp(change)), restated here on the energies, temperatures and the uniforms of the
+    exchange's own random stream: even and odd neighbour pairs alternate, each ladder ordered
+    by temperature."""
+    import math
+
+    from sc_gb300 import ReplicaSet
+
+    reps = open_systems("psc_nvt", 4)
+    temps = list(np.geomspace(0.9, 1.0, 4))
+    R = ReplicaSet(reps, temps, ladder=[0] * 4)
+    seed = 31
+    ex_seed = seed ^ 0xA5A5A5A5
+    T = np.array(temps)
+    decided = accepted = 0
+    for ev in range(40):
+        st, T_after, E, tried, acc = R.run(2, exchange_every=2, seed=seed)
+        ladder = list(np.argsort(T, kind="stable"))
+        want = T.copy()
+        u = _uniforms(ex_seed, 0xFFFFFFE0, ev & _M, ev >> 32)
+        for k in range(ev & 1, len(ladder) - 1, 2):
+            ri, rj = ladder[k], ladder[k + 1]
+            change = (1.0 / T[ri] - 1.0 / T[rj]) * (E[ri] - E[rj])     # NVT: equal volumes, no pressure term
+            x = next(u)
+            if change >= 0.0 or math.exp(change) > x:
+                want[ri], want[rj] = T[rj], T[ri]
+                accepted += 1
+            decided += 1
+        assert np.array_equal(T_after, want), (ev, T, T_after, want, E)
+        assert int(tried.sum()) == decided and int(acc.sum()) == accepted
+        T = T_after
+    assert 0 < accepted < decided
+    R.close()

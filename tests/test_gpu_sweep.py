@@ -290,3 +290,30 @@ def test_dataflow_wait_limit_reports_and_recovers():
     exact = s.all_to_all()
     assert abs(st.energy - exact) <= 1e-9 * max(1.0, abs(exact)), (st.energy, exact)
     s.close()
+
+
+def test_tuner_restores_state_and_is_used():
+    """sc_tune times every candidate launch shape on the current state and leaves that state
+    as it found it; runs with variant = -1 then use its choice, and stay exact."""
+    from sc_gb300 import System
+
+    g = goldens.load("syn_cpsc_spa_npt_small")
+    inp = g["inputs"]
+    s = System.from_text(inp["options"], inp["top.init"], inp["config.init"])
+    s.simulate(nsweeps=3, seed=2, check_every=0)
+    before = s.particles()
+    box = s.box.copy()
+    p = s.default_run()
+    p.seed, p.check_every = 4, 0
+    best, rates = s.tune(p, sweeps=2)
+    assert len(rates) == 18 and max(rates) > 0
+    assert best.stencil in (1, 2, 3) and 0 <= best.variant <= 7
+    assert rates[(best.stencil - 1) * 6 + best.variant] == max(rates)
+    after = s.particles()
+    assert np.array_equal(s.box, box)
+    for k in range(s.n):
+        assert list(after[k].pos) == list(before[k].pos) and list(after[k].dir) == list(before[k].dir)
+    st = s.simulate(p, nsweeps=4, variant=-1)
+    exact = s.all_to_all()
+    assert abs(st.energy - exact) <= 1e-9 * max(1.0, abs(exact))
+    s.close()
