@@ -1,28 +1,32 @@
 #!/usr/bin/env python3
 """Benchmark: attempted Metropolis moves per second on one GB300.
 
-Workload (default): the NPT binary mixture -- 4000 particles, 2000 CPSC (length 3,
-cylindrical patch 120 deg) + 2000 attractive spheres SPA (sigma 1, eps 0.5 kT, range
-1.5), P* = 0.5, T = 1, one isotropic volume move per sweep -- as a seeded synthetic
-start (sc_gb300/workloads.py).  A step is one sweep: N attempted single-particle
-moves on the checkerboard plus the volume move, all through the C ABI.
+Workload (default): psc_cpsc_65536 -- 65,536 patchy spherocylinders, half PSC (patch 90
+deg) and half CPSC (cylindrical patch 120 deg), length 3, eps 1, packing fraction 0.2,
+NVT T = 1, from a seeded aligned lattice start (sc_gb300/workloads.py).  A step is one
+sweep: N attempted single-particle moves (displacements and rotations) on the
+checkerboard, all through the C ABI, with the launch shape the library's tuner (sc_tune)
+picks on the start.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-Prints one JSON line.  `value` is device-timed moves/s (CUDA events on the library's
-stream, L2 flushed between steps); `e2e` is the same metric through the public API
-with host buffers (state uploaded before and downloaded after every step).
-`--impl reference` times the CPU restatement of the reference's own loop (oracle/,
-sequential Metropolis with the reference's Verlet list and O(N^2) volume move) on
-all host cores, independent seeds per core.
+Prints one JSON line.  `value` is device-timed moves/s of the plain FP64 kernel (CUDA
+events on the library's stream, L2 flushed between steps); `e2e` is the same metric
+through the public API with host buffers (state uploaded before and downloaded after
+every step); `delayed_acceptance` gives the surrogate two-stage moves on the same system
+after a melt.  `--impl reference` times the reference's own algorithm (the sequential
+loop with its Verlet list, restated in oracle/sc_oracle.cpp and built -Ofast, calibrated
+against the reference's own -Ofast binary by tests/test_cpu_baseline.py) on all host cores,
+independent seeds per core, on the same workload, set-up outside the timed region.
 
-Sections of the same line (rank 0, default run): `replicas` (64 uneven parallel-tempering
-replicas in one batch against the same replicas one after another), `surrogate` (65,536
-PSC/CPSC, plain against delayed acceptance with the network trained in the run),
-`bilayer` (30,000-particle lipid bilayers with chain moves), `wang_landau` (a particle
-above a bilayer with and without Wang-Landau weights, eight walkers sharing one table,
-and the oracle's sequential loop with the bias as the CPU baseline).  `--only <section>`
-runs one of them alone.
+Sections of the same line (rank 0, default run): `surrogate` (plain against delayed
+acceptance with the network trained in the run, after a melt), `mixture` (the
+4000-particle NPT binary mixture with one host core of the reference's loop beside it),
+`replicas` (64 uneven parallel-tempering replicas in one batch against the same replicas
+one after another), `bilayer` (30,000-particle lipid bilayers with chain moves),
+`wang_landau` (a particle above a bilayer with and without Wang-Landau weights, eight
+walkers sharing one table, and the reference's loop with the bias as the CPU baseline).
+`--only <section>` runs one of them alone.
 """
 import argparse
 import ctypes as C
@@ -41,7 +45,7 @@ sys.path.insert(0, os.path.join(ROOT, "tests"))
 
 METRIC = "MC moves/s on 1 GB300: plain FP64 kernel vs surrogate delayed-acceptance"
 UNIT = "moves/s"
-WORKLOAD = "npt_cpsc_spa_4000"
+WORKLOAD = "psc_cpsc_65536"
 
 
 def parse():
@@ -55,7 +59,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
-    ap.add_argument("--only", default="all", choices=["all", "main", "replicas", "surrogate", "bilayer", "wl"],
+    ap.add_argument("--only", default="all", choices=["all", "main", "replicas", "surrogate", "bilayer", "wl", "mixture"],
                     help="run one section alone (prints that section's JSON)")
     return ap.parse_args()
 
@@ -157,102 +161,6 @@ def open_workload(name, seed):
     return System.from_text(opts, top, cfg), (opts, top, cfg)
 
 
-def oracle_system(texts, seed):
-    """The oracle's view of the same start: parameters derived by the oracle itself."""
-    import numpy as np
-
-    import oracle_ffi as O
-    from sc_gb300 import System
-
-    opts, top, cfg = texts
-    s = System.from_text(opts, top, cfg)
-    parts = s.particles()
-    box = list(s.box)
-    p = s.default_run()
-    s.close()
-    types, excl = O.parse_types(top)
-    arr = (O.TypeIn * len(types))(*types)
-    table = (O.Param * (O.MAXT * O.MAXT))()
-    sq, mc = C.c_double(), C.c_double()
-    assert O.lib().or_derive_params(arr, len(types), excl.ctypes.data, table, C.byref(sq), C.byref(mc)) == 0
-    op = (O.Particle * len(parts))()
-    for k, q in enumerate(parts):
-        op[k].pos, op[k].dir = O.vec(q.pos), O.vec(q.dir)
-        for m in range(2):
-            op[k].pd[m], op[k].ch[m] = O.vec(q.patchdir[m]), O.vec(q.chdir[m])
-        for m in range(4):
-            op[k].ps[m] = O.vec(q.patchsides[m])
-        op[k].type, op[k].molType = q.type, q.molType
-    nmol = max(q.molType for q in parts) + 1
-    mols = (O.MolType * nmol)()
-    for m in range(nmol):
-        mols[m].size = 1
-        for key in ("bond1", "bond2", "bondd", "bondh", "angle1", "angle2"):
-            setattr(mols[m], key + "c", -1.0)
-    sysm = O.System()
-    sysm.n, sysm.nmol = len(parts), nmol
-    sysm.p = C.cast(op, C.POINTER(O.Particle))
-    sysm.mols = C.cast(mols, C.POINTER(O.MolType))
-    sysm.params = C.cast(table, C.POINTER(O.Param))
-    for k in range(3):
-        sysm.box[k] = box[k]
-    sysm.sqmaxcut = sq.value
-    o = O.McOpts()
-    o.seed = seed
-    o.temper, o.press, o.shave = p.temper, p.press, 1.0 if p.volume_every else 0.0
-    o.transmx, o.rot_angle, o.edge_mx = p.transmx, p.rot_angle, p.edge_mx
-    o.ptype = p.ptype
-    o.pairlist_update = 10
-    keep = (op, mols, table, arr)
-    return sysm, o, len(parts), keep
-
-
-def _oracle_molecules(top, O):
-    """Molecule records of a top.init for the oracle: size, first particle, count and bond
-    constants of each [Molecules] entry in definition order (the molType index), placed in
-    the particle vector in [System] order (Inicializer::setParticlesParamss)."""
-    defs, order, key, cur = [], [], None, None
-    for raw in top.splitlines():
-        line = raw.split("#", 1)[0].strip()
-        if not line:
-            continue
-        if line.startswith("["):
-            key = line[1:].split("]")[0].strip().upper()
-            continue
-        if key == "MOLECULES":
-            if "{" in line:
-                cur = {"name": line.split(":")[0].strip(), "size": 0, "bonds": {}}
-                defs.append(cur)
-            elif line.startswith("}"):
-                cur = None
-            elif cur is not None and ":" in line:
-                k, v = line.split(":", 1)
-                k = k.strip().lower()
-                if k == "particles":
-                    cur["size"] += 1
-                else:
-                    cur["bonds"][k] = [float(x) for x in v.split()[:2]]
-        elif key == "SYSTEM":
-            name, cnt = line.split()[:2]
-            order.append((name, int(cnt)))
-    mols = (O.MolType * max(1, len(defs)))()
-    first = 0
-    starts = {}
-    for name, cnt in order:
-        d = next(d for d in defs if d["name"] == name)
-        starts.setdefault(name, (first, cnt))
-        first += d["size"] * cnt
-    for k, d in enumerate(defs):
-        m = mols[k]
-        m.size = d["size"]
-        m.first, m.count = starts.get(d["name"], (0, 0))
-        for b in ("bond1", "bond2", "bondd", "bondh", "angle1", "angle2"):
-            c, eq = d["bonds"].get(b, [-1.0, -1.0])
-            setattr(m, b + "c", c)
-            setattr(m, b + "eq", eq)
-    return mols, len(defs)
-
-
 def wl_cpu_baseline(texts, wl_text, seed, max_moves=3000):
     """One core of the oracle's sequential loop with the Wang-Landau bias (or_wl_run, the
     reference's partDisplace / partRotate with WangLandau::run / runRot) on a bounded
@@ -262,9 +170,9 @@ def wl_cpu_baseline(texts, wl_text, seed, max_moves=3000):
     import oracle_ffi as O
 
     opts, top, cfg = texts
-    sysm, o, n, keep = oracle_system(texts, seed)
-    mols, nmol = _oracle_molecules(top, O)
-    sysm.mols, sysm.nmol = C.cast(mols, C.POINTER(O.MolType)), nmol
+    ts = O.TextSystem(opts, top, cfg)
+    sysm, o = ts.sys, ts.opts
+    o.seed = seed
     rows = [l.split() for l in wl_text.splitlines() if l.strip()]
     alpha, rows = float(rows[0][0]), [[float(x) for x in r] for r in rows[1:]]
     two = len(rows[0]) == 4
@@ -290,58 +198,133 @@ def wl_cpu_baseline(texts, wl_text, seed, max_moves=3000):
     st.cur[0], st.cur[1] = cur[0], cur[1]
     o.nsweeps, o.max_moves = 1 << 30, max_moves
     ms = O.McStats()
-    O.lib().or_wl_run(C.byref(sysm), C.byref(o), C.byref(st), C.byref(ms))
+    O.lib(fast=True).or_wl_run(C.byref(sysm), C.byref(o), C.byref(st), C.byref(ms))
     return ms.moves / max(ms.seconds, 1e-12), ms.moves
 
 
-def cpu_run(texts, seed, nsweeps, max_moves):
+REF_MAXN = 30003      # MAXN of the reference (scOOP/structures/macros.h:60)
+
+
+def _ref_worker(texts, seed, energy_matrix, probe_moves, warmup_steps, steps, step_moves, barrier, out):
+    """One host core running the reference's loop (the oracle's restatement at -Ofast) on its
+    own copy of the start: set-up, probe, warm-up and timed phases separated by barriers, so
+    that the caller's clock covers the timed moves only."""
     import oracle_ffi as O
 
-    sysm, o, n, keep = oracle_system(texts, seed)
-    o.nsweeps = nsweeps
-    o.max_moves = max_moves
-    st = O.McStats()
-    O.lib().or_mc_run(C.byref(sysm), C.byref(o), C.byref(st))
-    return st.moves, st.seconds
+    ts = O.TextSystem(*texts)
+    run = O.McRun(ts, seed=seed, energy_matrix=energy_matrix, fast=True)
+    st = run.advance(probe_moves)
+    out.put(("probe", st.moves / max(st.seconds, 1e-9), run.setup_seconds))
+    barrier.wait()                       # the caller sizes the steps from the probes
+    sm = step_moves.value
+    run.advance(sm * warmup_steps)
+    barrier.wait()                       # timed region starts
+    m0 = run.stats.moves
+    run.advance(sm * steps)
+    moves = run.stats.moves - m0
+    barrier.wait()                       # timed region ends
+    st = run.stats
+    out.put(("done", moves, (st.acc_trans + st.acc_rot) / max(1, st.moves), st.moves))
+    run.close()
 
 
-def _worker(args):
-    texts, seed, nsweeps, max_moves = args
-    return cpu_run(texts, seed, nsweeps, max_moves)
+def _neighbours_estimate(texts):
+    """Particles within the reference's pair-list cutoff of one particle (main.cpp:117-126)."""
+    import oracle_ffi as O
+
+    opts, top, cfg = texts
+    o = O.parse_options(opts)
+    box = [float(x) for x in cfg.strip().splitlines()[0].split()[:3]]
+    n = cfg.count("\n") - 1
+    rc = 2.0 * float(o.get("transmx", "0")) * (1 + int(o.get("pairlist_update", "0"))) * 2 + 5.0
+    return min(n, n / (box[0] * box[1] * box[2]) * 4.0 / 3.0 * math.pi * rc ** 3)
+
+
+def cpu_reference_rate(texts, cores, warmup_steps, steps, seed, seconds_budget):
+    """Moves/s of the reference's own algorithm on `cores` host cores: independent seeds, one
+    process each, timed between barriers after every process has set up its system (initial
+    energy / energy matrix, first pair list: what precedes the reference's timed loop).  The
+    energy calculator is the reference's default TotalEMatrix when N fits its MAXN, else
+    TotalEFull, both with the Verlet list every pairlist_update sweeps.  A step is at most one
+    sweep per process, sized so that warm-up plus timed steps take about seconds_budget; the
+    process count is bounded by the host memory the pair lists need."""
+    import multiprocessing as mp
+
+    n = texts[2].count("\n") - 1
+    matrix = n <= REF_MAXN
+    per = 8.0 * n * _neighbours_estimate(texts) + (8.0 * n * n if matrix else 0.0) + 64e6
+    try:
+        avail = os.sysconf("SC_AVPHYS_PAGES") * os.sysconf("SC_PAGE_SIZE")
+        cores = max(1, min(cores, int(0.5 * avail / per)))
+    except (ValueError, OSError):
+        pass
+    ctx = mp.get_context("spawn")
+    barrier = ctx.Barrier(cores + 1)
+    out = ctx.Queue()
+    step_moves = ctx.Value("l", n)
+    probe = min(n, 2000)
+    procs = [ctx.Process(target=_ref_worker, args=(texts, seed + 1000 + k, matrix, probe, warmup_steps, steps,
+                                                   step_moves, barrier, out)) for k in range(cores)]
+    for q in procs:
+        q.start()
+    limit = 1800.0                       # a process that died must not hang the caller
+    try:
+        rates, setups = [], []
+        for _ in range(cores):
+            tag, rate, setup = out.get(timeout=limit)
+            rates.append(rate)
+            setups.append(setup)
+        per_step = seconds_budget / max(1, warmup_steps + steps)
+        step_moves.value = int(max(200, min(n, per_step * min(rates))))
+        barrier.wait(timeout=limit)      # probes done, step size set
+        barrier.wait(timeout=limit)      # warm-up done
+        t0 = time.perf_counter()
+        barrier.wait(timeout=limit)      # timed moves done
+        wall = time.perf_counter() - t0
+        moves = 0
+        acc = []
+        for _ in range(cores):
+            tag, m, a, _tot = out.get(timeout=limit)
+            moves += m
+            acc.append(a)
+    finally:
+        for q in procs:
+            q.join(timeout=5)
+            if q.is_alive():
+                q.kill()
+    return {"value": moves / wall, "moves": moves, "seconds": wall, "cores": cores, "step_moves": step_moves.value,
+            "energy_calculator": "TotalEMatrix" if matrix else "TotalEFull", "setup_seconds": max(setups),
+            "acceptance": float(sum(acc) / len(acc))}
+
+
+def _reference_sample(r, workload, steps):
+    return (f"{r['cores']} processes x {steps} steps x {r['step_moves']} moves of {workload} (independent seeds; "
+            f"the reference's sequential loop restated in oracle/sc_oracle.cpp, built -Ofast: Verlet list every 10 "
+            f"sweeps, {r['energy_calculator']}, O(N^2) volume move with probability shave/N per move); set-up "
+            f"({r['setup_seconds']:.1f} s: initial energy, first pair list) outside the timed region; calibrated "
+            f"within 15 % of the reference's own -Ofast binary (tests/test_cpu_baseline.py)")
 
 
 def run_reference(a, rank, world):
-    """CPU arm: the oracle's restatement of the reference loop on all host cores."""
+    """CPU arm: the reference's loop on all host cores, same workload, metric and unit."""
     if rank != 0:
         return
-    import multiprocessing as mp
-
     from sc_gb300 import workloads
 
     texts = workloads.WORKLOADS[a.workload](a.seed)
     n = texts[2].count("\n") - 1
     cores = os.cpu_count() or 1
-    # size one step so that warm-up + steps stay within a few minutes
-    probe_moves, probe_s = cpu_run(texts, a.seed, 1, n)
-    per_move = probe_s / max(1, probe_moves)
-    budget = 150.0 / max(1, a.steps + a.warmup)
-    step_moves = int(max(100, min(n, budget / per_move)))
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(cores) as pool:
-        pool.map(_worker, [(texts, a.seed + 100 + k, 1, step_moves * a.warmup) for k in range(cores)])
-        t0 = time.perf_counter()
-        res = pool.map(_worker, [(texts, a.seed + 1000 + k, 1, step_moves * a.steps) for k in range(cores)])
-        wall = time.perf_counter() - t0
-    moves = sum(m for m, _ in res)
-    value = moves / wall
-    sample = (f"{cores} independent seeds x {step_moves * a.steps} moves of {a.workload} (sequential Metropolis, "
-              f"reference Verlet list every 10 sweeps, O(N^2) volume move with probability 1/N per move)")
+    r = cpu_reference_rate(texts, cores, a.warmup, a.steps, a.seed, seconds_budget=120.0)
+    value = r["value"]
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world,
-            "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * wall / a.steps, "higher_is_better": True,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * r["seconds"] / a.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": a.workload, "n_particles": n, "seed": a.seed, "cores": cores},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
-            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "config": {"workload": a.workload, "n_particles": n, "seed": a.seed, "cores": r["cores"],
+                       "step": f"{r['step_moves']} moves per process"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": r["cores"], "kind": "port",
+                             "sample": _reference_sample(r, a.workload, a.steps)},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "detail": {"acceptance": r["acceptance"], "timed_seconds": r["seconds"], "moves": r["moves"]}}
     print(json.dumps(line), flush=True)
 
 
@@ -390,7 +373,7 @@ def bench_replicas(steps, seed=1):
     # plain: every replica alone through the single-system loop (same tuned stencil, the
     # kernel variant that runs a single system fastest)
     s1 = System.from_text(*systems[0])
-    solo = tune_variant(s1, s1.default_run(), 0, stencil=best[0], candidates=(0, 4))
+    solo = s1.tune(s1.default_run(), sweeps=3)[0].variant
     s1.close()
     moves = secs = 0.0
     for g, texts in enumerate(systems):
@@ -412,23 +395,6 @@ def bench_replicas(steps, seed=1):
             "delayed_stage1_decided": std.da_stage1_rejected / max(1, std.moves),
             "exchanges_tried": int(tried.sum()), "exchange_acceptance": float(acc.sum() / max(1, tried.sum())),
             "sweeps": steps}
-
-
-def tune_variant(s, p, delayed=0, stencil=0, candidates=None):
-    """The move-kernel variant that runs s fastest (bit 0: more CTAs per SM instead of the
-    lowest latency per move; bit 1: paired passes, plain moves only; bit 2: one dataflow
-    launch per sweep instead of one launch per colour)."""
-    best = None
-    if candidates is None:
-        candidates = (0, 1, 4, 5) if delayed else (0, 1, 2, 3, 4, 5)
-    for v in candidates:
-        s.simulate(p, nsweeps=2, variant=v, delayed=delayed, stencil=stencil)
-        st = s.simulate(p, nsweeps=4, variant=v, delayed=delayed, stencil=stencil)
-        rate = st.moves / max(st.seconds, 1e-12)
-        if best is None or rate > best[1]:
-            best = (v, rate)
-    p.variant = best[0]
-    return best[0]
 
 
 def bench_surrogate(steps, seed=1, melt=300, snapshots=30, gap=10, epochs=8):
@@ -458,10 +424,11 @@ def bench_surrogate(steps, seed=1, melt=300, snapshots=30, gap=10, epochs=8):
     run_seed = seed + 4242
     pt = s.default_run()
     pt.seed, pt.check_every = run_seed, 0
-    variants = {0: tune_variant(s, pt, 0), 1: tune_variant(s, pt, 1)}   # each mode its fastest kernel
+    # each mode its fastest launch shape (the library's tuner; later runs pass variant = -1)
+    variants = {d: s.tune(pt, sweeps=4, delayed=d)[0] for d in (0, 1)}
 
     def timed(delayed):
-        variant = variants[delayed]
+        variant = -1
         s.simulate(nsweeps=3, seed=run_seed, check_every=0, delayed=delayed, variant=variant)
         dev = 0.0
         tot = dict(moves=0, acc=0, s1=0, s2=0, s2rej=0, err2=0.0, launches=0)
@@ -486,7 +453,8 @@ def bench_surrogate(steps, seed=1, melt=300, snapshots=30, gap=10, epochs=8):
     sur.close()
     s.close()
     return {"workload": "psc_cpsc_65536", "particles": 65536, "sweeps_timed": steps,
-            "kernel_variant": {"plain": variants[0], "delayed": variants[1]},
+            "kernel_variant": {"plain": variants[0].variant, "delayed": variants[1].variant},
+            "stencil": {"plain": variants[0].stencil, "delayed": variants[1].stencil},
             "plain_moves_per_s": plain["rate"], "delayed_moves_per_s": da["rate"],
             "speedup": da["rate"] / plain["rate"],
             "acceptance_plain": plain["acc"] / plain["moves"], "acceptance_delayed": da["acc"] / da["moves"],
@@ -514,7 +482,9 @@ def bench_bilayer(steps, seed=1, warm=20):
     p.check_every = 0
     p.seed = seed
     s.simulate(p, nsweeps=warm)
-    variant = tune_variant(s, p)
+    best, _ = s.tune(p, sweeps=4)
+    variant = best.variant
+    p.variant = -1
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
     dev = 0.0
     moves = chain = acc = chain_acc = launches = 0
@@ -621,19 +591,127 @@ def bench_wl(steps, seed=1, warm=20):
     return out
 
 
+def fp64_peak(device):
+    """This GPU's FP64 rates from the library's probe kernels (sc_fp64_rates)."""
+    from sc_gb300 import _lib as L
+
+    lib = L.load()
+    v = [C.c_double() for _ in range(4)]
+    L.check(lib.sc_fp64_rates(device, *[C.byref(x) for x in v]))
+    return {"dmul_dadd_ops_per_s": v[0].value, "one_lane_ops_per_s": v[1].value, "dfma_flops": v[2].value,
+            "latency_cycles": v[3].value}
+
+
+def timed_sweeps(s, p, steps, flush, dist=None, clocks=None):
+    """`steps` one-sweep steps, device-timed (CUDA events on the library's stream), L2 flushed
+    before each; the move launches are timed too (events recorded around them, read after the
+    sweep).  Returns the totals."""
+    import torch
+
+    p.time_phases = 1
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    if clocks:
+        clocks.start()
+    tot = dict(seconds=0.0, moves=0, launches=0, tested=0, evaluated=0, acc=0, phase_s=0.0, phase_n=0)
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        st = s.simulate(p, nsweeps=1)
+        tot["seconds"] += st.seconds
+        tot["moves"] += st.moves
+        tot["launches"] += st.launches
+        tot["tested"] += st.pairs_tested
+        tot["evaluated"] += st.pairs_evaluated
+        tot["acc"] += st.acc_trans + st.acc_rot
+        tot["phase_s"] += st.phase_seconds
+        tot["phase_n"] += st.phase_launches
+    p.time_phases = 0
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    tot["clocks"] = clocks.stop() if clocks else None
+    return tot
+
+
+KERNELS = {0: "kColour", 1: "kColourDense", 2: "kColour", 3: "kColourDense", 4: "kColourFlow", 5: "kColourFlowDense",
+           6: "kColourFlow", 7: "kColourFlowDense"}
+
+
+def roofline(tot, variant, workload, peaks, peak_kind, fp64):
+    """The move kernel against the HBM roofline (algorithmic bytes: 28 B position + type per
+    candidate pair tested, old and new configuration, 120 B axis + patch vectors per pair
+    evaluated) and against this GPU's measured FP64 instruction rate (17 FP64 operations per
+    candidate pair for the image and r^2, ~600 per evaluated pair, counted from the kernel
+    source)."""
+    n = max(1, tot["phase_n"])
+    t_launch = tot["phase_s"] / n
+    bytes_per_launch = (tot["tested"] * 28 + tot["evaluated"] * 120) / n
+    achieved = bytes_per_launch / t_launch / 1e9 if t_launch > 0 else None
+    kernel = KERNELS[int(variant) & 7]
+    roof = {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
+            "traffic": profiled_traffic(kernel, workload),
+            "traffic_source": f"profiles/{kernel}_{workload}.md (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
+            "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+            "avg_launch_us": t_launch * 1e6, "algorithmic_bytes_per_launch": bytes_per_launch,
+            "note": "the move kernel is bound by FP64 latency, not by HBM: see fp64"}
+    ops = (tot["tested"] * 17 + tot["evaluated"] * 600) / n
+    fp = {"achieved_ops_per_s": ops / t_launch if t_launch > 0 else None,
+          "note": "17 FP64 operations per candidate pair (image + r^2), ~600 per evaluated pair (counted from the "
+                  "kernel source); peaks from the library's own probe kernels on this GPU (sc_fp64_rates)"}
+    if fp64:
+        fp.update({"peak_ops_per_s": fp64["dmul_dadd_ops_per_s"], "frac": fp["achieved_ops_per_s"] /
+                   fp64["dmul_dadd_ops_per_s"] if fp["achieved_ops_per_s"] else None,
+                   "peak_dfma_tflops": fp64["dfma_flops"] / 1e12, "one_lane_ops_per_s": fp64["one_lane_ops_per_s"],
+                   "dependent_latency_cycles": fp64["latency_cycles"]})
+    return roof, fp
+
+
+def bench_mixture(steps, seed=1, cpu_seconds=15.0):
+    """The 4000-particle NPT binary mixture (2000 CPSC + 2000 SPA, P* = 0.5, one isotropic
+    volume move per sweep): device-timed plain sweeps (library tuner) and one host core of
+    the reference's loop (the reference's energy matrix) from the same start."""
+    import torch
+
+    from sc_gb300 import System, workloads
+
+    texts = workloads.npt_cpsc_spa(4000, seed=seed)
+    s = System.from_text(*texts)
+    p = s.default_run()
+    p.seed, p.check_every = seed, 0
+    best, rates = s.tune(p, sweeps=8)
+    p.variant = -1
+    s.simulate(p, nsweeps=5)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    tot = timed_sweeps(s, p, steps, flush)
+    s.close()
+    out = {"workload": "npt_cpsc_spa_4000", "particles": 4000, "sweeps_timed": steps,
+           "stencil": best.stencil, "kernel_variant": best.variant,
+           "moves_per_s": tot["moves"] / tot["seconds"], "ms_per_sweep": 1e3 * tot["seconds"] / steps,
+           "pair_evaluations_per_s": tot["evaluated"] / tot["seconds"]}
+    try:
+        r = cpu_reference_rate(texts, 1, 1, 3, seed, seconds_budget=cpu_seconds)
+        out["cpu_baseline"] = {"value": r["value"], "unit": UNIT, "cores": 1, "kind": "port",
+                               "sample": _reference_sample(r, "npt_cpsc_spa_4000", 3)}
+    except Exception as ex:
+        out["cpu_baseline"] = {"value": None, "sample": f"failed: {ex}"}
+    return out
+
+
 def main():
     a = parse()
     rank, world, local = dist_info()
     if a.impl == "reference":
         run_reference(a, rank, world)
         return
-    if a.only in ("replicas", "surrogate", "bilayer", "wl"):
+    if a.only in ("replicas", "surrogate", "bilayer", "wl", "mixture"):
         if rank == 0:
             fn = {"replicas": bench_replicas, "surrogate": bench_surrogate, "bilayer": bench_bilayer,
-                  "wl": bench_wl}[a.only]
+                  "wl": bench_wl, "mixture": bench_mixture}[a.only]
             print(json.dumps({a.only: fn(200 if a.only == "replicas" else a.steps, seed=a.seed)}), flush=True)
         return
-    import numpy as np
     import torch
 
     dist = None
@@ -642,11 +720,9 @@ def main():
 
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
-    from sc_gb300 import System  # noqa: F401
-
-    s, texts = open_workload(a.workload, a.seed)
     from sc_gb300 import _lib as L
 
+    s, texts = open_workload(a.workload, a.seed)
     L.check(s._lib.sc_set_device(s._h, local))
     n = s.n
     p = s.default_run()
@@ -654,149 +730,88 @@ def main():
     p.check_every = 0
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
 
-    def l2_flush():
-        flush.zero_()
-        torch.cuda.synchronize()
-
-    # tuner: the cell-list reach (cell size maxcut/s, (s+1)^3 colours) that moves this
-    # system fastest, timed on a few sweeps each
-    # (on a copy, so that the measured system starts from the same state as the reference arm)
-    # each candidate on a fresh copy of the start (an NPT system compresses while it runs,
-    # so one copy moved through all candidates would favour the first ones)
-    best = None
-    for reach, variant in ((1, 0), (2, 0), (3, 0), (2, 1), (1, 2), (2, 2), (1, 4), (2, 4), (3, 4), (2, 5)):
-        tune, _ = open_workload(a.workload, a.seed)
-        L.check(tune._lib.sc_set_device(tune._h, local))
-        try:
-            tune.simulate(p, nsweeps=4, stencil=reach, variant=variant)            # grid, graph capture
-            st = tune.simulate(p, nsweeps=10, stencil=reach, variant=variant)
-        except Exception:
-            tune.close()
-            continue
-        tune.close()
-        rate = st.moves / max(st.seconds, 1e-12)
-        if best is None or rate > best[2]:
-            best = (reach, variant, rate)
-    p.stencil, p.variant = best[0], best[1]
-    # warm-up
-    s.simulate(p, nsweeps=max(3, a.warmup))
-    # the state the timed sweeps start from: the end-to-end leg starts from it as well (an
-    # NPT system compresses while it runs, and denser states take longer per sweep)
+    # the library's tuner (sc_tune): every cell reach and kernel variant timed on the start,
+    # which it restores; the runs below use its choice (variant = -1)
+    best, rates = s.tune(p, sweeps=6)
+    p.variant = -1
+    s.simulate(p, nsweeps=max(3, a.warmup))          # warm-up
+    # the state the timed sweeps start from: the end-to-end leg starts from it as well
     start_state, start_box = s.particles(), s.box
-    # the timed sweeps also time their move launches with CUDA events on the library's
-    # stream (recorded around the launches, read after each sweep: no synchronisation inside)
-    p.time_phases = 1
-    clocks = Clocks(local)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    clocks.start()
-    dev_s = 0.0
-    moves = 0
-    launches = 0
-    tested = evaluated = 0
-    acc = 0
-    phase_s, phase_n = 0.0, 0
-    for k in range(a.steps):
-        l2_flush()
-        st = s.simulate(p, nsweeps=1)
-        dev_s += st.seconds
-        moves += st.moves
-        launches += st.launches
-        tested += st.pairs_tested
-        evaluated += st.pairs_evaluated
-        acc += st.acc_trans + st.acc_rot
-        phase_s += st.phase_seconds
-        phase_n += st.phase_launches
-    p.time_phases = 0
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    clk = clocks.stop()
-    t_max = max_over_ranks(dev_s, dist, f"cuda:{local}")
-    value = moves * world / t_max
+    tot = timed_sweeps(s, p, a.steps, flush, dist, Clocks(local))
+    t_max = max_over_ranks(tot["seconds"], dist, f"cuda:{local}")
+    value = tot["moves"] * world / t_max
 
     # end to end through the public API with host buffers, from the same start
     state = start_state
     s.box = start_box
     bytes_per_particle = C.sizeof(L.Particle)
     e2e_moves = 0
+    if dist:
+        dist.barrier()
     t0 = time.perf_counter()
     for k in range(0 if a.no_e2e else a.steps):
         s.set_particles(0, state)                 # host -> device (uploaded by the next call)
         st = s.simulate(p, nsweeps=1)
         state = s.particles()                     # device -> host
         e2e_moves += st.moves
-    e2e_s = max(time.perf_counter() - t0, 1e-12)
-    e2e = {"value": e2e_moves * world / e2e_s if e2e_moves else None, "unit": UNIT, "h2d_bytes_per_step": n * bytes_per_particle,
-           "d2h_bytes_per_step": 2 * n * bytes_per_particle + 64,
-           "note": "state passed in and out as host sc_particle arrays around every sweep (staged by the library through pinned host memory)"}
+    e2e_s = max_over_ranks(max(time.perf_counter() - t0, 1e-12), dist, f"cuda:{local}")
+    e2e = {"value": e2e_moves * world / e2e_s if e2e_moves else None, "unit": UNIT,
+           "h2d_bytes_per_step": n * bytes_per_particle, "d2h_bytes_per_step": 2 * n * bytes_per_particle + 64,
+           "note": "state passed in and out as host sc_particle arrays around every sweep (staged by the library "
+                   "through pinned host memory); the library recomputes the exact energy after each host change"}
 
     peaks, peak_kind = measured_peaks()
-    # algorithmic bytes of the move kernel: 28 B (position + type) per candidate pair tested
-    # (old and new configuration), 24 B axis + 96 B patch vectors per pair evaluated
-    bytes_per_launch = (tested * 28 + evaluated * 120) / max(1, phase_n)
-    t_launch = phase_s / max(1, phase_n)
-    achieved = bytes_per_launch / t_launch / 1e9 if t_launch > 0 else None
-    kernel = ["kColour", "kColourDense", None, None, "kColourFlow", "kColourFlowDense"][int(p.variant) & 5]
-    roof = {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-            "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
-            "traffic": profiled_traffic(kernel, a.workload),
-            "traffic_source": f"profiles/{kernel}_{a.workload}.md (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
-            "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-            "avg_launch_us": t_launch * 1e6, "algorithmic_bytes_per_launch": bytes_per_launch,
-            "note": "the move kernel is FP64-latency bound; see fp64 for its arithmetic rate"}
-    flops_per_launch = (tested * 17 + evaluated * 600) / max(1, phase_n)
-    fp64 = {"achieved_tflops": flops_per_launch / t_launch / 1e12 if t_launch > 0 else None,
-            "peak_tflops_nominal": 1.25,
-            "note": "17 FP64 ops per candidate pair (image + r^2), ~600 per evaluated pair (estimate from the kernel "
-                    "source); nominal GB300 FP64 peak, not measured"}
+    fp64_err = None
+    try:
+        fp64 = fp64_peak(local)
+    except Exception as ex:
+        fp64, fp64_err = None, str(ex)
+    roof, fp = roofline(tot, best.variant, a.workload, peaks, peak_kind, fp64)
+    if fp64_err:
+        fp["error"] = fp64_err
 
-    # CPU baseline: the oracle restatement of the reference loop, one core, bounded sample
+    # CPU baseline: one host core of the reference's loop on a bounded sample of the same start
     cpu = None
     if rank == 0 and not a.no_cpu:
         try:
-            probe_moves, probe_s = cpu_run(texts, a.seed, 1, 400)
-            per_move = probe_s / max(1, probe_moves)
-            target = int(max(1000, min(50 * n, a.cpu_seconds / per_move)))
-            m, sec = cpu_run(texts, a.seed, 100, target)
-            cpu = {"value": m / sec, "unit": UNIT, "cores": 1, "kind": "port",
-                   "sample": f"{m} moves of {a.workload} from the same start (oracle/sc_oracle.cpp or_mc_run: "
-                             f"sequential Metropolis, Verlet list every 10 sweeps, O(N^2) volume move)"}
+            r = cpu_reference_rate(texts, 1, 1, 3, a.seed, seconds_budget=a.cpu_seconds)
+            cpu = {"value": r["value"], "unit": UNIT, "cores": 1, "kind": "port",
+                   "sample": _reference_sample(r, a.workload, 3)}
         except Exception as ex:  # the baseline is reported, not required
             cpu = {"value": None, "unit": UNIT, "cores": 1, "kind": "port", "sample": f"failed: {ex}"}
 
-    replicas = surrogate = bilayer = wang_landau = None
+    sections = {}
     if rank == 0 and a.only == "all" and not a.no_e2e:
-        try:
-            replicas = bench_replicas(200, seed=a.seed)
-        except Exception as ex:
-            replicas = {"error": str(ex)}
-        try:
-            surrogate = bench_surrogate(max(5, a.steps // 2), seed=a.seed)
-        except Exception as ex:
-            surrogate = {"error": str(ex)}
-        try:
-            bilayer = bench_bilayer(max(5, a.steps // 2), seed=a.seed)
-        except Exception as ex:
-            bilayer = {"error": str(ex)}
-        try:
-            wang_landau = bench_wl(max(5, a.steps // 2), seed=a.seed)
-        except Exception as ex:
-            wang_landau = {"error": str(ex)}
+        for key, fn, steps in (("surrogate", bench_surrogate, max(5, a.steps // 2)),
+                               ("mixture", bench_mixture, max(10, a.steps)),
+                               ("replicas", bench_replicas, 200),
+                               ("bilayer", bench_bilayer, max(5, a.steps // 2)),
+                               ("wang_landau", bench_wl, max(5, a.steps // 2))):
+            try:
+                sections[key] = fn(steps, seed=a.seed)
+            except Exception as ex:
+                sections[key] = {"error": str(ex)}
     if rank == 0:
+        sur = sections.get("surrogate") or {}
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
                 "warmup": a.warmup, "ms_per_step": 1e3 * t_max / a.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": a.workload, "n_particles": n, "step": "one sweep (N moves) + volume move",
-                           "stencil": int(p.stencil), "kernel_variant": int(p.variant),
+                "config": {"workload": a.workload, "n_particles": n, "step": "one sweep (N attempted moves)",
+                           "start": "aligned lattice start after the warm-up sweeps",
+                           "stencil": int(best.stencil), "kernel_variant": int(best.variant),
                            "parallelism": "replicas" if world > 1 else "single", "l2": "flushed between steps",
                            "seed": a.seed, "plain_fp64": True},
-                "clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roof, "fp64": fp64,
-                "cpu_baseline": cpu, "replicas": replicas, "surrogate": surrogate, "bilayer": bilayer,
-                "wang_landau": wang_landau,
-                "detail": {"acceptance": acc / max(1, moves), "pairs_tested_per_move": tested / max(1, moves),
-                           "pairs_evaluated_per_move": evaluated / max(1, moves)}}
+                "clocks": tot["clocks"], "e2e": e2e, "gpu_launches": tot["launches"], "roofline": roof, "fp64": fp,
+                "cpu_baseline": cpu,
+                "pairs": {"evaluated_per_s": tot["evaluated"] / tot["seconds"],
+                          "tested_per_s": tot["tested"] / tot["seconds"],
+                          "evaluated_per_move": tot["evaluated"] / max(1, tot["moves"]),
+                          "tested_per_move": tot["tested"] / max(1, tot["moves"])},
+                "delayed_acceptance": {k: sur.get(k) for k in ("plain_moves_per_s", "delayed_moves_per_s", "speedup",
+                                                               "stage1_decided", "workload")} if sur else None,
+                "tuner": {"candidates_moves_per_s": rates},
+                "detail": {"acceptance": tot["acc"] / max(1, tot["moves"])}}
+        line.update(sections)
         print(json.dumps(line), flush=True)
     s.close()
     if dist:
