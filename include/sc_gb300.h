@@ -88,7 +88,9 @@ typedef struct {
     int delayed;            /* 1: two-stage moves with the context's surrogate (sc_set_surrogate) as first stage */
     int variant;            /* move kernel, bit 0: more moves in flight per SM (large systems), else lowest
                                latency per move; bit 1: paired passes (two moves per stage C); bit 2: one
-                               dataflow launch per sweep instead of one launch per colour; -1: the reach
+                               dataflow launch per sweep instead of one launch per colour; bit 3: the
+                               dataflow sweep with one warp per cell (plain moves, no Wang-Landau
+                               weights; bits 1 and 2 then ignored); -1: the reach
                                and variant sc_tune measured fastest for this context (stencil 0 takes
                                the tuned reach), else the dataflow sweep */
     int flow_wait_polls;    /* dataflow sweep: polls of one wait for a neighbouring cell before the
@@ -203,10 +205,11 @@ int sc_simulate(sc_context* ctx, const sc_run_params* p, sc_run_stats* stats);
  * current state, `sweeps` sweeps each after two warm-up sweeps: cell reach 1, 2, 3 (cells
  * maxcut/reach wide: how many cells move at once and how many neighbours each stages) times
  * kernel variants {colour-phase launches, dataflow sweep} x {lowest latency per move, more
- * CTAs per SM}, plus paired passes for plain moves.  The state is restored before every
+ * CTAs per SM}, plus paired passes and the warp-per-cell sweep for plain moves.  The state is
+ * restored before every
  * candidate and at the end (the next run recomputes the exact energy).  *best = *p with the
  * fastest stencil and variant, which later runs with variant = -1 use.  rates (may be NULL,
- * room for 18) gets each candidate's moves/s, *ncand (may be NULL) their number.  Not with
+ * room for 24) gets each candidate's moves/s, *ncand (may be NULL) their number.  Not with
  * Wang-Landau weights (SC_ERR_UNSUPPORTED: the tuning sweeps would change them). */
 int sc_tune(sc_context* ctx, const sc_run_params* p, int sweeps, sc_run_params* best, double* rates, int* ncand);
 

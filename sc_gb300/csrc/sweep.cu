@@ -636,10 +636,10 @@ __device__ double patchyRound(SplitShared& sp, const DevCtx& c, const double3& b
     return e;
 }
 
-__device__ __forceinline__ bool partnerInStencil(const SweepArgs& a, const Stencil& st, int j) {
+__device__ __forceinline__ bool partnerInStencil(const SweepArgs& a, const int* nbCell, int nNb, int j) {
     int cj = a.cellOf[j];
     bool near = false;
-    for (int w = 0; w < st.nNb; ++w) near |= (st.nbCell[w] == cj);
+    for (int w = 0; w < nNb; ++w) near |= (nbCell[w] == cj);
     return near;
 }
 
@@ -690,13 +690,13 @@ __device__ __forceinline__ void randomUnitSphere(Stream& r, double& x, double& y
 // lane forms the rotation matrix, lane k rotates vector k (axis, patch directions, patch
 // sides, chiral axes), then patchdir[0] is re-orthogonalised against the new axis as
 // partRotate does (movecreator.cpp:1007).
-__device__ void buildProposal(const SweepArgs& a, const MoveShared& sh, Proposal& P, int cell, int cnt, int m, int cx,
-                              int cy, int cz, const double3& box) {
+__device__ void buildProposal(const SweepArgs& a, const int* list, const int* nbCell, int nNb, Proposal& P, int cell,
+                              int cnt, int m, int cx, int cy, int cz, const double3& box) {
     const Control& ctl = *a.ctl;
     const int lane = threadIdx.x & 31;
     Stream r(a.seed, (uint32_t)cell, (uint32_t)m, (uint32_t)ctl.sweep ^ ((uint32_t)(ctl.sweep >> 32) << 20));
     int slotR = min((int)(r.next() * cnt), cnt - 1);
-    int t = sh.list[slotR];
+    int t = list[slotR];
     double4_32a p = a.s.pos[t];
     double4_32a d = a.s.dir[t];
     int type = (int)p.w;
@@ -774,7 +774,7 @@ __device__ void buildProposal(const SweepArgs& a, const MoveShared& sh, Proposal
         for (int q = 0; q < 4; ++q) {
             int j = con.idx[q];
             if (j < 0) continue;
-            if (!partnerInStencil(a, sh.st, j)) { atomicOr(a.err, E_PARTNER_FAR); skip = 1; }
+            if (!partnerInStencil(a, nbCell, nNb, j)) { atomicOr(a.err, E_PARTNER_FAR); skip = 1; }
             P.partners[np++] = j;
         }
         P.nPartners = np;
@@ -1031,7 +1031,7 @@ __device__ __forceinline__ void moveCell(const SweepArgs& a, int cx, int cy, int
     for (int k = tid; k < cnt; k += kMoveThreads) sh.list[k] = a.cellIdx[a.cellStart[cell] + k];
     if (tid < 4) sh.propFor[tid] = -1;
     stageStencil(a, cx, cy, cz, sh.st, sh.scan);
-    if (warp == 0) buildProposal(a, sh, sh.prop[0], cell, cnt, 0, cx, cy, cz, box);
+    if (warp == 0) buildProposal(a, sh.list, sh.st.nbCell, sh.st.nNb, sh.prop[0], cell, cnt, 0, cx, cy, cz, box);
     else if (tid == 64) acceptThresholds(a, sh.prop[0], cell, 0);
     __syncthreads();
     if (tid == 0) sh.propFor[0] = 0;
@@ -1066,11 +1066,11 @@ __device__ __forceinline__ void moveCell(const SweepArgs& a, int cx, int cy, int
             const bool need0 = sh.propFor[m & 3] != m;
             const bool need1 = pair && sh.propFor[(m + 1) & 3] != m + 1;
             if (need0) {
-                if (warp == 0) buildProposal(a, sh, sh.prop[m & 3], cell, cnt, m, cx, cy, cz, box);
+                if (warp == 0) buildProposal(a, sh.list, sh.st.nbCell, sh.st.nNb, sh.prop[m & 3], cell, cnt, m, cx, cy, cz, box);
                 else if (tid == 64) acceptThresholds(a, sh.prop[m & 3], cell, m);
             }
             if (need1) {
-                if (warp == 1) buildProposal(a, sh, sh.prop[(m + 1) & 3], cell, cnt, m + 1, cx, cy, cz, box);
+                if (warp == 1) buildProposal(a, sh.list, sh.st.nbCell, sh.st.nNb, sh.prop[(m + 1) & 3], cell, cnt, m + 1, cx, cy, cz, box);
                 else if (tid == 96) acceptThresholds(a, sh.prop[(m + 1) & 3], cell, m + 1);
             }
             __syncthreads();
@@ -1203,7 +1203,7 @@ __device__ __forceinline__ void moveCell(const SweepArgs& a, int cx, int cy, int
         auto speculate = [&](int mv) {
             if (sh.propFor[mv & 3] == mv) return;      // still valid from an earlier pass
             Proposal& N = sh.prop[mv & 3];
-            buildProposal(a, sh, N, cell, cnt, mv, cx, cy, cz, box);
+            buildProposal(a, sh.list, sh.st.nbCell, sh.st.nNb, N, cell, cnt, mv, cx, cy, cz, box);
             if ((tid & 31) == 0) {
                 acceptThresholds(a, N, cell, mv);
                 sh.propFor[mv & 3] = mv;
@@ -1601,6 +1601,298 @@ __device__ __forceinline__ void flowBody(const SweepArgs* __restrict__ A) {
 __global__ void __launch_bounds__(kMoveThreads, 1) kColourFlow(const SweepArgs* __restrict__ A) { flowBody<false>(A); }
 __global__ void __launch_bounds__(kMoveThreads, 3) kColourFlowDense(const SweepArgs* __restrict__ A) {
     flowBody<false>(A);
+}
+
+// ---- one warp per cell ---------------------------------------------------------------------
+// The dataflow sweep with a warp, not a CTA, per cell (variant bit 3; plain moves).  A cell of
+// a sparse system holds about one particle, so the CTA-wide kernels spend most of a cell's
+// time in block barriers and 128-thread scans around a handful of pair energies, with two or
+// three cells in flight per SM.  Here each warp takes cells from the sweep's ticket counter on
+// its own and runs the same move as moveCell -- the same proposal and threshold streams, the
+// same FP32 candidate (stage A) and exact-zero (stage B) screens, the same FP64 pair energy
+// -- with warp-synchronous compaction (ballots) and no barrier wider than the warp, so that
+// every warp of the SM is an independent cell in flight.  The pair energies of a move are
+// summed lane by lane and then over the warp in a fixed order (a different order from
+// moveCell's, so the running energies of the two kernels differ in the last bits).  Waiting,
+// publishing and the bounded wait are the dataflow sweep's (flowBody).
+constexpr int kWarpCand = 256;       // candidates staged per warp at a time (larger stencils: windows)
+constexpr int kCellWarps = 4;        // warps per CTA
+
+struct WarpCell {
+    float4 candPos[kWarpCand];
+    float4 candDir[kWarpCand];
+    Proposal prop;
+    int candIdx[kWarpCand];
+    int queue[2 * kWarpCand];
+    int list[kCellCap];
+    int nbCell[kNbCap];
+    int nbOff[kNbCap + 1];
+};
+constexpr size_t kDynSmemWarps = sizeof(WarpCell) * kCellWarps;
+
+__device__ __forceinline__ int warpExclusiveScan(int v, int& total) {
+    const int lane = threadIdx.x & 31;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    total = __shfl_sync(0xffffffffu, x, 31);
+    return x - v;
+}
+
+// Sum over the warp in a fixed order (butterfly), the same value in every lane.
+__device__ __forceinline__ double warpSumD(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// The moves of one cell by one warp; false when a wait for a neighbour gave up.
+__device__ bool warpMoveCell(const SweepArgs& a, WarpCell& W, int cx, int cy, int cz, int cell, int cnt, int phase,
+                             const int* posOf, unsigned stamp) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned ltMask = (1u << lane) - 1u;
+    const Grid& g = a.g;
+    const double3 box = mk(a.s.box[0], a.s.box[1], a.s.box[2]);
+    const int start = a.cellStart[cell];
+    for (int k = lane; k < cnt; k += 32) W.list[k] = a.cellIdx[start + k];
+    // the stencil's cells and their offsets in the candidate list (static during the sweep)
+    const int nx = axisCount(g.nc[0], g.s[0]), ny = axisCount(g.nc[1], g.s[1]), nz = axisCount(g.nc[2], g.s[2]);
+    const int nn = nx * ny * nz;
+    const int ownQ = ((g.nc[2] <= 2 * g.s[2] ? cz : g.s[2]) * ny + (g.nc[1] <= 2 * g.s[1] ? cy : g.s[1])) * nx +
+                     (g.nc[0] <= 2 * g.s[0] ? cx : g.s[0]);
+    int carry = 0;
+    for (int base = 0; base < nn; base += 32) {
+        const int q = base + lane;
+        int c = 0, cl = 0;
+        if (q < nn) {
+            const int x = axisCell(cx, q % nx, g.nc[0], g.s[0]);
+            const int y = axisCell(cy, (q / nx) % ny, g.nc[1], g.s[1]);
+            const int z = axisCell(cz, q / (nx * ny), g.nc[2], g.s[2]);
+            cl = (z * g.nc[1] + y) * g.nc[0] + x;
+            c = a.cellCount[cl];
+        }
+        int total;
+        const int off = warpExclusiveScan(c, total);
+        if (q < nn) { W.nbCell[q] = cl; W.nbOff[q] = carry + off; }
+        carry += total;
+    }
+    if (lane == 0) W.nbOff[nn] = carry;
+    __syncwarp();
+    const int nCand = carry;
+    const int ownOff = W.nbOff[ownQ];
+    const bool resident = nCand <= kWarpCand;
+    // the first proposal reads only this cell's own particles: built before the wait
+    buildProposal(a, W.list, W.nbCell, nn, W.prop, cell, cnt, 0, cx, cy, cz, box);
+    if (lane == 0) acceptThresholds(a, W.prop, cell, 0);
+    // the earlier-phase cells of the stencil have finished
+    bool fail = false;
+    for (int q = lane; q < nn && !fail; q += 32) {
+        const int x = axisCell(cx, q % nx, g.nc[0], g.s[0]);
+        const int y = axisCell(cy, (q / nx) % ny, g.nc[1], g.s[1]);
+        const int z = axisCell(cz, q / (nx * ny), g.nc[2], g.s[2]);
+        const int colour = (x % g.p[0]) + g.p[0] * ((y % g.p[1]) + g.p[1] * (z % g.p[2]));
+        if (posOf[colour] >= phase) continue;
+        const unsigned* f = &a.cellDone[(z * g.nc[1] + y) * g.nc[0] + x];
+        for (int spin = 0; loadAcquireGpu(f) != stamp; ++spin) {
+            if (spin >= a.flowSpin || ((spin & 255) == 255 && (*(volatile int*)a.err & E_FLOW_WAIT))) {
+                fail = true;
+                break;
+            }
+            __nanosleep(64);
+        }
+    }
+    fail = __any_sync(FULL, fail);
+    __syncwarp();
+    __threadfence();            // every lane reads the neighbours' states after the waits
+    if (fail) return false;
+    // candidates [first, first + count) of the stencil into the warp's buffers
+    auto load = [&](int first, int count) {
+        for (int kk = lane; kk < count; kk += 32) {
+            const int k = first + kk;
+            int lo = 0, hi = nn - 1;          // last q with nbOff[q] <= k
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (W.nbOff[mid] <= k) lo = mid; else hi = mid - 1;
+            }
+            const int slot = a.cellStart[W.nbCell[lo]] + (k - W.nbOff[lo]);
+            W.candIdx[kk] = a.cellIdx[slot];
+            W.candPos[kk] = a.cellPosF[slot];
+            W.candDir[kk] = a.cellDirF[slot];
+        }
+        __syncwarp();
+    };
+    if (resident) load(0, nCand);
+
+    DevCtx c;
+    c.params = a.t.params; c.mols = a.t.mols; c.ntypes = a.t.ntypes; c.n = a.s.n; c.sqmaxcut = a.t.sqmaxcut;
+    const float thr32 = candThreshold(c.sqmaxcut, box);
+    const float bxF = (float)box.x, byF = (float)box.y, bzF = (float)box.z;
+    double dECell = 0.0;
+    unsigned long long nAccT = 0, nRejT = 0, nAccR = 0, nRejR = 0, nTested = 0, nCellRej = 0;
+    unsigned nScr = 0, nEval = 0;
+    for (int m = 0; m < cnt; ++m) {
+        if (m > 0) {
+            buildProposal(a, W.list, W.nbCell, nn, W.prop, cell, cnt, m, cx, cy, cz, box);
+            if (lane == 0) acceptThresholds(a, W.prop, cell, m);
+            __syncwarp();
+        }
+        const Proposal& P = W.prop;
+        if (P.skip) {
+            if (lane == 0) { if (P.displace) { ++nRejT; ++nCellRej; } else ++nRejR; }
+            __syncwarp();
+            continue;
+        }
+        const int t = P.target;
+        const bool displace = P.displace;
+        const float3 oldF = P.oldF, newF = P.newF;
+        const float3 dOld = f3(P.odir[0], P.odir[1], P.odir[2]), dNew = f3(P.ndir[0], P.ndir[1], P.ndir[2]);
+        const Con con = makeCon(c, t, a.s.mol[t]);
+        double e0 = 0.0, e1 = 0.0;
+        // bonded partners: both configurations, whatever the distance
+        if (lane < P.nPartners) {
+            const PView b = viewAt(a.s, P.partners[lane]);
+            unsigned bb; double dd;
+            e0 += pairEnergy(c, moveView(a.s, P, false), b, con, box, &bb, &dd);
+            e1 += pairEnergy(c, moveView(a.s, P, true), b, con, box, &bb, &dd);
+        }
+        for (int wbase = 0; wbase < nCand; wbase += kWarpCand) {
+            const int wend = min(wbase + kWarpCand, nCand);
+            if (!resident) load(wbase, wend - wbase);
+            // stages A and B: FP32 candidate screen against the old and the new position, then
+            // the exact-zero screen on the FP32 separation and axes; survivors compacted
+            int qn = 0;
+            for (int r0 = wbase; r0 < wend; r0 += 32) {
+                const int k = r0 + lane - wbase;
+                bool k0 = false, k1 = false;
+                if (r0 + lane < wend) {
+                    const int j = W.candIdx[k];
+                    if (j != t && !isPartner(P, j)) {
+                        const float4 cp = W.candPos[k];
+                        const bool p0 = dist2f(cp, oldF, box) <= thr32;
+                        const bool p1 = displace ? dist2f(cp, newF, box) <= thr32 : p0;
+                        if (p0 || p1) {
+                            const float4 cd = W.candDir[k];
+                            const float3 dj = make_float3(cd.x, cd.y, cd.z);
+                            const PairParam& pp = c.params[P.type * c.ntypes + (int)cp.w];
+                            if (p0) {
+                                k0 = !screenedOutF(pp, pairVecF(oldF, cp, bxF, byF, bzF), dOld, dj);
+                                if (!k0) ++nScr;
+                            }
+                            if (p1) {
+                                k1 = !screenedOutF(pp, pairVecF(newF, cp, bxF, byF, bzF), dNew, dj);
+                                if (!k1) ++nScr;
+                            }
+                        }
+                    }
+                }
+                const unsigned b0 = __ballot_sync(FULL, k0), b1 = __ballot_sync(FULL, k1);
+                if (k0) W.queue[qn + __popc(b0 & ltMask)] = k << 1;
+                if (k1) W.queue[qn + __popc(b0) + __popc(b1 & ltMask)] = (k << 1) | 1;
+                qn += __popc(b0) + __popc(b1);
+            }
+            __syncwarp();
+            // stage C: the exact FP64 pair energies, one queue entry per lane
+            for (int e = lane; e < qn; e += 32) {
+                const int q = W.queue[e];
+                const PView b = viewAt(a.s, W.candIdx[q >> 1]);
+                unsigned bb; double dd;
+                const double en = pairEnergy(c, moveView(a.s, P, q & 1), b, con, box, &bb, &dd);
+                if (q & 1) e1 += en; else e0 += en;
+                ++nEval;
+            }
+            __syncwarp();           // the window's buffers are free
+        }
+        e0 = warpSumD(e0);
+        e1 = warpSumD(e1);
+        if (lane == 0) {
+            // MoveCreator::moveTry (movecreator.h:175-187)
+            const bool accept = (e1 <= e0) || ((e1 - e0) < P.thrMet);
+            nTested += (unsigned long long)nCand * (displace ? 2 : 1);
+            nEval += 2 * P.nPartners;
+            if (accept) {
+                a.s.pos[t] = make_double4_32a(P.npos[0], P.npos[1], P.npos[2], (double)P.type);
+                if (!displace) {
+                    a.s.dir[t] = make_double4_32a(P.ndir[0], P.ndir[1], P.ndir[2], P.dirW);
+                    a.s.patch[t] = P.npatch;
+                    const float4 nd = make_float4((float)P.ndir[0], (float)P.ndir[1], (float)P.ndir[2], 0.0f);
+                    a.cellDirF[start + P.slotR] = nd;
+                    if (resident) W.candDir[ownOff + P.slotR] = nd;
+                    ++nAccR;
+                } else {
+                    const float4 nf = make_float4(newF.x, newF.y, newF.z, (float)P.type);
+                    a.cellPosF[start + P.slotR] = nf;
+                    if (resident) W.candPos[ownOff + P.slotR] = nf;
+                    ++nAccT;
+                }
+                dECell += e1 - e0;
+            } else {
+                if (displace) ++nRejT; else ++nRejR;
+            }
+        }
+        __syncwarp();               // the new state before the next proposal reads it
+    }
+    if (lane == 0) {
+        a.cellDE[cell] = dECell;
+        atomicAdd(&a.counters[C_ACC_T], nAccT);
+        atomicAdd(&a.counters[C_REJ_T], nRejT);
+        atomicAdd(&a.counters[C_ACC_R], nAccR);
+        atomicAdd(&a.counters[C_REJ_R], nRejR);
+        atomicAdd(&a.counters[C_CELL_REJ], nCellRej);
+        atomicAdd(&a.counters[C_MOVES], (unsigned long long)cnt);
+        atomicAdd(&a.counters[C_TESTED], nTested);
+    }
+    nScr = __reduce_add_sync(FULL, nScr);
+    nEval = __reduce_add_sync(FULL, nEval);
+    if (lane == 0) {
+        if (nScr) atomicAdd(&a.counters[C_SCREENED], (unsigned long long)nScr);
+        if (nEval) atomicAdd(&a.counters[C_EVAL], (unsigned long long)nEval);
+    }
+    return true;
+}
+
+template <int MINB>
+__device__ __forceinline__ void warpFlowBody(const SweepArgs* __restrict__ A) {
+    const SweepArgs& a = A[blockIdx.y];
+    const Grid& g = a.g;
+    extern __shared__ float4 dynSmem[];
+    WarpCell& W = reinterpret_cast<WarpCell*>(dynSmem)[threadIdx.x >> 5];
+    __shared__ int posOf[kMaxColours];       // phase of each colour in this sweep
+    const int lane = threadIdx.x & 31;
+    const unsigned stamp = a.ctl->epoch;
+    for (int k = threadIdx.x; k < g.ncolours; k += blockDim.x) posOf[a.ctl->perm[k]] = k;
+    __syncthreads();
+    const int total = g.ncolours * g.nactive;
+    for (;;) {
+        int tk = 0;
+        if (lane == 0) tk = atomicAdd(&a.ctl->ticket, 1);
+        tk = __shfl_sync(0xffffffffu, tk, 0);
+        if (tk >= total) break;
+        const int phase = tk / g.nactive;
+        int cx, cy, cz;
+        decodeActive(g, a.ctl->perm[phase], tk - phase * g.nactive, cx, cy, cz);
+        const int cell = (cz * g.nc[1] + cy) * g.nc[0] + cx;
+        const int cnt = a.cellCount[cell];
+        if (cnt > 0 && cnt <= kCellCap) {
+            if (!warpMoveCell(a, W, cx, cy, cz, cell, cnt, phase, posOf, stamp)) {
+                if (lane == 0) atomicOr(a.err, E_FLOW_WAIT);
+                break;
+            }
+            __threadfence();        // each lane's state writes are visible GPU-wide ...
+            __syncwarp();
+        }
+        if (lane == 0) storeReleaseGpu(&a.cellDone[cell], stamp);     // ... before the flag
+    }
+}
+
+__global__ void __launch_bounds__(kCellWarps * 32, 2) kCellWarpsFlow(const SweepArgs* __restrict__ A) {
+    warpFlowBody<2>(A);
+}
+__global__ void __launch_bounds__(kCellWarps * 32, 3) kCellWarpsFlowDense(const SweepArgs* __restrict__ A) {
+    warpFlowBody<3>(A);
 }
 
 // ---- Wang-Landau: the order parameters' cells, chain moves, flatness ---------------------
@@ -2526,7 +2818,7 @@ struct Batch {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<cudaEvent_t> evPhase;     // time_phases: start / end of each sweep's move launches
     cudaGraphExec_t graph = nullptr;
-    int graphDims[14] = {0};   // launch shape the graph was captured with
+    int graphDims[15] = {0};   // launch shape the graph was captured with
     long graphLaunches = 0, graphPhaseLaunches = 0;
     // parallel tempering
     int* dLadder = nullptr;
@@ -2957,7 +3249,22 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
         if ((r = cudaFuncSetAttribute(kWlCells, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDynSmemColour)) !=
             cudaSuccess)
             return cudaFail(r, "shared memory attribute");
+        if ((r = cudaFuncSetAttribute(kCellWarpsFlow, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)kDynSmemWarps)) != cudaSuccess)
+            return cudaFail(r, "shared memory attribute");
+        if ((r = cudaFuncSetAttribute(kCellWarpsFlowDense, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)kDynSmemWarps)) != cudaSuccess)
+            return cudaFail(r, "shared memory attribute");
         attrSet |= devBit;
+    }
+    // resident CTAs per SM of the warp-per-cell kernels (their grids are persistent)
+    static int warpBlocks[2][64] = {};
+    if (!warpBlocks[0][b.device & 63]) {
+        int nb0 = 0, nb1 = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb0, kCellWarpsFlow, kCellWarps * 32, kDynSmemWarps);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb1, kCellWarpsFlowDense, kCellWarps * 32, kDynSmemWarps);
+        warpBlocks[0][b.device & 63] = std::max(1, nb0);
+        warpBlocks[1][b.device & 63] = std::max(1, nb1);
     }
     auto dims = [&](int x) { return dim3((unsigned)std::max(1, x), (unsigned)ns); };
     // systems with a surrogate stage their candidates' FP32 axes and patches as well
@@ -2967,10 +3274,13 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
     const bool dense = (p.variant & 1) != 0;
     // dataflow sweep: one launch per sweep, CTAs per system so that the batch fills the SMs
     // (two CTAs per SM at up to 255 registers, three at 170)
-    const bool flow = (p.variant & 4) != 0;
+    const bool warpCells = (p.variant & 8) != 0;          // one warp per cell (a dataflow sweep)
+    const bool flow = (p.variant & 4) != 0 || warpCells;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b.sys[0]->device);
     const int flowCtas = std::max(1, std::min(b.maxColours * b.maxActive, std::max(1, sms) * (dense ? 3 : 2) / ns));
+    const int warpCtas = std::max(1, std::min((b.maxColours * b.maxActive + kCellWarps - 1) / kCellWarps,
+                                              std::max(1, sms) * warpBlocks[dense ? 1 : 0][b.device & 63] / ns));
     auto launchCellsOf = [&](const SweepArgs* args, int maxCells) -> cudaError_t {
         kZeroCounts<<<dims((maxCells + 255) / 256), 256, 0, s>>>(args);
         kAssign<<<dims((b.maxN + 255) / 256), 256, 0, s>>>(args);
@@ -3004,7 +3314,10 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
         if (r2 != cudaSuccess) return r2;
         const bool timed = timing && 2 * phaseEvents + 1 < (int)b.evPhase.size();
         if (timed) cudaEventRecord(b.evPhase[2 * phaseEvents], s);
-        if (flow) {
+        if (warpCells) {
+            if (dense) kCellWarpsFlowDense<<<dims(warpCtas), kCellWarps * 32, kDynSmemWarps, s>>>(b.dArgs);
+            else kCellWarpsFlow<<<dims(warpCtas), kCellWarps * 32, kDynSmemWarps, s>>>(b.dArgs);
+        } else if (flow) {
             if (dense) kColourFlowDense<<<dims(flowCtas), kMoveThreads, colourSmem, s>>>(b.dArgs);
             else kColourFlow<<<dims(flowCtas), kMoveThreads, colourSmem, s>>>(b.dArgs);
         } else {
@@ -3087,9 +3400,9 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
         long left = nsweeps - sw;
         bool aligned = (sw % G == 0) && (nextExchange < 0 || nextExchange - sw >= G) && (nextWl < 0 || nextWl - sw >= G);
         if (useGraph && left >= G && aligned) {
-            int key[14] = {ns, b.maxN, b.maxCells, b.maxActive, b.maxColours, (int)G, anySurrogate ? 1 : 0,
+            int key[15] = {ns, b.maxN, b.maxCells, b.maxActive, b.maxColours, (int)G, anySurrogate ? 1 : 0,
                            b.chains ? 1 : 0, b.maxCellsC, b.maxActiveC, b.maxColoursC, dense ? 1 : 0, flow ? 1 : 0,
-                           b.wl ? 1 : 0};
+                           b.wl ? 1 : 0, warpCells ? 1 : 0};
             if (!b.graph || std::memcmp(key, b.graphDims, sizeof key) != 0) {
                 if (b.graph) { cudaGraphExecDestroy(b.graph); b.graph = nullptr; }
                 cudaGraph_t graph;
@@ -3202,7 +3515,9 @@ static int checkParams(const sc_run_params& p) {
     if (!(p.temper > 0)) return fail(SC_ERR_ARG, "temper must be positive");
     if (p.ptype < 0 || p.ptype > 5) return fail(SC_ERR_ARG, "ptype must be 0..5 (movecreator.cpp:349-546)");
     if (p.stencil < 0 || p.stencil > 3) return fail(SC_ERR_ARG, "stencil must be 0 (auto), 1, 2 or 3");
-    if (p.variant < -1 || p.variant > 7) return fail(SC_ERR_ARG, "variant must be -1 (tuned) or 0..7");
+    if (p.variant < -1 || p.variant > 15) return fail(SC_ERR_ARG, "variant must be -1 (tuned) or 0..15");
+    if (p.variant > 0 && (p.variant & 8) && p.delayed)
+        return fail(SC_ERR_UNSUPPORTED, "the warp-per-cell kernel (variant bit 3) runs plain moves only");
     if (p.flow_wait_polls < 0) return fail(SC_ERR_ARG, "flow_wait_polls must be >= 0");
     return SC_OK;
 }
@@ -3228,6 +3543,8 @@ int runSweeps(Context* c, const sc_run_params& p0, sc_run_stats& st) {
     if (p.delayed && !c->surrogate) return fail(SC_ERR_STATE, "delayed = 1 needs a surrogate (sc_set_surrogate)");
     if ((rc = checkMoves(c))) return rc;
     if ((rc = wlCheckRun(c, p))) return rc;
+    if ((p.variant & 8) && wlActive(c))
+        return fail(SC_ERR_UNSUPPORTED, "the warp-per-cell kernel (variant bit 3) does not run Wang-Landau moves");
     const bool npt = p.volume_every > 0;
     if ((rc = prepareSystem(c, p, npt))) return rc;
     if (!c->batch) {
@@ -3304,7 +3621,7 @@ int screenSurvivors(Context* c, int ntargets, const int* targets, long cap, int*
 // fastest for later runs with variant = -1.  Candidates: reach 1, 2, 3 (cells maxcut/s
 // wide: how many cells move at once and how many candidates each stages) times variants
 // {colour-phase launches, dataflow sweep} x {lowest latency, more CTAs per SM}, plus paired
-// passes for plain moves.
+// passes and the warp-per-cell dataflow sweep for plain moves.
 int tuneSweeps(Context* c, const sc_run_params& p, int sweeps, sc_run_params& best, double* rates, int* ncand) {
     if (sweeps < 1) return fail(SC_ERR_ARG, "sc_tune: sweeps must be >= 1");
     if (wlActive(c)) return fail(SC_ERR_UNSUPPORTED, "sc_tune with Wang-Landau weights: tuning sweeps would change them");
@@ -3321,7 +3638,8 @@ int tuneSweeps(Context* c, const sc_run_params& p, int sweeps, sc_run_params& be
         c->hostNewer = true;
         c->devNewer = false;
     };
-    std::vector<int> variants = p.delayed ? std::vector<int>{0, 1, 4, 5} : std::vector<int>{0, 1, 2, 3, 4, 5};
+    std::vector<int> variants = p.delayed ? std::vector<int>{0, 1, 4, 5} : std::vector<int>{0, 1, 2, 3, 4, 5, 8, 9};
+    if (wlActive(c)) variants = {0, 1, 4, 5};
     double bestRate = -1.0;
     int k = 0;
     best = p;
@@ -3431,6 +3749,8 @@ int runReplicas(void* h, const sc_run_params& p, int exchangeEvery, sc_run_stats
         q.variant = p.variant < 0 ? 4 : p.variant;     // a batch has no tuned choice of its own
         if (p.delayed && !c->surrogate) return fail(SC_ERR_STATE, "delayed = 1 needs a surrogate on every replica");
         if ((rc = wlCheckRun(c, q))) return rc;
+        if ((q.variant & 8) && wlActive(c))
+            return fail(SC_ERR_UNSUPPORTED, "the warp-per-cell kernel (variant bit 3) does not run Wang-Landau moves");
         if (p.transmx > 0) q.transmx = p.transmx;
         if (p.rot_angle > 0) q.rot_angle = p.rot_angle;
         q.chainprob = p.chainprob;

@@ -306,9 +306,10 @@ def test_tuner_restores_state_and_is_used():
     p = s.default_run()
     p.seed, p.check_every = 4, 0
     best, rates = s.tune(p, sweeps=2)
-    assert len(rates) == 18 and max(rates) > 0
-    assert best.stencil in (1, 2, 3) and 0 <= best.variant <= 7
-    assert rates[(best.stencil - 1) * 6 + best.variant] == max(rates)
+    variants = [0, 1, 2, 3, 4, 5, 8, 9]
+    assert len(rates) == 3 * len(variants) and max(rates) > 0
+    assert best.stencil in (1, 2, 3) and best.variant in variants
+    assert rates[(best.stencil - 1) * len(variants) + variants.index(best.variant)] == max(rates)
     after = s.particles()
     assert np.array_equal(s.box, box)
     for k in range(s.n):
@@ -317,3 +318,49 @@ def test_tuner_restores_state_and_is_used():
     exact = s.all_to_all()
     assert abs(st.energy - exact) <= 1e-9 * max(1.0, abs(exact))
     s.close()
+
+
+@pytest.mark.parametrize("variant", [8, 9])
+@pytest.mark.parametrize("name", ["syn_cpsc_spa_npt_small", "syn_bilayer_small", "syn_psc_nvt_small"])
+def test_warp_cells_exact_and_reproducible(name, variant):
+    """The warp-per-cell dataflow sweep (variant bit 3): the running energy stays the exact
+    total through moves, volume moves and chain moves, and a rerun from the same start with
+    the same seed reproduces the state bit for bit."""
+    from sc_gb300 import System
+
+    g = goldens.load(name)
+    inp = g["inputs"]
+    runs = []
+    for _ in range(2):
+        s = System.from_text(inp["options"], inp["top.init"], inp["config.init"])
+        st = s.simulate(nsweeps=30, seed=17, variant=variant, stencil=2 if "psc_nvt" in name else 0,
+                        check_every=10)
+        exact = s.all_to_all()
+        assert abs(st.energy - exact) <= 1e-9 * max(1.0, abs(exact)), (st.energy, exact)
+        assert st.max_drift <= 1e-9 * max(1.0, abs(exact))
+        assert st.acc_trans + st.acc_rot > 0 and st.moves >= 30 * s.n
+        runs.append((st.energy, [tuple(q.pos) + tuple(q.dir) for q in s.particles()], tuple(s.box)))
+        s.close()
+    assert runs[0] == runs[1]
+
+
+@pytest.mark.parametrize("name", ["syn_cpsc_spa_npt_small", "syn_psc_nvt_small"])
+def test_warp_cells_follow_the_cta_kernel(name):
+    """Same proposals, screens and pair energies as the CTA-per-cell dataflow kernel: from the
+    same start and seed both take the same decisions (the same states), and their running
+    energies differ only by the summation order."""
+    from sc_gb300 import System
+
+    g = goldens.load(name)
+    inp = g["inputs"]
+    out = {}
+    for v in (4, 8):
+        s = System.from_text(inp["options"], inp["top.init"], inp["config.init"])
+        st = s.simulate(nsweeps=6, seed=23, variant=v, stencil=2, check_every=0)
+        out[v] = (st, [tuple(q.pos) + tuple(q.dir) for q in s.particles()], tuple(s.box))
+        s.close()
+    a, b = out[4], out[8]
+    assert (a[0].acc_trans, a[0].acc_rot, a[0].acc_vol) == (b[0].acc_trans, b[0].acc_rot, b[0].acc_vol)
+    assert a[1] == b[1] and a[2] == b[2]
+    assert abs(a[0].energy - b[0].energy) <= 1e-11 * max(1.0, abs(a[0].energy))
+    assert a[0].pairs_tested == b[0].pairs_tested
