@@ -320,19 +320,26 @@ def test_tuner_restores_state_and_is_used():
     s.close()
 
 
+def _texts(name):
+    from sc_gb300 import workloads
+
+    if name == "lipids":            # three-bead lipids with bonds and chain moves, no overlaps
+        return workloads.lipids_dilute(64, seed=3)
+    inp = goldens.load(name)["inputs"]
+    return inp["options"], inp["top.init"], inp["config.init"]
+
+
 @pytest.mark.parametrize("variant", [8, 9])
-@pytest.mark.parametrize("name", ["syn_cpsc_spa_npt_small", "syn_bilayer_small", "syn_psc_nvt_small"])
+@pytest.mark.parametrize("name", ["syn_cpsc_spa_npt_small", "lipids", "syn_psc_nvt_small"])
 def test_warp_cells_exact_and_reproducible(name, variant):
     """The warp-per-cell dataflow sweep (variant bit 3): the running energy stays the exact
     total through moves, volume moves and chain moves, and a rerun from the same start with
     the same seed reproduces the state bit for bit."""
     from sc_gb300 import System
 
-    g = goldens.load(name)
-    inp = g["inputs"]
     runs = []
     for _ in range(2):
-        s = System.from_text(inp["options"], inp["top.init"], inp["config.init"])
+        s = System.from_text(*_texts(name))
         st = s.simulate(nsweeps=30, seed=17, variant=variant, stencil=2 if "psc_nvt" in name else 0,
                         check_every=10)
         exact = s.all_to_all()
@@ -344,18 +351,16 @@ def test_warp_cells_exact_and_reproducible(name, variant):
     assert runs[0] == runs[1]
 
 
-@pytest.mark.parametrize("name", ["syn_cpsc_spa_npt_small", "syn_psc_nvt_small"])
+@pytest.mark.parametrize("name", ["syn_cpsc_spa_npt_small", "syn_psc_nvt_small", "syn_bilayer_small", "lipids"])
 def test_warp_cells_follow_the_cta_kernel(name):
     """Same proposals, screens and pair energies as the CTA-per-cell dataflow kernel: from the
     same start and seed both take the same decisions (the same states), and their running
     energies differ only by the summation order."""
     from sc_gb300 import System
 
-    g = goldens.load(name)
-    inp = g["inputs"]
     out = {}
     for v in (4, 8):
-        s = System.from_text(inp["options"], inp["top.init"], inp["config.init"])
+        s = System.from_text(*_texts(name))
         st = s.simulate(nsweeps=6, seed=23, variant=v, stencil=2, check_every=0)
         out[v] = (st, [tuple(q.pos) + tuple(q.dir) for q in s.particles()], tuple(s.box))
         s.close()
