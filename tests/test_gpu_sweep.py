@@ -321,16 +321,22 @@ def test_tuner_restores_state_and_is_used():
 
 
 def _texts(name):
+    """Seeded starts without overlaps (the golden fixtures start with overlap energies up to
+    1e17, which a running energy cannot carry to 1e-9 of the relaxed total in FP64)."""
     from sc_gb300 import workloads
 
-    if name == "lipids":            # three-bead lipids with bonds and chain moves, no overlaps
+    if name == "lipids":            # three-bead lipids with bonds and chain moves
         return workloads.lipids_dilute(64, seed=3)
+    if name == "mixture":           # CPSC + SPA, NPT with isotropic volume moves
+        return workloads.npt_cpsc_spa(300, seed=2)
+    if name == "psc":
+        return workloads.nvt_psc(250, phi=0.15, seed=2)
     inp = goldens.load(name)["inputs"]
     return inp["options"], inp["top.init"], inp["config.init"]
 
 
 @pytest.mark.parametrize("variant", [8, 9])
-@pytest.mark.parametrize("name", ["syn_cpsc_spa_npt_small", "lipids", "syn_psc_nvt_small"])
+@pytest.mark.parametrize("name", ["mixture", "lipids", "psc"])
 def test_warp_cells_exact_and_reproducible(name, variant):
     """The warp-per-cell dataflow sweep (variant bit 3): the running energy stays the exact
     total through moves, volume moves and chain moves, and a rerun from the same start with
@@ -340,8 +346,7 @@ def test_warp_cells_exact_and_reproducible(name, variant):
     runs = []
     for _ in range(2):
         s = System.from_text(*_texts(name))
-        st = s.simulate(nsweeps=30, seed=17, variant=variant, stencil=2 if "psc_nvt" in name else 0,
-                        check_every=10)
+        st = s.simulate(nsweeps=30, seed=17, variant=variant, check_every=10)
         exact = s.all_to_all()
         assert abs(st.energy - exact) <= 1e-9 * max(1.0, abs(exact)), (st.energy, exact)
         assert st.max_drift <= 1e-9 * max(1.0, abs(exact))
@@ -351,7 +356,8 @@ def test_warp_cells_exact_and_reproducible(name, variant):
     assert runs[0] == runs[1]
 
 
-@pytest.mark.parametrize("name", ["syn_cpsc_spa_npt_small", "syn_psc_nvt_small", "syn_bilayer_small", "lipids"])
+@pytest.mark.parametrize("name", ["syn_cpsc_spa_npt_small", "syn_psc_nvt_small", "syn_bilayer_small", "lipids",
+                                  "mixture"])
 def test_warp_cells_follow_the_cta_kernel(name):
     """Same proposals, screens and pair energies as the CTA-per-cell dataflow kernel: from the
     same start and seed both take the same decisions (the same states), and their running
