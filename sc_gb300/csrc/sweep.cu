@@ -3724,12 +3724,15 @@ int createReplicas(Context* const* sys, int nrep, const double* temps, const int
 
 void destroyReplicas(void* h) { delete static_cast<ReplicaSet*>(h); }
 
-int runReplicas(void* h, const sc_run_params& p, int exchangeEvery, sc_run_stats& st, double* tempsOut,
+int runReplicas(void* h, const sc_run_params& p0, int exchangeEvery, sc_run_stats& st, double* tempsOut,
                 double* energiesOut, long* exTried, long* exAcc) {
     ReplicaSet* R = static_cast<ReplicaSet*>(h);
     std::memset(&st, 0, sizeof st);
-    int rc = checkParams(p);
+    int rc = checkParams(p0);
     if (rc) return rc;
+    // a batch has no tuned choice of its own: variant -1 is the dataflow sweep
+    sc_run_params p = p0;
+    if (p.variant < 0) p.variant = 4;
     Batch& b = R->b;
     const int nrep = (int)b.sys.size();
     const bool npt = p.volume_every > 0;
@@ -3746,7 +3749,7 @@ int runReplicas(void* h, const sc_run_params& p, int exchangeEvery, sc_run_stats
         q.nsweeps = p.nsweeps; q.seed = p.seed + 0x9E3779B97F4A7C15ull * (unsigned long long)(k + 1);
         q.temper = R->temps[k]; q.ptype = p.ptype; q.volume_every = p.volume_every; q.check_every = p.check_every;
         q.stencil = p.stencil; q.time_phases = p.time_phases; q.press = p.press; q.delayed = p.delayed;
-        q.variant = p.variant < 0 ? 4 : p.variant;     // a batch has no tuned choice of its own
+        q.variant = p.variant;
         if (p.delayed && !c->surrogate) return fail(SC_ERR_STATE, "delayed = 1 needs a surrogate on every replica");
         if ((rc = wlCheckRun(c, q))) return rc;
         if ((q.variant & 8) && wlActive(c))
