@@ -181,6 +181,12 @@ int sc_all_to_all(sc_context* ctx, double* e);
 /* Updater::alignmentOrder (scOOP/mc/updater.cpp:466-481): sum of axis dot products over pairs
  * whose centres are closer than 1.5 (the second column of energy.dat). */
 int sc_alignment_order(sc_context* ctx, double* order);
+/* No counterpart in the reference (its analysis reports the pair alignment above): the
+ * nematic order parameter S2, the largest eigenvalue of Q = <3/2 u u^T - 1/2 I> over the
+ * axes u of the spherocylinders (spheres excluded), and the director (its unit eigenvector,
+ * may be NULL).  1 for a perfectly aligned phase, about 0 for an isotropic one; 0 when the
+ * system holds no spherocylinder. */
+int sc_nematic_order(sc_context* ctx, double* s2, double director[3]);
 /* TotalEMatrix::mol2othersTrial (totalenergycalculator.h:453-499). */
 int sc_mol_to_others(sc_context* ctx, int first, int size, double* e);
 /* The energy half of MoveCreator::partDisplace / partRotate (movecreator.cpp:947-1028):
@@ -199,6 +205,34 @@ int sc_default_run(const sc_context* ctx, sc_run_params* p);
 /* Runs p->nsweeps sweeps on the device; stats->sweeps is the number run (fewer when a
  * Wang-Landau run converged, as the reference's loop stops there, updater.cpp:255-265). */
 int sc_simulate(sc_context* ctx, const sc_run_params* p, sc_run_stats* stats);
+
+/* --- equilibration: adaptation of the maximum steps (Updater::simulate's adjustment block,
+ * scOOP/mc/updater.cpp:238-253, with optimizeStep / optimizeRot, updater.cpp:395-464, and
+ * the equilibrate-then-produce sequence of main.cpp:270-297) ------------------------------ */
+typedef struct {
+    double trans[40];          /* maximum displacement per particle type (full length, as transmx) */
+    double rot_cos[40];        /* the reference's rotation record per type: cos of the maximum angle,
+                                  adapted by optimizeRot; as in the reference (whose rotations read
+                                  Disp::angle) the moves keep the options' rotation angle */
+    double chain_trans[8];     /* chain displacement per molecule type */
+    double chain_rot_cos[8];
+    double edge;               /* box edge change range (as edge_mx) */
+    long adjustments;          /* sc_adjust_steps applications so far */
+    long acc_trans[40], rej_trans[40], acc_rot[40], rej_rot[40];       /* the counts of the last run */
+    long acc_chain_trans[8], rej_chain_trans[8], acc_chain_rot[8], rej_chain_rot[8];
+    long acc_edge, rej_edge;
+} sc_step_sizes;
+int sc_get_step_sizes(sc_context* ctx, sc_step_sizes* out);
+/* One adjustment on the last run's acceptance counts: optimizeStep on the displacement of every
+ * particle type and chain molecule type that moved (upper bound 1.5), optimizeRot on their
+ * rotation records (5.0, 0.01) and optimizeStep on the box edge (1.0).  Later runs displace
+ * by the adapted per-type steps (scaled as the run's transmx / chainmmx scale the options'
+ * values) and sc_default_run returns the adapted edge range. */
+int sc_adjust_steps(sc_context* ctx);
+/* main.cpp:270-287: nequil/2 sweeps with an adjustment every `adjust` sweeps (none with
+ * adjust = 0), then nequil/2 sweeps without; stats sums both.  Write config.eq afterwards with
+ * sc_write_config (the same format). */
+int sc_equilibrate(sc_context* ctx, const sc_run_params* p, long nequil, long adjust, sc_run_stats* stats);
 
 /* No counterpart in the reference (its loop has no launch shapes to choose).  Times every
  * candidate launch shape of the move kernel for p's mode (plain or delayed) on the context's

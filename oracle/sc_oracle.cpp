@@ -712,6 +712,45 @@ void or_prefilter_pairs(const or_system* s, int nt, const int* targets, long cap
     *count = c;
 }
 
+// Nematic order parameter (no counterpart in the reference): S2, the largest eigenvalue of
+// Q = <3/2 u u^T - 1/2 I> over the axes of the spherocylinders (geotype < SP), and the
+// director, by cyclic Jacobi rotations.
+int or_nematic(const or_system* s, double* s2, double dir[3]) {
+    double m[7] = {0, 0, 0, 0, 0, 0, 0};
+    for (int i = 0; i < s->n; ++i) {
+        const or_particle& p = s->p[i];
+        if (P(s, p.type, p.type).geotype[0] >= SP) continue;
+        const or_vec& d = p.dir;
+        m[0] += 1.0;
+        m[1] += d.x * d.x; m[2] += d.y * d.y; m[3] += d.z * d.z;
+        m[4] += d.x * d.y; m[5] += d.x * d.z; m[6] += d.y * d.z;
+    }
+    if (m[0] < 1.0) { *s2 = 0.0; if (dir) dir[0] = dir[1] = dir[2] = 0.0; return 0; }
+    const double n = m[0];
+    double a[3][3] = {{1.5 * m[1] / n - 0.5, 1.5 * m[4] / n, 1.5 * m[5] / n},
+                      {1.5 * m[4] / n, 1.5 * m[2] / n - 0.5, 1.5 * m[6] / n},
+                      {1.5 * m[5] / n, 1.5 * m[6] / n, 1.5 * m[3] / n - 0.5}};
+    double v[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    for (int sweep = 0; sweep < 60; ++sweep) {
+        if (a[0][1] * a[0][1] + a[0][2] * a[0][2] + a[1][2] * a[1][2] < 1e-30) break;
+        for (int p = 0; p < 2; ++p)
+            for (int q = p + 1; q < 3; ++q) {
+                if (a[p][q] == 0.0) continue;
+                const double th = (a[q][q] - a[p][p]) / (2.0 * a[p][q]);
+                const double t = (th >= 0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1.0));
+                const double c = 1.0 / std::sqrt(t * t + 1.0), sn = t * c;
+                for (int k = 0; k < 3; ++k) { double x = a[k][p], y = a[k][q]; a[k][p] = c * x - sn * y; a[k][q] = sn * x + c * y; }
+                for (int k = 0; k < 3; ++k) { double x = a[p][k], y = a[q][k]; a[p][k] = c * x - sn * y; a[q][k] = sn * x + c * y; }
+                for (int k = 0; k < 3; ++k) { double x = v[k][p], y = v[k][q]; v[k][p] = c * x - sn * y; v[k][q] = sn * x + c * y; }
+            }
+    }
+    int b = 0;
+    for (int k = 1; k < 3; ++k) if (a[k][k] > a[b][b]) b = k;
+    *s2 = a[b][b];
+    if (dir) for (int k = 0; k < 3; ++k) dir[k] = v[k][b];
+    return 0;
+}
+
 // TotalEMatrix::mol2othersTrial (totalenergycalculator.h:453-499): empty conlist.
 double or_mol2others(const or_system* s, int first, int size) {
     // An empty conlist is what a moleculeless system would give: evaluate with a

@@ -79,6 +79,9 @@ double or_pair_energy(const or_system* s, int i, int j, unsigned* bits, double* 
 double or_one_to_all(const or_system* s, int target);
 double or_all_to_all(const or_system* s);
 double or_mol2others(const or_system* s, int first, int size);
+/* Nematic order S2 (largest eigenvalue of <3/2 u u^T - 1/2 I> over the spherocylinders'
+ * axes) and the director (may be NULL); no counterpart in the reference. */
+int or_nematic(const or_system* s, double* s2, double dir[3]);
 /* PairE over a batch of ordered pairs (bits, dsq may be NULL). */
 void or_pair_energies(const or_system* s, long n, const int* I, const int* J, double* E, unsigned* bits, double* dsq);
 /* The ordered pairs (i a target, or any particle when targets is NULL; j != i) that PairE's

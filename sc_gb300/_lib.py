@@ -21,6 +21,14 @@ class ScError(RuntimeError):
         self.code = code
 
 
+class StepSizes(C.Structure):
+    _fields_ = [("trans", C.c_double * 40), ("rot_cos", C.c_double * 40), ("chain_trans", C.c_double * 8),
+                ("chain_rot_cos", C.c_double * 8), ("edge", C.c_double), ("adjustments", C.c_long)] + [
+        (k, C.c_long * 40) for k in ("acc_trans", "rej_trans", "acc_rot", "rej_rot")] + [
+        (k, C.c_long * 8) for k in ("acc_chain_trans", "rej_chain_trans", "acc_chain_rot", "rej_chain_rot")] + [
+        ("acc_edge", C.c_long), ("rej_edge", C.c_long)]
+
+
 class PairParam(C.Structure):
     _fields_ = [("geotype", C.c_int * 2), ("exclude", C.c_int), ("kind", C.c_int),
                 ("sigma", C.c_double), ("epsilon", C.c_double), ("A", C.c_double), ("B", C.c_double),
@@ -106,6 +114,10 @@ SIGNATURES = [
     ("sc_trial_volume", C.c_int, [_P, C.c_double, _D]),
     ("sc_default_run", C.c_int, [_P, C.POINTER(RunParams)]),
     ("sc_simulate", C.c_int, [_P, C.POINTER(RunParams), C.POINTER(RunStats)]),
+    ("sc_nematic_order", C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    ("sc_get_step_sizes", C.c_int, [_P, C.c_void_p]),
+    ("sc_adjust_steps", C.c_int, [_P]),
+    ("sc_equilibrate", C.c_int, [_P, C.POINTER(RunParams), C.c_long, C.c_long, C.POINTER(RunStats)]),
     ("sc_tune", C.c_int, [_P, C.POINTER(RunParams), C.c_int, C.POINTER(RunParams), C.POINTER(C.c_double),
                           C.POINTER(C.c_int)]),
     ("sc_screen_survivors", C.c_int, [_P, C.c_int, C.POINTER(C.c_int), C.c_long, C.POINTER(C.c_int),

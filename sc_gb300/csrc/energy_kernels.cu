@@ -203,6 +203,35 @@ cudaError_t launchOneToAll(const DevState& s, const DevTables& t, int ntargets, 
 
 int allToAllBlocks(int n) { return ((n + 1) / 2 + kAllBlock - 1) / kAllBlock; }
 
+// Second-moment sums of the axes of the spherocylinders (geotype < SP): out[0] their count,
+// out[1..6] the sums of xx, yy, zz, xy, xz, yz.  One CTA; every thread sums a fixed strided
+// subset, then a fixed tree: the result does not depend on scheduling.
+__global__ void __launch_bounds__(256) kAxisMoments(DevState s, DevTables t, double* out) {
+    __shared__ double red[7][256];
+    double m[7] = {0, 0, 0, 0, 0, 0, 0};
+    for (int i = threadIdx.x; i < s.n; i += 256) {
+        const int ty = (int)s.pos[i].w;
+        if (t.params[ty * t.ntypes + ty].geotype[0] >= SP) continue;
+        const double4_32a d = s.dir[i];
+        m[0] += 1.0;
+        m[1] += d.x * d.x; m[2] += d.y * d.y; m[3] += d.z * d.z;
+        m[4] += d.x * d.y; m[5] += d.x * d.z; m[6] += d.y * d.z;
+    }
+    for (int k = 0; k < 7; ++k) red[k][threadIdx.x] = m[k];
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w)
+            for (int k = 0; k < 7; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x < 7) out[threadIdx.x] = red[threadIdx.x][0];
+}
+
+cudaError_t launchAxisMoments(const DevState& s, const DevTables& t, double* out, cudaStream_t st) {
+    kAxisMoments<<<1, 256, 0, st>>>(s, t, out);
+    return cudaGetLastError();
+}
+
 cudaError_t launchAlignment(const DevState& s, double* partial, int npartial, double* out, cudaStream_t st) {
     int nb = allToAllBlocks(s.n);
     if (nb > npartial) return cudaErrorInvalidValue;

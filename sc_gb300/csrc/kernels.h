@@ -43,6 +43,8 @@ cudaError_t launchAllToAll(const DevState& s, const DevTables& t, const double* 
 int allToAllBlocks(int n);
 // Updater::alignmentOrder: sum of axis dot products over pairs closer than 1.5.
 cudaError_t launchAlignment(const DevState& s, double* partial, int npartial, double* out, cudaStream_t st);
+// Count and second-moment sums (xx, yy, zz, xy, xz, yz) of the spherocylinders' axes (7 doubles).
+cudaError_t launchAxisMoments(const DevState& s, const DevTables& t, double* out, cudaStream_t st);
 // mol2othersTrial: molecule [first, first+size) against the rest with an empty conlist.
 cudaError_t launchMolToOthers(const DevState& s, const DevTables& t, int first, int size, double* out, cudaStream_t st);
 

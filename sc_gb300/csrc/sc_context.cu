@@ -2,6 +2,7 @@
 // and the energy entry points.  The move loop lives in sweep.cu.
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -529,6 +530,67 @@ int sc_alignment_order(sc_context* ctx, double* out) {
     return SC_OK;
 }
 
+// Largest eigenvalue and its unit eigenvector of a symmetric 3x3 matrix (cyclic Jacobi).
+static void largestEigen(double a[3][3], double* value, double vec[3]) {
+    double v[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    for (int sweep = 0; sweep < 50; ++sweep) {
+        double off = a[0][1] * a[0][1] + a[0][2] * a[0][2] + a[1][2] * a[1][2];
+        if (off < 1e-30) break;
+        for (int p = 0; p < 2; ++p)
+            for (int q = p + 1; q < 3; ++q) {
+                if (a[p][q] == 0.0) continue;
+                double theta = (a[q][q] - a[p][p]) / (2.0 * a[p][q]);
+                double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+                double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+                for (int k = 0; k < 3; ++k) {      // a = J^T a J
+                    double akp = a[k][p], akq = a[k][q];
+                    a[k][p] = c * akp - s * akq;
+                    a[k][q] = s * akp + c * akq;
+                }
+                for (int k = 0; k < 3; ++k) {
+                    double apk = a[p][k], aqk = a[q][k];
+                    a[p][k] = c * apk - s * aqk;
+                    a[q][k] = s * apk + c * aqk;
+                }
+                for (int k = 0; k < 3; ++k) {
+                    double vkp = v[k][p], vkq = v[k][q];
+                    v[k][p] = c * vkp - s * vkq;
+                    v[k][q] = s * vkp + c * vkq;
+                }
+            }
+    }
+    int best = 0;
+    for (int k = 1; k < 3; ++k) if (a[k][k] > a[best][best]) best = k;
+    *value = a[best][best];
+    for (int k = 0; k < 3; ++k) vec[k] = v[k][best];
+}
+
+int sc_nematic_order(sc_context* ctx, double* s2, double director[3]) {
+    if (!ctx || !s2) return fail(SC_ERR_ARG, "null argument");
+    Context* c = C(ctx);
+    DeviceScope dev(c->device);
+    int rc = c->ensureDevice();
+    if (rc) return rc;
+    cudaError_t e;
+    if ((e = launchAxisMoments(c->d, c->tables, c->dScalars, c->stream)) != cudaSuccess) return cudaFail(e, "axis moments");
+    double m[7];
+    if ((e = cudaMemcpyAsync(m, c->dScalars, sizeof m, cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess) return cudaFail(e, "copy");
+    if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess) return cudaFail(e, "nematic order");
+    if (m[0] < 1.0) {
+        *s2 = 0.0;
+        if (director) director[0] = director[1] = director[2] = 0.0;
+        return SC_OK;
+    }
+    const double n = m[0];
+    double q[3][3] = {{1.5 * m[1] / n - 0.5, 1.5 * m[4] / n, 1.5 * m[5] / n},
+                      {1.5 * m[4] / n, 1.5 * m[2] / n - 0.5, 1.5 * m[6] / n},
+                      {1.5 * m[5] / n, 1.5 * m[6] / n, 1.5 * m[3] / n - 0.5}};
+    double d[3];
+    largestEigen(q, s2, d);
+    if (director) for (int k = 0; k < 3; ++k) director[k] = d[k];
+    return SC_OK;
+}
+
 int sc_mol_to_others(sc_context* ctx, int first, int size, double* out) {
     if (!ctx || !out) return fail(SC_ERR_ARG, "null argument");
     Context* c = C(ctx);
@@ -684,6 +746,39 @@ int sc_screen_survivors(sc_context* ctx, int ntargets, const int* targets, long 
     if (!ctx || !count || cap < 0 || (cap > 0 && (!i || !j || !stage_b))) return fail(SC_ERR_ARG, "null argument");
     DeviceScope dev(C(ctx)->device);
     return screenSurvivors(C(ctx), targets ? ntargets : (int)C(ctx)->conf.p.size(), targets, cap, i, j, stage_b, count);
+}
+
+int sc_get_step_sizes(sc_context* ctx, sc_step_sizes* out) {
+    if (!ctx || !out) return fail(SC_ERR_ARG, "null argument");
+    Context* c = C(ctx);
+    initStepSizes(c);
+    std::memset(out, 0, sizeof *out);
+    for (int t = 0; t < MAXT && t < 40; ++t) {
+        out->trans[t] = c->trans[t].mx; out->rot_cos[t] = c->rot[t].mx;
+        out->acc_trans[t] = c->trans[t].acc; out->rej_trans[t] = c->trans[t].rej;
+        out->acc_rot[t] = c->rot[t].acc; out->rej_rot[t] = c->rot[t].rej;
+    }
+    for (int m = 0; m < Context::kMaxChainSteps && m < 8; ++m) {
+        out->chain_trans[m] = c->chainm[m].mx; out->chain_rot_cos[m] = c->chainr[m].mx;
+        out->acc_chain_trans[m] = c->chainm[m].acc; out->rej_chain_trans[m] = c->chainm[m].rej;
+        out->acc_chain_rot[m] = c->chainr[m].acc; out->rej_chain_rot[m] = c->chainr[m].rej;
+    }
+    out->edge = c->edge.mx;
+    out->acc_edge = c->edge.acc;
+    out->rej_edge = c->edge.rej;
+    out->adjustments = c->adjustments;
+    return SC_OK;
+}
+
+int sc_adjust_steps(sc_context* ctx) {
+    if (!ctx) return fail(SC_ERR_ARG, "null context");
+    return adjustSteps(C(ctx));
+}
+
+int sc_equilibrate(sc_context* ctx, const sc_run_params* p, long nequil, long adjust, sc_run_stats* stats) {
+    if (!ctx || !p || !stats) return fail(SC_ERR_ARG, "null argument");
+    DeviceScope dev(C(ctx)->device);
+    return equilibrate(C(ctx), *p, nequil, adjust, *stats);
 }
 
 int sc_tune(sc_context* ctx, const sc_run_params* p, int sweeps, sc_run_params* best, double* rates, int* ncand) {

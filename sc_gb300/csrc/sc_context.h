@@ -55,6 +55,15 @@ struct Context {
     SweepEngine* engine = nullptr;
     Batch* batch = nullptr;
     long lastLaunches = 0;     // kernels launched by the last move loop
+    // maximum steps the equilibration adapts (Updater::optimizeStep / optimizeRot, the Disp
+    // records of statistics.h:53-66): per particle type, per chain molecule type (the first
+    // kMaxChainSteps), and the box edge; the last run's acceptance counts feed them
+    struct Disp { double mx = 0.0, oldrmsd = 0.0, oldmx = 0.0; long acc = 0, rej = 0; };
+    static constexpr int kMaxChainSteps = 8;
+    bool stepsInit = false;
+    Disp trans[MAXT], rot[MAXT], chainm[kMaxChainSteps], chainr[kMaxChainSteps], edge;
+    double chainAdapted[kMaxChainSteps] = {0};   // chain displacement length per molecule type (0: options)
+    long adjustments = 0;
     // sc_tune's choice per mode (index: delayed 0 / 1): stencil reach and kernel variant
     // used by runs that pass variant = -1 (stencil 0 then takes the tuned reach too)
     int tunedStencil[2] = {0, 0};
@@ -105,6 +114,9 @@ float surrogateCutoff(const Surrogate* s);
 float surrogateRange(Context* c);
 int cudaFail(cudaError_t e, const char* where);
 int runSweeps(Context* c, const sc_run_params& p, sc_run_stats& st);
+int adjustSteps(Context* c);
+void initStepSizes(Context* c);      // the Disp records from the options (once)
+int equilibrate(Context* c, const sc_run_params& p, long nequil, long adjust, sc_run_stats& st);
 int tuneSweeps(Context* c, const sc_run_params& p, int sweeps, sc_run_params& best, double* rates, int* ncand);
 int screenSurvivors(Context* c, int ntargets, const int* targets, long cap, int* I, int* J, unsigned char* B,
                     long* count);

@@ -67,6 +67,9 @@ constexpr size_t kDynSmemSurrogate = kDynSmem + (size_t)kCandCap * 2 * sizeof(fl
 enum Ctr { C_ACC_T, C_REJ_T, C_ACC_R, C_REJ_R, C_ACC_V, C_REJ_V, C_VOL_CONSTR, C_TESTED, C_EVAL, C_CELL_REJ, C_MOVES,
            C_SCREENED, C_S1_REJ, C_S2_TRIED, C_S2_REJ, C_ACC_CH, C_REJ_CH, C_CH_CONSTR, C_COUNT };
 enum ErrBit { E_CELL_OVERFLOW = 1, E_PARTNER_FAR = 2, E_FLOW_WAIT = 4 };
+constexpr int kMaxChainTypes = 8;                         // chain molecule types with their own step
+constexpr int kTypeCtrChain = 4 * MAX_DEV_TYPES;
+constexpr int kTypeCtrCount = kTypeCtrChain + 4 * kMaxChainTypes;
 
 struct Grid {
     int nc[3];
@@ -140,7 +143,18 @@ struct SweepArgs {
     double boxMinChain[3];  // smallest box edges the chain grid allows (0: no chain phase)
     WlDev* wl;              // Wang-Landau bias (nullptr: none; only the particle grid's records)
     int flowSpin;           // dataflow sweep: polls of one wait before the CTA gives up
+    // per-type acceptance of the run (the reference's Disp counters, statistics.h:53-66):
+    // [4 t + 0..3] displacement acc / rej, rotation acc / rej of compact type t; then
+    // [kTypeCtrChain + 4 m + 0..3] chain displacement acc / rej, rotation acc / rej of molecule type m
+    unsigned long long* typeCtr;
+    double chainMxType[kMaxChainTypes];   // chain displacement length per molecule type
 };
+
+// One decided single-particle move of compact type `type` in the per-type counters.
+__device__ __forceinline__ void countMove(const SweepArgs& a, int type, bool displace, bool accept) {
+    if (a.typeCtr && type >= 0 && type < MAX_DEV_TYPES)
+        atomicAdd(&a.typeCtr[4 * type + (displace ? 0 : 2) + (accept ? 0 : 1)], 1ull);
+}
 
 __device__ __forceinline__ int wrapCell(double x, double shift, int nc) {
     double f = x - floor(x);
@@ -1085,6 +1099,7 @@ __device__ __forceinline__ void moveCell(const SweepArgs& a, int cx, int cy, int
         if (P0.skip) {
             if (tid == 0) {
                 if (P0.displace) { ++nRejT; ++nCellRej; } else ++nRejR;
+                countMove(a, P0.type, P0.displace, false);
                 if (WL) wlVisit(*a.wl);         // a rejected move visits the current bin
             }
             continue;
@@ -1148,7 +1163,7 @@ __device__ __forceinline__ void moveCell(const SweepArgs& a, int cx, int cy, int
             }
             bool pass = (dEs <= 0.0f) || ((double)dEs < P0.thrStage1);
             if (!pass) {
-                if (tid == 0) { ++nS1Rej; if (displace) ++nRejT; else ++nRejR; }
+                if (tid == 0) { ++nS1Rej; if (displace) ++nRejT; else ++nRejR; countMove(a, P0.type, displace, false); }
                 __syncthreads();
                 continue;
             }
@@ -1375,7 +1390,9 @@ __device__ __forceinline__ void moveCell(const SweepArgs& a, int cx, int cy, int
                         if (resident) candPat[sh.st.ownOff + P.slotR] = npd;
                     }
                     ++nAccR;
+                    countMove(a, P.type, false, true);
                 } else {
+                    countMove(a, P.type, true, true);
                     float4 nf = make_float4(P.newF.x, P.newF.y, P.newF.z, (float)P.type);
                     if (resident) candPos[sh.st.ownOff + P.slotR] = nf;
                     a.cellPosF[a.cellStart[cell] + P.slotR] = nf;
@@ -1393,6 +1410,7 @@ __device__ __forceinline__ void moveCell(const SweepArgs& a, int cx, int cy, int
                 invalidate(m, t);
             } else {
                 if (displace) ++nRejT; else ++nRejR;
+                countMove(a, P0.type, displace, false);
             }
             int done = 1;
             if (pair) {
@@ -1408,6 +1426,7 @@ __device__ __forceinline__ void moveCell(const SweepArgs& a, int cx, int cy, int
                     done = 2;
                     if (P1.skip) {
                         if (P1.displace) { ++nRejT; ++nCellRej; } else ++nRejR;
+                        countMove(a, P1.type, P1.displace, false);
                     } else {
                         nTested += (unsigned long long)nCand * (P1.displace ? 2 : 1);
                         evalMine += 2 * P1.nPartners;
@@ -1416,6 +1435,7 @@ __device__ __forceinline__ void moveCell(const SweepArgs& a, int cx, int cy, int
                             invalidate(m + 1, P1.target);
                         } else {
                             if (P1.displace) ++nRejT; else ++nRejR;
+                            countMove(a, P1.type, P1.displace, false);
                         }
                     }
                 }
@@ -1742,7 +1762,10 @@ __device__ bool warpMoveCell(const SweepArgs& a, WarpCell& W, int cx, int cy, in
         }
         const Proposal& P = W.prop;
         if (P.skip) {
-            if (lane == 0) { if (P.displace) { ++nRejT; ++nCellRej; } else ++nRejR; }
+            if (lane == 0) {
+                if (P.displace) { ++nRejT; ++nCellRej; } else ++nRejR;
+                countMove(a, P.type, P.displace, false);
+            }
             __syncwarp();
             continue;
         }
@@ -1832,6 +1855,7 @@ __device__ bool warpMoveCell(const SweepArgs& a, WarpCell& W, int cx, int cy, in
             } else {
                 if (displace) ++nRejT; else ++nRejR;
             }
+            countMove(a, P.type, displace, accept);
         }
         __syncwarp();               // the new state before the next proposal reads it
     }
@@ -2181,7 +2205,9 @@ __device__ void buildChainProposal(const SweepArgs& a, ChainShared& sh, int cell
     if (displace) {
         double x, y, z;
         randomUnitSphere(r, x, y, z);
-        dr[0] = x * a.chainMx / box.x; dr[1] = y * a.chainMx / box.y; dr[2] = z * a.chainMx / box.z;
+        const int mt = a.s.mol[first].x;
+        const double mx = mt < kMaxChainTypes ? a.chainMxType[mt] : a.chainMx;
+        dr[0] = x * mx / box.x; dr[1] = y * mx / box.y; dr[2] = z * mx / box.z;
     } else {
         double x, y, z;
         randomUnitSphere(r, x, y, z);
@@ -2428,6 +2454,9 @@ __device__ __forceinline__ void chainCell(const SweepArgs& a, int cx, int cy, in
             bool accept = (dE <= 0.0) || (dE < sh.thr);
             acceptS = accept;
             if (accept) { dECell += dE; ++nAcc; } else ++nRej;
+            const int mt = a.s.mol[first].x;
+            if (a.typeCtr && mt < kMaxChainTypes)
+                atomicAdd(&a.typeCtr[kTypeCtrChain + 4 * mt + (displace ? 0 : 2) + (accept ? 0 : 1)], 1ull);
         }
         __syncthreads();
         if (acceptS && tid < size) {
@@ -2776,6 +2805,7 @@ struct SweepEngine {
     int ncellsAlloc = 0;
     std::vector<void*> allocs;
     bool energyKnown = false;
+    unsigned long long* typeCtr = nullptr;        // per-type acceptance of the run (SweepArgs::typeCtr)
     uint64_t seed = ~0ull;
     int stencil = 0;
     double margin = 0.0;
@@ -2929,6 +2959,14 @@ static int ensureGrid(Context* c, SweepEngine* e, const double* box) {
     return SC_OK;
 }
 
+// Chain displacement length of molecule type m: the adapted step (sc_adjust_steps), scaled as
+// the run's chainmmx scales the options value, else the run's chainmmx.
+static double chainStep(const Context* c, int m, const sc_run_params& p) {
+    if (m < Context::kMaxChainSteps && c->chainAdapted[m] > 0.0 && c->opts.chainmmx > 0.0)
+        return c->chainAdapted[m] * (p.chainmmx / c->opts.chainmmx);
+    return p.chainmmx;
+}
+
 static void fillArgs(Context* c, SweepEngine* e, const sc_run_params& p) {
     SweepArgs& a = e->args;
     std::memset(&a, 0, sizeof a);
@@ -2964,6 +3002,8 @@ static void fillArgs(Context* c, SweepEngine* e, const sc_run_params& p) {
     }
     a.wl = wlDevice(c);
     a.flowSpin = p.flow_wait_polls > 0 ? p.flow_wait_polls : kFlowSpin;
+    a.typeCtr = e->typeCtr;
+    for (int m = 0; m < kMaxChainTypes; ++m) a.chainMxType[m] = chainStep(c, m, p);
 }
 
 // Chain phase of one system: chains (molecules of more than one particle), the bound R of
@@ -3010,9 +3050,11 @@ static int prepareChains(Context* c, SweepEngine* e, const sc_run_params& p, con
     float ext;
     std::memcpy(&ext, &bits, sizeof ext);
     C.R = std::max(1.2 * ext, ext + 0.5);
-    Grid g = makeGrid(box, c->topo.maxcut + 2.0 * (C.R + p.chainmmx), e->margin, 2);
+    double step = p.chainmmx;            // the longest chain displacement of any molecule type
+    for (int m = 0; m < kMaxChainTypes; ++m) step = std::max(step, chainStep(c, m, p));
+    Grid g = makeGrid(box, c->topo.maxcut + 2.0 * (C.R + step), e->margin, 2);
     if (g.ncolours > kMaxColours) return fail(SC_ERR_RANGE, "too many colour classes (chain grid)");
-    g.maxcut = c->topo.maxcut + 2.0 * (C.R + p.chainmmx);
+    g.maxcut = c->topo.maxcut + 2.0 * (C.R + step);
     if (g.ncells > C.ncellsAlloc) {
         for (void** q : {(void**)&C.cellStart, (void**)&C.cellCount, (void**)&C.cellCursor, (void**)&C.cellDE,
                          (void**)&C.chStart, (void**)&C.chCount, (void**)&C.cellDone}) {
@@ -3082,6 +3124,7 @@ static int prepareSystem(Context* c, const sc_run_params& p, bool npt) {
         if ((rc = engineAlloc(e, (void**)&e->cellOf, sizeof(int) * std::max(n, 1)))) return rc;
         if ((rc = engineAlloc(e, (void**)&e->counters, sizeof(unsigned long long) * C_COUNT))) return rc;
         if ((rc = engineAlloc(e, (void**)&e->err, sizeof(int)))) return rc;
+        if ((rc = engineAlloc(e, (void**)&e->typeCtr, sizeof(unsigned long long) * kTypeCtrCount))) return rc;
         Control z;
         std::memset(&z, 0, sizeof z);
         cudaMemcpy(e->ctl, &z, sizeof z, cudaMemcpyHostToDevice);
@@ -3103,6 +3146,7 @@ static int prepareSystem(Context* c, const sc_run_params& p, bool npt) {
     fillArgs(c, e, p);
     if ((rc = prepareChains(c, e, p, box))) return rc;
     cudaMemset(e->counters, 0, sizeof(unsigned long long) * C_COUNT);
+    cudaMemset(e->typeCtr, 0, sizeof(unsigned long long) * kTypeCtrCount);
     cudaMemset(e->err, 0, sizeof(int));
     cudaMemset(&e->ctl->maxDrift, 0, sizeof(double));
     cudaMemset(&e->ctl->daErr2, 0, 2 * sizeof(double));
@@ -3161,6 +3205,21 @@ static void collectStats(Context* c, sc_run_stats& st) {
     unsigned long long ctr[C_COUNT];
     Control hc;
     cudaMemcpy(ctr, e->counters, sizeof ctr, cudaMemcpyDeviceToHost);
+    // the run's acceptance per type into the Disp records (Updater::optimizeStep reads them)
+    unsigned long long tc[kTypeCtrCount];
+    cudaMemcpy(tc, e->typeCtr, sizeof tc, cudaMemcpyDeviceToHost);
+    for (int t = 0; t < MAXT; ++t) c->trans[t].acc = c->trans[t].rej = c->rot[t].acc = c->rot[t].rej = 0;
+    for (size_t k = 0; k < c->usedTypes.size() && k < (size_t)MAX_DEV_TYPES; ++k) {
+        const int t = c->usedTypes[k];
+        c->trans[t].acc = (long)tc[4 * k]; c->trans[t].rej = (long)tc[4 * k + 1];
+        c->rot[t].acc = (long)tc[4 * k + 2]; c->rot[t].rej = (long)tc[4 * k + 3];
+    }
+    for (int m = 0; m < kMaxChainTypes; ++m) {
+        c->chainm[m].acc = (long)tc[kTypeCtrChain + 4 * m]; c->chainm[m].rej = (long)tc[kTypeCtrChain + 4 * m + 1];
+        c->chainr[m].acc = (long)tc[kTypeCtrChain + 4 * m + 2]; c->chainr[m].rej = (long)tc[kTypeCtrChain + 4 * m + 3];
+    }
+    c->edge.acc = (long)ctr[C_ACC_V];
+    c->edge.rej = (long)ctr[C_REJ_V];
     cudaMemcpy(&hc, e->ctl, sizeof hc, cudaMemcpyDeviceToHost);
     st.moves = (long)ctr[C_MOVES];
     st.acc_trans = (long)ctr[C_ACC_T]; st.rej_trans = (long)ctr[C_REJ_T];
@@ -3612,6 +3671,133 @@ int screenSurvivors(Context* c, int ntargets, const int* targets, long cap, int*
     if (e != cudaSuccess) return cudaFail(e, "sc_screen_survivors");
     *count = (long)cnt;
     if ((long long)cnt > (long long)cap) return fail(SC_ERR_RANGE, "sc_screen_survivors: more survivors than cap");
+    return SC_OK;
+}
+
+// ---- step-size adaptation --------------------------------------------------------------
+// Updater::optimizeStep (scOOP/mc/updater.cpp:395-429): the change of the maximum step keeps
+// its direction while mx * acceptance grows and turns back when it falls; no accepted move
+// shrinks the step; bounds [lo, hi]; the counts restart.
+static void optimizeStep(Context::Disp& x, double hi, double lo) {
+    const double ratio = (x.acc + x.rej) > 0 ? (double)x.acc / (double)(x.acc + x.rej) : 0.0;
+    const double now = x.mx * ratio;
+    if (x.oldrmsd > 0) {
+        const bool worse = now < x.oldrmsd, grew = x.oldmx > 1;
+        if (worse == grew) { x.mx /= 1.05; x.oldmx = 0.95; }
+        else { x.mx *= 1.05; x.oldmx = 1.05; }
+    }
+    if (now > 0) {
+        x.oldrmsd = now;
+    } else {
+        x.oldrmsd = 0.0;
+        x.mx /= 1.05;
+        x.oldmx = 0.95;
+    }
+    if (x.mx > hi) x.mx = hi;
+    if (x.mx < lo) x.mx = lo;
+    x.acc = x.rej = 0;
+}
+
+// Updater::optimizeRot (updater.cpp:431-464): the same on cos(maximum angle), in 1 % steps
+// (mx is a cosine: a larger rotation is a smaller mx).
+static void optimizeRot(Context::Disp& x, double hi, double lo) {
+    const double ratio = (x.acc + x.rej) > 0 ? (double)x.acc / (double)(x.acc + x.rej) : 0.0;
+    const double now = x.mx * ratio;
+    if (x.oldrmsd > 0) {
+        const bool better = now > x.oldrmsd, grew = x.oldmx > 1;
+        if (better == grew) { x.mx *= 0.99; x.oldmx *= 0.99; }
+        else { x.mx *= 1.01; x.oldmx *= 1.01; }
+    }
+    if (now > 0) {
+        x.oldrmsd = now;
+    } else {
+        x.oldrmsd = 0.0;
+        x.mx *= 1.01;
+        x.oldmx = 1.01;
+    }
+    if (x.mx > hi) x.mx = hi;
+    if (x.mx < lo) x.mx = lo;
+    x.acc = x.rej = 0;
+}
+
+// The Disp records start from the options (Sim::readOptions, sim.h:359-373): displacement
+// per type, cos of the maximum rotation, chain steps, box edge range.
+void initStepSizes(Context* c) {
+    if (c->stepsInit) return;
+    const double pih = 1.57079632679489661923132169163975;
+    // (the acceptance counts of a run already made stay: they feed the first adjustment)
+    auto start = [](Context::Disp& d, double mx) { d.mx = mx; d.oldrmsd = 0.0; d.oldmx = 0.0; };
+    for (int t = 0; t < MAXT; ++t) {
+        start(c->trans[t], c->opts.trans_type[t]);
+        start(c->rot[t], cos(c->opts.rotmx_deg / 180.0 * pih));
+    }
+    for (int m = 0; m < Context::kMaxChainSteps; ++m) {
+        start(c->chainm[m], c->opts.chainmmx);
+        start(c->chainr[m], cos(c->opts.chainrmx_deg / 180.0 * pih));
+    }
+    start(c->edge, c->opts.edge_mx);
+    c->stepsInit = true;
+}
+
+// The adjustment block of Updater::simulate (updater.cpp:238-253) on the last run's counts:
+// optimizeStep on the displacement of every type and chain molecule type that moved (hi 1.5),
+// optimizeRot on their rotation records (5.0, 0.01), optimizeStep on the box edge (1.0).  The
+// adapted displacements and edge range take effect in later runs; as in the reference, whose
+// rotations read Disp::angle and not the adapted cosine, rotations keep the options' angle.
+int adjustSteps(Context* c) {
+    initStepSizes(c);
+    for (int t = 0; t < MAXT; ++t) {
+        if (c->trans[t].acc > 0 || c->trans[t].rej > 0) optimizeStep(c->trans[t], 1.5, 0.0);
+        if (c->rot[t].acc > 0 || c->rot[t].rej > 0) optimizeRot(c->rot[t], 5.0, 0.01);
+    }
+    for (int m = 0; m < Context::kMaxChainSteps; ++m) {
+        if (c->chainm[m].acc > 0 || c->chainm[m].rej > 0) optimizeStep(c->chainm[m], 1.5, 0.0);
+        if (c->chainr[m].acc > 0 || c->chainr[m].rej > 0) optimizeRot(c->chainr[m], 5.0, 0.01);
+    }
+    optimizeStep(c->edge, 1.0, 0.0);
+    for (int t = 0; t < MAXT; ++t) c->opts.trans_type[t] = c->trans[t].mx;
+    for (int m = 0; m < Context::kMaxChainSteps; ++m) c->chainAdapted[m] = c->chainm[m].mx;
+    c->opts.edge_mx = c->edge.mx;
+    ++c->adjustments;
+    return SC_OK;
+}
+
+// The equilibration of main.cpp:270-287: nequil/2 sweeps with the step adjustment every
+// `adjust` sweeps, then nequil/2 sweeps without.  Displacements follow the adapted per-type
+// steps; the box edge range is the adapted one.
+int equilibrate(Context* c, const sc_run_params& p, long nequil, long adjust, sc_run_stats& st) {
+    std::memset(&st, 0, sizeof st);
+    if (nequil < 0 || adjust < 0) return fail(SC_ERR_ARG, "sc_equilibrate: nequil and adjust must be >= 0");
+    initStepSizes(c);
+    const long half = nequil / 2;
+    sc_run_params q = p;
+    auto run = [&](long n) -> int {
+        q.nsweeps = n;
+        q.edge_mx = c->edge.mx;
+        sc_run_stats s1;
+        int rc = runSweeps(c, q, s1);
+        if (rc) return rc;
+        st.sweeps += s1.sweeps; st.moves += s1.moves;
+        st.acc_trans += s1.acc_trans; st.rej_trans += s1.rej_trans; st.acc_rot += s1.acc_rot; st.rej_rot += s1.rej_rot;
+        st.acc_vol += s1.acc_vol; st.rej_vol += s1.rej_vol; st.vol_constrained += s1.vol_constrained;
+        st.acc_chain += s1.acc_chain; st.rej_chain += s1.rej_chain;
+        st.pairs_tested += s1.pairs_tested; st.pairs_evaluated += s1.pairs_evaluated;
+        st.seconds += s1.seconds; st.launches += s1.launches;
+        st.energy = s1.energy; st.energy_check = s1.energy_check; st.max_drift = std::max(st.max_drift, s1.max_drift);
+        return SC_OK;
+    };
+    long done = 0;
+    while (done < half) {
+        const long blk = adjust > 0 ? std::min(adjust, half - done) : half - done;
+        int rc = run(blk);
+        if (rc) return rc;
+        done += blk;
+        if (adjust > 0 && blk == adjust) adjustSteps(c);     // at sweep == next_adjust
+    }
+    if (half > 0) {
+        int rc = run(half);
+        if (rc) return rc;
+    }
     return SC_OK;
 }
 

@@ -192,6 +192,13 @@ class System:
         L.check(self._lib.sc_default_run(self._h, C.byref(p)))
         return p
 
+    def nematic_order(self):
+        """(S2, director): the largest eigenvalue of the axes' Q tensor and its eigenvector."""
+        v = C.c_double()
+        d = np.zeros(3)
+        L.check(self._lib.sc_nematic_order(self._h, C.byref(v), _dptr(d)))
+        return v.value, d
+
     def screen_survivors(self, targets=None, cap=None):
         """The move kernels' candidate screens over every (target, particle) pair: (i, j,
         stage_b) of the pairs that pass stage A (see sc_screen_survivors)."""
@@ -206,6 +213,23 @@ class System:
                                               B.ctypes.data_as(C.POINTER(C.c_ubyte)), C.byref(cnt)))
         k = cnt.value
         return I[:k], J[:k], B[:k]
+
+    # --- equilibration (Updater::simulate's step adjustment, main.cpp:270-287) ----------------
+    def step_sizes(self):
+        st = L.StepSizes()
+        L.check(self._lib.sc_get_step_sizes(self._h, C.byref(st)))
+        return st
+
+    def adjust_steps(self):
+        L.check(self._lib.sc_adjust_steps(self._h))
+
+    def equilibrate(self, nequil, adjust, params=None, **overrides):
+        p = params if params is not None else self.default_run()
+        for k, v in overrides.items():
+            setattr(p, k, v)
+        st = L.RunStats()
+        L.check(self._lib.sc_equilibrate(self._h, C.byref(p), int(nequil), int(adjust), C.byref(st)))
+        return st
 
     def tune(self, params=None, sweeps=8, **overrides):
         """sc_tune: the fastest (stencil, variant) for params' mode on the current state (which

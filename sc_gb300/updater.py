@@ -34,14 +34,23 @@ def _frame(system, sweep):
     return "\n".join(lines) + "\n"
 
 
-def run(system, nsweeps, report=0, movie=0, directory=".", params=None, wl_file="wl-new.dat", **overrides):
+def run(system, nsweeps, report=0, movie=0, directory=".", params=None, wl_file="wl-new.dat", nequil=0, adjust=0,
+        **overrides):
     """Runs nsweeps sweeps on the GPU, writing energy.dat / stat.dat every `report` sweeps,
     movie frames every `movie` sweeps and config.last at the end (and, with Wang-Landau
-    weights, `wl_file`).  Returns the summed stats counters (moves, acceptances) of the
-    blocks and the sweeps run."""
+    weights, `wl_file`).  With nequil > 0 an equilibration comes first, as in main.cpp:270-287:
+    nequil/2 sweeps with the maximum steps adjusted every `adjust` sweeps, nequil/2 without,
+    then config.eq (Conf::draw with the box line).  Returns the summed stats counters (moves,
+    acceptances) of the production blocks and the sweeps run."""
     p = params if params is not None else system.default_run()
     for k, v in overrides.items():
         setattr(p, k, v)
+    eq_sweeps = 0
+    if nequil > 0:
+        est = system.equilibrate(nequil, adjust, params=p)
+        eq_sweeps = est.sweeps
+        system.write_config(os.path.join(directory, "config.eq"))
+        p.edge_mx = system.default_run().edge_mx       # the adapted box edge range
     ef = os.path.join(directory, "energy.dat")
     sf = os.path.join(directory, "stat.dat")
     mf = os.path.join(directory, "movie")
@@ -85,4 +94,5 @@ def run(system, nsweeps, report=0, movie=0, directory=".", params=None, wl_file=
     if wl:
         system.wl_end(wf)
     totals["sweeps"] = sweep
+    totals["equilibration_sweeps"] = eq_sweeps
     return totals

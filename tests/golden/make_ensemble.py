@@ -98,6 +98,36 @@ def cases():
                   pairlist_update=10),
         nsweeps=30000, report=20, seeds=6, burn=5000)
     assert float(lip_opts["chainprob"]) == 0.2
+    # the benchmark's own state points: 1000 PSC at packing fraction 0.1, T = 1 (NVT), and the
+    # CPSC + SPA mixture at P* = 0.5, T = 1 (NPT, isotropic volume moves), reduced to 500
+    # particles; the nematic order S2 from the reference's own movie frames
+    for name, texts, nsw, burn in (("psc_c0", workloads.nvt_psc(1000, phi=0.1, seed=1), 8000, 2000),
+                                   ("mixture_c1", workloads.npt_cpsc_spa(500, phi=0.1, seed=1), 12000, 3000)):
+        opts_text, top, config = texts
+        base = dict(l.split(" = ") for l in opts_text.strip().splitlines())
+        base.update(pairlist_update="10", nequil="0")
+        out[name] = dict(top=top, config=config, opts=base, nsweeps=nsw, report=20, seeds=6, burn=burn, s2=True)
+    return out
+
+
+def nematic_s2(dirs):
+    """Largest eigenvalue of <3/2 u u^T - 1/2 I> over unit axes (rows of dirs)."""
+    q = 1.5 * (dirs.T @ dirs) / len(dirs) - 0.5 * np.eye(3)
+    return float(np.linalg.eigvalsh(q)[-1])
+
+
+def movie_s2(path, sc_rows):
+    """S2 of every frame of the reference's movie file (frames: count line, 'sweep S; box ...'
+    line, then one 'x y z dx dy dz px py pz switched molType' line per particle)."""
+    lines = open(path).read().splitlines()
+    out, k = [], 0
+    while k < len(lines):
+        n = int(lines[k].split()[0])
+        sweep = int(lines[k + 1].split(";")[0].split()[1])
+        rows = lines[k + 2: k + 2 + n]
+        dirs = np.array([[float(x) for x in r.split()[3:6]] for r in rows])[sc_rows]
+        out.append((sweep, nematic_s2(dirs)))
+        k += 2 + n
     return out
 
 
@@ -106,6 +136,8 @@ def run_one(c, seed):
         opts = dict(OPTION_KEYS)
         opts.update(c["opts"])
         opts.update(nsweeps=c["nsweeps"], report=c["report"], seed=seed, paraltemper=opts["temper"])
+        if c.get("s2"):
+            opts.update(movie=c["report"])
         with open(os.path.join(tmp, "options"), "w") as f:
             f.write("".join(f"{k} = {v}\n" for k, v in opts.items()))
         with open(os.path.join(tmp, "top.init"), "w") as f:
@@ -125,7 +157,11 @@ def run_one(c, seed):
                 continue
             sw, v = line.split(";")
             vol.append((int(sw), float(v)))
-        return dict(seed=seed, energy=e, volume=vol)
+        s2 = []
+        if c.get("s2"):
+            n_sc = int(c["top"].split("[System]")[1].split()[1])     # the first [System] entry: the SCs
+            s2 = movie_s2(os.path.join(tmp, "movie"), slice(0, n_sc))
+        return dict(seed=seed, energy=e, volume=vol, s2=s2)
 
 
 def block_stats(series_per_seed, burn):
@@ -150,9 +186,10 @@ def main():
         e_ser = [[(s, en / n) for s, en, _ in r["energy"]] for r in runs]
         a_ser = [[(s, al / n) for s, _, al in r["energy"]] for r in runs]
         v_ser = [[(s, v / n) for s, v in r["volume"]] for r in runs]
-        stats = {k: block_stats(ser, c["burn"]) for k, ser in (("energy_per_particle", e_ser),
-                                                              ("alignment_per_particle", a_ser),
-                                                              ("volume_per_particle", v_ser))}
+        series = [("energy_per_particle", e_ser), ("alignment_per_particle", a_ser), ("volume_per_particle", v_ser)]
+        if c.get("s2"):
+            series.append(("nematic_s2", [r["s2"] for r in runs]))
+        stats = {k: block_stats(ser, c["burn"]) for k, ser in series}
         out = dict(name=name, n=n, inputs={"top.init": c["top"], "config.init": c["config"]}, options=c["opts"],
                    nsweeps=c["nsweeps"], report=c["report"], burn=c["burn"], seeds=c["seeds"],
                    stats={k: {"mean": m, "se": s} for k, (m, s) in stats.items()})

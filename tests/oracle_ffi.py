@@ -111,6 +111,8 @@ def _bind(L):
         L.or_wl_orders.argtypes = [C.POINTER(System), C.POINTER(C.c_int), C.POINTER(C.c_double),
                                    C.POINTER(C.c_double), C.POINTER(C.c_long), C.POINTER(C.c_double),
                                    C.POINTER(C.c_double)]
+        L.or_nematic.restype = C.c_int
+        L.or_nematic.argtypes = [C.POINTER(System), C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.or_pair_energies.restype = None
         L.or_pair_energies.argtypes = [C.POINTER(System), C.c_long, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                        C.POINTER(C.c_double), C.POINTER(C.c_uint), C.POINTER(C.c_double)]
@@ -434,6 +436,13 @@ class TextSystem:
 
     def one_to_all(self, t):
         return lib().or_one_to_all(C.byref(self.sys), int(t))
+
+    def nematic(self):
+        """(S2, director) of the oracle (or_nematic)."""
+        v = C.c_double()
+        d = (C.c_double * 3)()
+        lib().or_nematic(C.byref(self.sys), C.byref(v), d)
+        return v.value, np.array(d[:])
 
     def set_state(self, parts, box):
         """Takes a configuration from the GPU path (sc_particle records and box edges)."""

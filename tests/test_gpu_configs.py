@@ -106,3 +106,13 @@ def test_candidate_screens_cover_the_prefilter(moved):
     Ed, _, _ = ts.pair_energies(Ia[drop], Ja[drop])
     bonded = _bonded(ts, Ia[drop], Ja[drop])
     assert np.all(Ed[~bonded] == 0.0), (name, int(np.sum(Ed[~bonded] != 0.0)))
+
+
+def test_nematic_order_matches_oracle(moved):
+    """S2 and the director of the moved benchmark state: the GPU's fixed-order reduction and
+    the oracle's sums agree to rounding."""
+    name, s, ts, targets, _ = moved
+    s2, d = s.nematic_order()
+    s2o, do = ts.nematic()
+    assert abs(s2 - s2o) <= 1e-12, (name, s2, s2o)
+    assert abs(abs(float(np.dot(d, do))) - 1.0) <= 1e-9 or s2 < 1e-3, (name, d, do)
