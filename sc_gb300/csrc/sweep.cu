@@ -148,6 +148,8 @@ struct SweepArgs {
     // [kTypeCtrChain + 4 m + 0..3] chain displacement acc / rej, rotation acc / rej of molecule type m
     unsigned long long* typeCtr;
     double chainMxType[kMaxChainTypes];   // chain displacement length per molecule type
+    double coneAngle;       // options coneAngle (radians): rotations about axes in a cone around the
+                            // particle axis (MoveCreator::partAxialRotate); 0: about random axes
 };
 
 // One decided single-particle move of compact type `type` in the per-type counters.
@@ -732,7 +734,33 @@ __device__ void buildProposal(const SweepArgs& a, const int* list, const int* nb
     } else {
         double angle = a.rotAngle * r.next();
         double ax, ay, az;
-        randomUnitSphere(r, ax, ay, az);
+        if (a.coneAngle != 0.0) {
+            // MoveCreator::partAxialRotate (movecreator.cpp:1030-1073): the axis is
+            // Vector::getRandomUnitConeUniform(dir, coneAngle) (Vector.h:294-308) -- a vector
+            // orthogonal to dir (getOrthogonalVector, :256-260) turned about dir by a random angle
+            // (getRandomOrthogonalVector, :268-277, Vector::rotate, :138-160), mixed with dir so
+            // that the axis' component along dir is uniform in [cos(coneAngle), 1]
+            double ox = -d.y, oy = d.x, oz = 0.0;
+            if (d.x == 0.0 && d.y == 0.0) { ox = 0.0; oy = 1.0; oz = 0.0; }
+            const double cr = cos(r.next() * 2.0 * 3.141592653589793238462643383279);
+            const double sr = sqrt(1.0 - cr * cr);
+            const double qx = d.x * sr, qy = d.y * sr, qz = d.z * sr;
+            const double t2 = cr * qx, t3 = cr * qy, t4 = cr * qz, t5 = -qx * qx, t6 = qx * qy, t7 = qx * qz,
+                         t8 = -qy * qy, t9 = qy * qz, t10 = -qz * qz;
+            const double rx = 2.0 * ((t8 + t10) * ox + (t6 - t4) * oy + (t3 + t7) * oz) + ox;
+            const double ry = 2.0 * ((t4 + t6) * ox + (t5 + t10) * oy + (t9 - t2) * oz) + oy;
+            const double rz = 2.0 * ((t7 - t3) * ox + (t2 + t9) * oy + (t5 + t8) * oz) + oz;
+            const double cosA = cos(a.coneAngle);
+            const double mult = r.next() * (1.0 - cosA) + cosA;
+            const double dl = 1.0 / sqrt(d.x * d.x + d.y * d.y + d.z * d.z);
+            const double ol = 1.0 / sqrt(rx * rx + ry * ry + rz * rz);
+            const double side = sqrt(1.0 - mult * mult);
+            ax = d.x * dl * mult + side * (rx * ol);
+            ay = d.y * dl * mult + side * (ry * ol);
+            az = d.z * dl * mult + side * (rz * ol);
+        } else {
+            randomUnitSphere(r, ax, ay, az);
+        }
         bool positive = r.next() < 0.5;
         double vc = cos(angle);
         double vs = positive ? sqrt(1.0 - vc * vc) : -sqrt(1.0 - vc * vc);
@@ -760,7 +788,7 @@ __device__ void buildProposal(const SweepArgs& a, const int* list, const int* nb
         }
         double dx = __shfl_sync(0xffffffffu, v[0], 0), dy = __shfl_sync(0xffffffffu, v[1], 0),
                dz = __shfl_sync(0xffffffffu, v[2], 0);
-        if (lane == 1) {
+        if (lane == 1 && a.coneAngle == 0.0) {      // partRotate re-orthogonalises, partAxialRotate does not
             double dp = v[0] * dx + v[1] * dy + v[2] * dz;
             v[0] -= dp * dx; v[1] -= dp * dy; v[2] -= dp * dz;
         }
@@ -3003,6 +3031,7 @@ static void fillArgs(Context* c, SweepEngine* e, const sc_run_params& p) {
     a.wl = wlDevice(c);
     a.flowSpin = p.flow_wait_polls > 0 ? p.flow_wait_polls : kFlowSpin;
     a.typeCtr = e->typeCtr;
+    a.coneAngle = c->opts.coneAngle;
     for (int m = 0; m < kMaxChainTypes; ++m) a.chainMxType[m] = chainStep(c, m, p);
 }
 
@@ -3562,10 +3591,7 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
 
 // Moves of the options that the GPU loop does not make.
 static int checkMoves(const Context* c) {
-    if (c->opts.coneAngle != 0.0)
-        return fail(SC_ERR_UNSUPPORTED, "options coneAngle != 0: rotations about axes in a cone around the particle "
-                                        "axis (MoveCreator::partAxialRotate, movecreator.cpp:1030-1073) are not on "
-                                        "the GPU path");
+    (void)c;
     return SC_OK;
 }
 

@@ -1,0 +1,48 @@
+"""Run device sweeps of a seeded benchmark system with a chosen launch shape.
+
+    python -m sc_gb300.run_sweeps --workload psc_cpsc --n 16384 --variant 8 --stencil 1 \\
+        --warmup 2 --sweeps 1
+
+Prints one JSON line (moves/s of the timed sweeps, device time, launches).  The launch
+shape is fixed by the arguments (no tuner), so that a profiler can select the move kernel's
+launches by name and position: with --warmup W the timed sweeps' move launches come after
+W launches of the same kernel.
+"""
+import argparse
+import json
+
+from . import System, workloads
+
+BUILDERS = {
+    "psc_cpsc": lambda n, seed: workloads.psc_cpsc(n, phi=0.2, seed=seed),
+    "npt_cpsc_spa": lambda n, seed: workloads.npt_cpsc_spa(n, seed=seed),
+    "nvt_psc": lambda n, seed: workloads.nvt_psc(n, seed=seed),
+    "bilayers": lambda n, seed: workloads.bilayers(max(1, int(round((n / 12) ** 0.5))), seed=seed),
+}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="psc_cpsc", choices=sorted(BUILDERS))
+    ap.add_argument("--n", type=int, default=16384)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--variant", type=int, default=4)
+    ap.add_argument("--stencil", type=int, default=0)
+    ap.add_argument("--warmup", type=int, default=2)
+    ap.add_argument("--sweeps", type=int, default=1)
+    a = ap.parse_args()
+    s = System.from_text(*BUILDERS[a.workload](a.n, a.seed))
+    p = s.default_run()
+    p.check_every = 0
+    p.variant, p.stencil, p.seed = a.variant, a.stencil, a.seed
+    for _ in range(a.warmup):
+        s.simulate(p, nsweeps=1)
+    st = s.simulate(p, nsweeps=a.sweeps)
+    print(json.dumps({"workload": a.workload, "n": s.n, "variant": a.variant, "stencil": a.stencil,
+                      "sweeps": a.sweeps, "moves_per_s": st.moves / max(st.seconds, 1e-12), "seconds": st.seconds,
+                      "launches": st.launches, "phase_launches": st.phase_launches}))
+    s.close()
+
+
+if __name__ == "__main__":
+    main()

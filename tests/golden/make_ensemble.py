@@ -101,13 +101,38 @@ def cases():
     # the benchmark's own state points: 1000 PSC at packing fraction 0.1, T = 1 (NVT), and the
     # CPSC + SPA mixture at P* = 0.5, T = 1 (NPT, isotropic volume moves), reduced to 500
     # particles; the nematic order S2 from the reference's own movie frames
-    for name, texts, nsw, burn in (("psc_c0", workloads.nvt_psc(1000, phi=0.1, seed=1), 8000, 2000),
-                                   ("mixture_c1", workloads.npt_cpsc_spa(500, phi=0.1, seed=1), 12000, 3000)):
+    # the first case with axial rotations (partAxialRotate: rotation axes in a cone of 40 degrees
+    # around the particle axis), S2 and the alignment order
+    out["psc_cone"] = dict(out["psc_nvt"], opts=dict(out["psc_nvt"]["opts"], coneAngle=40.0), s2=True)
+    # Both start from one configuration the reference itself has equilibrated (`pre` sweeps from
+    # the seeded start): the patchy particles keep aggregating slowly from a random start, and
+    # averages over a relaxing window would depend on each sampler's kinetics.
+    for name, texts, pre, nsw, burn in (("psc_c0", workloads.nvt_psc(1000, phi=0.1, seed=1), 30000, 8000, 1000),
+                                        ("mixture_c1", workloads.npt_cpsc_spa(500, phi=0.1, seed=1), 60000, 12000,
+                                         2000)):
         opts_text, top, config = texts
         base = dict(l.split(" = ") for l in opts_text.strip().splitlines())
         base.update(pairlist_update="10", nequil="0")
-        out[name] = dict(top=top, config=config, opts=base, nsweeps=nsw, report=20, seeds=6, burn=burn, s2=True)
+        out[name] = dict(top=top, config=config, opts=base, nsweeps=nsw, report=20, seeds=6, burn=burn, s2=True,
+                         pre=pre)
     return out
+
+
+def pre_equilibrate(c, seed=999):
+    """config.last of one reference run of c["pre"] sweeps from c's start (its box and lines,
+    which the config.init reader takes as they are)."""
+    with tempfile.TemporaryDirectory() as tmp:
+        opts = dict(OPTION_KEYS)
+        opts.update(c["opts"])
+        opts.update(nsweeps=c["pre"], report=c["pre"], seed=seed, paraltemper=opts["temper"], movie=0)
+        with open(os.path.join(tmp, "options"), "w") as f:
+            f.write("".join(f"{k} = {v}\n" for k, v in opts.items()))
+        with open(os.path.join(tmp, "top.init"), "w") as f:
+            f.write(c["top"])
+        with open(os.path.join(tmp, "config.init"), "w") as f:
+            f.write(c["config"])
+        subprocess.run([SC_REF], cwd=tmp, check=True, capture_output=True)
+        return open(os.path.join(tmp, "config.last")).read()
 
 
 def nematic_s2(dirs):
@@ -178,6 +203,8 @@ def main():
     for name, c in cases().items():
         if only and name not in only:
             continue
+        if c.get("pre"):
+            c["config"] = pre_equilibrate(c)
         with ThreadPoolExecutor(max_workers=min(8, c["seeds"])) as ex:
             runs = list(ex.map(lambda s: run_one(c, s), [1000 + k for k in range(c["seeds"])]))
         n = c.get("n_particles") or sum(

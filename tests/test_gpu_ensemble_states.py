@@ -26,7 +26,12 @@ def ens(name):
 
 
 def _opts(d):
-    return "".join(f"{k} = {v}\n" for k, v in d.items())
+    from golden.make_golden import OPTION_KEYS
+
+    o = dict(OPTION_KEYS)
+    o.update(d)
+    o["paraltemper"] = o["temper"]
+    return "".join(f"{k} = {v}\n" for k, v in o.items())
 
 
 def mean_se(series):
@@ -45,7 +50,7 @@ def sample(systems, g, seed, delayed=0):
     p.check_every = 0
     p.delayed = delayed
     rep, burn, nsw = g["report"], g["burn"], g["nsweeps"]
-    E, S, V = ([[] for _ in systems] for _ in range(3))
+    E, S, V, A = ([[] for _ in systems] for _ in range(4))
     done = 0
     while done < nsw:
         _, _, en, _, _ = R.run(rep, exchange_every=0, seed=seed, params=p)
@@ -55,9 +60,10 @@ def sample(systems, g, seed, delayed=0):
                 E[k].append(en[k] / s.n)
                 S[k].append(s.nematic_order()[0])
                 V[k].append(float(np.prod(s.box)) / s.n)
+                A[k].append(s.alignment_order() / s.n)
     R.close()
     return {"energy_per_particle": [np.array(x) for x in E], "nematic_s2": [np.array(x) for x in S],
-            "volume_per_particle": [np.array(x) for x in V]}
+            "volume_per_particle": [np.array(x) for x in V], "alignment_per_particle": [np.array(x) for x in A]}
 
 
 def check(g, got, keys):
@@ -116,3 +122,17 @@ def test_delayed_acceptance_matches_reference_at_benchmark_state(name):
         s.close()
     sur.close()
     train.close()
+
+
+def test_axial_rotations_match_reference():
+    """Rotations about axes in a 40-degree cone around the particle axis (options coneAngle,
+    MoveCreator::partAxialRotate) sample the reference's ensemble: 250 PSC at T = 0.6."""
+    from sc_gb300 import System
+
+    g = ens("psc_cone")
+    systems = [System.from_text(_opts(g["options"]), g["inputs"]["top.init"], g["inputs"]["config.init"])
+               for _ in range(6)]
+    got = sample(systems, g, seed=777)
+    check(g, got, ["energy_per_particle", "nematic_s2", "alignment_per_particle"])
+    for s in systems:
+        s.close()

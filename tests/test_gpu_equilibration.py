@@ -113,18 +113,30 @@ def test_adjusted_steps_follow_the_reference_rule():
 
 
 def test_equilibration_then_production_writes_config_eq(tmp_path):
-    """main.cpp:270-297 through the output loop: nequil sweeps (adjusting every `adjust`
-    sweeps in the first half), config.eq, then the production run."""
+    """main.cpp:270-297 through the output loop: nequil/2 sweeps adjusting every `adjust`
+    sweeps, nequil/2 without, config.eq, then the production run.  The same sequence done by
+    hand (sc_simulate blocks and sc_adjust_steps) on an identical system and seed ends with
+    the same steps and the same state."""
     from sc_gb300 import System, updater, workloads
 
-    s = System.from_text(*workloads.nvt_psc(300, phi=0.15, seed=4))
-    before = s.step_sizes().trans[1]
+    texts = workloads.nvt_psc(300, phi=0.15, seed=4)
+    s = System.from_text(*texts)
     tot = updater.run(s, 40, report=20, directory=str(tmp_path), nequil=60, adjust=10, seed=3)
     assert tot["sweeps"] == 40 and tot["equilibration_sweeps"] == 60
     eq = (tmp_path / "config.eq").read_text().splitlines()
     assert len(eq) == 1 + s.n and len(eq[1].split()) == 11
     a = s.step_sizes()
-    assert a.adjustments == 3 and a.trans[1] != before
+    assert a.adjustments == 3
     last = (tmp_path / "config.last").read_text().splitlines()
     assert len(last) == 1 + s.n and last != eq
+    h = System.from_text(*texts)
+    for _ in range(3):
+        h.simulate(nsweeps=10, seed=3, check_every=100)
+        h.adjust_steps()
+    h.simulate(nsweeps=30, seed=3, check_every=100)
+    b = h.step_sizes()
+    assert b.adjustments == 3 and list(b.trans) == list(a.trans) and list(b.rot_cos) == list(a.rot_cos)
+    h.write_config(str(tmp_path / "by_hand.eq"))
+    assert (tmp_path / "by_hand.eq").read_text().splitlines() == eq
     s.close()
+    h.close()

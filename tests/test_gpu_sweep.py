@@ -378,3 +378,25 @@ def test_warp_cells_follow_the_cta_kernel(name):
         # the golden starts hold overlap energies up to 1e16, whose rounding the two summation
         # orders carry differently; on clean starts the running energies agree closely
         assert abs(a[0].energy - b[0].energy) <= 1e-11 * max(1.0, abs(a[0].energy))
+
+
+def test_axial_rotations_turn_about_the_particle_axis():
+    """options coneAngle > 0 (MoveCreator::partAxialRotate): rotation axes lie in a cone of that
+    angle around the particle's own axis.  With a cone of 1e-4 degrees the axes barely move
+    while the patches turn freely, and the running energy stays exact."""
+    from sc_gb300 import System, workloads
+
+    opts, top, cfg = workloads.nvt_psc(200, phi=0.1, seed=9)
+    opts = opts.replace("transmx = 0.4", "transmx = 0.05") + "coneAngle = 0.0001\n"
+    s = System.from_text(opts, top, cfg)
+    before = s.particles()
+    st = s.simulate(nsweeps=20, seed=5, check_every=0)
+    after = s.particles()
+    dd = max(max(abs(a.dir[k] - b.dir[k]) for k in range(3)) for a, b in zip(after, before))
+    dp = max(max(abs(a.patchdir[0][k] - b.patchdir[0][k]) for k in range(3)) for a, b in zip(after, before))
+    assert st.acc_rot > 100
+    assert dd < 1e-4, dd
+    assert dp > 0.1, dp
+    exact = s.all_to_all()
+    assert abs(st.energy - exact) <= 1e-9 * max(1.0, abs(exact))
+    s.close()
