@@ -101,16 +101,15 @@ def test_options_errors_are_reported_not_fatal(lib):
 
 
 def test_moves_outside_the_gpu_loop_are_refused(lib):
-    # options coneAngle != 0 asks for MoveCreator::partAxialRotate (movecreator.cpp:1030-1073):
-    # the move loop refuses before touching the device
+    # the warp-per-cell kernel (variant bit 3) runs plain moves only: delayed acceptance with it
+    # is refused before the device is touched
     from sc_gb300 import ScError, System
 
     g = goldens.load(NAMES[0])["inputs"]
-    opts = g["options"] + "coneAngle = 10.0\n"
-    s = System.from_text(opts, g["top.init"], g["config.init"])
+    s = System.from_text(g["options"], g["top.init"], g["config.init"])
     with pytest.raises(ScError) as ei:
-        s.simulate(nsweeps=1)
-    assert ei.value.code == -7 and "coneAngle" in str(ei.value)
+        s.simulate(nsweeps=1, variant=8, delayed=1)
+    assert ei.value.code == -7 and "plain moves" in str(ei.value)
     s.close()
 
 
