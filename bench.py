@@ -649,7 +649,7 @@ def roofline(tot, variant, workload, peaks, peak_kind, fp64):
     t_launch = tot["phase_s"] / n
     bytes_per_launch = (tot["tested"] * 28 + tot["evaluated"] * 120) / n
     achieved = bytes_per_launch / t_launch / 1e9 if t_launch > 0 else None
-    kernel = KERNELS[int(variant) & 7]
+    kernel = ("kCellWarpsFlowDense" if variant & 1 else "kCellWarpsFlow") if variant & 8 else KERNELS[int(variant) & 7]
     roof = {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
             "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
             "traffic": profiled_traffic(kernel, workload),

@@ -103,7 +103,8 @@ def cases():
     # particles; the nematic order S2 from the reference's own movie frames
     # the first case with axial rotations (partAxialRotate: rotation axes in a cone of 40 degrees
     # around the particle axis), S2 and the alignment order
-    out["psc_cone"] = dict(out["psc_nvt"], opts=dict(out["psc_nvt"]["opts"], coneAngle=40.0), s2=True)
+    out["psc_cone"] = dict(out["psc_nvt"], opts=dict(out["psc_nvt"]["opts"], coneAngle=40.0), s2=True, pre=20000,
+                           burn=2000)
     # Both start from one configuration the reference itself has equilibrated (`pre` sweeps from
     # the seeded start): the patchy particles keep aggregating slowly from a random start, and
     # averages over a relaxing window would depend on each sampler's kinetics.
