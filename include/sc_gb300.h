@@ -96,6 +96,12 @@ typedef struct {
     int flow_wait_polls;    /* dataflow sweep: polls of one wait for a neighbouring cell before the
                                kernel gives up and the call returns SC_ERR_DEVICE (0: 2^19, about
                                0.2 s; a wait in a sound run lasts well under 20 ms) */
+    int grand_every;        /* sweeps between grand-canonical insert / delete moves (options
+                               nGrandCanon; MoveCreator::muVTMove, movecreator.cpp:797-924); 0: none.
+                               Needs top.init ACTIVITY species; sc_simulate / sc_equilibrate only */
+    long sweep_offset;      /* sweeps the caller's loop ran before this call: a move due every
+                               grand_every sweeps follows sweep k of the loop when k % grand_every
+                               == 0 (updater.cpp:165), k counted from the loop's start */
 } sc_run_params;
 
 typedef struct {
@@ -119,7 +125,24 @@ typedef struct {
     long da_stage2_rejected;
     double da_err_rms;       /* rms of dE - dEs over the moves that reached the exact stage */
     double da_err_mean;      /* mean of dE - dEs over the same moves */
+    /* grand-canonical moves (grand_every > 0), all species together */
+    long acc_insert, rej_insert, acc_delete, rej_delete;
+    long particles;          /* particle count after the call */
 } sc_run_stats;
+
+/* Record of one grand-canonical species (Statistics::grand, scOOP/structures/statistics.h;
+ * printed by Updater::simulate, updater.cpp:358-373), summed over every run of the context. */
+typedef struct {
+    int mol_type;            /* molecule type (order of [Molecules]) */
+    int type;                /* its particle type */
+    int count;               /* molecules of it now */
+    int pad_;
+    double activity;         /* top.init ACTIVITY */
+    double chem_pot;         /* log(activity Nav 1e-24) (inicializer.cpp:1094) */
+    long steps;              /* muVtSteps: moves that drew this species */
+    long ins_acc, ins_rej, del_acc, del_rej;
+    double average_particles;   /* muVtAverageParticles / muVtSteps: mean count after its moves */
+} sc_grand_stats;
 
 const char* sc_last_error(void);
 const char* sc_version(void);
@@ -205,6 +228,17 @@ int sc_default_run(const sc_context* ctx, sc_run_params* p);
 /* Runs p->nsweeps sweeps on the device; stats->sweeps is the number run (fewer when a
  * Wang-Landau run converged, as the reference's loop stops there, updater.cpp:255-265). */
 int sc_simulate(sc_context* ctx, const sc_run_params* p, sc_run_stats* stats);
+/* Grand-canonical species (molecule types with a top.init ACTIVITY; options nGrandCanon must
+ * be > 0 then, and the species single particles listed after every chain type): *count gets
+ * their number.  sc_grand_stats_get fills species k's record (0 <= k < count).  With
+ * grand_every > 0 the particle count changes on the device: sc_num_particles and
+ * sc_get_particles see the new vector after the call, which keeps the reference's order
+ * (an insertion at the end of its species' block, a deletion closing its slot). */
+int sc_grand_species(const sc_context* ctx, int* count);
+int sc_grand_stats_get(const sc_context* ctx, int k, sc_grand_stats* out);
+/* top.last (main.cpp:313-331): the context's top.init text up to and including its [System]
+ * line, then "name count" for every molecule type with the current counts. */
+int sc_write_top_last(sc_context* ctx, const char* path);
 
 /* --- equilibration: adaptation of the maximum steps (Updater::simulate's adjustment block,
  * scOOP/mc/updater.cpp:238-253, with optimizeStep / optimizeRot, updater.cpp:395-464, and

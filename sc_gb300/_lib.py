@@ -52,7 +52,8 @@ class RunParams(C.Structure):
                 ("ptype", C.c_int), ("volume_every", C.c_int), ("transmx", C.c_double), ("rot_angle", C.c_double),
                 ("edge_mx", C.c_double), ("chainprob", C.c_double), ("chainmmx", C.c_double),
                 ("chain_angle", C.c_double), ("check_every", C.c_int), ("time_phases", C.c_int),
-                ("stencil", C.c_int), ("delayed", C.c_int), ("variant", C.c_int), ("flow_wait_polls", C.c_int)]
+                ("stencil", C.c_int), ("delayed", C.c_int), ("variant", C.c_int), ("flow_wait_polls", C.c_int),
+                ("grand_every", C.c_int), ("sweep_offset", C.c_long)]
 
 
 class RunStats(C.Structure):
@@ -62,7 +63,15 @@ class RunStats(C.Structure):
         (k, C.c_double) for k in ("energy", "energy_check", "max_drift", "seconds", "phase_seconds")] + [
         ("phase_launches", C.c_long), ("launches", C.c_long),
         ("da_stage1_rejected", C.c_long), ("da_stage2_tried", C.c_long), ("da_stage2_rejected", C.c_long),
-        ("da_err_rms", C.c_double), ("da_err_mean", C.c_double)]
+        ("da_err_rms", C.c_double), ("da_err_mean", C.c_double)] + [
+        (k, C.c_long) for k in ("acc_insert", "rej_insert", "acc_delete", "rej_delete", "particles")]
+
+
+class GrandStats(C.Structure):
+    _fields_ = [("mol_type", C.c_int), ("type", C.c_int), ("count", C.c_int), ("pad_", C.c_int),
+                ("activity", C.c_double), ("chem_pot", C.c_double)] + [
+        (k, C.c_long) for k in ("steps", "ins_acc", "ins_rej", "del_acc", "del_rej")] + [
+        ("average_particles", C.c_double)]
 
 
 class TrainParams(C.Structure):
@@ -114,6 +123,9 @@ SIGNATURES = [
     ("sc_trial_volume", C.c_int, [_P, C.c_double, _D]),
     ("sc_default_run", C.c_int, [_P, C.POINTER(RunParams)]),
     ("sc_simulate", C.c_int, [_P, C.POINTER(RunParams), C.POINTER(RunStats)]),
+    ("sc_grand_species", C.c_int, [_P, _I]),
+    ("sc_grand_stats_get", C.c_int, [_P, C.c_int, C.POINTER(GrandStats)]),
+    ("sc_write_top_last", C.c_int, [_P, C.c_char_p]),
     ("sc_nematic_order", C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("sc_get_step_sizes", C.c_int, [_P, C.c_void_p]),
     ("sc_adjust_steps", C.c_int, [_P]),

@@ -127,6 +127,44 @@ int Context::setup(std::string& err) {
         mols.push_back(mp);
     }
     if (mols.empty()) { MolParam z; std::memset(&z, 0, sizeof z); z.size = 1; mols.push_back(z); }
+    rebuildMolInfo();
+    // grand-canonical species (inicializer.cpp:36-47, 1087-1096; main.cpp:104-108, 128-139)
+    grand.clear();
+    int firstGrand = -1;
+    for (size_t m = 0; m < topo.mols.size(); ++m) {
+        if (topo.mols[m].activity == -1.0) continue;
+        if (opts.nGrandCanon == 0) { err = "Activity stated in top.init, But nGrandCanon=0 in options"; return SC_ERR_PARSE; }
+        if (topo.mols[m].types.size() != 1) {
+            err = "grand-canonical insertion of chains draws from a [Pool] configuration, which is outside the GPU path";
+            return SC_ERR_UNSUPPORTED;
+        }
+        Grand g;
+        g.molType = (int)m;
+        g.type = topo.mols[m].types[0];
+        g.activity = topo.mols[m].activity;
+        g.chemPot = std::log(g.activity * 6.022137e23 * 1e-24);   // Nav of inicializer.cpp:934
+        grand.push_back(g);
+        if (firstGrand < 0) firstGrand = (int)m;
+    }
+    if (opts.nGrandCanon != 0 && grand.empty()) {
+        err = "In options nGrandCanon != 0, but no activity set for any species in top.init";
+        return SC_ERR_PARSE;
+    }
+    if ((int)grand.size() > kMaxGrandSpecies) { err = "more than 8 grand-canonical species"; return SC_ERR_RANGE; }
+    // an insertion or deletion moves the particles behind it by one slot: only single
+    // particles may sit there (no bond partner index changes)
+    for (size_t m = firstGrand < 0 ? topo.mols.size() : (size_t)firstGrand; m < topo.mols.size(); ++m)
+        if (topo.mols[m].types.size() != 1) {
+            err = "the molecule types from the first grand-canonical species on must be single particles "
+                  "(list the grand-canonical species last)";
+            return SC_ERR_UNSUPPORTED;
+        }
+    return SC_OK;
+}
+
+// Molecule record of every particle: its type, position in the molecule, the molecule's
+// size and first particle (ParticleVector::first and the molecule sizes).
+void Context::rebuildMolInfo() {
     molInfo.resize(conf.p.size());
     for (size_t i = 0; i < conf.p.size(); ++i) {
         int m = conf.p[i].molType;
@@ -134,7 +172,6 @@ int Context::setup(std::string& err) {
         int pos = ((int)i - conf.first[m]) % size;
         molInfo[i] = make_int4(m, pos, size, (int)i - pos);
     }
-    return SC_OK;
 }
 
 int Context::ensureDevice() {
@@ -152,19 +189,23 @@ int Context::ensureDevice() {
         int n = (int)conf.p.size();
         int T = (int)usedTypes.size();
         int rc;
-        if ((rc = allocDev((void**)&d.pos, sizeof(double4_32a) * n))) return rc;
-        if ((rc = allocDev((void**)&d.dir, sizeof(double4_32a) * n))) return rc;
-        if ((rc = allocDev((void**)&d.patch, sizeof(PatchSet) * n))) return rc;
-        if ((rc = allocDev((void**)&d.mol, sizeof(int4) * n))) return rc;
+        // grand-canonical systems keep free slots for insertions (grown on demand by the
+        // move loop, Context::grow)
+        cap = grand.empty() ? n : n + std::max(256, n / 2);
+        const size_t slots = (size_t)std::max(cap, 1);
+        if ((rc = allocDev((void**)&d.pos, sizeof(double4_32a) * slots))) return rc;
+        if ((rc = allocDev((void**)&d.dir, sizeof(double4_32a) * slots))) return rc;
+        if ((rc = allocDev((void**)&d.patch, sizeof(PatchSet) * slots))) return rc;
+        if ((rc = allocDev((void**)&d.mol, sizeof(int4) * slots))) return rc;
         if ((rc = allocDev((void**)&d.box, sizeof(double) * 4))) return rc;
         if ((rc = allocDev((void**)&dParams, sizeof(PairParam) * T * T))) return rc;
         if ((rc = allocDev((void**)&dMols, sizeof(MolParam) * mols.size()))) return rc;
         if ((rc = allocDev((void**)&dTrial, sizeof(TrialSlot)))) return rc;
         if ((rc = allocDev((void**)&dScalars, sizeof(double) * 64))) return rc;
-        nPartial = allToAllBlocks(n) + 1;
+        nPartial = allToAllBlocks((int)slots) + 1;
         if ((rc = allocDev((void**)&dPartial, sizeof(double) * nPartial))) return rc;
         d.n = n;
-        e = cudaMallocHost(&hostStage, (sizeof(double4_32a) * 2 + sizeof(PatchSet)) * std::max(n, 1) + 64);
+        e = cudaMallocHost(&hostStage, (sizeof(double4_32a) * 2 + sizeof(PatchSet)) * slots + 64);
         if (e != cudaSuccess) { hostStage = nullptr; return cudaFail(e, "cudaMallocHost (state staging)"); }
         std::vector<PairParam> hp(T * T);
         for (int a = 0; a < T; ++a)
@@ -189,8 +230,53 @@ int Context::ensureDevice() {
     return SC_OK;
 }
 
+// Moves the device state into arrays of newCap slots, keeping the first d.n particles (the
+// grand-canonical moves fill the free slots; the caller has synchronised the stream).
+int Context::grow(int newCap) {
+    if (newCap <= cap) return SC_OK;
+    DeviceScope dev(device);
+    const size_t slots = (size_t)newCap;
+    const size_t n = (size_t)d.n;
+    auto replace = [&](void** p, size_t elem) -> int {
+        void* q = nullptr;
+        int rc = allocDev(&q, elem * slots);
+        if (rc) return rc;
+        cudaError_t e = cudaMemcpy(q, *p, elem * n, cudaMemcpyDeviceToDevice);
+        if (e != cudaSuccess) return cudaFail(e, "grow state");
+        cudaFree(*p);
+        allocations.erase(std::find(allocations.begin(), allocations.end(), *p));
+        *p = q;
+        return SC_OK;
+    };
+    int rc;
+    if ((rc = replace((void**)&d.pos, sizeof(double4_32a)))) return rc;
+    if ((rc = replace((void**)&d.dir, sizeof(double4_32a)))) return rc;
+    if ((rc = replace((void**)&d.patch, sizeof(PatchSet)))) return rc;
+    if ((rc = replace((void**)&d.mol, sizeof(int4)))) return rc;
+    const int np = allToAllBlocks(newCap) + 1;
+    if (np > nPartial) {
+        cudaFree(dPartial);
+        allocations.erase(std::find(allocations.begin(), allocations.end(), (void*)dPartial));
+        dPartial = nullptr;
+        if ((rc = allocDev((void**)&dPartial, sizeof(double) * np))) return rc;
+        nPartial = np;
+    }
+    void* stage = nullptr;
+    cudaError_t e = cudaMallocHost(&stage, (sizeof(double4_32a) * 2 + sizeof(PatchSet)) * slots + 64);
+    if (e != cudaSuccess) return cudaFail(e, "cudaMallocHost (state staging)");
+    cudaFreeHost(hostStage);
+    hostStage = stage;
+    cap = newCap;
+    return SC_OK;
+}
+
 int Context::uploadState() {
     int n = (int)conf.p.size();
+    if (n > cap) {                 // a grand-canonical vector longer than the slots
+        int rc = grow(n + std::max(256, n / 2));
+        if (rc) return rc;
+    }
+    d.n = n;
     // the state goes through one pinned staging block, so the copies are true DMA
     double* box = (double*)hostStage;
     double4_32a* hp = (double4_32a*)((char*)hostStage + 64);
@@ -207,6 +293,10 @@ int Context::uploadState() {
     }
     box[0] = conf.box.x; box[1] = conf.box.y; box[2] = conf.box.z; box[3] = 0.0;
     cudaError_t e;
+    // grand-canonical moves reorder the molecule records on the device: the host's go up too
+    if (!grand.empty() && n > 0 &&
+        (e = cudaMemcpyAsync(d.mol, molInfo.data(), sizeof(int4) * n, cudaMemcpyHostToDevice, stream)) != cudaSuccess)
+        return cudaFail(e, "upload molecule records");
     if ((e = cudaMemcpyAsync(d.pos, hp, sizeof(double4_32a) * n, cudaMemcpyHostToDevice, stream)) != cudaSuccess) return cudaFail(e, "upload pos");
     if ((e = cudaMemcpyAsync(d.dir, hd, sizeof(double4_32a) * n, cudaMemcpyHostToDevice, stream)) != cudaSuccess) return cudaFail(e, "upload dir");
     if ((e = cudaMemcpyAsync(d.patch, hs, sizeof(PatchSet) * n, cudaMemcpyHostToDevice, stream)) != cudaSuccess) return cudaFail(e, "upload patch");
@@ -234,6 +324,8 @@ int Context::downloadState() {
         Particle& p = conf.p[i];
         p.pos = {hp[i].x, hp[i].y, hp[i].z};
         p.dir = {hd[i].x, hd[i].y, hd[i].z};
+        const int ct = (int)hp[i].w;      // compact type (inserted particles take their species')
+        if (ct >= 0 && ct < (int)usedTypes.size()) p.type = usedTypes[ct];
         const PatchSet& s = hs[i];
         for (int k = 0; k < 2; ++k) p.pd[k] = {s.pd[k][0], s.pd[k][1], s.pd[k][2]};
         for (int k = 0; k < 4; ++k) p.ps[k] = {s.ps[k][0], s.ps[k][1], s.ps[k][2]};
@@ -264,6 +356,7 @@ int initContext(Context* c, const std::string& opt, const std::string& top, cons
     int rc;
     if (readOptionsText(opt, c->opts, err)) return fail(SC_ERR_PARSE, err);
     if (readTopologyText(top, c->topo, err)) return fail(err.find("outside") != std::string::npos ? SC_ERR_UNSUPPORTED : SC_ERR_PARSE, err);
+    c->topText = top;
     if (buildParticles(c->topo, c->conf, err)) return fail(SC_ERR_PARSE, err);
     if (readConfigText(cfg, c->topo, c->conf, err)) return fail(err.find("outside") != std::string::npos ? SC_ERR_UNSUPPORTED : SC_ERR_PARSE, err);
     partVecInit(c->topo, c->conf);
@@ -732,6 +825,60 @@ int sc_default_run(const sc_context* ctx, sc_run_params* p) {
     p->chain_angle = o.chain_angle;
     p->check_every = 100;
     p->variant = -1;       // sc_tune's choice for this context, else the dataflow sweep
+    p->grand_every = (int)o.nGrandCanon;
+    return SC_OK;
+}
+
+int sc_grand_species(const sc_context* ctx, int* count) {
+    if (!ctx || !count) return fail(SC_ERR_ARG, "null argument");
+    *count = (int)C(ctx)->grand.size();
+    return SC_OK;
+}
+
+int sc_write_top_last(sc_context* ctx, const char* path) {
+    if (!ctx || !path) return fail(SC_ERR_ARG, "null argument");
+    const Context* c = C(ctx);
+    std::string out;
+    size_t pos = 0;
+    bool seen = false;
+    while (pos < c->topText.size() && !seen) {
+        size_t e = c->topText.find('\n', pos);
+        std::string line = c->topText.substr(pos, e == std::string::npos ? std::string::npos : e - pos + 1);
+        pos = e == std::string::npos ? c->topText.size() : e + 1;
+        out += line;
+        if (line.compare(0, 8, "[System]") == 0) seen = true;
+    }
+    if (!seen) return fail(SC_ERR_STATE, "Error writing Topology [System] not found");
+    if (!out.empty() && out.back() != '\n') out += '\n';
+    for (int m = 0; m < c->conf.molTypeCount; ++m) {
+        const int size = std::max(1, (int)c->topo.mols[m].types.size());
+        char buf[256];
+        std::snprintf(buf, sizeof buf, "%s %d\n", c->topo.mols[m].name.c_str(),
+                      (c->conf.first[m + 1] - c->conf.first[m]) / size);
+        out += buf;
+    }
+    FILE* f = std::fopen(path, "w");
+    if (!f) return fail(SC_ERR_IO, std::string("cannot write ") + path);
+    std::fwrite(out.data(), 1, out.size(), f);
+    std::fclose(f);
+    return SC_OK;
+}
+
+int sc_grand_stats_get(const sc_context* ctx, int k, sc_grand_stats* out) {
+    if (!ctx || !out) return fail(SC_ERR_ARG, "null argument");
+    const Context* c = C(ctx);
+    if (k < 0 || k >= (int)c->grand.size()) return fail(SC_ERR_ARG, "grand-canonical species index out of range");
+    const Context::Grand& g = c->grand[k];
+    std::memset(out, 0, sizeof *out);
+    out->mol_type = g.molType;
+    out->type = g.type;
+    out->count = c->conf.first[g.molType + 1] - c->conf.first[g.molType];
+    out->activity = g.activity;
+    out->chem_pot = g.chemPot;
+    out->steps = g.steps;
+    out->ins_acc = g.insAcc; out->ins_rej = g.insRej;
+    out->del_acc = g.delAcc; out->del_rej = g.delRej;
+    out->average_particles = g.steps > 0 ? g.countSum / (double)g.steps : 0.0;
     return SC_OK;
 }
 

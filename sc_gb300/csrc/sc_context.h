@@ -19,9 +19,12 @@ struct MlpPacked;     // surrogate.cuh: its BF16 weights in mma fragment order
 struct WlHost;        // wanglandau.cu: Wang-Landau weights and histogram
 struct WlDev;         // wanglandau.h: their device record
 
+constexpr int kMaxGrandSpecies = 8;
+
 struct Context {
     Options opts;
     Topology topo;
+    std::string topText;       // the top.init text the context was opened with (top.last)
     Config conf;
     std::vector<MolParam> mols;
     std::vector<int4> molInfo;
@@ -68,6 +71,17 @@ struct Context {
     // used by runs that pass variant = -1 (stencil 0 then takes the tuned reach too)
     int tunedStencil[2] = {0, 0};
     int tunedVariant[2] = {-1, -1};
+    // grand-canonical species: the molecule types with an ACTIVITY (MoleculeParams::activity,
+    // chemPot; moleculeparams.h:43-52), in molecule-type order, with the acceptance record of
+    // Statistics::grand (steps, insertions, deletions, the sum of counts after each step)
+    struct Grand {
+        int molType = 0, type = 0;
+        double activity = -1.0, chemPot = -1.0;
+        long steps = 0, insAcc = 0, insRej = 0, delAcc = 0, delRej = 0;
+        double countSum = 0.0;
+    };
+    std::vector<Grand> grand;
+    int cap = 0;              // particle slots of the device state arrays (>= the particle count)
 
     Context() = default;
     Context(const Context&) = delete;
@@ -75,10 +89,12 @@ struct Context {
     ~Context();
 
     int setup(std::string& err);
+    void rebuildMolInfo();
     int ensureDevice();
     int uploadState();
     int downloadState();
     int allocDev(void** p, size_t bytes);
+    int grow(int newCap);     // state arrays of newCap slots, keeping the first d.n particles
     int scratch(size_t bytes);
     void freeDevice();
     PairParam devParam(int t1, int t2) const;

@@ -212,8 +212,11 @@ int fillMolLine(MolType& m, const std::string& cmdIn, const std::string& params,
     if (cmd == "ANGLE1") { if (!two("angle1")) return -1; m.angle1c = k; m.angle1eq = eq * kDEGTORAD; return 0; }
     if (cmd == "ANGLE2") { if (!two("angle2")) return -1; m.angle2c = k; m.angle2eq = eq * kDEGTORAD; return 0; }
     if (cmd == "ACTIVITY") {
-        err = "top.init: ACTIVITY (grand-canonical insertion) is outside the GPU hot path";
-        return -1;
+        // inicializer.cpp:1087-1096; the options' nGrandCanon is checked against it once
+        // both files are read (Context::setup), chemPot = log(activity Nav 1e-24) there
+        if (w.empty() || !parseDouble(w[0], k)) { err = "top.init: could not read the activity"; return -1; }
+        m.activity = k;
+        return 0;
     }
     err = "top.init: unknown molecule parameter: " + cmd;
     return -1;

@@ -66,7 +66,7 @@ constexpr size_t kDynSmemSurrogate = kDynSmem + (size_t)kCandCap * 2 * sizeof(fl
 
 enum Ctr { C_ACC_T, C_REJ_T, C_ACC_R, C_REJ_R, C_ACC_V, C_REJ_V, C_VOL_CONSTR, C_TESTED, C_EVAL, C_CELL_REJ, C_MOVES,
            C_SCREENED, C_S1_REJ, C_S2_TRIED, C_S2_REJ, C_ACC_CH, C_REJ_CH, C_CH_CONSTR, C_COUNT };
-enum ErrBit { E_CELL_OVERFLOW = 1, E_PARTNER_FAR = 2, E_FLOW_WAIT = 4 };
+enum ErrBit { E_CELL_OVERFLOW = 1, E_PARTNER_FAR = 2, E_FLOW_WAIT = 4, E_GC_FULL = 8 };
 constexpr int kMaxChainTypes = 8;                         // chain molecule types with their own step
 constexpr int kTypeCtrChain = 4 * MAX_DEV_TYPES;
 constexpr int kTypeCtrCount = kTypeCtrChain + 4 * kMaxChainTypes;
@@ -98,6 +98,8 @@ struct Control {
     unsigned epoch;       // sweeps begun, never reset (stamps of the dataflow sweep's cells)
     int ticket;           // next cell of the dataflow sweep
 };
+
+struct GcDev;   // grand-canonical species and their record (kGrandCanon)
 
 struct SweepArgs {
     DevState s;
@@ -150,6 +152,8 @@ struct SweepArgs {
     double chainMxType[kMaxChainTypes];   // chain displacement length per molecule type
     double coneAngle;       // options coneAngle (radians): rotations about axes in a cone around the
                             // particle axis (MoveCreator::partAxialRotate); 0: about random axes
+    GcDev* gc;              // grand-canonical moves of the run (nullptr: none); kGrandCanon writes
+                            // the particle count s.n of these records
 };
 
 // One decided single-particle move of compact type `type` in the per-type counters.
@@ -2815,6 +2819,282 @@ __global__ void kExchange(SweepArgs* A, SweepArgs* AC, int* ladder, const int* l
     }
 }
 
+
+// ---- grand-canonical moves -----------------------------------------------------------------
+// MoveCreator::muVTMove (scOOP/mc/movecreator.cpp:797-924), one move every nGrandCanon sweeps
+// (updater.cpp:164-179).  A species is drawn among the grand-canonical ones (getRandomMuVTType,
+// :926-945).  With probability 1/2 a particle of it is inserted at a uniform position
+// (Cuboid::randomPos, geometry.h:130-132) with a uniform axis and patch direction
+// (Vector::randomUnitSphere, Vector.h:190-205) put through Particle::init (particle.cpp:3-79),
+// and kept if V/(N+1) exp(chemPot - E/T) > u; otherwise a uniformly chosen particle of it is
+// removed if N/V exp(E/T - chemPot) > u (nothing to remove: rejected).  E is the particle's
+// energy against every other particle with an empty conlist (TotalE::mol2others,
+// totalenergycalculator.h:211-228).  An insertion takes slot first[m+1], the end of the
+// species' block (ParticleVector::insertMolecule, Conf.h:267-275); a removal closes its slot
+// (removeMolecule, :277-289): the particles behind move by one slot, so the particle order is
+// the reference's.  Only single particles sit behind the first species (Context::setup), so no
+// bond partner index changes.
+//
+// One CTA per system: thread 0 draws the move, every thread sums a strided share of E (fixed
+// reduction order), the CTA moves the tail, and the new count goes into the system's device
+// arguments (and the chain phase's), which the next sweep's kernels read.
+
+constexpr int kGcThreads = 256;
+
+struct GcSpecies {
+    int molType;          // molecule type (index of ParticleVector::first)
+    int ctype;            // compact type of its particle
+    int geo;              // geotype[0] of the particle type
+    int pad_;
+    double chemPot;       // log(activity Nav 1e-24), inicializer.cpp:1094
+    double pcos0, psin0, pcos2, psin2;   // pcoshalfi / psinhalfi of patches 0 and 2
+    double csec, ssec;                   // csecpatchrot[0], ssecpatchrot[0]
+    double chcos, chsin;                 // chiral_cos[0], chiral_sin[0]
+};
+
+struct GcDev {
+    int nSpecies;
+    int molTypeCount;
+    int cap;              // particle slots of the state arrays (the host keeps one free per move)
+    int pad_;
+    double chainprob;     // chain moves per particle move: the chain phase's share follows N
+    GcSpecies sp[kMaxGrandSpecies];
+    int first[MAXMT + 1];                             // ParticleVector::first, kept current
+    unsigned long long ctr[kMaxGrandSpecies][5];      // steps, insert acc / rej, delete acc / rej
+    double countSum[kMaxGrandSpecies];                // Statistics::grand muVtAverageParticles
+};
+
+// Vector::rotate(axis, cos, sin) (Vector.h:133-157): v turned about a unit axis.
+__device__ __forceinline__ void gcRotate(double (&v)[3], const double (&ax)[3], double c, double s) {
+    const double qw = c, qx = ax[0] * s, qy = ax[1] * s, qz = ax[2] * s;
+    const double t2 = qw * qx, t3 = qw * qy, t4 = qw * qz, t5 = -qx * qx, t6 = qx * qy, t7 = qx * qz, t8 = -qy * qy,
+                 t9 = qy * qz, t10 = -qz * qz;
+    const double x = v[0], y = v[1], z = v[2];
+    v[0] = 2.0 * ((t8 + t10) * x + (t6 - t4) * y + (t3 + t7) * z) + x;
+    v[1] = 2.0 * ((t4 + t6) * x + (t5 + t10) * y + (t9 - t2) * z) + y;
+    v[2] = 2.0 * ((t7 - t3) * x + (t2 + t9) * y + (t5 + t8) * z) + z;
+}
+__device__ __forceinline__ void gcNormalise(double (&v)[3]) {
+    double t = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    if (t != 0.0) { t = 1.0 / t; v[0] *= t; v[1] *= t; v[2] *= t; }
+}
+__device__ __forceinline__ void gcOrthogonalise(double (&v)[3], const double (&b)[3]) {
+    const double dp = v[0] * b[0] + v[1] * b[1] + v[2] * b[2];
+    v[0] -= dp * b[0]; v[1] -= dp * b[1]; v[2] -= dp * b[2];
+}
+__device__ __forceinline__ void gcCopy(double (&d)[3], const double (&s)[3]) { d[0] = s[0]; d[1] = s[1]; d[2] = s[2]; }
+
+// Particle::init (particle.cpp:3-79) of an inserted particle: dir and P.pd[0] hold the drawn
+// axis and patch direction; the patch sides (and chiral axes) follow from them.
+__device__ void gcInitParticle(const GcSpecies& g, double (&dir)[3], PatchSet& P) {
+    const int geo = g.geo;
+    if (geo == SCA || geo == SCN) return;
+    gcNormalise(dir);
+    gcOrthogonalise(P.pd[0], dir);
+    gcNormalise(P.pd[0]);
+    if (geo == PSC || geo == CPSC || geo == TPSC || geo == TCPSC) {
+        gcCopy(P.ps[0], P.pd[0]); gcRotate(P.ps[0], dir, g.pcos0, g.psin0);
+        gcCopy(P.ps[1], P.pd[0]); gcRotate(P.ps[1], dir, g.pcos0, -1.0 * g.psin0);
+    }
+    if (isTwoPatch(geo)) {
+        gcCopy(P.pd[1], P.pd[0]);
+        gcRotate(P.pd[1], dir, g.csec, g.ssec);
+        gcOrthogonalise(P.pd[1], dir);
+        gcNormalise(P.pd[1]);
+    }
+    if (geo == TPSC || geo == TCPSC) {
+        gcCopy(P.ps[2], P.pd[1]); gcRotate(P.ps[2], dir, g.pcos2, g.psin2);
+        gcCopy(P.ps[3], P.pd[1]); gcRotate(P.ps[3], dir, g.pcos2, -1.0 * g.psin2);
+    }
+    if (isChiral(geo)) {
+        gcCopy(P.ch[0], dir); gcRotate(P.ch[0], P.pd[0], g.chcos, g.chsin);
+        gcCopy(P.ps[0], P.pd[0]); gcRotate(P.ps[0], P.ch[0], g.pcos0, g.psin0);
+        gcCopy(P.ps[1], P.pd[0]); gcRotate(P.ps[1], P.ch[0], g.pcos0, -1.0 * g.psin0);
+    }
+    if (geo == TCHPSC || geo == TCHCPSC) {
+        gcCopy(P.ch[1], dir); gcRotate(P.ch[1], P.pd[1], g.chcos, g.chsin);
+        gcCopy(P.ps[2], P.pd[1]); gcRotate(P.ps[2], P.ch[1], g.pcos2, g.psin2);
+        gcCopy(P.ps[3], P.pd[1]); gcRotate(P.ps[3], P.ch[1], g.pcos2, -1.0 * g.psin2);
+    }
+}
+
+// Moves particle slot `from` to slot `to` (the state arrays and the molecule record, whose
+// first-particle field is the slot itself for the single particles that move).
+struct GcSlot {
+    double4_32a pos, dir;
+    PatchSet patch;
+    int4 mol;
+};
+__device__ __forceinline__ void gcLoad(const DevState& s, int i, GcSlot& v) {
+    v.pos = s.pos[i];
+    v.dir = s.dir[i];
+    v.patch = s.patch[i];
+    v.mol = s.mol[i];
+}
+__device__ __forceinline__ void gcStore(const DevState& s, int i, const GcSlot& v) {
+    s.pos[i] = v.pos;
+    s.dir[i] = v.dir;
+    s.patch[i] = v.patch;
+    int4 m = v.mol;
+    m.w = i;
+    s.mol[i] = m;
+}
+
+__global__ void __launch_bounds__(kGcThreads) kGrandCanon(SweepArgs* A, SweepArgs* AC) {
+    SweepArgs& a = A[blockIdx.y];
+    if (!a.gc || blockIdx.x != 0) return;
+    GcDev& g = *a.gc;
+    Control& ctl = *a.ctl;
+    __shared__ int sSpecies, sInsert, sSlot, sCount, sSkip, sAccept;
+    __shared__ double sU, sPos[3], sDir[3];
+    __shared__ PatchSet sPatch;
+    __shared__ double sWarp[kGcThreads / 32];
+    const int n = a.s.n;
+    if (threadIdx.x == 0) {
+        Stream r(a.seed ^ 0xA0761D6478BD642Full, 0xFFFFFFE8u, (uint32_t)ctl.sweep, (uint32_t)(ctl.sweep >> 32));
+        const int k = min((int)(r.next() * g.nSpecies), g.nSpecies - 1);
+        const GcSpecies& sp = g.sp[k];
+        const int count = g.first[sp.molType + 1] - g.first[sp.molType];
+        sSpecies = k;
+        sCount = count;
+        sSkip = 0;
+        sInsert = r.next() > 0.5 ? 1 : 0;
+        if (sInsert) {
+            for (int d = 0; d < 3; ++d) sPos[d] = r.next();
+            double dir[3], pd[3];
+            randomUnitSphere(r, dir[0], dir[1], dir[2]);
+            randomUnitSphere(r, pd[0], pd[1], pd[2]);
+            PatchSet P;
+            for (int q = 0; q < 3; ++q) {
+                P.pd[0][q] = pd[q]; P.pd[1][q] = 0.0;
+                for (int w = 0; w < 4; ++w) P.ps[w][q] = 0.0;
+                P.ch[0][q] = 0.0; P.ch[1][q] = 0.0;
+            }
+            gcInitParticle(sp, dir, P);
+            for (int d = 0; d < 3; ++d) sDir[d] = dir[d];
+            sPatch = P;
+            sSlot = g.first[sp.molType + 1];
+            if (n >= g.cap) {             // the host keeps a free slot before every move
+                atomicOr(a.err, E_GC_FULL);
+                sSkip = 2;
+            }
+        } else if (count == 0) {
+            sSkip = 1;                    // nothing to remove (movecreator.cpp:882-886)
+        } else {
+            sSlot = g.first[sp.molType] + min((int)(r.next() * count), count - 1);
+        }
+        sU = r.next();
+    }
+    __syncthreads();
+    const int k = sSpecies;
+    const GcSpecies& sp = g.sp[k];
+    if (sSkip) {
+        if (threadIdx.x == 0 && sSkip == 1) {
+            g.ctr[k][0] += 1ull;
+            g.ctr[k][4] += 1ull;
+            g.countSum[k] += (double)sCount;
+        }
+        return;
+    }
+    DevCtx c;
+    c.params = a.t.params; c.mols = a.t.mols; c.ntypes = a.t.ntypes; c.n = n; c.sqmaxcut = a.t.sqmaxcut;
+    const double3 box = mk(a.s.box[0], a.s.box[1], a.s.box[2]);
+    const bool insert = sInsert != 0;
+    const int slot = sSlot;
+    PView me;
+    if (insert) {
+        me.pos = mk(sPos[0], sPos[1], sPos[2]);
+        me.dir = mk(sDir[0], sDir[1], sDir[2]);
+        me.patch = &sPatch;
+        me.type = sp.ctype;
+        me.index = -1;
+        me.molType = sp.molType;
+    } else {
+        const double4_32a p = a.s.pos[slot], d = a.s.dir[slot];
+        me.pos = mk(p.x, p.y, p.z);
+        me.dir = mk(d.x, d.y, d.z);
+        me.patch = &a.s.patch[slot];
+        me.type = (int)p.w;
+        me.index = slot;
+        me.molType = a.s.mol[slot].x;
+    }
+    const Con con = emptyCon(c);
+    double e = 0.0;
+    for (int j = threadIdx.x; j < n; j += kGcThreads) {
+        if (!insert && j == slot) continue;
+        const double4_32a p = a.s.pos[j], d = a.s.dir[j];
+        PView b;
+        b.pos = mk(p.x, p.y, p.z);
+        b.dir = mk(d.x, d.y, d.z);
+        b.patch = &a.s.patch[j];
+        b.type = (int)p.w;
+        b.index = j;
+        b.molType = a.s.mol[j].x;
+        unsigned bits;
+        double dsq;
+        e += pairEnergy(c, me, b, con, box, &bits, &dsq);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
+    if ((threadIdx.x & 31) == 0) sWarp[threadIdx.x >> 5] = e;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double E = 0.0;
+        for (int w = 0; w < kGcThreads / 32; ++w) E += sWarp[w];
+        const double V = box.x * box.y * box.z;
+        const int count = sCount;
+        bool acc;
+        if (insert) acc = (V / (count + 1.0)) * exp(sp.chemPot - E / a.temper) > sU;
+        else acc = ((double)count / V) * exp(E / a.temper - sp.chemPot) > sU;
+        g.ctr[k][0] += 1ull;
+        g.ctr[k][insert ? (acc ? 1 : 2) : (acc ? 3 : 4)] += 1ull;
+        g.countSum[k] += (double)(acc ? (insert ? count + 1 : count - 1) : count);
+        if (acc) ctl.energy += insert ? E : -1.0 * E;
+        sAccept = acc ? 1 : 0;
+    }
+    __syncthreads();
+    if (!sAccept) return;
+    GcSlot v;
+    if (insert) {
+        // the tail [slot, n) moves up by one, highest chunk first: a chunk reads all its slots
+        // before any thread writes, and writes only slots the chunks below do not read
+        for (int hi = n; hi > slot; hi -= kGcThreads) {
+            const int lo = max(slot, hi - kGcThreads);
+            const int i = lo + (int)threadIdx.x;
+            if (i < hi) gcLoad(a.s, i, v);
+            __syncthreads();
+            if (i < hi) gcStore(a.s, i + 1, v);
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            v.pos = make_double4_32a(sPos[0], sPos[1], sPos[2], (double)sp.ctype);
+            v.dir = make_double4_32a(sDir[0], sDir[1], sDir[2], 0.0);
+            v.patch = sPatch;
+            v.mol = make_int4(sp.molType, 0, 1, slot);
+            gcStore(a.s, slot, v);
+        }
+    } else {
+        // the tail (slot, n) moves down by one, lowest chunk first
+        for (int lo = slot + 1; lo < n; lo += kGcThreads) {
+            const int i = lo + (int)threadIdx.x;
+            if (i < n) gcLoad(a.s, i, v);
+            __syncthreads();
+            if (i < n) gcStore(a.s, i - 1, v);
+            __syncthreads();
+        }
+    }
+    if (threadIdx.x == 0) {
+        const int dn = insert ? 1 : -1;
+        for (int m = sp.molType + 1; m <= g.molTypeCount; ++m) g.first[m] += dn;
+        a.s.n = n + dn;
+        if (AC) {           // the chain phase: its count, and N chainprob chain moves per sweep
+            SweepArgs& ac = AC[blockIdx.y];
+            ac.s.n = n + dn;
+            if (ac.nChains > 0) ac.chainFrac = g.chainprob * (double)(n + dn) / (double)ac.nChains;
+        }
+    }
+}
+
 }  // namespace
 
 // Device state of the move loop of one system.
@@ -2834,6 +3114,9 @@ struct SweepEngine {
     std::vector<void*> allocs;
     bool energyKnown = false;
     unsigned long long* typeCtr = nullptr;        // per-type acceptance of the run (SweepArgs::typeCtr)
+    GcDev* gc = nullptr;          // grand-canonical record (kGrandCanon)
+    bool gcOn = false;            // this run makes grand-canonical moves
+    int slots = 0;                // particle slots of the per-particle buffers below and of the chain phase
     uint64_t seed = ~0ull;
     int stencil = 0;
     double margin = 0.0;
@@ -2959,6 +3242,37 @@ void destroyEngine(Context* c) {
     c->engine = nullptr;
 }
 
+static void engineFree(SweepEngine* e, void** p) {
+    if (!*p) return;
+    cudaFree(*p);
+    e->allocs.erase(std::find(e->allocs.begin(), e->allocs.end(), *p));
+    *p = nullptr;
+}
+
+// Per-particle buffers of the cell lists (and of the chain phase's, once it exists) for
+// `slots` particles; their contents are rebuilt every sweep.
+static int particleBuffers(SweepEngine* e, int slots) {
+    int rc;
+    for (void** p : {(void**)&e->cellIdx, (void**)&e->cellPosF, (void**)&e->cellDirF, (void**)&e->cellPatF,
+                     (void**)&e->cellOf})
+        engineFree(e, p);
+    if ((rc = engineAlloc(e, (void**)&e->cellIdx, sizeof(int) * slots))) return rc;
+    if ((rc = engineAlloc(e, (void**)&e->cellPosF, sizeof(float4) * slots))) return rc;
+    if ((rc = engineAlloc(e, (void**)&e->cellDirF, sizeof(float4) * slots))) return rc;
+    if ((rc = engineAlloc(e, (void**)&e->cellPatF, sizeof(float4) * slots))) return rc;
+    if ((rc = engineAlloc(e, (void**)&e->cellOf, sizeof(int) * slots))) return rc;
+    SweepEngine::Chains& C = e->ch;
+    if (C.ctl) {
+        for (void** p : {(void**)&C.cellIdx, (void**)&C.cellOf, (void**)&C.slotOf, (void**)&C.cellPosF}) engineFree(e, p);
+        if ((rc = engineAlloc(e, (void**)&C.cellIdx, sizeof(int) * slots))) return rc;
+        if ((rc = engineAlloc(e, (void**)&C.cellOf, sizeof(int) * slots))) return rc;
+        if ((rc = engineAlloc(e, (void**)&C.slotOf, sizeof(int) * slots))) return rc;
+        if ((rc = engineAlloc(e, (void**)&C.cellPosF, sizeof(float4) * slots))) return rc;
+    }
+    e->slots = slots;
+    return SC_OK;
+}
+
 static int ensureGrid(Context* c, SweepEngine* e, const double* box) {
     Grid g = makeGrid(box, c->topo.maxcut, e->margin, e->stencil);
     if (g.ncolours > kMaxColours) return fail(SC_ERR_RANGE, "too many colour classes");
@@ -3033,6 +3347,7 @@ static void fillArgs(Context* c, SweepEngine* e, const sc_run_params& p) {
     a.typeCtr = e->typeCtr;
     a.coneAngle = c->opts.coneAngle;
     for (int m = 0; m < kMaxChainTypes; ++m) a.chainMxType[m] = chainStep(c, m, p);
+    a.gc = e->gcOn ? e->gc : nullptr;
 }
 
 // Chain phase of one system: chains (molecules of more than one particle), the bound R of
@@ -3052,10 +3367,11 @@ static int prepareChains(Context* c, SweepEngine* e, const sc_run_params& p, con
     if (!C.ctl) {
         if ((rc = engineAlloc(e, (void**)&C.ctl, sizeof(Control)))) return rc;
         cudaMemset(C.ctl, 0, sizeof(Control));
-        if ((rc = engineAlloc(e, (void**)&C.cellIdx, sizeof(int) * n))) return rc;
-        if ((rc = engineAlloc(e, (void**)&C.cellOf, sizeof(int) * n))) return rc;
-        if ((rc = engineAlloc(e, (void**)&C.slotOf, sizeof(int) * n))) return rc;
-        if ((rc = engineAlloc(e, (void**)&C.cellPosF, sizeof(float4) * n))) return rc;
+        const int slots = std::max(e->slots, 1);
+        if ((rc = engineAlloc(e, (void**)&C.cellIdx, sizeof(int) * slots))) return rc;
+        if ((rc = engineAlloc(e, (void**)&C.cellOf, sizeof(int) * slots))) return rc;
+        if ((rc = engineAlloc(e, (void**)&C.slotOf, sizeof(int) * slots))) return rc;
+        if ((rc = engineAlloc(e, (void**)&C.cellPosF, sizeof(float4) * slots))) return rc;
         if ((rc = engineAlloc(e, (void**)&C.chains, sizeof(int2) * chains.size()))) return rc;
         if ((rc = engineAlloc(e, (void**)&C.chIdx, sizeof(int) * chains.size()))) return rc;
         cudaMemcpy(C.chains, chains.data(), sizeof(int2) * chains.size(), cudaMemcpyHostToDevice);
@@ -3133,6 +3449,97 @@ static int prepareChains(Context* c, SweepEngine* e, const sc_run_params& p, con
     return SC_OK;
 }
 
+// Grand-canonical record of a run: the species with what Particle::init needs of their type,
+// ParticleVector::first, the capacity, zeroed counters.
+static int prepareGrand(Context* c, SweepEngine* e, const sc_run_params& p) {
+    e->gcOn = p.grand_every > 0 && !c->grand.empty();
+    if (!e->gcOn) return SC_OK;
+    if (c->conf.molTypeCount > MAXMT) return fail(SC_ERR_RANGE, "more than 100 molecule types (MAXMT)");
+    int rc;
+    if (!e->gc && (rc = engineAlloc(e, (void**)&e->gc, sizeof(GcDev)))) return rc;
+    GcDev h;
+    std::memset(&h, 0, sizeof h);
+    h.nSpecies = (int)c->grand.size();
+    h.molTypeCount = c->conf.molTypeCount;
+    h.cap = c->cap;
+    h.chainprob = p.chainprob;
+    for (int k = 0; k < h.nSpecies; ++k) {
+        const Context::Grand& g = c->grand[k];
+        const IaParam& ia = c->topo.ia[g.type][g.type];
+        GcSpecies& sp = h.sp[k];
+        sp.molType = g.molType;
+        sp.ctype = c->compactOf[g.type];
+        sp.geo = ia.geotype[0];
+        sp.chemPot = g.chemPot;
+        sp.pcos0 = ia.pcoshalfi[0]; sp.psin0 = ia.psinhalfi[0];
+        sp.pcos2 = ia.pcoshalfi[2]; sp.psin2 = ia.psinhalfi[2];
+        sp.csec = ia.csecpatchrot[0]; sp.ssec = ia.ssecpatchrot[0];
+        sp.chcos = ia.chiral_cos[0]; sp.chsin = ia.chiral_sin[0];
+    }
+    for (int m = 0; m <= h.molTypeCount; ++m) h.first[m] = c->conf.first[m];
+    cudaError_t r = cudaMemcpy(e->gc, &h, sizeof h, cudaMemcpyHostToDevice);
+    if (r != cudaSuccess) return cudaFail(r, "upload grand-canonical record");
+    return SC_OK;
+}
+
+// After a run with grand-canonical moves: the device's count, ParticleVector::first and
+// counters back on the host, and the host particle vector brought to the device's.
+static int finishGrand(Context* c, const SweepArgs* dArgs) {
+    SweepEngine* e = c->engine;
+    if (!e || !e->gcOn) return SC_OK;
+    GcDev h;
+    SweepArgs cur;
+    cudaError_t r = cudaMemcpy(&h, e->gc, sizeof h, cudaMemcpyDeviceToHost);
+    if (r == cudaSuccess) r = cudaMemcpy(&cur, dArgs, sizeof cur, cudaMemcpyDeviceToHost);
+    if (r != cudaSuccess) return cudaFail(r, "grand-canonical record");
+    for (int k = 0; k < h.nSpecies && k < (int)c->grand.size(); ++k) {
+        Context::Grand& g = c->grand[k];
+        g.steps += (long)h.ctr[k][0];
+        g.insAcc += (long)h.ctr[k][1]; g.insRej += (long)h.ctr[k][2];
+        g.delAcc += (long)h.ctr[k][3]; g.delRej += (long)h.ctr[k][4];
+        g.countSum += h.countSum[k];
+    }
+    const int n = cur.s.n;
+    c->conf.first.assign(h.first, h.first + h.molTypeCount + 1);
+    c->conf.p.resize((size_t)n);
+    for (int m = 0; m < h.molTypeCount; ++m)
+        for (int i = h.first[m]; i < h.first[m + 1] && i < n; ++i) c->conf.p[i].molType = m;
+    c->d.n = n;
+    e->args.s.n = n;
+    e->ch.args.s.n = n;
+    c->devNewer = true;
+    int rc = c->downloadState();       // positions, axes, patches, types
+    c->rebuildMolInfo();
+    return rc;
+}
+
+// A grand-canonical system whose free slots ran out: larger state arrays and per-particle
+// buffers, and the arguments (with the device's count) uploaded again.
+static int uploadArgs(Batch& b);
+
+static int growSystem(Context* c, Batch& b, const SweepArgs& cur, const sc_run_params& p) {
+    SweepEngine* e = c->engine;
+    c->d.n = cur.s.n;
+    const int newCap = std::max(2 * c->cap, c->cap + 256);
+    int rc;
+    if ((rc = c->grow(newCap))) return rc;
+    if ((rc = particleBuffers(e, newCap))) return rc;
+    SweepArgs& a = e->args;
+    a.s = c->d;
+    a.temper = cur.temper;
+    a.cellIdx = e->cellIdx; a.cellPosF = e->cellPosF; a.cellDirF = e->cellDirF; a.cellPatF = e->cellPatF;
+    a.cellOf = e->cellOf;
+    if (e->ch.on) {
+        SweepArgs& ac = e->ch.args;
+        ac.s = c->d;
+        ac.cellIdx = e->ch.cellIdx; ac.cellOf = e->ch.cellOf; ac.slotOf = e->ch.slotOf; ac.cellPosF = e->ch.cellPosF;
+        if (ac.nChains > 0) ac.chainFrac = p.chainprob * (double)c->d.n / (double)ac.nChains;
+    }
+    cudaError_t r = cudaMemcpy(&e->gc->cap, &newCap, sizeof newCap, cudaMemcpyHostToDevice);
+    if (r != cudaSuccess) return cudaFail(r, "grand-canonical capacity");
+    return uploadArgs(b);
+}
+
 // Device state, grid and arguments of one system for a run with parameters p.
 static int prepareSystem(Context* c, const sc_run_params& p, bool npt) {
     const bool hostChanged = c->hostNewer;    // the running energy must be recomputed
@@ -3140,17 +3547,12 @@ static int prepareSystem(Context* c, const sc_run_params& p, bool npt) {
     if (rc) return rc;
     if ((rc = wlPrepare(c, hostChanged))) return rc;
     if (hostChanged && c->engine) c->engine->energyKnown = false;
-    int n = c->d.n;
     SweepEngine* e = c->engine;
     if (!e) {
         e = new SweepEngine();
         c->engine = e;
         if ((rc = engineAlloc(e, (void**)&e->ctl, sizeof(Control)))) return rc;
-        if ((rc = engineAlloc(e, (void**)&e->cellIdx, sizeof(int) * std::max(n, 1)))) return rc;
-        if ((rc = engineAlloc(e, (void**)&e->cellPosF, sizeof(float4) * std::max(n, 1)))) return rc;
-        if ((rc = engineAlloc(e, (void**)&e->cellDirF, sizeof(float4) * std::max(n, 1)))) return rc;
-        if ((rc = engineAlloc(e, (void**)&e->cellPatF, sizeof(float4) * std::max(n, 1)))) return rc;
-        if ((rc = engineAlloc(e, (void**)&e->cellOf, sizeof(int) * std::max(n, 1)))) return rc;
+        if ((rc = particleBuffers(e, std::max(c->cap, 1)))) return rc;
         if ((rc = engineAlloc(e, (void**)&e->counters, sizeof(unsigned long long) * C_COUNT))) return rc;
         if ((rc = engineAlloc(e, (void**)&e->err, sizeof(int)))) return rc;
         if ((rc = engineAlloc(e, (void**)&e->typeCtr, sizeof(unsigned long long) * kTypeCtrCount))) return rc;
@@ -3158,6 +3560,7 @@ static int prepareSystem(Context* c, const sc_run_params& p, bool npt) {
         std::memset(&z, 0, sizeof z);
         cudaMemcpy(e->ctl, &z, sizeof z, cudaMemcpyHostToDevice);
     }
+    if (e->slots < c->cap && (rc = particleBuffers(e, c->cap))) return rc;   // the state grew
     if (e->seed != p.seed) {
         // a new seed restarts the sweep counter of the Philox streams
         unsigned long long zero = 0;
@@ -3172,6 +3575,7 @@ static int prepareSystem(Context* c, const sc_run_params& p, bool npt) {
     // widest cells
     e->stencil = chooseStencil(box, c->topo.maxcut, p.stencil == 0 && wlActive(c) ? 1 : p.stencil);
     if ((rc = ensureGrid(c, e, box))) return rc;
+    if ((rc = prepareGrand(c, e, p))) return rc;
     fillArgs(c, e, p);
     if ((rc = prepareChains(c, e, p, box))) return rc;
     cudaMemset(e->counters, 0, sizeof(unsigned long long) * C_COUNT);
@@ -3193,7 +3597,8 @@ static int uploadArgs(Batch& b) {
     b.maxN = b.maxCells = b.maxActive = b.maxColours = 0;
     for (int k = 0; k < ns; ++k) {
         b.hArgs[k] = b.sys[k]->engine->args;
-        b.maxN = std::max(b.maxN, b.hArgs[k].s.n);
+        // grand-canonical systems: grids over every slot (the count changes on the device)
+        b.maxN = std::max(b.maxN, b.hArgs[k].gc ? b.sys[k]->cap : b.hArgs[k].s.n);
         b.maxCells = std::max(b.maxCells, b.hArgs[k].g.ncells);
         b.maxActive = std::max(b.maxActive, b.hArgs[k].g.nactive);
         b.maxColours = std::max(b.maxColours, b.hArgs[k].g.ncolours);
@@ -3274,6 +3679,7 @@ static int systemErrors(Context* c) {
     if (err & E_CELL_OVERFLOW) return fail(SC_ERR_DEVICE, "a cell holds more than 256 particles (density too high for the cell list)");
     if (err & E_PARTNER_FAR) return fail(SC_ERR_DEVICE, "a bonded partner lies beyond the cell stencil (bond longer than maxcut)");
     if (err & E_FLOW_WAIT) return fail(SC_ERR_DEVICE, "dataflow sweep: a cell waited too long for its neighbours");
+    if (err & E_GC_FULL) return fail(SC_ERR_DEVICE, "grand-canonical insertion found no free particle slot");
     return SC_OK;
 }
 
@@ -3463,6 +3869,12 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
     const int ve = npt ? p.volume_every : 1;
     long G = (long)ve * std::max(1, (8 + ve - 1) / ve);
     if (exchangeEvery > 0) G = std::max(1L, std::min(G, (long)exchangeEvery));
+    // grand-canonical moves: after every grand_every-th sweep of the call (updater.cpp:164-165),
+    // between the captured blocks; the host keeps a free slot for every insertion
+    const bool gc = p.grand_every > 0 && ns == 1 && b.hArgs[0].gc != nullptr;
+    long nextGc = gc ? p.grand_every - (long)(p.sweep_offset % p.grand_every) : -1;
+    long nUpper = gc ? b.hArgs[0].s.n : 0;     // bound on the device's count
+    if (gc) G = std::max(1L, std::min(G, (long)p.grand_every));
     const bool useGraph = !p.time_phases;
     const long chunk = 48;
     long nextCheck = p.check_every > 0 ? p.check_every : -1;
@@ -3486,7 +3898,8 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
     long sw = 0;
     while (sw < nsweeps) {
         long left = nsweeps - sw;
-        bool aligned = (sw % G == 0) && (nextExchange < 0 || nextExchange - sw >= G) && (nextWl < 0 || nextWl - sw >= G);
+        bool aligned = (sw % G == 0) && (nextExchange < 0 || nextExchange - sw >= G) && (nextWl < 0 || nextWl - sw >= G) &&
+                       (nextGc < 0 || nextGc - sw >= G);
         if (useGraph && left >= G && aligned) {
             int key[15] = {ns, b.maxN, b.maxCells, b.maxActive, b.maxColours, (int)G, anySurrogate ? 1 : 0,
                            b.chains ? 1 : 0, b.maxCellsC, b.maxActiveC, b.maxColoursC, dense ? 1 : 0, flow ? 1 : 0,
@@ -3531,6 +3944,21 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
             launches += 1;
             while (nextExchange <= sw) nextExchange += exchangeEvery;
         }
+        if (nextGc > 0 && sw >= nextGc) {
+            while (nextGc <= sw) nextGc += p.grand_every;
+            Context* c = b.sys[0];
+            if (nUpper + 1 > c->cap) {
+                if ((r = cudaStreamSynchronize(s)) != cudaSuccess) return cudaFail(r, "sweep");
+                SweepArgs cur;
+                if ((r = cudaMemcpy(&cur, b.dArgs, sizeof cur, cudaMemcpyDeviceToHost)) != cudaSuccess)
+                    return cudaFail(r, "sweep arguments");
+                nUpper = cur.s.n;
+                if (nUpper + 1 > c->cap && (rc = growSystem(c, b, cur, p))) return rc;
+            }
+            kGrandCanon<<<dims(1), kGcThreads, 0, s>>>(b.dArgs, b.chains ? b.dArgsC : nullptr);
+            launches += 1;
+            nUpper += 1;
+        }
         if (nextCheck > 0 && sw >= nextCheck) {
             // the cell list (box fractions) stays valid after an accepted volume move
             if ((r = exactEnergy(true)) != cudaSuccess) return cudaFail(r, "energy check");
@@ -3554,6 +3982,7 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
                     SweepArgs cur;
                     cudaMemcpy(&cur, b.dArgs + k, sizeof cur, cudaMemcpyDeviceToHost);
                     double T = cur.temper;
+                    c->d.n = cur.s.n;            // grand-canonical moves change it on the device
                     sc_run_params q = p;
                     q.seed = e->args.seed;
                     q.temper = T;
@@ -3604,6 +4033,8 @@ static int checkParams(const sc_run_params& p) {
     if (p.variant > 0 && (p.variant & 8) && p.delayed)
         return fail(SC_ERR_UNSUPPORTED, "the warp-per-cell kernel (variant bit 3) runs plain moves only");
     if (p.flow_wait_polls < 0) return fail(SC_ERR_ARG, "flow_wait_polls must be >= 0");
+    if (p.grand_every < 0) return fail(SC_ERR_ARG, "grand_every must be >= 0");
+    if (p.sweep_offset < 0) return fail(SC_ERR_ARG, "sweep_offset must be >= 0");
     return SC_OK;
 }
 
@@ -3624,7 +4055,10 @@ int runSweeps(Context* c, const sc_run_params& p0, sc_run_stats& st) {
     int rc = checkParams(p0);
     if (rc) return rc;
     const sc_run_params p = resolveTuned(c, p0);
-    if (c->conf.p.empty()) return SC_OK;
+    const bool grandRun = p.grand_every > 0 && !c->grand.empty();
+    if (c->conf.p.empty() && !grandRun) return SC_OK;     // an empty grand-canonical box can fill up
+    if (grandRun && wlActive(c))
+        return fail(SC_ERR_UNSUPPORTED, "grand-canonical moves with Wang-Landau weights are outside the GPU path");
     if (p.delayed && !c->surrogate) return fail(SC_ERR_STATE, "delayed = 1 needs a surrogate (sc_set_surrogate)");
     if ((rc = checkMoves(c))) return rc;
     if ((rc = wlCheckRun(c, p))) return rc;
@@ -3641,8 +4075,21 @@ int runSweeps(Context* c, const sc_run_params& p0, sc_run_stats& st) {
     Batch& b = *c->batch;
     if ((rc = uploadArgs(b))) return rc;
     RunOut out;
-    if ((rc = runBatch(b, p, p.nsweeps, 0, 0, out))) return rc;
+    rc = runBatch(b, p, p.nsweeps, 0, 0, out);
+    // the device's particle vector, whatever happened (a failed run leaves it consistent too)
+    const int rcG = finishGrand(c, b.dArgs);
+    if (rc) return rc;
+    if (rcG) return rcG;
     collectStats(c, st);
+    if (c->engine->gcOn) {
+        GcDev h;
+        cudaMemcpy(&h, c->engine->gc, sizeof h, cudaMemcpyDeviceToHost);
+        for (int k = 0; k < h.nSpecies; ++k) {
+            st.acc_insert += (long)h.ctr[k][1]; st.rej_insert += (long)h.ctr[k][2];
+            st.acc_delete += (long)h.ctr[k][3]; st.rej_delete += (long)h.ctr[k][4];
+        }
+    }
+    st.particles = (long)c->conf.p.size();
     st.sweeps = out.sweeps;
     st.seconds = out.seconds;
     st.phase_seconds = out.phaseSeconds;
@@ -3797,8 +4244,11 @@ int equilibrate(Context* c, const sc_run_params& p, long nequil, long adjust, sc
     initStepSizes(c);
     const long half = nequil / 2;
     sc_run_params q = p;
-    auto run = [&](long n) -> int {
+    // the reference's two loops (main.cpp:270-287): sweeps, and the grand-canonical schedule,
+    // count from each loop's start
+    auto run = [&](long n, long offset) -> int {
         q.nsweeps = n;
+        q.sweep_offset = offset;
         q.edge_mx = c->edge.mx;
         sc_run_stats s1;
         int rc = runSweeps(c, q, s1);
@@ -3810,18 +4260,21 @@ int equilibrate(Context* c, const sc_run_params& p, long nequil, long adjust, sc
         st.pairs_tested += s1.pairs_tested; st.pairs_evaluated += s1.pairs_evaluated;
         st.seconds += s1.seconds; st.launches += s1.launches;
         st.energy = s1.energy; st.energy_check = s1.energy_check; st.max_drift = std::max(st.max_drift, s1.max_drift);
+        st.acc_insert += s1.acc_insert; st.rej_insert += s1.rej_insert;
+        st.acc_delete += s1.acc_delete; st.rej_delete += s1.rej_delete;
+        st.particles = s1.particles;
         return SC_OK;
     };
     long done = 0;
     while (done < half) {
         const long blk = adjust > 0 ? std::min(adjust, half - done) : half - done;
-        int rc = run(blk);
+        int rc = run(blk, done);
         if (rc) return rc;
         done += blk;
         if (adjust > 0 && blk == adjust) adjustSteps(c);     // at sweep == next_adjust
     }
     if (half > 0) {
-        int rc = run(half);
+        int rc = run(half, 0);
         if (rc) return rc;
     }
     return SC_OK;
@@ -3863,6 +4316,7 @@ int tuneSweeps(Context* c, const sc_run_params& p, int sweeps, sc_run_params& be
             q.variant = v;
             q.check_every = 0;
             q.time_phases = 0;
+            q.grand_every = 0;                 // the candidates move the same particles
             q.nsweeps = 2;                     // grid, graph capture, caches
             sc_run_stats st;
             double rate = 0.0;
@@ -3945,6 +4399,9 @@ int runReplicas(void* h, const sc_run_params& p0, int exchangeEvery, sc_run_stat
     // a batch has no tuned choice of its own: variant -1 is the dataflow sweep
     sc_run_params p = p0;
     if (p.variant < 0) p.variant = 4;
+    if (p.grand_every > 0)
+        return fail(SC_ERR_UNSUPPORTED, "grand-canonical moves in replica exchange (the exchange would need the "
+                                        "chemical-potential terms, movecreator.cpp:728-734): use sc_simulate");
     Batch& b = R->b;
     const int nrep = (int)b.sys.size();
     const bool npt = p.volume_every > 0;
@@ -3962,6 +4419,7 @@ int runReplicas(void* h, const sc_run_params& p0, int exchangeEvery, sc_run_stat
         q.temper = R->temps[k]; q.ptype = p.ptype; q.volume_every = p.volume_every; q.check_every = p.check_every;
         q.stencil = p.stencil; q.time_phases = p.time_phases; q.press = p.press; q.delayed = p.delayed;
         q.variant = p.variant;
+        q.grand_every = 0;
         if (p.delayed && !c->surrogate) return fail(SC_ERR_STATE, "delayed = 1 needs a surrogate on every replica");
         if ((rc = wlCheckRun(c, q))) return rc;
         if ((q.variant & 8) && wlActive(c))

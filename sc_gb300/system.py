@@ -252,6 +252,24 @@ class System:
         L.check(self._lib.sc_simulate(self._h, C.byref(p), C.byref(st)))
         return st
 
+    # --- grand-canonical species (MoveCreator::muVTMove, movecreator.cpp:797-924) -------------
+    def write_top_last(self, path):
+        """top.last (main.cpp:313-331): top.init up to [System], then the current counts."""
+        L.check(self._lib.sc_write_top_last(self._h, str(path).encode()))
+
+    def grand_stats(self):
+        """Statistics::grand of every grand-canonical species, summed over the context's runs:
+        a list of sc_grand_stats records (mol_type, count, activity, chem_pot, steps, ins_acc,
+        ins_rej, del_acc, del_rej, average_particles)."""
+        k = C.c_int()
+        L.check(self._lib.sc_grand_species(self._h, C.byref(k)))
+        out = []
+        for i in range(k.value):
+            g = L.GrandStats()
+            L.check(self._lib.sc_grand_stats_get(self._h, i, C.byref(g)))
+            out.append(g)
+        return out
+
     # --- Wang-Landau (WangLandau, scOOP/mc/wanglandau.h, wanglandau.cpp) ----------------
     def wl_load(self, path=None, text=None):
         """WangLandau::initCalc + init: weights file by path or as text."""

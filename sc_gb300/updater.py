@@ -6,8 +6,10 @@ sweeps a frame to the movie file (Updater::dumpMovie, updater.h:82-93, with Conf
 Conf.h:388-424), and at the end writes config.last (Conf.h:413-422).  With Wang-Landau
 weights it also writes the weights file every `report` sweeps (WangLandau::write,
 updater.cpp:320-322), stops where the flatness schedule ends the run (updater.cpp:255-265)
-and writes the final file (WangLandau::endWangLandau, updater.cpp:388).  `run` does the
-same around blocks of GPU sweeps, in the reference's formats.
+and writes the final file (WangLandau::endWangLandau, updater.cpp:388).  With
+grand-canonical species it writes top.last with the final counts (main.cpp:313-331).
+`run` does the same around blocks of GPU sweeps, in the reference's formats; the blocks
+pass their offset in the loop, so that grand-canonical moves fall on the reference's sweeps.
 """
 import os
 
@@ -70,7 +72,7 @@ def run(system, nsweeps, report=0, movie=0, directory=".", params=None, wl_file=
     while sweep < nsweeps:
         stops = [nsweeps] + [x for x in (next_dump, next_frame) if x]
         block = min(stops) - sweep
-        st = system.simulate(p, nsweeps=block)
+        st = system.simulate(p, nsweeps=block, sweep_offset=sweep)
         for name, _ in type(st)._fields_:
             if name.startswith(("acc_", "rej_", "moves", "pairs_")):
                 totals[name] = totals.get(name, 0) + getattr(st, name)
@@ -91,6 +93,13 @@ def run(system, nsweeps, report=0, movie=0, directory=".", params=None, wl_file=
                 f.write(_frame(system, sweep))
             next_frame += movie
     system.write_config(os.path.join(directory, "config.last"))
+    grand = system.grand_stats()
+    if grand:
+        system.write_top_last(os.path.join(directory, "top.last"))
+        # Updater::simulate's closing report of each species (updater.cpp:358-373)
+        totals["grand"] = [dict(mol_type=g.mol_type, count=g.count, steps=g.steps, ins_acc=g.ins_acc,
+                                ins_rej=g.ins_rej, del_acc=g.del_acc, del_rej=g.del_rej,
+                                average_particles=g.average_particles) for g in grand]
     if wl:
         system.wl_end(wf)
     totals["sweeps"] = sweep

@@ -116,7 +116,45 @@ def cases():
         base.update(pairlist_update="10", nequil="0")
         out[name] = dict(top=top, config=config, opts=base, nsweeps=nsw, report=20, seeds=6, burn=burn, s2=True,
                          pre=pre)
+    # grand-canonical (muVT) moves, one every sweep (nGrandCanon = 1): attractive spheres as the
+    # only species, and patchy spherocylinders inserted and removed among fixed spheres (the
+    # species listed last, so removals inside its block shift the particles behind); the count
+    # from the reference's movie frames, the total energy from energy.dat
+    box = np.full(3, 8.0)
+    pos = place_spheres(rng, 30, box, 1.1)
+    out["gc_spa"] = dict(
+        top=top_text([("A", 1, "SPA", [1.0, 1.0, 1.1225, 0.5])], [("A", [1], ["ACTIVITY: 0.1"])], [("A", 30)]),
+        config=config_text(box, pos, rand_unit(rng, 30), rand_perp(rng, rand_unit(rng, 30))),
+        opts=dict(temper=1.0, transmx=0.6, rotmx=30.0, nGrandCanon=1, pairlist_update=0),
+        nsweeps=24000, report=20, seeds=8, burn=4000, gc=True)
+    box = np.full(3, 12.0)
+    ps, ds, qs = place(rng, 15, box, L)
+    sp = []
+    while len(sp) < 20:          # spheres clear of the spherocylinders and of each other
+        p = rng.uniform(0, 1, 3) * box
+        if all(np.linalg.norm((p - q) - box * np.round((p - q) / box)) > 1.2 for q in sp) and all(
+                seg_dist(p, np.array([0.0, 0.0, 1.0]), p + ((q - p) - box * np.round((q - p) / box)), d, L) > 1.2
+                and np.linalg.norm((p - q) - box * np.round((p - q) / box)) > 0 for q, d in zip(ps, ds)):
+            sp.append(p)
+    sp = np.array(sp)
+    out["gc_psc"] = dict(
+        top=top_text([("A", 2, "SPA", [0.5, 1.0, 1.1225, 0.3775]),
+                      ("P", 1, "PSC", [1.0, 1.0, 1.12, 0.2, 90.0, 10.0, L, 0.0])],
+                     [("A", [2], []), ("P", [1], ["ACTIVITY: 0.02"])], [("A", 20), ("P", 15)]),
+        config=config_text(box, np.vstack([sp, ps]), np.vstack([rand_unit(rng, 20), ds]),
+                           np.vstack([rand_perp(rng, rand_unit(rng, 20)), qs])),
+        opts=dict(temper=1.0, transmx=0.5, rotmx=30.0, nGrandCanon=1, pairlist_update=0),
+        nsweeps=24000, report=20, seeds=8, burn=4000, gc=True)
     return out
+
+
+def place_spheres(rng, n, box, dmin):
+    pos = []
+    while len(pos) < n:
+        p = rng.uniform(0, 1, 3) * box
+        if all(np.linalg.norm((p - q) - box * np.round((p - q) / box)) > dmin for q in pos):
+            pos.append(p)
+    return np.array(pos)
 
 
 def pre_equilibrate(c, seed=999):
@@ -162,7 +200,7 @@ def run_one(c, seed):
         opts = dict(OPTION_KEYS)
         opts.update(c["opts"])
         opts.update(nsweeps=c["nsweeps"], report=c["report"], seed=seed, paraltemper=opts["temper"])
-        if c.get("s2"):
+        if c.get("s2") or c.get("gc"):
             opts.update(movie=c["report"])
         with open(os.path.join(tmp, "options"), "w") as f:
             f.write("".join(f"{k} = {v}\n" for k, v in opts.items()))
@@ -183,11 +221,24 @@ def run_one(c, seed):
                 continue
             sw, v = line.split(";")
             vol.append((int(sw), float(v)))
-        s2 = []
+        s2, counts = [], []
         if c.get("s2"):
             n_sc = int(c["top"].split("[System]")[1].split()[1])     # the first [System] entry: the SCs
             s2 = movie_s2(os.path.join(tmp, "movie"), slice(0, n_sc))
-        return dict(seed=seed, energy=e, volume=vol, s2=s2)
+        if c.get("gc"):
+            counts = movie_counts(os.path.join(tmp, "movie"))
+        return dict(seed=seed, energy=e, volume=vol, s2=s2, counts=counts)
+
+
+def movie_counts(path):
+    """(sweep, particle count) of every frame of the reference's movie file."""
+    lines = open(path).read().splitlines()
+    out, k = [], 0
+    while k < len(lines):
+        n = int(lines[k].split()[0])
+        out.append((int(lines[k + 1].split(";")[0].split()[1]), n))
+        k += 2 + n
+    return out
 
 
 def block_stats(series_per_seed, burn):
@@ -215,6 +266,9 @@ def main():
         a_ser = [[(s, al / n) for s, _, al in r["energy"]] for r in runs]
         v_ser = [[(s, v / n) for s, v in r["volume"]] for r in runs]
         series = [("energy_per_particle", e_ser), ("alignment_per_particle", a_ser), ("volume_per_particle", v_ser)]
+        if c.get("gc"):     # the count changes: totals, and the count itself
+            series = [("energy_total", [[(s, en) for s, en, _ in r["energy"]] for r in runs]),
+                      ("particles", [[(s, float(k)) for s, k in r["counts"]] for r in runs])]
         if c.get("s2"):
             series.append(("nematic_s2", [r["s2"] for r in runs]))
         stats = {k: block_stats(ser, c["burn"]) for k, ser in series}

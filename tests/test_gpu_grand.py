@@ -1,0 +1,192 @@
+"""Grand-canonical insert / delete moves on the GPU (MoveCreator::muVTMove,
+scOOP/mc/movecreator.cpp:797-924, one move every nGrandCanon sweeps, updater.cpp:164-179).
+
+Ensemble parity: tests/golden/ens_gc_spa.json and ens_gc_psc.json hold the mean particle
+count (from the reference's movie frames) and the mean total energy (energy.dat) sampled
+by the reference's own loop (oracle/_ref/sc_ref, eight seeds, tests/golden/make_ensemble.py)
+for attractive spheres exchanged with a reservoir, and for patchy spherocylinders
+exchanged among fixed spheres (the species listed last, so removals inside its block shift
+the particles behind).  The GPU runs eight trajectories from the same start for the same
+sweeps; both means must agree within 2 combined standard errors.
+
+Exactness: the running energy (the moves' energy changes, insertions and removals
+included) equals the exact total energy after the run; the particle vector keeps the
+reference's order (each molecule type in its block, the inserted particles of a species at
+its block's end); capacity growth from an empty box; chains before the species with chain
+moves; the schedule over calls (sweep_offset); bitwise reproducibility.
+"""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _case(name):
+    with open(os.path.join(GOLDEN, f"ens_{name}.json")) as f:
+        g = json.load(f)
+    from golden.make_golden import OPTION_KEYS
+
+    o = dict(OPTION_KEYS)
+    o.update(g["options"])
+    o["paraltemper"] = o["temper"]
+    return g, "".join(f"{k} = {v}\n" for k, v in o.items()), g["inputs"]["top.init"], g["inputs"]["config.init"]
+
+
+def _check_layout(s):
+    """Each molecule type in one block in [Molecules] order; the species counts match."""
+    mt = np.array([p.molType for p in s.particles()], dtype=np.int64)
+    assert np.all(np.diff(mt) >= 0)
+    for g in s.grand_stats():
+        assert int(np.sum(mt == g.mol_type)) == g.count
+
+
+@pytest.mark.parametrize("name", ["gc_spa", "gc_psc"])
+def test_ensemble_matches_reference(name):
+    from sc_gb300 import System
+
+    g, opts, top, cfg = _case(name)
+    rep, burn, nsw = g["report"], g["burn"], g["nsweeps"]
+    N, E = [], []
+    for k in range(g["seeds"]):
+        s = System.from_text(opts, top, cfg)
+        p = s.default_run()
+        p.check_every = 0
+        p.seed = 7000 + k
+        n_ser, e_ser = [], []
+        done = 0
+        while done < nsw:
+            st = s.simulate(p, nsweeps=rep, sweep_offset=done)
+            done += rep
+            if done > burn:
+                n_ser.append(st.particles)
+                e_ser.append(st.energy)
+        exact = s.all_to_all()
+        assert abs(st.energy - exact) <= 1e-9 * max(1.0, abs(exact)), (st.energy, exact)
+        assert st.particles == s.n
+        _check_layout(s)
+        N.append(np.array(n_ser, dtype=float))
+        E.append(np.array(e_ser))
+        s.close()
+    report = {}
+    for key, ser in (("particles", N), ("energy_total", E)):
+        m = np.array([x.mean() for x in ser])
+        mean, se = float(m.mean()), float(m.std(ddof=1) / math.sqrt(len(m)))
+        ref = g["stats"][key]
+        sigma = math.sqrt(se ** 2 + ref["se"] ** 2)
+        report[key] = (mean, se, ref["mean"], ref["se"])
+        assert abs(mean - ref["mean"]) <= 2.0 * sigma, report
+
+
+def test_growth_from_an_empty_box():
+    """A crowding species from an empty box: the free slots run out and grow (first 256),
+    the count passes them, and the running energy stays exact."""
+    from golden.make_golden import options_text, top_text
+    from sc_gb300 import System
+
+    top = top_text([("A", 1, "SPA", [1.0, 1.0, 1.1225, 0.5])], [("A", [1], ["ACTIVITY: 50.0"])], [("A", 0)])
+    s = System.from_text(options_text(nGrandCanon=1, transmx=0.4, temper=1.0), top, "9 9 9\n")
+    p = s.default_run()
+    p.check_every = 0
+    p.seed = 11
+    total = 0
+    for _ in range(8):
+        st = s.simulate(p, nsweeps=250, sweep_offset=total)
+        total += 250
+        exact = s.all_to_all()
+        assert abs(st.energy - exact) <= 1e-9 * max(1.0, abs(exact)), (st.energy, exact)
+    assert s.n > 300, s.n
+    (g,) = s.grand_stats()
+    assert g.steps == 2000 and g.ins_acc - g.del_acc == s.n
+    assert g.ins_acc + g.ins_rej + g.del_acc + g.del_rej == g.steps
+    pos = np.array([p.pos for p in s.particles()])
+    assert np.all(np.isfinite(pos))
+    s.close()
+
+
+def test_chains_before_the_species():
+    """Three-bead lipids with chain moves, then solvent spheres exchanged with a reservoir:
+    the chains keep their slots, the chain phase follows the count, the energy stays exact."""
+    from sc_gb300 import System, workloads
+
+    opts_text, top, config = workloads.lipids_dilute(24, seed=5)
+    top = top.replace("[System]", "S: {\nparticles: 9\nACTIVITY: 0.05\n}\n[System]", 1)
+    top = top.replace("[Molecules]", "S 9 SPA 0.5 1.0 1.1225 0.3775\n[Molecules]", 1)
+    top = top.rstrip("\n") + "\nS 0\n"
+    o = dict(l.split(" = ") for l in opts_text.strip().splitlines())
+    o.update(nGrandCanon="2", chainprob="0.2")
+    s = System.from_text("".join(f"{k} = {v}\n" for k, v in o.items()), top, config)
+    p = s.default_run()
+    p.check_every = 0
+    p.seed = 3
+    st = s.simulate(p, nsweeps=400)
+    exact = s.all_to_all()
+    assert abs(st.energy - exact) <= 1e-9 * max(1.0, abs(exact)), (st.energy, exact)
+    assert st.acc_chain > 0 and st.acc_insert > 0
+    mt = np.array([q.molType for q in s.particles()])
+    assert np.all(mt[:72] == 0) and np.all(mt[72:] == 1) and s.n == 72 + s.grand_stats()[0].count
+    s.close()
+
+
+def test_schedule_counts_from_the_loop_start():
+    from sc_gb300 import System
+
+    g, opts, top, cfg = _case("gc_spa")
+    s = System.from_text(opts.replace("nGrandCanon = 1", "nGrandCanon = 3"), top, cfg)
+    p = s.default_run()
+    p.check_every = 0
+    s.simulate(p, nsweeps=10, sweep_offset=0)       # sweeps 1..10: moves after 3, 6, 9
+    assert s.grand_stats()[0].steps == 3
+    s.simulate(p, nsweeps=10, sweep_offset=11)      # sweeps 12..21: after 12, 15, 18, 21
+    assert s.grand_stats()[0].steps == 7
+    s.close()
+
+
+def test_bitwise_reproducible():
+    from sc_gb300 import System
+
+    g, opts, top, cfg = _case("gc_psc")
+    out = []
+    for _ in range(2):
+        s = System.from_text(opts, top, cfg)
+        p = s.default_run()
+        p.seed = 99
+        st = s.simulate(p, nsweeps=300)
+        out.append((st.energy, s.n, np.array([q.pos for q in s.particles()]).tobytes()))
+        s.close()
+    assert out[0] == out[1]
+
+
+def test_replica_exchange_refuses_grand_moves():
+    from sc_gb300 import ReplicaSet, ScError, System
+
+    g, opts, top, cfg = _case("gc_spa")
+    systems = [System.from_text(opts, top, cfg) for _ in range(2)]
+    R = ReplicaSet(systems, [1.0, 1.1], ladder=[0, 1])
+    p = systems[0].default_run()
+    with pytest.raises(ScError) as ei:
+        R.run(10, exchange_every=5, seed=1, params=p)
+    assert ei.value.code == -7
+    p.grand_every = 0
+    R.run(10, exchange_every=5, seed=1, params=p)
+    R.close()
+    for s in systems:
+        s.close()
+
+
+def test_output_loop_writes_top_last(tmp_path):
+    from sc_gb300 import System, updater
+
+    g, opts, top, cfg = _case("gc_spa")
+    s = System.from_text(opts, top, cfg)
+    tot = updater.run(s, 200, report=50, movie=50, directory=str(tmp_path))
+    text = (tmp_path / "top.last").read_text()
+    assert text.endswith(f"[System]\nA {s.n}\n")
+    counts = [int(l.split()[0]) for l in (tmp_path / "movie").read_text().splitlines() if len(l.split()) == 1]
+    assert len(counts) == 4 and counts[-1] == s.n
+    assert tot["grand"][0]["steps"] == 200
+    s.close()
