@@ -102,6 +102,9 @@ typedef struct {
     long sweep_offset;      /* sweeps the caller's loop ran before this call: a move due every
                                grand_every sweeps follows sweep k of the loop when k % grand_every
                                == 0 (updater.cpp:165), k counted from the loop's start */
+    double switchprob;      /* type switch attempts per particle move (options switchprob;
+                               MoveCreator::switchTypeMove, movecreator.cpp:233-303): N switchprob
+                               attempts per sweep over the particles with a switch type; 0: none */
 } sc_run_params;
 
 typedef struct {
@@ -128,6 +131,7 @@ typedef struct {
     /* grand-canonical moves (grand_every > 0), all species together */
     long acc_insert, rej_insert, acc_delete, rej_delete;
     long particles;          /* particle count after the call */
+    long acc_switch, rej_switch;   /* type switch moves (switchprob > 0) */
 } sc_run_stats;
 
 /* Record of one grand-canonical species (Statistics::grand, scOOP/structures/statistics.h;

@@ -53,7 +53,7 @@ class RunParams(C.Structure):
                 ("edge_mx", C.c_double), ("chainprob", C.c_double), ("chainmmx", C.c_double),
                 ("chain_angle", C.c_double), ("check_every", C.c_int), ("time_phases", C.c_int),
                 ("stencil", C.c_int), ("delayed", C.c_int), ("variant", C.c_int), ("flow_wait_polls", C.c_int),
-                ("grand_every", C.c_int), ("sweep_offset", C.c_long)]
+                ("grand_every", C.c_int), ("sweep_offset", C.c_long), ("switchprob", C.c_double)]
 
 
 class RunStats(C.Structure):
@@ -64,7 +64,8 @@ class RunStats(C.Structure):
         ("phase_launches", C.c_long), ("launches", C.c_long),
         ("da_stage1_rejected", C.c_long), ("da_stage2_tried", C.c_long), ("da_stage2_rejected", C.c_long),
         ("da_err_rms", C.c_double), ("da_err_mean", C.c_double)] + [
-        (k, C.c_long) for k in ("acc_insert", "rej_insert", "acc_delete", "rej_delete", "particles")]
+        (k, C.c_long) for k in ("acc_insert", "rej_insert", "acc_delete", "rej_delete", "particles", "acc_switch",
+                                "rej_switch")]
 
 
 class GrandStats(C.Structure):

@@ -128,6 +128,16 @@ int Context::setup(std::string& err) {
     }
     if (mols.empty()) { MolParam z; std::memset(&z, 0, sizeof z); z.size = 1; mols.push_back(z); }
     rebuildMolInfo();
+    // switch types (setParticlesParams / initSwitchList, inicializer.cpp:60-87, 428-431)
+    switchTab.assign(mols.size() * MAXCHL, make_int4(-1, -1, 0, 0));
+    anySwitch = false;
+    for (size_t m = 0; m < topo.mols.size(); ++m)
+        for (size_t k = 0; k < topo.mols[m].types.size(); ++k) {
+            const int sw = topo.mols[m].switchTypes[k];
+            switchTab[m * MAXCHL + k] = make_int4(compactOf[topo.mols[m].types[k]], sw >= 0 ? compactOf[sw] : -1,
+                                                  (int)topo.mols[m].deltaMu[k], 0);
+            anySwitch |= sw >= 0;
+        }
     // grand-canonical species (inicializer.cpp:36-47, 1087-1096; main.cpp:104-108, 128-139)
     grand.clear();
     int firstGrand = -1;
@@ -202,6 +212,9 @@ int Context::ensureDevice() {
         if ((rc = allocDev((void**)&dMols, sizeof(MolParam) * mols.size()))) return rc;
         if ((rc = allocDev((void**)&dTrial, sizeof(TrialSlot)))) return rc;
         if ((rc = allocDev((void**)&dScalars, sizeof(double) * 64))) return rc;
+        if ((rc = allocDev((void**)&dSwitch, sizeof(int4) * switchTab.size()))) return rc;
+        e = cudaMemcpy(dSwitch, switchTab.data(), sizeof(int4) * switchTab.size(), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cudaFail(e, "upload switch types");
         nPartial = allToAllBlocks((int)slots) + 1;
         if ((rc = allocDev((void**)&dPartial, sizeof(double) * nPartial))) return rc;
         d.n = n;
@@ -285,7 +298,7 @@ int Context::uploadState() {
     for (int i = 0; i < n; ++i) {
         const Particle& p = conf.p[i];
         hp[i] = make_double4_32a(p.pos.x, p.pos.y, p.pos.z, (double)compactOf[p.type]);
-        hd[i] = make_double4_32a(p.dir.x, p.dir.y, p.dir.z, 0.0);
+        hd[i] = make_double4_32a(p.dir.x, p.dir.y, p.dir.z, (double)p.switched);   // w: switched
         PatchSet& s = hs[i];
         for (int k = 0; k < 2; ++k) { s.pd[k][0] = p.pd[k].x; s.pd[k][1] = p.pd[k].y; s.pd[k][2] = p.pd[k].z; }
         for (int k = 0; k < 4; ++k) { s.ps[k][0] = p.ps[k].x; s.ps[k][1] = p.ps[k].y; s.ps[k][2] = p.ps[k].z; }
@@ -324,8 +337,9 @@ int Context::downloadState() {
         Particle& p = conf.p[i];
         p.pos = {hp[i].x, hp[i].y, hp[i].z};
         p.dir = {hd[i].x, hd[i].y, hd[i].z};
-        const int ct = (int)hp[i].w;      // compact type (inserted particles take their species')
+        const int ct = (int)hp[i].w;      // compact type (inserted and switched particles change it)
         if (ct >= 0 && ct < (int)usedTypes.size()) p.type = usedTypes[ct];
+        p.switched = (int)hd[i].w;
         const PatchSet& s = hs[i];
         for (int k = 0; k < 2; ++k) p.pd[k] = {s.pd[k][0], s.pd[k][1], s.pd[k][2]};
         for (int k = 0; k < 4; ++k) p.ps[k] = {s.ps[k][0], s.ps[k][1], s.ps[k][2]};
@@ -826,6 +840,8 @@ int sc_default_run(const sc_context* ctx, sc_run_params* p) {
     p->check_every = 100;
     p->variant = -1;       // sc_tune's choice for this context, else the dataflow sweep
     p->grand_every = (int)o.nGrandCanon;
+    // no switchable particle: no switch moves (initSwitchList, inicializer.cpp:77-81)
+    p->switchprob = C(ctx)->anySwitch ? o.switchprob : 0.0;
     return SC_OK;
 }
 

@@ -82,6 +82,12 @@ struct Context {
     };
     std::vector<Grand> grand;
     int cap = 0;              // particle slots of the device state arrays (>= the particle count)
+    // type switching (MoveCreator::switchTypeMove): per molecule type and position in the
+    // molecule (MAXCHL each) the compact type, the compact switch type (-1: none) and delta_mu
+    // as the move reads it, an int (movecreator.cpp:238-243)
+    std::vector<int4> switchTab;
+    int4* dSwitch = nullptr;
+    bool anySwitch = false;   // some molecule type has a switch type
 
     Context() = default;
     Context(const Context&) = delete;

@@ -189,11 +189,21 @@ int fillMolLine(MolType& m, const std::string& cmdIn, const std::string& params,
     std::string cmd = upper(trim(cmdIn));
     std::vector<std::string> w = words(params);
     if (cmd == "PARTICLES") {
-        long ty;
+        // "TYPE [SWITCHTYPE DELTA_MU]" (inicializer.cpp:955-985): one field, or three
+        long ty, sw = -1;
+        double dmu = 0.0;
         if (w.empty() || !parseLong(w[0], ty)) { err = "top.init: could not read a particle"; return -1; }
+        if (w.size() >= 2) {
+            if (w.size() < 3 || !parseLong(w[1], sw) || !parseDouble(w[2], dmu)) {
+                err = "top.init: could not read a particle"; return -1;
+            }
+            if (sw < 0 || sw >= MAXT) { err = "top.init: switch type out of range"; return -1; }
+        }
         if (ty < 0) { err = "top.init: particles include negative type"; return -1; }
         if (ty > MAXT) { err = "top.init: particle type out of range"; return -1; }
         m.types.push_back((int)ty);
+        m.switchTypes.push_back((int)sw);
+        m.deltaMu.push_back(dmu);
         return 0;
     }
     double k = 0, eq = 0;
@@ -375,6 +385,8 @@ int readTopologyText(const std::string& text, Topology& t, std::string& err) {
         if ((int)m.types.size() > MAXCHL) { err = "top.init: molecule longer than MAXCHL"; return -1; }
         for (int ty : m.types)
             if (t.ia[ty][ty].geotype[0] == 0) { err = "top.init: molecule uses an undefined type"; return -1; }
+        for (int ty : m.switchTypes)
+            if (ty >= 0 && t.ia[ty][ty].geotype[0] == 0) { err = "top.init: molecule uses an undefined switch type"; return -1; }
     }
     // Topo::genParamPairs (topo.cpp:5-138)
     double length = 0;
@@ -456,9 +468,10 @@ int buildParticles(const Topology& t, Config& c, std::string& err) {
         for (size_t m = 0; m < t.mols.size(); ++m) if (t.mols[m].name == sys.first) { mol = (int)m; break; }
         if (mol < 0) { err = "top.init: molecule " + sys.first + " is not defined"; return -1; }
         for (long j = 0; j < sys.second; ++j)
-            for (int ty : t.mols[mol].types) {
+            for (size_t k = 0; k < t.mols[mol].types.size(); ++k) {
                 Particle p;
-                p.type = ty;
+                p.type = t.mols[mol].types[k];
+                p.switchtype = t.mols[mol].switchTypes[k];   // setParticlesParams, inicializer.cpp:428-431
                 p.molType = mol;
                 c.p.push_back(p);
             }
@@ -533,7 +546,13 @@ int readConfigText(const std::string& text, const Topology& t, Config& c, std::s
         if (g < SP && g != SCN && dot(p.pd[0], p.pd[0]) < kZEROTOL) { err = "config.init: null patch vector for particle " + std::to_string(i + 1); return -1; }
         orthogonalise(p.pd[0], p.dir);
         normalise(p.pd[0]);
-        if (p.switched) { err = "config.init: switched particles (type switching) are outside the GPU hot path"; return -1; }
+        if (p.switched) {          // the particle carries its switch type (inicializer.cpp:226-236)
+            if (p.switchtype < 0) {
+                err = "config.init: particle " + std::to_string(i + 1) + " switched even though it has no switchtype";
+                return -1;
+            }
+            std::swap(p.type, p.switchtype);
+        }
     }
     // Conf::makeMoleculeWhole for every chain (inicializer.cpp:268-278, Conf.h:373-382)
     for (int m = 0; m < c.molTypeCount; ++m) {

@@ -21,7 +21,7 @@ struct Vec3 { double x = 0, y = 0, z = 0; };
 
 struct Particle {
     Vec3 pos, dir, pd[2], ps[4], ch[2];
-    int type = 0, molType = 0, switchtype = 0, switched = 0;
+    int type = 0, molType = 0, switchtype = -1, switched = 0;   // switchtype: the other type (-1: none)
 };
 
 // Full Ia_param (scOOP/structures/structures.h:187-254).
@@ -41,6 +41,8 @@ struct IaParam {
 struct MolType {
     std::string name;
     std::vector<int> types;
+    std::vector<int> switchTypes;      // per particle of the molecule: its switch type, -1 for none
+    std::vector<double> deltaMu;       // per particle: the chemical-potential difference of the switch
     double bond1eq = -1, bond1c = -1, bond2eq = -1, bond2c = -1, bonddeq = -1, bonddc = -1, bondheq = -1, bondhc = -1;
     double angle1eq = -1, angle1c = -1, angle2eq = -1, angle2c = -1;
     double activity = -1;

@@ -65,7 +65,7 @@ constexpr size_t kDynSmemColour = kDynSmem + (size_t)kCandCap * sizeof(float4); 
 constexpr size_t kDynSmemSurrogate = kDynSmem + (size_t)kCandCap * 2 * sizeof(float4);   // + FP32 axes, patches
 
 enum Ctr { C_ACC_T, C_REJ_T, C_ACC_R, C_REJ_R, C_ACC_V, C_REJ_V, C_VOL_CONSTR, C_TESTED, C_EVAL, C_CELL_REJ, C_MOVES,
-           C_SCREENED, C_S1_REJ, C_S2_TRIED, C_S2_REJ, C_ACC_CH, C_REJ_CH, C_CH_CONSTR, C_COUNT };
+           C_SCREENED, C_S1_REJ, C_S2_TRIED, C_S2_REJ, C_ACC_CH, C_REJ_CH, C_CH_CONSTR, C_ACC_SW, C_REJ_SW, C_COUNT };
 enum ErrBit { E_CELL_OVERFLOW = 1, E_PARTNER_FAR = 2, E_FLOW_WAIT = 4, E_GC_FULL = 8 };
 constexpr int kMaxChainTypes = 8;                         // chain molecule types with their own step
 constexpr int kTypeCtrChain = 4 * MAX_DEV_TYPES;
@@ -100,6 +100,15 @@ struct Control {
 };
 
 struct GcDev;   // grand-canonical species and their record (kGrandCanon)
+
+// What Particle::init (scOOP/structures/particle.cpp:3-79) reads of a particle type.
+struct TypeInit {
+    int geo;                             // geotype[0]
+    int pad_;
+    double pcos0, psin0, pcos2, psin2;   // pcoshalfi / psinhalfi of patches 0 and 2
+    double csec, ssec;                   // csecpatchrot[0], ssecpatchrot[0]
+    double chcos, chsin;                 // chiral_cos[0], chiral_sin[0]
+};
 
 struct SweepArgs {
     DevState s;
@@ -154,6 +163,10 @@ struct SweepArgs {
                             // particle axis (MoveCreator::partAxialRotate); 0: about random axes
     GcDev* gc;              // grand-canonical moves of the run (nullptr: none); kGrandCanon writes
                             // the particle count s.n of these records
+    const TypeInit* tinit;  // Particle::init parameters per compact type
+    const int4* swTab;      // type switching (nullptr: none): per molecule type and position
+                            // (MAXCHL each) compact type, compact switch type (-1), int delta_mu
+    double switchRate;      // switch attempts per particle slot of a cell per sweep
 };
 
 // One decided single-particle move of compact type `type` in the per-type counters.
@@ -2844,12 +2857,7 @@ constexpr int kGcThreads = 256;
 struct GcSpecies {
     int molType;          // molecule type (index of ParticleVector::first)
     int ctype;            // compact type of its particle
-    int geo;              // geotype[0] of the particle type
-    int pad_;
     double chemPot;       // log(activity Nav 1e-24), inicializer.cpp:1094
-    double pcos0, psin0, pcos2, psin2;   // pcoshalfi / psinhalfi of patches 0 and 2
-    double csec, ssec;                   // csecpatchrot[0], ssecpatchrot[0]
-    double chcos, chsin;                 // chiral_cos[0], chiral_sin[0]
 };
 
 struct GcDev {
@@ -2884,9 +2892,9 @@ __device__ __forceinline__ void gcOrthogonalise(double (&v)[3], const double (&b
 }
 __device__ __forceinline__ void gcCopy(double (&d)[3], const double (&s)[3]) { d[0] = s[0]; d[1] = s[1]; d[2] = s[2]; }
 
-// Particle::init (particle.cpp:3-79) of an inserted particle: dir and P.pd[0] hold the drawn
-// axis and patch direction; the patch sides (and chiral axes) follow from them.
-__device__ void gcInitParticle(const GcSpecies& g, double (&dir)[3], PatchSet& P) {
+// Particle::init (particle.cpp:3-79) for type g: the axis is normalised, P.pd[0] made a unit
+// vector orthogonal to it, and the patch sides (second patch, chiral axes) follow from them.
+__device__ void gcInitParticle(const TypeInit& g, double (&dir)[3], PatchSet& P) {
     const int geo = g.geo;
     if (geo == SCA || geo == SCN) return;
     gcNormalise(dir);
@@ -2970,7 +2978,7 @@ __global__ void __launch_bounds__(kGcThreads) kGrandCanon(SweepArgs* A, SweepArg
                 for (int w = 0; w < 4; ++w) P.ps[w][q] = 0.0;
                 P.ch[0][q] = 0.0; P.ch[1][q] = 0.0;
             }
-            gcInitParticle(sp, dir, P);
+            gcInitParticle(a.tinit[sp.ctype], dir, P);
             for (int d = 0; d < 3; ++d) sDir[d] = dir[d];
             sPatch = P;
             sSlot = g.first[sp.molType + 1];
@@ -3095,6 +3103,179 @@ __global__ void __launch_bounds__(kGcThreads) kGrandCanon(SweepArgs* A, SweepArg
     }
 }
 
+
+// ---- type switching ----------------------------------------------------------------------
+// MoveCreator::switchTypeMove (scOOP/mc/movecreator.cpp:233-303): a particle with a switch
+// type takes the other type of its pair -- its switch type when unswitched, its molecule's
+// type when switched -- and Particle::init re-derives its patch vectors for that type; the
+// move is kept under moveTry(E_old, E_new + delta_mu (1 - 2 switched)) (movecreator.h:175-187),
+// E the particle against every other with its conlist (oneToAll / oneToAllTrial), delta_mu
+// the int the reference reads it into.  A rejected move re-initialises the patch vectors
+// for the old type, as the reference does.  The reference makes N switchprob attempts per
+// sweep, each on a uniformly chosen switchable particle.
+//
+// On the GPU the attempts are a checkerboard phase after each sweep's particle moves, over
+// the sweep's cell list (every particle is still in its cell: a move that would leave it is
+// rejected): one CTA per active cell of a colour, the colours in the sweep's order.  A cell
+// makes cnt * rate attempts (rate = switchprob N / switchable particles, the fraction rounded
+// at random), each on a uniformly chosen particle of the cell and skipped when that one has
+// no switch type, so every switchable particle sees the reference's attempt rate.  The
+// energies are full FP64 pair energies against the cell's stencil (reach s: every particle
+// within maxcut), reduced in a fixed order.
+
+constexpr int kSwThreads = 128;
+
+struct SwitchShared {
+    Stencil st;
+    Scan scan;
+    PatchSet newP, oldP;         // patch vectors under the new type / re-derived for the old one
+    double dirNew[3], dirOld[3];
+    double u;
+    int target, oldType, newType, switched, dmu, go;
+    double redO[kSwThreads / 32], redN[kSwThreads / 32];
+    int redP[kSwThreads / 32];
+};
+
+__global__ void __launch_bounds__(kSwThreads) kSwitchColour(const SweepArgs* __restrict__ A, int phase) {
+    const SweepArgs& a = A[blockIdx.y];
+    if (!a.swTab || !(a.switchRate > 0.0)) return;
+    const Grid& g = a.g;
+    if ((int)blockIdx.x >= g.nactive || phase >= g.ncolours) return;
+    int cx, cy, cz;
+    decodeActive(g, a.ctl->perm[phase], blockIdx.x, cx, cy, cz);
+    const int cell = (cz * g.nc[1] + cy) * g.nc[0] + cx;
+    const int cnt = a.cellCount[cell];
+    if (cnt == 0 || cnt > kCellCap) return;
+    __shared__ SwitchShared sh;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    stageStencil<kSwThreads>(a, cx, cy, cz, sh.st, sh.scan);
+    const Control& ctl = *a.ctl;
+    const uint32_t sk = (uint32_t)ctl.sweep ^ ((uint32_t)(ctl.sweep >> 32) << 20);
+    const uint64_t seed = a.seed ^ 0x5851F42D4C957F2Dull;
+    int nAtt;
+    {
+        Stream r(seed, (uint32_t)cell, 0xFFFFFFFFu, sk);
+        const double want = cnt * a.switchRate;
+        nAtt = (int)want;
+        if (r.next() < want - nAtt) ++nAtt;
+    }
+    DevCtx c;
+    c.params = a.t.params; c.mols = a.t.mols; c.ntypes = a.t.ntypes; c.n = a.s.n; c.sqmaxcut = a.t.sqmaxcut;
+    const double3 box = mk(a.s.box[0], a.s.box[1], a.s.box[2]);
+    double dE = 0.0;
+    unsigned long long nAcc = 0, nRej = 0;
+    for (int m = 0; m < nAtt; ++m) {
+        if (tid == 0) {
+            Stream r(seed, (uint32_t)cell, (uint32_t)m, sk);
+            const int slot = min((int)(r.next() * cnt), cnt - 1);
+            const int t = a.cellIdx[a.cellStart[cell] + slot];
+            const int4 mol = a.s.mol[t];
+            const int4 sw = mol.y < MAXCHL ? a.swTab[mol.x * MAXCHL + mol.y] : make_int4(-1, -1, 0, 0);
+            sh.go = 0;
+            if (sw.y >= 0) {
+                const double4_32a d = a.s.dir[t];
+                const int switched = d.w != 0.0 ? 1 : 0;
+                sh.go = 1;
+                sh.target = t;
+                sh.switched = switched;
+                sh.oldType = (int)a.s.pos[t].w;
+                sh.newType = switched ? sw.x : sw.y;
+                sh.dmu = sw.z;
+                double dir[3] = {d.x, d.y, d.z};
+                PatchSet P = a.s.patch[t];
+                gcInitParticle(a.tinit[sh.newType], dir, P);
+                for (int q = 0; q < 3; ++q) sh.dirNew[q] = dir[q];
+                sh.newP = P;
+                gcInitParticle(a.tinit[sh.oldType], dir, P);     // the reject path: init again, old type
+                for (int q = 0; q < 3; ++q) sh.dirOld[q] = dir[q];
+                sh.oldP = P;
+                sh.u = r.next();
+            }
+        }
+        __syncthreads();
+        if (sh.go) {
+            const int t = sh.target;
+            const double4_32a p = a.s.pos[t], d = a.s.dir[t];
+            const int4 mol = a.s.mol[t];
+            PView vo, vn;
+            vo.pos = vn.pos = mk(p.x, p.y, p.z);
+            vo.dir = mk(d.x, d.y, d.z);
+            vn.dir = mk(sh.dirNew[0], sh.dirNew[1], sh.dirNew[2]);
+            vo.patch = &a.s.patch[t];
+            vn.patch = &sh.newP;
+            vo.type = sh.oldType;
+            vn.type = sh.newType;
+            vo.index = vn.index = t;
+            vo.molType = vn.molType = mol.x;
+            const Con con = makeCon(c, t, mol);
+            double eo = 0.0, en = 0.0;
+            int partners = 0;
+            for (int k = tid; k < sh.st.nCand; k += kSwThreads) {
+                int lo = 0, hi = sh.st.nNb;          // nbOff[lo] <= k < nbOff[hi]
+                while (hi - lo > 1) {
+                    const int mid = (lo + hi) >> 1;
+                    if (sh.st.nbOff[mid] <= k) lo = mid;
+                    else hi = mid;
+                }
+                const int j = a.cellIdx[a.cellStart[sh.st.nbCell[lo]] + (k - sh.st.nbOff[lo])];
+                if (j == t) continue;
+                const double4_32a q = a.s.pos[j], e = a.s.dir[j];
+                PView b;
+                b.pos = mk(q.x, q.y, q.z);
+                b.dir = mk(e.x, e.y, e.z);
+                b.patch = &a.s.patch[j];
+                b.type = (int)q.w;
+                b.index = j;
+                b.molType = a.s.mol[j].x;
+                unsigned bits;
+                double dsq;
+                eo += pairEnergy(c, vo, b, con, box, &bits, &dsq);
+                en += pairEnergy(c, vn, b, con, box, &bits, &dsq);
+                partners += (j == con.idx[0]) + (j == con.idx[1]) + (j == con.idx[2]) + (j == con.idx[3]);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                eo += __shfl_down_sync(0xffffffffu, eo, o);
+                en += __shfl_down_sync(0xffffffffu, en, o);
+                partners += __shfl_down_sync(0xffffffffu, partners, o);
+            }
+            if (lane == 0) { sh.redO[warp] = eo; sh.redN[warp] = en; sh.redP[warp] = partners; }
+            __syncthreads();
+            if (tid == 0) {
+                double Eo = 0.0, En = 0.0;
+                int found = 0;
+                for (int w = 0; w < kSwThreads / 32; ++w) { Eo += sh.redO[w]; En += sh.redN[w]; found += sh.redP[w]; }
+                const int want = (con.idx[0] >= 0) + (con.idx[1] >= 0) + (con.idx[2] >= 0) + (con.idx[3] >= 0);
+                if (found < want) {             // a bonded partner outside the stencil: no decision
+                    atomicOr(a.err, E_PARTNER_FAR);
+                } else {
+                    const int pmone = 1 - 2 * sh.switched;
+                    const double enew = En + (double)(sh.dmu * pmone);
+                    const bool acc = (enew <= Eo) || (exp(-1.0 * (enew - Eo) / a.temper) > sh.u);
+                    if (acc) {
+                        a.s.pos[t] = make_double4_32a(p.x, p.y, p.z, (double)sh.newType);
+                        a.s.dir[t] = make_double4_32a(sh.dirNew[0], sh.dirNew[1], sh.dirNew[2],
+                                                      (double)(sh.switched + pmone));
+                        a.s.patch[t] = sh.newP;
+                        dE += En - Eo;
+                        ++nAcc;
+                    } else {
+                        a.s.dir[t] = make_double4_32a(sh.dirOld[0], sh.dirOld[1], sh.dirOld[2], d.w);
+                        a.s.patch[t] = sh.oldP;
+                        ++nRej;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        a.cellDE[cell] += dE;
+        if (nAcc) atomicAdd(&a.counters[C_ACC_SW], nAcc);
+        if (nRej) atomicAdd(&a.counters[C_REJ_SW], nRej);
+    }
+}
+
 }  // namespace
 
 // Device state of the move loop of one system.
@@ -3115,6 +3296,7 @@ struct SweepEngine {
     bool energyKnown = false;
     unsigned long long* typeCtr = nullptr;        // per-type acceptance of the run (SweepArgs::typeCtr)
     GcDev* gc = nullptr;          // grand-canonical record (kGrandCanon)
+    TypeInit* tinit = nullptr;    // Particle::init parameters per compact type
     bool gcOn = false;            // this run makes grand-canonical moves
     int slots = 0;                // particle slots of the per-particle buffers below and of the chain phase
     uint64_t seed = ~0ull;
@@ -3150,6 +3332,7 @@ struct Batch {
     // chain phase (every system of the batch holds chains, or none does)
     bool chains = false;
     bool wl = false;          // a system carries a Wang-Landau bias
+    bool switching = false;   // a system makes type switch moves
     std::vector<SweepArgs> hArgsC;
     SweepArgs* dArgsC = nullptr;
     int nArgsCAlloc = 0;
@@ -3159,7 +3342,7 @@ struct Batch {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<cudaEvent_t> evPhase;     // time_phases: start / end of each sweep's move launches
     cudaGraphExec_t graph = nullptr;
-    int graphDims[15] = {0};   // launch shape the graph was captured with
+    int graphDims[16] = {0};   // launch shape the graph was captured with
     long graphLaunches = 0, graphPhaseLaunches = 0;
     // parallel tempering
     int* dLadder = nullptr;
@@ -3348,6 +3531,20 @@ static void fillArgs(Context* c, SweepEngine* e, const sc_run_params& p) {
     a.coneAngle = c->opts.coneAngle;
     for (int m = 0; m < kMaxChainTypes; ++m) a.chainMxType[m] = chainStep(c, m, p);
     a.gc = e->gcOn ? e->gc : nullptr;
+    a.tinit = e->tinit;
+    // type switching: N switchprob attempts per sweep spread over the switchable particles
+    // (each cell makes cnt * rate attempts on random particles of the cell)
+    a.swTab = nullptr;
+    a.switchRate = 0.0;
+    if (p.switchprob > 0.0 && c->anySwitch) {
+        long nsw = 0;
+        for (const int4& mi : c->molInfo)
+            if (mi.y < MAXCHL && c->switchTab[(size_t)mi.x * MAXCHL + mi.y].y >= 0) ++nsw;
+        if (nsw > 0) {
+            a.swTab = c->dSwitch;
+            a.switchRate = p.switchprob * (double)c->d.n / (double)nsw;
+        }
+    }
 }
 
 // Chain phase of one system: chains (molecules of more than one particle), the bound R of
@@ -3465,16 +3662,10 @@ static int prepareGrand(Context* c, SweepEngine* e, const sc_run_params& p) {
     h.chainprob = p.chainprob;
     for (int k = 0; k < h.nSpecies; ++k) {
         const Context::Grand& g = c->grand[k];
-        const IaParam& ia = c->topo.ia[g.type][g.type];
         GcSpecies& sp = h.sp[k];
         sp.molType = g.molType;
         sp.ctype = c->compactOf[g.type];
-        sp.geo = ia.geotype[0];
         sp.chemPot = g.chemPot;
-        sp.pcos0 = ia.pcoshalfi[0]; sp.psin0 = ia.psinhalfi[0];
-        sp.pcos2 = ia.pcoshalfi[2]; sp.psin2 = ia.psinhalfi[2];
-        sp.csec = ia.csecpatchrot[0]; sp.ssec = ia.ssecpatchrot[0];
-        sp.chcos = ia.chiral_cos[0]; sp.chsin = ia.chiral_sin[0];
     }
     for (int m = 0; m <= h.molTypeCount; ++m) h.first[m] = c->conf.first[m];
     cudaError_t r = cudaMemcpy(e->gc, &h, sizeof h, cudaMemcpyHostToDevice);
@@ -3556,6 +3747,18 @@ static int prepareSystem(Context* c, const sc_run_params& p, bool npt) {
         if ((rc = engineAlloc(e, (void**)&e->counters, sizeof(unsigned long long) * C_COUNT))) return rc;
         if ((rc = engineAlloc(e, (void**)&e->err, sizeof(int)))) return rc;
         if ((rc = engineAlloc(e, (void**)&e->typeCtr, sizeof(unsigned long long) * kTypeCtrCount))) return rc;
+        if ((rc = engineAlloc(e, (void**)&e->tinit, sizeof(TypeInit) * MAX_DEV_TYPES))) return rc;
+        TypeInit ti[MAX_DEV_TYPES];
+        std::memset(ti, 0, sizeof ti);
+        for (size_t k = 0; k < c->usedTypes.size() && k < (size_t)MAX_DEV_TYPES; ++k) {
+            const IaParam& ia = c->topo.ia[c->usedTypes[k]][c->usedTypes[k]];
+            ti[k].geo = ia.geotype[0];
+            ti[k].pcos0 = ia.pcoshalfi[0]; ti[k].psin0 = ia.psinhalfi[0];
+            ti[k].pcos2 = ia.pcoshalfi[2]; ti[k].psin2 = ia.psinhalfi[2];
+            ti[k].csec = ia.csecpatchrot[0]; ti[k].ssec = ia.ssecpatchrot[0];
+            ti[k].chcos = ia.chiral_cos[0]; ti[k].chsin = ia.chiral_sin[0];
+        }
+        cudaMemcpy(e->tinit, ti, sizeof ti, cudaMemcpyHostToDevice);
         Control z;
         std::memset(&z, 0, sizeof z);
         cudaMemcpy(e->ctl, &z, sizeof z, cudaMemcpyHostToDevice);
@@ -3606,7 +3809,11 @@ static int uploadArgs(Batch& b) {
     cudaError_t r = cudaMemcpy(b.dArgs, b.hArgs.data(), sizeof(SweepArgs) * ns, cudaMemcpyHostToDevice);
     if (r != cudaSuccess) return cudaFail(r, "upload sweep arguments");
     b.wl = false;
-    for (const SweepArgs& h : b.hArgs) b.wl |= (h.wl != nullptr);
+    b.switching = false;
+    for (const SweepArgs& h : b.hArgs) {
+        b.wl |= (h.wl != nullptr);
+        b.switching |= (h.swTab != nullptr);
+    }
     int on = 0;
     for (Context* c : b.sys) on += c->engine->ch.on ? 1 : 0;
     if (on != 0 && on != ns) return fail(SC_ERR_UNSUPPORTED, "chain moves need every system of a batch to hold chains");
@@ -3666,6 +3873,8 @@ static void collectStats(Context* c, sc_run_stats& st) {
     st.da_stage1_rejected = (long)ctr[C_S1_REJ];
     st.da_stage2_tried = (long)ctr[C_S2_TRIED];
     st.da_stage2_rejected = (long)ctr[C_S2_REJ];
+    st.acc_switch = (long)ctr[C_ACC_SW];
+    st.rej_switch = (long)ctr[C_REJ_SW];
     st.da_err_rms = ctr[C_S2_TRIED] ? std::sqrt(hc.daErr2 / (double)ctr[C_S2_TRIED]) : 0.0;
     st.da_err_mean = ctr[C_S2_TRIED] ? hc.daErrSum / (double)ctr[C_S2_TRIED] : 0.0;
     st.energy = hc.energy;
@@ -3825,6 +4034,11 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
             ++phaseEvents;
         }
         if (timed || !timing) phaseLaunches += flow ? 1 : b.maxColours;
+        if (b.switching) {      // type switch moves: a checkerboard phase over the same cells
+            for (int ph = 0; ph < b.maxColours; ++ph)
+                kSwitchColour<<<dims(b.maxActive), kSwThreads, 0, s>>>(b.dArgs, ph);
+            launches += b.maxColours;
+        }
         if (b.wl) {         // Wang-Landau: the cells of the order parameters' particles, last
             kWlCells<<<dims(1), kMoveThreads, kDynSmemColour, s>>>(b.dArgs);
             launches += 1;
@@ -3901,9 +4115,9 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
         bool aligned = (sw % G == 0) && (nextExchange < 0 || nextExchange - sw >= G) && (nextWl < 0 || nextWl - sw >= G) &&
                        (nextGc < 0 || nextGc - sw >= G);
         if (useGraph && left >= G && aligned) {
-            int key[15] = {ns, b.maxN, b.maxCells, b.maxActive, b.maxColours, (int)G, anySurrogate ? 1 : 0,
+            int key[16] = {ns, b.maxN, b.maxCells, b.maxActive, b.maxColours, (int)G, anySurrogate ? 1 : 0,
                            b.chains ? 1 : 0, b.maxCellsC, b.maxActiveC, b.maxColoursC, dense ? 1 : 0, flow ? 1 : 0,
-                           b.wl ? 1 : 0, warpCells ? 1 : 0};
+                           b.wl ? 1 : 0, warpCells ? 1 : 0, b.switching ? 1 : 0};
             if (!b.graph || std::memcmp(key, b.graphDims, sizeof key) != 0) {
                 if (b.graph) { cudaGraphExecDestroy(b.graph); b.graph = nullptr; }
                 cudaGraph_t graph;
@@ -4035,6 +4249,7 @@ static int checkParams(const sc_run_params& p) {
     if (p.flow_wait_polls < 0) return fail(SC_ERR_ARG, "flow_wait_polls must be >= 0");
     if (p.grand_every < 0) return fail(SC_ERR_ARG, "grand_every must be >= 0");
     if (p.sweep_offset < 0) return fail(SC_ERR_ARG, "sweep_offset must be >= 0");
+    if (!(p.switchprob >= 0.0)) return fail(SC_ERR_ARG, "switchprob must be >= 0");
     return SC_OK;
 }
 
@@ -4059,6 +4274,9 @@ int runSweeps(Context* c, const sc_run_params& p0, sc_run_stats& st) {
     if (c->conf.p.empty() && !grandRun) return SC_OK;     // an empty grand-canonical box can fill up
     if (grandRun && wlActive(c))
         return fail(SC_ERR_UNSUPPORTED, "grand-canonical moves with Wang-Landau weights are outside the GPU path");
+    if (p.switchprob > 0.0 && c->anySwitch && wlActive(c))
+        return fail(SC_ERR_UNSUPPORTED, "type switch moves with Wang-Landau weights (WangLandau::runSwitch) are outside the "
+                                        "GPU path");
     if (p.delayed && !c->surrogate) return fail(SC_ERR_STATE, "delayed = 1 needs a surrogate (sc_set_surrogate)");
     if ((rc = checkMoves(c))) return rc;
     if ((rc = wlCheckRun(c, p))) return rc;
@@ -4260,6 +4478,7 @@ int equilibrate(Context* c, const sc_run_params& p, long nequil, long adjust, sc
         st.pairs_tested += s1.pairs_tested; st.pairs_evaluated += s1.pairs_evaluated;
         st.seconds += s1.seconds; st.launches += s1.launches;
         st.energy = s1.energy; st.energy_check = s1.energy_check; st.max_drift = std::max(st.max_drift, s1.max_drift);
+        st.acc_switch += s1.acc_switch; st.rej_switch += s1.rej_switch;
         st.acc_insert += s1.acc_insert; st.rej_insert += s1.rej_insert;
         st.acc_delete += s1.acc_delete; st.rej_delete += s1.rej_delete;
         st.particles = s1.particles;
@@ -4317,6 +4536,7 @@ int tuneSweeps(Context* c, const sc_run_params& p, int sweeps, sc_run_params& be
             q.check_every = 0;
             q.time_phases = 0;
             q.grand_every = 0;                 // the candidates move the same particles
+            q.switchprob = 0.0;
             q.nsweeps = 2;                     // grid, graph capture, caches
             sc_run_stats st;
             double rate = 0.0;
@@ -4420,6 +4640,7 @@ int runReplicas(void* h, const sc_run_params& p0, int exchangeEvery, sc_run_stat
         q.stencil = p.stencil; q.time_phases = p.time_phases; q.press = p.press; q.delayed = p.delayed;
         q.variant = p.variant;
         q.grand_every = 0;
+        q.switchprob = c->anySwitch ? p.switchprob : 0.0;
         if (p.delayed && !c->surrogate) return fail(SC_ERR_STATE, "delayed = 1 needs a surrogate on every replica");
         if ((rc = wlCheckRun(c, q))) return rc;
         if ((q.variant & 8) && wlActive(c))
@@ -4461,6 +4682,7 @@ int runReplicas(void* h, const sc_run_params& p0, int exchangeEvery, sc_run_stat
         st.acc_rot += s1.acc_rot; st.rej_rot += s1.rej_rot;
         st.acc_vol += s1.acc_vol; st.rej_vol += s1.rej_vol; st.vol_constrained += s1.vol_constrained;
         st.acc_chain += s1.acc_chain; st.rej_chain += s1.rej_chain;
+        st.acc_switch += s1.acc_switch; st.rej_switch += s1.rej_switch;
         st.pairs_tested += s1.pairs_tested; st.pairs_evaluated += s1.pairs_evaluated;
         st.da_stage1_rejected += s1.da_stage1_rejected;
         st.da_stage2_tried += s1.da_stage2_tried;

@@ -145,6 +145,28 @@ def cases():
                            np.vstack([rand_perp(rng, rand_unit(rng, 20)), qs])),
         opts=dict(temper=1.0, transmx=0.5, rotmx=30.0, nGrandCanon=1, pairlist_update=0),
         nsweeps=24000, report=20, seeds=8, burn=4000, gc=True)
+    # type switching (switchTypeMove): PSC particles that switch to a CPSC type and back with a
+    # chemical-potential difference of 1.6 (read as the int 1 by the reference), beside fixed
+    # spheres; the switched fraction from the movie frames' switched column
+    box = np.full(3, 16.0)
+    ps, ds, qs = place(rng, 150, box, L)
+    sp = []
+    while len(sp) < 50:
+        p = rng.uniform(0, 1, 3) * box
+        if all(np.linalg.norm((p - q) - box * np.round((p - q) / box)) > 1.2 for q in sp) and all(
+                seg_dist(p, np.array([0.0, 0.0, 1.0]), p + ((q - p) - box * np.round((q - p) / box)), d, L) > 1.2
+                for q, d in zip(ps, ds)):
+            sp.append(p)
+    sp = np.array(sp)
+    out["switch_psc"] = dict(
+        top=top_text([("P", 1, "PSC", [1.0, 1.0, 1.12, 0.2, 90.0, 10.0, L, 0.0]),
+                      ("Q", 2, "CPSC", [1.0, 1.0, 1.12, 0.2, 120.0, 10.0, L, 0.0]),
+                      ("A", 3, "SPA", [0.5, 1.0, 1.1225, 0.3775])],
+                     [("P", ["1 2 1.6"], []), ("A", [3], [])], [("P", 150), ("A", 50)]),
+        config=config_text(box, np.vstack([ps, sp]), np.vstack([ds, rand_unit(rng, 50)]),
+                           np.vstack([qs, rand_perp(rng, rand_unit(rng, 50))])),
+        opts=dict(temper=1.0, transmx=0.35, rotmx=30.0, switchprob=0.1, pairlist_update=0),
+        nsweeps=24000, report=20, seeds=12, burn=3000, switch_rows=150)
     return out
 
 
@@ -200,7 +222,7 @@ def run_one(c, seed):
         opts = dict(OPTION_KEYS)
         opts.update(c["opts"])
         opts.update(nsweeps=c["nsweeps"], report=c["report"], seed=seed, paraltemper=opts["temper"])
-        if c.get("s2") or c.get("gc"):
+        if c.get("s2") or c.get("gc") or c.get("switch_rows"):
             opts.update(movie=c["report"])
         with open(os.path.join(tmp, "options"), "w") as f:
             f.write("".join(f"{k} = {v}\n" for k, v in opts.items()))
@@ -227,7 +249,23 @@ def run_one(c, seed):
             s2 = movie_s2(os.path.join(tmp, "movie"), slice(0, n_sc))
         if c.get("gc"):
             counts = movie_counts(os.path.join(tmp, "movie"))
-        return dict(seed=seed, energy=e, volume=vol, s2=s2, counts=counts)
+        switched = []
+        if c.get("switch_rows"):
+            switched = movie_switched(os.path.join(tmp, "movie"), c["switch_rows"])
+        return dict(seed=seed, energy=e, volume=vol, s2=s2, counts=counts, switched=switched)
+
+
+def movie_switched(path, rows):
+    """(sweep, fraction of the first `rows` particles marked switched) of every movie frame."""
+    lines = open(path).read().splitlines()
+    out, k = [], 0
+    while k < len(lines):
+        n = int(lines[k].split()[0])
+        sweep = int(lines[k + 1].split(";")[0].split()[1])
+        flags = [int(r.split()[9]) for r in lines[k + 2: k + 2 + rows]]
+        out.append((sweep, sum(flags) / rows))
+        k += 2 + n
+    return out
 
 
 def movie_counts(path):
@@ -271,6 +309,8 @@ def main():
                       ("particles", [[(s, float(k)) for s, k in r["counts"]] for r in runs])]
         if c.get("s2"):
             series.append(("nematic_s2", [r["s2"] for r in runs]))
+        if c.get("switch_rows"):
+            series = series[:1] + [("switched_fraction", [r["switched"] for r in runs])]
         stats = {k: block_stats(ser, c["burn"]) for k, ser in series}
         out = dict(name=name, n=n, inputs={"top.init": c["top"], "config.init": c["config"]}, options=c["opts"],
                    nsweeps=c["nsweeps"], report=c["report"], burn=c["burn"], seeds=c["seeds"],
