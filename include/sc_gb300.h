@@ -98,7 +98,8 @@ typedef struct {
                                0.2 s; a wait in a sound run lasts well under 20 ms) */
     int grand_every;        /* sweeps between grand-canonical insert / delete moves (options
                                nGrandCanon; MoveCreator::muVTMove, movecreator.cpp:797-924); 0: none.
-                               Needs top.init ACTIVITY species; sc_simulate / sc_equilibrate only */
+                               Needs top.init ACTIVITY species; replicas add the grand-canonical
+                               term to their exchanges (movecreator.cpp:728-734) */
     long sweep_offset;      /* sweeps the caller's loop ran before this call: a move due every
                                grand_every sweeps follows sweep k of the loop when k % grand_every
                                == 0 (updater.cpp:165), k counted from the loop's start */

@@ -2800,6 +2800,8 @@ __global__ void kCheckEnergy(const SweepArgs* __restrict__ A) {
 // at rank k (colder) and the one at rank k+1 is accepted with
 // min(1, exp((1/T_k - 1/T_k+1)(E_k - E_k+1) + (P_k/T_k - P_k+1/T_k+1)(V_k - V_k+1))),
 // the canonical plus isobaric rule of the reference (the pressure term vanishes in NVT).
+__device__ double gcExchangeTerm(const SweepArgs& ai, const SweepArgs& aj, double Ti, double Tj);
+
 __global__ void kExchange(SweepArgs* A, SweepArgs* AC, int* ladder, const int* ladderStart, int nLadders,
                           uint64_t seed, unsigned long long* ctr) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
@@ -2818,6 +2820,7 @@ __global__ void kExchange(SweepArgs* A, SweepArgs* AC, int* ladder, const int* l
             // canonical and isobaric terms of movecreator.cpp:721-727
             double delta = (1.0 / Ti - 1.0 / Tj) * (Ei - Ej);
             delta += (A[ri].press / Ti - A[rj].press / Tj) * (Vi - Vj);
+            delta += gcExchangeTerm(A[ri], A[rj], Ti, Tj);     // grand-canonical term (movecreator.cpp:728-734)
             double u = r.next();
             ctr[1 + 2 * k] += 1ull;
             if (delta >= 0.0 || exp(delta) > u) {
@@ -2871,6 +2874,22 @@ struct GcDev {
     unsigned long long ctr[kMaxGrandSpecies][5];      // steps, insert acc / rej, delete acc / rej
     double countSum[kMaxGrandSpecies];                // Statistics::grand muVtAverageParticles
 };
+
+// The grand-canonical term of the exchange criterion (movecreator.cpp:728-734): for every
+// species, (1/T_i - 1/T_j) chemPot T_i (N_i - N_j), chemPot and the species those of system
+// i (the replicas share one topology), the counts each system's own.
+__device__ double gcExchangeTerm(const SweepArgs& ai, const SweepArgs& aj, double Ti, double Tj) {
+    if (!ai.gc || !aj.gc) return 0.0;
+    const GcDev& gi = *ai.gc;
+    const GcDev& gj = *aj.gc;
+    double t = 0.0;
+    for (int k = 0; k < gi.nSpecies; ++k) {
+        const int m = gi.sp[k].molType;
+        const double ni = gi.first[m + 1] - gi.first[m], nj = gj.first[m + 1] - gj.first[m];
+        t += (1.0 / Ti - 1.0 / Tj) * gi.sp[k].chemPot * Ti * (ni - nj);
+    }
+    return t;
+}
 
 // Vector::rotate(axis, cos, sin) (Vector.h:133-157): v turned about a unit axis.
 __device__ __forceinline__ void gcRotate(double (&v)[3], const double (&ax)[3], double c, double s) {
@@ -3297,6 +3316,7 @@ struct SweepEngine {
     unsigned long long* typeCtr = nullptr;        // per-type acceptance of the run (SweepArgs::typeCtr)
     GcDev* gc = nullptr;          // grand-canonical record (kGrandCanon)
     TypeInit* tinit = nullptr;    // Particle::init parameters per compact type
+    sc_run_params runParams{};    // the parameters the system's arguments were filled from
     bool gcOn = false;            // this run makes grand-canonical moves
     int slots = 0;                // particle slots of the per-particle buffers below and of the chain phase
     uint64_t seed = ~0ull;
@@ -3706,29 +3726,55 @@ static int finishGrand(Context* c, const SweepArgs* dArgs) {
 
 // A grand-canonical system whose free slots ran out: larger state arrays and per-particle
 // buffers, and the arguments (with the device's count) uploaded again.
-static int uploadArgs(Batch& b);
+// The device copy of a batch's arguments runs ahead of the host's during a run: replica
+// exchange swaps temperatures, grand-canonical moves change the particle count (and the chain
+// phase's share of moves).  Brings the host copies (and every context's count) up to it, so
+// that an upload keeps them (the stream is synchronised).
+static int syncDeviceArgs(Batch& b) {
+    const int ns = (int)b.sys.size();
+    std::vector<SweepArgs> cur(ns), curC;
+    cudaError_t r = cudaMemcpy(cur.data(), b.dArgs, sizeof(SweepArgs) * ns, cudaMemcpyDeviceToHost);
+    if (r == cudaSuccess && b.chains) {
+        curC.resize(ns);
+        r = cudaMemcpy(curC.data(), b.dArgsC, sizeof(SweepArgs) * ns, cudaMemcpyDeviceToHost);
+    }
+    if (r != cudaSuccess) return cudaFail(r, "sweep arguments");
+    for (int k = 0; k < ns; ++k) {
+        SweepEngine* e = b.sys[k]->engine;
+        e->args.temper = cur[k].temper;
+        e->args.s.n = cur[k].s.n;
+        b.sys[k]->d.n = cur[k].s.n;
+        e->runParams.temper = cur[k].temper;
+        if (b.chains) {
+            e->ch.args.temper = curC[k].temper;
+            e->ch.args.s.n = curC[k].s.n;
+            e->ch.args.chainFrac = curC[k].chainFrac;
+        }
+    }
+    return SC_OK;
+}
 
-static int growSystem(Context* c, Batch& b, const SweepArgs& cur, const sc_run_params& p) {
+// A grand-canonical system whose free slots ran out (its host arguments synchronised):
+// larger state arrays and per-particle buffers, the new pointers in its arguments.  The
+// caller uploads the batch's arguments afterwards.
+static int growSystem(Context* c) {
     SweepEngine* e = c->engine;
-    c->d.n = cur.s.n;
     const int newCap = std::max(2 * c->cap, c->cap + 256);
     int rc;
     if ((rc = c->grow(newCap))) return rc;
     if ((rc = particleBuffers(e, newCap))) return rc;
     SweepArgs& a = e->args;
     a.s = c->d;
-    a.temper = cur.temper;
     a.cellIdx = e->cellIdx; a.cellPosF = e->cellPosF; a.cellDirF = e->cellDirF; a.cellPatF = e->cellPatF;
     a.cellOf = e->cellOf;
     if (e->ch.on) {
         SweepArgs& ac = e->ch.args;
         ac.s = c->d;
         ac.cellIdx = e->ch.cellIdx; ac.cellOf = e->ch.cellOf; ac.slotOf = e->ch.slotOf; ac.cellPosF = e->ch.cellPosF;
-        if (ac.nChains > 0) ac.chainFrac = p.chainprob * (double)c->d.n / (double)ac.nChains;
     }
     cudaError_t r = cudaMemcpy(&e->gc->cap, &newCap, sizeof newCap, cudaMemcpyHostToDevice);
     if (r != cudaSuccess) return cudaFail(r, "grand-canonical capacity");
-    return uploadArgs(b);
+    return SC_OK;
 }
 
 // Device state, grid and arguments of one system for a run with parameters p.
@@ -3779,6 +3825,7 @@ static int prepareSystem(Context* c, const sc_run_params& p, bool npt) {
     e->stencil = chooseStencil(box, c->topo.maxcut, p.stencil == 0 && wlActive(c) ? 1 : p.stencil);
     if ((rc = ensureGrid(c, e, box))) return rc;
     if ((rc = prepareGrand(c, e, p))) return rc;
+    e->runParams = p;
     fillArgs(c, e, p);
     if ((rc = prepareChains(c, e, p, box))) return rc;
     cudaMemset(e->counters, 0, sizeof(unsigned long long) * C_COUNT);
@@ -4085,9 +4132,12 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
     if (exchangeEvery > 0) G = std::max(1L, std::min(G, (long)exchangeEvery));
     // grand-canonical moves: after every grand_every-th sweep of the call (updater.cpp:164-165),
     // between the captured blocks; the host keeps a free slot for every insertion
-    const bool gc = p.grand_every > 0 && ns == 1 && b.hArgs[0].gc != nullptr;
+    std::vector<long> nUpper(ns, -1);      // bound on each grand-canonical system's device count
+    bool gc = false;
+    if (p.grand_every > 0)
+        for (int k = 0; k < ns; ++k)
+            if (b.hArgs[k].gc) { gc = true; nUpper[k] = b.hArgs[k].s.n; }
     long nextGc = gc ? p.grand_every - (long)(p.sweep_offset % p.grand_every) : -1;
-    long nUpper = gc ? b.hArgs[0].s.n : 0;     // bound on the device's count
     if (gc) G = std::max(1L, std::min(G, (long)p.grand_every));
     const bool useGraph = !p.time_phases;
     const long chunk = 48;
@@ -4160,18 +4210,26 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
         }
         if (nextGc > 0 && sw >= nextGc) {
             while (nextGc <= sw) nextGc += p.grand_every;
-            Context* c = b.sys[0];
-            if (nUpper + 1 > c->cap) {
+            bool full = false;
+            for (int k = 0; k < ns; ++k) full |= nUpper[k] >= 0 && nUpper[k] + 1 > b.sys[k]->cap;
+            if (full) {          // read the counts; grow the systems that have no free slot
                 if ((r = cudaStreamSynchronize(s)) != cudaSuccess) return cudaFail(r, "sweep");
-                SweepArgs cur;
-                if ((r = cudaMemcpy(&cur, b.dArgs, sizeof cur, cudaMemcpyDeviceToHost)) != cudaSuccess)
-                    return cudaFail(r, "sweep arguments");
-                nUpper = cur.s.n;
-                if (nUpper + 1 > c->cap && (rc = growSystem(c, b, cur, p))) return rc;
+                if ((rc = syncDeviceArgs(b))) return rc;
+                bool grown = false;
+                for (int k = 0; k < ns; ++k) {
+                    if (nUpper[k] < 0) continue;
+                    nUpper[k] = b.sys[k]->d.n;
+                    if (nUpper[k] + 1 > b.sys[k]->cap) {
+                        if ((rc = growSystem(b.sys[k]))) return rc;
+                        grown = true;
+                    }
+                }
+                if (grown && (rc = uploadArgs(b))) return rc;
             }
             kGrandCanon<<<dims(1), kGcThreads, 0, s>>>(b.dArgs, b.chains ? b.dArgsC : nullptr);
             launches += 1;
-            nUpper += 1;
+            for (int k = 0; k < ns; ++k)
+                if (nUpper[k] >= 0) nUpper[k] += 1;
         }
         if (nextCheck > 0 && sw >= nextCheck) {
             // the cell list (box fractions) stays valid after an accepted volume move
@@ -4182,6 +4240,8 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
             // the box changed on the device: re-derive the cell grids when needed
             while (nextRegrid <= sw) nextRegrid += chunk;
             if ((r = cudaStreamSynchronize(s)) != cudaSuccess) return cudaFail(r, "sweep");
+            // an upload below must keep the device's temperatures and counts, for every system
+            if ((rc = syncDeviceArgs(b))) return rc;
             bool changed = false;
             for (int k = 0; k < ns; ++k) {
                 Context* c = b.sys[k];
@@ -4192,17 +4252,10 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
                 const bool mainChanged = ng.nc[0] != e->g.nc[0] || ng.nc[1] != e->g.nc[1] || ng.nc[2] != e->g.nc[2];
                 if (mainChanged || e->ch.on) {
                     if (mainChanged && (rc = ensureGrid(c, e, box))) return rc;
-                    // keep the device-side temperature (replica exchange may have changed it)
-                    SweepArgs cur;
-                    cudaMemcpy(&cur, b.dArgs + k, sizeof cur, cudaMemcpyDeviceToHost);
-                    double T = cur.temper;
-                    c->d.n = cur.s.n;            // grand-canonical moves change it on the device
-                    sc_run_params q = p;
-                    q.seed = e->args.seed;
-                    q.temper = T;
+                    // the system's own parameters, at the temperature it has now
+                    sc_run_params q = e->runParams;
                     Grid oldC = e->ch.g;
                     fillArgs(c, e, q);
-                    e->args.temper = T;
                     if (e->ch.on) {
                         if ((rc = prepareChains(c, e, q, box))) return rc;
                         changed |= e->ch.g.nc[0] != oldC.nc[0] || e->ch.g.nc[1] != oldC.nc[1] ||
@@ -4619,9 +4672,6 @@ int runReplicas(void* h, const sc_run_params& p0, int exchangeEvery, sc_run_stat
     // a batch has no tuned choice of its own: variant -1 is the dataflow sweep
     sc_run_params p = p0;
     if (p.variant < 0) p.variant = 4;
-    if (p.grand_every > 0)
-        return fail(SC_ERR_UNSUPPORTED, "grand-canonical moves in replica exchange (the exchange would need the "
-                                        "chemical-potential terms, movecreator.cpp:728-734): use sc_simulate");
     Batch& b = R->b;
     const int nrep = (int)b.sys.size();
     const bool npt = p.volume_every > 0;
@@ -4639,7 +4689,17 @@ int runReplicas(void* h, const sc_run_params& p0, int exchangeEvery, sc_run_stat
         q.temper = R->temps[k]; q.ptype = p.ptype; q.volume_every = p.volume_every; q.check_every = p.check_every;
         q.stencil = p.stencil; q.time_phases = p.time_phases; q.press = p.press; q.delayed = p.delayed;
         q.variant = p.variant;
-        q.grand_every = 0;
+        q.grand_every = c->grand.empty() ? 0 : p.grand_every;
+        q.sweep_offset = p.sweep_offset;
+        if (q.grand_every > 0) {          // the exchange reads the species of one replica for both
+            const Context* c0 = b.sys[0];
+            bool same = c0->grand.size() == c->grand.size();
+            for (size_t g = 0; same && g < c->grand.size(); ++g)
+                same = c0->grand[g].molType == c->grand[g].molType && c0->grand[g].chemPot == c->grand[g].chemPot;
+            if (!same) return fail(SC_ERR_UNSUPPORTED, "grand-canonical replicas need the same species and activities");
+            if (wlActive(c))
+                return fail(SC_ERR_UNSUPPORTED, "grand-canonical moves with Wang-Landau weights are outside the GPU path");
+        }
         q.switchprob = c->anySwitch ? p.switchprob : 0.0;
         if (p.delayed && !c->surrogate) return fail(SC_ERR_STATE, "delayed = 1 needs a surrogate on every replica");
         if ((rc = wlCheckRun(c, q))) return rc;
@@ -4670,7 +4730,12 @@ int runReplicas(void* h, const sc_run_params& p0, int exchangeEvery, sc_run_stat
     }
     if ((rc = uploadArgs(b))) return rc;
     RunOut out;
-    if ((rc = runBatch(b, p, p.nsweeps, exchangeEvery, p.seed ^ 0xA5A5A5A5ull, out))) return rc;
+    rc = runBatch(b, p, p.nsweeps, exchangeEvery, p.seed ^ 0xA5A5A5A5ull, out);
+    for (int k = 0; k < nrep; ++k) {     // the device's particle vectors (grand-canonical moves)
+        const int rcG = finishGrand(b.sys[k], b.dArgs + k);
+        if (!rc) rc = rcG;
+    }
+    if (rc) return rc;
     std::vector<SweepArgs> cur(nrep);
     cudaMemcpy(cur.data(), b.dArgs, sizeof(SweepArgs) * nrep, cudaMemcpyDeviceToHost);
     for (int k = 0; k < nrep; ++k) {
@@ -4684,6 +4749,15 @@ int runReplicas(void* h, const sc_run_params& p0, int exchangeEvery, sc_run_stat
         st.acc_chain += s1.acc_chain; st.rej_chain += s1.rej_chain;
         st.acc_switch += s1.acc_switch; st.rej_switch += s1.rej_switch;
         st.pairs_tested += s1.pairs_tested; st.pairs_evaluated += s1.pairs_evaluated;
+        st.particles += (long)b.sys[k]->conf.p.size();
+        if (b.sys[k]->engine->gcOn) {
+            GcDev h;
+            cudaMemcpy(&h, b.sys[k]->engine->gc, sizeof h, cudaMemcpyDeviceToHost);
+            for (int g = 0; g < h.nSpecies; ++g) {
+                st.acc_insert += (long)h.ctr[g][1]; st.rej_insert += (long)h.ctr[g][2];
+                st.acc_delete += (long)h.ctr[g][3]; st.rej_delete += (long)h.ctr[g][4];
+            }
+        }
         st.da_stage1_rejected += s1.da_stage1_rejected;
         st.da_stage2_tried += s1.da_stage2_tried;
         st.da_stage2_rejected += s1.da_stage2_rejected;

@@ -13,7 +13,8 @@ Exactness: the running energy (the moves' energy changes, insertions and removal
 included) equals the exact total energy after the run; the particle vector keeps the
 reference's order (each molecule type in its block, the inserted particles of a species at
 its block's end); capacity growth from an empty box; chains before the species with chain
-moves; the schedule over calls (sweep_offset); bitwise reproducibility.
+moves; the schedule over calls (sweep_offset); bitwise reproducibility; replica exchange
+with the grand-canonical term.
 """
 import json
 import math
@@ -162,20 +163,54 @@ def test_bitwise_reproducible():
     assert out[0] == out[1]
 
 
-def test_replica_exchange_refuses_grand_moves():
-    from sc_gb300 import ReplicaSet, ScError, System
+def test_replica_exchange_with_grand_moves():
+    """Grand-canonical replicas: every exchange decision is the reference's rule with its
+    grand-canonical term (movecreator.cpp:713-745: change = (1/T_i - 1/T_j)(E_i - E_j) +
+    (1/T_i - 1/T_j) chemPot T_i (N_i - N_j), NVT), restated on the energies, counts,
+    temperatures and the uniforms of the exchange's own stream; each call makes a
+    grand-canonical move after its first sweep (grand_every 2 from loop sweep 2) and the
+    exchange after its second, so the call's final energies and counts are the ones the
+    exchange saw.  Running energies stay exact and the counts follow the device."""
+    from test_gpu_replicas import _M, _uniforms
+    from sc_gb300 import ReplicaSet, System
 
     g, opts, top, cfg = _case("gc_spa")
-    systems = [System.from_text(opts, top, cfg) for _ in range(2)]
-    R = ReplicaSet(systems, [1.0, 1.1], ladder=[0, 1])
+    systems = [System.from_text(opts, top, cfg) for _ in range(4)]
+    chem = systems[0].grand_stats()[0].chem_pot
+    temps = list(np.geomspace(0.9, 1.0, 4))
+    R = ReplicaSet(systems, temps, ladder=[0] * 4)
     p = systems[0].default_run()
-    with pytest.raises(ScError) as ei:
-        R.run(10, exchange_every=5, seed=1, params=p)
-    assert ei.value.code == -7
-    p.grand_every = 0
-    R.run(10, exchange_every=5, seed=1, params=p)
+    p.grand_every, p.sweep_offset, p.check_every = 2, 1, 0
+    seed = 31
+    u_seed = seed ^ 0xA5A5A5A5
+    T = np.array(temps)
+    decided = accepted = 0
+    counts = set()
+    for ev in range(40):
+        st, T_after, E, tried, acc = R.run(2, exchange_every=2, seed=seed, params=p)
+        N = np.array([s.n for s in systems], dtype=float)
+        counts.update(N.tolist())
+        ladder = list(np.argsort(T, kind="stable"))
+        want = T.copy()
+        u = _uniforms(u_seed, 0xFFFFFFE0, ev & _M, ev >> 32)
+        for k in range(ev & 1, len(ladder) - 1, 2):
+            ri, rj = ladder[k], ladder[k + 1]
+            change = (1.0 / T[ri] - 1.0 / T[rj]) * (E[ri] - E[rj])
+            change += (1.0 / T[ri] - 1.0 / T[rj]) * chem * T[ri] * (N[ri] - N[rj])
+            x = next(u)
+            if change >= 0.0 or math.exp(change) > x:
+                want[ri], want[rj] = T[rj], T[ri]
+                accepted += 1
+            decided += 1
+        assert np.array_equal(T_after, want), (ev, T, T_after, want, E, N)
+        T = T_after
+    assert 0 < accepted < decided and len(counts) > 1
     R.close()
     for s in systems:
+        exact = s.all_to_all()
+        st = s.simulate(p, nsweeps=0)
+        assert abs(st.energy - exact) <= 1e-9 * max(1.0, abs(exact))
+        _check_layout(s)
         s.close()
 
 
