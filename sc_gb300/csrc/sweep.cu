@@ -301,35 +301,56 @@ __global__ void kAssign(const SweepArgs* __restrict__ A) {
     }
 }
 
-__global__ void kScan(const SweepArgs* __restrict__ A) {
+// Exclusive scan of the cell counts, one CTA of kScanThreads per system.  Each thread owns
+// kScanPer consecutive cells of a tile (their loads are independent, so a tile costs one
+// memory latency), the thread totals are scanned across the CTA, and the carry moves to the
+// next tile: a 40,000-cell grid takes five tiles.
+constexpr int kScanThreads = 1024;
+constexpr int kScanPer = 8;
+
+__global__ void __launch_bounds__(kScanThreads) kScan(const SweepArgs* __restrict__ A) {
     const SweepArgs& a = A[blockIdx.y];
-    // single block: exclusive scan of the cell counts
-    __shared__ int warpTot[32];
-    __shared__ int carry;
-    if (threadIdx.x == 0) carry = 0;
-    __syncthreads();
-    int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int base = 0; base < a.g.ncells; base += blockDim.x) {
-        int k = base + threadIdx.x;
-        int v = k < a.g.ncells ? a.cellCount[k] : 0;
-        if (v > kCellCap && !a.chains) atomicOr(a.err, E_CELL_OVERFLOW);   // chain grids: any size
-        int incl = v;
+    __shared__ int warpTot[kScanThreads / 32];
+    const int n = a.g.ncells;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int carry = 0;                         // the same in every thread
+    for (int base = 0; base < n; base += kScanThreads * kScanPer) {
+        const int k0 = base + (int)threadIdx.x * kScanPer;
+        int v[kScanPer];
+        int sum = 0;
+#pragma unroll
+        for (int q = 0; q < kScanPer; ++q) v[q] = k0 + q < n ? a.cellCount[k0 + q] : 0;
+#pragma unroll
+        for (int q = 0; q < kScanPer; ++q) {
+            if (v[q] > kCellCap && !a.chains) atomicOr(a.err, E_CELL_OVERFLOW);   // chain grids: any size
+            sum += v[q];
+        }
+        int incl = sum;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            int t = __shfl_up_sync(0xffffffffu, incl, o);
+            const int t = __shfl_up_sync(0xffffffffu, incl, o);
             if (lane >= o) incl += t;
         }
         if (lane == 31) warpTot[w] = incl;
         __syncthreads();
         int woff = 0, tot = 0;
-        for (int q = 0; q < nw; ++q) { if (q < w) woff += warpTot[q]; tot += warpTot[q]; }
-        if (k < a.g.ncells) {
-            a.cellStart[k] = carry + woff + incl - v;
-            a.cellCursor[k] = 0;
+#pragma unroll
+        for (int q = 0; q < kScanThreads / 32; ++q) {
+            const int t = warpTot[q];
+            if (q < w) woff += t;
+            tot += t;
         }
         __syncthreads();
-        if (threadIdx.x == 0) carry += tot;
-        __syncthreads();
+        int run = carry + woff + incl - sum;
+#pragma unroll
+        for (int q = 0; q < kScanPer; ++q) {
+            if (k0 + q < n) {
+                a.cellStart[k0 + q] = run;
+                a.cellCursor[k0 + q] = 0;
+            }
+            run += v[q];
+        }
+        carry += tot;
     }
 }
 
@@ -2093,13 +2114,25 @@ __global__ void kWlEndSweep(const SweepArgs* __restrict__ A) {
 
 // Adds the cells' energy changes of this sweep, in a fixed order, and clears them (a cell
 // without particles writes nothing during the sweep).
-__global__ void kEndSweep(const SweepArgs* __restrict__ A) {
+// The sweep's energy change: the per-cell changes summed in a fixed order (each thread a
+// strided set of 4-cell groups whose loads are independent, then a shuffle tree per warp,
+// the warps in order) and cleared for the next sweep.  One CTA of kEndThreads per system.
+constexpr int kEndThreads = 1024;
+
+__global__ void __launch_bounds__(kEndThreads) kEndSweep(const SweepArgs* __restrict__ A) {
     const SweepArgs& a = A[blockIdx.y];
-    __shared__ double ws[32];
+    __shared__ double ws[kEndThreads / 32];
+    const int n = a.g.ncells;
     double v = 0.0;
-    for (int k = threadIdx.x; k < a.g.ncells; k += blockDim.x) {
-        v += a.cellDE[k];
-        a.cellDE[k] = 0.0;
+    for (int k0 = (int)threadIdx.x * 4; k0 < n; k0 += kEndThreads * 4) {
+        double x[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) x[q] = k0 + q < n ? a.cellDE[k0 + q] : 0.0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            v += x[q];
+            if (k0 + q < n) a.cellDE[k0 + q] = 0.0;
+        }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -2704,7 +2737,14 @@ __global__ void __launch_bounds__(kCellThreads) kCellEnergy(const SweepArgs* __r
 __device__ double sumPartials(const double* p, int n) {
     __shared__ double ws[32];
     double v = 0.0;
-    for (int k = threadIdx.x; k < n; k += blockDim.x) v += p[k];
+    const int stride = (int)blockDim.x * 8;
+    for (int k0 = (int)threadIdx.x * 8; k0 < n; k0 += stride) {     // 8 independent loads a thread
+        double x[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) x[q] = k0 + q < n ? p[k0 + q] : 0.0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) v += x[q];
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
@@ -4034,7 +4074,7 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
     auto launchCellsOf = [&](const SweepArgs* args, int maxCells) -> cudaError_t {
         kZeroCounts<<<dims((maxCells + 255) / 256), 256, 0, s>>>(args);
         kAssign<<<dims((b.maxN + 255) / 256), 256, 0, s>>>(args);
-        kScan<<<dims(1), 1024, 0, s>>>(args);
+        kScan<<<dims(1), kScanThreads, 0, s>>>(args);
         kScatter<<<dims((b.maxN + 255) / 256), 256, 0, s>>>(args);
         kSortCells<<<dims((maxCells + 127) / 128), 128, 0, s>>>(args);
         launches += 5;
@@ -4043,8 +4083,8 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
     auto launchCells = [&]() -> cudaError_t { return launchCellsOf(b.dArgs, b.maxCells); };
     auto exactEnergy = [&](bool check) -> cudaError_t {
         kCellEnergy<<<dims(b.maxCells), kCellThreads, kDynSmemCell, s>>>(b.dArgs, 0);
-        if (check) kCheckEnergy<<<dims(1), 256, 0, s>>>(b.dArgs);
-        else kSetEnergy<<<dims(1), 256, 0, s>>>(b.dArgs);
+        if (check) kCheckEnergy<<<dims(1), 1024, 0, s>>>(b.dArgs);
+        else kSetEnergy<<<dims(1), 1024, 0, s>>>(b.dArgs);
         launches += 2;
         return cudaGetLastError();
     };
@@ -4090,7 +4130,7 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
             kWlCells<<<dims(1), kMoveThreads, kDynSmemColour, s>>>(b.dArgs);
             launches += 1;
         }
-        kEndSweep<<<dims(1), 256, 0, s>>>(b.dArgs);
+        kEndSweep<<<dims(1), kEndThreads, 0, s>>>(b.dArgs);
         launches += 2 + (flow ? 1 : b.maxColours);
         if (b.chains) {       // chain moves: their own grid, colours and cell list
             kBeginSweep<<<dims(1), 32, 0, s>>>(b.dArgsC, 0);
@@ -4103,7 +4143,7 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
                 for (int ph = 0; ph < b.maxColoursC; ++ph)
                     kChainColour<<<dims(b.maxActiveC), kMoveThreads, kDynSmem, s>>>(b.dArgsC, ph);
             }
-            kEndSweep<<<dims(1), 256, 0, s>>>(b.dArgsC);
+            kEndSweep<<<dims(1), kEndThreads, 0, s>>>(b.dArgsC);
             launches += 3 + (flow ? 1 : b.maxColoursC);
             if (b.wl) {
                 kWlAfterChains<<<dims(1), 32, 0, s>>>(b.dArgs);
