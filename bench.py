@@ -752,7 +752,7 @@ def main():
     for k in range(0 if a.no_e2e else a.steps):
         s.set_particles(0, state)                 # host -> device (uploaded by the next call)
         st = s.simulate(p, nsweeps=1)
-        state = s.particles()                     # device -> host
+        state = s.particles(out=state)            # device -> host, into the caller's buffer
         e2e_moves += st.moves
     e2e_s = max_over_ranks(max(time.perf_counter() - t0, 1e-12), dist, f"cuda:{local}")
     e2e = {"value": e2e_moves * world / e2e_s if e2e_moves else None, "unit": UNIT,

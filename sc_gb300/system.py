@@ -93,11 +93,15 @@ class System:
         L.check(self._lib.sc_get_pair_param(self._h, t1, t2, C.byref(p)))
         return p
 
-    def particles(self, first=0, count=None):
+    def particles(self, first=0, count=None, out=None):
         """A ctypes array of ``sc_particle`` records (indexable, iterable, and accepted
-        as is by ``set_particles``)."""
+        as is by ``set_particles``).  ``out``: an array of at least ``count`` records to
+        fill instead of a new one (a caller that reads the state every step keeps one)."""
         count = self.n - first if count is None else count
-        arr = (L.Particle * count)()
+        if out is not None and isinstance(out, C.Array) and out._type_ is L.Particle and len(out) >= count:
+            arr = out
+        else:
+            arr = (L.Particle * count)()
         L.check(self._lib.sc_get_particles(self._h, first, count, arr))
         return arr
 

@@ -100,7 +100,7 @@ def test_plain_moves_match_reference_at_benchmark_state(name):
 @pytest.mark.parametrize("name", ["psc_c0", "mixture_c1"])
 def test_delayed_acceptance_matches_reference_at_benchmark_state(name):
     """Delayed acceptance with a network trained on this system's own configurations (the
-    exact FP64 stage judges every move the surrogate lets through) samples the reference's
+    exact FP64 stage decides every move the surrogate lets through) samples the reference's
     ensemble."""
     from sc_gb300 import Surrogate, System
 
