@@ -30,6 +30,10 @@ sys.path.insert(0, HERE)
 from make_golden import config_text, options_text, rand_perp, rand_unit, top_text  # noqa: E402
 
 REPO = os.path.dirname(os.path.dirname(HERE))
+# the reference checkout, as the oracle's recipe locates it (SC_REFERENCE overrides)
+from make_golden import REF_ROOT  # noqa: E402
+
+MEMBRANE = os.path.join(REF_ROOT, "Tests", "SC_PSC_MEMBRANE_WANG")
 DUMP = os.path.join(REPO, "oracle", "_ref", "ref_dump")
 SCREF = os.path.join(REPO, "oracle", "_ref", "sc_ref")
 
@@ -145,12 +149,28 @@ def cases():
     out.append(dict(name="o9_wall", wlm=(9, 0), options=dict(wlm="9 0", transmx=0.2, rotmx=0.0, nsweeps=3000,
                                                                seed=17, shave=1, ptype=5, edge_mx=0.1),
                     top=top, config=cfg, wl=wl_text(0.0, grid1(6.0, 0.05, 21), wall)))
+    # (7) the reference's own membrane test (Tests/SC_PSC_MEMBRANE_WANG/scOOP_test): a CPSC
+    # protein and 200 three-bead lipids, orders 1 and 3, NPT (ptype 2) with chain moves, and
+    # the converged weights of its legacy run (wl_orig_results.dat) as the weights file.  Its
+    # options file lacks the ptype and press lines, which the reference requires (sim.h:177);
+    # they are taken from the test's other options file (ptype 2, press 0).
+    if os.path.isdir(MEMBRANE):
+        d = os.path.join(MEMBRANE, "scOOP_test")
+        opts = open(os.path.join(d, "options")).read().rstrip("\n") + "\nptype = 2\npress = 0.0\n"
+        out.append(dict(name="membrane_ref", wlm=(1, 3), options_text=opts,
+                        top=open(os.path.join(d, "top.init")).read(),
+                        config=open(os.path.join(d, "config.init")).read(),
+                        wl=open(os.path.join(d, "wl_orig_results.dat")).read()))
     return out
+
+
+def case_options(c):
+    return c["options_text"] if "options_text" in c else options_text(**c["options"])
 
 
 def write_case(d, c):
     with open(os.path.join(d, "options"), "w") as f:
-        f.write(options_text(**c["options"]))
+        f.write(case_options(c))
     with open(os.path.join(d, "top.init"), "w") as f:
         f.write(c["top"])
     with open(os.path.join(d, "config.init"), "w") as f:
@@ -177,14 +197,22 @@ def main():
     for exe in (DUMP, SCREF):
         if not os.path.exists(exe):
             sys.exit(f"{exe} missing: run make -C oracle ref first")
+    only = sys.argv[1:]           # names: regenerate those cases only, keep the others
+    old = []
+    path = os.path.join(HERE, "wl", "cases.json.gz")
+    if only and os.path.exists(path):
+        with gzip.open(path, "rt") as f:
+            old = [e for e in json.load(f)["cases"] if e["name"] not in only]
     result = []
     for c in cases():
+        if only and c["name"] not in only:
+            continue
         tmp = tempfile.mkdtemp()
         try:
             write_case(tmp, c)
             r = subprocess.run([DUMP, tmp, "0", "0"], capture_output=True, text=True, check=True)
             dump = json.loads(r.stdout)
-            entry = {"name": c["name"], "inputs": {"options": options_text(**c["options"]), "top.init": c["top"],
+            entry = {"name": c["name"], "inputs": {"options": case_options(c), "top.init": c["top"],
                                                    "config.init": c["config"], "wl.dat": c["wl"]},
                      "ref": dump["wl"], "n": dump["n"],
                      "system": {k: dump[k] for k in ("box", "sqmaxcut", "ia_params", "particles", "molecules")}}
@@ -209,7 +237,9 @@ def main():
         finally:
             shutil.rmtree(tmp)
     os.makedirs(os.path.join(HERE, "wl"), exist_ok=True)
-    with gzip.open(os.path.join(HERE, "wl", "cases.json.gz"), "wt") as f:
+    order = [c["name"] for c in cases()]
+    result = sorted(old + result, key=lambda e: order.index(e["name"]) if e["name"] in order else len(order))
+    with gzip.open(path, "wt") as f:
         json.dump({"generator": "tests/golden/make_wl.py", "cases": result}, f)
 
 

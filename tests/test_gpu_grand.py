@@ -46,33 +46,47 @@ def _check_layout(s):
         assert int(np.sum(mt == g.mol_type)) == g.count
 
 
-@pytest.mark.parametrize("name", ["gc_spa", "gc_psc"])
-def test_ensemble_matches_reference(name):
-    from sc_gb300 import System
+@pytest.mark.parametrize("name,batched", [("gc_spa", False), ("gc_psc", True)])
+def test_ensemble_matches_reference(name, batched):
+    """gc_spa: one system at a time through sc_simulate; gc_psc: the trajectories moved
+    together as a replica batch without exchanges (each keeps its own slots and count)."""
+    from sc_gb300 import ReplicaSet, System
 
     g, opts, top, cfg = _case(name)
     rep, burn, nsw = g["report"], g["burn"], g["nsweeps"]
     N, E = [], []
-    for k in range(g["seeds"]):
-        s = System.from_text(opts, top, cfg)
-        p = s.default_run()
+    groups = [list(range(g["seeds"]))] if batched else [[k] for k in range(g["seeds"])]
+    for group in groups:
+        systems = [System.from_text(opts, top, cfg) for _ in group]
+        p = systems[0].default_run()
         p.check_every = 0
-        p.seed = 7000 + k
-        n_ser, e_ser = [], []
+        p.seed = 7000 + group[0]
+        R = ReplicaSet(systems, [float(g["options"]["temper"])] * len(systems),
+                       ladder=list(range(len(systems)))) if batched else None
+        n_ser = [[] for _ in group]
+        e_ser = [[] for _ in group]
         done = 0
         while done < nsw:
-            st = s.simulate(p, nsweeps=rep, sweep_offset=done)
+            if batched:
+                _, _, en, _, _ = R.run(rep, exchange_every=0, seed=p.seed, params=p, sweep_offset=done)
+            else:
+                en = [systems[0].simulate(p, nsweeps=rep, sweep_offset=done).energy]
             done += rep
             if done > burn:
-                n_ser.append(st.particles)
-                e_ser.append(st.energy)
-        exact = s.all_to_all()
-        assert abs(st.energy - exact) <= 1e-9 * max(1.0, abs(exact)), (st.energy, exact)
-        assert st.particles == s.n
-        _check_layout(s)
-        N.append(np.array(n_ser, dtype=float))
-        E.append(np.array(e_ser))
-        s.close()
+                for k, s in enumerate(systems):
+                    n_ser[k].append(s.n)
+                    e_ser[k].append(en[k])
+        if R is not None:
+            R.close()
+        for k, s in enumerate(systems):
+            exact = s.all_to_all()
+            st = s.simulate(p, nsweeps=0)
+            assert abs(st.energy - exact) <= 1e-9 * max(1.0, abs(exact)), (st.energy, exact)
+            assert st.particles == s.n
+            _check_layout(s)
+            N.append(np.array(n_ser[k], dtype=float))
+            E.append(np.array(e_ser[k]))
+            s.close()
     report = {}
     for key, ser in (("particles", N), ("energy_total", E)):
         m = np.array([x.mean() for x in ser])

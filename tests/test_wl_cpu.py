@@ -6,6 +6,8 @@ reference itself computes with its WangLandau::init and writes with WangLandau::
 restatement (or_wl_orders) and the library's host code (sc_wl_load / sc_wl_get_info /
 sc_wl_write, which run before any device work) must reproduce them exactly.  The oracle's
 sequential Wang-Landau loop (or_wl_run) is checked against the reference's own adaptive runs.
+The cases include the reference's own membrane test (a CPSC protein and 200 lipids, orders 1
+and 3) with the converged weights of its legacy run as the weights file.
 """
 import gzip
 import json
@@ -41,7 +43,7 @@ def wlm_of(c):
     for line in c["inputs"]["options"].splitlines():
         k, _, v = line.partition("=")
         if k.strip() == "wlm":
-            w = [int(x) for x in v.split()]
+            w = [int(x) for x in v.split("#")[0].split()]
             return (w + [0])[:2]
     raise KeyError("wlm")
 
