@@ -149,6 +149,13 @@ def cases():
     out.append(dict(name="o9_wall", wlm=(9, 0), options=dict(wlm="9 0", transmx=0.2, rotmx=0.0, nsweeps=3000,
                                                                seed=17, shave=1, ptype=5, edge_mx=0.1),
                     top=top, config=cfg, wl=wl_text(0.0, grid1(6.0, 0.05, 21), wall)))
+    # (8) order 1 under fixed weights (alpha 0): a harmonic well w = -0.5 z^2 for the height
+    # of particle 0 above the system centre, in the interacting bath of (5); the reference's
+    # histograms of several seeds bound the effect of the centre's unbiased moves
+    zs = grid1(-4.5, 0.1, 91)
+    out.append(dict(name="o1_fixed", wlm=(1, 0), options=dict(wlm="1 0", transmx=0.2, rotmx=0.0, nsweeps=20000,
+                                                                seed=18, shave=0, ptype=0),
+                    top=top, config=cfg, wl=wl_text(0.0, zs, [-0.5 * z[0] * z[0] for z in zs])))
     # (7) the reference's own membrane test (Tests/SC_PSC_MEMBRANE_WANG/scOOP_test): a CPSC
     # protein and 200 three-bead lipids, orders 1 and 3, NPT (ptype 2) with chain moves, and
     # the converged weights of its legacy run (wl_orig_results.dat) as the weights file.  Its
@@ -216,10 +223,11 @@ def main():
                                                    "config.init": c["config"], "wl.dat": c["wl"]},
                      "ref": dump["wl"], "n": dump["n"],
                      "system": {k: dump[k] for k in ("box", "sqmaxcut", "ia_params", "particles", "molecules")}}
-            if c["name"] in ("o4_pair", "o3_orient", "o9_wall"):
+            if c["name"] in ("o4_pair", "o3_orient", "o9_wall", "o1_fixed"):
                 # the reference's own adaptive runs, three seeds
                 runs = []
-                for seed in ((101,) if c["name"] == "o9_wall" else (101, 202, 303)):
+                seeds = {"o9_wall": (101,), "o1_fixed": (101, 202, 303, 404, 505, 606)}.get(c["name"], (101, 202, 303))
+                for seed in seeds:
                     opts = dict(c["options"], seed=seed)
                     if c["name"] == "o3_orient":
                         opts["nsweeps"] = 20000

@@ -214,6 +214,42 @@ def test_reference_membrane_test_runs_with_its_converged_weights():
     assert i.currorder[0] == math.ceil(((parts[0].pos[2] - i.syscm[2]) * box[2] - i.minorder[0]) / i.dorder[0])
 
 
+def test_order1_fixed_weights_sample_the_reference_distribution():
+    """Order 1 under fixed weights (a harmonic well in the height of particle 0 above the
+    system centre, alpha 0) in an interacting bath: the mean and the variance of the visited
+    bin over six trajectories agree with six runs of the reference's own loop within 2
+    combined standard errors.  This bounds the effect of the stated deviation -- the centre's
+    shifts by the other cells' displacements are not biased (they are in the reference)."""
+    from sc_gb300 import ReplicaSet, System
+
+    c = CASES["o1_fixed"]
+    inp = c["inputs"]
+    ws = []
+    for _ in c["ref_runs"]:
+        s = System.from_text(inp["options"], inp["top.init"], inp["config.init"])
+        s.wl_load(text=inp["wl.dat"])
+        ws.append(s)
+    h0 = [s.wl_weights()[1] for s in ws]
+    R = ReplicaSet(ws, temperatures=[1.0] * len(ws), ladder=list(range(len(ws))))
+    R.run(20000, exchange_every=0, seed=31, variant=4)
+    R.close()
+
+    def moments(h):
+        h = np.asarray(h, dtype=float)
+        i = np.arange(len(h))
+        m = (h * i).sum() / h.sum()
+        return m, (h * (i - m) ** 2).sum() / h.sum()
+
+    got = np.array([moments(s.wl_weights()[1] - h) for s, h in zip(ws, h0)])
+    ref = np.array([moments(r["hist"]) for r in c["ref_runs"]])
+    for s in ws:
+        assert np.array_equal(s.wl_weights()[0], ws[0].wl_weights()[0])     # alpha 0: fixed
+        s.close()
+    for k, name in enumerate(("mean bin", "bin variance")):
+        se = math.sqrt(got[:, k].var(ddof=1) / len(got) + ref[:, k].var(ddof=1) / len(ref))
+        assert abs(got[:, k].mean() - ref[:, k].mean()) <= 2.0 * se, (name, got[:, k], ref[:, k])
+
+
 def test_walkers_share_one_table():
     # four walkers of the two-particle distance case update one table (the reference's
     # multiple walkers): every walker's moves count in the shared histogram, the owner's
