@@ -32,7 +32,7 @@ extern "C" {
 #define SC_ERR_RANGE (-5)      /* a size beyond a documented maximum */
 #define SC_ERR_STATE (-6)      /* call not valid in the current state */
 #define SC_ERR_UNSUPPORTED (-7) /* input outside the GPU path (see sc_last_error) */
-#define SC_ERR_DEVICE (-8)     /* a kernel reported an error status (e.g. cell overflow) */
+#define SC_ERR_DEVICE (-8)     /* a kernel reported an error status (e.g. a dataflow wait that gave up) */
 
 typedef struct sc_context sc_context;
 

@@ -54,7 +54,7 @@ namespace {
 
 constexpr int kMoveThreads = 128;
 constexpr int kWarps = kMoveThreads / 32;
-constexpr int kCellCap = 256;        // particles per cell
+constexpr int kCellCap = 256;        // particles of a cell staged in shared memory (larger cells: read from the cell list)
 constexpr int kNbCap = 343;          // stencil cells, (2*3+1)^3
 constexpr int kCandCap = 1024;       // candidates staged in shared memory at a time
 constexpr int kQueueCap = 2048;      // pair queue entries (old + new of a full window)
@@ -66,7 +66,7 @@ constexpr size_t kDynSmemSurrogate = kDynSmem + (size_t)kCandCap * 2 * sizeof(fl
 
 enum Ctr { C_ACC_T, C_REJ_T, C_ACC_R, C_REJ_R, C_ACC_V, C_REJ_V, C_VOL_CONSTR, C_TESTED, C_EVAL, C_CELL_REJ, C_MOVES,
            C_SCREENED, C_S1_REJ, C_S2_TRIED, C_S2_REJ, C_ACC_CH, C_REJ_CH, C_CH_CONSTR, C_ACC_SW, C_REJ_SW, C_COUNT };
-enum ErrBit { E_CELL_OVERFLOW = 1, E_PARTNER_FAR = 2, E_FLOW_WAIT = 4, E_GC_FULL = 8 };
+enum ErrBit { E_PARTNER_FAR = 2, E_FLOW_WAIT = 4, E_GC_FULL = 8 };
 constexpr int kMaxChainTypes = 8;                         // chain molecule types with their own step
 constexpr int kTypeCtrChain = 4 * MAX_DEV_TYPES;
 constexpr int kTypeCtrCount = kTypeCtrChain + 4 * kMaxChainTypes;
@@ -321,10 +321,7 @@ __global__ void __launch_bounds__(kScanThreads) kScan(const SweepArgs* __restric
 #pragma unroll
         for (int q = 0; q < kScanPer; ++q) v[q] = k0 + q < n ? a.cellCount[k0 + q] : 0;
 #pragma unroll
-        for (int q = 0; q < kScanPer; ++q) {
-            if (v[q] > kCellCap && !a.chains) atomicOr(a.err, E_CELL_OVERFLOW);   // chain grids: any size
-            sum += v[q];
-        }
+        for (int q = 0; q < kScanPer; ++q) sum += v[q];
         int incl = sum;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -1105,13 +1102,17 @@ __device__ __forceinline__ void moveCell(const SweepArgs& a, int cx, int cy, int
     const Grid& g = a.g;
     int cell = (cz * g.nc[1] + cy) * g.nc[0] + cx;
     int cnt = a.cellCount[cell];
-    if (cnt == 0 || cnt > kCellCap) return;
+    if (cnt == 0) return;
     const int tid = threadIdx.x, warp = tid >> 5;
     const double3 box = mk(a.s.box[0], a.s.box[1], a.s.box[2]);
-    for (int k = tid; k < cnt; k += kMoveThreads) sh.list[k] = a.cellIdx[a.cellStart[cell] + k];
+    // the cell's particles: staged in shared memory, or read from the cell list itself when
+    // the cell holds more than kCellCap (the list does not change during the sweep)
+    const int* list = cnt <= kCellCap ? sh.list : a.cellIdx + a.cellStart[cell];
+    if (cnt <= kCellCap)
+        for (int k = tid; k < cnt; k += kMoveThreads) sh.list[k] = a.cellIdx[a.cellStart[cell] + k];
     if (tid < 4) sh.propFor[tid] = -1;
     stageStencil(a, cx, cy, cz, sh.st, sh.scan);
-    if (warp == 0) buildProposal(a, sh.list, sh.st.nbCell, sh.st.nNb, sh.prop[0], cell, cnt, 0, cx, cy, cz, box);
+    if (warp == 0) buildProposal(a, list, sh.st.nbCell, sh.st.nNb, sh.prop[0], cell, cnt, 0, cx, cy, cz, box);
     else if (tid == 64) acceptThresholds(a, sh.prop[0], cell, 0);
     __syncthreads();
     if (tid == 0) sh.propFor[0] = 0;
@@ -1146,11 +1147,11 @@ __device__ __forceinline__ void moveCell(const SweepArgs& a, int cx, int cy, int
             const bool need0 = sh.propFor[m & 3] != m;
             const bool need1 = pair && sh.propFor[(m + 1) & 3] != m + 1;
             if (need0) {
-                if (warp == 0) buildProposal(a, sh.list, sh.st.nbCell, sh.st.nNb, sh.prop[m & 3], cell, cnt, m, cx, cy, cz, box);
+                if (warp == 0) buildProposal(a, list, sh.st.nbCell, sh.st.nNb, sh.prop[m & 3], cell, cnt, m, cx, cy, cz, box);
                 else if (tid == 64) acceptThresholds(a, sh.prop[m & 3], cell, m);
             }
             if (need1) {
-                if (warp == 1) buildProposal(a, sh.list, sh.st.nbCell, sh.st.nNb, sh.prop[(m + 1) & 3], cell, cnt, m + 1, cx, cy, cz, box);
+                if (warp == 1) buildProposal(a, list, sh.st.nbCell, sh.st.nNb, sh.prop[(m + 1) & 3], cell, cnt, m + 1, cx, cy, cz, box);
                 else if (tid == 96) acceptThresholds(a, sh.prop[(m + 1) & 3], cell, m + 1);
             }
             __syncthreads();
@@ -1284,7 +1285,7 @@ __device__ __forceinline__ void moveCell(const SweepArgs& a, int cx, int cy, int
         auto speculate = [&](int mv) {
             if (sh.propFor[mv & 3] == mv) return;      // still valid from an earlier pass
             Proposal& N = sh.prop[mv & 3];
-            buildProposal(a, sh.list, sh.st.nbCell, sh.st.nNb, N, cell, cnt, mv, cx, cy, cz, box);
+            buildProposal(a, list, sh.st.nbCell, sh.st.nNb, N, cell, cnt, mv, cx, cy, cz, box);
             if ((tid & 31) == 0) {
                 acceptThresholds(a, N, cell, mv);
                 sh.propFor[mv & 3] = mv;
@@ -1744,7 +1745,9 @@ __device__ bool warpMoveCell(const SweepArgs& a, WarpCell& W, int cx, int cy, in
     const Grid& g = a.g;
     const double3 box = mk(a.s.box[0], a.s.box[1], a.s.box[2]);
     const int start = a.cellStart[cell];
-    for (int k = lane; k < cnt; k += 32) W.list[k] = a.cellIdx[start + k];
+    const int* list = cnt <= kCellCap ? W.list : a.cellIdx + start;     // large cells: the cell list itself
+    if (cnt <= kCellCap)
+        for (int k = lane; k < cnt; k += 32) W.list[k] = a.cellIdx[start + k];
     // the stencil's cells and their offsets in the candidate list (static during the sweep)
     const int nx = axisCount(g.nc[0], g.s[0]), ny = axisCount(g.nc[1], g.s[1]), nz = axisCount(g.nc[2], g.s[2]);
     const int nn = nx * ny * nz;
@@ -1772,7 +1775,7 @@ __device__ bool warpMoveCell(const SweepArgs& a, WarpCell& W, int cx, int cy, in
     const int ownOff = W.nbOff[ownQ];
     const bool resident = nCand <= kWarpCand;
     // the first proposal reads only this cell's own particles: built before the wait
-    buildProposal(a, W.list, W.nbCell, nn, W.prop, cell, cnt, 0, cx, cy, cz, box);
+    buildProposal(a, list, W.nbCell, nn, W.prop, cell, cnt, 0, cx, cy, cz, box);
     if (lane == 0) acceptThresholds(a, W.prop, cell, 0);
     // the earlier-phase cells of the stencil have finished
     bool fail = false;
@@ -1822,7 +1825,7 @@ __device__ bool warpMoveCell(const SweepArgs& a, WarpCell& W, int cx, int cy, in
     unsigned nScr = 0, nEval = 0;
     for (int m = 0; m < cnt; ++m) {
         if (m > 0) {
-            buildProposal(a, W.list, W.nbCell, nn, W.prop, cell, cnt, m, cx, cy, cz, box);
+            buildProposal(a, list, W.nbCell, nn, W.prop, cell, cnt, m, cx, cy, cz, box);
             if (lane == 0) acceptThresholds(a, W.prop, cell, m);
             __syncwarp();
         }
@@ -1966,7 +1969,7 @@ __device__ __forceinline__ void warpFlowBody(const SweepArgs* __restrict__ A) {
         decodeActive(g, a.ctl->perm[phase], tk - phase * g.nactive, cx, cy, cz);
         const int cell = (cz * g.nc[1] + cy) * g.nc[0] + cx;
         const int cnt = a.cellCount[cell];
-        if (cnt > 0 && cnt <= kCellCap) {
+        if (cnt > 0) {
             if (!warpMoveCell(a, W, cx, cy, cz, cell, cnt, phase, posOf, stamp)) {
                 if (lane == 0) atomicOr(a.err, E_FLOW_WAIT);
                 break;
@@ -2267,14 +2270,14 @@ __device__ __forceinline__ void quatRotate(const double (&q)[4], double* v) {
 }
 
 // Warp 0: the chain move proposal of move m of this cell.
-__device__ void buildChainProposal(const SweepArgs& a, ChainShared& sh, int cell, int cnt, int m, int cx, int cy,
-                                   int cz, const double3& box) {
+__device__ void buildChainProposal(const SweepArgs& a, ChainShared& sh, const int* list, int cell, int cnt, int m,
+                                   int cx, int cy, int cz, const double3& box) {
     const Control& ctl = *a.ctl;
     const int lane = threadIdx.x & 31;
     const uint32_t sk = (uint32_t)ctl.sweep ^ ((uint32_t)(ctl.sweep >> 32) << 20);
     Stream r(a.seed, (uint32_t)cell, (uint32_t)m, sk);
     int slot = min((int)(r.next() * cnt), cnt - 1);
-    int2 fs = a.chains[sh.list[slot]];
+    int2 fs = a.chains[list[slot]];
     const int first = fs.x, size = min(fs.y, kMaxChain);
     bool displace = r.next() < 0.5;          // chainMove: ran2() < 0.5 displaces
     double3 cm = chainCentre(a, first, size);
@@ -2361,8 +2364,7 @@ __device__ __forceinline__ void chainCell(const SweepArgs& a, int cx, int cy, in
     const Grid& g = a.g;
     const int cell = (cz * g.nc[1] + cy) * g.nc[0] + cx;
     const int cnt = a.chainCellCount[cell];
-    if (cnt > kCellCap && threadIdx.x == 0) atomicOr(a.err, E_CELL_OVERFLOW);
-    if (cnt == 0 || cnt > kCellCap) return;
+    if (cnt == 0) return;
     const int tid = threadIdx.x;
     // attempts of this cell this sweep: cnt * chainFrac, the fraction rounded at random
     Stream rm(a.seed ^ 0x9E3779B97F4A7C15ull, (uint32_t)cell, 0xC4A1u,
@@ -2370,7 +2372,11 @@ __device__ __forceinline__ void chainCell(const SweepArgs& a, int cx, int cy, in
     const double want = cnt * a.chainFrac;
     const int moves = (int)want + ((rm.next() < want - floor(want)) ? 1 : 0);
     if (moves == 0) return;
-    for (int k = tid; k < cnt; k += kMoveThreads) sh.list[k] = a.chainCellIdx[a.chainCellStart[cell] + k];
+    // the cell's chains: staged in shared memory, or read from the chain list itself when the
+    // cell holds more than kCellCap
+    const int* list = cnt <= kCellCap ? sh.list : a.chainCellIdx + a.chainCellStart[cell];
+    if (cnt <= kCellCap)
+        for (int k = tid; k < cnt; k += kMoveThreads) sh.list[k] = a.chainCellIdx[a.chainCellStart[cell] + k];
     stageStencil(a, cx, cy, cz, sh.st, sh.scan);
     if (!wait()) return;
     const int nCand = sh.st.nCand;
@@ -2388,7 +2394,7 @@ __device__ __forceinline__ void chainCell(const SweepArgs& a, int cx, int cy, in
     unsigned long long nAcc = 0, nRej = 0, nConstr = 0, nTested = 0, nEval = 0;
 
     for (int m = 0; m < moves; ++m) {
-        if (tid < 32) buildChainProposal(a, sh, cell, cnt, m, cx, cy, cz, box);
+        if (tid < 32) buildChainProposal(a, sh, list, cell, cnt, m, cx, cy, cz, box);
         __syncthreads();
         if (sh.skip) {
             if (tid == 0) { ++nRej; nConstr += sh.constrained; }
@@ -2631,13 +2637,15 @@ __global__ void __launch_bounds__(kCellThreads) kCellEnergy(const SweepArgs* __r
         return;
     }
     int cnt = a.cellCount[cell];
-    if (cnt == 0 || cnt > kCellCap) {
+    if (cnt == 0) {
         if (tid == 0) a.partial[cell] = 0.0;
         return;
     }
     int cx = cell % g.nc[0], cy = (cell / g.nc[0]) % g.nc[1], cz = cell / (g.nc[0] * g.nc[1]);
     const int own0 = a.cellStart[cell];
-    for (int k = tid; k < cnt; k += kCellThreads) sh.list[k] = a.cellIdx[own0 + k];
+    const int* list = cnt <= kCellCap ? sh.list : a.cellIdx + own0;      // large cells: the cell list itself
+    if (cnt <= kCellCap)
+        for (int k = tid; k < cnt; k += kCellThreads) sh.list[k] = a.cellIdx[own0 + k];
     stageStencil<kCellThreads>(a, cx, cy, cz, sh.st, sh.scan);
     const int nCand = sh.st.nCand;
     DevCtx c;
@@ -2648,7 +2656,7 @@ __global__ void __launch_bounds__(kCellThreads) kCellEnergy(const SweepArgs* __r
     double sum = 0.0;
     // bonded partners j < i, whatever the distance
     for (int k = tid; k < cnt; k += kCellThreads) {
-        int i = sh.list[k];
+        int i = list[k];
         Con con = makeCon(c, i, a.s.mol[i]);
         PView vi = viewAt(a.s, i);
         for (int q = 0; q < 4; ++q) {
@@ -2664,7 +2672,7 @@ __global__ void __launch_bounds__(kCellThreads) kCellEnergy(const SweepArgs* __r
         __syncthreads();                   // queue entries of every thread are visible
         for (int e = tid; e < count; e += kCellThreads) {
             int q = sh.queueB[e];
-            int i = sh.list[q / wlen], j = candIdx[q % wlen];
+            int i = list[q / wlen], j = candIdx[q % wlen];
             Con con = makeCon(c, i, a.s.mol[i]);
             unsigned bb; double dd;
             sum += pairEnergy(c, viewAt(a.s, i), viewAt(a.s, j), con, box, &bb, &dd);
@@ -2684,7 +2692,7 @@ __global__ void __launch_bounds__(kCellThreads) kCellEnergy(const SweepArgs* __r
             int keep = 0;
             if (q < end) {
                 int li = q / wlen, k = q % wlen;
-                int i = sh.list[li], j = candIdx[k];
+                int i = list[li], j = candIdx[k];
                 if (j < i) {
                     float4 pi = a.cellPosF[own0 + li];
                     keep = dist2f(candPos[k], make_float3(pi.x, pi.y, pi.z), box) <= thr32;
@@ -2701,7 +2709,7 @@ __global__ void __launch_bounds__(kCellThreads) kCellEnergy(const SweepArgs* __r
             int keep = 0, q = 0;
             if (e < qa) {
                 q = sh.queueA[e];
-                int i = sh.list[q / wlen], j = candIdx[q % wlen];
+                int i = list[q / wlen], j = candIdx[q % wlen];
                 int4 mi = a.s.mol[i];
                 Con con = makeCon(c, i, mi);
                 bool partner = (j == con.idx[0] || j == con.idx[1] || j == con.idx[2] || j == con.idx[3]);
@@ -3204,7 +3212,7 @@ __global__ void __launch_bounds__(kSwThreads) kSwitchColour(const SweepArgs* __r
     decodeActive(g, a.ctl->perm[phase], blockIdx.x, cx, cy, cz);
     const int cell = (cz * g.nc[1] + cy) * g.nc[0] + cx;
     const int cnt = a.cellCount[cell];
-    if (cnt == 0 || cnt > kCellCap) return;
+    if (cnt == 0) return;
     __shared__ SwitchShared sh;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     stageStencil<kSwThreads>(a, cx, cy, cz, sh.st, sh.scan);
@@ -3972,7 +3980,6 @@ static void collectStats(Context* c, sc_run_stats& st) {
 static int systemErrors(Context* c) {
     int err = 0;
     cudaMemcpy(&err, c->engine->err, sizeof err, cudaMemcpyDeviceToHost);
-    if (err & E_CELL_OVERFLOW) return fail(SC_ERR_DEVICE, "a cell holds more than 256 particles (density too high for the cell list)");
     if (err & E_PARTNER_FAR) return fail(SC_ERR_DEVICE, "a bonded partner lies beyond the cell stencil (bond longer than maxcut)");
     if (err & E_FLOW_WAIT) return fail(SC_ERR_DEVICE, "dataflow sweep: a cell waited too long for its neighbours");
     if (err & E_GC_FULL) return fail(SC_ERR_DEVICE, "grand-canonical insertion found no free particle slot");
@@ -4408,7 +4415,7 @@ int runSweeps(Context* c, const sc_run_params& p0, sc_run_stats& st) {
     st.launches = out.launches;
     c->lastLaunches = out.launches;
     rc = systemErrors(c);
-    // a sweep that stopped early (a dataflow wait gave up, a cell overflowed) leaves cells
+    // a sweep that stopped early (a dataflow wait gave up, a partner lay beyond the stencil) leaves cells
     // unmoved and their energy changes unsummed: the next run recomputes the exact energy
     if (rc) c->engine->energyKnown = false;
     return rc;

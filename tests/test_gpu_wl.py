@@ -190,24 +190,34 @@ def test_chain_moves_visit_the_current_bin(variant):
     assert i.currorder[0] == math.ceil(((parts[0].pos[2] - i.syscm[2]) * box[2] - i.minorder[0]) / i.dorder[0])
 
 
-def test_reference_membrane_test_is_refused_cleanly():
+def test_reference_membrane_test_runs_with_its_converged_weights():
     """The reference's own Wang-Landau test (Tests/SC_PSC_MEMBRANE_WANG: a CPSC protein of
-    length 6 above 200 three-bead lipids in a 10.9 x 10.9 x 50 box) is outside the move
-    loop's cell list: the protein makes the cutoff about 9, so the grid is one cell wide in x
-    and y and the bilayer's 600 particles share a cell, beyond the 256 a cell holds.  The
-    sweep reports SC_ERR_DEVICE and the context stays usable (its weights file and starting
-    bins are pinned on the host by tests/test_wl_cpu.py)."""
-    from sc_gb300 import ScError
-
+    length 6 above 200 three-bead lipids in a 10.9 x 10.9 x 50 box, orders 1 and 3, volume
+    moves at constant z (ptype 2), chain moves) with the converged weights of its legacy run.
+    The protein makes the cutoff about 9, so the grid is one cell wide in x and y and the
+    bilayer's 600 particles share a cell (more than a cell stages in shared memory: read from
+    the cell list).  Every move, volume move and chain move visits the histogram once, the
+    bins follow the state, the running energy stays exact."""
     s, c = open_case("membrane_ref")
-    for _ in range(2):
-        with pytest.raises(ScError) as ei:
-            s.simulate(s.default_run(), nsweeps=2, seed=5)
-        assert ei.value.code == -8 and "256 particles" in str(ei.value)
-        e = s.all_to_all()
-        assert math.isfinite(e)
-        assert s.one_to_all([0])[0] == pytest.approx(s.one_to_all([0])[0])
+    _, h0 = s.wl_weights()
+    p = s.default_run()
+    assert p.ptype == 2 and p.volume_every == 1 and p.chainprob == 0.1
+    p.check_every = 50
+    st = s.simulate(p, nsweeps=200, seed=5)
+    i = s.wl_info()
+    _, h1 = s.wl_weights()
+    parts = s.particles()
+    box = s.box
+    exact = s.all_to_all()            # over all pairs, no cell list
     s.close()
+    assert abs(st.energy - exact) <= 1e-9 * max(1.0, abs(exact)), (st.energy, exact)
+    chain = st.acc_chain + st.rej_chain
+    assert chain > 0 and st.moves == 200 * c["n"] and st.acc_vol + st.rej_vol == 200
+    assert st.acc_trans > 0 and st.acc_rot > 0
+    assert int((h1 - h0).sum()) == st.moves + chain + st.acc_vol + st.rej_vol
+    assert st.max_drift <= 1e-9 * max(1.0, abs(st.energy)), (st.max_drift, st.energy)
+    assert i.currorder[1] == math.floor((parts[0].dir[2] - i.minorder[1]) / i.dorder[1])
+    assert i.currorder[0] == math.ceil(((parts[0].pos[2] - i.syscm[2]) * box[2] - i.minorder[0]) / i.dorder[0])
 
 
 def test_order1_fixed_weights_sample_the_reference_distribution():
@@ -238,9 +248,12 @@ def test_order1_fixed_weights_sample_the_reference_distribution():
 
     got = np.array([moments(s.wl_weights()[1] - h) for s, h in zip(ws, h0)])
     ref = np.array([moments(r["hist"]) for r in c["ref_runs"]])
+    w0 = ws[0].wl_weights()[0]
     for s in ws:
-        assert np.array_equal(s.wl_weights()[0], ws[0].wl_weights()[0])     # alpha 0: fixed
+        assert np.array_equal(s.wl_weights()[0], w0)                       # alpha 0: fixed
+    for s in ws:
         s.close()
+    print("order 1 fixed weights (GPU, reference: mean bin, bin variance):", got.mean(0), ref.mean(0))
     for k, name in enumerate(("mean bin", "bin variance")):
         se = math.sqrt(got[:, k].var(ddof=1) / len(got) + ref[:, k].var(ddof=1) / len(ref))
         assert abs(got[:, k].mean() - ref[:, k].mean()) <= 2.0 * se, (name, got[:, k], ref[:, k])
