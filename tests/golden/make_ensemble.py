@@ -144,7 +144,7 @@ def cases():
         config=config_text(box, np.vstack([sp, ps]), np.vstack([rand_unit(rng, 20), ds]),
                            np.vstack([rand_perp(rng, rand_unit(rng, 20)), qs])),
         opts=dict(temper=1.0, transmx=0.5, rotmx=30.0, nGrandCanon=1, pairlist_update=0),
-        nsweeps=24000, report=20, seeds=16, burn=4000, gc=True)
+        nsweeps=24000, report=20, seeds=48, burn=4000, gc=True)
     # type switching (switchTypeMove): PSC particles that switch to a CPSC type and back with a
     # chemical-potential difference of 1.6 (read as the int 1 by the reference), beside fixed
     # spheres; the switched fraction from the movie frames' switched column

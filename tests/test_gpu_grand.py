@@ -98,6 +98,34 @@ def test_ensemble_matches_reference(name, batched):
         assert abs(mean - rm) <= 2.0 * math.sqrt(se ** 2 + rse ** 2), report
 
 
+def test_batched_systems_reproduce_single_runs():
+    """Grand-canonical systems moved together as a replica batch (no exchanges) follow the
+    same trajectories, bit for bit, as the same systems run one at a time with the seeds the
+    batch derives for them: the moves, the counts and the particle order do not depend on
+    the batch."""
+    from test_gpu_replicas import GOLDEN
+    from sc_gb300 import ReplicaSet, System
+
+    g, opts, top, cfg = _case("gc_psc")
+    sysA = [System.from_text(opts, top, cfg) for _ in range(3)]
+    sysB = [System.from_text(opts, top, cfg) for _ in range(3)]
+    R = ReplicaSet(sysA, [1.0] * 3, ladder=[0, 1, 2])
+    p = sysA[0].default_run()
+    p.check_every = 0
+    _, _, E, _, _ = R.run(200, exchange_every=0, seed=77, params=p, stencil=2)
+    R.close()
+    for k, s in enumerate(sysB):
+        q = s.default_run()
+        q.check_every = 0
+        single = s.simulate(q, nsweeps=200, seed=(77 + GOLDEN * (k + 1)) % (1 << 64), stencil=2)
+        assert sysA[k].n == s.n, (k, sysA[k].n, s.n)
+        pa, pb = sysA[k].particles(), s.particles()
+        assert [list(x.pos) for x in pa] == [list(y.pos) for y in pb]
+        assert single.energy == E[k]
+    for s in sysA + sysB:
+        s.close()
+
+
 def test_growth_from_an_empty_box():
     """A crowding species from an empty box: the free slots run out and grow (first 256),
     the count passes them, and the running energy stays exact."""
