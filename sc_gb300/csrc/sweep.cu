@@ -4279,7 +4279,10 @@ static int runBatch(Batch& b, const sc_run_params& p, long nsweeps, int exchange
                 if (nUpper[k] >= 0) nUpper[k] += 1;
         }
         if (nextCheck > 0 && sw >= nextCheck) {
-            // the cell list (box fractions) stays valid after an accepted volume move
+            // the cell list (box fractions) stays valid after an accepted volume move, not after
+            // chain moves (particles left their cells) or grand-canonical moves (slots moved):
+            // then it is built anew, on the sweep's grid
+            if ((b.chains || gc) && (r = launchCells()) != cudaSuccess) return cudaFail(r, "cell list");
             if ((r = exactEnergy(true)) != cudaSuccess) return cudaFail(r, "energy check");
             while (nextCheck <= sw) nextCheck += p.check_every;
         }

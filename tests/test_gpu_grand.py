@@ -126,6 +126,28 @@ def test_batched_systems_reproduce_single_runs():
         s.close()
 
 
+def test_energy_checks_during_grand_and_chain_moves():
+    """The exact-energy checks inside a run (check_every) see the particles where they are:
+    after grand-canonical moves (slots moved) and chain moves (particles left their cells) the
+    cell list is built anew, so the largest drift stays at rounding level."""
+    from sc_gb300 import System, workloads
+
+    opts_text, top, config = workloads.lipids_dilute(24, seed=5)
+    top = top.replace("[System]", "S: {\nparticles: 9\nACTIVITY: 0.05\n}\n[System]", 1)
+    top = top.replace("[Molecules]", "S 9 SPA 0.5 1.0 1.1225 0.3775\n[Molecules]", 1)
+    top = top.rstrip("\n") + "\nS 0\n"
+    o = dict(l.split(" = ") for l in opts_text.strip().splitlines())
+    o.update(nGrandCanon="1", chainprob="0.2")
+    s = System.from_text("".join(f"{k} = {v}\n" for k, v in o.items()), top, config)
+    p = s.default_run()
+    p.check_every = 7
+    p.seed = 4
+    st = s.simulate(p, nsweeps=300)
+    assert st.acc_insert > 0 and st.acc_chain > 0
+    assert st.max_drift <= 1e-9 * max(1.0, abs(st.energy)), (st.max_drift, st.energy)
+    s.close()
+
+
 def test_growth_from_an_empty_box():
     """A crowding species from an empty box: the free slots run out and grow (first 256),
     the count passes them, and the running energy stays exact."""
