@@ -18,6 +18,7 @@ BUILDERS = {
     "npt_cpsc_spa": lambda n, seed: workloads.npt_cpsc_spa(n, seed=seed),
     "nvt_psc": lambda n, seed: workloads.nvt_psc(n, seed=seed),
     "bilayers": lambda n, seed: workloads.bilayers(max(1, int(round((n / 12) ** 0.5))), seed=seed),
+    "psc_grand_switch": lambda n, seed: workloads.nvt_psc_grand_switch(n, seed=seed),
 }
 
 

@@ -352,6 +352,17 @@ def pt_ladders(n_ladders=8, per_ladder=8, seed=1, n_range=(500, 4000), phi_range
     return systems, temps
 
 
+def nvt_psc_grand_switch(n=1000, phi=0.1, seed=1, temper=1.0, activity=0.01, switchprob=0.1):
+    """nvt_psc with its molecule grand-canonical (top.init ACTIVITY, one insert / delete move
+    per sweep) and switchable to a CPSC type of the same length (patch 120 degrees, delta_mu
+    1), switchprob type switch attempts per particle move."""
+    opts, top, cfg = nvt_psc(n, phi=phi, seed=seed, temper=temper)
+    top = top.replace("particles: 1\n", f"particles: 1 2 1.0\nACTIVITY: {activity}\n", 1)
+    top = top.replace("[Molecules]", "Q 2 CPSC 1.0 1.0 1.12 0.2 120.0 10.0 3.0 0.0\n[Molecules]", 1)
+    opts = opts.replace("nGrandCanon = 0", "nGrandCanon = 1").replace("switchprob = 0.0", f"switchprob = {switchprob}")
+    return opts, top, cfg
+
+
 WORKLOADS = {
     "npt_cpsc_spa_4000": lambda seed=1: npt_cpsc_spa(4000, seed=seed),
     "nvt_psc_1000": lambda seed=1: nvt_psc(1000, seed=seed),
