@@ -244,6 +244,29 @@ def synthetic_cases():
         options=options_text(transmx=0.2, rotmx=10.0, chainprob=0.1),
         top=top_text(types, [("L", [1, 2, 2], ["bond1: 50.0 1.0"])], [("L", nmol)]),
         config=config_text(box, pos, dirs, rand_perp(rng, dirs)))
+
+    # switch types ("particles: TYPE SWITCHTYPE DELTA_MU"), and particles that config.init
+    # marks switched (they start in their switch type, whose patch vectors Particle::init
+    # derives): PSC <-> CPSC, TPSC <-> TCHPSC, and spheres without a switch type
+    rng_s = np.random.default_rng(20261204)
+    types = [("P", 1, "PSC", [1.0, 1.0, 1.12, 0.2, 90.0, 10.0, L, 0.0]),
+             ("C", 2, "CPSC", [1.2, 1.1, 1.23, 0.25, 120.0, 10.0, L, 0.0]),
+             ("T", 3, "TPSC", [1.0, 1.0, 1.12, 0.2, 90.0, 10.0, L, 0.0, 180.0, 90.0, 10.0]),
+             ("V", 4, "TCHPSC", [1.1, 1.0, 1.12, 0.2, 90.0, 10.0, L, 0.0, 150.0, 90.0, 10.0, 12.0]),
+             ("A", 5, "SPA", [0.8, 1.0, 1.1225, 0.4])]
+    counts = [("M", 40), ("N", 30), ("S", 30)]
+    n = sum(c for _, c in counts)
+    box = np.array([11.0, 11.5, 12.0])
+    pos = rng_s.uniform(0, 1, (n, 3)) * box
+    dirs = rand_unit(rng_s, n)
+    flags = np.concatenate([rng_s.integers(0, 2, 70), np.zeros(30, int)])
+    cfg = config_text(box, pos, dirs, rand_perp(rng_s, dirs))
+    lines = cfg.splitlines()
+    lines = [lines[0]] + [l[:-1] + str(f) for l, f in zip(lines[1:], flags)]    # the switched column
+    cases["switched_types"] = dict(
+        options=options_text(transmx=0.2, rotmx=10.0, switchprob=0.1),
+        top=top_text(types, [("M", ["1 2 0.7"], []), ("N", ["3 4 -1.5"], []), ("S", [5], [])], counts),
+        config="\n".join(lines) + "\n")
     return cases
 
 
@@ -269,7 +292,8 @@ def main():
     dirs = [(f"ref_{d}", os.path.join(tests, d, "new"), f"Tests/{d}/new") for d in fixtures]
     dirs += [(f"ref_volumeChange_{v}", os.path.join(tests, "volumeChange", v, "new"), f"Tests/volumeChange/{v}/new")
              for v in sorted(os.listdir(os.path.join(tests, "volumeChange"))) if os.path.isdir(os.path.join(tests, "volumeChange", v))]
-    for name, src, origin in dirs:
+    only = sys.argv[2:]          # synthetic case names: regenerate those only
+    for name, src, origin in ([] if only else dirs):
         with tempfile.TemporaryDirectory() as tmp:
             inputs = {}
             for fn in ("options", "top.init", "config.init"):
@@ -277,6 +301,8 @@ def main():
                 inputs[fn] = open(os.path.join(src, fn), encoding="latin-1").read()
             save(name, inputs, run_dump(tmp), origin)
     for name, c in synthetic_cases().items():
+        if only and name not in only:
+            continue
         with tempfile.TemporaryDirectory() as tmp:
             inputs = {"options": c["options"], "top.init": c["top"], "config.init": c["config"]}
             for fn, txt in inputs.items():
