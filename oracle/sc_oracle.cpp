@@ -1052,6 +1052,8 @@ struct or_mc {
     long sweep = 1;                  // current sweep (1-based, as updater.cpp)
     long step = 1;                   // next step of the current sweep (1..N)
     double setupSeconds = 0.0;
+    double swprob = 0.0;             // switchprob when switchable particles exist, else 0
+    std::vector<int> switchable;     // the particles with a switch type, in index order
 };
 
 namespace {
@@ -1129,6 +1131,41 @@ double mcAllPairs(or_mc& m, std::vector<double>* out) {
     return e;
 }
 
+// MoveCreator::switchTypeMove (movecreator.cpp:233-303): a uniformly chosen particle with a
+// switch type takes the other type of its pair, Particle::init re-derives its patch vectors,
+// and moveTry(E_old, E_new + delta_mu (1 - 2 switched)) decides; a rejected switch
+// re-initialises the vectors for the old type, as the reference does.  The reference draws
+// the particle through ParticleVector::getSwitchPart over the molecule types; here the
+// switchable particles are listed once in index order and one is drawn uniformly.
+void switchMove(or_mc& m, or_mc_stats* st) {
+    or_system* s = m.s;
+    const or_mc_opts& o = m.o;
+    const int nsw = (int)m.switchable.size();
+    int k = (int)(m.rng() * nsw);
+    if (k >= nsw) k = nsw - 1;
+    const int t = m.switchable[k];
+    const double eold = mcOld(m, t);
+    const int sw = o.switched[t];
+    const int pmone = 1 - 2 * sw;
+    const int oldType = s->p[t].type, newType = o.switch_other[t];
+    s->p[t].type = newType;
+    or_particle_init(&s->p[t], &P(s, newType, newType));
+    const double switchE = (double)(o.switch_dmu[t] * pmone);
+    const double enew = mcTrial(m, t);
+    const bool rej = !(enew + switchE <= eold) && !(exp(-1.0 * (enew + switchE - eold) / o.temper) > m.rng());
+    if (rej) {
+        s->p[t].type = oldType;
+        or_particle_init(&s->p[t], &P(s, oldType, oldType));
+        ++st->rej_switch;
+    } else {
+        m.energy += enew - eold;
+        mcCommit(m, t);
+        o.switch_other[t] = oldType;
+        o.switched[t] = sw + pmone;
+        ++st->acc_switch;
+    }
+}
+
 }  // namespace
 
 extern "C" or_mc* or_mc_open(or_system* s, const or_mc_opts* o) {
@@ -1159,6 +1196,12 @@ extern "C" or_mc* or_mc_open(or_system* s, const or_mc_opts* o) {
         m->energy = or_all_to_all(s);
     }
     if (m->list) m->pl.build(s, m->cut2);          // before the first sweep (updater.cpp:176-190)
+    if (o->switchprob > 0.0 && o->switch_other && o->switch_dmu && o->switched) {
+        for (int i = 0; i < s->n; ++i)
+            if (o->switch_other[i] >= 0) m->switchable.push_back(i);
+        // no switchable particle: no switch moves (initSwitchList, inicializer.cpp:77-81)
+        if (!m->switchable.empty()) m->swprob = o->switchprob;
+    }
     m->setupSeconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return m;
 }
@@ -1201,6 +1244,10 @@ extern "C" int or_mc_advance(or_mc* m, long moves, or_mc_stats* st) {
                 m->energy = enew;
                 if (m->matrix) std::swap(m->em, m->emTrial);   // update(): swapEMatrices
             }
+            continue;
+        }
+        if (u < m->shprob + m->swprob) {      // updater.cpp:219-222 (this loop has no chain moves)
+            switchMove(*m, st);
             continue;
         }
         int target = (int)(m->rng() * N);

@@ -1,7 +1,8 @@
 /* sc_oracle.h -- CPU oracle for the SC Metropolis hot path.
  *
  * TEST INFRASTRUCTURE ONLY.  This is a plain C++ restatement of the reference's
- * pair energy, one-particle / total energy and single-particle move loop
+ * pair energy, one-particle / total energy and single-particle move loop (with its volume
+ * and type switch moves)
  * (robertvacha/SC, scOOP/mc/paire.h, paire.cpp, totalenergycalculator.h,
  * movecreator.cpp, updater.cpp, structures/topo.cpp, particle.*), used by the
  * tests as the checker and by bench.py as the timed CPU baseline.  The product
@@ -108,6 +109,13 @@ typedef struct {
     int energy_matrix;   /* 1: TotalEMatrix (old energies from the stored pair energies, the reference's
                             default); 0: TotalEFull (old and new energies by pair evaluation) */
     int pad_;
+    /* type switching (MoveCreator::switchTypeMove, movecreator.cpp:233-303), chosen with
+     * probability switchprob per step after the volume move's shprob (updater.cpp:219-222; this
+     * loop makes no chain moves); the arrays are per particle, NULL without switching */
+    double switchprob;
+    int* switch_other;       /* the other type of the particle's switch pair, -1 for none (swapped by moves) */
+    const int* switch_dmu;   /* delta_mu as the reference's move reads it (an int) */
+    int* switched;           /* 1 while the particle is in its switch type (updated by moves) */
 } or_mc_opts;
 
 typedef struct {
@@ -115,6 +123,7 @@ typedef struct {
     double energy;       /* running total energy */
     double energy_start;
     double seconds;
+    long acc_switch, rej_switch;
 } or_mc_stats;
 
 int or_mc_run(or_system* s, const or_mc_opts* o, or_mc_stats* st);

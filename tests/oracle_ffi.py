@@ -59,13 +59,16 @@ class McOpts(C.Structure):
                 ("shave", C.c_double), ("chainprob", C.c_double), ("transmx", C.c_double),
                 ("rot_angle", C.c_double), ("edge_mx", C.c_double), ("chainmmx", C.c_double),
                 ("chainr_angle", C.c_double), ("ptype", C.c_int), ("pairlist_update", C.c_int),
-                ("max_moves", C.c_long), ("energy_matrix", C.c_int), ("pad_", C.c_int)]
+                ("max_moves", C.c_long), ("energy_matrix", C.c_int), ("pad_", C.c_int),
+                ("switchprob", C.c_double), ("switch_other", C.POINTER(C.c_int)), ("switch_dmu", C.POINTER(C.c_int)),
+                ("switched", C.POINTER(C.c_int))]
 
 
 class McStats(C.Structure):
     _fields_ = [(k, C.c_long) for k in ("moves", "acc_trans", "rej_trans", "acc_rot", "rej_rot", "acc_vol",
                                         "rej_vol", "acc_chain", "rej_chain")] + [
-        ("energy", C.c_double), ("energy_start", C.c_double), ("seconds", C.c_double)]
+        ("energy", C.c_double), ("energy_start", C.c_double), ("seconds", C.c_double),
+        ("acc_switch", C.c_long), ("rej_switch", C.c_long)]
 
 
 class WlState(C.Structure):
@@ -322,8 +325,10 @@ def molecules(top):
             elif cur is not None and ":" in line:
                 k, v = line.split(":", 1)
                 k = k.strip().lower()
-                if k == "particles":
-                    cur["types"].append(int(v.split()[0]))
+                if k == "particles":     # TYPE [SWITCHTYPE DELTA_MU] (inicializer.cpp:955-985)
+                    w = v.split()
+                    cur["types"].append(int(w[0]))
+                    cur.setdefault("switch", []).append((int(w[1]), float(w[2])) if len(w) >= 3 else (-1, 0.0))
                 else:
                     cur["bonds"][k] = [float(x) for x in v.split()[:2]]
         elif key == "SYSTEM":
@@ -353,15 +358,16 @@ class TextSystem:
         if lib().or_derive_params(arr, len(types), excl.ctypes.data, self.params, C.byref(sq), C.byref(mc)) != 0:
             raise ValueError("oracle: top.init rejected")
         defs, order = molecules(top)
-        ptypes, pmol = [], []
+        ptypes, pmol, psw = [], [], []
         first = {}
         for name, cnt in order:
             m = next(k for k, d in enumerate(defs) if d["name"] == name)
             first.setdefault(m, (len(ptypes), cnt))
             for _ in range(cnt):
-                for ty in defs[m]["types"]:
+                for q, ty in enumerate(defs[m]["types"]):
                     ptypes.append(ty)
                     pmol.append(m)
+                    psw.append(defs[m].get("switch", [(-1, 0.0)] * len(defs[m]["types"]))[q])
         self.mols = (MolType * max(1, len(defs)))()
         for k, d in enumerate(defs):
             ms = self.mols[k]
@@ -378,6 +384,10 @@ class TextSystem:
         if len(lines) - 1 < n:
             raise ValueError("config.init: fewer particle lines than [System] declares")
         self.parts = (Particle * n)()
+        # per particle: the other type of its switch pair (-1: none), delta_mu as the move's int
+        self.switch_other = (C.c_int * max(1, n))(*([t for t, _ in psw] + [0] * (n == 0)))
+        self.switch_dmu = (C.c_int * max(1, n))(*([int(d) for _, d in psw] + [0] * (n == 0)))
+        self.switched = (C.c_int * max(1, n))()
         for i in range(n):
             f = [float(x) for x in lines[1 + i].split()[:9]]
             pos = [f[0] / box[0], f[1] / box[1], f[2] / box[2]]
@@ -393,6 +403,12 @@ class TextSystem:
             p = self.parts[i]
             p.pos, p.dir, p.pd[0] = vec(pos), vec(d), vec(pd)
             p.type, p.molType = ptypes[i], pmol[i]
+            # the switched column: the particle starts in its switch type (inicializer.cpp:226-236)
+            fields = lines[1 + i].split()
+            if len(fields) >= 10 and int(fields[9]) and psw[i][0] >= 0:
+                self.switched[i] = 1
+                p.type = psw[i][0]
+                self.switch_other[i] = ptypes[i]
         for k, d in enumerate(defs):                # Conf::makeMoleculeWhole
             size = len(d["types"])
             if size <= 1:
@@ -429,6 +445,8 @@ class TextSystem:
         o.ptype = int(opts.get("ptype", "0").split()[0])
         o.pairlist_update = int(opts.get("pairlist_update", "0"))
         o.nsweeps = int(opts.get("nsweeps", "0"))
+        o.switchprob = float(opts.get("switchprob", "0"))
+        o.switch_other, o.switch_dmu, o.switched = self.switch_other, self.switch_dmu, self.switched
         self.opts = o
 
     def all_to_all(self):

@@ -74,3 +74,64 @@ def test_particle_line_needs_one_or_three_fields(lib):
     assert "could not read a particle" in str(ei.value)
     with pytest.raises(ScError):
         System.from_text(opts, top.replace("particles: 1 2 1.6", "particles: 1 7 1.6"), cfg)
+
+
+def test_oracle_switch_of_a_lone_particle_follows_delta_mu():
+    """The oracle's restatement of switchTypeMove on one PSC alone in a box: with no partner
+    the switched fraction is exp(-dmu/T) / (1 + exp(-dmu/T)), dmu read as the reference's int
+    (1.7 acts as 1)."""
+    import math
+
+    import numpy as np
+
+    import oracle_ffi as O
+    from golden.make_golden import options_text, top_text
+
+    top = top_text([("P", 1, "PSC", [1.0, 1.0, 1.12, 0.2, 90.0, 10.0, 3.0, 0.0]),
+                    ("C", 2, "CPSC", [1.0, 1.0, 1.12, 0.2, 120.0, 10.0, 3.0, 0.0])],
+                   [("M", ["1 2 1.7"], [])], [("M", 1)])
+    ts = O.TextSystem(options_text(switchprob=0.5, transmx=0.2, rotmx=10.0), top, "20 20 20\n1 1 1 0 0 1 1 0 0 0\n")
+    run = O.McRun(ts, seed=5)
+    frac = []
+    for _ in range(400):
+        st = run.advance(500)
+        frac.append(ts.switched[0])
+    run.close()
+    want = math.exp(-1.0) / (1.0 + math.exp(-1.0))
+    assert st.acc_switch > 1000 and st.rej_switch > 1000
+    assert abs(np.mean(frac) - want) < 0.06, (np.mean(frac), want)
+    # every accepted switch flipped the type and the flag together
+    assert (ts.parts[0].type == 2) == (ts.switched[0] == 1)
+
+
+def test_oracle_switching_samples_the_reference_ensemble():
+    """The oracle's switch moves on the switching golden's system (150 PSC <-> CPSC with
+    delta_mu 1.6, 50 spheres): the switched fraction and the energy per particle of four
+    short oracle runs agree with the reference's own twelve long runs within 3 combined
+    standard errors."""
+    import math
+
+    import numpy as np
+
+    import oracle_ffi as O
+
+    opts, top, cfg = _case()
+    with open(os.path.join(GOLDEN, "ens_switch_psc.json")) as f:
+        g = json.load(f)
+    F, E = [], []
+    for seed in (11, 12, 13, 14):
+        ts = O.TextSystem(opts, top, cfg)
+        run = O.McRun(ts, seed=seed, fast=True)
+        f_ser, e_ser = [], []
+        for k in range(150):                  # 3000 sweeps, samples every 20 after 600
+            st = run.advance(20 * ts.sys.n)
+            if k >= 30:
+                f_ser.append(sum(ts.switched[i] for i in range(150)) / 150.0)
+                e_ser.append(st.energy / ts.sys.n)
+        run.close()
+        F.append(np.mean(f_ser))
+        E.append(np.mean(e_ser))
+    for key, got in (("switched_fraction", F), ("energy_per_particle", E)):
+        ref = g["stats"][key]
+        se = math.sqrt(np.var(got, ddof=1) / len(got) + ref["se"] ** 2)
+        assert abs(np.mean(got) - ref["mean"]) <= 3.0 * se, (key, np.mean(got), ref)
