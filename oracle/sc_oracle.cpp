@@ -1054,6 +1054,7 @@ struct or_mc {
     double setupSeconds = 0.0;
     double swprob = 0.0;             // switchprob when switchable particles exist, else 0
     std::vector<int> switchable;     // the particles with a switch type, in index order
+    bool gc = false;                 // grand-canonical moves after every grand_every-th sweep
 };
 
 namespace {
@@ -1166,10 +1167,88 @@ void switchMove(or_mc& m, or_mc_stats* st) {
     }
 }
 
+// After a grand-canonical move changed N: the loop's count, the energy matrix and the pair
+// list built anew (updater.cpp:166-179: initEM, genPairList); the running energy continues.
+void gcResize(or_mc& m) {
+    m.N = m.s->n;
+    if (m.matrix) {
+        const size_t sz = (size_t)m.N * (m.N > 0 ? m.N - 1 : 0) / 2 + 1;
+        m.em.assign(sz, 0.0);
+        m.emTrial.assign(sz, 0.0);
+        mcAllPairs(m, &m.em);
+    }
+    if (m.list) m.pl.build(m.s, m.cut2);
+}
+
+// MoveCreator::muVTMove (movecreator.cpp:797-924) for single-particle species: a species
+// drawn uniformly (getRandomMuVTType); with probability 1/2 a particle at a uniform position
+// with uniform axis and patch direction (Particle::init) is inserted at the end of the
+// species' block if V/(N+1) exp(chemPot - E/T) > u, else a uniformly chosen particle of the
+// species is removed if N/V exp(E/T - chemPot) > u; E is the particle against every other
+// with an empty conlist (mol2others), the particles behind the slot move by one.
+void gcMove(or_mc& m, or_mc_stats* st) {
+    or_system* s = m.s;
+    const or_mc_opts& o = m.o;
+    int k = (int)(m.rng() * o.n_gc);
+    if (k >= o.n_gc) k = o.n_gc - 1;
+    const int mt = o.gc_moltype[k];
+    or_moltype* mols = const_cast<or_moltype*>(s->mols);    // the caller's records, kept current
+    const int count = mols[mt].count;
+    const double V = s->box[0] * s->box[1] * s->box[2];
+    const Con empty;
+    if (m.rng() > 0.5) {
+        or_particle np;
+        std::memset(&np, 0, sizeof np);
+        np.pos.x = m.rng(); np.pos.y = m.rng(); np.pos.z = m.rng();
+        np.dir = randomUnitSphere(m.rng);
+        np.pd[0] = randomUnitSphere(m.rng);
+        np.type = o.gc_type[k];
+        np.molType = mt;
+        or_particle_init(&np, &P(s, np.type, np.type));
+        if (s->n >= o.gc_cap) { ++st->rej_insert; return; }      // no slot left (the caller sizes gc_cap)
+        s->p[s->n] = np;                                          // the candidate, past the last particle
+        double E = 0.0;
+        for (int j = 0; j < s->n; ++j) E += pairEnergyCon(s, s->n, j, empty, nullptr, nullptr);
+        if ((V / (count + 1.0)) * exp(o.gc_chempot[k] - E / o.temper) > m.rng()) {
+            const int slot = mols[mt].first + count;
+            std::memmove(&s->p[slot + 1], &s->p[slot], sizeof(or_particle) * (size_t)(s->n - slot));
+            s->p[slot] = np;
+            mols[mt].count += 1;
+            for (int q = mt + 1; q < s->nmol; ++q) mols[q].first += 1;
+            s->n += 1;
+            m.energy += E;
+            ++st->acc_insert;
+            gcResize(m);
+        } else {
+            ++st->rej_insert;
+        }
+    } else {
+        if (count == 0) { ++st->rej_delete; return; }
+        int t = mols[mt].first + (int)(m.rng() * count);
+        if (t >= mols[mt].first + count) t = mols[mt].first + count - 1;
+        double E = 0.0;
+        for (int j = 0; j < s->n; ++j)
+            if (j != t) E += pairEnergyCon(s, t, j, empty, nullptr, nullptr);
+        if (((double)count / V) * exp(E / o.temper - o.gc_chempot[k]) > m.rng()) {
+            std::memmove(&s->p[t], &s->p[t + 1], sizeof(or_particle) * (size_t)(s->n - t - 1));
+            mols[mt].count -= 1;
+            for (int q = mt + 1; q < s->nmol; ++q) mols[q].first -= 1;
+            s->n -= 1;
+            m.energy -= E;
+            ++st->acc_delete;
+            gcResize(m);
+        } else {
+            ++st->rej_delete;
+        }
+    }
+}
+
 }  // namespace
 
 extern "C" or_mc* or_mc_open(or_system* s, const or_mc_opts* o) {
-    if (!s || !o || s->n <= 0) return nullptr;
+    const bool gc = o && o->grand_every > 0 && o->n_gc > 0 && o->gc_moltype && o->gc_type && o->gc_chempot;
+    if (!s || !o || (s->n <= 0 && !gc)) return nullptr;
+    if (gc && o->switchprob > 0.0) return nullptr;             // not combined with switching here
     if (o->shave > 0.0 && o->ptype != 1) return nullptr;     // ptype 1 volume moves only
     auto t0 = std::chrono::steady_clock::now();
     or_mc* m = new or_mc();
@@ -1177,7 +1256,8 @@ extern "C" or_mc* or_mc_open(or_system* s, const or_mc_opts* o) {
     m->o = *o;
     m->rng = Rng{(uint64_t)o->seed * 0x2545F4914F6CDD1Dull + 1};
     m->N = s->n;
-    m->shprob = o->shave / (double)s->n;
+    m->shprob = s->n > 0 ? o->shave / (double)s->n : 0.0;
+    m->gc = gc;
     m->matrix = o->energy_matrix != 0;
     if (o->pairlist_update > 0) {
         // the pair-list cutoff of main.cpp:117-126 (equal step sizes: AVER is the step)
@@ -1218,14 +1298,28 @@ extern "C" int or_mc_advance(or_mc* m, long moves, or_mc_stats* st) {
     if (!m || !st || moves < 0) return -1;
     or_system* s = m->s;
     const or_mc_opts* o = &m->o;
-    const int N = m->N;
     auto t0 = std::chrono::steady_clock::now();
+    // the end of a sweep: its grand-canonical move when one is due (updater.cpp:164-179)
+    auto endSweep = [&]() {
+        if (m->gc && m->sweep % o->grand_every == 0) gcMove(*m, st);
+        m->step = 1;
+        ++m->sweep;
+    };
     long done = 0;
     while (done < moves) {
-        if (m->step > N) { m->step = 1; ++m->sweep; }
+        if (m->N == 0) {                    // an empty box: a sweep of no steps, counted as one
+            ++done;
+            endSweep();
+            continue;
+        }
+        if (m->step > m->N) {
+            endSweep();
+            if (m->N == 0) continue;        // its grand-canonical move emptied the box
+        }
         if (m->step == 1 && m->list && m->sweep > 1 && m->sweep % o->pairlist_update == 0) m->pl.build(s, m->cut2);
         ++m->step;
         ++done;
+        const int N = m->N;
         double u = m->rng();
         if (u < m->shprob) {
             // pressureMove, ptype 1 (movecreator.cpp:390-421)
@@ -1277,9 +1371,22 @@ extern "C" int or_mc_advance(or_mc* m, long moves, or_mc_stats* st) {
             if (displace) ++st->acc_trans; else ++st->acc_rot;
         }
     }
+    if (m->N > 0 && m->step > m->N) endSweep();  // the block ended on a sweep's last step
     st->moves += done;
     st->energy = m->energy;
     st->seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return 0;
+}
+
+// Runs whole sweeps: the steps left in the current sweep, then full sweeps of the particle
+// count each has at its start (grand-canonical moves change it between sweeps).
+extern "C" int or_mc_sweeps(or_mc* m, long sweeps, or_mc_stats* st) {
+    if (!m || !st || sweeps < 0) return -1;
+    const long target = m->sweep + sweeps;
+    while (m->sweep < target) {
+        const long left = m->N > 0 ? m->N - m->step + 1 : 1;
+        if (or_mc_advance(m, left, st) != 0) return -1;
+    }
     return 0;
 }
 
@@ -1290,7 +1397,7 @@ extern "C" int or_mc_run(or_system* s, const or_mc_opts* o, or_mc_stats* st) {
     st->energy_start = m->energy;
     long total = o->nsweeps * (long)s->n;
     if (o->max_moves > 0 && o->max_moves < total) total = o->max_moves;
-    int rc = or_mc_advance(m, total, st);
+    int rc = m->gc ? or_mc_sweeps(m, o->nsweeps, st) : or_mc_advance(m, total, st);
     st->seconds += m->setupSeconds;
     or_mc_close(m);
     return rc;

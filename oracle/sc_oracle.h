@@ -1,8 +1,8 @@
 /* sc_oracle.h -- CPU oracle for the SC Metropolis hot path.
  *
  * TEST INFRASTRUCTURE ONLY.  This is a plain C++ restatement of the reference's
- * pair energy, one-particle / total energy and single-particle move loop (with its volume
- * and type switch moves)
+ * pair energy, one-particle / total energy and single-particle move loop (with its volume,
+ * type switch and grand-canonical moves)
  * (robertvacha/SC, scOOP/mc/paire.h, paire.cpp, totalenergycalculator.h,
  * movecreator.cpp, updater.cpp, structures/topo.cpp, particle.*), used by the
  * tests as the checker and by bench.py as the timed CPU baseline.  The product
@@ -116,6 +116,14 @@ typedef struct {
     int* switch_other;       /* the other type of the particle's switch pair, -1 for none (swapped by moves) */
     const int* switch_dmu;   /* delta_mu as the reference's move reads it (an int) */
     int* switched;           /* 1 while the particle is in its switch type (updated by moves) */
+    /* grand-canonical moves (MoveCreator::muVTMove, movecreator.cpp:797-924), one after every
+     * grand_every-th sweep (updater.cpp:164-179), for n_gc single-particle species; the system's
+     * particle array holds gc_cap slots and its n, and the molecule records' first / count,
+     * follow the moves (not combined with switching) */
+    int grand_every, n_gc, gc_cap, pad2_;
+    const int* gc_moltype;   /* molecule type of each species */
+    const int* gc_type;      /* its particle type */
+    const double* gc_chempot;   /* log(activity Nav 1e-24) (inicializer.cpp:1094) */
 } or_mc_opts;
 
 typedef struct {
@@ -124,17 +132,22 @@ typedef struct {
     double energy_start;
     double seconds;
     long acc_switch, rej_switch;
+    long acc_insert, rej_insert, acc_delete, rej_delete;
 } or_mc_stats;
 
 int or_mc_run(or_system* s, const or_mc_opts* o, or_mc_stats* st);
 
 /* The same loop as a resumable state, so that the moves can be timed apart from the set-up
  * the reference does before its timed loop (initial energy / energy matrix, first pair
- * list).  or_mc_open returns NULL for an empty system or volume moves of a ptype other than
- * 1; or_mc_advance runs `moves` more steps and adds to *st (moves, acceptances, seconds). */
+ * list).  or_mc_open returns NULL for an empty system without grand-canonical species,
+ * volume moves of a ptype other than 1, or grand-canonical moves together with switching;
+ * or_mc_advance runs `moves` more steps and adds to *st (moves, acceptances, seconds). */
 typedef struct or_mc or_mc;
 or_mc* or_mc_open(or_system* s, const or_mc_opts* o);
 int or_mc_advance(or_mc* m, long moves, or_mc_stats* st);
+/* Runs the rest of the current sweep and then sweeps-1 more (grand-canonical runs count sweeps,
+ * since their particle count changes between sweeps). */
+int or_mc_sweeps(or_mc* m, long sweeps, or_mc_stats* st);
 double or_mc_energy(const or_mc* m);
 double or_mc_setup_seconds(const or_mc* m);
 void or_mc_close(or_mc* m);

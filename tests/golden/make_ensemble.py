@@ -126,7 +126,7 @@ def cases():
         top=top_text([("A", 1, "SPA", [1.0, 1.0, 1.1225, 0.5])], [("A", [1], ["ACTIVITY: 0.1"])], [("A", 30)]),
         config=config_text(box, pos, rand_unit(rng, 30), rand_perp(rng, rand_unit(rng, 30))),
         opts=dict(temper=1.0, transmx=0.6, rotmx=30.0, nGrandCanon=1, pairlist_update=0),
-        nsweeps=24000, report=20, seeds=8, burn=4000, gc=True)
+        nsweeps=24000, report=20, seeds=32, burn=4000, gc=True)
     box = np.full(3, 12.0)
     ps, ds, qs = place(rng, 15, box, L)
     sp = []

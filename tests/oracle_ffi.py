@@ -61,14 +61,17 @@ class McOpts(C.Structure):
                 ("chainr_angle", C.c_double), ("ptype", C.c_int), ("pairlist_update", C.c_int),
                 ("max_moves", C.c_long), ("energy_matrix", C.c_int), ("pad_", C.c_int),
                 ("switchprob", C.c_double), ("switch_other", C.POINTER(C.c_int)), ("switch_dmu", C.POINTER(C.c_int)),
-                ("switched", C.POINTER(C.c_int))]
+                ("switched", C.POINTER(C.c_int)), ("grand_every", C.c_int), ("n_gc", C.c_int), ("gc_cap", C.c_int),
+                ("pad2_", C.c_int), ("gc_moltype", C.POINTER(C.c_int)), ("gc_type", C.POINTER(C.c_int)),
+                ("gc_chempot", C.POINTER(C.c_double))]
 
 
 class McStats(C.Structure):
     _fields_ = [(k, C.c_long) for k in ("moves", "acc_trans", "rej_trans", "acc_rot", "rej_rot", "acc_vol",
                                         "rej_vol", "acc_chain", "rej_chain")] + [
         ("energy", C.c_double), ("energy_start", C.c_double), ("seconds", C.c_double),
-        ("acc_switch", C.c_long), ("rej_switch", C.c_long)]
+        ("acc_switch", C.c_long), ("rej_switch", C.c_long), ("acc_insert", C.c_long), ("rej_insert", C.c_long),
+        ("acc_delete", C.c_long), ("rej_delete", C.c_long)]
 
 
 class WlState(C.Structure):
@@ -126,6 +129,8 @@ def _bind(L):
         L.or_mc_open.argtypes = [C.POINTER(System), C.POINTER(McOpts)]
         L.or_mc_advance.restype = C.c_int
         L.or_mc_advance.argtypes = [C.c_void_p, C.c_long, C.POINTER(McStats)]
+        L.or_mc_sweeps.restype = C.c_int
+        L.or_mc_sweeps.argtypes = [C.c_void_p, C.c_long, C.POINTER(McStats)]
         L.or_mc_energy.restype = C.c_double
         L.or_mc_energy.argtypes = [C.c_void_p]
         L.or_mc_setup_seconds.restype = C.c_double
@@ -329,6 +334,8 @@ def molecules(top):
                     w = v.split()
                     cur["types"].append(int(w[0]))
                     cur.setdefault("switch", []).append((int(w[1]), float(w[2])) if len(w) >= 3 else (-1, 0.0))
+                elif k == "activity":    # inicializer.cpp:1087-1096
+                    cur["activity"] = float(v.split()[0])
                 else:
                     cur["bonds"][k] = [float(x) for x in v.split()[:2]]
         elif key == "SYSTEM":
@@ -383,7 +390,10 @@ class TextSystem:
         n = len(ptypes)
         if len(lines) - 1 < n:
             raise ValueError("config.init: fewer particle lines than [System] declares")
-        self.parts = (Particle * n)()
+        # grand-canonical species (single particles with an ACTIVITY): free slots for insertions
+        gcs = [k for k, d in enumerate(defs) if "activity" in d and len(d["types"]) == 1]
+        self.cap = n + (max(256, 2 * n) if gcs else 0)
+        self.parts = (Particle * max(1, self.cap))()
         # per particle: the other type of its switch pair (-1: none), delta_mu as the move's int
         self.switch_other = (C.c_int * max(1, n))(*([t for t, _ in psw] + [0] * (n == 0)))
         self.switch_dmu = (C.c_int * max(1, n))(*([int(d) for _, d in psw] + [0] * (n == 0)))
@@ -423,6 +433,10 @@ class TextSystem:
         for i in range(n):
             t = self.parts[i].type
             lib().or_particle_init(C.byref(self.parts[i]), C.byref(self.params[t * MAXT + t]))
+        self.gc_moltype = (C.c_int * max(1, len(gcs)))(*(gcs or [0]))
+        self.gc_type = (C.c_int * max(1, len(gcs)))(*([defs[k]["types"][0] for k in gcs] or [0]))
+        self.gc_chempot = (C.c_double * max(1, len(gcs)))(
+            *([math.log(defs[k]["activity"] * 6.022137e23 * 1e-24) for k in gcs] or [0.0]))
         self.sys = System()
         self.sys.n, self.sys.nmol = n, len(defs)
         self.sys.p = C.cast(self.parts, C.POINTER(Particle))
@@ -447,6 +461,9 @@ class TextSystem:
         o.nsweeps = int(opts.get("nsweeps", "0"))
         o.switchprob = float(opts.get("switchprob", "0"))
         o.switch_other, o.switch_dmu, o.switched = self.switch_other, self.switch_dmu, self.switched
+        o.grand_every = int(opts.get("nGrandCanon", "0")) if gcs else 0
+        o.n_gc, o.gc_cap = len(gcs), self.cap
+        o.gc_moltype, o.gc_type, o.gc_chempot = self.gc_moltype, self.gc_type, self.gc_chempot
         self.opts = o
 
     def all_to_all(self):
@@ -505,7 +522,8 @@ class McRun:
         o.energy_matrix = 1 if energy_matrix else 0
         self.h = self.L.or_mc_open(C.byref(ts.sys), C.byref(o))
         if not self.h:
-            raise ValueError("oracle: loop refused (empty system or volume moves of a ptype other than 1)")
+            raise ValueError("oracle: loop refused (empty system without grand-canonical species, volume moves "
+                             "of a ptype other than 1, or grand-canonical moves with switching)")
         self.stats = McStats()
 
     @property
@@ -520,6 +538,16 @@ class McRun:
         if self.L.or_mc_advance(self.h, int(moves), C.byref(self.stats)) != 0:
             raise RuntimeError("oracle: or_mc_advance failed")
         return self.stats
+
+    def sweeps(self, n):
+        if self.L.or_mc_sweeps(self.h, int(n), C.byref(self.stats)) != 0:
+            raise RuntimeError("oracle: or_mc_sweeps failed")
+        return self.stats
+
+    @property
+    def n(self):
+        """The particle count now (grand-canonical moves change it)."""
+        return self.ts.sys.n
 
     def close(self):
         if self.h:

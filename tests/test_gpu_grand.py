@@ -3,11 +3,12 @@ scOOP/mc/movecreator.cpp:797-924, one move every nGrandCanon sweeps, updater.cpp
 
 Ensemble parity: tests/golden/ens_gc_spa.json and ens_gc_psc.json hold the mean particle
 count (from the reference's movie frames) and the mean total energy (energy.dat) sampled
-by the reference's own loop (oracle/_ref/sc_ref, eight seeds, tests/golden/make_ensemble.py)
-for attractive spheres exchanged with a reservoir, and for patchy spherocylinders
-exchanged among fixed spheres (the species listed last, so removals inside its block shift
-the particles behind).  The GPU runs eight trajectories from the same start for the same
-sweeps; both means must agree within 2 combined standard errors.
+by the reference's own loop (oracle/_ref/sc_ref, tests/golden/make_ensemble.py) for
+attractive spheres exchanged with a reservoir (32 seeds), and for patchy spherocylinders
+exchanged among fixed spheres (48 seeds; the species listed last, so removals inside its
+block shift the particles behind).  The GPU runs trajectories from the same start for the
+same sweeps (the spheres eight, one at a time; the spherocylinders as many as the
+reference, as one batch); both means must agree within 2 combined standard errors.
 
 Exactness: the running energy (the moves' energy changes, insertions and removals
 included) equals the exact total energy after the run; the particle vector keeps the
@@ -55,7 +56,7 @@ def test_ensemble_matches_reference(name, batched):
     g, opts, top, cfg = _case(name)
     rep, burn, nsw = g["report"], g["burn"], g["nsweeps"]
     N, E = [], []
-    groups = [list(range(g["seeds"]))] if batched else [[k] for k in range(g["seeds"])]
+    groups = [list(range(g["seeds"]))] if batched else [[k] for k in range(min(8, g["seeds"]))]
     for group in groups:
         systems = [System.from_text(opts, top, cfg) for _ in group]
         p = systems[0].default_run()
