@@ -193,7 +193,8 @@ def wl_cpu_baseline(texts, wl_text, seed, max_moves=3000):
     cur = (C.c_long * 2)()
     cm = (C.c_double * 3)()
     sv = C.c_double()
-    if O.lib().or_wl_orders(C.byref(sysm), st.wlm, st.minorder, st.dorder, cur, cm, C.byref(sv)) != 0:
+    st.wlmtype = -1
+    if O.lib().or_wl_orders(C.byref(sysm), st.wlm, -1, st.minorder, st.dorder, cur, cm, C.byref(sv)) != 0:
         raise RuntimeError("oracle: order parameters outside its restatement")
     st.cur[0], st.cur[1] = cur[0], cur[1]
     o.nsweeps, o.max_moves = 1 << 30, max_moves

@@ -1404,13 +1404,140 @@ extern "C" int or_mc_run(or_system* s, const or_mc_opts* o, or_mc_stats* st) {
 }
 
 // ---- Wang-Landau order parameters --------------------------------------------------------
+namespace {
+
+// Order 7 (WangLandau::particlesInContact / contParticlesAll, scOOP/mc/wanglandau.h:603-676):
+// a particle is in contact with particle 0 when its minimum-image distance squared is below
+// WL_CONTACTS = 36 (scOOP/structures/macros.h:107); the count runs over particles 1..N-1 of
+// type wlmtype, the bin is ceil((count - minorder) / dorder) (contParticlesOrder).
+bool wlInContact(const or_system* s, const or_vec& a, const or_vec& p0) {
+    double x = a.x - p0.x, y = a.y - p0.y, z = a.z - p0.z;
+    x = s->box[0] * (x - anint(x));
+    y = s->box[1] * (y - anint(y));
+    z = s->box[2] * (z - anint(z));
+    return x * x + y * y + z * z < 36.0;
+}
+
+long wlContactsAll(const or_system* s, int wlmtype) {
+    long c = 0;
+    for (int i = 1; i < s->n; ++i)
+        if (s->p[i].type == wlmtype && wlInContact(s, s->p[i].pos, s->p[0].pos)) ++c;
+    return c;
+}
+
+long wlContactBin(long count, double minorder, double dorder) {
+    return (long)std::ceil(((double)count - minorder) / dorder);
+}
+
+// Order 2 (Mesh, scOOP/mc/mesh.cpp; WangLandau::meshOrderMoveMolecule, wanglandau.cpp:7-47):
+// an xy mesh of squares sigma(wlmtype) / 3 wide; every particle of type wlmtype occupies
+// the 3 x 3 squares around the one holding it (each occupation counts down from 0); the
+// order is the size of the largest 4-connected periodic cluster of free squares
+// (findHoles), binned as (long)((size - minorder) / dorder).
+double wlInbox(double a) {          // INBOX (macros.h:119)
+    double ip;
+    return a > 0 ? std::modf(a, &ip) : std::modf(a, &ip) + 1;
+}
+
+struct WlMesh {
+    int dim[2] = {0, 0};
+    std::vector<int> data, tmp;
+
+    int square(int x, int y) const { return x + dim[0] * y; }
+    void squares(int x, int y, int sq[9]) const {       // Mesh::meshSquare
+        const int xm = x - 1 < 0 ? dim[0] - 1 : x - 1, xp = x + 1 == dim[0] ? 0 : x + 1;
+        const int ym = y - 1 < 0 ? dim[1] - 1 : y - 1, yp = y + 1 == dim[1] ? 0 : y + 1;
+        sq[0] = square(x, y); sq[1] = square(xm, y); sq[2] = square(xp, y);
+        sq[3] = square(x, ym); sq[4] = square(xm, ym); sq[5] = square(xp, ym);
+        sq[6] = square(x, yp); sq[7] = square(xm, yp); sq[8] = square(xp, yp);
+    }
+    int cellX(double x) const { return (int)(wlInbox(x) * dim[0]); }
+    int cellY(double y) const { return (int)(wlInbox(y) * dim[1]); }
+    bool valid(int q) const { return q >= 0 && q < dim[0] * dim[1]; }
+    // Mesh::addPart: 1 when every square was occupied already (no hole shrank)
+    int add(double x, double y) {
+        int sq[9], onhole = 1;
+        squares(cellX(x), cellY(y), sq);
+        for (int i = 0; i < 9; ++i) {
+            if (!valid(sq[i])) continue;        // the reference reports these and writes anyway
+            if (data[sq[i]] >= 0) onhole = 0;
+            data[sq[i]]--;
+        }
+        return onhole;
+    }
+    // Mesh::removePart: 0 at the first square it frees (the rest are left as they are)
+    int remove(double x, double y) {
+        int sq[9];
+        squares(cellX(x), cellY(y), sq);
+        for (int i = 0; i < 9; ++i) {
+            if (!valid(sq[i])) continue;
+            data[sq[i]]++;
+            if (data[sq[i]] == 0) return 0;
+        }
+        return 1;
+    }
+    void fill(const or_system* s, int wlmtype) {       // Mesh::meshFill
+        std::fill(data.begin(), data.end(), 0);
+        for (int i = 0; i < s->n; ++i)
+            if (s->p[i].type == wlmtype) add(s->p[i].pos.x, s->p[i].pos.y);
+    }
+    int findHoles() {                                   // Mesh::findHoles
+        const int L = dim[0] * dim[1];
+        int n = 0, maxsize = 0;
+        for (int i = 0; i < L; ++i) {
+            tmp[i] = 0;
+            if (data[i] > 0) data[i] = 0;
+        }
+        for (int i = 0; i < L;) {
+            if (data[i] != 0) { ++i; continue; }
+            ++n;
+            data[i] = n;
+            int size = 1, li = 0;
+            tmp[0] = i;
+            while (li < size) {
+                const int j = tmp[li], x = j % dim[0], y = j / dim[0];
+                const int nb[4] = {square(x - 1 < 0 ? dim[0] - 1 : x - 1, y), square(x + 1 == dim[0] ? 0 : x + 1, y),
+                                   square(x, y - 1 < 0 ? dim[1] - 1 : y - 1), square(x, y + 1 == dim[1] ? 0 : y + 1)};
+                for (int k = 0; k < 4; ++k)
+                    if (data[nb[k]] == 0) {
+                        data[nb[k]] = n;
+                        tmp[size++] = nb[k];
+                    }
+                ++li;
+            }
+            if (size > maxsize) maxsize = size;
+        }
+        return maxsize;
+    }
+    // Mesh::meshInit with the box now: -1 when the mesh has no square
+    int init(const or_system* s, int wlmtype) {
+        if (wlmtype < 0 || wlmtype >= OR_MAXT) return -1;
+        const double ms = s->params[wlmtype * OR_MAXT + wlmtype].sigma / 3.0;
+        if (!(ms > 0.0)) return -1;
+        dim[0] = (int)(s->box[0] / ms);
+        dim[1] = (int)(s->box[1] / ms);
+        if (dim[0] < 1 || dim[1] < 1) return -1;
+        data.assign((size_t)dim[0] * dim[1], 0);
+        tmp.assign((size_t)dim[0] * dim[1] + 1, 0);
+        fill(s, wlmtype);
+        return findHoles();
+    }
+};
+
+long wlMeshBin(int size, double minorder, double dorder) { return (long)(((double)size - minorder) / dorder); }
+
+}  // namespace
+
 // WangLandau::init (scOOP/mc/wanglandau.cpp:49-137): the starting bin of each order
 // parameter.  Order 1: Conf::massCenter (scOOP/structures/Conf.cpp:78-95) over the
 // anInt-wrapped positions weighted by the Ia_param volumes, then zOrder
-// (wanglandau.h:551-554); 3: zOrient (:321-324, floor); 4: twoPartDist (:395-398); 8 / 9:
-// the box lengths (:375-382).  Returns -1 for an order parameter outside {1, 3, 4, 8, 9}.
-extern "C" int or_wl_orders(const or_system* s, const int wlm[2], const double minorder[2], const double dorder[2],
-                            long out[2], double syscm[3], double* sysvolume) {
+// (wanglandau.h:551-554); 2: the mesh hole (above); 3: zOrient (:321-324, floor); 4:
+// twoPartDist (:395-398); 7: the contacts (above); 8 / 9: the box lengths (:375-382).
+// Returns -1 for another order parameter (5 and 6, the pore orders, end the reference's
+// own init with a null-pointer write: radiusholeAll, wanglandau.cpp:306-318, never
+// allocates its histogram) or a mesh without squares.
+extern "C" int or_wl_orders(const or_system* s, const int wlm[2], int wlmtype, const double minorder[2],
+                            const double dorder[2], long out[2], double syscm[3], double* sysvolume) {
     double sv = 0.0;
     for (int i = 0; i < s->n; ++i) sv += s->params[s->p[i].type * OR_MAXT + s->p[i].type].volume;
     or_vec cm = V(0, 0, 0);
@@ -1435,6 +1562,14 @@ extern "C" int or_wl_orders(const or_system* s, const int wlm[2], const double m
             out[k] = (long)std::ceil((std::sqrt(r.x * r.x + r.y * r.y) - minorder[k]) / dorder[k]);
             break;
         }
+        case 2: {
+            WlMesh m;
+            const int size = m.init(s, wlmtype);
+            if (size < 0) return -1;
+            out[k] = wlMeshBin(size, minorder[k], dorder[k]);
+            break;
+        }
+        case 7: out[k] = wlContactBin(wlContactsAll(s, wlmtype), minorder[k], dorder[k]); break;
         case 8: out[k] = (long)std::ceil((s->box[0] - minorder[k]) / dorder[k]); break;
         case 9: out[k] = (long)std::ceil((s->box[1] - minorder[k]) / dorder[k]); break;
         default: return -1;
@@ -1448,7 +1583,10 @@ extern "C" int or_wl_orders(const or_system* s, const int wlm[2], const double m
 // MoveCreator::partDisplace / partRotate with WangLandau::run / runRot (movecreator.cpp:
 // 947-1028, wanglandau.h:124-217): the bins after the move (order 1: the system centre moves
 // by volume * displacement / sysvolume, zDir :293-299; 3: zOrient of particle 0; 4:
-// twoPartDist), a bin outside the histogram rejects the move, else
+// twoPartDist; 7: the contact count, recounted when particle 0 moves, else changed by the
+// moved particle's old and new contact (contParticlesMoveMolecule, :516-532); 2: the mesh,
+// updated by Mesh::addPart / removePart and refilled when a hole may have changed
+// (meshOrderMoveMolecule), restored on rejection), a bin outside the histogram rejects the move, else
 // moveTry(energy + w[new] - w[cur], enermove); then accept / reject (:262-290): the current
 // bin's weight drops by alpha and its count grows by one.  Every 1000 sweeps
 // WangLandau::update (:66-120, integer max / min) halves alpha when the histogram is flat;
@@ -1469,6 +1607,15 @@ extern "C" int or_wl_run(or_system* s, const or_mc_opts* o, or_wl* wl, or_mc_sta
         cm.x += (r.x - anint(r.x)) * v; cm.y += (r.y - anint(r.y)) * v; cm.z += (r.z - anint(r.z)) * v;
     }
     cm.x /= sv; cm.y /= sv; cm.z /= sv;
+    bool uses[10] = {};
+    for (int k = 0; k < dim; ++k) {
+        if (wl->wlm[k] < 1 || wl->wlm[k] > 9 || wl->wlm[k] == 5 || wl->wlm[k] == 6) return -3;
+        uses[wl->wlm[k]] = true;
+    }
+    const int wlmtype = wl->wlmtype;
+    long contacts = uses[7] ? wlContactsAll(s, wlmtype) : 0;
+    WlMesh mesh, origmesh;
+    if (uses[2] && mesh.init(s, wlmtype) < 0) return -3;
     auto idx = [&](const long* b) { return b[0] + b[1] * (long)wl->len[0]; };
     auto inRange = [&](const long* b) {
         for (int k = 0; k < dim; ++k)
@@ -1522,8 +1669,15 @@ extern "C" int or_wl_run(or_system* s, const or_mc_opts* o, or_wl* wl, or_mc_sta
         }
         }
         long nw[2] = {wl->cur[0], wl->cur[1]};
+        long cntNew = contacts;
+        if (uses[2]) origmesh = mesh;
         for (int k = 0; k < dim; ++k) {
             switch (wl->wlm[k]) {
+            case 2: nw[k] = wlMeshBin(mesh.init(s, wlmtype), wl->minorder[k], wl->dorder[k]); break;
+            case 7:
+                cntNew = wlContactsAll(s, wlmtype);
+                nw[k] = wlContactBin(cntNew, wl->minorder[k], wl->dorder[k]);
+                break;
             case 1:
                 if (o->ptype != 2)
                     nw[k] = (long)std::ceil(((s->p[0].pos.z - cm.z) * s->box[2] - wl->minorder[k]) / wl->dorder[k]);
@@ -1546,9 +1700,11 @@ extern "C" int or_wl_run(or_system* s, const or_mc_opts* o, or_wl* wl, or_mc_sta
         }
         if (rej) {
             s->box[0] = b0[0]; s->box[1] = b0[1]; s->box[2] = b0[2];
+            if (uses[2]) mesh = origmesh;
             ++st->rej_vol;
         } else {
             wl->cur[0] = nw[0]; wl->cur[1] = nw[1];
+            contacts = cntNew;
             ++st->acc_vol;
         }
         visit();
@@ -1570,6 +1726,8 @@ extern "C" int or_wl_run(or_system* s, const or_mc_opts* o, or_wl* wl, or_mc_sta
             double eold = or_one_to_all(s, target);
             bool displace = (rng() < 0.5) || d.geotype[0] >= SP;
             long nw[2] = {wl->cur[0], wl->cur[1]};
+            long cntNew = contacts;
+            if (uses[2]) origmesh = mesh;
             if (displace) {
                 or_vec dr = randomUnitSphere(rng);
                 dr.x *= o->transmx / s->box[0]; dr.y *= o->transmx / s->box[1]; dr.z *= o->transmx / s->box[2];
@@ -1581,6 +1739,24 @@ extern "C" int or_wl_run(or_system* s, const or_mc_opts* o, or_wl* wl, or_mc_sta
                     } else if (wl->wlm[k] == 4) {
                         or_vec r = image(s->p[0].pos, s->p[1].pos, s->box);
                         nw[k] = (long)std::ceil((std::sqrt(r.x * r.x + r.y * r.y) - wl->minorder[k]) / wl->dorder[k]);
+                    } else if (wl->wlm[k] == 7) {
+                        if (target == 0) {
+                            cntNew = wlContactsAll(s, wlmtype);
+                        } else if (orig.type == wlmtype) {
+                            cntNew += wlInContact(s, s->p[target].pos, s->p[0].pos) ? 1 : 0;
+                            cntNew -= wlInContact(s, orig.pos, s->p[0].pos) ? 1 : 0;
+                        }
+                        nw[k] = wlContactBin(cntNew, wl->minorder[k], wl->dorder[k]);
+                    } else if (wl->wlm[k] == 2 && orig.type == wlmtype) {
+                        const or_vec& np = s->p[target].pos;
+                        if (mesh.cellX(np.x) != mesh.cellX(orig.pos.x) || mesh.cellY(np.y) != mesh.cellY(orig.pos.y)) {
+                            int change = mesh.add(np.x, np.y);
+                            if (change) change = mesh.remove(orig.pos.x, orig.pos.y);
+                            if (!change) {
+                                mesh.fill(s, wlmtype);
+                                nw[k] = wlMeshBin(mesh.findHoles(), wl->minorder[k], wl->dorder[k]);
+                            }
+                        }
                     }
                 }
             } else {
@@ -1603,9 +1779,11 @@ extern "C" int or_wl_run(or_system* s, const or_mc_opts* o, or_wl* wl, or_mc_sta
             if (rej) {
                 s->p[target] = orig;
                 cm = cmOld;
+                if (uses[2]) mesh = origmesh;
                 if (displace) ++st->rej_trans; else ++st->rej_rot;
             } else {
                 wl->cur[0] = nw[0]; wl->cur[1] = nw[1];
+                contacts = cntNew;
                 st->energy += enew - eold;
                 if (displace) ++st->acc_trans; else ++st->acc_rot;
             }

@@ -163,19 +163,21 @@ typedef struct {
     long cur[2];           /* current bins (set by the caller, e.g. from or_wl_orders) */
     long updates;
     int converged;
-    int pad_;
+    int wlmtype;           /* the particle type of orders 2 and 7 (options wlmtype) */
 } or_wl;
 
 /* The reference's sequential loop with a Wang-Landau bias (single-particle moves; volume
- * moves of ptype 0, 1, 2, 5 with probability shave / N per step; order parameters 1, 3, 4,
- * 8, 9), WangLandau::run / runRot / runPress / accept / reject / update.  Returns -2 for
- * volume moves of another ptype (3, 4), -1 for an empty system, else 0. */
+ * moves of ptype 0, 1, 2, 5 with probability shave / N per step; order parameters 1, 2, 3,
+ * 4, 7, 8, 9), WangLandau::run / runRot / runPress / accept / reject / update.  Returns -2
+ * for volume moves of another ptype (3, 4), -3 for orders 5 / 6 or a mesh without squares,
+ * -1 for an empty system, else 0. */
 int or_wl_run(or_system* s, const or_mc_opts* o, or_wl* wl, or_mc_stats* st);
 
 /* Wang-Landau starting bins (WangLandau::init, scOOP/mc/wanglandau.cpp:49-137) of order
- * parameters 1, 3, 4, 8, 9, with the system centre and sysvolume they use. */
-int or_wl_orders(const or_system* s, const int wlm[2], const double minorder[2], const double dorder[2], long out[2],
-                 double syscm[3], double* sysvolume);
+ * parameters 1, 2, 3, 4, 7, 8, 9 (wlmtype: the particle type of the mesh and contact orders),
+ * with the system centre and sysvolume they use. */
+int or_wl_orders(const or_system* s, const int wlm[2], int wlmtype, const double minorder[2], const double dorder[2],
+                 long out[2], double syscm[3], double* sysvolume);
 
 #ifdef __cplusplus
 }

@@ -209,6 +209,12 @@ __global__ void kBeginSweep(const SweepArgs* __restrict__ A, int volumeDue) {
         if (j > k) j = k;
         int tmp = c.perm[k]; c.perm[k] = c.perm[j]; c.perm[j] = tmp;
     }
+    if (a.wl && a.wl->useContacts) {
+        // Wang-Landau order 7: the cells whose particles can come within the contact distance
+        // of particle 0 wherever it is in its cell (no move leaves its cell): offsets below
+        // sqrt(WL_CONTACTS) / width + 1 along each axis, for the box of this sweep
+        for (int d = 0; d < 3; ++d) a.wl->reach[d] = (int)(sqrt(kWlContacts) * a.g.nc[d] / a.s.box[d]) + 1;
+    }
     c.volValid = 0;
     if (volumeDue) {
         // MoveCreator::pressureMove (movecreator.cpp:330-546): the box proposal and the
@@ -901,7 +907,49 @@ __device__ void acceptThresholds(const SweepArgs& a, Proposal& P, int cell, int 
 // parameters) are not moved in their colour phase: kWlCells moves them, one after the other,
 // after every other cell of the sweep, so that each of their moves sees the current bins and
 // weights, exactly as the reference's sequential loop does for some order of the sweep's moves.
-__device__ __forceinline__ bool isWlCell(const WlDev& w, int cell) { return cell == w.cell[0] || cell == w.cell[1]; }
+// With order 7 the block of cells within w.reach of particle 0's cell (every cell along an
+// axis the block spans whole) joins them: only their particles can change the contact count.
+__device__ __forceinline__ bool wlNear(int c, int c0, int nc, int r) {
+    if (nc <= 2 * r) return true;
+    int d = c > c0 ? c - c0 : c0 - c;
+    if (nc - d < d) d = nc - d;
+    return d <= r;
+}
+__device__ __forceinline__ bool wlInBlock(const WlDev& w, const Grid& g, int cell) {
+    const int c0 = w.cell[0];
+    if (!w.useContacts || c0 < 0 || c0 >= g.ncells) return false;
+    return wlNear(cell % g.nc[0], c0 % g.nc[0], g.nc[0], w.reach[0]) &&
+           wlNear((cell / g.nc[0]) % g.nc[1], (c0 / g.nc[0]) % g.nc[1], g.nc[1], w.reach[1]) &&
+           wlNear(cell / (g.nc[0] * g.nc[1]), c0 / (g.nc[0] * g.nc[1]), g.nc[2], w.reach[2]);
+}
+__device__ __forceinline__ bool isWlCell(const WlDev& w, const Grid& g, int cell) {
+    return cell == w.cell[0] || cell == w.cell[1] || wlInBlock(w, g, cell);
+}
+// The cells kWlCells moves, in its order: slots 0 .. wlCellSlots - 1, each a cell or -1 (a
+// slot with none, or a cell an earlier slot holds).  Without order 7: particle 0's cell, then
+// particle 1's; with it: the block around particle 0's cell, then particle 1's cell when the
+// block misses it.
+__device__ __forceinline__ int wlCellSlots(const WlDev& w, const Grid& g) {
+    if (!w.useContacts) return 2;
+    return axisCount(g.nc[0], w.reach[0]) * axisCount(g.nc[1], w.reach[1]) * axisCount(g.nc[2], w.reach[2]) + 1;
+}
+__device__ int wlCellAt(const WlDev& w, const Grid& g, int k) {
+    if (!w.useContacts || k == wlCellSlots(w, g) - 1) {
+        const int q = w.useContacts ? 1 : k;
+        const int cell = w.cell[q];
+        if (cell < 0 || cell >= g.ncells || (q == 1 && cell == w.cell[0])) return -1;
+        if (w.useContacts && wlInBlock(w, g, cell)) return -1;
+        return cell;
+    }
+    const int c0 = w.cell[0];
+    if (c0 < 0 || c0 >= g.ncells) return -1;
+    const int nx = axisCount(g.nc[0], w.reach[0]), ny = axisCount(g.nc[1], w.reach[1]);
+    const int qx = k % nx, qy = (k / nx) % ny, qz = k / (nx * ny);
+    const int x = axisCell(c0 % g.nc[0], qx, g.nc[0], w.reach[0]);
+    const int y = axisCell((c0 / g.nc[0]) % g.nc[1], qy, g.nc[1], w.reach[1]);
+    const int z = axisCell(c0 / (g.nc[0] * g.nc[1]), qz, g.nc[2], w.reach[2]);
+    return (z * g.nc[1] + y) * g.nc[0] + x;
+}
 
 // One visit of the current bin (WangLandau::accept / reject, wanglandau.h:262-290): the
 // histogram counts it and the weight drops by alpha (implicit in wlWeight).
@@ -913,8 +961,9 @@ __device__ __forceinline__ void wlVisit(WlDev& w) {
 // wanglandau.h:124-217) and the system centre after it (zDir, :293-299); false when a bin
 // leaves the histogram (the move is rejected).
 __device__ bool wlProposal(const SweepArgs& a, const WlDev& w, const Proposal& P, const double3& box, long long nw[2],
-                           double cmNew[3]) {
+                           double cmNew[3], long long& contactsNew) {
     const int t = P.target;
+    contactsNew = w.contacts;
     for (int d = 0; d < 3; ++d) cmNew[d] = w.syscm[d];
     if (P.displace && w.needCM) {
         const double vol = a.volW[P.type];
@@ -940,6 +989,26 @@ __device__ bool wlProposal(const SweepArgs& a, const WlDev& w, const Proposal& P
                 double* moved = t == 0 ? p0 : p1;
                 for (int d = 0; d < 3; ++d) moved[d] = P.npos[d];
                 nw[k] = wlDistOrder(w, k, p0, p1, bx);
+            }
+            break;
+        case 7:             // contacts with particle 0 (contParticlesMoveMolecule, wanglandau.h:516-532):
+                            // recounted when particle 0 moves, else the moved particle's old and
+                            // new contact (only displacements of the counted type change it)
+            if (P.displace) {
+                if (t == 0) {
+                    long long n = 0;
+                    for (int i = 1; i < a.s.n; ++i) {
+                        const double4_32a q = a.s.pos[i];
+                        const double pi[3] = {q.x, q.y, q.z};
+                        if ((int)q.w == w.contactType && wlInContact(pi, P.npos, bx)) ++n;
+                    }
+                    contactsNew = n;
+                } else if (P.type == w.contactType) {
+                    const double4_32a q0 = a.s.pos[0];
+                    const double p0[3] = {q0.x, q0.y, q0.z};
+                    contactsNew += (wlInContact(P.npos, p0, bx) ? 1 : 0) - (wlInContact(P.opos, p0, bx) ? 1 : 0);
+                }
+                nw[k] = wlContactOrder(w, k, contactsNew);
             }
             break;
         default:            // 8, 9: box lengths, changed by volume moves only
@@ -1424,15 +1493,16 @@ __device__ __forceinline__ void moveCell(const SweepArgs& a, int cx, int cy, int
                 // bin outside the histogram rejects it, else the weight difference wlener
                 // enters moveTry(energy + wlener, enermove) (movecreator.cpp:966-987, 1009-1023)
                 WlDev& w = *a.wl;
-                long long nw[2];
+                long long nw[2], contactsNew;
                 double cmNew[3];
-                const bool inRange = wlProposal(a, w, P0, box, nw, cmNew);
+                const bool inRange = wlProposal(a, w, P0, box, nw, cmNew, contactsNew);
                 double eOld = e0;
                 if (inRange) eOld += wlWeight(*w.tab, wlIndex(w, nw)) - wlWeight(*w.tab, wlIndex(w, w.cur));
                 accept = inRange && ((e1 <= eOld) || ((e1 - eOld) < P0.thrMet));
                 if (accept) {
                     w.cur[0] = nw[0]; w.cur[1] = nw[1];
                     for (int d = 0; d < 3; ++d) w.syscm[d] = cmNew[d];
+                    w.contacts = contactsNew;
                 }
                 wlVisit(w);
             } else {
@@ -1543,7 +1613,7 @@ __device__ __forceinline__ void colourBody(const SweepArgs* __restrict__ A, int 
     if ((int)blockIdx.x >= g.nactive || phase >= g.ncolours) return;
     int cx, cy, cz;
     decodeActive(g, a.ctl->perm[phase], blockIdx.x, cx, cy, cz);
-    if (a.wl && isWlCell(*a.wl, (cz * g.nc[1] + cy) * g.nc[0] + cx)) return;     // moved by kWlCells
+    if (a.wl && isWlCell(*a.wl, g, (cz * g.nc[1] + cy) * g.nc[0] + cx)) return;     // moved by kWlCells
     moveCell<false>(a, cx, cy, cz, NoWait());
 }
 
@@ -1646,7 +1716,7 @@ __device__ __forceinline__ void flowBody(const SweepArgs* __restrict__ A) {
         const int cell = (cz * g.nc[1] + cy) * g.nc[0] + cx;
         // no moves (or, with a Wang-Landau bias, the cells kWlCells moves after the sweep's
         // other cells): nothing to wait for, nothing to publish first
-        if (counts[cell] == 0 || (!CHAIN && a.wl && isWlCell(*a.wl, cell))) {
+        if (counts[cell] == 0 || (!CHAIN && a.wl && isWlCell(*a.wl, g, cell))) {
             if (tid == 0) storeReleaseGpu(&a.cellDone[cell], stamp);
             continue;
         }
@@ -2025,11 +2095,12 @@ __global__ void __launch_bounds__(kMoveThreads, 1) kWlCells(const SweepArgs* __r
     if (!a.wl) return;
     WlDev& w = *a.wl;
     const Grid& g = a.g;
+    const int slots = wlCellSlots(w, g);
     if (threadIdx.x == 0) {
         long long others = a.s.n;
-        for (int q = 0; q < 2; ++q) {
-            const int cell = w.cell[q];
-            if (cell >= 0 && !(q == 1 && cell == w.cell[0])) others -= a.cellCount[cell];
+        for (int k = 0; k < slots; ++k) {
+            const int cell = wlCellAt(w, g, k);
+            if (cell >= 0) others -= a.cellCount[cell];
         }
         atomicAdd((unsigned long long*)&w.tab->hist[wlIndex(w, w.cur)], (unsigned long long)others);
     }
@@ -2043,10 +2114,9 @@ __global__ void __launch_bounds__(kMoveThreads, 1) kWlCells(const SweepArgs* __r
         }
     }
     __syncthreads();
-    for (int q = 0; q < 2; ++q) {
-        const int cell = w.cell[q];
-        const bool run = cell >= 0 && cell < g.ncells && !(q == 1 && cell == w.cell[0]);
-        if (run) {
+    for (int k = 0; k < slots; ++k) {
+        const int cell = wlCellAt(w, g, k);
+        if (cell >= 0 && a.cellCount[cell] > 0) {      // an empty cell makes no move
             const int cx = cell % g.nc[0], cy = (cell / g.nc[0]) % g.nc[1], cz = cell / (g.nc[0] * g.nc[1]);
             moveCell<true>(a, cx, cy, cz, NoWait());
         }
@@ -2763,6 +2833,26 @@ __device__ double sumPartials(const double* p, int n) {
 }
 
 // MoveCreator::pressureMove, ptype 1 (movecreator.cpp:390-421), decided on the device.
+// Wang-Landau order 7 in a trial box (runPress calls contParticlesAll, wanglandau.h:603-615):
+// the particles 1..N-1 of the counted type within the contact distance of particle 0,
+// counted by the whole block (integer sums: the order of the additions does not matter).
+__device__ long long wlContactsBlock(const SweepArgs& a, const WlDev& w, const double* box) {
+    __shared__ unsigned long long tot;
+    if (threadIdx.x == 0) tot = 0;
+    __syncthreads();
+    const double4_32a q0 = a.s.pos[0];
+    const double p0[3] = {q0.x, q0.y, q0.z};
+    unsigned long long n = 0;
+    for (int i = 1 + (int)threadIdx.x; i < a.s.n; i += blockDim.x) {
+        const double4_32a q = a.s.pos[i];
+        const double pi[3] = {q.x, q.y, q.z};
+        if ((int)q.w == w.contactType && wlInContact(pi, p0, box)) ++n;
+    }
+    if (n) atomicAdd(&tot, n);
+    __syncthreads();
+    return (long long)tot;
+}
+
 __global__ void kVolumeAccept(const SweepArgs* __restrict__ A) {
     const SweepArgs& a = A[blockIdx.y];
     if (blockIdx.x != 0) return;
@@ -2777,6 +2867,7 @@ __global__ void kVolumeAccept(const SweepArgs* __restrict__ A) {
     }
     double eNew = sumPartials(a.partial, a.g.ncells);
     if (a.wl && a.wl->needCM) wlCentre(a, *a.wl);
+    const long long contactsTrial = a.wl && a.wl->useContacts ? wlContactsBlock(a, *a.wl, c.trialBox) : 0;
     if (threadIdx.x != 0) return;
     double enermove = c.pvTerm;
     enermove += eNew;
@@ -2787,8 +2878,8 @@ __global__ void kVolumeAccept(const SweepArgs* __restrict__ A) {
     bool inRange = true;
     if (a.wl) {
         // WangLandau::runPress (wanglandau.h:168-196) with the trial box: order 1 (not for
-        // ptype 2, whose z stays), 4 and the box lengths 8 / 9 change; wlener enters
-        // moveTry(energy + wlener, enermove)
+        // ptype 2, whose z stays), 4, the contacts 7 and the box lengths 8 / 9 change; wlener
+        // enters moveTry(energy + wlener, enermove)
         WlDev& w = *a.wl;
         const double* tb = c.trialBox;
         nw[0] = w.cur[0]; nw[1] = w.cur[1];
@@ -2803,6 +2894,7 @@ __global__ void kVolumeAccept(const SweepArgs* __restrict__ A) {
                 nw[k] = wlDistOrder(w, k, p0, p1, tb);
                 break;
             }
+            case 7: nw[k] = wlContactOrder(w, k, contactsTrial); break;
             case 8: nw[k] = wlBoxOrder(w, k, tb[0]); break;
             case 9: nw[k] = wlBoxOrder(w, k, tb[1]); break;
             default: break;
@@ -2816,7 +2908,10 @@ __global__ void kVolumeAccept(const SweepArgs* __restrict__ A) {
         for (int d = 0; d < 3; ++d) a.s.box[d] = c.trialBox[d];
         c.energy = eNew;
         atomicAdd(&a.counters[C_ACC_V], 1ull);
-        if (a.wl) { a.wl->cur[0] = nw[0]; a.wl->cur[1] = nw[1]; }
+        if (a.wl) {
+            a.wl->cur[0] = nw[0]; a.wl->cur[1] = nw[1];
+            if (a.wl->useContacts) a.wl->contacts = contactsTrial;
+        }
     } else {
         atomicAdd(&a.counters[C_REJ_V], 1ull);
     }

@@ -47,7 +47,9 @@ struct WlHost {
 
 // Bins of the current configuration (WangLandau::init): order 1 needs the system centre
 // (Conf::massCenter, scOOP/structures/Conf.cpp:78-95, over anInt-wrapped positions,
-// weighted by the Ia_param volumes; sysvolume as Inicializer sums it, inicializer.cpp:32-34).
+// weighted by the Ia_param volumes; sysvolume as Inicializer sums it, inicializer.cpp:32-34);
+// order 7 counts the particles 1..N-1 of type wlmtype in contact with particle 0
+// (contParticlesAll, wanglandau.h:603-615).
 static int wlOrders(const Context* c, WlDev& w, std::string& err) {
     const std::vector<Particle>& p = c->conf.p;
     const int n = (int)p.size();
@@ -75,6 +77,17 @@ static int wlOrders(const Context* c, WlDev& w, std::string& err) {
         case 4: {
             const double p0[3] = {p[0].pos.x, p[0].pos.y, p[0].pos.z}, p1[3] = {p[1].pos.x, p[1].pos.y, p[1].pos.z};
             w.cur[q] = wlDistOrder(w, q, p0, p1, box);
+            break;
+        }
+        case 7: {
+            long long cnt = 0;
+            const double p0[3] = {p[0].pos.x, p[0].pos.y, p[0].pos.z};
+            for (int i = 1; i < n; ++i) {
+                const double pi[3] = {p[i].pos.x, p[i].pos.y, p[i].pos.z};
+                if (p[i].type == c->opts.wlmtype && wlInContact(pi, p0, box)) ++cnt;
+            }
+            w.contacts = cnt;
+            w.cur[q] = wlContactOrder(w, q, cnt);
             break;
         }
         case 8: w.cur[q] = wlBoxOrder(w, q, box[0]); break;
@@ -176,6 +189,14 @@ int wlCheckRun(const Context* c, const sc_run_params& p) {
             if (i >= 0 && c->molInfo[i].z > 1)
                 return fail(SC_ERR_UNSUPPORTED, "Wang-Landau: a particle of the order parameters belongs to a chain "
                                                 "and chain moves are on");
+        }
+        // order 7: chain moves of chains holding counted particles would change the count
+        // outside the serialised cells
+        if (c->wl->h.useContacts) {
+            for (size_t i = 0; i < c->conf.p.size(); ++i)
+                if (c->conf.p[i].type == c->opts.wlmtype && c->molInfo[i].z > 1)
+                    return fail(SC_ERR_UNSUPPORTED, "Wang-Landau order 7: particles of type wlmtype belong to chains "
+                                                    "and chain moves are on");
         }
     }
     return SC_OK;
@@ -285,9 +306,9 @@ static int wlLoad(Context* c, const std::string& text) {
     if (m[0] <= 0) return fail(SC_ERR_STATE, "options wlm is 0: no Wang-Landau order parameter to load weights for");
     for (int q = 0; q < 2; ++q) {
         if (m[q] == 0) continue;
-        if (m[q] != 1 && m[q] != 3 && m[q] != 4 && m[q] != 8 && m[q] != 9)
+        if (m[q] != 1 && m[q] != 3 && m[q] != 4 && m[q] != 7 && m[q] != 8 && m[q] != 9)
             return fail(SC_ERR_UNSUPPORTED, "Wang-Landau order parameter " + std::to_string(m[q]) +
-                                                " (supported: 1, 3, 4, 8, 9; the mesh, pore and contact orders 2, 5, 6, 7 "
+                                                " (supported: 1, 3, 4, 7, 8, 9; the mesh-hole and pore orders 2, 5, 6 "
                                                 "are not on the GPU path)");
     }
     if ((m[0] == 4 || m[1] == 4) && c->conf.p.size() < 2)
@@ -311,9 +332,14 @@ static int wlLoad(Context* c, const std::string& text) {
     bool uses[10] = {};
     for (int q = 0; q < w.dim; ++q) uses[m[q]] = true;
     w.needCM = uses[1] ? 1 : 0;
-    w.part[0] = (uses[1] || uses[3] || uses[4]) ? 0 : -1;
+    w.part[0] = (uses[1] || uses[3] || uses[4] || uses[7]) ? 0 : -1;
     w.part[1] = uses[4] ? 1 : -1;
     w.cell[0] = w.cell[1] = -1;
+    w.useContacts = uses[7] ? 1 : 0;
+    const int wt = c->opts.wlmtype;
+    w.contactType = (wt >= 0 && wt < MAXT) ? c->compactOf[wt] : -1;
+    for (int d = 0; d < 3; ++d) w.reach[d] = 0;
+    w.contacts = 0;
     w.owner = 1;
     if ((rc = wlOrders(c, w, err))) { delete W; return fail(rc, err); }
     destroyWl(c);

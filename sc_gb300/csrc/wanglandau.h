@@ -4,10 +4,13 @@
 // every move by weights of one or two order parameters and lowers the weight of the
 // visited bin by alpha after every move (accept / reject, wanglandau.h:262-290); alpha is
 // halved when the histogram is flat (update, :66-120).  This build supports the order
-// parameters whose value only the moves of particles 0 and 1 and the box change:
+// parameters whose value only the moves of particles 0 and 1, of the particles near
+// particle 0, and the box change:
 //   1  z of particle 0 relative to the system's volume-weighted centre   (zOrder,  :551-554)
 //   3  z component of particle 0's axis                                  (zOrient, :321-324)
 //   4  xy distance of particles 0 and 1                                  (twoPartDist, :395-398)
+//   7  particles of type wlmtype within sqrt(WL_CONTACTS) of particle 0  (contParticlesAll,
+//      :603-676): only moves of particles within that distance of particle 0's cell change it
 //   8  box length in x, 9 box length in y                                (boxSize_x/_y, :376-382)
 //
 // Weights are kept as w[i] = base[i] - alpha * (hist[i] - hist0[i]): base and hist0 are
@@ -27,6 +30,7 @@ constexpr double kWlGerr = 0.0001;        // WL_GERR     scOOP/structures/macros
 constexpr double kWlAlphaTol = 1.0e-8;    // WL_ALPHATOL macros.h:104
 constexpr long kWlMinHist = 1000;         // WL_MINHIST  macros.h:105
 constexpr int kWlUpdateEvery = 1000;      // sweeps between flatness checks, updater.cpp:255
+constexpr double kWlContacts = 36.0;      // WL_CONTACTS macros.h:107 (squared contact distance)
 
 // Weights and histogram, shared by the walkers of one Wang-Landau run.
 struct WlTable {
@@ -55,6 +59,15 @@ struct WlDev {
     long long cur[2];        // current bins
     unsigned long long chainSeen;   // chain-move attempts already counted
     WlTable* tab;            // weights and histogram (device)
+    // order 7: the compact type counted (-1: none present), the count now, and the reach in
+    // cells (per axis, set at every sweep's start) of the block of cells around particle 0's
+    // cell whose particles can come within the contact distance of particle 0 (0: order 7
+    // not in use)
+    int contactType;
+    int useContacts;
+    int reach[3];
+    int pad7_;
+    long long contacts;
 };
 
 __host__ __device__ inline double wlWeight(const WlTable& t, long long i) {
@@ -86,6 +99,19 @@ __host__ __device__ inline long long wlDistOrder(const WlDev& w, int k, const do
 }
 __host__ __device__ inline long long wlBoxOrder(const WlDev& w, int k, double edge) {
     return (long long)ceil((edge - w.minorder[k]) / w.dorder[k]);
+}
+// WangLandau::particlesInContact (wanglandau.h:660-676): minimum image of box fractions
+// (anInt, the reference's round-half-even: rint), scaled by the box
+__host__ __device__ inline bool wlInContact(const double* a, const double* p0, const double* box) {
+    double x = a[0] - p0[0], y = a[1] - p0[1], z = a[2] - p0[2];
+    x = box[0] * (x - rint(x));
+    y = box[1] * (y - rint(y));
+    z = box[2] * (z - rint(z));
+    return x * x + y * y + z * z < kWlContacts;
+}
+// contParticlesOrder (wanglandau.h:652-654)
+__host__ __device__ inline long long wlContactOrder(const WlDev& w, int k, long long count) {
+    return (long long)ceil(((double)count - w.minorder[k]) / w.dorder[k]);
 }
 
 }  // namespace scg

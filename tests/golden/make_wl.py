@@ -9,8 +9,9 @@ a weights file ``wl.dat``:
   starting bins, the system centre and sysvolume, and the text the reference writes back
   for the weights it read;
 * ``oracle/_ref/sc_ref`` (the reference's own ``main``), several seeds: adaptive runs of
-  the two-particle distance case and fixed-weight runs of the orientation case, the weights
-  and histogram they end with (``wl-new.dat``), for the comparisons.
+  the two-particle distance case and fixed-weight runs of the orientation, system-centre,
+  contact-count and mesh-hole cases, the weights and histogram they end with
+  (``wl-new.dat``), for the comparisons.
 
 Run here (needs the reference tree):  python tests/golden/make_wl.py
 """
@@ -156,6 +157,37 @@ def cases():
     out.append(dict(name="o1_fixed", wlm=(1, 0), options=dict(wlm="1 0", transmx=0.2, rotmx=0.0, nsweeps=20000,
                                                                 seed=18, shave=0, ptype=0),
                     top=top, config=cfg, wl=wl_text(0.0, zs, [-0.5 * z[0] * z[0] for z in zs])))
+    # (9) order 7, the number of bath spheres (type 2, wlmtype) within 6 sigma of particle 0,
+    # under fixed weights linear in the count (alpha 0); NVT, then NPT (isotropic volume moves
+    # recount the contacts in the trial box)
+    box = np.array([12.0, 12.0, 12.0])
+    p0 = [np.array([0.5, 0.5, 0.5])]
+    pos = p0 + bath(rng, box, 100, p0)
+    dirs = rand_unit(rng, len(pos))
+    top = top_text([spn(1, "A"), ("S", 2, "SPA", [1.0, 1.0, 1.1225, 0.3775])], [("A", [1], []), ("S", [2], [])],
+                   [("A", 1), ("S", 100)])
+    cfg = config_text(box, np.array(pos) * box, dirs, rand_perp(rng, dirs))
+    counts = grid1(0.0, 1.0, 101)
+    wl7 = wl_text(0.0, counts, [0.08 * c[0] for c in counts])
+    out.append(dict(name="o7_contact", wlm=(7, 0), options=dict(wlm="7 0", wlmtype=2, transmx=0.5, rotmx=0.0,
+                                                                  nsweeps=4000, seed=19, shave=0, ptype=0),
+                    top=top, config=cfg, wl=wl7))
+    out.append(dict(name="o7_npt", wlm=(7, 0), options=dict(wlm="7 0", wlmtype=2, transmx=0.5, rotmx=0.0,
+                                                              nsweeps=4000, seed=20, shave=1, ptype=1, press=0.06,
+                                                              edge_mx=0.2),
+                    top=top, config=cfg, wl=wl7))
+    # (10) order 2, the largest hole of the xy mesh (squares sigma / 3) that 60 spheres of type
+    # 2 (wlmtype) leave, under fixed weights linear in its bin (alpha 0)
+    box = np.array([8.0, 8.0, 8.0])
+    p0 = [np.array([0.5, 0.5, 0.5])]
+    pos = p0 + bath(rng, box, 60, p0)
+    dirs = rand_unit(rng, len(pos))
+    top = top_text([spn(1, "A"), spn(2, "B")], [("A", [1], []), ("B", [2], [])], [("A", 1), ("B", 60)])
+    holes = grid1(0.0, 4.0, 145)
+    out.append(dict(name="o2_mesh", wlm=(2, 0), options=dict(wlm="2 0", wlmtype=2, transmx=0.4, rotmx=0.0,
+                                                               nsweeps=6000, seed=21, shave=0, ptype=0),
+                    top=top, config=config_text(box, np.array(pos) * box, dirs, rand_perp(rng, dirs)),
+                    wl=wl_text(0.0, holes, [0.05 * k for k in range(len(holes))])))
     # (7) the reference's own membrane test (Tests/SC_PSC_MEMBRANE_WANG/scOOP_test): a CPSC
     # protein and 200 three-bead lipids, orders 1 and 3, NPT (ptype 2) with chain moves, and
     # the converged weights of its legacy run (wl_orig_results.dat) as the weights file.  Its
@@ -223,10 +255,13 @@ def main():
                                                    "config.init": c["config"], "wl.dat": c["wl"]},
                      "ref": dump["wl"], "n": dump["n"],
                      "system": {k: dump[k] for k in ("box", "sqmaxcut", "ia_params", "particles", "molecules")}}
-            if c["name"] in ("o4_pair", "o3_orient", "o9_wall", "o1_fixed"):
+            if c["name"] in ("o4_pair", "o3_orient", "o9_wall", "o1_fixed", "o7_contact", "o7_npt", "o2_mesh"):
                 # the reference's own adaptive runs, three seeds
                 runs = []
-                seeds = {"o9_wall": (101,), "o1_fixed": (101, 202, 303, 404, 505, 606)}.get(c["name"], (101, 202, 303))
+                six = (101, 202, 303, 404, 505, 606)
+                twelve = six + (707, 808, 909, 1010, 1111, 1212)
+                seeds = {"o9_wall": (101,), "o1_fixed": six, "o7_contact": six, "o7_npt": twelve,
+                         "o2_mesh": six}.get(c["name"], (101, 202, 303))
                 for seed in seeds:
                     opts = dict(c["options"], seed=seed)
                     if c["name"] == "o3_orient":

@@ -77,7 +77,7 @@ class McStats(C.Structure):
 class WlState(C.Structure):
     _fields_ = [("wlm", C.c_int * 2), ("len", C.c_int * 2), ("minorder", C.c_double * 2), ("dorder", C.c_double * 2),
                 ("alpha", C.c_double), ("weights", C.POINTER(C.c_double)), ("hist", C.POINTER(C.c_long)),
-                ("cur", C.c_long * 2), ("updates", C.c_long), ("converged", C.c_int), ("pad_", C.c_int)]
+                ("cur", C.c_long * 2), ("updates", C.c_long), ("converged", C.c_int), ("wlmtype", C.c_int)]
 
 
 LIB_FAST = os.path.join(ROOT, "oracle", "_build", "liboracle_fast.so")
@@ -114,7 +114,7 @@ def _bind(L):
         L.or_wl_run.restype = C.c_int
         L.or_wl_run.argtypes = [C.POINTER(System), C.POINTER(McOpts), C.POINTER(WlState), C.POINTER(McStats)]
         L.or_wl_orders.restype = C.c_int
-        L.or_wl_orders.argtypes = [C.POINTER(System), C.POINTER(C.c_int), C.POINTER(C.c_double),
+        L.or_wl_orders.argtypes = [C.POINTER(System), C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_double),
                                    C.POINTER(C.c_double), C.POINTER(C.c_long), C.POINTER(C.c_double),
                                    C.POINTER(C.c_double)]
         L.or_nematic.restype = C.c_int
@@ -230,7 +230,7 @@ class OracleSystem:
     def mol2others(self, first, size):
         return lib().or_mol2others(C.byref(self.sys), first, size)
 
-    def wl_run(self, opts, wlm, minorder, dorder, length, alpha, weights, hist):
+    def wl_run(self, opts, wlm, minorder, dorder, length, alpha, weights, hist, wlmtype=-1):
         """Sequential Wang-Landau run (or_wl_run); returns (weights, hist, state, stats)."""
         w = np.ascontiguousarray(weights, dtype=np.float64).copy()
         h = np.ascontiguousarray(hist, dtype=np.int64).copy()
@@ -242,7 +242,8 @@ class OracleSystem:
         st.alpha = alpha
         st.weights = w.ctypes.data_as(C.POINTER(C.c_double))
         st.hist = h.ctypes.data_as(C.POINTER(C.c_long))
-        rc, cur, _, _ = self.wl_orders(wlm, minorder, dorder)
+        st.wlmtype = wlmtype
+        rc, cur, _, _ = self.wl_orders(wlm, minorder, dorder, wlmtype)
         assert rc == 0
         st.cur[0], st.cur[1] = cur
         ms = McStats()
@@ -250,15 +251,16 @@ class OracleSystem:
         assert rc == 0
         return w, h, st, ms
 
-    def wl_orders(self, wlm, minorder, dorder):
-        """Starting Wang-Landau bins, system centre and sysvolume (or_wl_orders)."""
+    def wl_orders(self, wlm, minorder, dorder, wlmtype=-1):
+        """Starting Wang-Landau bins, system centre and sysvolume (or_wl_orders; wlmtype: the
+        particle type of the mesh and contact orders)."""
         m = (C.c_int * 2)(*wlm)
         lo = (C.c_double * 2)(*minorder)
         d = (C.c_double * 2)(*dorder)
         out = (C.c_long * 2)()
         cm = (C.c_double * 3)()
         sv = C.c_double()
-        rc = lib().or_wl_orders(C.byref(self.sys), m, lo, d, out, cm, C.byref(sv))
+        rc = lib().or_wl_orders(C.byref(self.sys), m, int(wlmtype), lo, d, out, cm, C.byref(sv))
         return rc, [out[0], out[1]], [cm[0], cm[1], cm[2]], sv.value
 
 
