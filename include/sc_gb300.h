@@ -314,7 +314,10 @@ int sc_fp64_rates(int device, double* dmul_dadd_per_s, double* one_lane_per_s, d
  * by alpha after every move, and every 1000 sweeps alpha is halved once the histogram is
  * flat (the run ends when alpha falls below 1e-8).  Supported order parameters (options wlm):
  * 1 z of particle 0 relative to the system's volume-weighted centre, 3 z component of
- * particle 0's axis, 4 xy distance of particles 0 and 1, 8 / 9 box length in x / y.
+ * particle 0's axis, 4 xy distance of particles 0 and 1, 7 particles of type wlmtype within
+ * distance 6 of particle 0, 8 / 9 box length in x / y; the mesh-hole and pore orders 2, 5, 6
+ * are SC_ERR_UNSUPPORTED, and so is order 7 with chain moves of chains that hold particles
+ * of type wlmtype.
  * sc_simulate applies the bias once weights are loaded; with wlm > 0 and none loaded it
  * returns SC_ERR_STATE (the reference stops without wl.dat).  sc_open loads wl.dat from
  * the options file's directory when it exists.  Wang-Landau weights in a replica batch
