@@ -380,3 +380,23 @@ def test_reference_pore_orders_end_at_init():
             assert "Wang-Landau method init" in r.stdout
         finally:
             shutil.rmtree(d)
+
+
+def test_contact_order_refuses_chain_moves_of_counted_chains(System):
+    # order 7 with chain moves: chains that hold particles of type wlmtype would change the
+    # count outside the cells moved in sequence, so the run is refused before any device work
+    from sc_gb300._lib import ScError
+
+    c = next(c for c in CASES if c["name"] == "o7_contact")
+    inp = c["inputs"]
+    top = inp["top.init"].replace("S: {\nparticles: 2\n}", "S: {\nparticles: 2\nparticles: 2\nbond1: 50 1.0\n}")
+    top = top.replace("S 100", "S 50")
+    assert top != inp["top.init"]
+    opts = _sub(_sub(_sub(inp["options"], "chainprob", "0.1"), "chainmmx", "0.3"), "chainrmx", "10")
+    s = System.from_text(opts, top, inp["config.init"])
+    s.wl_load(text=inp["wl.dat"])
+    assert s.wl_info().currorder[0] == c["ref"]["currorder"][0]
+    with pytest.raises(ScError) as e:
+        s.simulate(nsweeps=1)
+    assert e.value.code == ERR_UNSUPPORTED and "order 7" in str(e.value)
+    s.close()
