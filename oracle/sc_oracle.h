@@ -5,7 +5,7 @@
  * type switch and grand-canonical moves)
  * (robertvacha/SC, scOOP/mc/paire.h, paire.cpp, totalenergycalculator.h,
  * movecreator.cpp, updater.cpp, structures/topo.cpp, particle.*), used by the
- * tests as the checker and by bench.py as the timed CPU baseline.  The product
+ * tests as the reference to compare against and by bench.py as the timed CPU baseline.  The product
  * (sc_gb300/) never includes, links or loads it.
  *
  * Parity is pinned: tests/test_oracle_golden.py compares every function below

@@ -1,7 +1,7 @@
 """CPU restatement of the pair-energy surrogate -- TEST INFRASTRUCTURE ONLY.
 
-Only tests/ (and the bench's CPU leg) import this module, as the checker of the GPU
-surrogate (sc_gb300/csrc/surrogate.cuh, surrogate.cu).  The surrogate has no
+Only tests/ (and the bench's CPU leg) import this module, as the CPU statement that the GPU
+surrogate (sc_gb300/csrc/surrogate.cuh, surrogate.cu) is compared with.  The surrogate has no
 counterpart in the reference (robertvacha/SC evaluates every pair exactly), so there is
 nothing of the reference to pin it to; what it pins is the GPU code itself:
 

@@ -3,7 +3,7 @@
 // The reference's WangLandau class (scOOP/mc/wanglandau.h:16-690, wanglandau.cpp) biases
 // every move by weights of one or two order parameters and lowers the weight of the
 // visited bin by alpha after every move (accept / reject, wanglandau.h:262-290); alpha is
-// halved when the histogram is flat (update, :66-120).  This build supports the order
+// halved when the histogram is flat (update, :66-120).  This library supports the order
 // parameters whose value only the moves of particles 0 and 1, of the particles near
 // particle 0, and the box change:
 //   1  z of particle 0 relative to the system's volume-weighted centre   (zOrder,  :551-554)

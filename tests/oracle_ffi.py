@@ -1,7 +1,7 @@
 """ctypes binding of the CPU oracle (oracle/_build/liboracle.so) for the tests.
 
 The oracle is test infrastructure: only tests/, __graft_entry__.smoke() and the
-CPU-baseline leg of bench.py use it, always as the checker.
+CPU-baseline leg of bench.py use it, always to check or time against, never as a product path.
 """
 import ctypes as C
 import math
