@@ -12,6 +12,7 @@
 
 #include "../../include/sc_gb300.h"
 #include "kernels.h"
+#include "host_parallel.h"
 #include "sc_context.h"
 
 namespace scg {
@@ -295,15 +296,17 @@ int Context::uploadState() {
     double4_32a* hp = (double4_32a*)((char*)hostStage + 64);
     double4_32a* hd = hp + n;
     PatchSet* hs = (PatchSet*)(hd + n);
-    for (int i = 0; i < n; ++i) {
-        const Particle& p = conf.p[i];
-        hp[i] = make_double4_32a(p.pos.x, p.pos.y, p.pos.z, (double)compactOf[p.type]);
-        hd[i] = make_double4_32a(p.dir.x, p.dir.y, p.dir.z, (double)p.switched);   // w: switched
-        PatchSet& s = hs[i];
-        for (int k = 0; k < 2; ++k) { s.pd[k][0] = p.pd[k].x; s.pd[k][1] = p.pd[k].y; s.pd[k][2] = p.pd[k].z; }
-        for (int k = 0; k < 4; ++k) { s.ps[k][0] = p.ps[k].x; s.ps[k][1] = p.ps[k].y; s.ps[k][2] = p.ps[k].z; }
-        for (int k = 0; k < 2; ++k) { s.ch[k][0] = p.ch[k].x; s.ch[k][1] = p.ch[k].y; s.ch[k][2] = p.ch[k].z; }
-    }
+    parallelRange(n, [&](int lo, int hi) {
+        for (int i = lo; i < hi; ++i) {
+            const Particle& p = conf.p[i];
+            hp[i] = make_double4_32a(p.pos.x, p.pos.y, p.pos.z, (double)compactOf[p.type]);
+            hd[i] = make_double4_32a(p.dir.x, p.dir.y, p.dir.z, (double)p.switched);   // w: switched
+            PatchSet& s = hs[i];
+            for (int k = 0; k < 2; ++k) { s.pd[k][0] = p.pd[k].x; s.pd[k][1] = p.pd[k].y; s.pd[k][2] = p.pd[k].z; }
+            for (int k = 0; k < 4; ++k) { s.ps[k][0] = p.ps[k].x; s.ps[k][1] = p.ps[k].y; s.ps[k][2] = p.ps[k].z; }
+            for (int k = 0; k < 2; ++k) { s.ch[k][0] = p.ch[k].x; s.ch[k][1] = p.ch[k].y; s.ch[k][2] = p.ch[k].z; }
+        }
+    });
     box[0] = conf.box.x; box[1] = conf.box.y; box[2] = conf.box.z; box[3] = 0.0;
     cudaError_t e;
     // grand-canonical moves reorder the molecule records on the device: the host's go up too
@@ -333,18 +336,20 @@ int Context::downloadState() {
     if ((e = cudaMemcpyAsync(hs, d.patch, sizeof(PatchSet) * n, cudaMemcpyDeviceToHost, stream)) != cudaSuccess) return cudaFail(e, "download patch");
     if ((e = cudaMemcpyAsync(box, d.box, sizeof(double) * 4, cudaMemcpyDeviceToHost, stream)) != cudaSuccess) return cudaFail(e, "download box");
     if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return cudaFail(e, "download sync");
-    for (int i = 0; i < n; ++i) {
-        Particle& p = conf.p[i];
-        p.pos = {hp[i].x, hp[i].y, hp[i].z};
-        p.dir = {hd[i].x, hd[i].y, hd[i].z};
-        const int ct = (int)hp[i].w;      // compact type (inserted and switched particles change it)
-        if (ct >= 0 && ct < (int)usedTypes.size()) p.type = usedTypes[ct];
-        p.switched = (int)hd[i].w;
-        const PatchSet& s = hs[i];
-        for (int k = 0; k < 2; ++k) p.pd[k] = {s.pd[k][0], s.pd[k][1], s.pd[k][2]};
-        for (int k = 0; k < 4; ++k) p.ps[k] = {s.ps[k][0], s.ps[k][1], s.ps[k][2]};
-        for (int k = 0; k < 2; ++k) p.ch[k] = {s.ch[k][0], s.ch[k][1], s.ch[k][2]};
-    }
+    parallelRange(n, [&](int lo, int hi) {
+        for (int i = lo; i < hi; ++i) {
+            Particle& p = conf.p[i];
+            p.pos = {hp[i].x, hp[i].y, hp[i].z};
+            p.dir = {hd[i].x, hd[i].y, hd[i].z};
+            const int ct = (int)hp[i].w;      // compact type (inserted and switched particles change it)
+            if (ct >= 0 && ct < (int)usedTypes.size()) p.type = usedTypes[ct];
+            p.switched = (int)hd[i].w;
+            const PatchSet& s = hs[i];
+            for (int k = 0; k < 2; ++k) p.pd[k] = {s.pd[k][0], s.pd[k][1], s.pd[k][2]};
+            for (int k = 0; k < 4; ++k) p.ps[k] = {s.ps[k][0], s.ps[k][1], s.ps[k][2]};
+            for (int k = 0; k < 2; ++k) p.ch[k] = {s.ch[k][0], s.ch[k][1], s.ch[k][2]};
+        }
+    });
     conf.box = {box[0], box[1], box[2]};
     devNewer = false;
     return SC_OK;
@@ -515,7 +520,9 @@ int sc_get_particles(sc_context* ctx, int first, int count, sc_particle* out) {
     if (first < 0 || count < 0 || first + count > (int)c->conf.p.size()) return fail(SC_ERR_ARG, "particle range out of bounds");
     int rc = c->downloadState();
     if (rc) return rc;
-    for (int k = 0; k < count; ++k) toParticle(c->conf.p[first + k], &out[k]);
+    parallelRange(count, [&](int lo, int hi) {
+        for (int k = lo; k < hi; ++k) toParticle(c->conf.p[first + k], &out[k]);
+    });
     return SC_OK;
 }
 
@@ -525,16 +532,21 @@ int sc_set_particles(sc_context* ctx, int first, int count, const sc_particle* i
     if (first < 0 || count < 0 || first + count > (int)c->conf.p.size()) return fail(SC_ERR_ARG, "particle range out of bounds");
     int rc = c->downloadState();
     if (rc) return rc;
-    for (int k = 0; k < count; ++k) {
-        Particle& p = c->conf.p[first + k];
-        const sc_particle& s = in[k];
-        if (s.type != p.type) return fail(SC_ERR_ARG, "sc_set_particles cannot change a particle's type");
-        p.pos = {s.pos[0], s.pos[1], s.pos[2]};
-        p.dir = {s.dir[0], s.dir[1], s.dir[2]};
-        for (int q = 0; q < 2; ++q) p.pd[q] = {s.patchdir[q][0], s.patchdir[q][1], s.patchdir[q][2]};
-        for (int q = 0; q < 4; ++q) p.ps[q] = {s.patchsides[q][0], s.patchsides[q][1], s.patchsides[q][2]};
-        for (int q = 0; q < 2; ++q) p.ch[q] = {s.chdir[q][0], s.chdir[q][1], s.chdir[q][2]};
-    }
+    // every type is checked before anything is written: a refused call changes nothing
+    for (int k = 0; k < count; ++k)
+        if (in[k].type != c->conf.p[first + k].type)
+            return fail(SC_ERR_ARG, "sc_set_particles cannot change a particle's type");
+    parallelRange(count, [&](int lo, int hi) {
+        for (int k = lo; k < hi; ++k) {
+            Particle& p = c->conf.p[first + k];
+            const sc_particle& s = in[k];
+            p.pos = {s.pos[0], s.pos[1], s.pos[2]};
+            p.dir = {s.dir[0], s.dir[1], s.dir[2]};
+            for (int q = 0; q < 2; ++q) p.pd[q] = {s.patchdir[q][0], s.patchdir[q][1], s.patchdir[q][2]};
+            for (int q = 0; q < 4; ++q) p.ps[q] = {s.patchsides[q][0], s.patchsides[q][1], s.patchsides[q][2]};
+            for (int q = 0; q < 2; ++q) p.ch[q] = {s.chdir[q][0], s.chdir[q][1], s.chdir[q][2]};
+        }
+    });
     c->hostNewer = true;
     return SC_OK;
 }
