@@ -37,6 +37,34 @@ def test_exports_every_declared_symbol(lib):
     assert sorted(n for n, _, _ in _lib.SIGNATURES) == syms
 
 
+def test_every_entry_point_refuses_null_arguments(lib):
+    """Every call given a NULL handle and NULL buffers (zero counts, zero sizes) returns an
+    error code and leaves a message, instead of dereferencing them (the reference's calls
+    exit the process on bad input; the C ABI never does).  sc_fp64_rates takes no handle and
+    needs a GPU; destroying a NULL surrogate is a no-op, as free(NULL) is."""
+    from sc_gb300 import _lib
+
+    skip = {"sc_last_error", "sc_version", "sc_fp64_rates", "sc_surrogate_destroy"}
+    checked = 0
+    for name, _, argtypes in _lib.SIGNATURES:
+        if name in skip:
+            continue
+        args = []
+        for a in argtypes:
+            if a in (C.c_int, C.c_long, C.c_ulonglong):
+                args.append(0)
+            elif a is C.c_double:
+                args.append(0.0)
+            else:
+                args.append(None)
+        rc = getattr(lib, name)(*args)
+        assert rc < 0, (name, rc)
+        assert lib.sc_last_error().decode(), name
+        checked += 1
+    assert checked >= 50
+    assert lib.sc_surrogate_destroy(None) == 0
+
+
 NAMES = goldens.names()
 
 
