@@ -964,7 +964,7 @@ void or_psc_rotate(or_particle* p, int g, double angle, or_vec ax, int positive)
 // ---------------------------------------------------------------------------------------------
 // Sequential Metropolis loop: the reference's Updater::simulate step loop
 // (scOOP/mc/updater.cpp:206-230) with particleMove / partDisplace / partRotate
-// (movecreator.cpp:11-33, 947-1028), the ptype-1 volume move (390-421) and the
+// (movecreator.cpp:11-33, 947-1028), the volume move of every coupling (330-546) and the
 // Verlet pair list of genSimplePairList (updater.cpp:484-552, cutoff main.cpp:117-126).
 // Used only as the timed CPU baseline; it draws from a splitmix64 stream
 // instead of dSFMT, which changes the trajectory but not the algorithm.
@@ -978,6 +978,83 @@ struct Rng {
         z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
         z ^= z >> 31;
         return (z >> 11) * (1.0 / 9007199254740992.0);
+    }
+};
+
+// MoveCreator::pressureMove's box change for every coupling (movecreator.cpp:349-546), with
+// the reference's arithmetic: propose() changes the box and returns the pressure-volume part
+// of enermove, p dV - N T ln(V'/V) for the coupling's dV and V'/V (ptype 3 keeps the volume
+// and has none); reject() undoes the change as the reference does, by subtracting it again
+// (ptype 0 restores the saved edge, ptype 3 re-derives z from the kept volume).
+struct BoxTrial {
+    int ptype = 1;
+    int side = 0;                       // ptype 0: the edge that changed
+    double old = 0.0;                   // ptype 0: its length before
+    double d[3] = {0.0, 0.0, 0.0};      // the change of each edge
+    double pvol = 0.0;                  // ptype 3: the kept volume
+    double propose(double* box, const or_mc_opts* o, int N, Rng& rng) {
+        ptype = o->ptype;
+        d[0] = d[1] = d[2] = 0.0;
+        const double NT = (double)N * o->temper;
+        switch (ptype) {
+        case 0: {           // one edge chosen at random (movecreator.cpp:349-389)
+            const double rs = rng();
+            side = rs < 1.0 / 3.0 ? 0 : (rs < 2.0 / 3.0 ? 1 : 2);
+            const double area = side == 0 ? box[1] * box[2] : (side == 1 ? box[0] * box[2] : box[0] * box[1]);
+            old = box[side];
+            box[side] += o->edge_mx * (rng() - 0.5);
+            return o->press * area * (box[side] - old) - NT * log(box[side] / old);
+        }
+        case 2: {           // x and y together, z kept (:422-450)
+            const double psch = o->edge_mx * (rng() - 0.5);
+            const double pv = box[0] * box[1];
+            box[0] += psch; box[1] += psch;
+            d[0] = d[1] = psch;
+            const double pvoln = box[0] * box[1];
+            return o->press * box[2] * (pvoln - pv) - NT * log(pvoln / pv);
+        }
+        case 3: {           // x and y together, z re-derived to keep the volume (:451-477)
+            const double psch = o->edge_mx * (rng() - 0.5);
+            pvol = box[0] * box[1] * box[2];
+            box[0] += psch; box[1] += psch;
+            box[2] = pvol / box[0] / box[1];
+            d[0] = d[1] = psch;
+            return 0.0;
+        }
+        case 4: {           // x or y (:478-509); the reference's test `if (ran2() - 0.5)` is true
+                            // unless the draw is exactly 0.5, so x changes
+            const double pv = box[0] * box[1];
+            if (rng() - 0.5 != 0.0) d[0] = o->edge_mx * (rng() - 0.5);
+            else d[1] = o->edge_mx * (rng() - 0.5);
+            box[0] += d[0]; box[1] += d[1];
+            const double pvoln = box[0] * box[1];
+            return o->press * box[2] * (pvoln - pv) - NT * log(pvoln / pv);
+        }
+        case 5: {           // y only (:510-539)
+            const double pv = box[1];
+            d[1] = o->edge_mx * (rng() - 0.5);
+            box[1] += d[1];
+            const double pvoln = box[1];
+            return o->press * box[2] * box[0] * (pvoln - pv) - NT * log(pvoln / pv);
+        }
+        default: {          // 1: isotropic (:390-421)
+            const double psch = o->edge_mx * (rng() - 0.5);
+            const double pv = box[0] * box[1] * box[2];
+            box[0] += psch; box[1] += psch; box[2] += psch;
+            d[0] = d[1] = d[2] = psch;
+            const double pvoln = box[0] * box[1] * box[2];
+            return o->press * (pvoln - pv) - NT * log(pvoln / pv);
+        }
+        }
+    }
+    void reject(double* box) const {
+        if (ptype == 0) {
+            box[side] = old;
+            return;
+        }
+        box[0] -= d[0]; box[1] -= d[1];
+        if (ptype == 3) box[2] = pvol / box[0] / box[1];
+        else box[2] -= d[2];
     }
 };
 
@@ -1249,7 +1326,7 @@ extern "C" or_mc* or_mc_open(or_system* s, const or_mc_opts* o) {
     const bool gc = o && o->grand_every > 0 && o->n_gc > 0 && o->gc_moltype && o->gc_type && o->gc_chempot;
     if (!s || !o || (s->n <= 0 && !gc)) return nullptr;
     if (gc && o->switchprob > 0.0) return nullptr;             // not combined with switching here
-    if (o->shave > 0.0 && o->ptype != 1) return nullptr;     // ptype 1 volume moves only
+    if (o->shave > 0.0 && (o->ptype < 0 || o->ptype > 5)) return nullptr;     // couplings 0..5
     auto t0 = std::chrono::steady_clock::now();
     or_mc* m = new or_mc();
     m->s = s;
@@ -1322,17 +1399,18 @@ extern "C" int or_mc_advance(or_mc* m, long moves, or_mc_stats* st) {
         const int N = m->N;
         double u = m->rng();
         if (u < m->shprob) {
-            // pressureMove, ptype 1 (movecreator.cpp:390-421)
-            double psch = o->edge_mx * (m->rng() - 0.5);
-            double pvol = s->box[0] * s->box[1] * s->box[2];
-            double b0[3] = {s->box[0], s->box[1], s->box[2]};
-            s->box[0] += psch; s->box[1] += psch; s->box[2] += psch;
-            double pvoln = s->box[0] * s->box[1] * s->box[2];
-            double enermove = o->press * (pvoln - pvol) - (double)N * o->temper * log(pvoln / pvol);
-            double enew = mcAllPairs(*m, m->matrix ? &m->emTrial : nullptr);
-            enermove += enew;
-            bool rej = !(enermove <= m->energy) && !(exp(-1.0 * (enermove - m->energy) / o->temper) > m->rng());
-            if (rej) { s->box[0] = b0[0]; s->box[1] = b0[1]; s->box[2] = b0[2]; ++st->rej_vol; }
+            // pressureMove (movecreator.cpp:330-546), every coupling; a box with an edge that is
+            // not positive is rejected before its energy is evaluated
+            BoxTrial bt;
+            double enermove = bt.propose(s->box, o, N, m->rng);
+            bool rej = !(s->box[0] > 0.0 && s->box[1] > 0.0 && s->box[2] > 0.0);
+            double enew = 0.0;
+            if (!rej) {
+                enew = mcAllPairs(*m, m->matrix ? &m->emTrial : nullptr);
+                enermove += enew;
+                rej = !(enermove <= m->energy) && !(exp(-1.0 * (enermove - m->energy) / o->temper) > m->rng());
+            }
+            if (rej) { bt.reject(s->box); ++st->rej_vol; }
             else {
                 ++st->acc_vol;
                 m->energy = enew;
@@ -1627,47 +1705,14 @@ extern "C" int or_wl_run(or_system* s, const or_mc_opts* o, or_wl* wl, or_mc_sta
         wl->hist[idx(wl->cur)] += 1;
     };
     const double shprob = o->shave / (double)N;
-    // volume moves of ptype 3 and 4 (movecreator.cpp:454-510) are not restated here
-    if (shprob > 0.0 && o->ptype != 0 && o->ptype != 1 && o->ptype != 2 && o->ptype != 5) return -2;
+    if (shprob > 0.0 && (o->ptype < 0 || o->ptype > 5)) return -2;
     // MoveCreator::pressureMove (movecreator.cpp:330-546) with WangLandau::runPress
     // (wanglandau.h:168-196): the bins of the trial box (order 1 keeps the centre, and ptype
     // 2 keeps order 1; 4 the two particles' distance; 8 / 9 the box lengths)
     auto volumeMove = [&]() {
         const double energy = or_all_to_all(s);
-        const double b0[3] = {s->box[0], s->box[1], s->box[2]};
-        const double NT = (double)N * o->temper;
-        double enermove = 0.0;
-        switch (o->ptype) {
-        case 0: {
-            double rs = rng();
-            int side = rs < 1.0 / 3.0 ? 0 : (rs < 2.0 / 3.0 ? 1 : 2);
-            double area = side == 0 ? b0[1] * b0[2] : (side == 1 ? b0[0] * b0[2] : b0[0] * b0[1]);
-            s->box[side] += o->edge_mx * (rng() - 0.5);
-            enermove = o->press * area * (s->box[side] - b0[side]) - NT * log(s->box[side] / b0[side]);
-            break;
-        }
-        case 2: {
-            double psch = o->edge_mx * (rng() - 0.5);
-            double pvol = b0[0] * b0[1];
-            s->box[0] += psch; s->box[1] += psch;
-            double pvoln = s->box[0] * s->box[1];
-            enermove = o->press * s->box[2] * (pvoln - pvol) - NT * log(pvoln / pvol);
-            break;
-        }
-        case 5: {
-            s->box[1] += o->edge_mx * (rng() - 0.5);
-            enermove = o->press * s->box[2] * s->box[0] * (s->box[1] - b0[1]) - NT * log(s->box[1] / b0[1]);
-            break;
-        }
-        case 1: {           // isotropic
-            double psch = o->edge_mx * (rng() - 0.5);
-            double pvol = b0[0] * b0[1] * b0[2];
-            for (int k = 0; k < 3; ++k) s->box[k] += psch;
-            double pvoln = s->box[0] * s->box[1] * s->box[2];
-            enermove = o->press * (pvoln - pvol) - NT * log(pvoln / pvol);
-            break;
-        }
-        }
+        BoxTrial bt;
+        double enermove = bt.propose(s->box, o, N, rng);
         long nw[2] = {wl->cur[0], wl->cur[1]};
         long cntNew = contacts;
         if (uses[2]) origmesh = mesh;
@@ -1699,7 +1744,7 @@ extern "C" int or_wl_run(or_system* s, const or_mc_opts* o, or_wl* wl, or_mc_sta
             rej = !(enermove <= eo) && !(exp(-1.0 * (enermove - eo) / o->temper) > rng());
         }
         if (rej) {
-            s->box[0] = b0[0]; s->box[1] = b0[1]; s->box[2] = b0[2];
+            bt.reject(s->box);
             if (uses[2]) mesh = origmesh;
             ++st->rej_vol;
         } else {

@@ -139,8 +139,10 @@ int or_mc_run(or_system* s, const or_mc_opts* o, or_mc_stats* st);
 
 /* The same loop as a resumable state, so that the moves can be timed apart from the set-up
  * the reference does before its timed loop (initial energy / energy matrix, first pair
- * list).  or_mc_open returns NULL for an empty system without grand-canonical species,
- * volume moves of a ptype other than 1, or grand-canonical moves together with switching;
+ * list).  Volume moves follow every coupling of pressureMove (ptype 0..5), undone on
+ * rejection by the reference's own subtraction.  or_mc_open returns NULL for an empty system
+ * without grand-canonical species, a ptype outside 0..5, or grand-canonical moves together
+ * with switching;
  * or_mc_advance runs `moves` more steps and adds to *st (moves, acceptances, seconds). */
 typedef struct or_mc or_mc;
 or_mc* or_mc_open(or_system* s, const or_mc_opts* o);
@@ -167,10 +169,10 @@ typedef struct {
 } or_wl;
 
 /* The reference's sequential loop with a Wang-Landau bias (single-particle moves; volume
- * moves of ptype 0, 1, 2, 5 with probability shave / N per step; order parameters 1, 2, 3,
- * 4, 7, 8, 9), WangLandau::run / runRot / runPress / accept / reject / update.  Returns -2
- * for volume moves of another ptype (3, 4), -3 for orders 5 / 6 or a mesh without squares,
- * -1 for an empty system, else 0. */
+ * moves of every coupling, ptype 0..5, with probability shave / N per step; order parameters
+ * 1, 2, 3, 4, 7, 8, 9), WangLandau::run / runRot / runPress / accept / reject / update.
+ * Returns -2 for a ptype outside 0..5, -3 for orders 5 / 6 or a mesh without squares, -1 for
+ * an empty system, else 0. */
 int or_wl_run(or_system* s, const or_mc_opts* o, or_wl* wl, or_mc_stats* st);
 
 /* Wang-Landau starting bins (WangLandau::init, scOOP/mc/wanglandau.cpp:49-137) of order

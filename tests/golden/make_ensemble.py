@@ -167,6 +167,20 @@ def cases():
                            np.vstack([qs, rand_perp(rng, rand_unit(rng, 50))])),
         opts=dict(temper=1.0, transmx=0.35, rotmx=30.0, switchprob=0.1, pairlist_update=0),
         nsweeps=24000, report=20, seeds=12, burn=3000, switch_rows=150)
+    # every volume coupling of pressureMove (movecreator.cpp:349-546) on one small fluid of
+    # attractive spheres (T = 2, P* = 1): ptype 0 one edge at a time, 2 x and y with z kept,
+    # 3 x and y with z re-derived to keep the volume (no volume term: the box x from the movie
+    # frames is the observable), 4 x alone (the reference's x-or-y test always takes x), 5 y alone
+    n = 64
+    box = np.full(3, 5.04)
+    pos = place_spheres(rng, n, box, 1.0)
+    sph = dict(top=top_text([("A", 1, "SPA", [1.0, 1.0, 1.1225, 0.5])], [("A", [1], [])], [("A", n)]),
+               config=config_text(box, pos, rand_unit(rng, n), rand_perp(rng, rand_unit(rng, n))),
+               nsweeps=20000, report=20, seeds=8, burn=2000)
+    for pt in (0, 2, 3, 4, 5):
+        out[f"spa_ptype{pt}"] = dict(sph, opts=dict(temper=2.0, press=1.0, ptype=pt, shave=1, edge_mx=0.1,
+                                                     transmx=0.25, rotmx=30.0, pairlist_update=10),
+                                     box_x=pt == 3)
     return out
 
 
@@ -222,7 +236,7 @@ def run_one(c, seed):
         opts = dict(OPTION_KEYS)
         opts.update(c["opts"])
         opts.update(nsweeps=c["nsweeps"], report=c["report"], seed=seed, paraltemper=opts["temper"])
-        if c.get("s2") or c.get("gc") or c.get("switch_rows"):
+        if c.get("s2") or c.get("gc") or c.get("switch_rows") or c.get("box_x"):
             opts.update(movie=c["report"])
         with open(os.path.join(tmp, "options"), "w") as f:
             f.write("".join(f"{k} = {v}\n" for k, v in opts.items()))
@@ -252,7 +266,20 @@ def run_one(c, seed):
         switched = []
         if c.get("switch_rows"):
             switched = movie_switched(os.path.join(tmp, "movie"), c["switch_rows"])
-        return dict(seed=seed, energy=e, volume=vol, s2=s2, counts=counts, switched=switched)
+        box_x = movie_box_x(os.path.join(tmp, "movie")) if c.get("box_x") else []
+        return dict(seed=seed, energy=e, volume=vol, s2=s2, counts=counts, switched=switched, box_x=box_x)
+
+
+def movie_box_x(path):
+    """(sweep, box x) of every frame of the reference's movie file ('sweep S; box x y z')."""
+    lines = open(path).read().splitlines()
+    out, k = [], 0
+    while k < len(lines):
+        n = int(lines[k].split()[0])
+        head = lines[k + 1]
+        out.append((int(head.split(";")[0].split()[1]), float(head.split("box")[1].split()[0])))
+        k += 2 + n
+    return out
 
 
 def movie_switched(path, rows):
@@ -311,6 +338,8 @@ def main():
             series.append(("nematic_s2", [r["s2"] for r in runs]))
         if c.get("switch_rows"):
             series = series[:1] + [("switched_fraction", [r["switched"] for r in runs])]
+        if c.get("box_x"):
+            series.append(("box_x", [r["box_x"] for r in runs]))
         stats = {k: block_stats(ser, c["burn"]) for k, ser in series}
         out = dict(name=name, n=n, inputs={"top.init": c["top"], "config.init": c["config"]}, options=c["opts"],
                    nsweeps=c["nsweeps"], report=c["report"], burn=c["burn"], seeds=c["seeds"],

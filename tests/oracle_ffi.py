@@ -524,8 +524,8 @@ class McRun:
         o.energy_matrix = 1 if energy_matrix else 0
         self.h = self.L.or_mc_open(C.byref(ts.sys), C.byref(o))
         if not self.h:
-            raise ValueError("oracle: loop refused (empty system without grand-canonical species, volume moves "
-                             "of a ptype other than 1, or grand-canonical moves with switching)")
+            raise ValueError("oracle: loop refused (empty system without grand-canonical species, a ptype "
+                             "outside 0..5, or grand-canonical moves with switching)")
         self.stats = McStats()
 
     @property
