@@ -297,6 +297,36 @@ def test_oracle_volume_moves_respect_a_weight_wall_like_the_reference():
     assert ms.acc_vol > 0 and ms.rej_vol > 0
 
 
+@pytest.mark.parametrize("ptype", [3, 4])
+def test_oracle_wl_loop_with_couplings_3_and_4(ptype):
+    # the same wall on the box length in y under the two couplings restated last: ptype 4
+    # (the reference's x-or-y test always takes x) never changes y, so every visit stays in
+    # the starting bin; ptype 3 changes x and y together at constant volume, so y moves
+    # between bins but never into the wall, and the volume stays what it was
+    import numpy as np
+
+    c = next(c for c in CASES if c["name"] == "o9_wall")
+    ref = c["ref"]
+    o = O.OracleSystem(c["system"])
+    v0 = o.sys.box[0] * o.sys.box[1] * o.sys.box[2]
+    y0 = o.sys.box[1]
+    opts = O.McOpts()
+    opts.nsweeps, opts.seed, opts.temper, opts.press = 3000, 7, 1.0, 0.0
+    opts.transmx, opts.edge_mx, opts.shave, opts.ptype = 0.4, 0.2, 1.0, ptype
+    nb = ref["length"][0]
+    w0 = np.array([0.0 if 5 <= k <= 15 else -1e4 for k in range(nb)])
+    w, h, st, ms = o.wl_run(opts, (9, 0), ref["minorder"], ref["dorder"], (nb, 1), 0.0, w0,
+                            np.zeros(nb, dtype=np.int64))
+    assert int(h.sum()) == ms.moves == 3000 * c["n"]
+    assert ms.acc_vol > 0 and ms.rej_vol > 0
+    assert h[:5].sum() == 0 and h[16:].sum() == 0
+    if ptype == 4:
+        assert np.count_nonzero(h) == 1 and o.sys.box[1] == y0
+    else:
+        assert np.count_nonzero(h) > 3
+        assert abs(o.sys.box[0] * o.sys.box[1] * o.sys.box[2] - v0) <= 1e-12 * v0
+
+
 def _options(c):
     d = {}
     for line in c["inputs"]["options"].splitlines():
