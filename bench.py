@@ -23,8 +23,8 @@ Sections of the same line (rank 0, default run): `surrogate` (plain against dela
 acceptance with the network trained in the run, after a melt), `mixture` (the
 4000-particle NPT binary mixture with one host core of the reference's loop beside it),
 `replicas` (64 uneven parallel-tempering replicas in one batch against the same replicas
-one after another), `bilayer` (30,000-particle lipid bilayers with chain moves),
-`wang_landau` (a particle above a bilayer with and without Wang-Landau weights, eight
+one after another, and one host core of the reference's loop over the ladders' systems),
+`bilayer` (30,000-particle lipid bilayers with chain moves), `wang_landau` (a particle above a bilayer with and without Wang-Landau weights, eight
 walkers sharing one table, and the reference's loop with the bias as the CPU baseline).
 `--only <section>` runs one of them alone.
 """
@@ -204,6 +204,39 @@ def wl_cpu_baseline(texts, wl_text, seed, max_moves=3000):
 
 
 REF_MAXN = 30003      # MAXN of the reference (scOOP/structures/macros.h:60)
+
+
+def replicas_cpu_baseline(systems, temps, seed, seconds=8.0):
+    """The reference's loop on one host core for the parallel-tempering replicas: each
+    ladder's system at one of its temperatures (cycling through the ladder), the -Ofast
+    restatement with the reference's defaults (TotalEMatrix, Verlet list every 10 sweeps),
+    set-up outside the timing, a bounded sample of moves each.  Without MPI the reference runs
+    its replicas as independent processes (no exchange); one core moving all of them one
+    after another, each for the same number of sweeps, makes sum(N) moves per sum(N / rate)
+    seconds, which is the rate returned."""
+    import oracle_ffi as O
+
+    budget = seconds / len(systems)
+    work = time_ = 0.0
+    moves = 0
+    for g, texts in enumerate(systems):
+        ts = O.TextSystem(*texts)
+        ts.opts.temper = float(temps[g % len(temps)])
+        n = ts.sys.n
+        run = O.McRun(ts, seed=seed + 77 * g, energy_matrix=n <= REF_MAXN, fast=True)
+        probe = run.advance(min(n, 1000))
+        rate = probe.moves / max(probe.seconds, 1e-9)
+        m0, s0 = run.stats.moves, run.stats.seconds
+        st = run.advance(max(n, int(budget * rate)))
+        rate = (st.moves - m0) / max(st.seconds - s0, 1e-9)
+        moves += st.moves - m0
+        work += n
+        time_ += n / rate
+        run.close()
+    return {"value": work / time_, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{moves} moves over the {len(systems)} ladders' systems (one temperature each) of the "
+                      f"reference's sequential loop restated in oracle/sc_oracle.cpp, built -Ofast (TotalEMatrix, "
+                      f"Verlet list every 10 sweeps), set-up outside the timing; the 64 replicas one after another"}
 
 
 def _ref_worker(texts, seed, energy_matrix, probe_moves, warmup_steps, steps, step_moves, barrier, out):
@@ -389,9 +422,14 @@ def bench_replicas(steps, seed=1):
     particles = sum(c.n for c in ctxs)
     for c in ctxs:
         c.close()
+    try:
+        cpu = replicas_cpu_baseline(systems, temps, seed)
+    except Exception as ex:                 # the oracle is not built: the section stands without it
+        cpu = {"error": str(ex)}
     return {"workload": "pt64_psc_uneven", "replicas": len(ctxs), "particles": particles, "stencil": best[0],
             "kernel_variant": {"batched": best[1], "plain": solo},
             "batched_moves_per_s": batched, "plain_moves_per_s": plain, "speedup": batched / plain,
+            "cpu_baseline": cpu, "speedup_vs_cpu_core": batched / cpu["value"] if "value" in cpu else None,
             "batched_delayed_moves_per_s": batched_da, "speedup_batched_delayed": batched_da / plain,
             "delayed_stage1_decided": std.da_stage1_rejected / max(1, std.moves),
             "exchanges_tried": int(tried.sum()), "exchange_acceptance": float(acc.sum() / max(1, tried.sum())),
