@@ -7,6 +7,7 @@
 
 #include "sc_oracle.h"
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdint>
@@ -964,7 +965,8 @@ void or_psc_rotate(or_particle* p, int g, double angle, or_vec ax, int positive)
 // ---------------------------------------------------------------------------------------------
 // Sequential Metropolis loop: the reference's Updater::simulate step loop
 // (scOOP/mc/updater.cpp:206-230) with particleMove / partDisplace / partRotate
-// (movecreator.cpp:11-33, 947-1028), the volume move of every coupling (330-546) and the
+// (movecreator.cpp:11-33, 947-1028), chainMove (305-328, 1075-1392), the volume move of every
+// coupling (330-546) and the
 // Verlet pair list of genSimplePairList (updater.cpp:484-552, cutoff main.cpp:117-126).
 // Used only as the timed CPU baseline; it draws from a splitmix64 stream
 // instead of dSFMT, which changes the trajectory but not the algorithm.
@@ -1132,6 +1134,8 @@ struct or_mc {
     double swprob = 0.0;             // switchprob when switchable particles exist, else 0
     std::vector<int> switchable;     // the particles with a switch type, in index order
     bool gc = false;                 // grand-canonical moves after every grand_every-th sweep
+    std::vector<std::pair<int, int>> chains;                 // (first particle, size) of every chain
+    std::vector<std::pair<size_t, double>> chainChanges;     // a chain trial's matrix slots and energies
 };
 
 namespace {
@@ -1191,6 +1195,120 @@ void mcCommit(or_mc& m, int t) {
         for (int k = 0; k < m.pl.count[t]; ++k) m.em[emIdx(t, id[k])] = m.changes[k];
     } else {
         for (int i = 0; i < m.N; ++i) if (i != t) m.em[emIdx(t, i)] = m.changes[i];
+    }
+}
+
+// ParticleVector::getChainCount / getChain: the molecules of more than one particle, in
+// particle order, as (first particle, size).
+void buildChains(or_mc& m) {
+    m.chains.clear();
+    for (int t = 0; t < m.s->nmol; ++t) {
+        const or_moltype& mt = m.s->mols[t];
+        if (mt.size < 2) continue;
+        for (int k = 0; k < mt.count; ++k) m.chains.emplace_back(mt.first + k * mt.size, mt.size);
+    }
+    std::sort(m.chains.begin(), m.chains.end());
+}
+
+// TotalEMatrix::mol2others / mol2othersTrial (totalenergycalculator.h:417-499) and
+// TotalEFull's (:583-619): the chain's pairs, under an empty conlist, with every particle
+// outside it, or with its pair-list neighbours outside it.  The old energy reads the matrix;
+// a trial keeps each pair energy with its matrix slot for the commit (fixEMatrixChain,
+// :81-114).
+double mcChain(or_mc& m, int first, int size, bool trial) {
+    const int last = first + size - 1;
+    const Con none;
+    if (trial) m.chainChanges.clear();
+    double e = 0.0;
+    auto term = [&](int j, int i) {
+        if (!trial && m.matrix) {
+            e += m.em[emIdx(j, i)];
+            return;
+        }
+        const double v = pairEnergyCon(m.s, j, i, none, nullptr, nullptr);
+        if (trial && m.matrix) m.chainChanges.emplace_back(emIdx(j, i), v);
+        e += v;
+    };
+    for (int j = first; j <= last; ++j) {
+        if (m.list) {
+            const int* id = m.pl.ids.data() + m.pl.start[j];
+            for (int k = 0; k < m.pl.count[j]; ++k)
+                if (id[k] < first || id[k] > last) term(j, id[k]);
+        } else {
+            for (int i = 0; i < first; ++i) term(j, i);
+            for (int i = last + 1; i < m.N; ++i) term(j, i);
+        }
+    }
+    return e;
+}
+
+// Vector::rotate(Quat) (scOOP/structures/Vector.h:162-183).
+inline void quatRotate(or_vec& v, double w, double qx, double qy, double qz) {
+    const double t2 = w * qx, t3 = w * qy, t4 = w * qz, t5 = -qx * qx, t6 = qx * qy, t7 = qx * qz, t8 = -qy * qy,
+                 t9 = qy * qz, t10 = -qz * qz;
+    const double nx = 2.0 * ((t8 + t10) * v.x + (t6 - t4) * v.y + (t3 + t7) * v.z) + v.x;
+    const double ny = 2.0 * ((t4 + t6) * v.x + (t5 + t10) * v.y + (t9 - t2) * v.z) + v.y;
+    const double nz = 2.0 * ((t7 - t3) * v.x + (t2 + t9) * v.y + (t5 + t8) * v.z) + v.z;
+    v.x = nx; v.y = ny; v.z = nz;
+}
+
+// MoveCreator::chainMove (movecreator.cpp:305-328) with chainDisplace (:1075-1137),
+// chainRotate (:1139-1256) and clusterRotate / clusterCM (:1307-1392): a random chain is
+// displaced by chainmmx in a random direction or turned about its volume-weighted centre of
+// (unwrapped) positions by a quaternion of half-angle up to chainr_angle, as one move.
+void chainMove(or_mc& m, or_mc_stats* st) {
+    if (m.chains.empty()) return;
+    or_system* s = m.s;
+    const or_mc_opts* o = &m.o;
+    const auto ch = m.chains[(size_t)(m.rng() * m.chains.size())];
+    const int first = ch.first, size = ch.second;
+    std::vector<or_particle> orig(s->p + first, s->p + first + size);
+    const double eold = mcChain(m, first, size, false);
+    const bool displace = m.rng() < 0.5;
+    if (displace) {
+        or_vec dr = randomUnitSphere(m.rng);
+        dr.x *= o->chainmmx / s->box[0];
+        dr.y *= o->chainmmx / s->box[1];
+        dr.z *= o->chainmmx / s->box[2];
+        for (int j = first; j < first + size; ++j) {
+            s->p[j].pos.x += dr.x; s->p[j].pos.y += dr.y; s->p[j].pos.z += dr.z;
+        }
+    } else {
+        or_vec cm = V(0, 0, 0);
+        double vol = 0.0;
+        for (int j = first; j < first + size; ++j) {
+            const double v = P(s, s->p[j].type, s->p[j].type).volume;
+            cm.x += s->p[j].pos.x * v; cm.y += s->p[j].pos.y * v; cm.z += s->p[j].pos.z * v;
+            vol += v;
+        }
+        cm.x /= vol; cm.y /= vol; cm.z /= vol;
+        const or_vec ax = randomUnitSphere(m.rng);
+        const double vc = cos(o->chainr_angle * m.rng());
+        const double vs = m.rng() < 0.5 ? sqrt(1.0 - vc * vc) : -sqrt(1.0 - vc * vc);
+        const double qw = vc, qx = ax.x * vs, qy = ax.y * vs, qz = ax.z * vs;
+        for (int j = first; j < first + size; ++j) {
+            or_particle& p = s->p[j];
+            p.pos.x -= cm.x; p.pos.y -= cm.y; p.pos.z -= cm.z;
+            p.pos.x *= s->box[0]; p.pos.y *= s->box[1]; p.pos.z *= s->box[2];
+            quatRotate(p.pos, qw, qx, qy, qz);
+            quatRotate(p.dir, qw, qx, qy, qz);
+            for (int k = 0; k < 2; ++k) quatRotate(p.pd[k], qw, qx, qy, qz);
+            for (int k = 0; k < 2; ++k) quatRotate(p.ch[k], qw, qx, qy, qz);
+            for (int k = 0; k < 4; ++k) quatRotate(p.ps[k], qw, qx, qy, qz);
+            p.pos.x /= s->box[0]; p.pos.y /= s->box[1]; p.pos.z /= s->box[2];
+            p.pos.x += cm.x; p.pos.y += cm.y; p.pos.z += cm.z;
+        }
+    }
+    const double enew = mcChain(m, first, size, true);
+    const bool rej = !(enew <= eold) && !(exp(-1.0 * (enew - eold) / o->temper) > m.rng());
+    if (rej) {
+        std::copy(orig.begin(), orig.end(), s->p + first);
+        ++st->rej_chain;
+    } else {
+        m.energy += enew - eold;
+        if (m.matrix)
+            for (const auto& c : m.chainChanges) m.em[c.first] = c.second;
+        ++st->acc_chain;
     }
 }
 
@@ -1353,6 +1471,7 @@ extern "C" or_mc* or_mc_open(or_system* s, const or_mc_opts* o) {
         m->energy = or_all_to_all(s);
     }
     if (m->list) m->pl.build(s, m->cut2);          // before the first sweep (updater.cpp:176-190)
+    if (o->chainprob > 0.0) buildChains(*m);
     if (o->switchprob > 0.0 && o->switch_other && o->switch_dmu && o->switched) {
         for (int i = 0; i < s->n; ++i)
             if (o->switch_other[i] >= 0) m->switchable.push_back(i);
@@ -1418,7 +1537,11 @@ extern "C" int or_mc_advance(or_mc* m, long moves, or_mc_stats* st) {
             }
             continue;
         }
-        if (u < m->shprob + m->swprob) {      // updater.cpp:219-222 (this loop has no chain moves)
+        if (u < m->shprob + m->o.chainprob) {  // updater.cpp:215-218
+            chainMove(*m, st);
+            continue;
+        }
+        if (u < m->shprob + m->o.chainprob + m->swprob) {      // updater.cpp:219-222
             switchMove(*m, st);
             continue;
         }

@@ -109,9 +109,12 @@ typedef struct {
     int energy_matrix;   /* 1: TotalEMatrix (old energies from the stored pair energies, the reference's
                             default); 0: TotalEFull (old and new energies by pair evaluation) */
     int pad_;
-    /* type switching (MoveCreator::switchTypeMove, movecreator.cpp:233-303), chosen with
-     * probability switchprob per step after the volume move's shprob (updater.cpp:219-222; this
-     * loop makes no chain moves); the arrays are per particle, NULL without switching */
+    /* chain moves (MoveCreator::chainMove, movecreator.cpp:305-328) are chosen with probability
+     * chainprob per step after the volume move's shprob (updater.cpp:215-218), displacing a
+     * random chain by chainmmx or turning it by up to chainr_angle (a quaternion half-angle);
+     * type switching (MoveCreator::switchTypeMove, movecreator.cpp:233-303) with probability
+     * switchprob after those (updater.cpp:219-222); the arrays are per particle, NULL without
+     * switching */
     double switchprob;
     int* switch_other;       /* the other type of the particle's switch pair, -1 for none (swapped by moves) */
     const int* switch_dmu;   /* delta_mu as the reference's move reads it (an int) */
