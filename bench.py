@@ -24,7 +24,8 @@ acceptance with the network trained in the run, after a melt), `mixture` (the
 4000-particle NPT binary mixture with one host core of the reference's loop beside it),
 `replicas` (64 uneven parallel-tempering replicas in one batch against the same replicas
 one after another, and one host core of the reference's loop over the ladders' systems),
-`bilayer` (30,000-particle lipid bilayers with chain moves), `wang_landau` (a particle above a bilayer with and without Wang-Landau weights, eight
+`bilayer` (30,000-particle lipid bilayers with chain moves, and one host core of the
+reference's loop on them), `wang_landau` (a particle above a bilayer with and without Wang-Landau weights, eight
 walkers sharing one table, and the reference's loop with the bias as the CPU baseline).
 `--only <section>` runs one of them alone.
 """
@@ -204,6 +205,29 @@ def wl_cpu_baseline(texts, wl_text, seed, max_moves=3000):
 
 
 REF_MAXN = 30003      # MAXN of the reference (scOOP/structures/macros.h:60)
+
+
+def bilayer_cpu_baseline(texts, seed, seconds=8.0):
+    """The reference's loop on one host core for the 30,000-particle bilayers: particle and
+    chain moves (chainprob of the options), the -Ofast restatement with TotalEFull and the
+    Verlet list every 10 sweeps (the reference's energy matrix would take 3.6 GB and an O(N^2)
+    set-up of unfiltered chain pairs), set-up outside the timing, a bounded sample of moves."""
+    import oracle_ffi as O
+
+    ts = O.TextSystem(*texts)
+    run = O.McRun(ts, seed=seed, energy_matrix=False, fast=True)
+    probe = run.advance(2000)
+    rate = probe.moves / max(probe.seconds, 1e-9)
+    m0, s0, c0 = run.stats.moves, run.stats.seconds, run.stats.acc_chain + run.stats.rej_chain
+    st = run.advance(max(2000, int(seconds * rate)))
+    moves, secs = st.moves - m0, st.seconds - s0
+    chains = st.acc_chain + st.rej_chain - c0
+    setup = run.setup_seconds
+    run.close()
+    return {"value": moves / max(secs, 1e-9), "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{moves} moves ({chains} of them chain moves) of bilayer_30000 by the reference's sequential "
+                      f"loop restated in oracle/sc_oracle.cpp, built -Ofast (TotalEFull, Verlet list every 10 "
+                      f"sweeps); set-up ({setup:.1f} s: initial energy, first pair list) outside the timing"}
 
 
 def replicas_cpu_baseline(systems, temps, seed, seconds=8.0):
@@ -540,8 +564,13 @@ def bench_bilayer(steps, seed=1, warm=20):
     exact = s.all_to_all()
     drift = abs(st.energy - exact)
     s.close()
+    try:
+        cpu = bilayer_cpu_baseline(workloads.bilayers(50, seed=seed), seed)
+    except Exception as ex:                 # the oracle is not built: the section stands without it
+        cpu = {"error": str(ex)}
     return {"workload": "bilayer_30000", "particles": 30000, "chains": 10000, "sweeps_timed": steps,
-            "kernel_variant": variant,
+            "kernel_variant": variant, "cpu_baseline": cpu,
+            "speedup_vs_cpu_core": (moves + chain) / dev / cpu["value"] if "value" in cpu else None,
             "moves_per_s": (moves + chain) / dev, "particle_moves_per_s": moves / dev,
             "chain_moves_per_s": chain / dev, "acceptance": acc / max(1, moves),
             "chain_acceptance": chain_acc / max(1, chain), "ms_per_sweep": 1e3 * dev / steps,

@@ -24,3 +24,11 @@ def test_wang_landau_cpu_baseline():
     opts, top, cfg, wl = workloads.protein_bilayer(seed=1, wlm=(1, 3), chainprob=0.0)
     rate, moves = bench.wl_cpu_baseline((opts, top, cfg), wl, 1, max_moves=300)
     assert moves == 300 and rate > 0
+
+
+def test_bilayer_cpu_baseline_on_a_small_bilayer():
+    r = bench.bilayer_cpu_baseline(workloads.bilayers(6, seed=2), seed=3, seconds=0.3)
+    assert r["value"] > 0 and r["cores"] == 1
+    words = r["sample"].split()
+    moves, chains = int(words[0]), int(words[2].lstrip("("))
+    assert moves >= 2000 and chains > 0
