@@ -32,3 +32,23 @@ def test_bilayer_cpu_baseline_on_a_small_bilayer():
     words = r["sample"].split()
     moves, chains = int(words[0]), int(words[2].lstrip("("))
     assert moves >= 2000 and chains > 0
+
+
+def test_roofline_arithmetic():
+    """achieved = algorithmic bytes per launch / average launch time; frac = achieved / the
+    measured peak; the dominant kernel is named from the launch shape, and its DRAM traffic is
+    read from the committed ncu summary of that kernel and workload."""
+    tot = {"phase_n": 10, "phase_s": 0.05, "tested": 1_000_000, "evaluated": 30_000}
+    peaks = {"hbm_gbs": 6765.7}
+    roof, fp = bench.roofline(tot, 8, "psc_cpsc_65536", peaks, "measured", None)
+    per_launch = (1_000_000 * 28 + 30_000 * 120) / 10
+    assert roof["kernel"] == "kCellWarpsFlow" and roof["unit"] == "GB/s" and roof["bound"] == "hbm"
+    assert abs(roof["algorithmic_bytes_per_launch"] - per_launch) < 1e-6
+    assert abs(roof["achieved"] - per_launch / 0.005 / 1e9) < 1e-9
+    assert abs(roof["frac"] - roof["achieved"] / 6765.7) < 1e-15
+    assert abs(roof["avg_launch_us"] - 5000.0) < 1e-9
+    assert abs(fp["achieved_ops_per_s"] - (1_000_000 * 17 + 30_000 * 600) / 10 / 0.005) < 1e-3
+    fp64 = {"dmul_dadd_ops_per_s": 5.29e11, "dfma_flops": 1.26e12, "one_lane_ops_per_s": 1.6e10,
+            "latency_cycles": 64.0}
+    _, fp = bench.roofline(tot, 8, "psc_cpsc_65536", peaks, "measured", fp64)
+    assert abs(fp["frac"] - fp["achieved_ops_per_s"] / 5.29e11) < 1e-15
